@@ -1,0 +1,262 @@
+"""ctypes binding of the FP64 CPU oracle (oracle/komd_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and
+by bench.py's CPU-baseline leg -- never by the engine in komd_gb300/.
+
+`OracleSim` restates one reference MD step (Simulation.cpp:49-74 without the
+thermostat) on numpy arrays:
+
+    integrate0 -> update_container (COM, wrap, f = 0, COM, bin)
+               -> LJ (+ FENE) (+ Limit) (+ ATM) -> integrate1
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libkomd_oracle.so")
+
+P = C.c_void_p
+I64 = C.c_int64
+D = C.c_double
+
+VIRIAL_COMPAT, VIRIAL_CORRECT = 0, 1
+ATM_SIGN_REFERENCE, ATM_SIGN_PHYSICAL = 0, 1
+
+
+class Grid(C.Structure):
+    _fields_ = [("low", D * 3), ("high", D * 3), ("L", D * 3), ("cs", D), ("nd", I64 * 3), ("nc", I64 * 3),
+                ("ncell", I64), ("bl", P * 3), ("bh", P * 3)]
+
+
+class Cells(C.Structure):
+    _fields_ = [("ncell", I64), ("count", C.POINTER(I64)), ("start", C.POINTER(I64)), ("idx", C.POINTER(I64)),
+                ("total", I64)]
+
+
+class LJOut(C.Structure):
+    _fields_ = [("u_total", D), ("virial", D * 6), ("pairs_in_cutoff", I64)]
+
+
+class ATMOut(C.Structure):
+    _fields_ = [("energy", D), ("virial", D * 6), ("triplets", I64)]
+
+
+def build() -> str:
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = C.CDLL(_LIB_PATH)
+        L.kor_grid_init.argtypes = [C.POINTER(Grid), P, P, D]
+        L.kor_grid_free.argtypes = [C.POINTER(Grid)]
+        L.kor_com.argtypes = [I64, P, P, P, P]
+        L.kor_wrap.argtypes = [C.POINTER(Grid), I64, P, P, P]
+        L.kor_bin.argtypes = [C.POINTER(Grid), I64, P, P, C.POINTER(Cells)]
+        L.kor_cells_free.argtypes = [C.POINTER(Cells)]
+        L.kor_c08_pairs.argtypes = [C.POINTER(Grid), I64, P, P]
+        L.kor_c08_pairs.restype = I64
+        L.kor_c08_triples.argtypes = [C.POINTER(Grid), I64, P, P]
+        L.kor_c08_triples.restype = I64
+        L.kor_pair_list.argtypes = [C.POINTER(Grid), C.POINTER(Cells), I64, P, P]
+        L.kor_pair_list.restype = I64
+        L.kor_lj.argtypes = [C.POINTER(Grid), I64, P, P, P, P, P, P, D, C.c_int, P, P, C.POINTER(LJOut), I64, D, P, P, P, P]
+        L.kor_atm_compat.argtypes = [C.POINTER(Grid), C.POINTER(Cells), P, D, D, C.c_int, C.c_int, C.c_int, P,
+                                     C.POINTER(ATMOut)]
+        L.kor_atm_vertex.argtypes = [C.POINTER(Grid), C.POINTER(Cells), P, D, D, C.c_int, C.c_int, P, C.POINTER(ATMOut)]
+        L.kor_atm_comp_force.argtypes = [D, D, D, D]
+        L.kor_atm_comp_force.restype = D
+        L.kor_atm_energy.argtypes = [D, D, D, D]
+        L.kor_atm_energy.restype = D
+        L.kor_fene.argtypes = [I64, P, P, P, P, P, P, D, P]
+        L.kor_limit.argtypes = [I64, P, P, D, P]
+        L.kor_bonded.argtypes = [I64, P, D, D, I64, P, D, D, P, P, P, P]
+        L.kor_bonded.restype = D
+        L.kor_step0.argtypes = [I64, P, P, P, P, D]
+        L.kor_step1.argtypes = [I64, P, P, P, D]
+        L.kor_temperature.argtypes = [I64, P, P, P, P, P]
+        L.kor_temperature.restype = D
+        L.kor_momentum.argtypes = [I64, P, P, P]
+        L.kor_rdf_nbins.argtypes = [D, D]
+        L.kor_rdf_nbins.restype = I64
+        L.kor_rdf.argtypes = [I64, P, P, D, D, I64, P]
+        L.kor_pressure_factor.restype = D
+        L.kor_num_threads.restype = C.c_int
+        L.kor_set_num_threads.argtypes = [C.c_int]
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def set_threads(n: int) -> None:
+    lib().kor_set_num_threads(int(n))
+
+
+def num_threads() -> int:
+    return int(lib().kor_num_threads())
+
+
+class OracleSim:
+    """Owns copies of the site arrays and runs reference-semantics steps."""
+
+    def __init__(self, sysm, cell_size, cutoff, dt=0.005, nu=0.0, cutoff_atm=None, limit=1e30,
+                 stiffness=30.0, lj=True, atm=False, atm_mode="compat", atm_sign=ATM_SIGN_REFERENCE,
+                 fene=False, bonded=None, virial_mode=VIRIAL_COMPAT):
+        self.L = lib()
+        self.r = np.ascontiguousarray(sysm.r, dtype=np.float64).copy()
+        self.v = np.ascontiguousarray(sysm.v, dtype=np.float64).copy()
+        self.f = np.zeros_like(self.r)
+        self.m = np.ascontiguousarray(sysm.m, dtype=np.float64)
+        self.eps = np.ascontiguousarray(sysm.eps, dtype=np.float64)
+        self.sig = np.ascontiguousarray(sysm.sig, dtype=np.float64)
+        self.id = np.ascontiguousarray(sysm.mol_id, dtype=np.uint64)
+        self.mol_off = np.ascontiguousarray(sysm.mol_off, dtype=np.int64)
+        self.n = self.r.shape[0]
+        self.n_mol = self.mol_off.shape[0] - 1
+        self.com = np.zeros((self.n_mol, 3))
+        self.low = np.ascontiguousarray(sysm.low, dtype=np.float64)
+        self.high = np.ascontiguousarray(sysm.high, dtype=np.float64)
+        self.g = Grid()
+        if self.L.kor_grid_init(C.byref(self.g), _p(self.low), _p(self.high), float(cell_size)) != 0:
+            raise ValueError("domain smaller than one cell")
+        self.cells = Cells()
+        self.cutoff, self.cutoff_atm = float(cutoff), float(cutoff if cutoff_atm is None else cutoff_atm)
+        self.dt, self.nu, self.limit, self.stiffness = float(dt), float(nu), float(limit), float(stiffness)
+        self.use_lj, self.use_atm, self.use_fene = lj, atm, fene
+        self.atm_mode, self.atm_sign, self.virial_mode = atm_mode, atm_sign, virial_mode
+        self.bonded = bonded
+        self.lj_out, self.atm_out = LJOut(), ATMOut()
+        self.e_bonded = 0.0
+        self.ncount = None
+
+    def __del__(self):
+        try:
+            self.L.kor_cells_free(C.byref(self.cells))
+            self.L.kor_grid_free(C.byref(self.g))
+        except Exception:
+            pass
+
+    # --- container -------------------------------------------------------
+    def update_container(self):
+        L = self.L
+        L.kor_com(self.n_mol, _p(self.mol_off), _p(self.r), _p(self.m), _p(self.com))
+        L.kor_wrap(C.byref(self.g), self.n_mol, _p(self.mol_off), _p(self.com), _p(self.r))
+        self.f[:] = 0
+        L.kor_com(self.n_mol, _p(self.mol_off), _p(self.r), _p(self.m), _p(self.com))
+        L.kor_bin(C.byref(self.g), self.n_mol, _p(self.mol_off), _p(self.com), C.byref(self.cells))
+
+    def cell_lists(self):
+        """(count, start, idx) of the reference's (nd+2)^3 grid incl. halo copies."""
+        c = self.cells
+        count = np.ctypeslib.as_array(c.count, shape=(c.ncell,)).copy()
+        start = np.ctypeslib.as_array(c.start, shape=(c.ncell + 1,)).copy()
+        idx = np.ctypeslib.as_array(c.idx, shape=(max(c.total, 1),))[:c.total].copy()
+        return count, start, idx
+
+    @property
+    def nd(self):
+        return tuple(int(x) for x in self.g.nd)
+
+    def pair_list(self):
+        n = self.L.kor_pair_list(C.byref(self.g), C.byref(self.cells), 0, None, None)
+        pairs = np.zeros((max(n, 1), 2), np.int64)
+        shifts = np.zeros((max(n, 1), 6), np.float64)
+        self.L.kor_pair_list(C.byref(self.g), C.byref(self.cells), n, _p(pairs), _p(shifts))
+        return pairs[:n], shifts[:n]
+
+    # --- forces ------------------------------------------------------------
+    def forces(self, nbins=0, max_sigma=1.0, with_atm_virial=False, ncount=False):
+        pairs, shifts = self.pair_list()
+        self.ncount = np.zeros(self.n, np.int64) if ncount else None
+        if self.use_lj:
+            self.hist = None
+            if nbins > 0:
+                self.hist = (np.zeros(nbins), np.zeros(nbins), np.zeros(nbins, np.uint64), np.zeros(nbins, np.uint64))
+            h = self.hist
+            self.L.kor_lj(C.byref(self.g), pairs.shape[0], _p(pairs), _p(shifts), _p(self.r), _p(self.eps),
+                          _p(self.sig), _p(self.id), self.cutoff, self.virial_mode, _p(self.f),
+                          _p(self.ncount) if ncount else None, C.byref(self.lj_out), nbins, max_sigma,
+                          _p(h[0]) if h else None, _p(h[1]) if h else None, _p(h[2]) if h else None,
+                          _p(h[3]) if h else None)
+        if self.use_fene:
+            self.L.kor_fene(pairs.shape[0], _p(pairs), _p(shifts), _p(self.r), _p(self.eps), _p(self.sig),
+                            _p(self.id), self.stiffness, _p(self.f))
+        if self.bonded is not None:
+            b = self.bonded
+            bonds = np.ascontiguousarray(b["bonds"], np.int64)
+            angles = np.ascontiguousarray(b["angles"], np.int64)
+            w = np.zeros(6)
+            self.e_bonded = self.L.kor_bonded(bonds.shape[0], _p(bonds), b["kb"], b["r0"], angles.shape[0],
+                                              _p(angles), b["ka"], b["theta0"], _p(self.r), None, _p(self.f), _p(w))
+            self.w_bonded = w
+        self.L.kor_limit(self.n, _p(self.eps), _p(self.sig), self.limit, _p(self.f))
+        if self.use_atm:
+            self.atm_forces(with_atm_virial)
+
+    def atm_forces(self, with_virial=False):
+        if self.atm_mode == "compat":
+            self.L.kor_atm_compat(C.byref(self.g), C.byref(self.cells), _p(self.r), self.nu, self.cutoff_atm,
+                                  self.atm_sign, self.virial_mode, int(with_virial), _p(self.f), C.byref(self.atm_out))
+        else:
+            self.L.kor_atm_vertex(C.byref(self.g), C.byref(self.cells), _p(self.r), self.nu, self.cutoff_atm,
+                                  self.atm_sign, 1 if self.atm_mode == "vertex_compat" else 0, _p(self.f),
+                                  C.byref(self.atm_out))
+
+    # --- integration & sensors ---------------------------------------------
+    def integrate0(self):
+        self.L.kor_step0(self.n, _p(self.r), _p(self.v), _p(self.f), _p(self.m), self.dt)
+
+    def integrate1(self):
+        self.L.kor_step1(self.n, _p(self.v), _p(self.f), _p(self.m), self.dt)
+
+    def step(self, first=False):
+        if not first:
+            self.integrate0()
+        self.update_container()
+        self.forces()
+        if not first:
+            self.integrate1()
+
+    def temperature(self):
+        return self.L.kor_temperature(self.n, _p(self.r), _p(self.v), _p(self.m), _p(self.low), _p(self.high))
+
+    def momentum(self, n_terms=None):
+        acc = np.zeros(6)
+        self.L.kor_momentum(self.n_mol if n_terms is None else n_terms, _p(self.v), _p(self.m), _p(acc))
+        return acc
+
+    def rdf(self, max_r, dr):
+        nb = int(self.L.kor_rdf_nbins(max_r, dr))
+        bins = np.zeros(nb)
+        com = np.zeros((self.n_mol, 3))
+        self.L.kor_com(self.n_mol, _p(self.mol_off), _p(self.r), _p(self.m), _p(com))
+        box = (self.high - self.low).copy()
+        self.L.kor_rdf(self.n_mol, _p(com), _p(box), max_r, dr, nb, _p(bins))
+        return bins
+
+
+def comp_force(nu, a, b, c):
+    return lib().kor_atm_comp_force(nu, a, b, c)
+
+
+def atm_energy(nu, a, b, c):
+    return lib().kor_atm_energy(nu, a, b, c)
+
+
+def pressure_factor():
+    return lib().kor_pressure_factor()

@@ -1,0 +1,163 @@
+"""Generates the golden fixtures under tests/golden/ by running the reference.
+
+The reference harness (oracle/ref/harness.cpp, built by oracle/ref/Makefile
+from the reference's own sources into oracle/_ref/) is fed seeded synthetic
+inputs in KoMD's own input and checkpoint formats; its dumps (positions,
+velocities, forces, cell lists incl. halo copies, neighbour counts,
+temperature, LJ potential, pressure tensor, RDF histogram) are stored as
+compressed .npz files together with the inputs that produced them.
+
+Run from the repo root in a container where the reference is present:
+
+    make -C oracle/ref -j8 && python tests/golden/make_golden.py
+
+The fixtures are then read by the tests without the reference.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from komd_gb300 import lattice, komd_io  # noqa: E402
+
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "komd_ref_harness")
+OUT = os.path.dirname(os.path.abspath(__file__))
+EPS_J = 1.0 / lattice.CONV_J_EI          # eps* = 1 as the COMP line's Joule value
+
+
+def parse_dump(path):
+    steps = {}
+    with open(path) as fh:
+        lines = fh.read().split("\n")
+    i = 0
+    cur = None
+    while i < len(lines):
+        ln = lines[i].split()
+        i += 1
+        if not ln:
+            continue
+        key = ln[0]
+        if key == "STEP":
+            cur = steps.setdefault(int(ln[1]), {})
+        elif key in ("R", "V", "F"):
+            n = int(ln[1])
+            cur[key] = np.array([[float(x) for x in lines[i + k].split()] for k in range(n)]).reshape(n, 3)
+            i += n
+        elif key == "CELLS":
+            n = int(ln[1])
+            counts, idx = [], []
+            for k in range(n):
+                p = [int(x) for x in lines[i + k].split()]
+                counts.append(p[0])
+                idx.extend(p[1:])
+            cur["cell_count"] = np.array(counts, np.int64)
+            cur["cell_idx"] = np.array(idx, np.int64)
+            i += n
+        elif key == "NCOUNT":
+            n = int(ln[1])
+            cur["ncount"] = np.array([int(lines[i + k]) for k in range(n)], np.int64)
+            i += n
+        elif key == "PRESSURE":
+            cur["pressure"] = np.array([float(lines[i + k]) for k in range(6)])
+            i += 6
+        elif key in ("TEMP", "UPOT"):
+            cur[key.lower()] = float(ln[1])
+        elif key == "NPAIRS":
+            cur["npairs"] = int(ln[1])
+    return steps
+
+
+def run_case(name, sysm, values, steps, dumps, comps=None):
+    tmp = tempfile.mkdtemp(prefix=f"komd_golden_{name}_")
+    try:
+        ps = os.path.join(tmp, "in.ps")
+        komd_io.write_checkpoint(ps, sysm)
+        comps = comps or [(0, EPS_J, 1.0, 1.0)]
+        with open(os.path.join(tmp, "in.dat"), "w") as fh:
+            fh.write(komd_io.format_input(values, ps, comps))
+        res = subprocess.run([HARNESS, "in.dat", "out.txt", str(steps)] + [str(d) for d in dumps], cwd=tmp,
+                             capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"{name}: harness failed\n{res.stdout}\n{res.stderr}")
+        dump = parse_dump(os.path.join(tmp, "out.txt"))
+        arrays = dict(r0=sysm.r, v0=sysm.v, m=sysm.m, eps=sysm.eps, sig=sysm.sig, mol_id=sysm.mol_id,
+                      low=np.asarray(values["domain_low"], float), high=np.asarray(values["domain_high"], float),
+                      dumps=np.array(dumps, np.int64))
+        for k in ("cutoff", "cell_size", "delta_t", "limit", "energy_3b", "stiffness", "sensor_rdf_max",
+                  "sensor_rdf_dr"):
+            if k in values:
+                arrays["p_" + k] = np.float64(values[k])
+        for k in ("enable_3b", "enable_3b_direct", "enable_sensor_rdf", "enable_sensor_lj", "enable_sensor_pres"):
+            if k in values:
+                arrays["p_" + k] = np.int64(values[k])
+        for s, d in dump.items():
+            for k, v in d.items():
+                arrays[f"s{s}_{k}"] = np.asarray(v)
+            rdf = os.path.join(tmp, f"rdf_{s}.txt")
+            if os.path.exists(rdf):
+                tab = np.loadtxt(rdf)
+                arrays[f"s{s}_rdf"] = tab[:, 2].copy()
+        np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **arrays)
+        print(f"{name}: n={sysm.n} steps={steps} dumps={dumps} -> {name}.npz")
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+
+
+def base_values(sysm, cutoff, cell, dt, steps, **kw):
+    v = dict(temperature=100.0, delta_t=dt, cutoff=cutoff, cell_size=cell, timesteps=steps, density=0.8,
+             limit=1e30, energy_3b=0.0, domain_low=tuple(sysm.low), domain_high=tuple(sysm.high),
+             pair_steps=1, triple_steps=1, write_freq=100000000, enable_3b=0, enable_3b_direct=1,
+             enable_sensor_lj=1, enable_sensor_pres=1, enable_sensor_rdf=0)
+    v.update(kw)
+    return v
+
+
+def main():
+    if not os.path.exists(HARNESS):
+        raise SystemExit("build the reference harness first: make -C oracle/ref -j8")
+
+    # 1. plain LJ argon, 864 atoms, jittered FCC, rc = cell = 2.5, RDF 200 bins
+    s = lattice.argon_fcc(6, rho=0.8442, t_star=0.722, seed=11, jitter=0.05)
+    run_case("lj864", s, base_values(s, 2.5, 2.5, 0.005, 100, enable_sensor_rdf=1, sensor_rdf_max=2.5,
+                                      sensor_rdf_dr=0.0125), 100, [0, 1, 100])
+
+    # 2. LJ + ATM (direct enumeration), single cutoff 2.0 (the reference has one cutoff)
+    s = lattice.argon_fcc(6, rho=0.8442, t_star=0.722, seed=12, jitter=0.05)
+    e3b = lattice.nu_star_to_energy_3b(0.073)
+    run_case("ljatm864", s, base_values(s, 2.0, 2.0, 0.005, 20, enable_3b=1, enable_3b_direct=1, energy_3b=e3b),
+             20, [0, 1, 20])
+
+    # 3. ATM via the triplet list (ATM + ATM_Pressure), 500 atoms, stretched last cell
+    s = lattice.argon_fcc(5, rho=0.8442, t_star=0.722, seed=13, jitter=0.05)
+    run_case("atmlist500", s, base_values(s, 2.0, 2.0, 0.005, 5, enable_3b=1, enable_3b_direct=0, energy_3b=e3b),
+             5, [0, 1, 5])
+
+    # 4. three-site molecules with FENE (all same-molecule pairs) and intermolecular LJ
+    s = lattice.triatomic_sc(5, rho_site=0.25, t_star=0.5, seed=14, r0=0.97, theta0_deg=90.0)
+    run_case("fene375", s, base_values(s, 2.5, 2.5, 0.002, 20, stiffness=30.0), 20, [0, 1, 20])
+
+    # 5. non-cubic box, non-zero domain_low, atoms on the domain faces, hot gas so
+    #    that sites cross the periodic boundary; small force clamp (Limit)
+    rng = np.random.default_rng(15)
+    low = np.array([-2.0, 0.5, 1.0])
+    box = np.array([10.3, 11.1, 9.7])
+    g = np.stack(np.meshgrid(*(np.arange(int(b // 1.15)) for b in box), indexing="ij"), -1).reshape(-1, 3)
+    r = low + (g + 0.5) * (box / np.floor(box / 1.15)) + rng.normal(0, 0.04, g.shape)
+    r[0] = low                  # exactly on the low corner
+    r[1] = low + box * np.array([1.0, 0.5, 0.5])   # exactly on the high x face
+    n = r.shape[0]
+    s = lattice.System(r=r, v=lattice.maxwell_boltzmann(n, 2.0, np.ones(n), rng), m=np.ones(n), eps=np.ones(n),
+                       sig=np.ones(n), mol_id=np.arange(1, n + 1, dtype=np.uint64), low=low, high=low + box)
+    run_case("edge_box", s, base_values(s, 2.5, 2.5, 0.004, 50, limit=40.0), 50, [0, 1, 50])
+
+
+if __name__ == "__main__":
+    main()
