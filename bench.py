@@ -1,0 +1,360 @@
+"""Benchmark: atom-steps/s of the KoMD hot path on one GB300 (per rank).
+
+Workload (default): LJ + Axilrod-Teller-Muto argon, 256,000 atoms on an FCC
+lattice (40^3 unit cells) at rho* = 0.8442, T* = 0.722 (seeded Maxwell-
+Boltzmann, zero momentum), LJ cutoff 2.5, ATM cutoff 2.0, nu* = 0.073, cell
+edge 2.5 (26^3 cells), dt* = 0.005.  One step = one full velocity-Verlet MD
+step: integrate0, COM/wrap/counting-sort binning, LJ pair kernel (which also
+writes the ATM neighbour list), ATM triplet kernel, integrate1.  Forces are
+FP32 arithmetic, integration and reductions FP64, the ATM term is the FULL
+triplet set with F = -grad V (the physical form).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  Under torchrun each rank advances its own
+replica (weak scaling, no collective on the data path); the timed region is
+bracketed by a barrier and the max over ranks is taken.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "atom-steps/s, LJ+ATM argon 256k: exact vs FP32+surrogate at stated force RMSE"
+UNIT = "atom-steps/s"
+
+WORKLOADS = {
+    # name: (fcc cells, rho, T*, cell size, rc_lj, rc_atm, nu*, dt)
+    "lj_atm_argon_256k": dict(ncell=40, rho=0.8442, t=0.722, cell=2.5, rc=2.5, rc3=2.0, nu=0.073, dt=0.005, atm=True),
+    "lj_atm_argon_32k": dict(ncell=20, rho=0.8442, t=0.722, cell=2.5, rc=2.5, rc3=2.0, nu=0.073, dt=0.005, atm=True),
+    "lj_argon_4k": dict(ncell=10, rho=0.8442, t=0.722, cell=2.5, rc=2.5, rc3=2.5, nu=0.0, dt=0.005, atm=False),
+}
+# algorithmic work per unit (frozen constants): the exact ATM
+# term costs 200 FLOP per in-cutoff triplet in the reference's formulation
+FLOP_PER_TRIPLET = 200.0
+
+
+def env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if p[5 + k].lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": smax, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_system(w, seed):
+    from komd_gb300 import lattice
+    return lattice.argon_fcc(w["ncell"], rho=w["rho"], t_star=w["t"], seed=seed)
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            return json.load(fh), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def fp32_simt_peak_tflops(torch):
+    """FP32 (non-tensor) peak, measured here: cuBLAS SGEMM with TF32 disabled."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        n = 8192
+        a = torch.randn(n, n, device="cuda", dtype=torch.float32)
+        b = torch.randn(n, n, device="cuda", dtype=torch.float32)
+        for _ in range(2):
+            torch.matmul(a, b)
+        torch.cuda.synchronize()
+        best = 1e9
+        for _ in range(5):
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            torch.matmul(a, b)
+            e.record()
+            torch.cuda.synchronize()
+            best = min(best, s.elapsed_time(e) / 1e3)
+        del a, b
+        return 2.0 * n ** 3 / best / 1e12
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+
+
+def committed_traffic(kernel, workload):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as fh:
+        d = json.load(fh)
+    e = d.get(kernel, {}).get(workload)
+    return None if e is None else float(e["bytes_per_launch"])
+
+
+def cpu_baseline(w, seed, budget_s=25.0, threads=None):
+    """The oracle's restatement of the reference's algorithm (COMPAT triplet
+    enumeration, pair sweep of the reference's cell pairs) on the host cores,
+    on a bounded sample: whole MD steps of the same system until budget_s."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    pyoracle.build()
+    if threads:
+        pyoracle.set_threads(threads)
+    s = make_system(w, seed)
+    sim = pyoracle.OracleSim(s, w["cell"], w["rc"], dt=w["dt"], nu=w["nu"], cutoff_atm=w["rc3"], atm=w["atm"],
+                             atm_mode="compat")
+    sim.update_container()
+    sim.forces(listless=True)
+    t0 = time.perf_counter()
+    steps = 0
+    while True:
+        sim.step(listless=True)
+        steps += 1
+        if time.perf_counter() - t0 > budget_s or steps >= 50:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": s.n * steps / dt, "unit": UNIT, "cores": pyoracle.num_threads(), "kind": "port",
+            "sample": f"{steps} full MD step(s) of the {s.n}-atom system ({dt:.1f} s), oracle/komd_oracle.c (OpenMP)"}
+
+
+def run_reference(args, w, name):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return 0
+    budget = float(os.environ.get("KOMD_REF_BUDGET_S", "60"))
+    per_step = budget / max(1, args.steps + args.warmup)
+    cb = cpu_baseline(w, seed=1, budget_s=max(per_step * args.steps, 5.0))
+    line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded FCC lattice, Maxwell-Boltzmann velocities)",
+            "config": {"workload": name, "form": "reference algorithm on CPU (COMPAT triplets, reference sign)",
+                       "sites": 4 * w["ncell"] ** 3},
+            "impl": "reference",
+            "cpu_baseline": {"value": cb["value"], "unit": UNIT, "cores": cb["cores"], "kind": cb["kind"],
+                             "sample": cb["sample"]},
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, w, name):
+    import torch
+    from komd_gb300 import gpu
+
+    rank, world, local = env_rank()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    s = make_system(w, seed=1 + rank)
+    terms = gpu.TERM_LJ | (gpu.TERM_ATM if w["atm"] else 0)
+    cfg = gpu.make_config(s.low, s.high, w["cell"], cutoff=w["rc"], cutoff_3b=w["rc3"], nu=w["nu"], dt=w["dt"],
+                          terms=terms, precision=gpu.FP32, atm_sign=gpu.ATM_SIGN_PHYSICAL,
+                          atm_enum=gpu.ATM_ENUM_FULL, virial_mode=gpu.VIRIAL_CORRECT)
+    g = gpu.GpuSystem(s, cfg, device=local)
+    # the engine runs on a torch-created stream so that torch's CUDA events
+    # time exactly the engine's launches (the legacy default stream would not
+    # order against the engine's non-blocking stream)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    g.set_stream(stream.cuda_stream)
+    g.update_container()
+    g.forces()
+    obs0 = g.measure(gpu.MEASURE_ENERGY | gpu.MEASURE_TEMPERATURE)
+    triplets = int(obs0["triplets"])
+
+    # warm-up (also captures the CUDA graph)
+    g.step(max(args.warmup, 3))
+    torch.cuda.synchronize()
+
+    # ---- timed region: K steps, per-kernel CUDA events on the launching stream
+    g.set_profiling(True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        g.step(args.steps)
+        t1.record(stream)
+        torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1)
+    prof = g.profile()
+    g.set_profiling(False)
+    if dist:
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+        dist.barrier()
+    value = world * s.n * args.steps / (ms / 1e3)
+
+    # graph-replay timing of the same K steps (no per-kernel events)
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    g.step(args.steps)
+    b.record(stream)
+    torch.cuda.synchronize()
+    graph_ms = a.elapsed_time(b)
+
+    # ---- end to end through the C ABI from pinned host buffers
+    r_h = torch.empty((s.n, 3), dtype=torch.float64).pin_memory()
+    v_h = torch.empty((s.n, 3), dtype=torch.float64).pin_memory()
+    f_h = torch.empty((s.n, 3), dtype=torch.float64).pin_memory()
+    rr, vv, _ = g.download()
+    r_h.numpy()[:] = rr
+    v_h.numpy()[:] = vv
+    g.step_host(1, r_h.numpy(), v_h.numpy(), f_h.numpy())
+    if dist:
+        dist.barrier()
+    e0 = time.perf_counter()
+    for _ in range(args.steps):
+        g.step_host(1, r_h.numpy(), v_h.numpy(), f_h.numpy())
+    e_s = time.perf_counter() - e0
+    if dist:
+        tt = torch.tensor([e_s], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e_s = float(tt.item())
+    e2e = world * s.n * args.steps / e_s
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+
+    peaks, peak_kind = measured_peaks()
+    atm_launches, atm_ms = prof.get("atm", (0, 0.0))
+    pair_launches, pair_ms = prof.get("pair", (0, 0.0))
+    total_prof = sum(v[1] for v in prof.values())
+    if w["atm"] and atm_launches:
+        t_launch = atm_ms / atm_launches / 1e3
+        achieved = FLOP_PER_TRIPLET * triplets / t_launch / 1e12
+        peak = fp32_simt_peak_tflops(torch)
+        traffic = committed_traffic("k_atm", name)
+        roof = {"bound": "fp32", "kernel": "k_atm (ATM triplets, FULL)", "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
+                "peak_source": "measured here: cuBLAS SGEMM 8192^3, TF32 off (FP32 SIMT pipe; not in MEASURED_PEAKS.json)",
+                "work": f"{FLOP_PER_TRIPLET:.0f} FLOP x {triplets} in-cutoff triplets per launch",
+                "launch_ms": t_launch * 1e3, "share_of_step": atm_ms / total_prof if total_prof else None}
+    else:
+        t_launch = pair_ms / max(pair_launches, 1) / 1e3
+        pairs = int(obs0["pairs_in_cutoff"])
+        achieved = 40.0 * pairs / t_launch / 1e12
+        peak = fp32_simt_peak_tflops(torch)
+        roof = {"bound": "fp32", "kernel": "k_pair (LJ)", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": committed_traffic("k_pair", name),
+                "peak_source": "measured here: cuBLAS SGEMM 8192^3, TF32 off", "launch_ms": t_launch * 1e3}
+    cb = None
+    if not args.no_cpu_baseline:
+        cb = cpu_baseline(w, seed=1, budget_s=args.cpu_budget)
+    kernels = g.kernels_per_step()
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32 forces / fp64 integration",
+            "data": "synthetic (seeded FCC lattice, Maxwell-Boltzmann velocities)",
+            "config": {"workload": name, "form": "exact FP32 (LJ + FULL ATM, F = -grad V)", "sites": s.n,
+                       "rc_lj": w["rc"], "rc_atm": w["rc3"], "nu_star": w["nu"], "cell": w["cell"], "dt": w["dt"],
+                       "triplets_per_step": triplets, "parallelism": f"replicas x{world}",
+                       "l2": "no flush: the per-step working set exceeds L2 (the ATM neighbour list alone, "
+                             "16 B x capacity per site, is written and re-read every step)"},
+            "gpu_launches": kernels * args.steps,
+            "graph_ms_per_step": graph_ms / args.steps,
+            "kernel_ms": {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()},
+            "roofline": roof, "peak_kind": peak_kind,
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * s.n * 24, "d2h_bytes_per_step": 3 * s.n * 24},
+            "clocks": clk.summary(),
+            "energy": {"u_lj_per_atom": obs0["u_lj"] / s.n, "u_atm_per_atom": obs0["u_atm"] / s.n}}
+    if cb:
+        line["cpu_baseline"] = cb
+    print(json.dumps(line), flush=True)
+    g.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="lj_atm_argon_256k", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    w = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, w, args.workload)
+    return run_ours(args, w, args.workload)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,186 @@
+/*
+ * komd_gpu.h -- C ABI of the GB300 force engine for KoMD's hot path.
+ *
+ * One opaque handle owns one periodic system on one GPU (device buffers are
+ * engine-owned, every host buffer is caller-owned).  Every call returns an
+ * int status (0 = KOMD_OK); the message of the last failure on the calling
+ * thread is komd_gpu_last_error().  Calls are synchronous from the caller's
+ * view (they end with a stream synchronize), like the reference's functor
+ * calls that end in Kokkos::fence (potentials/ForceFunctor.cpp:13,
+ * integrators/Integrator.cpp:16,25), unless documented otherwise.
+ *
+ * Each entry point names the reference interface it replaces
+ * (Snapex2409/KoMD, src/...).  No Kokkos, torch or other types cross the
+ * boundary: plain pointers, sizes and PODs only.
+ */
+#ifndef KOMD_GPU_H
+#define KOMD_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KOMD_GPU_ABI_VERSION 1
+
+/* status codes */
+enum {
+    KOMD_OK = 0,
+    KOMD_ERR_ARG = 1,        /* invalid argument or configuration                  */
+    KOMD_ERR_CUDA = 2,       /* CUDA runtime error (message has the CUDA string)   */
+    KOMD_ERR_OVERFLOW = 3,   /* a device-side capacity was exceeded (flagged, not trapped) */
+    KOMD_ERR_STATE = 4,      /* call out of order (e.g. no sites uploaded)         */
+    KOMD_ERR_NOMEM = 5,      /* device allocation failed                           */
+    KOMD_ERR_NONFINITE = 6   /* a NaN/Inf force or position was detected           */
+};
+
+/* arithmetic of the pair and triplet kernels (integration and reductions are FP64 always) */
+enum { KOMD_FP32 = 0, KOMD_FP64 = 1 };
+/* ATM force sign: REFERENCE reproduces potentials/ATM.cpp:55-57 (adds +grad V);
+ * PHYSICAL uses F = -grad V */
+enum { KOMD_ATM_SIGN_REFERENCE = 0, KOMD_ATM_SIGN_PHYSICAL = 1 };
+/* ATM triplet set: COMPAT = the reference's cell-triple enumeration
+ * (container/LinkedCells.h:126-152 + same-cell triples: all three cells equal
+ * or all distinct); FULL = every triplet with all sides inside the cutoff */
+enum { KOMD_ATM_ENUM_COMPAT = 0, KOMD_ATM_ENUM_FULL = 1 };
+/* virial: COMPAT reproduces sensors/PressureSensor.cpp:143-286 (boundary pairs
+ * counted per list entry, no ZZ term for ATM, direct ATM contributes nothing);
+ * CORRECT counts every pair / triplet once */
+enum { KOMD_VIRIAL_COMPAT = 0, KOMD_VIRIAL_CORRECT = 1 };
+
+/* force terms (bit mask) */
+#define KOMD_TERM_LJ      0x01u  /* potentials/LJ12_6.cpp:15-43                 */
+#define KOMD_TERM_FENE    0x02u  /* potentials/FENE.cpp:15-43                   */
+#define KOMD_TERM_LIMIT   0x04u  /* potentials/Limit.cpp:19-25                  */
+#define KOMD_TERM_ATM     0x08u  /* potentials/ATM.cpp / ATM_NOLIST.cpp         */
+#define KOMD_TERM_BONDED  0x10u  /* harmonic bond + angle (no reference counterpart) */
+
+/* measurements (bit mask) */
+#define KOMD_MEASURE_TEMPERATURE 0x01u  /* sensors/TemperatureSensor.cpp:27-48   */
+#define KOMD_MEASURE_ENERGY      0x02u  /* LJ12_6_Sensor total U, ATM and bonded energy */
+#define KOMD_MEASURE_PRESSURE    0x04u  /* sensors/PressureSensor.cpp:28-33        */
+#define KOMD_MEASURE_RDF         0x08u  /* sensors/RDFSensor.cpp:23-34             */
+#define KOMD_MEASURE_LJ_HIST     0x10u  /* Potential_Sensor U(r), F(r) histograms  */
+
+typedef struct komd_config {
+    double domain_low[3];      /* configuration()->domainLow  (IO/Configuration.h)   */
+    double domain_high[3];     /* configuration()->domainHigh                        */
+    double cell_size;          /* configuration()->cell_size; >= both cutoffs        */
+    double cutoff;             /* LJ cutoff, configuration()->cutoff                 */
+    double cutoff_3b;          /* ATM cutoff (the reference reuses cutoff)           */
+    double nu;                 /* ATM coefficient in internal units (ATM.cpp:11-14)  */
+    double delta_t;            /* configuration()->delta_t                           */
+    double stiffness;          /* FENE stiffness factor                              */
+    double limit;              /* Limit factor                                       */
+    double bond_k, bond_r0;    /* harmonic bond  U = k/2 (r - r0)^2                  */
+    double angle_k, angle_theta0; /* harmonic angle U = k/2 (theta - theta0)^2, radians */
+    double max_sigma;          /* LJ sensor histogram range 3*max_sigma              */
+    double rdf_max, rdf_dr;    /* RDF sensor range and bin width                     */
+    uint32_t terms;            /* KOMD_TERM_*                                        */
+    int32_t precision;         /* KOMD_FP32 | KOMD_FP64                              */
+    int32_t atm_sign;          /* KOMD_ATM_SIGN_*                                    */
+    int32_t atm_enum;          /* KOMD_ATM_ENUM_*                                    */
+    int32_t virial_mode;       /* KOMD_VIRIAL_*                                      */
+    int32_t atm_direct;        /* 1: ATM_NOLIST semantics (no ATM virial in COMPAT)  */
+    int32_t lj_bins;           /* sensor_lj_bins                                     */
+    int32_t atm_list_cap;      /* per-site neighbour capacity inside cutoff_3b (0 = 64) */
+} komd_config;
+
+typedef struct komd_observables {
+    double temperature;        /* K, sites inside the domain only                    */
+    double mv2;                /* sum m v^2 over those sites (internal units)        */
+    double n_in_box;           /* number of those sites                              */
+    double u_lj;               /* LJ12_6_Sensor::getCurrentPotential                 */
+    double u_atm;              /* ATM energy (physical V, each triplet once)         */
+    double u_bonded;           /* harmonic bond + angle energy                       */
+    double kinetic[6];         /* sum m v v (XX XY YY XZ YZ ZZ), per virial_mode's site set */
+    double virial[6];          /* pair + triplet (+ bonded in CORRECT) virial         */
+    double pressure[6];        /* kinetic + virial, unscaled (PressureSensor::m_pressures) */
+    int64_t pairs_in_cutoff;   /* LJ site pairs inside the cutoff (each once)        */
+    int64_t triplets;          /* ATM triplets inside the cutoff (each once)         */
+} komd_observables;
+
+typedef struct komd_gpu komd_gpu;
+
+/* ---- lifetime ---------------------------------------------------------- */
+/* Replaces main.cpp:43-66 (container + functors from Configuration). */
+int  komd_gpu_create(const komd_config *cfg, int device, komd_gpu **out);
+int  komd_gpu_destroy(komd_gpu *h);
+const char *komd_gpu_last_error(void);
+int  komd_gpu_abi_version(void);
+/* Runs the engine's work on a caller-provided cudaStream_t (NULL = engine's own). */
+int  komd_gpu_set_stream(komd_gpu *h, void *cuda_stream);
+/* Domain cells per dimension, floor(L / cell_size) (LinkedCells.cpp:19). */
+int  komd_gpu_grid_dims(komd_gpu *h, int64_t nd[3]);
+
+/* ---- sites -------------------------------------------------------------- */
+/* Replaces MoleculeContainer::addMolecule + constructSOAs
+ * (container/MoleculeContainer.cpp:13-53) and CheckpointIO::loadCheckpoint.
+ * Sites in molecule order; consecutive sites with equal mol_id form one
+ * molecule.  r, v: n*3 doubles (x y z per site); m, eps (internal units),
+ * sig: n doubles; mol_id: n uint64. */
+int  komd_gpu_upload_sites(komd_gpu *h, int64_t n, const double *r, const double *v, const double *m,
+                           const double *eps, const double *sig, const uint64_t *mol_id);
+/* Overwrites positions and/or velocities only (NULL keeps a field). */
+int  komd_gpu_set_state(komd_gpu *h, const double *r, const double *v);
+/* Harmonic topology: bonds as site-index pairs, angles as (i, vertex, k). */
+int  komd_gpu_set_topology(komd_gpu *h, int64_t n_bonds, const int64_t *bonds, int64_t n_angles,
+                           const int64_t *angles);
+/* Copies r, v, f (n*3 doubles each, site order) to the host; NULL skips. */
+int  komd_gpu_download(komd_gpu *h, double *r, double *v, double *f);
+int64_t komd_gpu_num_sites(komd_gpu *h);
+
+/* ---- hot path ----------------------------------------------------------- */
+/* LinkedCells::updateContainer (LinkedCells.cpp:65-81): COM, periodic wrap,
+ * f = 0, COM, counting-sort binning, cell-sorted FP32/FP64 positions. */
+int  komd_gpu_update_container(komd_gpu *h);
+/* All configured ForceFunctor / ForceFunctor3B terms in the reference order
+ * (LJ, FENE, bonded, Limit, then ATM; Simulation.cpp:57-59); needs a prior
+ * update_container. */
+int  komd_gpu_forces(komd_gpu *h);
+/* Integrator::integrate0 / integrate1 (integrators/Integrator.cpp:10-37). */
+int  komd_gpu_integrate0(komd_gpu *h);
+int  komd_gpu_integrate1(komd_gpu *h);
+/* n full steps of Simulation::run's loop body without thermostat or plugins
+ * (integrate0, updateContainer, forces, integrate1), replayed from one CUDA
+ * graph.  Requires forces of the current positions (call update_container +
+ * forces once before the first step_n). */
+int  komd_gpu_step(komd_gpu *h, int64_t n_steps);
+/* Same as komd_gpu_step, end to end from host buffers: uploads r, v (n*3) from
+ * the host, runs n_steps, downloads r, v and f.  Host buffers may be pinned. */
+int  komd_gpu_step_host(komd_gpu *h, int64_t n_steps, double *r, double *v, double *f);
+
+/* ---- sensors ------------------------------------------------------------ */
+/* Sensor::measure of the selected sensors (sensors/Sensor.h:15-33).  Uses
+ * the current container/forces state; rdf (may be NULL) receives the raw
+ * histogram of this call (RDFSensor::m_bins for one sample), lj_hist (may be
+ * NULL) 4*lj_bins doubles: U sums, F sums, U counts, F counts. */
+int  komd_gpu_measure(komd_gpu *h, uint32_t mask, komd_observables *obs, double *rdf, double *lj_hist);
+int64_t komd_gpu_rdf_bins(komd_gpu *h);
+
+/* ---- parity dumps ------------------------------------------------------- */
+/* Cell lists of the reference layout ((nd+2)^3 cells incl. halo copies,
+ * LCCellIterator order, LinkedCells.cpp:83-121): count[ncell] and the site
+ * indices of all cells concatenated (idx capacity cap; *total gets the
+ * needed size). */
+int  komd_gpu_get_cells(komd_gpu *h, int64_t *count, int64_t ncell, int64_t *idx, int64_t cap, int64_t *total);
+/* Per-site number of LJ partners with dr2 <= cutoff^2 and a different
+ * molecule ID, evaluated in FP64 with the reference's arithmetic
+ * (LJ12_6.cpp:23-28), so counts are bit-exact. */
+int  komd_gpu_neighbour_counts(komd_gpu *h, int64_t *counts);
+
+/* ---- profiling ---------------------------------------------------------- */
+/* When enabled, every kernel launch outside komd_gpu_step's graph is
+ * bracketed by CUDA events; komd_gpu_profile reports per kernel family the
+ * number of launches and the summed device milliseconds since the last
+ * reset.  names is a '\n'-separated list of families (<= cap bytes). */
+int  komd_gpu_set_profiling(komd_gpu *h, int on);
+int  komd_gpu_profile(komd_gpu *h, int max_families, int64_t *launches, double *ms, char *names, int cap);
+/* Number of kernels one komd_gpu_step launches per step (for accounting). */
+int  komd_gpu_kernels_per_step(komd_gpu *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,701 @@
+// capi.cu -- the C ABI of include/komd_gpu.h: engine lifetime, buffers,
+// the per-step launch sequence, CUDA-graph replay, sensors and parity dumps.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "engine.cuh"
+#include "kernels.cuh"
+
+using namespace komd;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define CK(call)                                                                                       \
+    do {                                                                                               \
+        cudaError_t _e = (call);                                                                       \
+        if (_e != cudaSuccess)                                                                         \
+            return fail(_e == cudaErrorMemoryAllocation ? KOMD_ERR_NOMEM : KOMD_ERR_CUDA,              \
+                        std::string(#call) + ": " + cudaGetErrorString(_e));                          \
+    } while (0)
+
+template <typename T>
+void dfree(T *&p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+template <typename T>
+cudaError_t dalloc(T *&p, size_t count) {
+    dfree(p);
+    if (count == 0) count = 1;
+    return cudaMalloc(reinterpret_cast<void **>(&p), sizeof(T) * count);
+}
+
+// SciValue arithmetic (math/SciValue.{h,cpp}): mantissa normalised into
+// (0.1, 10) by repeated /10, *10; converted as m * pow(10, e).
+struct Sci { double m; long long e; };
+Sci sci_norm(double m, long long e) {
+    double a = std::fabs(m);
+    while (a >= 10.0) { m /= 10.0; e += 1; a = std::fabs(m); }
+    while (a <= 0.1) { m *= 10.0; e -= 1; a = std::fabs(m); }
+    return {m, e};
+}
+Sci sci_from(double v) { return v == 0.0 ? Sci{0.0, 0} : sci_norm(v, 0); }
+Sci sci_mul(Sci a, Sci b) { return sci_norm(a.m * b.m, a.e + b.e); }
+Sci sci_div(Sci a, Sci b) { return sci_norm(a.m / b.m, a.e - b.e); }
+double sci_val(Sci a) { return a.m * std::pow(10.0, (double)a.e); }
+
+// TemperatureSensor's conversion (TemperatureSensor.cpp:44-47)
+double temperature_from(double mv2, double n_in_box) {
+    const Sci kB = sci_norm(1.380649, -23), da = sci_norm(1.66053906892, -27), aps = sci_norm(1.0, 2);
+    const Sci factor = sci_mul(sci_mul(aps, aps), sci_div(da, kB));
+    return sci_val(sci_mul(factor, sci_from(mv2 / (n_in_box * 3))));
+}
+
+// ---------------------------------------------------------------------------
+// profiling: event pairs per kernel family
+// ---------------------------------------------------------------------------
+const char *kFamilies[] = {"container", "pair", "bonded", "limit", "atm", "integrate", "measure"};
+constexpr int kNumFamilies = 7;
+enum Fam { F_CONTAINER = 0, F_PAIR, F_BONDED, F_LIMIT, F_ATM, F_INTEGRATE, F_MEASURE };
+
+}  // namespace
+
+struct komd_gpu {
+    Engine e;
+    double *f_scratch = nullptr;
+    double *acc = nullptr;            // R_NSLOTS
+    int partial_cap = 0;
+    bool want_posd = false;
+    // profiling
+    std::vector<cudaEvent_t> pool;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+    int64_t launches[kNumFamilies] = {0};
+    double ms[kNumFamilies] = {0};
+    int64_t graph_steps = 0;
+};
+
+namespace {
+
+cudaEvent_t take_event(komd_gpu *h) {
+    if (!h->pool.empty()) {
+        cudaEvent_t ev = h->pool.back();
+        h->pool.pop_back();
+        return ev;
+    }
+    cudaEvent_t ev;
+    cudaEventCreate(&ev);
+    return ev;
+}
+
+struct ProfScope {
+    komd_gpu *h;
+    int fam;
+    cudaEvent_t a = nullptr, b = nullptr;
+    ProfScope(komd_gpu *h_, int fam_) : h(h_), fam(fam_) {
+        if (!h->e.profiling) return;
+        a = take_event(h);
+        b = take_event(h);
+        cudaEventRecord(a, h->e.stream);
+    }
+    ~ProfScope() {
+        if (!a) return;
+        cudaEventRecord(b, h->e.stream);
+        h->pending.push_back({fam, {a, b}});
+    }
+};
+
+void collect_profile(komd_gpu *h) {
+    if (h->pending.empty()) return;
+    cudaStreamSynchronize(h->e.stream);
+    for (auto &p : h->pending) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, p.second.first, p.second.second);
+        h->launches[p.first] += 1;
+        h->ms[p.first] += t;
+        h->pool.push_back(p.second.first);
+        h->pool.push_back(p.second.second);
+    }
+    h->pending.clear();
+}
+
+int check_launch(const char *what) {
+    const cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return fail(KOMD_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(err));
+    return KOMD_OK;
+}
+
+int ensure_partials(komd_gpu *h) {
+    Engine &e = h->e;
+    int need = pair_grid(e);
+    need = std::max(need, atm_grid(e));
+    need = std::max(need, kinetic_grid(e));
+    if (need > h->partial_cap) {
+        CK(dalloc(e.partials, (size_t)need * R_NSLOTS));
+        h->partial_cap = need;
+    }
+    return KOMD_OK;
+}
+
+// the force sequence of Simulation::run: 2-body functors (LJ / FENE, bonded,
+// Limit), then the 3-body functor (ATM)
+void enqueue_forces(komd_gpu *h, bool measure, double *lj_hist) {
+    Engine &e = h->e;
+    cudaStream_t st = e.stream;
+    {
+        ProfScope ps(h, F_PAIR);
+        launch_pair(e, st, measure, lj_hist);
+    }
+    if (measure) launch_sum_partials(st, pair_grid(e), e.partials, h->acc);
+    if ((e.cfg.terms & KOMD_TERM_BONDED) && (e.n_bonds > 0 || e.n_angles > 0)) {
+        ProfScope ps(h, F_BONDED);
+        launch_bonded(e, st, measure, h->acc);
+    }
+    if (e.cfg.terms & KOMD_TERM_LIMIT) {
+        ProfScope ps(h, F_LIMIT);
+        launch_limit(e, st);
+    }
+    if (e.cfg.terms & KOMD_TERM_ATM) {
+        ProfScope ps(h, F_ATM);
+        launch_atm(e, st, measure);
+    }
+    if (measure && (e.cfg.terms & KOMD_TERM_ATM)) launch_sum_partials(st, atm_grid(e), e.partials, h->acc);
+}
+
+void enqueue_step(komd_gpu *h) {
+    Engine &e = h->e;
+    {
+        ProfScope ps(h, F_INTEGRATE);
+        launch_step0(e, e.stream);
+    }
+    {
+        ProfScope ps(h, F_CONTAINER);
+        launch_container(e, e.stream);
+    }
+    enqueue_forces(h, false, nullptr);
+    {
+        ProfScope ps(h, F_INTEGRATE);
+        launch_step1(e, e.stream);
+    }
+}
+
+int read_flags(komd_gpu *h, int flags[E_NFLAGS], bool clear) {
+    Engine &e = h->e;
+    CK(cudaMemcpyAsync(flags, e.err, sizeof(int) * E_NFLAGS, cudaMemcpyDeviceToHost, e.stream));
+    if (clear) CK(cudaMemsetAsync(e.err, 0, sizeof(int) * E_NFLAGS, e.stream));
+    CK(cudaStreamSynchronize(e.stream));
+    return KOMD_OK;
+}
+
+int alloc_atm_list(komd_gpu *h, int cap) {
+    Engine &e = h->e;
+    e.nl_cap = cap;
+    if (e.cfg.terms & KOMD_TERM_ATM) {
+        const size_t entry = e.cfg.precision == KOMD_FP64 ? 32 : 16;
+        float4 *p = nullptr;
+        dfree(e.nl);
+        CK(cudaMalloc(reinterpret_cast<void **>(&p), entry * (size_t)cap * (size_t)std::max<int64_t>(e.n, 1)));
+        e.nl = p;
+        CK(dalloc(e.nl_count, e.n));
+        set_kernel_attributes(e);
+    }
+    if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+    e.graph_valid = false;
+    return KOMD_OK;
+}
+
+int ensure_posd(komd_gpu *h) {
+    Engine &e = h->e;
+    if (e.posd) return KOMD_OK;
+    CK(dalloc(e.posd, 3 * (size_t)e.n));
+    CK(dalloc(e.seps_d, e.n));
+    CK(dalloc(e.sig_d, e.n));
+    if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+    e.graph_valid = false;
+    return KOMD_OK;
+}
+
+int validate(const komd_config *c, Grid &g) {
+    if (!c) return fail(KOMD_ERR_ARG, "null config");
+    if (!(c->cell_size > 0)) return fail(KOMD_ERR_ARG, "cell_size must be > 0");
+    const bool lj = (c->terms & KOMD_TERM_LJ) != 0, atm = (c->terms & KOMD_TERM_ATM) != 0;
+    if (lj && !(c->cutoff > 0)) return fail(KOMD_ERR_ARG, "cutoff must be > 0");
+    if (c->cell_size < c->cutoff)
+        return fail(KOMD_ERR_ARG, "cell size must be larger or equal to cutoff radius");
+    if (atm && (!(c->cutoff_3b > 0) || c->cell_size < c->cutoff_3b))
+        return fail(KOMD_ERR_ARG, "cutoff_3b must be > 0 and <= cell_size");
+    if (!(c->delta_t > 0)) return fail(KOMD_ERR_ARG, "delta_t must be > 0");
+    if (c->precision != KOMD_FP32 && c->precision != KOMD_FP64) return fail(KOMD_ERR_ARG, "bad precision");
+    g.cs = c->cell_size;
+    g.ncell = 1;
+    for (int d = 0; d < 3; d++) {
+        g.low[d] = c->domain_low[d];
+        g.high[d] = c->domain_high[d];
+        g.L[d] = c->domain_high[d] - c->domain_low[d];
+        const double q = std::floor(g.L[d] / c->cell_size);   // math::ufloor (LinkedCells.cpp:19)
+        if (!(q >= 3.0))
+            return fail(KOMD_ERR_ARG, "need at least 3 domain cells per dimension (floor(L / cell_size) >= 3)");
+        if (q > 1 << 20) return fail(KOMD_ERR_ARG, "too many cells");
+        g.nd[d] = (int)q;
+        g.ncell *= g.nd[d];
+    }
+    return KOMD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *komd_gpu_last_error(void) { return g_last_error.c_str(); }
+int komd_gpu_abi_version(void) { return KOMD_GPU_ABI_VERSION; }
+
+int komd_gpu_create(const komd_config *cfg, int device, komd_gpu **out) {
+    if (!out) return fail(KOMD_ERR_ARG, "null output handle");
+    *out = nullptr;
+    Grid g;
+    const int rc = validate(cfg, g);
+    if (rc) return rc;
+    CK(cudaSetDevice(device));
+    komd_gpu *h = new komd_gpu();
+    Engine &e = h->e;
+    e.cfg = *cfg;
+    if (e.cfg.lj_bins <= 0) e.cfg.lj_bins = 100;
+    if (!(e.cfg.max_sigma > 0)) e.cfg.max_sigma = 1.0;
+    e.g = g;
+    e.device = device;
+    if (cudaStreamCreateWithFlags(&e.stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete h;
+        return fail(KOMD_ERR_CUDA, "stream creation failed");
+    }
+    e.own_stream = true;
+    if (dalloc(e.cell_count, g.ncell) || dalloc(e.cell_start, g.ncell + 1) || dalloc(e.cell_mcount, g.ncell) ||
+        dalloc(e.cell_mstart, g.ncell + 1) || dalloc(e.err, E_NFLAGS) || dalloc(h->acc, R_NSLOTS)) {
+        komd_gpu_destroy(h);
+        return fail(KOMD_ERR_NOMEM, "device allocation failed");
+    }
+    cudaMemset(e.err, 0, sizeof(int) * E_NFLAGS);
+    if (e.cfg.rdf_dr > 0 && e.cfg.rdf_max > 0) {
+        e.rdf_bins = (int64_t)(uint64_t)(e.cfg.rdf_max / e.cfg.rdf_dr);   // RDFSensor.cpp:18
+        if (e.rdf_bins > 0 && dalloc(e.rdf, e.rdf_bins)) { komd_gpu_destroy(h); return fail(KOMD_ERR_NOMEM, "rdf"); }
+    }
+    if (dalloc(e.lj_hist, 4 * (size_t)e.cfg.lj_bins)) { komd_gpu_destroy(h); return fail(KOMD_ERR_NOMEM, "hist"); }
+    h->want_posd = e.cfg.precision == KOMD_FP64;
+    *out = h;
+    return KOMD_OK;
+}
+
+int komd_gpu_destroy(komd_gpu *h) {
+    if (!h) return KOMD_OK;
+    Engine &e = h->e;
+    cudaSetDevice(e.device);
+    if (e.stream) cudaStreamSynchronize(e.stream);
+    if (e.graph) cudaGraphExecDestroy(e.graph);
+    dfree(e.r); dfree(e.v); dfree(e.f); dfree(e.m); dfree(e.eps); dfree(e.sig);
+    dfree(e.key); dfree(e.site_mol); dfree(e.site_slot);
+    dfree(e.mol_off); dfree(e.mol_cell); dfree(e.mol_rank); dfree(e.com);
+    dfree(e.cell_count); dfree(e.cell_start); dfree(e.cell_mcount); dfree(e.cell_mstart); dfree(e.cell_mols);
+    dfree(e.slot_site); dfree(e.skey); dfree(e.pos4); dfree(e.seps); dfree(e.posd); dfree(e.seps_d); dfree(e.sig_d);
+    dfree(e.nl); dfree(e.nl_count); dfree(e.bonds); dfree(e.angles); dfree(e.partials); dfree(e.err);
+    dfree(e.rdf); dfree(e.lj_hist); dfree(e.counts); dfree(h->f_scratch); dfree(h->acc);
+    for (auto &p : h->pending) { h->pool.push_back(p.second.first); h->pool.push_back(p.second.second); }
+    for (auto ev : h->pool) cudaEventDestroy(ev);
+    if (e.own_stream && e.stream) cudaStreamDestroy(e.stream);
+    delete h;
+    return KOMD_OK;
+}
+
+int komd_gpu_set_stream(komd_gpu *h, void *stream) {
+    if (!h) return fail(KOMD_ERR_ARG, "null handle");
+    Engine &e = h->e;
+    CK(cudaStreamSynchronize(e.stream));
+    if (e.own_stream) cudaStreamDestroy(e.stream);
+    if (stream) {
+        e.stream = (cudaStream_t)stream;
+        e.own_stream = false;
+    } else {
+        CK(cudaStreamCreateWithFlags(&e.stream, cudaStreamNonBlocking));
+        e.own_stream = true;
+    }
+    if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+    e.graph_valid = false;
+    return KOMD_OK;
+}
+
+int komd_gpu_grid_dims(komd_gpu *h, int64_t nd[3]) {
+    if (!h || !nd) return fail(KOMD_ERR_ARG, "null argument");
+    for (int d = 0; d < 3; d++) nd[d] = h->e.g.nd[d];
+    return KOMD_OK;
+}
+
+int64_t komd_gpu_num_sites(komd_gpu *h) { return h ? h->e.n : -1; }
+
+int komd_gpu_upload_sites(komd_gpu *h, int64_t n, const double *r, const double *v, const double *m,
+                          const double *eps, const double *sig, const uint64_t *mol_id) {
+    if (!h || n <= 0 || !r || !v || !m || !eps || !sig || !mol_id) return fail(KOMD_ERR_ARG, "bad site arrays");
+    if (n >= (int64_t)1 << 31) return fail(KOMD_ERR_ARG, "too many sites");
+    Engine &e = h->e;
+    CK(cudaSetDevice(e.device));
+    if ((e.cfg.terms & KOMD_TERM_ATM) && n > kMaxAtmSlot)
+        return fail(KOMD_ERR_ARG, "ATM supports at most 2^25 - 1 sites per system");
+    // molecules: consecutive equal IDs (CheckpointIO.cpp:55-72); dense keys keep ID equality
+    std::vector<int> off, key(n), site_mol(n);
+    std::unordered_map<uint64_t, int> dense;
+    dense.reserve((size_t)n);
+    for (int64_t s = 0; s < n; s++) {
+        if (s == 0 || mol_id[s] != mol_id[s - 1]) off.push_back((int)s);
+        site_mol[s] = (int)off.size() - 1;
+        auto it = dense.find(mol_id[s]);
+        if (it == dense.end()) it = dense.emplace(mol_id[s], (int)dense.size()).first;
+        key[s] = it->second;
+        if (!(m[s] > 0)) return fail(KOMD_ERR_ARG, "site masses must be > 0");
+    }
+    off.push_back((int)n);
+    e.n = n;
+    e.n_mol = (int64_t)off.size() - 1;
+    CK(dalloc(e.r, 3 * n)); CK(dalloc(e.v, 3 * n)); CK(dalloc(e.f, 3 * n)); CK(dalloc(h->f_scratch, 3 * n));
+    CK(dalloc(e.m, n)); CK(dalloc(e.eps, n)); CK(dalloc(e.sig, n));
+    CK(dalloc(e.key, n)); CK(dalloc(e.site_mol, n)); CK(dalloc(e.site_slot, n));
+    CK(dalloc(e.mol_off, e.n_mol + 1)); CK(dalloc(e.mol_cell, e.n_mol)); CK(dalloc(e.mol_rank, e.n_mol));
+    CK(dalloc(e.com, 3 * e.n_mol)); CK(dalloc(e.cell_mols, e.n_mol));
+    CK(dalloc(e.slot_site, n)); CK(dalloc(e.skey, n)); CK(dalloc(e.pos4, n)); CK(dalloc(e.seps, n));
+    CK(dalloc(e.counts, n));
+    dfree(e.posd); dfree(e.seps_d); dfree(e.sig_d);
+    if (h->want_posd) {
+        CK(dalloc(e.posd, 3 * (size_t)n)); CK(dalloc(e.seps_d, n)); CK(dalloc(e.sig_d, n));
+    }
+    CK(cudaMemcpy(e.r, r, sizeof(double) * 3 * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e.v, v, sizeof(double) * 3 * n, cudaMemcpyHostToDevice));
+    CK(cudaMemset(e.f, 0, sizeof(double) * 3 * n));
+    CK(cudaMemcpy(e.m, m, sizeof(double) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e.eps, eps, sizeof(double) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e.sig, sig, sizeof(double) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e.key, key.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e.site_mol, site_mol.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e.mol_off, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice));
+    // ATM list capacity: 1.6x the mean neighbour count inside cutoff_3b + 16
+    int cap = e.cfg.atm_list_cap;
+    if (cap <= 0) {
+        const double vol = e.g.L[0] * e.g.L[1] * e.g.L[2];
+        const double rc = e.cfg.cutoff_3b;
+        const double mean = (double)n / vol * 4.18879 * rc * rc * rc;
+        cap = (int)std::ceil(1.6 * mean + 16);
+        cap = std::max(32, std::min(1024, (cap + 7) / 8 * 8));
+    }
+    int rc = alloc_atm_list(h, cap);
+    if (rc) return rc;
+    rc = ensure_partials(h);
+    if (rc) return rc;
+    e.have_sites = true;
+    e.have_cells = e.have_forces = false;
+    if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+    e.graph_valid = false;
+    return KOMD_OK;
+}
+
+int komd_gpu_set_state(komd_gpu *h, const double *r, const double *v) {
+    if (!h || !h->e.have_sites) return fail(KOMD_ERR_STATE, "no sites uploaded");
+    Engine &e = h->e;
+    if (r) CK(cudaMemcpyAsync(e.r, r, sizeof(double) * 3 * e.n, cudaMemcpyHostToDevice, e.stream));
+    if (v) CK(cudaMemcpyAsync(e.v, v, sizeof(double) * 3 * e.n, cudaMemcpyHostToDevice, e.stream));
+    CK(cudaStreamSynchronize(e.stream));
+    if (r) e.have_cells = e.have_forces = false;
+    return KOMD_OK;
+}
+
+int komd_gpu_set_topology(komd_gpu *h, int64_t n_bonds, const int64_t *bonds, int64_t n_angles,
+                          const int64_t *angles) {
+    if (!h || !h->e.have_sites) return fail(KOMD_ERR_STATE, "no sites uploaded");
+    Engine &e = h->e;
+    std::vector<int> b(2 * std::max<int64_t>(n_bonds, 0)), a(3 * std::max<int64_t>(n_angles, 0));
+    for (int64_t k = 0; k < 2 * n_bonds; k++) {
+        if (bonds[k] < 0 || bonds[k] >= e.n) return fail(KOMD_ERR_ARG, "bond index out of range");
+        b[k] = (int)bonds[k];
+    }
+    for (int64_t k = 0; k < 3 * n_angles; k++) {
+        if (angles[k] < 0 || angles[k] >= e.n) return fail(KOMD_ERR_ARG, "angle index out of range");
+        a[k] = (int)angles[k];
+    }
+    CK(dalloc(e.bonds, b.size()));
+    CK(dalloc(e.angles, a.size()));
+    if (!b.empty()) CK(cudaMemcpy(e.bonds, b.data(), sizeof(int) * b.size(), cudaMemcpyHostToDevice));
+    if (!a.empty()) CK(cudaMemcpy(e.angles, a.data(), sizeof(int) * a.size(), cudaMemcpyHostToDevice));
+    e.n_bonds = std::max<int64_t>(n_bonds, 0);
+    e.n_angles = std::max<int64_t>(n_angles, 0);
+    if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+    e.graph_valid = false;
+    return KOMD_OK;
+}
+
+int komd_gpu_download(komd_gpu *h, double *r, double *v, double *f) {
+    if (!h || !h->e.have_sites) return fail(KOMD_ERR_STATE, "no sites uploaded");
+    Engine &e = h->e;
+    if (r) CK(cudaMemcpyAsync(r, e.r, sizeof(double) * 3 * e.n, cudaMemcpyDeviceToHost, e.stream));
+    if (v) CK(cudaMemcpyAsync(v, e.v, sizeof(double) * 3 * e.n, cudaMemcpyDeviceToHost, e.stream));
+    if (f) CK(cudaMemcpyAsync(f, e.f, sizeof(double) * 3 * e.n, cudaMemcpyDeviceToHost, e.stream));
+    CK(cudaStreamSynchronize(e.stream));
+    return KOMD_OK;
+}
+
+int komd_gpu_update_container(komd_gpu *h) {
+    if (!h || !h->e.have_sites) return fail(KOMD_ERR_STATE, "no sites uploaded");
+    Engine &e = h->e;
+    {
+        ProfScope ps(h, F_CONTAINER);
+        launch_container(e, e.stream);
+    }
+    CK(cudaMemsetAsync(e.f, 0, sizeof(double) * 3 * e.n, e.stream));   // FReset_Kernel
+    int rc = check_launch("update_container");
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(e.stream));
+    e.have_cells = true;
+    e.have_forces = false;
+    return KOMD_OK;
+}
+
+int komd_gpu_forces(komd_gpu *h) {
+    if (!h || !h->e.have_cells) return fail(KOMD_ERR_STATE, "update_container must run before forces");
+    Engine &e = h->e;
+    for (int attempt = 0; attempt < 6; attempt++) {
+        enqueue_forces(h, false, nullptr);
+        int rc = check_launch("forces");
+        if (rc) return rc;
+        int flags[E_NFLAGS];
+        rc = read_flags(h, flags, true);
+        if (rc) return rc;
+        if (!flags[E_ATM_OVERFLOW]) {
+            e.have_forces = true;
+            return KOMD_OK;
+        }
+        if (e.nl_cap >= 1024) break;
+        rc = alloc_atm_list(h, std::min(1024, e.nl_cap * 2));   // grow and recompute
+        if (rc) return rc;
+    }
+    return fail(KOMD_ERR_OVERFLOW, "ATM neighbour list exceeds 1024 entries per site");
+}
+
+int komd_gpu_integrate0(komd_gpu *h) {
+    if (!h || !h->e.have_sites) return fail(KOMD_ERR_STATE, "no sites uploaded");
+    {
+        ProfScope ps(h, F_INTEGRATE);
+        launch_step0(h->e, h->e.stream);
+    }
+    int rc = check_launch("integrate0");
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(h->e.stream));
+    h->e.have_cells = h->e.have_forces = false;
+    return KOMD_OK;
+}
+
+int komd_gpu_integrate1(komd_gpu *h) {
+    if (!h || !h->e.have_sites) return fail(KOMD_ERR_STATE, "no sites uploaded");
+    {
+        ProfScope ps(h, F_INTEGRATE);
+        launch_step1(h->e, h->e.stream);
+    }
+    int rc = check_launch("integrate1");
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(h->e.stream));
+    return KOMD_OK;
+}
+
+static int finish_steps(komd_gpu *h) {
+    int flags[E_NFLAGS];
+    int rc = read_flags(h, flags, true);
+    if (rc) return rc;
+    if (flags[E_ATM_OVERFLOW])
+        return fail(KOMD_ERR_OVERFLOW, "ATM neighbour list overflowed during the steps (raise atm_list_cap)");
+    if (flags[E_NONFINITE]) return fail(KOMD_ERR_NONFINITE, "non-finite velocity after a step");
+    return KOMD_OK;
+}
+
+int komd_gpu_step(komd_gpu *h, int64_t n_steps) {
+    if (!h || !h->e.have_sites) return fail(KOMD_ERR_STATE, "no sites uploaded");
+    Engine &e = h->e;
+    if (!e.have_forces) return fail(KOMD_ERR_STATE, "call update_container and forces before step");
+    if (n_steps <= 0) return KOMD_OK;
+    if (e.profiling) {
+        for (int64_t k = 0; k < n_steps; k++) enqueue_step(h);
+        int rc = check_launch("step");
+        if (rc) return rc;
+        return finish_steps(h);
+    }
+    if (!e.graph_valid) {
+        cudaGraph_t graph;
+        CK(cudaStreamBeginCapture(e.stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_step(h);
+        CK(cudaStreamEndCapture(e.stream, &graph));
+        if (e.graph) cudaGraphExecDestroy(e.graph);
+        const cudaError_t ie = cudaGraphInstantiate(&e.graph, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) return fail(KOMD_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+        e.graph_valid = true;
+    }
+    for (int64_t k = 0; k < n_steps; k++) CK(cudaGraphLaunch(e.graph, e.stream));
+    h->graph_steps += n_steps;
+    return finish_steps(h);
+}
+
+int komd_gpu_step_host(komd_gpu *h, int64_t n_steps, double *r, double *v, double *f) {
+    if (!h || !h->e.have_sites) return fail(KOMD_ERR_STATE, "no sites uploaded");
+    Engine &e = h->e;
+    if (r) CK(cudaMemcpyAsync(e.r, r, sizeof(double) * 3 * e.n, cudaMemcpyHostToDevice, e.stream));
+    if (v) CK(cudaMemcpyAsync(e.v, v, sizeof(double) * 3 * e.n, cudaMemcpyHostToDevice, e.stream));
+    int rc = komd_gpu_step(h, n_steps);
+    if (rc) return rc;
+    return komd_gpu_download(h, r, v, f);
+}
+
+int64_t komd_gpu_rdf_bins(komd_gpu *h) { return h ? h->e.rdf_bins : -1; }
+
+int komd_gpu_measure(komd_gpu *h, uint32_t mask, komd_observables *obs, double *rdf, double *lj_hist) {
+    if (!h || !obs) return fail(KOMD_ERR_ARG, "null argument");
+    Engine &e = h->e;
+    if (!e.have_cells) return fail(KOMD_ERR_STATE, "update_container must run before measure");
+    std::memset(obs, 0, sizeof(*obs));
+    cudaStream_t st = e.stream;
+    ProfScope ps(h, F_MEASURE);
+    CK(cudaMemsetAsync(h->acc, 0, sizeof(double) * R_NSLOTS, st));
+    const bool need_forces = (mask & (KOMD_MEASURE_ENERGY | KOMD_MEASURE_PRESSURE | KOMD_MEASURE_LJ_HIST)) != 0;
+    if (need_forces) {
+        // re-evaluate the force terms into a scratch force buffer (the sensors of
+        // the reference re-run their functors as well); f itself is untouched
+        if (mask & KOMD_MEASURE_LJ_HIST) CK(cudaMemsetAsync(e.lj_hist, 0, sizeof(double) * 4 * e.cfg.lj_bins, st));
+        double *keep = e.f;
+        CK(cudaMemsetAsync(h->f_scratch, 0, sizeof(double) * 3 * e.n, st));
+        e.f = h->f_scratch;
+        enqueue_forces(h, true, (mask & KOMD_MEASURE_LJ_HIST) ? e.lj_hist : nullptr);
+        e.f = keep;
+    }
+    const int n_terms = e.cfg.virial_mode == KOMD_VIRIAL_COMPAT ? (int)e.n_mol : (int)e.n;
+    launch_kinetic(e, st, n_terms);
+    launch_sum_partials(st, kinetic_grid(e), e.partials, h->acc);
+    if ((mask & KOMD_MEASURE_RDF) && e.rdf_bins > 0) {
+        CK(cudaMemsetAsync(e.rdf, 0, sizeof(double) * e.rdf_bins, st));
+        double minw = 1e300;
+        for (int d = 0; d < 3; d++) minw = std::min(minw, e.cfg.cell_size);
+        launch_rdf(e, st, e.rdf, e.cfg.rdf_max <= minw);
+    }
+    int rc = check_launch("measure");
+    if (rc) return rc;
+    double acc[R_NSLOTS];
+    CK(cudaMemcpyAsync(acc, h->acc, sizeof(acc), cudaMemcpyDeviceToHost, st));
+    if (rdf && (mask & KOMD_MEASURE_RDF) && e.rdf_bins > 0)
+        CK(cudaMemcpyAsync(rdf, e.rdf, sizeof(double) * e.rdf_bins, cudaMemcpyDeviceToHost, st));
+    if (lj_hist && (mask & KOMD_MEASURE_LJ_HIST))
+        CK(cudaMemcpyAsync(lj_hist, e.lj_hist, sizeof(double) * 4 * e.cfg.lj_bins, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    int flags[E_NFLAGS];
+    rc = read_flags(h, flags, true);
+    if (rc) return rc;
+    if (flags[E_ATM_OVERFLOW]) return fail(KOMD_ERR_OVERFLOW, "ATM neighbour list overflow during measure");
+    obs->mv2 = acc[R_MV2];
+    obs->n_in_box = acc[R_NBOX];
+    obs->temperature = acc[R_NBOX] > 0 ? temperature_from(acc[R_MV2], acc[R_NBOX]) : 0.0;
+    obs->u_lj = acc[R_ULJ];
+    obs->u_atm = acc[R_UATM];
+    obs->u_bonded = acc[R_UBOND];
+    for (int k = 0; k < 6; k++) {
+        obs->kinetic[k] = acc[R_K0 + k];
+        obs->virial[k] = acc[R_W0 + k];
+        obs->pressure[k] = obs->kinetic[k] + obs->virial[k];
+    }
+    obs->pairs_in_cutoff = (int64_t)std::llround(acc[R_PAIRS]);
+    obs->triplets = (int64_t)std::llround(acc[R_TRIPS]);
+    return KOMD_OK;
+}
+
+int komd_gpu_get_cells(komd_gpu *h, int64_t *count, int64_t ncell, int64_t *idx, int64_t cap, int64_t *total) {
+    if (!h || !h->e.have_cells) return fail(KOMD_ERR_STATE, "update_container must run first");
+    Engine &e = h->e;
+    const int nx = e.g.nd[0] + 2, ny = e.g.nd[1] + 2, nz = e.g.nd[2] + 2;
+    const int64_t nall = (int64_t)nx * ny * nz;
+    std::vector<int> start(e.g.ncell + 1), slot_site(e.n);
+    CK(cudaMemcpy(start.data(), e.cell_start, sizeof(int) * (e.g.ncell + 1), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(slot_site.data(), e.slot_site, sizeof(int) * e.n, cudaMemcpyDeviceToHost));
+    int64_t need = 0, w = 0;
+    for (int z = 0; z < nz; z++)
+        for (int y = 0; y < ny; y++)
+            for (int x = 0; x < nx; x++) {
+                // halo layer 0 copies domain cell nd, layer nd+1 copies cell 1 (LinkedCells.cpp:105-120)
+                auto src = [](int c, int nd) { return c == 0 ? nd - 1 : (c == nd + 1 ? 0 : c - 1); };
+                const int dc = src(x, e.g.nd[0]) + e.g.nd[0] * (src(y, e.g.nd[1]) + e.g.nd[1] * src(z, e.g.nd[2]));
+                const int64_t lin = x + (int64_t)nx * (y + (int64_t)ny * z);
+                const int s0 = start[dc], s1 = start[dc + 1];
+                if (count && lin < ncell) count[lin] = s1 - s0;
+                for (int s = s0; s < s1; s++) {
+                    if (idx && w < cap) idx[w] = slot_site[s];
+                    w++;
+                }
+                need += s1 - s0;
+            }
+    if (total) *total = need;
+    if (count && ncell < nall) return fail(KOMD_ERR_ARG, "count array too small for (nd+2)^3 cells");
+    return KOMD_OK;
+}
+
+int komd_gpu_neighbour_counts(komd_gpu *h, int64_t *counts) {
+    if (!h || !counts) return fail(KOMD_ERR_ARG, "null argument");
+    Engine &e = h->e;
+    if (!e.have_cells) return fail(KOMD_ERR_STATE, "update_container must run first");
+    if (!e.posd) {
+        h->want_posd = true;
+        int rc = ensure_posd(h);
+        if (rc) return rc;
+        launch_container(e, e.stream);   // idempotent: positions are already wrapped
+    }
+    launch_counts(e, e.stream);
+    int rc = check_launch("neighbour_counts");
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(counts, e.counts, sizeof(int64_t) * e.n, cudaMemcpyDeviceToHost, e.stream));
+    CK(cudaStreamSynchronize(e.stream));
+    return KOMD_OK;
+}
+
+int komd_gpu_set_profiling(komd_gpu *h, int on) {
+    if (!h) return fail(KOMD_ERR_ARG, "null handle");
+    collect_profile(h);
+    h->e.profiling = on != 0;
+    for (int k = 0; k < kNumFamilies; k++) { h->launches[k] = 0; h->ms[k] = 0.0; }
+    return KOMD_OK;
+}
+
+int komd_gpu_profile(komd_gpu *h, int max_families, int64_t *launches, double *ms, char *names, int cap) {
+    if (!h) return fail(KOMD_ERR_ARG, "null handle");
+    collect_profile(h);
+    std::string s;
+    for (int k = 0; k < kNumFamilies && k < max_families; k++) {
+        if (launches) launches[k] = h->launches[k];
+        if (ms) ms[k] = h->ms[k];
+        s += kFamilies[k];
+        s += '\n';
+    }
+    if (names && cap > 0) {
+        std::strncpy(names, s.c_str(), (size_t)cap - 1);
+        names[cap - 1] = 0;
+    }
+    return kNumFamilies;
+}
+
+int komd_gpu_kernels_per_step(komd_gpu *h) {
+    if (!h) return -1;
+    const Engine &e = h->e;
+    int k = 2 /* integrate */ + 4 /* com/wrap/bin, scan, scatter, cell sort */ + 1 /* pair */;
+    if ((e.cfg.terms & KOMD_TERM_BONDED) && e.n_bonds > 0) k++;
+    if ((e.cfg.terms & KOMD_TERM_BONDED) && e.n_angles > 0) k++;
+    if (e.cfg.terms & KOMD_TERM_LIMIT) k++;
+    if (e.cfg.terms & KOMD_TERM_ATM) k++;
+    return k;
+}
+
+}  // extern "C"

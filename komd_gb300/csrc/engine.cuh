@@ -1,0 +1,194 @@
+// engine.cuh -- device-side state and helpers of the GB300 KoMD force engine.
+//
+// Layout in HBM (n sites, M molecules, C = nd_x*nd_y*nd_z domain cells):
+//   site order (the caller's order, molecules contiguous), FP64:
+//     r, v, f          3 doubles per site (x y z), like the reference's SOA
+//     m, eps, sig      1 double per site
+//   per site: key (dense 32-bit molecule key: equal keys <=> equal mol IDs),
+//             mol (molecule index), slot (position in cell order)
+//   per molecule: off (CSR into sites), com (3 doubles), cell, rank
+//   per cell:     count / start (sites, exclusive prefix), mcount / mstart
+//                 (molecules), mols (molecule indices grouped by cell)
+//   cell order (rebuilt every step by a counting sort, ascending site index
+//   inside a cell, which is the reference's cell-list order):
+//     slot_site    site index per slot
+//     pos4         float4 (x, y, z relative to the cell centre, sigma/2)
+//     posd         3 doubles: absolute position (FP64 kernels, exact counts)
+//     skey         molecule key per slot, seps: sqrt(eps) per slot
+//   ATM neighbour list: cap float4 per slot (vector r_i - r_j, packed code)
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "komd_gpu.h"
+
+namespace komd {
+
+constexpr int kWarpsPerBlock = 8;
+constexpr int kBlock = 32 * kWarpsPerBlock;
+
+// Grid geometry of LinkedCells (LinkedCells.cpp:11-45): nd domain cells per
+// dimension of edge cs, the last one stretched to the domain's high bound.
+struct Grid {
+    double low[3], high[3], L[3];
+    double cs;
+    int nd[3];
+    int ncell;
+};
+
+// Reduction slots (FP64) written per block and summed on the host side of a measure.
+enum RedSlot {
+    R_ULJ = 0, R_UATM, R_UBOND, R_W0, R_W1, R_W2, R_W3, R_W4, R_W5, R_PAIRS, R_TRIPS,
+    R_MV2, R_NBOX, R_K0, R_K1, R_K2, R_K3, R_K4, R_K5, R_NSLOTS
+};
+
+// device error flags
+enum ErrFlag { E_ATM_OVERFLOW = 0, E_NONFINITE = 1, E_NFLAGS = 4 };
+
+// ---------------------------------------------------------------------------
+// exact FP64 helpers: the reference is built without FMA contraction, so the
+// binning, integration and the FP64 distance test use explicit round-to-
+// nearest intrinsics that the compiler never fuses.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+
+// Reference point of a cell for the FP32 cell-local coordinates.  Any fixed
+// choice works as long as the sort and the force kernels agree; the centre
+// keeps |local| <= half a cell so FP32 keeps ~1e-7 absolute precision.
+__host__ __device__ inline double cell_centre(const Grid &g, int d, int k) {
+    if (k < g.nd[d] - 1) return g.low[d] + (k + 0.5) * g.cs;
+    return 0.5 * ((g.low[d] + (g.nd[d] - 1) * g.cs) + g.high[d]);
+}
+
+__host__ __device__ inline void cell_coords(const Grid &g, int c, int &x, int &y, int &z) {
+    x = c % g.nd[0];
+    y = (c / g.nd[0]) % g.nd[1];
+    z = c / (g.nd[0] * g.nd[1]);
+}
+
+// Neighbour nb in 0..26 of a domain cell (dx fastest), wrapped periodically.
+// shift[d] = +L / -L / 0 exactly like the reference's halo layers
+// (LinkedCells.cpp:494-502): a neighbour beyond the high face is an image
+// shifted by +L.  Returns the linear index of the wrapped domain cell.
+struct NbCell {
+    int cell;
+    double shift[3];
+    bool crosses;
+};
+
+__host__ __device__ inline NbCell neighbour_cell(const Grid &g, int cx, int cy, int cz, int nb) {
+    const int dd[3] = {nb % 3 - 1, (nb / 3) % 3 - 1, nb / 9 - 1};
+    const int cc[3] = {cx, cy, cz};
+    int w[3];
+    NbCell out;
+    out.crosses = false;
+    for (int d = 0; d < 3; d++) {
+        int k = cc[d] + dd[d];
+        out.shift[d] = 0.0;
+        if (k < 0) { k += g.nd[d]; out.shift[d] = -g.L[d]; out.crosses = true; }
+        else if (k >= g.nd[d]) { k -= g.nd[d]; out.shift[d] = g.L[d]; out.crosses = true; }
+        w[d] = k;
+    }
+    out.cell = w[0] + g.nd[0] * (w[1] + g.nd[1] * w[2]);
+    return out;
+}
+
+// ATM neighbour entry code: bits 0-4 neighbour-cell index (13 = home cell),
+// bit 5 set when the neighbour is a periodic image, bits 6-30 neighbour slot.
+__host__ __device__ inline int atm_code(int nb, bool crosses, int slot) {
+    return nb | (crosses ? 32 : 0) | (slot << 6);
+}
+constexpr int kMaxAtmSlot = (1 << 25) - 1;
+
+struct PairParams {
+    Grid g;
+    const int *cell_start;     // C+1
+    const int *slot_site;
+    const float4 *pos4;
+    const double *posd;        // 3 per slot (FP64 kernels)
+    const int *skey;
+    const float *seps;         // sqrt(eps) per slot
+    const double *seps_d;      // FP64 sqrt(eps) per slot
+    const double *sig_d;       // FP64 sigma per slot
+    double *f;                 // 3 per site, overwritten (pair terms)
+    int64_t *counts;           // per site (neighbour counts), optional
+    float4 *nl;                // ATM list (cap per slot)
+    int *nl_count;
+    int nl_cap;
+    int *err;
+    double *partials;          // R_NSLOTS per block
+    double *lj_hist;           // 4*bins (u sums, f sums, u counts, f counts), optional
+    int lj_bins;
+    double max_sigma;
+    double rc2, rc3sq, scan2;  // LJ cutoff^2, ATM cutoff^2, max of both
+    double stiffness;
+    int use_lj;
+    int virial_compat;
+};
+
+struct AtmParams {
+    int n;
+    const int *slot_site;
+    const float4 *nl;
+    const int *nl_count;
+    int nl_cap;
+    double *f;
+    double *partials;
+    float nu;
+    float rc2;
+    float sign;                // +1 reference (+grad V), -1 physical
+    int virial_compat;         // weights and missing ZZ of ATM_Pressure
+    int atm_direct;            // COMPAT + direct: no virial contribution
+};
+
+struct Engine {
+    komd_config cfg;
+    Grid g;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+
+    int64_t n = 0, n_mol = 0;
+    // site arrays
+    double *r = nullptr, *v = nullptr, *f = nullptr, *m = nullptr, *eps = nullptr, *sig = nullptr;
+    int *key = nullptr, *site_mol = nullptr, *site_slot = nullptr;
+    // molecules
+    int *mol_off = nullptr, *mol_cell = nullptr, *mol_rank = nullptr;
+    double *com = nullptr;
+    // cells
+    int *cell_count = nullptr, *cell_start = nullptr, *cell_mcount = nullptr, *cell_mstart = nullptr;
+    int *cell_mols = nullptr;
+    // cell order
+    int *slot_site = nullptr, *skey = nullptr;
+    float4 *pos4 = nullptr;
+    float *seps = nullptr;
+    double *posd = nullptr, *seps_d = nullptr, *sig_d = nullptr;
+    // ATM list
+    float4 *nl = nullptr;
+    int *nl_count = nullptr;
+    int nl_cap = 64;
+    // topology
+    int *bonds = nullptr, *angles = nullptr;
+    int64_t n_bonds = 0, n_angles = 0;
+    // reductions / flags
+    double *partials = nullptr;
+    int partial_blocks = 0;
+    int *err = nullptr;
+    double *rdf = nullptr;
+    int64_t rdf_bins = 0;
+    double *lj_hist = nullptr;
+    int64_t *counts = nullptr;
+    // state
+    bool have_sites = false, have_cells = false, have_forces = false;
+    // graph
+    cudaGraphExec_t graph = nullptr;
+    bool graph_valid = false;
+    // profiling
+    bool profiling = false;
+};
+
+}  // namespace komd

@@ -1,0 +1,915 @@
+// kernels.cu -- hand-written sm_103a kernels of the KoMD hot path.
+//
+// Per step (komd_gpu_step): integrate0 -> com/wrap/bin -> scan -> scatter ->
+// cell sort+gather -> pair (LJ, FENE, ATM neighbour list) -> [bonded] ->
+// [limit] -> [ATM triplets] -> integrate1.
+//
+// Citations are to Snapex2409/KoMD, src/.
+#include <cfloat>
+#include <climits>
+
+#include "engine.cuh"
+#include "kernels.cuh"
+
+namespace komd {
+
+// ===========================================================================
+// container: COM, periodic wrap, binning (LinkedCells.cpp:65-121,390-400;
+// MoleculeContainer.cpp:55-75).  One thread per molecule.
+// ===========================================================================
+__global__ void k_com_wrap_bin(Grid g, int n_mol, const int *__restrict__ mol_off, double *__restrict__ r,
+                               const double *__restrict__ m, double *__restrict__ com, int *__restrict__ mol_cell,
+                               int *__restrict__ mol_rank, int *__restrict__ cell_count, int *__restrict__ cell_mcount) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_mol) return;
+    const int s0 = mol_off[k], s1 = mol_off[k + 1];
+    // com += r * m ; M += m ; com /= M   (updateCOM, no FMA)
+    double c[3] = {0.0, 0.0, 0.0}, tm = 0.0;
+    for (int s = s0; s < s1; s++) {
+        const double ms = m[s];
+        for (int d = 0; d < 3; d++) c[d] = dadd(c[d], dmul(r[3 * s + d], ms));
+        tm = dadd(tm, ms);
+    }
+    for (int d = 0; d < 3; d++) c[d] = ddiv(c[d], tm);
+    // Periodic_Kernel: strict comparisons against the domain bounds
+    double off[3];
+    bool moved = false;
+    for (int d = 0; d < 3; d++) {
+        off[d] = 0.0;
+        if (c[d] < g.low[d]) off[d] = g.L[d];
+        if (c[d] > g.high[d]) off[d] = -g.L[d];
+        moved |= (off[d] != 0.0);
+    }
+    if (moved) {
+        double c2[3] = {0.0, 0.0, 0.0};
+        for (int s = s0; s < s1; s++) {
+            const double ms = m[s];
+            for (int d = 0; d < 3; d++) {
+                const double x = dadd(r[3 * s + d], off[d]);
+                r[3 * s + d] = x;
+                c2[d] = dadd(c2[d], dmul(x, ms));
+            }
+        }
+        for (int d = 0; d < 3; d++) c[d] = ddiv(c2[d], tm);
+    }
+    // writeIndices: (int64)((com - low) / cs) clamped to [0, nd-1]
+    int b[3];
+    for (int d = 0; d < 3; d++) {
+        const double fbin = ddiv(dsub(c[d], g.low[d]), g.cs);
+        long long q = __double2ll_rz(fbin);
+        if (q < 0) q = 0;
+        if (q > g.nd[d] - 1) q = g.nd[d] - 1;
+        b[d] = (int)q;
+        com[3 * k + d] = c[d];
+    }
+    const int cell = b[0] + g.nd[0] * (b[1] + g.nd[1] * b[2]);
+    mol_cell[k] = cell;
+    mol_rank[k] = atomicAdd(&cell_mcount[cell], 1);
+    atomicAdd(&cell_count[cell], s1 - s0);
+}
+
+// exclusive scan of two count arrays of length nc (one block of 1024 threads,
+// each owning a contiguous chunk)
+__global__ void __launch_bounds__(1024) k_scan2(int nc, const int *__restrict__ a, int *__restrict__ sa,
+                                                const int *__restrict__ b, int *__restrict__ sb) {
+    __shared__ int wa[32], wb[32];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int per = (nc + 1023) / 1024;
+    const int lo = min(t * per, nc), hi = min(lo + per, nc);
+    int ta = 0, tb = 0;
+    for (int i = lo; i < hi; i++) { ta += a[i]; tb += b[i]; }
+    // inclusive warp scan
+    int xa = ta, xb = tb;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int ya = __shfl_up_sync(0xffffffffu, xa, o), yb = __shfl_up_sync(0xffffffffu, xb, o);
+        if (lane >= o) { xa += ya; xb += yb; }
+    }
+    if (lane == 31) { wa[w] = xa; wb[w] = xb; }
+    __syncthreads();
+    if (w == 0) {
+        int va = wa[lane], vb = wb[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const int ya = __shfl_up_sync(0xffffffffu, va, o), yb = __shfl_up_sync(0xffffffffu, vb, o);
+            if (lane >= o) { va += ya; vb += yb; }
+        }
+        wa[lane] = va;
+        wb[lane] = vb;
+    }
+    __syncthreads();
+    int pa = xa - ta + (w > 0 ? wa[w - 1] : 0), pb = xb - tb + (w > 0 ? wb[w - 1] : 0);
+    for (int i = lo; i < hi; i++) {
+        sa[i] = pa; pa += a[i];
+        sb[i] = pb; pb += b[i];
+    }
+    if (t == 1023) { sa[nc] = wa[31]; sb[nc] = wb[31]; }
+}
+
+__global__ void k_scatter_mol(int n_mol, const int *__restrict__ mol_cell, const int *__restrict__ mol_rank,
+                              const int *__restrict__ cell_mstart, int *__restrict__ cell_mols) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_mol) return;
+    cell_mols[cell_mstart[mol_cell[k]] + mol_rank[k]] = k;
+}
+
+// One warp per domain cell: order the cell's molecules by index (ascending
+// site index, the reference's cell-list order), assign slots and gather the
+// cell-ordered arrays.
+__global__ void __launch_bounds__(kBlock) k_cell_sort(Grid g, const int *__restrict__ mol_off,
+                                                      const int *__restrict__ cell_mstart,
+                                                      const int *__restrict__ cell_start,
+                                                      const int *__restrict__ cell_mols, const double *__restrict__ r,
+                                                      const double *__restrict__ eps, const double *__restrict__ sig,
+                                                      const int *__restrict__ key, int *__restrict__ slot_site,
+                                                      int *__restrict__ site_slot, float4 *__restrict__ pos4,
+                                                      int *__restrict__ skey, float *__restrict__ seps,
+                                                      double *__restrict__ posd, double *__restrict__ seps_d,
+                                                      double *__restrict__ sig_d) {
+    const int lane = threadIdx.x & 31;
+    const int cell = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+    if (cell >= g.ncell) return;
+    int cx, cy, cz;
+    cell_coords(g, cell, cx, cy, cz);
+    const double cen[3] = {cell_centre(g, 0, cx), cell_centre(g, 1, cy), cell_centre(g, 2, cz)};
+    const int ms = cell_mstart[cell], mc = cell_mstart[cell + 1] - ms;
+    const int ss = cell_start[cell];
+    for (int base = 0; base < mc; base += 32) {
+        const int t = base + lane;
+        const int mine = (t < mc) ? cell_mols[ms + t] : INT_MAX;
+        int off = 0;
+        for (int u = 0; u < mc; u++) {
+            const int other = cell_mols[ms + u];
+            if (other < mine) off += mol_off[other + 1] - mol_off[other];
+        }
+        if (t < mc) {
+            const int s0 = mol_off[mine], s1 = mol_off[mine + 1];
+            for (int s = s0; s < s1; s++) {
+                const int slot = ss + off + (s - s0);
+                slot_site[slot] = s;
+                site_slot[s] = slot;
+                const double x = r[3 * s], y = r[3 * s + 1], z = r[3 * s + 2];
+                pos4[slot] = make_float4(__double2float_rn(x - cen[0]), __double2float_rn(y - cen[1]),
+                                         __double2float_rn(z - cen[2]), __double2float_rn(0.5 * sig[s]));
+                skey[slot] = key[s];
+                seps[slot] = __double2float_rn(sqrt(eps[s]));
+                if (posd) {
+                    posd[3 * slot] = x; posd[3 * slot + 1] = y; posd[3 * slot + 2] = z;
+                    seps_d[slot] = eps[s];
+                    sig_d[slot] = sig[s];
+                }
+            }
+        }
+    }
+}
+
+// ===========================================================================
+// pair kernel: LJ 12-6 (LJ12_6.cpp:15-43), FENE (FENE.cpp:15-43), the ATM
+// neighbour list inside cutoff_3b, energy / virial / histograms / counts.
+//
+// One warp per home cell, full shell (27 neighbour cells, periodic images by
+// cell wrap), no atomics on forces: lane = (home site il, group grp); the G
+// groups split each neighbour cell's sites and their partial forces are
+// reduced through shared memory.  Real = float: cell-local FP32 coordinates;
+// Real = double: absolute FP64 positions with the reference's exact
+// dr = r_i - (r_j + shift) arithmetic.
+// ===========================================================================
+template <typename Real>
+struct AtmEntry;
+template <>
+struct AtmEntry<float> { using T = float4; };
+struct alignas(16) AtmEntryD { double x, y, z; long long code; };
+template <>
+struct AtmEntry<double> { using T = AtmEntryD; };
+
+__device__ __forceinline__ float4 make_entry(float x, float y, float z, int code) {
+    return make_float4(x, y, z, __int_as_float(code));
+}
+__device__ __forceinline__ AtmEntryD make_entry(double x, double y, double z, int code) {
+    AtmEntryD e; e.x = x; e.y = y; e.z = z; e.code = code; return e;
+}
+
+template <typename Real, bool MEASURE, bool EMIT, bool FENE, bool COUNT>
+__global__ void __launch_bounds__(kBlock) k_pair(PairParams p) {
+    using Entry = typename AtmEntry<Real>::T;
+    constexpr bool FP64 = sizeof(Real) == 8;
+    __shared__ int s_cnt[kWarpsPerBlock][32];
+    __shared__ Real s_red[kWarpsPerBlock][32][3];
+    __shared__ double s_part[kWarpsPerBlock][R_NSLOTS];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int cell = blockIdx.x * kWarpsPerBlock + wib;
+    double a_u = 0.0, a_w[6] = {0, 0, 0, 0, 0, 0}, a_pairs = 0.0;
+    const Real rc2 = (Real)p.rc2, rc3sq = (Real)p.rc3sq, scan2 = (Real)p.scan2;
+    Entry *nl = reinterpret_cast<Entry *>(p.nl);
+
+    if (cell < p.g.ncell) {
+        int cx, cy, cz;
+        cell_coords(p.g, cell, cx, cy, cz);
+        const double cen[3] = {cell_centre(p.g, 0, cx), cell_centre(p.g, 1, cy), cell_centre(p.g, 2, cz)};
+        const int hs = p.cell_start[cell], hn = p.cell_start[cell + 1] - hs;
+        for (int base = 0; base < hn; base += 32) {
+            const int hc = min(32, hn - base);
+            const int G = 32 / hc;
+            const int il = lane % hc, grp = lane / hc;
+            const bool act = grp < G;
+            const int is = hs + base + il;
+            Real pix, piy, piz, sgi, epi;
+            if (FP64) {
+                pix = (Real)p.posd[3 * is]; piy = (Real)p.posd[3 * is + 1]; piz = (Real)p.posd[3 * is + 2];
+                sgi = (Real)p.sig_d[is]; epi = (Real)p.seps_d[is];
+            } else {
+                const float4 q = p.pos4[is];
+                pix = q.x; piy = q.y; piz = q.z; sgi = q.w; epi = p.seps[is];
+            }
+            const int ki = p.skey[is];
+            const int site_i = p.slot_site[is];
+            Real fx = 0, fy = 0, fz = 0;
+            int cnt = 0;
+            if (EMIT && lane < hc) s_cnt[wib][lane] = 0;
+            __syncwarp();
+            for (int nb = 0; nb < 27; nb++) {
+                const NbCell q = neighbour_cell(p.g, cx, cy, cz, nb);
+                const int js = p.cell_start[q.cell], jn = p.cell_start[q.cell + 1] - js;
+                int qx, qy, qz;
+                cell_coords(p.g, q.cell, qx, qy, qz);
+                Real ox, oy, oz;
+                if (FP64) {
+                    ox = (Real)q.shift[0]; oy = (Real)q.shift[1]; oz = (Real)q.shift[2];
+                } else {
+                    ox = (Real)((cell_centre(p.g, 0, qx) + q.shift[0]) - cen[0]);
+                    oy = (Real)((cell_centre(p.g, 1, qy) + q.shift[1]) - cen[1]);
+                    oz = (Real)((cell_centre(p.g, 2, qz) + q.shift[2]) - cen[2]);
+                }
+                const bool vir_full = p.virial_compat && q.crosses;  // COMPAT: images counted per list entry
+                if (!act) continue;
+                for (int jj = grp; jj < jn; jj += G) {
+                    const int j = js + jj;
+                    if (j == is) continue;
+                    Real dx, dy, dz, r2;
+                    if (FP64) {
+                        const double *pj = p.posd + 3 * j;
+                        dx = (Real)dsub((double)pix, dadd(pj[0], (double)ox));
+                        dy = (Real)dsub((double)piy, dadd(pj[1], (double)oy));
+                        dz = (Real)dsub((double)piz, dadd(pj[2], (double)oz));
+                        r2 = (Real)dadd(dadd(dmul((double)dx, (double)dx), dmul((double)dy, (double)dy)),
+                                        dmul((double)dz, (double)dz));
+                    } else {
+                        const float4 pj = p.pos4[j];
+                        dx = pix - (pj.x + ox);
+                        dy = piy - (pj.y + oy);
+                        dz = piz - (pj.z + oz);
+                        r2 = dx * dx + dy * dy + dz * dz;
+                    }
+                    int kj = 0;
+                    if (FENE) {
+                        kj = p.skey[j];
+                        if (kj == ki && !q.crosses) {
+                            // FENE on same-molecule pairs, no cutoff: force on i
+                            // along (r_j - r_i), overstretch -> 1e30 / (r_j - r_i)
+                            const Real sgj = FP64 ? (Real)p.sig_d[j] : (Real)(2.0f * p.pos4[j].w);
+                            const Real sgm = FP64 ? (sgi + sgj) / (Real)2.0 : (sgi + (Real)0.5 * sgj);
+                            const Real R0 = (Real)1.5 * sgm;
+                            const Real R02 = R0 * R0;
+                            if (R02 <= r2) {
+                                // invdr * 1e+30 with invdr = 1 / (r_j - r_i), as FENE.cpp:28-33
+                                fx += ((Real)1 / (-dx)) * (Real)1e30;
+                                fy += ((Real)1 / (-dy)) * (Real)1e30;
+                                fz += ((Real)1 / (-dz)) * (Real)1e30;
+                            } else {
+                                Real e;
+                                if (FP64) e = (Real)sqrt((double)epi * (double)p.seps_d[j]);
+                                else e = epi * p.seps[j];
+                                const Real k = (Real)p.stiffness * e / (sgm * sgm);
+                                const Real fac = k / ((Real)1 - (r2 / R02));
+                                fx -= dx * fac; fy -= dy * fac; fz -= dz * fac;
+                            }
+                        }
+                    }
+                    if (r2 > scan2) continue;
+                    if (!FENE) kj = p.skey[j];
+                    if (EMIT && r2 <= rc3sq) {
+                        const int c = atomicAdd(&s_cnt[wib][il], 1);
+                        if (c < p.nl_cap) nl[(size_t)is * p.nl_cap + c] = make_entry(dx, dy, dz, atm_code(nb, q.crosses, j));
+                    }
+                    if (!p.use_lj || r2 > rc2 || kj == ki) continue;
+                    if (COUNT) { cnt++; continue; }
+                    Real fac, u, ljd;
+                    if (FP64) {
+                        // LJ12_6_Force arithmetic in FP64 (pow(x, 3.0), pow(lj6, 2.0) as products)
+                        const double inv = ddiv(1.0, (double)r2);
+                        const double sgm = (p.sig_d[is] + p.sig_d[j]) / 2.0;
+                        const double e = sqrt(p.seps_d[is] * p.seps_d[j]);
+                        const double x = sgm * sgm * inv;
+                        const double lj6 = x * x * x, lj12 = lj6 * lj6;
+                        fac = (Real)(24.0 * e * (2.0 * lj12 - lj6) * inv);
+                        u = (Real)(4.0 * e * (lj12 - lj6));
+                        ljd = (Real)(24.0 * e * (2.0 * lj12 - lj6));
+                    } else {
+                        const float inv = __frcp_rn((float)r2);
+                        const float sgm = (float)sgi + p.pos4[j].w;
+                        const float x = sgm * sgm * inv;
+                        const float lj6 = x * x * x, lj12 = lj6 * lj6;
+                        const float e = (float)epi * p.seps[j];
+                        ljd = 24.0f * e * (2.0f * lj12 - lj6);
+                        fac = ljd * inv;
+                        u = 4.0f * e * (lj12 - lj6);
+                    }
+                    fx += dx * fac; fy += dy * fac; fz += dz * fac;
+                    if (MEASURE) {
+                        const double wt = vir_full ? 1.0 : 0.5;
+                        const double gx = (double)dx * (double)fac, gy = (double)dy * (double)fac,
+                                     gz = (double)dz * (double)fac;
+                        a_u += 0.5 * (double)u;
+                        a_pairs += 0.5;
+                        a_w[0] += wt * ((double)dx * gx);
+                        a_w[1] += wt * 0.5 * ((double)dx * gy + (double)dy * gx);
+                        a_w[2] += wt * ((double)dy * gy);
+                        a_w[3] += wt * 0.5 * ((double)dx * gz + (double)dz * gx);
+                        a_w[4] += wt * 0.5 * ((double)dy * gz + (double)dz * gy);
+                        a_w[5] += wt * ((double)dz * gz);
+                        if (p.lj_hist) {
+                            const int site_j = p.slot_site[j];
+                            if (site_i < site_j) {
+                                const double rp = sqrt((double)r2);
+                                const double bw = 3.0 * p.max_sigma / (double)p.lj_bins;
+                                unsigned long long bin = (unsigned long long)(rp / bw);
+                                if (bin > (unsigned long long)(p.lj_bins - 1)) bin = p.lj_bins - 1;
+                                atomicAdd(&p.lj_hist[bin], (double)u);
+                                atomicAdd(&p.lj_hist[p.lj_bins + bin], (double)ljd / rp);
+                                atomicAdd(&p.lj_hist[2 * p.lj_bins + bin], 1.0);
+                                atomicAdd(&p.lj_hist[3 * p.lj_bins + bin], 1.0);
+                            }
+                        }
+                    }
+                }
+            }
+            // reduce the G partial sums of every home site
+            if (COUNT) {
+                s_cnt[wib][lane] = cnt;
+                __syncwarp();
+                if (act && grp == 0) {
+                    long long c = 0;
+                    for (int k = 0; k < G; k++) c += s_cnt[wib][il + k * hc];
+                    p.counts[site_i] = c;
+                }
+                __syncwarp();
+                continue;
+            }
+            s_red[wib][lane][0] = fx; s_red[wib][lane][1] = fy; s_red[wib][lane][2] = fz;
+            __syncwarp();
+            if (act && grp == 0) {
+                Real sx = 0, sy = 0, sz = 0;
+                for (int k = 0; k < G; k++) {
+                    sx += s_red[wib][il + k * hc][0];
+                    sy += s_red[wib][il + k * hc][1];
+                    sz += s_red[wib][il + k * hc][2];
+                }
+                p.f[3 * site_i] = (double)sx;
+                p.f[3 * site_i + 1] = (double)sy;
+                p.f[3 * site_i + 2] = (double)sz;
+            }
+            if (EMIT && lane < hc) {
+                const int c = s_cnt[wib][lane];
+                p.nl_count[hs + base + lane] = min(c, p.nl_cap);
+                if (c > p.nl_cap) atomicOr(&p.err[E_ATM_OVERFLOW], 1);
+            }
+            __syncwarp();
+        }
+    }
+    if (MEASURE) {
+        double vals[9] = {a_u, a_w[0], a_w[1], a_w[2], a_w[3], a_w[4], a_w[5], a_pairs, 0.0};
+        for (int k = 0; k < 8; k++) {
+            double x = vals[k];
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            vals[k] = x;
+        }
+        if (lane == 0) {
+            s_part[wib][R_ULJ] = vals[0];
+            for (int k = 0; k < 6; k++) s_part[wib][R_W0 + k] = vals[1 + k];
+            s_part[wib][R_PAIRS] = vals[7];
+        }
+        __syncthreads();
+        if (threadIdx.x < R_NSLOTS) {
+            const int t = threadIdx.x;
+            double s = 0.0;
+            if (t == R_ULJ || t == R_PAIRS || (t >= R_W0 && t <= R_W5))
+                for (int w = 0; w < kWarpsPerBlock; w++) s += s_part[w][t];
+            p.partials[(size_t)blockIdx.x * R_NSLOTS + t] = s;
+        }
+    }
+}
+
+// ===========================================================================
+// ATM triplet kernel (ATM.cpp:22-62 / ATM_NOLIST.cpp:124-159): one warp per
+// site i, every pair (a, b) of i's neighbours inside cutoff_3b with
+// |r_a - r_b| inside too.  Force on i only (each triplet is visited from all
+// three vertices, no atomics).  With A=|r_ia|^2, B=|r_ib|^2, C=|r_ab|^2:
+//   V = nu [ (ABC)^-3/2 + 3/8 P (ABC)^-5/2 ],  P = (A+B-C)(A-B+C)(-A+B+C)
+//   dV/dA = nu (ABC)^-5/2 [ -3/2 BC + 3/8 dP/dA - 15/16 P/A ]
+//   F_i(physical) = -2 (dV/dA e_a + dV/dB e_b),  e_a = r_i - r_a
+// which equals the reference's comp_force terms (comp_force = 2 dV/dA).
+// ===========================================================================
+template <bool MEASURE, bool COMPAT>
+__global__ void __launch_bounds__(kBlock) k_atm(AtmParams p) {
+    extern __shared__ float4 s_dyn[];
+    __shared__ double s_part[kWarpsPerBlock][4 + 6];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int cap = p.nl_cap;
+    float4 *se = s_dyn + wib * cap;
+    float2 *sq = reinterpret_cast<float2 *>(s_dyn + kWarpsPerBlock * cap) + wib * cap;
+    const int i = blockIdx.x * kWarpsPerBlock + wib;
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+    double a_e = 0.0, a_t = 0.0, a_w[6] = {0, 0, 0, 0, 0, 0};
+    const float rc2 = p.rc2;
+    if (i < p.n) {
+        const int ni = p.nl_count[i];
+        for (int k = lane; k < ni; k += 32) {
+            const float4 e = p.nl[(size_t)i * cap + k];
+            const float A = e.x * e.x + e.y * e.y + e.z * e.z;
+            se[k] = e;
+            sq[k] = make_float2(A, 1.0f / A);
+        }
+        __syncwarp();
+        for (int a0 = 0; a0 < ni; a0 += 32) {
+            const int a = a0 + lane;
+            const bool av = a < ni;
+            float4 ea = make_float4(0.f, 0.f, 0.f, 0.f);
+            float2 qa = make_float2(1.f, 1.f);
+            if (av) { ea = se[a]; qa = sq[a]; }
+            const int ca = __float_as_int(ea.w);
+            const float wa = rsqrtf(qa.x);
+            for (int d = 1; d <= ni / 2; d++) {
+                if (!av || (2 * d == ni && a >= d)) continue;
+                int b = a + d;
+                if (b >= ni) b -= ni;
+                const float4 eb = se[b];
+                const float2 qb = sq[b];
+                if (COMPAT) {
+                    const int nba = ca & 31, nbb = __float_as_int(eb.w) & 31;
+                    const bool ok = (nba == 13 && nbb == 13) || (nba != 13 && nbb != 13 && nba != nbb);
+                    if (!ok) continue;
+                }
+                const float cx = eb.x - ea.x, cy = eb.y - ea.y, cz = eb.z - ea.z;
+                const float C = cx * cx + cy * cy + cz * cz;
+                if (C > rc2) continue;
+                const float A = qa.x, B = qb.x;
+                const float wc = rsqrtf(C);
+                const float s = wa * rsqrtf(B) * wc;       // 1/(abc)
+                const float s2 = s * s;
+                const float s5 = s2 * s2 * s;
+                const float t1 = A + B - C, t2 = A - B + C, t3 = B + C - A;
+                const float u = t2 * t3, v = t1 * t3, w = t1 * t2;
+                const float P = t1 * u;
+                const float vA = s5 * (-1.5f * B * C + 0.375f * (u + v - w) - 0.9375f * P * qa.y);
+                const float vB = s5 * (-1.5f * A * C + 0.375f * (u - v + w) - 0.9375f * P * qb.y);
+                gx += vA * ea.x + vB * eb.x;
+                gy += vA * ea.y + vB * eb.y;
+                gz += vA * ea.z + vB * eb.z;
+                if (MEASURE) {
+                    const float vC = s5 * (-1.5f * A * B + 0.375f * (-u + v + w) - 0.9375f * P * (wc * wc));
+                    a_e += (double)(s2 * s * (1.0f + 0.375f * P * s2)) * (1.0 / 3.0);
+                    a_t += 1.0 / 3.0;
+                    double wt;
+                    if (p.virial_compat) {
+                        const int k = 1 + ((ca & 32) ? 0 : 1) + ((__float_as_int(eb.w) & 32) ? 0 : 1);
+                        wt = p.atm_direct ? 0.0 : 1.0 / (double)k;
+                    } else {
+                        wt = 1.0 / 3.0;
+                    }
+                    // pair-decomposed virial sum_pairs P_ab d (x) d with P_ab = -2 dV/d(r_ab^2)
+                    const double pa = -2.0 * vA, pb = -2.0 * vB, pc = -2.0 * vC;
+                    const double ax = ea.x, ay = ea.y, az = ea.z, bx = eb.x, by = eb.y, bz = eb.z;
+                    a_w[0] += wt * (pa * ax * ax + pb * bx * bx + pc * cx * cx);
+                    a_w[1] += wt * (pa * ax * ay + pb * bx * by + pc * cx * cy);
+                    a_w[2] += wt * (pa * ay * ay + pb * by * by + pc * cy * cy);
+                    a_w[3] += wt * (pa * ax * az + pb * bx * bz + pc * cx * cz);
+                    a_w[4] += wt * (pa * ay * az + pb * by * bz + pc * cy * cz);
+                    if (!p.virial_compat) a_w[5] += wt * (pa * az * az + pb * bz * bz + pc * cz * cz);
+                }
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            gx += __shfl_xor_sync(0xffffffffu, gx, o);
+            gy += __shfl_xor_sync(0xffffffffu, gy, o);
+            gz += __shfl_xor_sync(0xffffffffu, gz, o);
+        }
+        if (lane == 0) {
+            const int site = p.slot_site[i];
+            // reference sign: +2 nu (vA e_a + vB e_b); physical: the negative
+            const double sc = 2.0 * (double)p.sign * (double)p.nu;
+            p.f[3 * site] += sc * (double)gx;
+            p.f[3 * site + 1] += sc * (double)gy;
+            p.f[3 * site + 2] += sc * (double)gz;
+        }
+    }
+    if (MEASURE) {
+        double vals[8] = {a_e, a_t, a_w[0], a_w[1], a_w[2], a_w[3], a_w[4], a_w[5]};
+        for (int k = 0; k < 8; k++) {
+            double x = vals[k];
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            vals[k] = x;
+        }
+        if (lane == 0) for (int k = 0; k < 8; k++) s_part[wib][k] = vals[k];
+        __syncthreads();
+        if (threadIdx.x < R_NSLOTS) {
+            const int t = threadIdx.x;
+            double s = 0.0;
+            int src = -1;
+            if (t == R_UATM) src = 0;
+            else if (t == R_TRIPS) src = 1;
+            else if (t >= R_W0 && t <= R_W5) src = 2 + (t - R_W0);
+            if (src >= 0)
+                for (int w = 0; w < kWarpsPerBlock; w++) s += s_part[w][src];
+            // nu scaling of energy and virial
+            if (t == R_UATM || (t >= R_W0 && t <= R_W5)) s *= (double)p.nu;
+            p.partials[(size_t)blockIdx.x * R_NSLOTS + t] = s;
+        }
+    }
+}
+
+// ===========================================================================
+// bonded terms (no reference counterpart): harmonic bond and angle, FP32
+// arithmetic on FP64 differences, FP64 atomic accumulation into f.
+// ===========================================================================
+__global__ void k_bonds(int nb, const int *__restrict__ bonds, const double *__restrict__ r, double *f, float kb,
+                        float r0, double *partials, int measure) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0.0, w[6] = {0, 0, 0, 0, 0, 0};
+    if (t < nb) {
+        const int i = bonds[2 * t], j = bonds[2 * t + 1];
+        const float dx = (float)(r[3 * i] - r[3 * j]), dy = (float)(r[3 * i + 1] - r[3 * j + 1]),
+                    dz = (float)(r[3 * i + 2] - r[3 * j + 2]);
+        const float rr = sqrtf(dx * dx + dy * dy + dz * dz);
+        const float dl = rr - r0;
+        const float fs = -kb * dl / rr;
+        atomicAdd(&f[3 * i], (double)(fs * dx)); atomicAdd(&f[3 * i + 1], (double)(fs * dy));
+        atomicAdd(&f[3 * i + 2], (double)(fs * dz));
+        atomicAdd(&f[3 * j], (double)(-fs * dx)); atomicAdd(&f[3 * j + 1], (double)(-fs * dy));
+        atomicAdd(&f[3 * j + 2], (double)(-fs * dz));
+        if (measure) {
+            e = 0.5 * (double)kb * (double)dl * (double)dl;
+            w[0] = fs * dx * dx; w[1] = fs * dx * dy; w[2] = fs * dy * dy;
+            w[3] = fs * dx * dz; w[4] = fs * dy * dz; w[5] = fs * dz * dz;
+        }
+    }
+    if (measure) {
+        double vals[7] = {e, w[0], w[1], w[2], w[3], w[4], w[5]};
+        for (int k = 0; k < 7; k++) {
+            double x = vals[k];
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            if ((threadIdx.x & 31) == 0) atomicAdd(&partials[k == 0 ? R_UBOND : R_W0 + k - 1], x);
+        }
+    }
+}
+
+__global__ void k_angles(int na, const int *__restrict__ angles, const double *__restrict__ r, double *f, float ka,
+                         float th0, double *partials, int measure) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0.0, w[6] = {0, 0, 0, 0, 0, 0};
+    if (t < na) {
+        const int i = angles[3 * t], j = angles[3 * t + 1], k = angles[3 * t + 2];
+        float u[3], v[3];
+        for (int d = 0; d < 3; d++) {
+            u[d] = (float)(r[3 * i + d] - r[3 * j + d]);
+            v[d] = (float)(r[3 * k + d] - r[3 * j + d]);
+        }
+        const float uu = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+        const float vv = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+        const float uv = u[0] * v[0] + u[1] * v[1] + u[2] * v[2];
+        const float inu = rsqrtf(uu), inv_ = rsqrtf(vv);
+        float cs = uv * inu * inv_;
+        cs = fminf(1.0f, fmaxf(-1.0f, cs));
+        const float th = acosf(cs);
+        const float dth = th - th0;
+        const float sn = fmaxf(sqrtf(1.0f - cs * cs), 1e-6f);
+        const float pre = ka * dth / sn;
+        float fi[3], fk[3];
+        for (int d = 0; d < 3; d++) {
+            fi[d] = pre * (v[d] * inu * inv_ - cs * u[d] * inu * inu);
+            fk[d] = pre * (u[d] * inu * inv_ - cs * v[d] * inv_ * inv_);
+            atomicAdd(&f[3 * i + d], (double)fi[d]);
+            atomicAdd(&f[3 * k + d], (double)fk[d]);
+            atomicAdd(&f[3 * j + d], -(double)(fi[d] + fk[d]));
+        }
+        if (measure) {
+            e = 0.5 * (double)ka * (double)dth * (double)dth;
+            w[0] = u[0] * fi[0] + v[0] * fk[0]; w[1] = u[0] * fi[1] + v[0] * fk[1];
+            w[2] = u[1] * fi[1] + v[1] * fk[1]; w[3] = u[0] * fi[2] + v[0] * fk[2];
+            w[4] = u[1] * fi[2] + v[1] * fk[2]; w[5] = u[2] * fi[2] + v[2] * fk[2];
+        }
+    }
+    if (measure) {
+        double vals[7] = {e, w[0], w[1], w[2], w[3], w[4], w[5]};
+        for (int q = 0; q < 7; q++) {
+            double x = vals[q];
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            if ((threadIdx.x & 31) == 0) atomicAdd(&partials[q == 0 ? R_UBOND : R_W0 + q - 1], x);
+        }
+    }
+}
+
+// Limit_Force (Limit.cpp:19-25): clamp with Kokkos::min / max semantics
+__global__ void k_limit(int n, const double *__restrict__ eps, const double *__restrict__ sig, double limit,
+                        double *__restrict__ f) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const double fmax = limit * eps[s] / sig[s];
+    for (int d = 0; d < 3; d++) {
+        double x = f[3 * s + d];
+        x = (fmax < x) ? fmax : x;
+        x = (x < -fmax) ? -fmax : x;
+        f[3 * s + d] = x;
+    }
+}
+
+// ===========================================================================
+// velocity Verlet (Integrator.cpp:28-37), FP64 without contraction
+// ===========================================================================
+__global__ void k_step0(int n, double *__restrict__ r, double *__restrict__ v, const double *__restrict__ f,
+                        const double *__restrict__ m, double dt_half, double dt) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const double c = ddiv(dt_half, m[s]);
+    for (int d = 0; d < 3; d++) {
+        const double vv = dadd(v[3 * s + d], dmul(f[3 * s + d], c));
+        v[3 * s + d] = vv;
+        r[3 * s + d] = dadd(r[3 * s + d], dmul(vv, dt));
+    }
+}
+
+__global__ void k_step1(int n, double *__restrict__ v, const double *__restrict__ f, const double *__restrict__ m,
+                        double dt_half, int *err) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const double c = ddiv(dt_half, m[s]);
+    bool bad = false;
+    for (int d = 0; d < 3; d++) {
+        const double vv = dadd(v[3 * s + d], dmul(f[3 * s + d], c));
+        v[3 * s + d] = vv;
+        bad |= !isfinite(vv);
+    }
+    if (bad) atomicOr(&err[E_NONFINITE], 1);
+}
+
+// ===========================================================================
+// sensors
+// ===========================================================================
+// TemperatureSensor::measure (sites inside [low, high]) + kinetic tensor
+// (PressureSensor::MomentumKernel) over the first n_terms sites.
+__global__ void __launch_bounds__(kBlock) k_kinetic(Grid g, int n, int n_terms, const double *__restrict__ r,
+                                                    const double *__restrict__ v, const double *__restrict__ m,
+                                                    double *__restrict__ partials) {
+    __shared__ double s_part[kWarpsPerBlock][8];
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    double vals[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (s < n) {
+        const double x = r[3 * s], y = r[3 * s + 1], z = r[3 * s + 2];
+        const double vx = v[3 * s], vy = v[3 * s + 1], vz = v[3 * s + 2], ms = m[s];
+        if (x >= g.low[0] && y >= g.low[1] && z >= g.low[2] && x <= g.high[0] && y <= g.high[1] && z <= g.high[2]) {
+            vals[0] = dmul(ms, dadd(dadd(dmul(vx, vx), dmul(vy, vy)), dmul(vz, vz)));
+            vals[1] = 1.0;
+        }
+        if (s < n_terms) {
+            vals[2] = vx * vx * ms; vals[3] = vx * vy * ms; vals[4] = vy * vy * ms;
+            vals[5] = vx * vz * ms; vals[6] = vy * vz * ms; vals[7] = vz * vz * ms;
+        }
+    }
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    for (int k = 0; k < 8; k++) {
+        double xk = vals[k];
+        for (int o = 16; o > 0; o >>= 1) xk += __shfl_xor_sync(0xffffffffu, xk, o);
+        if (lane == 0) s_part[wib][k] = xk;
+    }
+    __syncthreads();
+    if (threadIdx.x < R_NSLOTS) {
+        const int t = threadIdx.x;
+        double acc = 0.0;
+        int src = -1;
+        if (t == R_MV2) src = 0;
+        else if (t == R_NBOX) src = 1;
+        else if (t >= R_K0 && t <= R_K5) src = 2 + t - R_K0;
+        if (src >= 0)
+            for (int w = 0; w < kWarpsPerBlock; w++) acc += s_part[w][src];
+        partials[(size_t)blockIdx.x * R_NSLOTS + t] = acc;
+    }
+}
+
+// RDF over molecule COMs (RDFSensor::RDF_Kernel, RDFSensor.cpp:61-72):
+// minimum image delta - L*round(delta/L), bin (uint64)(r/dr) clamped.
+__device__ __forceinline__ void rdf_pair(const double *ca, const double *cb, Grid g, double max_r, double dr,
+                                         long long nbins, double *bins) {
+    double q[3];
+    for (int d = 0; d < 3; d++) {
+        const double delta = dsub(ca[d], cb[d]);
+        q[d] = dsub(delta, dmul(g.L[d], (double)(long long)round(ddiv(delta, g.L[d]))));
+    }
+    const double rr = sqrt(dadd(dadd(dmul(q[0], q[0]), dmul(q[1], q[1])), dmul(q[2], q[2])));
+    if (rr > max_r) return;
+    unsigned long long b = (unsigned long long)ddiv(rr, dr);
+    if (b > (unsigned long long)(nbins - 1)) b = nbins - 1;
+    atomicAdd(&bins[b], 1.0);
+}
+
+__global__ void k_rdf_cells(Grid g, int n_mol, const double *__restrict__ com, const int *__restrict__ mol_cell,
+                            const int *__restrict__ cell_mstart, const int *__restrict__ cell_mols, double max_r,
+                            double dr, long long nbins, double *bins) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_mol) return;
+    int cx, cy, cz;
+    cell_coords(g, mol_cell[k], cx, cy, cz);
+    for (int nb = 0; nb < 27; nb++) {
+        const NbCell q = neighbour_cell(g, cx, cy, cz, nb);
+        for (int u = cell_mstart[q.cell]; u < cell_mstart[q.cell + 1]; u++) {
+            const int o = cell_mols[u];
+            if (o == k) continue;
+            rdf_pair(com + 3 * k, com + 3 * o, g, max_r, dr, nbins, bins);
+        }
+    }
+}
+
+__global__ void k_rdf_all(Grid g, int n_mol, const double *__restrict__ com, double max_r, double dr,
+                          long long nbins, double *bins) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_mol) return;
+    for (int o = 0; o < n_mol; o++)
+        if (o != k) rdf_pair(com + 3 * k, com + 3 * o, g, max_r, dr, nbins, bins);
+}
+
+__global__ void k_sum_partials(int nblocks, const double *__restrict__ partials, double *__restrict__ out) {
+    const int t = threadIdx.x;   // one thread per slot, sequential over blocks (deterministic)
+    if (t >= R_NSLOTS) return;
+    double s = 0.0;
+    for (int b = 0; b < nblocks; b++) s += partials[(size_t)b * R_NSLOTS + t];
+    out[t] += s;
+}
+
+// ===========================================================================
+// launchers
+// ===========================================================================
+static inline int nblk(long long n, int b) { return (int)((n + b - 1) / b); }
+
+void launch_container(Engine &e, cudaStream_t st) {
+    const Grid &g = e.g;
+    cudaMemsetAsync(e.cell_count, 0, sizeof(int) * g.ncell, st);
+    cudaMemsetAsync(e.cell_mcount, 0, sizeof(int) * g.ncell, st);
+    k_com_wrap_bin<<<nblk(e.n_mol, 256), 256, 0, st>>>(g, (int)e.n_mol, e.mol_off, e.r, e.m, e.com, e.mol_cell,
+                                                         e.mol_rank, e.cell_count, e.cell_mcount);
+    k_scan2<<<1, 1024, 0, st>>>(g.ncell, e.cell_count, e.cell_start, e.cell_mcount, e.cell_mstart);
+    k_scatter_mol<<<nblk(e.n_mol, 256), 256, 0, st>>>((int)e.n_mol, e.mol_cell, e.mol_rank, e.cell_mstart,
+                                                        e.cell_mols);
+    const bool fp64 = e.cfg.precision == KOMD_FP64 || e.posd != nullptr;
+    k_cell_sort<<<nblk(g.ncell, kWarpsPerBlock), kBlock, 0, st>>>(
+        g, e.mol_off, e.cell_mstart, e.cell_start, e.cell_mols, e.r, e.eps, e.sig, e.key, e.slot_site, e.site_slot,
+        e.pos4, e.skey, e.seps, fp64 ? e.posd : nullptr, e.seps_d, e.sig_d);
+}
+
+static PairParams pair_params(Engine &e) {
+    PairParams p;
+    p.g = e.g;
+    p.cell_start = e.cell_start;
+    p.slot_site = e.slot_site;
+    p.pos4 = e.pos4;
+    p.posd = e.posd;
+    p.skey = e.skey;
+    p.seps = e.seps;
+    p.seps_d = e.seps_d;
+    p.sig_d = e.sig_d;
+    p.f = e.f;
+    p.counts = e.counts;
+    p.nl = e.nl;
+    p.nl_count = e.nl_count;
+    p.nl_cap = e.nl_cap;
+    p.err = e.err;
+    p.partials = e.partials;
+    p.lj_hist = nullptr;
+    p.lj_bins = e.cfg.lj_bins;
+    p.max_sigma = e.cfg.max_sigma;
+    p.rc2 = e.cfg.cutoff * e.cfg.cutoff;
+    p.rc3sq = e.cfg.cutoff_3b * e.cfg.cutoff_3b;
+    const bool atm = (e.cfg.terms & KOMD_TERM_ATM) != 0;
+    const bool lj = (e.cfg.terms & KOMD_TERM_LJ) != 0;
+    p.scan2 = 0.0;
+    if (lj) p.scan2 = p.rc2;
+    if (atm && p.rc3sq > p.scan2) p.scan2 = p.rc3sq;
+    p.stiffness = e.cfg.stiffness;
+    p.use_lj = lj ? 1 : 0;
+    p.virial_compat = e.cfg.virial_mode == KOMD_VIRIAL_COMPAT;
+    return p;
+}
+
+template <typename Real, bool M, bool E, bool F>
+static void pair_dispatch_c(PairParams &p, int grid, cudaStream_t st) {
+    k_pair<Real, M, E, F, false><<<grid, kBlock, 0, st>>>(p);
+}
+
+template <typename Real>
+static void pair_dispatch(PairParams &p, bool measure, bool emit, bool fene, int grid, cudaStream_t st) {
+    const int code = (measure ? 4 : 0) | (emit ? 2 : 0) | (fene ? 1 : 0);
+    switch (code) {
+        case 0: pair_dispatch_c<Real, false, false, false>(p, grid, st); break;
+        case 1: pair_dispatch_c<Real, false, false, true>(p, grid, st); break;
+        case 2: pair_dispatch_c<Real, false, true, false>(p, grid, st); break;
+        case 3: pair_dispatch_c<Real, false, true, true>(p, grid, st); break;
+        case 4: pair_dispatch_c<Real, true, false, false>(p, grid, st); break;
+        case 5: pair_dispatch_c<Real, true, false, true>(p, grid, st); break;
+        case 6: pair_dispatch_c<Real, true, true, false>(p, grid, st); break;
+        default: pair_dispatch_c<Real, true, true, true>(p, grid, st); break;
+    }
+}
+
+int pair_grid(const Engine &e) { return nblk(e.g.ncell, kWarpsPerBlock); }
+int atm_grid(const Engine &e) { return nblk(e.n, kWarpsPerBlock); }
+
+void launch_pair(Engine &e, cudaStream_t st, bool measure, double *lj_hist) {
+    PairParams p = pair_params(e);
+    p.lj_hist = lj_hist;
+    const bool emit = (e.cfg.terms & KOMD_TERM_ATM) != 0;
+    const bool fene = (e.cfg.terms & KOMD_TERM_FENE) != 0;
+    if (e.cfg.precision == KOMD_FP64) pair_dispatch<double>(p, measure, emit, fene, pair_grid(e), st);
+    else pair_dispatch<float>(p, measure, emit, fene, pair_grid(e), st);
+}
+
+void launch_counts(Engine &e, cudaStream_t st) {
+    PairParams p = pair_params(e);
+    p.use_lj = 1;
+    p.scan2 = p.rc2;
+    k_pair<double, false, false, false, true><<<pair_grid(e), kBlock, 0, st>>>(p);
+}
+
+void launch_bonded(Engine &e, cudaStream_t st, bool measure, double *acc) {
+    if (e.n_bonds > 0)
+        k_bonds<<<nblk(e.n_bonds, 256), 256, 0, st>>>((int)e.n_bonds, e.bonds, e.r, e.f, (float)e.cfg.bond_k,
+                                                        (float)e.cfg.bond_r0, acc, measure ? 1 : 0);
+    if (e.n_angles > 0)
+        k_angles<<<nblk(e.n_angles, 256), 256, 0, st>>>((int)e.n_angles, e.angles, e.r, e.f, (float)e.cfg.angle_k,
+                                                          (float)e.cfg.angle_theta0, acc, measure ? 1 : 0);
+}
+
+void launch_limit(Engine &e, cudaStream_t st) {
+    k_limit<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.eps, e.sig, e.cfg.limit, e.f);
+}
+
+size_t atm_smem(const Engine &e) { return (size_t)kWarpsPerBlock * e.nl_cap * (sizeof(float4) + sizeof(float2)); }
+
+void launch_atm(Engine &e, cudaStream_t st, bool measure) {
+    AtmParams p;
+    p.n = (int)e.n;
+    p.slot_site = e.slot_site;
+    p.nl = e.nl;
+    p.nl_count = e.nl_count;
+    p.nl_cap = e.nl_cap;
+    p.f = e.f;
+    p.partials = e.partials;
+    p.nu = (float)e.cfg.nu;
+    p.rc2 = (float)(e.cfg.cutoff_3b * e.cfg.cutoff_3b);
+    p.sign = e.cfg.atm_sign == KOMD_ATM_SIGN_REFERENCE ? 1.0f : -1.0f;
+    p.virial_compat = e.cfg.virial_mode == KOMD_VIRIAL_COMPAT;
+    p.atm_direct = e.cfg.atm_direct;
+    const bool compat = e.cfg.atm_enum == KOMD_ATM_ENUM_COMPAT;
+    const size_t sm = atm_smem(e);
+    const int grid = atm_grid(e);
+    if (measure) {
+        if (compat) k_atm<true, true><<<grid, kBlock, sm, st>>>(p);
+        else k_atm<true, false><<<grid, kBlock, sm, st>>>(p);
+    } else {
+        if (compat) k_atm<false, true><<<grid, kBlock, sm, st>>>(p);
+        else k_atm<false, false><<<grid, kBlock, sm, st>>>(p);
+    }
+}
+
+void launch_step0(Engine &e, cudaStream_t st) {
+    k_step0<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.r, e.v, e.f, e.m, e.cfg.delta_t * 0.5, e.cfg.delta_t);
+}
+
+void launch_step1(Engine &e, cudaStream_t st) {
+    k_step1<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.v, e.f, e.m, e.cfg.delta_t * 0.5, e.err);
+}
+
+int kinetic_grid(const Engine &e) { return nblk(e.n, kBlock); }
+
+void launch_kinetic(Engine &e, cudaStream_t st, int n_terms) {
+    k_kinetic<<<kinetic_grid(e), kBlock, 0, st>>>(e.g, (int)e.n, n_terms, e.r, e.v, e.m, e.partials);
+}
+
+void launch_sum_partials(cudaStream_t st, int nblocks, const double *partials, double *out) {
+    k_sum_partials<<<1, 32, 0, st>>>(nblocks, partials, out);
+}
+
+void launch_rdf(Engine &e, cudaStream_t st, double *bins, bool cells) {
+    if (cells)
+        k_rdf_cells<<<nblk(e.n_mol, 128), 128, 0, st>>>(e.g, (int)e.n_mol, e.com, e.mol_cell, e.cell_mstart,
+                                                          e.cell_mols, e.cfg.rdf_max, e.cfg.rdf_dr, e.rdf_bins, bins);
+    else
+        k_rdf_all<<<nblk(e.n_mol, 128), 128, 0, st>>>(e.g, (int)e.n_mol, e.com, e.cfg.rdf_max, e.cfg.rdf_dr,
+                                                        e.rdf_bins, bins);
+}
+
+void set_kernel_attributes(Engine &e) {
+    const size_t sm = atm_smem(e);
+    if (sm > 48 * 1024) {
+        cudaFuncSetAttribute(k_atm<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaFuncSetAttribute(k_atm<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaFuncSetAttribute(k_atm<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaFuncSetAttribute(k_atm<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    }
+}
+
+}  // namespace komd

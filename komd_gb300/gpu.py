@@ -1,0 +1,252 @@
+"""Python binding of the engine's C ABI (include/komd_gpu.h) via ctypes.
+
+The engine is the in-tree shared library komd_gb300/_build/libkomd_gpu.so;
+there is no Python or CPU fallback: if the library is missing or cannot be
+loaded, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Dict, Optional
+
+import numpy as np
+
+from .build import LIB_GPU
+
+KOMD_OK = 0
+STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_OVERFLOW", 4: "ERR_STATE", 5: "ERR_NOMEM", 6: "ERR_NONFINITE"}
+
+FP32, FP64 = 0, 1
+ATM_SIGN_REFERENCE, ATM_SIGN_PHYSICAL = 0, 1
+ATM_ENUM_COMPAT, ATM_ENUM_FULL = 0, 1
+VIRIAL_COMPAT, VIRIAL_CORRECT = 0, 1
+
+TERM_LJ, TERM_FENE, TERM_LIMIT, TERM_ATM, TERM_BONDED = 0x01, 0x02, 0x04, 0x08, 0x10
+MEASURE_TEMPERATURE, MEASURE_ENERGY, MEASURE_PRESSURE, MEASURE_RDF, MEASURE_LJ_HIST = 0x01, 0x02, 0x04, 0x08, 0x10
+
+EXPORTS = [
+    "komd_gpu_create", "komd_gpu_destroy", "komd_gpu_last_error", "komd_gpu_abi_version", "komd_gpu_set_stream",
+    "komd_gpu_grid_dims", "komd_gpu_upload_sites", "komd_gpu_set_state", "komd_gpu_set_topology",
+    "komd_gpu_download", "komd_gpu_num_sites", "komd_gpu_update_container", "komd_gpu_forces",
+    "komd_gpu_integrate0", "komd_gpu_integrate1", "komd_gpu_step", "komd_gpu_step_host", "komd_gpu_measure",
+    "komd_gpu_rdf_bins", "komd_gpu_get_cells", "komd_gpu_neighbour_counts", "komd_gpu_set_profiling",
+    "komd_gpu_profile", "komd_gpu_kernels_per_step",
+]
+
+
+class KomdConfig(C.Structure):
+    _fields_ = [
+        ("domain_low", C.c_double * 3), ("domain_high", C.c_double * 3), ("cell_size", C.c_double),
+        ("cutoff", C.c_double), ("cutoff_3b", C.c_double), ("nu", C.c_double), ("delta_t", C.c_double),
+        ("stiffness", C.c_double), ("limit", C.c_double), ("bond_k", C.c_double), ("bond_r0", C.c_double),
+        ("angle_k", C.c_double), ("angle_theta0", C.c_double), ("max_sigma", C.c_double), ("rdf_max", C.c_double),
+        ("rdf_dr", C.c_double), ("terms", C.c_uint32), ("precision", C.c_int32), ("atm_sign", C.c_int32),
+        ("atm_enum", C.c_int32), ("virial_mode", C.c_int32), ("atm_direct", C.c_int32), ("lj_bins", C.c_int32),
+        ("atm_list_cap", C.c_int32),
+    ]
+
+
+class Observables(C.Structure):
+    _fields_ = [
+        ("temperature", C.c_double), ("mv2", C.c_double), ("n_in_box", C.c_double), ("u_lj", C.c_double),
+        ("u_atm", C.c_double), ("u_bonded", C.c_double), ("kinetic", C.c_double * 6), ("virial", C.c_double * 6),
+        ("pressure", C.c_double * 6), ("pairs_in_cutoff", C.c_int64), ("triplets", C.c_int64),
+    ]
+
+
+class KomdError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"komd_gpu {STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return LIB_GPU
+
+
+def load() -> C.CDLL:
+    """Loads the native engine; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_GPU):
+        raise RuntimeError(f"native engine {LIB_GPU} is not built: run `python -m komd_gb300.build` first "
+                           "(there is no CPU fallback)")
+    L = C.CDLL(LIB_GPU)
+    P, I64, I32 = C.c_void_p, C.c_int64, C.c_int
+    L.komd_gpu_create.argtypes = [C.POINTER(KomdConfig), I32, C.POINTER(P)]
+    L.komd_gpu_destroy.argtypes = [P]
+    L.komd_gpu_last_error.restype = C.c_char_p
+    L.komd_gpu_set_stream.argtypes = [P, P]
+    L.komd_gpu_grid_dims.argtypes = [P, P]
+    L.komd_gpu_upload_sites.argtypes = [P, I64, P, P, P, P, P, P]
+    L.komd_gpu_set_state.argtypes = [P, P, P]
+    L.komd_gpu_set_topology.argtypes = [P, I64, P, I64, P]
+    L.komd_gpu_download.argtypes = [P, P, P, P]
+    L.komd_gpu_num_sites.argtypes = [P]
+    L.komd_gpu_num_sites.restype = I64
+    for fn in ("komd_gpu_update_container", "komd_gpu_forces", "komd_gpu_integrate0", "komd_gpu_integrate1"):
+        getattr(L, fn).argtypes = [P]
+    L.komd_gpu_step.argtypes = [P, I64]
+    L.komd_gpu_step_host.argtypes = [P, I64, P, P, P]
+    L.komd_gpu_measure.argtypes = [P, C.c_uint32, C.POINTER(Observables), P, P]
+    L.komd_gpu_rdf_bins.argtypes = [P]
+    L.komd_gpu_rdf_bins.restype = I64
+    L.komd_gpu_get_cells.argtypes = [P, P, I64, P, I64, C.POINTER(I64)]
+    L.komd_gpu_neighbour_counts.argtypes = [P, P]
+    L.komd_gpu_set_profiling.argtypes = [P, I32]
+    L.komd_gpu_profile.argtypes = [P, I32, P, P, C.c_char_p, I32]
+    L.komd_gpu_kernels_per_step.argtypes = [P]
+    _lib = L
+    return L
+
+
+def _p(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def make_config(low, high, cell_size, cutoff=2.5, cutoff_3b=None, nu=0.0, dt=0.005, terms=TERM_LJ,
+                precision=FP32, atm_sign=ATM_SIGN_REFERENCE, atm_enum=ATM_ENUM_COMPAT, virial_mode=VIRIAL_COMPAT,
+                atm_direct=1, stiffness=30.0, limit=1e30, bond_k=0.0, bond_r0=1.0, angle_k=0.0, angle_theta0=0.0,
+                max_sigma=1.0, rdf_max=0.0, rdf_dr=0.0, lj_bins=100, atm_list_cap=0) -> KomdConfig:
+    c = KomdConfig()
+    for d in range(3):
+        c.domain_low[d] = float(low[d])
+        c.domain_high[d] = float(high[d])
+    c.cell_size = float(cell_size)
+    c.cutoff = float(cutoff)
+    c.cutoff_3b = float(cutoff if cutoff_3b is None else cutoff_3b)
+    c.nu, c.delta_t, c.stiffness, c.limit = float(nu), float(dt), float(stiffness), float(limit)
+    c.bond_k, c.bond_r0, c.angle_k, c.angle_theta0 = float(bond_k), float(bond_r0), float(angle_k), float(angle_theta0)
+    c.max_sigma, c.rdf_max, c.rdf_dr = float(max_sigma), float(rdf_max), float(rdf_dr)
+    c.terms, c.precision, c.atm_sign, c.atm_enum = int(terms), int(precision), int(atm_sign), int(atm_enum)
+    c.virial_mode, c.atm_direct, c.lj_bins, c.atm_list_cap = int(virial_mode), int(atm_direct), int(lj_bins), int(atm_list_cap)
+    return c
+
+
+class GpuSystem:
+    """One periodic system on one GPU behind the C ABI."""
+
+    def __init__(self, sysm, cfg: KomdConfig, device: int = 0):
+        self.L = load()
+        self.h = C.c_void_p()
+        self._check(self.L.komd_gpu_create(C.byref(cfg), int(device), C.byref(self.h)))
+        self.cfg = cfg
+        self.n = int(sysm.n)
+        r = np.ascontiguousarray(sysm.r, np.float64)
+        v = np.ascontiguousarray(sysm.v, np.float64)
+        self._keep = [np.ascontiguousarray(x, np.float64) for x in (sysm.m, sysm.eps, sysm.sig)]
+        mid = np.ascontiguousarray(sysm.mol_id, np.uint64)
+        self._check(self.L.komd_gpu_upload_sites(self.h, self.n, _p(r), _p(v), _p(self._keep[0]), _p(self._keep[1]),
+                                                 _p(self._keep[2]), _p(mid)))
+        bonds = getattr(sysm, "bonds", None)
+        angles = getattr(sysm, "angles", None)
+        if (bonds is not None and len(bonds)) or (angles is not None and len(angles)):
+            b = np.ascontiguousarray(bonds if bonds is not None else np.zeros((0, 2)), np.int64)
+            a = np.ascontiguousarray(angles if angles is not None else np.zeros((0, 3)), np.int64)
+            self._check(self.L.komd_gpu_set_topology(self.h, b.shape[0], _p(b), a.shape[0], _p(a)))
+
+    def _check(self, code):
+        if code != KOMD_OK:
+            raise KomdError(code, self.L.komd_gpu_last_error().decode())
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.L.komd_gpu_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --- hot path ---------------------------------------------------------
+    def update_container(self):
+        self._check(self.L.komd_gpu_update_container(self.h))
+
+    def forces(self):
+        self._check(self.L.komd_gpu_forces(self.h))
+
+    def integrate0(self):
+        self._check(self.L.komd_gpu_integrate0(self.h))
+
+    def integrate1(self):
+        self._check(self.L.komd_gpu_integrate1(self.h))
+
+    def step(self, n: int = 1):
+        self._check(self.L.komd_gpu_step(self.h, int(n)))
+
+    def step_host(self, n, r, v, f):
+        self._check(self.L.komd_gpu_step_host(self.h, int(n), _p(r), _p(v), _p(f)))
+
+    def set_state(self, r=None, v=None):
+        r = None if r is None else np.ascontiguousarray(r, np.float64)
+        v = None if v is None else np.ascontiguousarray(v, np.float64)
+        self._check(self.L.komd_gpu_set_state(self.h, _p(r), _p(v)))
+
+    def set_stream(self, stream_ptr: int):
+        self._check(self.L.komd_gpu_set_stream(self.h, C.c_void_p(stream_ptr)))
+
+    def download(self):
+        r = np.empty((self.n, 3))
+        v = np.empty((self.n, 3))
+        f = np.empty((self.n, 3))
+        self._check(self.L.komd_gpu_download(self.h, _p(r), _p(v), _p(f)))
+        return r, v, f
+
+    # --- sensors ----------------------------------------------------------
+    def measure(self, mask: int) -> Dict[str, object]:
+        obs = Observables()
+        nb = int(self.L.komd_gpu_rdf_bins(self.h))
+        rdf = np.zeros(max(nb, 1))
+        hist = np.zeros(4 * self.cfg.lj_bins)
+        self._check(self.L.komd_gpu_measure(self.h, int(mask), C.byref(obs), _p(rdf), _p(hist)))
+        out = {k: getattr(obs, k) for k, _ in Observables._fields_}
+        for k in ("kinetic", "virial", "pressure"):
+            out[k] = np.array(out[k][:])
+        out["rdf"] = rdf[:nb] if nb > 0 else None
+        out["lj_hist"] = hist.reshape(4, -1)
+        return out
+
+    # --- parity dumps -----------------------------------------------------
+    def grid_dims(self):
+        nd = np.zeros(3, np.int64)
+        self._check(self.L.komd_gpu_grid_dims(self.h, _p(nd)))
+        return tuple(int(x) for x in nd)
+
+    def cells(self):
+        nd = self.grid_dims()
+        ncell = (nd[0] + 2) * (nd[1] + 2) * (nd[2] + 2)
+        count = np.zeros(ncell, np.int64)
+        total = C.c_int64(0)
+        self._check(self.L.komd_gpu_get_cells(self.h, _p(count), ncell, None, 0, C.byref(total)))
+        idx = np.zeros(max(total.value, 1), np.int64)
+        self._check(self.L.komd_gpu_get_cells(self.h, _p(count), ncell, _p(idx), total.value, C.byref(total)))
+        return count, idx[:total.value]
+
+    def neighbour_counts(self):
+        c = np.zeros(self.n, np.int64)
+        self._check(self.L.komd_gpu_neighbour_counts(self.h, _p(c)))
+        return c
+
+    # --- profiling --------------------------------------------------------
+    def set_profiling(self, on: bool):
+        self._check(self.L.komd_gpu_set_profiling(self.h, 1 if on else 0))
+
+    def profile(self):
+        launches = np.zeros(16, np.int64)
+        ms = np.zeros(16)
+        names = C.create_string_buffer(512)
+        nf = self.L.komd_gpu_profile(self.h, 16, _p(launches), _p(ms), names, 512)
+        if nf < 0:
+            self._check(nf)
+        fams = names.value.decode().split("\n")[:nf]
+        return {f: (int(launches[i]), float(ms[i])) for i, f in enumerate(fams)}
+
+    def kernels_per_step(self) -> int:
+        return int(self.L.komd_gpu_kernels_per_step(self.h))

@@ -433,6 +433,68 @@ void kor_lj(const kor_grid *g, int64_t n_pairs, const int64_t *pairs, const doub
     }
 }
 
+
+/* LJ over the same entries as kor_lj, generated on the fly from the C08 cell
+ * pairs and the same-cell pairs instead of a materialised pair list (the
+ * reference's PLU kernels write that list; the arithmetic per entry is
+ * identical).  Used for large systems, where the list would take GBs. */
+void kor_lj_cells(const kor_grid *g, const kor_cells *c, const double *r, const double *eps, const double *sig,
+                  const uint64_t *id, double cutoff, double *f, kor_lj_out *out) {
+    const double cutoff2 = pow(cutoff, 2);
+    const int64_t ncp = kor_c08_pairs(g, 0, NULL, NULL);
+    int64_t *cp = (int64_t *)malloc(sizeof(int64_t) * 2 * (size_t)(ncp > 0 ? ncp : 1));
+    double *sp = (double *)malloc(sizeof(double) * 6 * (size_t)(ncp > 0 ? ncp : 1));
+    kor_c08_pairs(g, ncp, cp, sp);
+    const int64_t ndc = domain_cells(g, NULL);
+    int64_t *dc = (int64_t *)malloc(sizeof(int64_t) * (size_t)(ndc > 0 ? ndc : 1));
+    domain_cells(g, dc);
+    static const double zero6[6] = {0, 0, 0, 0, 0, 0};
+    double u_total = 0;
+    int64_t inside = 0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : u_total, inside)
+#endif
+    for (int64_t q = 0; q < ncp + ndc; q++) {
+        int64_t c0, c1;
+        const double *sh;
+        int single = q >= ncp;
+        if (!single) { c0 = cp[2 * q]; c1 = cp[2 * q + 1]; sh = sp + 6 * q; }
+        else { c0 = c1 = dc[q - ncp]; sh = zero6; }
+        const int64_t n0 = c->count[c0], n1 = c->count[c1];
+        const int64_t *i0 = c->idx + c->start[c0], *i1 = c->idx + c->start[c1];
+        const int64_t total = single ? n0 * (n0 - 1) / 2 : n0 * n1;
+        const int dom0 = !shift_nonzero(sh), dom1 = !shift_nonzero(sh + 3);
+        for (int64_t loc = 0; loc < total; loc++) {
+            int64_t a, b;
+            if (single) single_pair(loc, &a, &b);
+            else { a = loc % n0; b = loc / n0; }
+            const int64_t s0 = i0[a], s1 = i1[b];
+            if (id[s0] == id[s1]) continue;
+            double dr[3];
+            for (int d = 0; d < 3; d++) dr[d] = (r[3 * s0 + d] + sh[d]) - (r[3 * s1 + d] + sh[3 + d]);
+            const double dr2 = dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2];
+            if (dr2 > cutoff2) continue;
+            inside++;
+            const double invdr2 = 1. / dr2;
+            const double sigma = (sig[s0] + sig[s1]) / 2.0;
+            const double epsilon = sqrt(eps[s0] * eps[s1]);
+            const double sig2 = sigma * sigma;
+            const double lj6 = pow(sig2 * invdr2, 3.0);
+            const double lj12 = pow(lj6, 2.0);
+            const double fac = 24.0 * epsilon * (2.0 * lj12 - lj6) * invdr2;
+            if (dom0) for (int d = 0; d < 3; d++) atomic_addd(&f[3 * s0 + d], dr[d] * fac);
+            if (dom1) for (int d = 0; d < 3; d++) atomic_addd(&f[3 * s1 + d], -(dr[d] * fac));
+            if (dom1) u_total += 4.0 * epsilon * (lj12 - lj6);
+        }
+    }
+    free(dc); free(cp); free(sp);
+    if (out) {
+        out->u_total = u_total;
+        for (int d = 0; d < 6; d++) out->virial[d] = 0.0;
+        out->pairs_in_cutoff = inside;
+    }
+}
+
 /* ------------------------------------------------------------------------ */
 /* ATM                                                                      */
 /* ------------------------------------------------------------------------ */
@@ -686,8 +748,8 @@ void kor_limit(int64_t n, const double *eps, const double *sig, double limit_fac
         const double fmax = limit_factor * eps[s] / sig[s];
         for (int d = 0; d < 3; d++) {
             double x = f[3 * s + d];
-            x = (x < fmax) ? x : fmax;     /* math::min(force, fmax) */
-            x = (x > -fmax) ? x : -fmax;   /* math::max(.., -fmax)   */
+            x = (fmax < x) ? fmax : x;     /* Kokkos::min(force, fmax): keeps NaN */
+            x = (x < -fmax) ? -fmax : x;   /* Kokkos::max(.., -fmax)              */
             f[3 * s + d] = x;
         }
     }

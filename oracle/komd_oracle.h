@@ -113,6 +113,11 @@ typedef struct {
     int64_t triplets;      /* triplets inside the cutoff that were counted */
 } kor_atm_out;
 
+/* kor_lj without a materialised pair list: the same entries in C08 order,
+ * generated from the cells (no virial, no histograms). */
+void kor_lj_cells(const kor_grid *g, const kor_cells *c, const double *r, const double *eps, const double *sig,
+                  const uint64_t *id, double cutoff, double *f, kor_lj_out *out);
+
 /* ATM comp_force (ATM.h:36-69), returned as in the reference. */
 double kor_atm_comp_force(double nu, double r_ab, double r_ac, double r_bc);
 

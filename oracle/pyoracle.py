@@ -73,6 +73,7 @@ def lib():
         L.kor_pair_list.argtypes = [C.POINTER(Grid), C.POINTER(Cells), I64, P, P]
         L.kor_pair_list.restype = I64
         L.kor_lj.argtypes = [C.POINTER(Grid), I64, P, P, P, P, P, P, D, C.c_int, P, P, C.POINTER(LJOut), I64, D, P, P, P, P]
+        L.kor_lj_cells.argtypes = [C.POINTER(Grid), C.POINTER(Cells), P, P, P, P, D, P, C.POINTER(LJOut)]
         L.kor_atm_compat.argtypes = [C.POINTER(Grid), C.POINTER(Cells), P, D, D, C.c_int, C.c_int, C.c_int, P,
                                      C.POINTER(ATMOut)]
         L.kor_atm_vertex.argtypes = [C.POINTER(Grid), C.POINTER(Cells), P, D, D, C.c_int, C.c_int, P, C.POINTER(ATMOut)]
@@ -180,7 +181,18 @@ class OracleSim:
         return pairs[:n], shifts[:n]
 
     # --- forces ------------------------------------------------------------
-    def forces(self, nbins=0, max_sigma=1.0, with_atm_virial=False, ncount=False):
+    def forces(self, nbins=0, max_sigma=1.0, with_atm_virial=False, ncount=False, listless=False):
+        if listless:
+            # large systems: LJ straight from the cells, no materialised pair list
+            if self.use_fene or self.bonded is not None or nbins or ncount:
+                raise ValueError("listless forces cover LJ, Limit and ATM only")
+            if self.use_lj:
+                self.L.kor_lj_cells(C.byref(self.g), C.byref(self.cells), _p(self.r), _p(self.eps), _p(self.sig),
+                                    _p(self.id), self.cutoff, _p(self.f), C.byref(self.lj_out))
+            self.L.kor_limit(self.n, _p(self.eps), _p(self.sig), self.limit, _p(self.f))
+            if self.use_atm:
+                self.atm_forces(with_atm_virial)
+            return
         pairs, shifts = self.pair_list()
         self.ncount = np.zeros(self.n, np.int64) if ncount else None
         if self.use_lj:
@@ -224,11 +236,11 @@ class OracleSim:
     def integrate1(self):
         self.L.kor_step1(self.n, _p(self.v), _p(self.f), _p(self.m), self.dt)
 
-    def step(self, first=False):
+    def step(self, first=False, listless=False):
         if not first:
             self.integrate0()
         self.update_container()
-        self.forces()
+        self.forces(listless=listless)
         if not first:
             self.integrate1()
 

@@ -1,0 +1,266 @@
+"""CUDA engine vs the reference (golden fixtures) and the CPU oracle, through
+the C ABI (komd_gb300/_build/libkomd_gpu.so via ctypes).
+
+Bars (from the engine's contract):
+  * cell lists (incl. halo copies) and neighbour counts: bit-exact;
+  * FP32 pair/triplet forces: relative RMSE <= 1e-5 against the reference's FP64;
+  * FP64 mode: relative RMSE <= 1e-12;
+  * temperature, potential energy, pressure: FP64 reductions, tolerances below;
+  * RDF histogram counts: bit-exact for the same configuration.
+"""
+import numpy as np
+import pytest
+
+from conftest import CASES, case_system, load_case
+
+pytestmark = pytest.mark.gpu
+
+FP32_FORCE_RMSE = 1e-5
+FP64_FORCE_RMSE = 1e-12
+
+
+def rel_rmse(a, b):
+    return float(np.sqrt(((a - b) ** 2).sum(1).mean()) / np.sqrt((b ** 2).sum(1).mean()))
+
+
+def gpu_for_case(z, precision=None, **over):
+    from komd_gb300 import gpu, lattice
+    s = case_system(z)
+    terms = gpu.TERM_LJ | gpu.TERM_FENE | gpu.TERM_LIMIT
+    if int(z["p_enable_3b"]):
+        terms |= gpu.TERM_ATM
+    kw = dict(cutoff=float(z["p_cutoff"]), cutoff_3b=float(z["p_cutoff"]), nu=lattice.energy_3b_to_nu(float(z["p_energy_3b"])),
+              dt=float(z["p_delta_t"]), terms=terms, precision=gpu.FP32 if precision is None else precision,
+              atm_direct=int(z["p_enable_3b_direct"]), stiffness=float(z.get("p_stiffness", 30.0)),
+              limit=float(z["p_limit"]), rdf_max=float(z.get("p_sensor_rdf_max", 0.0)),
+              rdf_dr=float(z.get("p_sensor_rdf_dr", 0.0)))
+    kw.update(over)
+    cfg = gpu.make_config(z["low"], z["high"], float(z["p_cell_size"]), **kw)
+    return gpu.GpuSystem(s, cfg), s
+
+
+def _state_at(z, step):
+    return (z["r0"], z["v0"]) if step == 0 else (z[f"s{step}_R"], z[f"s{step}_V"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_cells_and_neighbour_counts_bitexact(name):
+    z = load_case(name)
+    g, _ = gpu_for_case(z)
+    for step in [int(d) for d in z["dumps"]]:
+        r, v = _state_at(z, step)
+        g.set_state(r, v)
+        g.update_container()
+        count, idx = g.cells()
+        assert np.array_equal(count, z[f"s{step}_cell_count"]), f"{name} step {step}"
+        assert np.array_equal(idx, z[f"s{step}_cell_idx"]), f"{name} step {step}"
+        r_gpu, _, _ = g.download()
+        assert np.array_equal(r_gpu, z[f"s{step}_R"]), "periodic wrap must be bit-exact"
+        assert np.array_equal(g.neighbour_counts(), z[f"s{step}_ncount"])
+    g.close()
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_forces_match_reference(name, prec):
+    from komd_gb300 import gpu
+    z = load_case(name)
+    g, _ = gpu_for_case(z, precision=gpu.FP32 if prec == "fp32" else gpu.FP64)
+    tol = FP32_FORCE_RMSE if prec == "fp32" else FP64_FORCE_RMSE
+    for step in [int(d) for d in z["dumps"]]:
+        r, v = _state_at(z, step)
+        g.set_state(r, v)
+        g.update_container()
+        g.forces()
+        _, _, f = g.download()
+        ref = z[f"s{step}_F"]
+        finite = np.all(np.abs(ref) < 1e29, axis=1)     # FENE overstretch rows are 1e30 by design
+        err = rel_rmse(f[finite], ref[finite])
+        assert err < tol, f"{name} step {step} {prec}: rel RMSE {err:.3e}"
+    g.close()
+
+
+@pytest.mark.parametrize("name", ["lj864", "ljatm864", "atmlist500", "fene375"])
+def test_sensors_match_reference(name):
+    from komd_gb300 import gpu
+    z = load_case(name)
+    for prec, rtol in ((gpu.FP64, 1e-11), (gpu.FP32, 2e-5)):
+        g, _ = gpu_for_case(z, precision=prec)
+        step = int(z["dumps"][0])
+        r, v = _state_at(z, step)
+        g.set_state(r, v)
+        g.update_container()
+        g.forces()
+        obs = g.measure(gpu.MEASURE_TEMPERATURE | gpu.MEASURE_ENERGY | gpu.MEASURE_PRESSURE | gpu.MEASURE_RDF)
+        assert obs["temperature"] == pytest.approx(float(z[f"s{step}_temp"]), rel=1e-13)
+        assert obs["u_lj"] == pytest.approx(float(z[f"s{step}_upot"]), rel=rtol)
+        pres = z[f"s{step}_pressure"]
+        scale = np.abs(pres).max()
+        np.testing.assert_allclose(obs["pressure"], pres, rtol=0, atol=rtol * 10 * scale)
+        if f"s{step}_rdf" in z:
+            assert np.array_equal(obs["rdf"], z[f"s{step}_rdf"])
+        g.close()
+
+
+def test_fp64_trajectory_follows_reference():
+    """100 NVE steps in FP64 mode through the graph-replayed step: positions
+    stay on the reference's trajectory."""
+    from komd_gb300 import gpu
+    z = load_case("lj864")
+    g, _ = gpu_for_case(z, precision=gpu.FP64)
+    g.update_container()
+    g.forces()
+    g.step(1)
+    r1, v1, _ = g.download()
+    assert np.abs(r1 - z["s1_R"]).max() < 1e-12
+    g.step(99)
+    r, v, f = g.download()
+    assert np.abs(r - z["s100_R"]).max() < 1e-8
+    assert rel_rmse(f, z["s100_F"]) < 1e-6
+    g.close()
+
+
+def test_fp32_trajectory_close_to_reference():
+    from komd_gb300 import gpu
+    z = load_case("ljatm864")
+    g, _ = gpu_for_case(z, precision=gpu.FP32)
+    g.update_container()
+    g.forces()
+    g.step(20)
+    r, v, f = g.download()
+    assert np.abs(r - z["s20_R"]).max() < 1e-4
+    assert rel_rmse(f, z["s20_F"]) < 1e-3
+    g.close()
+
+
+def _oracle_vertex(oracle_lib, s, cell, rc3, nu, full=True):
+    sim = oracle_lib.OracleSim(s, cell, rc3, nu=nu, lj=False, atm=True, atm_mode="full" if full else "vertex_compat",
+                               atm_sign=oracle_lib.ATM_SIGN_PHYSICAL, virial_mode=oracle_lib.VIRIAL_CORRECT)
+    sim.update_container()
+    sim.forces()
+    return sim
+
+
+def test_atm_full_physical_vs_oracle(oracle_lib):
+    """FULL enumeration with F = -grad V (the physics mode): forces, energy,
+    triplet count and virial against the oracle's vertex enumeration."""
+    from komd_gb300 import gpu, lattice
+    s = lattice.argon_fcc(6, rho=0.8442, t_star=0.722, seed=21, jitter=0.06)
+    nu = 0.073
+    sim = _oracle_vertex(oracle_lib, s, 2.0, 2.0, nu)
+    cfg = gpu.make_config(s.low, s.high, 2.0, cutoff=2.0, cutoff_3b=2.0, nu=nu, terms=gpu.TERM_ATM,
+                          atm_sign=gpu.ATM_SIGN_PHYSICAL, atm_enum=gpu.ATM_ENUM_FULL, virial_mode=gpu.VIRIAL_CORRECT)
+    g = gpu.GpuSystem(s, cfg)
+    g.update_container()
+    g.forces()
+    _, _, f = g.download()
+    assert rel_rmse(f, sim.f) < FP32_FORCE_RMSE
+    obs = g.measure(gpu.MEASURE_ENERGY | gpu.MEASURE_PRESSURE)
+    assert obs["triplets"] == sim.atm_out.triplets
+    assert obs["u_atm"] == pytest.approx(sim.atm_out.energy, rel=1e-5)
+    np.testing.assert_allclose(obs["virial"], np.array(sim.atm_out.virial[:]), rtol=0,
+                               atol=1e-4 * np.abs(np.array(sim.atm_out.virial[:])).max())
+    g.close()
+
+
+def test_atm_physical_is_minus_gradient():
+    """Finite differences of the GPU ATM energy equal the GPU physical force."""
+    from komd_gb300 import gpu, lattice
+    s = lattice.argon_fcc(4, rho=0.8442, t_star=0.722, seed=22, jitter=0.08)
+    cfg = gpu.make_config(s.low, s.high, 2.0, cutoff=2.0, cutoff_3b=2.0, nu=0.073, terms=gpu.TERM_ATM,
+                          precision=gpu.FP32, atm_sign=gpu.ATM_SIGN_PHYSICAL, atm_enum=gpu.ATM_ENUM_FULL)
+    g = gpu.GpuSystem(s, cfg)
+    g.update_container()
+    g.forces()
+    _, _, f = g.download()
+    h = 2e-3
+    for atom in (0, 7, 31):
+        for d in range(3):
+            e = []
+            for sgn in (1, -1):
+                r = s.r.copy()
+                r[atom, d] += sgn * h
+                g.set_state(r, None)
+                g.update_container()
+                e.append(g.measure(gpu.MEASURE_ENERGY)["u_atm"])
+            fd = -(e[0] - e[1]) / (2 * h)
+            assert fd == pytest.approx(f[atom, d], rel=2e-2, abs=2e-4)
+    g.close()
+
+
+def test_bonded_vs_oracle(oracle_lib):
+    from komd_gb300 import gpu, lattice
+    s = lattice.triatomic_sc(4, rho_site=0.5, t_star=1.0, seed=23)
+    s.r = s.r + np.random.default_rng(5).normal(0, 0.03, s.r.shape)   # strain bonds and angles
+    th0 = np.deg2rad(109.47)
+    cfg = gpu.make_config(s.low, s.high, 2.5, cutoff=2.5, terms=gpu.TERM_LJ | gpu.TERM_BONDED, bond_k=1000.0,
+                          bond_r0=1.0, angle_k=100.0, angle_theta0=th0, virial_mode=gpu.VIRIAL_CORRECT)
+    g = gpu.GpuSystem(s, cfg)
+    g.update_container()
+    g.forces()
+    _, _, f = g.download()
+    sim = oracle_lib.OracleSim(s, 2.5, 2.5, bonded=dict(bonds=s.bonds, angles=s.angles, kb=1000.0, r0=1.0, ka=100.0,
+                                                        theta0=th0))
+    sim.update_container()
+    sim.forces()
+    assert rel_rmse(f, sim.f) < 2e-5
+    obs = g.measure(gpu.MEASURE_ENERGY)
+    assert obs["u_bonded"] == pytest.approx(sim.e_bonded, rel=1e-4)
+    assert obs["u_lj"] == pytest.approx(sim.lj_out.u_total, rel=1e-5)
+    g.close()
+
+
+def test_graph_step_equals_manual_sequence():
+    from komd_gb300 import gpu
+    z = load_case("ljatm864")
+    a, _ = gpu_for_case(z)
+    b, _ = gpu_for_case(z)
+    for g in (a, b):
+        g.update_container()
+        g.forces()
+    a.step(5)
+    for _ in range(5):
+        b.integrate0()
+        b.update_container()
+        b.forces()
+        b.integrate1()
+    ra, va, fa = a.download()
+    rb, vb, fb = b.download()
+    assert np.abs(ra - rb).max() < 1e-9
+    assert rel_rmse(fa, fb) < 1e-6
+
+
+def test_full_size_binning_and_momentum():
+    """256,000-site FCC LJ+ATM (the benchmark size): the cell lists agree with
+    a numpy restatement of the binning formula, every site is in exactly one
+    domain cell in ascending order, and the physical force sums to zero."""
+    from komd_gb300 import gpu, lattice
+    s = lattice.argon_fcc(40, rho=0.8442, t_star=0.722, seed=4, jitter=0.02)
+    cfg = gpu.make_config(s.low, s.high, 2.5, cutoff=2.5, cutoff_3b=2.0, nu=0.073,
+                          terms=gpu.TERM_LJ | gpu.TERM_ATM, atm_sign=gpu.ATM_SIGN_PHYSICAL,
+                          atm_enum=gpu.ATM_ENUM_FULL, virial_mode=gpu.VIRIAL_CORRECT)
+    g = gpu.GpuSystem(s, cfg)
+    g.update_container()
+    nd = np.array(g.grid_dims())
+    count, idx = g.cells()
+    b = np.clip(np.trunc((s.r - s.low) / 2.5).astype(np.int64), 0, nd - 1) + 1
+    lin = b[:, 0] + (nd[0] + 2) * (b[:, 1] + (nd[1] + 2) * b[:, 2])
+    expect = np.bincount(lin, minlength=count.size)
+    c3 = count.reshape(nd[2] + 2, nd[1] + 2, nd[0] + 2)
+    dom = np.zeros_like(c3, dtype=bool)
+    dom[1:-1, 1:-1, 1:-1] = True
+    assert np.array_equal(count.reshape(c3.shape)[dom], expect.reshape(c3.shape)[dom])
+    starts = np.concatenate(([0], np.cumsum(count)))
+    dom_flat = dom.ravel()
+    seen = np.concatenate([idx[starts[c]:starts[c + 1]] for c in np.flatnonzero(dom_flat)])
+    assert np.array_equal(np.sort(seen), np.arange(s.n))
+    for c in np.flatnonzero(dom_flat)[:2000]:
+        seg = idx[starts[c]:starts[c + 1]]
+        assert np.all(np.diff(seg) > 0)
+    g.forces()
+    _, _, f = g.download()
+    assert np.abs(f.sum(0)).max() < 1e-3 * np.sqrt(s.n) * np.abs(f).mean()
+    obs = g.measure(gpu.MEASURE_ENERGY | gpu.MEASURE_TEMPERATURE)
+    assert obs["n_in_box"] == s.n
+    assert obs["triplets"] > 50 * s.n
+    g.close()

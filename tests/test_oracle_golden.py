@@ -1,0 +1,107 @@
+"""The CPU oracle against the reference itself (CPU, no GPU).
+
+The fixtures under tests/golden/ were produced by the reference's own code
+(oracle/ref/harness.cpp linked against the reference sources; see
+tests/golden/make_golden.py).  The oracle must reproduce them bit for bit:
+positions, forces, cell lists incl. halo copies, neighbour counts,
+temperature, the LJ sensor potential, the pressure tensor and the RDF
+histogram, along 0, 1 and up to 100 steps of NVE dynamics.
+"""
+import numpy as np
+import pytest
+
+from conftest import CASES, case_system, load_case
+
+
+def _sim(oracle_lib, z, **kw):
+    from komd_gb300 import lattice
+    s = case_system(z)
+    nu = lattice.energy_3b_to_nu(float(z["p_energy_3b"]))
+    return oracle_lib.OracleSim(s, float(z["p_cell_size"]), float(z["p_cutoff"]), dt=float(z["p_delta_t"]), nu=nu,
+                                limit=float(z["p_limit"]), stiffness=float(z.get("p_stiffness", 30.0)),
+                                atm=bool(z["p_enable_3b"]), fene=True, **kw)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_matches_reference_bitwise(oracle_lib, name):
+    oracle_lib.set_threads(1)   # the reference harness runs Kokkos Serial: same summation order
+    z = load_case(name)
+    sim = _sim(oracle_lib, z)
+    dumps = [int(d) for d in z["dumps"]]
+    list_atm = bool(z["p_enable_3b"]) and not bool(z["p_enable_3b_direct"])
+    rdf_sum, n_rdf = None, 0
+    for step in range(max(dumps) + 1):
+        if step > 0:
+            sim.integrate0()
+        sim.update_container()
+        sim.forces(ncount=True, with_atm_virial=list_atm)
+        if step > 0:
+            sim.integrate1()
+        if step not in dumps:
+            continue
+        p = f"s{step}_"
+        count, _, idx = sim.cell_lists()
+        assert np.array_equal(count, z[p + "cell_count"]), f"{name} step {step}: cell counts"
+        assert np.array_equal(idx, z[p + "cell_idx"]), f"{name} step {step}: cell lists"
+        assert np.array_equal(sim.r, z[p + "R"]), f"{name} step {step}: positions"
+        assert np.array_equal(sim.v, z[p + "V"]), f"{name} step {step}: velocities"
+        assert np.array_equal(sim.f, z[p + "F"]), f"{name} step {step}: forces"
+        assert np.array_equal(sim.ncount, z[p + "ncount"]), f"{name} step {step}: neighbour counts"
+        assert sim.temperature() == z[p + "temp"]
+        assert sim.lj_out.u_total == pytest.approx(float(z[p + "upot"]), rel=1e-13, abs=1e-12)
+        # PressureSensor: momentum over the first getNumMolecules() sites + LJ
+        # list virial (+ ATM_Pressure for the list-based ATM only)
+        pres = sim.momentum() + np.array(sim.lj_out.virial[:])
+        if list_atm:
+            pres = pres + np.array(sim.atm_out.virial[:])
+        np.testing.assert_allclose(pres, z[p + "pressure"], rtol=1e-12, atol=1e-9)
+        if p + "rdf" in z:
+            # RDFSensor accumulates its bins over every measure() and writes the
+            # running mean bins / samples with 6 significant digits
+            rdf = sim.rdf(float(z["p_sensor_rdf_max"]), float(z["p_sensor_rdf_dr"]))
+            rdf_sum = rdf if rdf_sum is None else rdf_sum + rdf
+            n_rdf += 1
+            if n_rdf == 1:
+                assert np.array_equal(rdf, z[p + "rdf"])
+            np.testing.assert_allclose(rdf_sum / n_rdf, z[p + "rdf"], rtol=1e-5, atol=1e-5)
+
+
+def test_halo_copies_and_stretched_cells(oracle_lib):
+    """edge_box: non-zero domain_low, non-cubic box and a stretched last cell."""
+    z = load_case("edge_box")
+    sim = _sim(oracle_lib, z)
+    sim.update_container()
+    nd = sim.nd
+    count, start, idx = sim.cell_lists()
+    nx, ny, nz = (d + 2 for d in nd)
+    c3 = count.reshape(nz, ny, nx)
+    # every halo cell repeats its periodic source cell
+    assert np.array_equal(c3[:, :, 0], c3[:, :, nx - 2]) and np.array_equal(c3[:, :, nx - 1], c3[:, :, 1])
+    # every site appears exactly once in the domain cells
+    dom = c3[1:-1, 1:-1, 1:-1].sum()
+    assert dom == sim.n
+
+
+def test_momentum_conservation_full_atm(oracle_lib):
+    """FULL enumeration, physical sign: total force vanishes (Newton's third law
+    holds per triplet), and the vertex form with the COMPAT restriction equals
+    the reference's enumeration."""
+    z = load_case("ljatm864")
+    from komd_gb300 import lattice
+    nu = lattice.energy_3b_to_nu(float(z["p_energy_3b"]))
+    s = case_system(z)
+    ref = oracle_lib.OracleSim(s, 2.0, 2.0, nu=nu, lj=False, atm=True, atm_mode="compat")
+    ref.update_container()
+    ref.forces()
+    vc = oracle_lib.OracleSim(s, 2.0, 2.0, nu=nu, lj=False, atm=True, atm_mode="vertex_compat")
+    vc.update_container()
+    vc.forces()
+    scale = np.sqrt((ref.f ** 2).sum(1).mean())
+    assert np.sqrt(((vc.f - ref.f) ** 2).sum(1).mean()) / scale < 1e-12
+    full = oracle_lib.OracleSim(s, 2.0, 2.0, nu=nu, lj=False, atm=True, atm_mode="full",
+                                atm_sign=oracle_lib.ATM_SIGN_PHYSICAL)
+    full.update_container()
+    full.forces()
+    assert np.abs(full.f.sum(0)).max() < 1e-10 * np.abs(full.f).max()
+    # the COMPAT set misses the (A,A,B) classes: it holds fewer triplets
+    assert full.atm_out.triplets > vc.atm_out.triplets
