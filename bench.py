@@ -226,9 +226,14 @@ def run_ours(args, w, name):
     obs0 = g.measure(gpu.MEASURE_ENERGY | gpu.MEASURE_TEMPERATURE)
     triplets = int(obs0["triplets"])
 
-    # warm-up (also captures the CUDA graph)
+    # equilibration from the lattice (untimed), then the warm-up steps (which
+    # also capture the CUDA graph); the triplet count is taken after both
+    if args.equil > 0:
+        g.step(args.equil)
     g.step(max(args.warmup, 3))
     torch.cuda.synchronize()
+    obs0 = g.measure(gpu.MEASURE_ENERGY | gpu.MEASURE_TEMPERATURE)
+    triplets = int(obs0["triplets"])
 
     # ---- timed region: K steps, per-kernel CUDA events on the launching stream
     g.set_profiling(True)
@@ -318,6 +323,7 @@ def run_ours(args, w, name):
             "vs_baseline": None, "dtype": "fp32 forces / fp64 integration",
             "data": "synthetic (seeded FCC lattice, Maxwell-Boltzmann velocities)",
             "config": {"workload": name, "form": "exact FP32 (LJ + FULL ATM, F = -grad V)", "sites": s.n,
+                       "equilibration_steps": args.equil, "temperature_K_at_timing": obs0["temperature"],
                        "rc_lj": w["rc"], "rc_atm": w["rc3"], "nu_star": w["nu"], "cell": w["cell"], "dt": w["dt"],
                        "triplets_per_step": triplets, "parallelism": f"replicas x{world}",
                        "l2": "no flush: the per-step working set exceeds L2 (the ATM neighbour list alone, "
@@ -346,6 +352,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="lj_atm_argon_256k", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--equil", type=int, default=400,
+                    help="untimed NVE steps from the lattice before the warm-up (thermalises the crystal)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -138,7 +138,7 @@ int check_launch(const char *what) {
 
 int ensure_partials(komd_gpu *h) {
     Engine &e = h->e;
-    int need = pair_grid(e);
+    int need = e.g.ncell;                      // pair kernels write at most one partial row per cell
     need = std::max(need, atm_grid(e));
     need = std::max(need, kinetic_grid(e));
     if (need > h->partial_cap) {
@@ -153,11 +153,12 @@ int ensure_partials(komd_gpu *h) {
 void enqueue_forces(komd_gpu *h, bool measure, double *lj_hist) {
     Engine &e = h->e;
     cudaStream_t st = e.stream;
+    int pair_blocks;
     {
         ProfScope ps(h, F_PAIR);
-        launch_pair(e, st, measure, lj_hist);
+        pair_blocks = launch_pair(e, st, measure, lj_hist);
     }
-    if (measure) launch_sum_partials(st, pair_grid(e), e.partials, h->acc);
+    if (measure) launch_sum_partials(st, pair_blocks, e.partials, h->acc);
     if ((e.cfg.terms & KOMD_TERM_BONDED) && (e.n_bonds > 0 || e.n_angles > 0)) {
         ProfScope ps(h, F_BONDED);
         launch_bonded(e, st, measure, h->acc);
@@ -290,6 +291,25 @@ int komd_gpu_create(const komd_config *cfg, int device, komd_gpu **out) {
         if (e.rdf_bins > 0 && dalloc(e.rdf, e.rdf_bins)) { komd_gpu_destroy(h); return fail(KOMD_ERR_NOMEM, "rdf"); }
     }
     if (dalloc(e.lj_hist, 4 * (size_t)e.cfg.lj_bins)) { komd_gpu_destroy(h); return fail(KOMD_ERR_NOMEM, "hist"); }
+    {
+        // home-relative centre offsets of the 3 neighbour cells per dimension,
+        // in FP64 once and rounded to FP32 (the FP32 kernels never touch FP64)
+        std::vector<float> tab;
+        for (int d = 0; d < 3; d++)
+            for (int k = 0; k < g.nd[d]; k++)
+                for (int dd = -1; dd <= 1; dd++) {
+                    int q = k + dd;
+                    double shift = 0.0;
+                    if (q < 0) { q += g.nd[d]; shift = -g.L[d]; }
+                    else if (q >= g.nd[d]) { q -= g.nd[d]; shift = g.L[d]; }
+                    tab.push_back((float)((cell_centre(g, d, q) + shift) - cell_centre(g, d, k)));
+                }
+        if (dalloc(e.offtab, tab.size()) ||
+            cudaMemcpy(e.offtab, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+            komd_gpu_destroy(h);
+            return fail(KOMD_ERR_NOMEM, "offset table");
+        }
+    }
     h->want_posd = e.cfg.precision == KOMD_FP64;
     *out = h;
     return KOMD_OK;
@@ -307,7 +327,7 @@ int komd_gpu_destroy(komd_gpu *h) {
     dfree(e.cell_count); dfree(e.cell_start); dfree(e.cell_mcount); dfree(e.cell_mstart); dfree(e.cell_mols);
     dfree(e.slot_site); dfree(e.skey); dfree(e.pos4); dfree(e.seps); dfree(e.posd); dfree(e.seps_d); dfree(e.sig_d);
     dfree(e.nl); dfree(e.nl_count); dfree(e.bonds); dfree(e.angles); dfree(e.partials); dfree(e.err);
-    dfree(e.rdf); dfree(e.lj_hist); dfree(e.counts); dfree(h->f_scratch); dfree(h->acc);
+    dfree(e.rdf); dfree(e.lj_hist); dfree(e.counts); dfree(h->f_scratch); dfree(h->acc); dfree(e.offtab);
     for (auto &p : h->pending) { h->pool.push_back(p.second.first); h->pool.push_back(p.second.second); }
     for (auto ev : h->pool) cudaEventDestroy(ev);
     if (e.own_stream && e.stream) cudaStreamDestroy(e.stream);

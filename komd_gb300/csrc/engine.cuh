@@ -128,6 +128,7 @@ struct PairParams {
     double stiffness;
     int use_lj;
     int virial_compat;
+    const float *offtab;       // per dimension nd*3 FP32 offsets centre(k+d) + shift - centre(k)
 };
 
 struct AtmParams {
@@ -138,9 +139,9 @@ struct AtmParams {
     int nl_cap;
     double *f;
     double *partials;
-    float nu;
-    float rc2;
-    float sign;                // +1 reference (+grad V), -1 physical
+    double nu;
+    double rc2;
+    double sign;               // +1 reference (+grad V), -1 physical
     int virial_compat;         // weights and missing ZZ of ATM_Pressure
     int atm_direct;            // COMPAT + direct: no virial contribution
 };
@@ -167,6 +168,7 @@ struct Engine {
     float4 *pos4 = nullptr;
     float *seps = nullptr;
     double *posd = nullptr, *seps_d = nullptr, *sig_d = nullptr;
+    float *offtab = nullptr;   // see PairParams::offtab
     // ATM list
     float4 *nl = nullptr;
     int *nl_count = nullptr;

@@ -407,82 +407,98 @@ __global__ void __launch_bounds__(kBlock) k_pair(PairParams p) {
 //   F_i(physical) = -2 (dV/dA e_a + dV/dB e_b),  e_a = r_i - r_a
 // which equals the reference's comp_force terms (comp_force = 2 dV/dA).
 // ===========================================================================
-template <bool MEASURE, bool COMPAT>
+__device__ __forceinline__ int entry_code(const float4 &e) { return __float_as_int(e.w); }
+__device__ __forceinline__ int entry_code(const AtmEntryD &e) { return (int)e.code; }
+__device__ __forceinline__ float rsqrt_r(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double rsqrt_r(double x) { return 1.0 / sqrt(x); }
+
+template <typename Real, bool MEASURE, bool COMPAT>
 __global__ void __launch_bounds__(kBlock) k_atm(AtmParams p) {
+    using Entry = typename AtmEntry<Real>::T;
+    struct Q2 { Real A, invA; };
     extern __shared__ float4 s_dyn[];
     __shared__ double s_part[kWarpsPerBlock][4 + 6];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int cap = p.nl_cap;
-    float4 *se = s_dyn + wib * cap;
-    float2 *sq = reinterpret_cast<float2 *>(s_dyn + kWarpsPerBlock * cap) + wib * cap;
+    Entry *se = reinterpret_cast<Entry *>(s_dyn) + wib * cap;
+    Q2 *sq = reinterpret_cast<Q2 *>(reinterpret_cast<Entry *>(s_dyn) + kWarpsPerBlock * cap) + wib * cap;
+    const Entry *nl = reinterpret_cast<const Entry *>(p.nl);
     const int i = blockIdx.x * kWarpsPerBlock + wib;
-    float gx = 0.f, gy = 0.f, gz = 0.f;
+    Real gx = 0, gy = 0, gz = 0;
     double a_e = 0.0, a_t = 0.0, a_w[6] = {0, 0, 0, 0, 0, 0};
-    const float rc2 = p.rc2;
+    const Real rc2 = (Real)p.rc2;
     if (i < p.n) {
         const int ni = p.nl_count[i];
         for (int k = lane; k < ni; k += 32) {
-            const float4 e = p.nl[(size_t)i * cap + k];
-            const float A = e.x * e.x + e.y * e.y + e.z * e.z;
+            const Entry e = nl[(size_t)i * cap + k];
+            const Real A = (Real)e.x * (Real)e.x + (Real)e.y * (Real)e.y + (Real)e.z * (Real)e.z;
             se[k] = e;
-            sq[k] = make_float2(A, 1.0f / A);
+            sq[k] = Q2{A, (Real)1 / A};
         }
         __syncwarp();
         for (int a0 = 0; a0 < ni; a0 += 32) {
             const int a = a0 + lane;
             const bool av = a < ni;
-            float4 ea = make_float4(0.f, 0.f, 0.f, 0.f);
-            float2 qa = make_float2(1.f, 1.f);
-            if (av) { ea = se[a]; qa = sq[a]; }
-            const int ca = __float_as_int(ea.w);
-            const float wa = rsqrtf(qa.x);
+            Real ax = 0, ay = 0, az = 0;
+            Q2 qa{1, 1};
+            int ca = 0;
+            if (av) {
+                const Entry ea = se[a];
+                ax = (Real)ea.x; ay = (Real)ea.y; az = (Real)ea.z;
+                ca = entry_code(ea);
+                qa = sq[a];
+            }
+            const Real wa = rsqrt_r(qa.A);
             for (int d = 1; d <= ni / 2; d++) {
                 if (!av || (2 * d == ni && a >= d)) continue;
                 int b = a + d;
                 if (b >= ni) b -= ni;
-                const float4 eb = se[b];
-                const float2 qb = sq[b];
+                const Entry eb = se[b];
+                const Q2 qb = sq[b];
+                const int cb = entry_code(eb);
                 if (COMPAT) {
-                    const int nba = ca & 31, nbb = __float_as_int(eb.w) & 31;
+                    const int nba = ca & 31, nbb = cb & 31;
                     const bool ok = (nba == 13 && nbb == 13) || (nba != 13 && nbb != 13 && nba != nbb);
                     if (!ok) continue;
                 }
-                const float cx = eb.x - ea.x, cy = eb.y - ea.y, cz = eb.z - ea.z;
-                const float C = cx * cx + cy * cy + cz * cz;
+                const Real bx = (Real)eb.x, by = (Real)eb.y, bz = (Real)eb.z;
+                const Real cx = bx - ax, cy = by - ay, cz = bz - az;
+                const Real C = cx * cx + cy * cy + cz * cz;
                 if (C > rc2) continue;
-                const float A = qa.x, B = qb.x;
-                const float wc = rsqrtf(C);
-                const float s = wa * rsqrtf(B) * wc;       // 1/(abc)
-                const float s2 = s * s;
-                const float s5 = s2 * s2 * s;
-                const float t1 = A + B - C, t2 = A - B + C, t3 = B + C - A;
-                const float u = t2 * t3, v = t1 * t3, w = t1 * t2;
-                const float P = t1 * u;
-                const float vA = s5 * (-1.5f * B * C + 0.375f * (u + v - w) - 0.9375f * P * qa.y);
-                const float vB = s5 * (-1.5f * A * C + 0.375f * (u - v + w) - 0.9375f * P * qb.y);
-                gx += vA * ea.x + vB * eb.x;
-                gy += vA * ea.y + vB * eb.y;
-                gz += vA * ea.z + vB * eb.z;
+                const Real A = qa.A, B = qb.A;
+                const Real wc = rsqrt_r(C);
+                const Real sv = wa * rsqrt_r(B) * wc;       // 1/(abc)
+                const Real s2 = sv * sv;
+                const Real s5 = s2 * s2 * sv;
+                const Real t1 = A + B - C, t2 = A - B + C, t3 = B + C - A;
+                const Real u = t2 * t3, v = t1 * t3, w = t1 * t2;
+                const Real P = t1 * u;
+                const Real vA = s5 * ((Real)-1.5 * B * C + (Real)0.375 * (u + v - w) - (Real)0.9375 * P * qa.invA);
+                const Real vB = s5 * ((Real)-1.5 * A * C + (Real)0.375 * (u - v + w) - (Real)0.9375 * P * qb.invA);
+                gx += vA * ax + vB * bx;
+                gy += vA * ay + vB * by;
+                gz += vA * az + vB * bz;
                 if (MEASURE) {
-                    const float vC = s5 * (-1.5f * A * B + 0.375f * (-u + v + w) - 0.9375f * P * (wc * wc));
-                    a_e += (double)(s2 * s * (1.0f + 0.375f * P * s2)) * (1.0 / 3.0);
+                    const Real vC = s5 * ((Real)-1.5 * A * B + (Real)0.375 * (-u + v + w) - (Real)0.9375 * P * (wc * wc));
+                    a_e += (double)(s2 * sv * ((Real)1 + (Real)0.375 * P * s2)) * (1.0 / 3.0);
                     a_t += 1.0 / 3.0;
                     double wt;
                     if (p.virial_compat) {
-                        const int k = 1 + ((ca & 32) ? 0 : 1) + ((__float_as_int(eb.w) & 32) ? 0 : 1);
+                        const int k = 1 + ((ca & 32) ? 0 : 1) + ((cb & 32) ? 0 : 1);
                         wt = p.atm_direct ? 0.0 : 1.0 / (double)k;
                     } else {
                         wt = 1.0 / 3.0;
                     }
                     // pair-decomposed virial sum_pairs P_ab d (x) d with P_ab = -2 dV/d(r_ab^2)
-                    const double pa = -2.0 * vA, pb = -2.0 * vB, pc = -2.0 * vC;
-                    const double ax = ea.x, ay = ea.y, az = ea.z, bx = eb.x, by = eb.y, bz = eb.z;
-                    a_w[0] += wt * (pa * ax * ax + pb * bx * bx + pc * cx * cx);
-                    a_w[1] += wt * (pa * ax * ay + pb * bx * by + pc * cx * cy);
-                    a_w[2] += wt * (pa * ay * ay + pb * by * by + pc * cy * cy);
-                    a_w[3] += wt * (pa * ax * az + pb * bx * bz + pc * cx * cz);
-                    a_w[4] += wt * (pa * ay * az + pb * by * bz + pc * cy * cz);
-                    if (!p.virial_compat) a_w[5] += wt * (pa * az * az + pb * bz * bz + pc * cz * cz);
+                    const double pa = -2.0 * (double)vA, pb = -2.0 * (double)vB, pc = -2.0 * (double)vC;
+                    const double dax = ax, day = ay, daz = az, dbx = bx, dby = by, dbz = bz;
+                    const double dcx = cx, dcy = cy, dcz = cz;
+                    a_w[0] += wt * (pa * dax * dax + pb * dbx * dbx + pc * dcx * dcx);
+                    a_w[1] += wt * (pa * dax * day + pb * dbx * dby + pc * dcx * dcy);
+                    a_w[2] += wt * (pa * day * day + pb * dby * dby + pc * dcy * dcy);
+                    a_w[3] += wt * (pa * dax * daz + pb * dbx * dbz + pc * dcx * dcz);
+                    a_w[4] += wt * (pa * day * daz + pb * dby * dbz + pc * dcy * dcz);
+                    if (!p.virial_compat) a_w[5] += wt * (pa * daz * daz + pb * dbz * dbz + pc * dcz * dcz);
                 }
             }
         }
@@ -494,7 +510,7 @@ __global__ void __launch_bounds__(kBlock) k_atm(AtmParams p) {
         if (lane == 0) {
             const int site = p.slot_site[i];
             // reference sign: +2 nu (vA e_a + vB e_b); physical: the negative
-            const double sc = 2.0 * (double)p.sign * (double)p.nu;
+            const double sc = 2.0 * (double)p.sign * p.nu;
             p.f[3 * site] += sc * (double)gx;
             p.f[3 * site + 1] += sc * (double)gy;
             p.f[3 * site + 2] += sc * (double)gz;
@@ -511,16 +527,16 @@ __global__ void __launch_bounds__(kBlock) k_atm(AtmParams p) {
         __syncthreads();
         if (threadIdx.x < R_NSLOTS) {
             const int t = threadIdx.x;
-            double s = 0.0;
+            double sum = 0.0;
             int src = -1;
             if (t == R_UATM) src = 0;
             else if (t == R_TRIPS) src = 1;
             else if (t >= R_W0 && t <= R_W5) src = 2 + (t - R_W0);
             if (src >= 0)
-                for (int w = 0; w < kWarpsPerBlock; w++) s += s_part[w][src];
+                for (int w = 0; w < kWarpsPerBlock; w++) sum += s_part[w][src];
             // nu scaling of energy and virial
-            if (t == R_UATM || (t >= R_W0 && t <= R_W5)) s *= (double)p.nu;
-            p.partials[(size_t)blockIdx.x * R_NSLOTS + t] = s;
+            if (t == R_UATM || (t >= R_W0 && t <= R_W5)) sum *= p.nu;
+            p.partials[(size_t)blockIdx.x * R_NSLOTS + t] = sum;
         }
     }
 }
@@ -792,6 +808,7 @@ static PairParams pair_params(Engine &e) {
     p.stiffness = e.cfg.stiffness;
     p.use_lj = lj ? 1 : 0;
     p.virial_compat = e.cfg.virial_mode == KOMD_VIRIAL_COMPAT;
+    p.offtab = e.offtab;
     return p;
 }
 
@@ -815,23 +832,31 @@ static void pair_dispatch(PairParams &p, bool measure, bool emit, bool fene, int
     }
 }
 
-int pair_grid(const Engine &e) { return nblk(e.g.ncell, kWarpsPerBlock); }
 int atm_grid(const Engine &e) { return nblk(e.n, kWarpsPerBlock); }
 
-void launch_pair(Engine &e, cudaStream_t st, bool measure, double *lj_hist) {
+// The FP32 force path runs the tiled kernel (pair_tile.cu, one CTA per cell);
+// FP64 mode, FENE and the LJ sensor histograms use the warp-per-cell kernel
+// above.  Returns the number of blocks whose partial sums were written.
+int launch_pair(Engine &e, cudaStream_t st, bool measure, double *lj_hist) {
     PairParams p = pair_params(e);
     p.lj_hist = lj_hist;
     const bool emit = (e.cfg.terms & KOMD_TERM_ATM) != 0;
     const bool fene = (e.cfg.terms & KOMD_TERM_FENE) != 0;
-    if (e.cfg.precision == KOMD_FP64) pair_dispatch<double>(p, measure, emit, fene, pair_grid(e), st);
-    else pair_dispatch<float>(p, measure, emit, fene, pair_grid(e), st);
+    if (e.cfg.precision == KOMD_FP32 && !fene && !lj_hist) {
+        launch_pair_tile(p, e.g.ncell, measure, emit, st);
+        return e.g.ncell;
+    }
+    const int grid = nblk(e.g.ncell, kWarpsPerBlock);
+    if (e.cfg.precision == KOMD_FP64) pair_dispatch<double>(p, measure, emit, fene, grid, st);
+    else pair_dispatch<float>(p, measure, emit, fene, grid, st);
+    return grid;
 }
 
 void launch_counts(Engine &e, cudaStream_t st) {
     PairParams p = pair_params(e);
     p.use_lj = 1;
     p.scan2 = p.rc2;
-    k_pair<double, false, false, false, true><<<pair_grid(e), kBlock, 0, st>>>(p);
+    k_pair<double, false, false, false, true><<<nblk(e.g.ncell, kWarpsPerBlock), kBlock, 0, st>>>(p);
 }
 
 void launch_bonded(Engine &e, cudaStream_t st, bool measure, double *acc) {
@@ -847,7 +872,22 @@ void launch_limit(Engine &e, cudaStream_t st) {
     k_limit<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.eps, e.sig, e.cfg.limit, e.f);
 }
 
-size_t atm_smem(const Engine &e) { return (size_t)kWarpsPerBlock * e.nl_cap * (sizeof(float4) + sizeof(float2)); }
+size_t atm_smem(const Engine &e) {
+    const size_t per = e.cfg.precision == KOMD_FP64 ? (sizeof(AtmEntryD) + 2 * sizeof(double))
+                                                    : (sizeof(float4) + 2 * sizeof(float));
+    return (size_t)kWarpsPerBlock * e.nl_cap * per;
+}
+
+template <typename Real>
+static void atm_dispatch(AtmParams &p, bool measure, bool compat, int grid, size_t sm, cudaStream_t st) {
+    if (measure) {
+        if (compat) k_atm<Real, true, true><<<grid, kBlock, sm, st>>>(p);
+        else k_atm<Real, true, false><<<grid, kBlock, sm, st>>>(p);
+    } else {
+        if (compat) k_atm<Real, false, true><<<grid, kBlock, sm, st>>>(p);
+        else k_atm<Real, false, false><<<grid, kBlock, sm, st>>>(p);
+    }
+}
 
 void launch_atm(Engine &e, cudaStream_t st, bool measure) {
     AtmParams p;
@@ -858,21 +898,14 @@ void launch_atm(Engine &e, cudaStream_t st, bool measure) {
     p.nl_cap = e.nl_cap;
     p.f = e.f;
     p.partials = e.partials;
-    p.nu = (float)e.cfg.nu;
-    p.rc2 = (float)(e.cfg.cutoff_3b * e.cfg.cutoff_3b);
-    p.sign = e.cfg.atm_sign == KOMD_ATM_SIGN_REFERENCE ? 1.0f : -1.0f;
+    p.nu = e.cfg.nu;
+    p.rc2 = e.cfg.cutoff_3b * e.cfg.cutoff_3b;
+    p.sign = e.cfg.atm_sign == KOMD_ATM_SIGN_REFERENCE ? 1.0 : -1.0;
     p.virial_compat = e.cfg.virial_mode == KOMD_VIRIAL_COMPAT;
     p.atm_direct = e.cfg.atm_direct;
     const bool compat = e.cfg.atm_enum == KOMD_ATM_ENUM_COMPAT;
-    const size_t sm = atm_smem(e);
-    const int grid = atm_grid(e);
-    if (measure) {
-        if (compat) k_atm<true, true><<<grid, kBlock, sm, st>>>(p);
-        else k_atm<true, false><<<grid, kBlock, sm, st>>>(p);
-    } else {
-        if (compat) k_atm<false, true><<<grid, kBlock, sm, st>>>(p);
-        else k_atm<false, false><<<grid, kBlock, sm, st>>>(p);
-    }
+    if (e.cfg.precision == KOMD_FP64) atm_dispatch<double>(p, measure, compat, atm_grid(e), atm_smem(e), st);
+    else atm_dispatch<float>(p, measure, compat, atm_grid(e), atm_smem(e), st);
 }
 
 void launch_step0(Engine &e, cudaStream_t st) {
@@ -903,12 +936,16 @@ void launch_rdf(Engine &e, cudaStream_t st, double *bins, bool cells) {
 }
 
 void set_kernel_attributes(Engine &e) {
-    const size_t sm = atm_smem(e);
+    const int sm = (int)atm_smem(e);
     if (sm > 48 * 1024) {
-        cudaFuncSetAttribute(k_atm<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        cudaFuncSetAttribute(k_atm<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        cudaFuncSetAttribute(k_atm<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        cudaFuncSetAttribute(k_atm<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaFuncSetAttribute(k_atm<float, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        cudaFuncSetAttribute(k_atm<float, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        cudaFuncSetAttribute(k_atm<float, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        cudaFuncSetAttribute(k_atm<float, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        cudaFuncSetAttribute(k_atm<double, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        cudaFuncSetAttribute(k_atm<double, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        cudaFuncSetAttribute(k_atm<double, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        cudaFuncSetAttribute(k_atm<double, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     }
 }
 

@@ -4,7 +4,8 @@
 
 namespace komd {
 void launch_container(Engine &e, cudaStream_t st);
-void launch_pair(Engine &e, cudaStream_t st, bool measure, double *lj_hist);
+int launch_pair(Engine &e, cudaStream_t st, bool measure, double *lj_hist);
+void launch_pair_tile(PairParams &p, int ncell, bool measure, bool emit, cudaStream_t st);
 void launch_counts(Engine &e, cudaStream_t st);
 void launch_bonded(Engine &e, cudaStream_t st, bool measure, double *acc);
 void launch_limit(Engine &e, cudaStream_t st);
@@ -15,7 +16,6 @@ void launch_kinetic(Engine &e, cudaStream_t st, int n_terms);
 void launch_sum_partials(cudaStream_t st, int nblocks, const double *partials, double *out);
 void launch_rdf(Engine &e, cudaStream_t st, double *bins, bool cells);
 void set_kernel_attributes(Engine &e);
-int pair_grid(const Engine &e);
 int atm_grid(const Engine &e);
 int kinetic_grid(const Engine &e);
 size_t atm_smem(const Engine &e);

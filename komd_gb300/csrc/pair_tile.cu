@@ -1,0 +1,258 @@
+// pair_tile.cu -- the FP32 pair kernel of the hot path: LJ 12-6 forces
+// (LJ12_6.cpp:15-43), energy and virial, and the ATM neighbour list inside
+// cutoff_3b, for one home cell per CTA.
+//
+//   1. threads 0..26 resolve the 27 neighbour cells (periodic wrap) and their
+//      home-relative offsets from a per-dimension FP32 table computed once in
+//      FP64 on the host, so no FP64 instruction runs in this kernel;
+//   2. the neighbourhood's sites are staged in shared memory in home-cell
+//      coordinates (float4 position + slot, key, cell code, sqrt(eps));
+//   3. every warp owns a subset of home sites; for a home site the 32 lanes
+//      test 32 staged candidates at a time and ballot-compact the hits into a
+//      per-warp queue, so the force arithmetic always runs on full warps;
+//   4. each dequeued pair adds its LJ force to the home site's shared-memory
+//      accumulator and, inside cutoff_3b, appends (r_i - r_j, code) to the
+//      home site's ATM list in queue order (deterministic list order).
+// Full shell: each site's force is summed by its own CTA, no global atomics.
+#include "engine.cuh"
+#include "kernels.cuh"
+
+namespace komd {
+
+constexpr int kTileWarps = 4;
+constexpr int kTileThreads = 32 * kTileWarps;
+constexpr int kStage = 640;   // staged neighbour sites per round (more rounds if a neighbourhood is larger)
+constexpr int kHome = 64;     // home sites per round
+constexpr int kQ = 64;        // per-warp hit queue
+
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// neighbour nb (dx fastest) of domain cell (cx, cy, cz), wrapped; integer only
+__device__ __forceinline__ int nb_cell(const Grid &g, int cx, int cy, int cz, int nb, int &kx, int &ky, int &kz,
+                                       bool &crosses) {
+    kx = cx + nb % 3 - 1;
+    ky = cy + (nb / 3) % 3 - 1;
+    kz = cz + nb / 9 - 1;
+    crosses = false;
+    if (kx < 0) { kx += g.nd[0]; crosses = true; } else if (kx >= g.nd[0]) { kx -= g.nd[0]; crosses = true; }
+    if (ky < 0) { ky += g.nd[1]; crosses = true; } else if (ky >= g.nd[1]) { ky -= g.nd[1]; crosses = true; }
+    if (kz < 0) { kz += g.nd[2]; crosses = true; } else if (kz >= g.nd[2]) { kz -= g.nd[2]; crosses = true; }
+    return kx + g.nd[0] * (ky + g.nd[1] * kz);
+}
+
+template <bool MEASURE, bool EMIT>
+__global__ void __launch_bounds__(kTileThreads) k_pair_tile(PairParams p) {
+    __shared__ float4 s_pos[kStage];
+    __shared__ int4 s_aux[kStage];        // slot, key, code (nb | crosses << 5), sqrt(eps) bits
+    __shared__ float4 s_hpos[kHome];
+    __shared__ int2 s_haux[kHome];        // key, sqrt(eps) bits
+    __shared__ float s_f[kHome * 3];
+    __shared__ int s_cnt[kHome];
+    __shared__ unsigned s_q[kTileWarps][kQ];
+    __shared__ int s_nbs[27], s_nbn[27], s_nbpre[28], s_nbc[27];
+    __shared__ float s_nbo[27][3];
+    __shared__ double s_part[kTileWarps][8];
+
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int cell = blockIdx.x;
+    int cx, cy, cz;
+    cell_coords(p.g, cell, cx, cy, cz);
+    if (tid < 27) {
+        int kx, ky, kz;
+        bool cr;
+        const int c = nb_cell(p.g, cx, cy, cz, tid, kx, ky, kz, cr);
+        const int s0 = p.cell_start[c];
+        s_nbs[tid] = s0;
+        s_nbn[tid] = p.cell_start[c + 1] - s0;
+        s_nbc[tid] = cr ? 32 : 0;
+        // home-relative offset of the neighbour cell's centre (FP32 table, per dimension)
+        s_nbo[tid][0] = p.offtab[cx * 3 + tid % 3];
+        s_nbo[tid][1] = p.offtab[p.g.nd[0] * 3 + cy * 3 + (tid / 3) % 3];
+        s_nbo[tid][2] = p.offtab[(p.g.nd[0] + p.g.nd[1]) * 3 + cz * 3 + tid / 9];
+    }
+    __syncthreads();
+    if (tid == 0) {
+        int acc = 0;
+        for (int k = 0; k < 27; k++) { s_nbpre[k] = acc; acc += s_nbn[k]; }
+        s_nbpre[27] = acc;
+    }
+    __syncthreads();
+    const int Nn = s_nbpre[27];
+    const int hs = s_nbs[13], hn = s_nbn[13];
+    const float rc2 = (float)p.rc2, rc3sq = (float)p.rc3sq, scan2 = (float)p.scan2;
+    float4 *nl = p.nl;
+    double a_u = 0.0, a_pairs = 0.0, a_w[6] = {0, 0, 0, 0, 0, 0};
+
+    for (int hb = 0; hb < hn; hb += kHome) {
+        const int hc = min(kHome, hn - hb);
+        for (int t = tid; t < hc; t += kTileThreads) {
+            s_hpos[t] = p.pos4[hs + hb + t];
+            s_haux[t] = make_int2(p.skey[hs + hb + t], __float_as_int(p.seps[hs + hb + t]));
+            s_f[3 * t] = 0.f; s_f[3 * t + 1] = 0.f; s_f[3 * t + 2] = 0.f;
+            s_cnt[t] = 0;
+        }
+        const int self_base = s_nbpre[13] + hb;
+        for (int sb = 0; sb < Nn; sb += kStage) {
+            const int ns = min(kStage, Nn - sb);
+            __syncthreads();
+            for (int t = tid; t < ns; t += kTileThreads) {
+                const int gi = sb + t;
+                int lo = 0, hi = 27;            // largest nb with s_nbpre[nb] <= gi
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (s_nbpre[mid] <= gi) lo = mid; else hi = mid;
+                }
+                const int nb = lo;
+                const int j = s_nbs[nb] + (gi - s_nbpre[nb]);
+                float4 q = p.pos4[j];
+                q.x += s_nbo[nb][0];
+                q.y += s_nbo[nb][1];
+                q.z += s_nbo[nb][2];
+                s_pos[t] = q;
+                s_aux[t] = make_int4(j, p.skey[j], nb | s_nbc[nb], __float_as_int(p.seps[j]));
+            }
+            __syncthreads();
+
+            // process one queued pair per lane (valid = lane holds an entry)
+            auto process = [&](unsigned e, bool valid) {
+                const int i = valid ? (int)(e >> 16) : 0;
+                const int j = valid ? (int)(e & 0xffffu) : 0;
+                const float4 pi = s_hpos[i];
+                const float4 pj = s_pos[j];
+                const int4 a = s_aux[j];
+                const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                if (p.use_lj && valid && r2 <= rc2 && s_haux[i].x != a.y) {
+                    const float inv = rcp_approx(r2);
+                    const float sg = pi.w + pj.w;
+                    const float x = sg * sg * inv;
+                    const float lj6 = x * x * x;
+                    const float ee = __int_as_float(s_haux[i].y) * __int_as_float(a.w);
+                    const float ljd = 24.0f * ee * (2.0f * lj6 * lj6 - lj6);
+                    const float fac = ljd * inv;
+                    atomicAdd(&s_f[3 * i], dx * fac);
+                    atomicAdd(&s_f[3 * i + 1], dy * fac);
+                    atomicAdd(&s_f[3 * i + 2], dz * fac);
+                    if (MEASURE) {
+                        const double wt = (p.virial_compat && (a.z & 32)) ? 1.0 : 0.5;
+                        const double gx = (double)dx * fac, gy = (double)dy * fac, gz = (double)dz * fac;
+                        a_u += 0.5 * (double)(4.0f * ee * (lj6 * lj6 - lj6));
+                        a_pairs += 0.5;
+                        a_w[0] += wt * (dx * gx);
+                        a_w[1] += wt * 0.5 * (dx * gy + dy * gx);
+                        a_w[2] += wt * (dy * gy);
+                        a_w[3] += wt * 0.5 * (dx * gz + dz * gx);
+                        a_w[4] += wt * 0.5 * (dy * gz + dz * gy);
+                        a_w[5] += wt * (dz * gz);
+                    }
+                }
+                if (EMIT) {
+                    const bool emit = valid && r2 <= rc3sq;
+                    const unsigned grp = __match_any_sync(0xffffffffu, valid ? i : (0x10000 | lane));
+                    const unsigned em = __ballot_sync(0xffffffffu, emit) & grp;
+                    int base = 0;
+                    if (emit) base = s_cnt[i];
+                    __syncwarp();
+                    if (valid && lane == __ffs(grp) - 1) s_cnt[i] += __popc(em);
+                    if (emit) {
+                        const int c = base + __popc(em & lanemask_lt());
+                        const int slot_i = hs + hb + i;
+                        if (c < p.nl_cap)
+                            nl[(size_t)slot_i * p.nl_cap + c] = make_float4(dx, dy, dz, __int_as_float(a.z | (a.x << 6)));
+                    }
+                    __syncwarp();
+                }
+            };
+
+            int qn = 0;
+            for (int i = w; i < hc; i += kTileWarps) {
+                const float4 pi = s_hpos[i];
+                const int self = self_base + i - sb;
+                for (int j0 = 0; j0 < ns; j0 += 32) {
+                    const int j = j0 + lane;
+                    bool hit = false;
+                    if (j < ns && j != self) {
+                        const float4 pj = s_pos[j];
+                        const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                        hit = dx * dx + dy * dy + dz * dz <= scan2;
+                    }
+                    const unsigned m = __ballot_sync(0xffffffffu, hit);
+                    if (hit) s_q[w][qn + __popc(m & lanemask_lt())] = ((unsigned)i << 16) | (unsigned)j;
+                    qn += __popc(m);
+                    if (qn >= 32) {
+                        __syncwarp();
+                        const unsigned e = s_q[w][lane];
+                        const unsigned tail = (lane < qn - 32) ? s_q[w][lane + 32] : 0u;
+                        __syncwarp();
+                        if (lane < qn - 32) s_q[w][lane] = tail;
+                        __syncwarp();
+                        qn -= 32;
+                        process(e, true);
+                    }
+                }
+            }
+            __syncwarp();
+            if (qn > 0) {
+                const unsigned e = (lane < qn) ? s_q[w][lane] : 0u;
+                __syncwarp();
+                process(e, lane < qn);
+            }
+        }
+        __syncthreads();
+        for (int t = tid; t < hc; t += kTileThreads) {
+            const int slot = hs + hb + t;
+            const int site = p.slot_site[slot];
+            p.f[3 * site] = (double)s_f[3 * t];
+            p.f[3 * site + 1] = (double)s_f[3 * t + 1];
+            p.f[3 * site + 2] = (double)s_f[3 * t + 2];
+            if (EMIT) {
+                const int c = s_cnt[t];
+                p.nl_count[slot] = min(c, p.nl_cap);
+                if (c > p.nl_cap) atomicOr(&p.err[E_ATM_OVERFLOW], 1);
+            }
+        }
+        __syncthreads();
+    }
+    if (MEASURE) {
+        double vals[8] = {a_u, a_w[0], a_w[1], a_w[2], a_w[3], a_w[4], a_w[5], a_pairs};
+        for (int k = 0; k < 8; k++) {
+            double x = vals[k];
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            vals[k] = x;
+        }
+        if (lane == 0) for (int k = 0; k < 8; k++) s_part[w][k] = vals[k];
+        __syncthreads();
+        if (tid < R_NSLOTS) {
+            double s = 0.0;
+            int src = -1;
+            if (tid == R_ULJ) src = 0;
+            else if (tid >= R_W0 && tid <= R_W5) src = 1 + tid - R_W0;
+            else if (tid == R_PAIRS) src = 7;
+            if (src >= 0)
+                for (int k = 0; k < kTileWarps; k++) s += s_part[k][src];
+            p.partials[(size_t)blockIdx.x * R_NSLOTS + tid] = s;
+        }
+    }
+}
+
+void launch_pair_tile(PairParams &p, int ncell, bool measure, bool emit, cudaStream_t st) {
+    if (measure) {
+        if (emit) k_pair_tile<true, true><<<ncell, kTileThreads, 0, st>>>(p);
+        else k_pair_tile<true, false><<<ncell, kTileThreads, 0, st>>>(p);
+    } else {
+        if (emit) k_pair_tile<false, true><<<ncell, kTileThreads, 0, st>>>(p);
+        else k_pair_tile<false, false><<<ncell, kTileThreads, 0, st>>>(p);
+    }
+}
+
+}  // namespace komd

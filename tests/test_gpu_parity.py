@@ -164,17 +164,19 @@ def test_atm_full_physical_vs_oracle(oracle_lib):
 
 
 def test_atm_physical_is_minus_gradient():
-    """Finite differences of the GPU ATM energy equal the GPU physical force."""
+    """Central differences of the GPU ATM energy equal the GPU physical force
+    (FP64 mode, step 1e-6: small enough that no triplet side crosses the
+    truncation at cutoff_3b, where the energy jumps)."""
     from komd_gb300 import gpu, lattice
     s = lattice.argon_fcc(4, rho=0.8442, t_star=0.722, seed=22, jitter=0.08)
     cfg = gpu.make_config(s.low, s.high, 2.0, cutoff=2.0, cutoff_3b=2.0, nu=0.073, terms=gpu.TERM_ATM,
-                          precision=gpu.FP32, atm_sign=gpu.ATM_SIGN_PHYSICAL, atm_enum=gpu.ATM_ENUM_FULL)
+                          precision=gpu.FP64, atm_sign=gpu.ATM_SIGN_PHYSICAL, atm_enum=gpu.ATM_ENUM_FULL)
     g = gpu.GpuSystem(s, cfg)
     g.update_container()
     g.forces()
     _, _, f = g.download()
-    h = 2e-3
-    for atom in (0, 7, 31):
+    h = 1e-6
+    for atom in (0, 7, 31, 100):
         for d in range(3):
             e = []
             for sgn in (1, -1):
@@ -184,13 +186,13 @@ def test_atm_physical_is_minus_gradient():
                 g.update_container()
                 e.append(g.measure(gpu.MEASURE_ENERGY)["u_atm"])
             fd = -(e[0] - e[1]) / (2 * h)
-            assert fd == pytest.approx(f[atom, d], rel=2e-2, abs=2e-4)
+            assert fd == pytest.approx(f[atom, d], rel=1e-5, abs=1e-7)
     g.close()
 
 
 def test_bonded_vs_oracle(oracle_lib):
     from komd_gb300 import gpu, lattice
-    s = lattice.triatomic_sc(4, rho_site=0.5, t_star=1.0, seed=23)
+    s = lattice.triatomic_sc(5, rho_site=0.5, t_star=1.0, seed=23)
     s.r = s.r + np.random.default_rng(5).normal(0, 0.03, s.r.shape)   # strain bonds and angles
     th0 = np.deg2rad(109.47)
     cfg = gpu.make_config(s.low, s.high, 2.5, cutoff=2.5, terms=gpu.TERM_LJ | gpu.TERM_BONDED, bond_k=1000.0,
@@ -262,5 +264,5 @@ def test_full_size_binning_and_momentum():
     assert np.abs(f.sum(0)).max() < 1e-3 * np.sqrt(s.n) * np.abs(f).mean()
     obs = g.measure(gpu.MEASURE_ENERGY | gpu.MEASURE_TEMPERATURE)
     assert obs["n_in_box"] == s.n
-    assert obs["triplets"] > 50 * s.n
+    assert obs["triplets"] > 15 * s.n     # thermalised FCC: 18 neighbours inside 2.0
     g.close()

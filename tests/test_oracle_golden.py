@@ -105,3 +105,32 @@ def test_momentum_conservation_full_atm(oracle_lib):
     assert np.abs(full.f.sum(0)).max() < 1e-10 * np.abs(full.f).max()
     # the COMPAT set misses the (A,A,B) classes: it holds fewer triplets
     assert full.atm_out.triplets > vc.atm_out.triplets
+
+
+@pytest.mark.parametrize("sign", ["physical", "reference"])
+def test_oracle_atm_force_is_gradient(oracle_lib, sign):
+    """ATM force of the oracle against central differences of its energy:
+    PHYSICAL is -grad V; REFERENCE reproduces the reference kernel's +grad V."""
+    from komd_gb300 import lattice
+    s = lattice.argon_fcc(4, rho=0.8442, t_star=0.722, seed=22, jitter=0.08)
+    sg = oracle_lib.ATM_SIGN_PHYSICAL if sign == "physical" else oracle_lib.ATM_SIGN_REFERENCE
+
+    def run(r):
+        s2 = lattice.System(r=r, v=s.v, m=s.m, eps=s.eps, sig=s.sig, mol_id=s.mol_id, low=s.low, high=s.high)
+        o = oracle_lib.OracleSim(s2, 2.0, 2.0, nu=0.073, lj=False, atm=True, atm_mode="full", atm_sign=sg,
+                                 virial_mode=oracle_lib.VIRIAL_CORRECT)
+        o.update_container()
+        o.forces()
+        return o
+    o = run(s.r.copy())
+    h = 1e-6
+    for atom in (0, 7, 31):
+        for d in range(3):
+            e = []
+            for k in (1, -1):
+                r = s.r.copy()
+                r[atom, d] += k * h
+                e.append(run(r).atm_out.energy)
+            grad = (e[0] - e[1]) / (2 * h)
+            expect = -grad if sign == "physical" else grad
+            assert o.f[atom, d] == pytest.approx(expect, rel=1e-6, abs=1e-9)
