@@ -541,6 +541,168 @@ __global__ void __launch_bounds__(kBlock) k_atm(AtmParams p) {
     }
 }
 
+// FP32 ATM kernel with ballot compaction: lanes test candidate pairs (a, b)
+// of the vertex's neighbour list (round-robin pairing a, a+d mod n, so each
+// unordered pair is tested once) and queue the ones inside the cutoff; the
+// triplet arithmetic then always runs on 32 queued pairs at a time.  All
+// queued pairs share vertex i, so each lane keeps a private force sum.
+template <bool MEASURE, bool COMPAT>
+__global__ void __launch_bounds__(kBlock) k_atm_q(AtmParams p) {
+    extern __shared__ float4 s_dyn[];
+    __shared__ unsigned s_q[kWarpsPerBlock][64];
+    __shared__ float s_qc[kWarpsPerBlock][64];
+    __shared__ double s_part[kWarpsPerBlock][8];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int cap = p.nl_cap;
+    float4 *se = s_dyn + wib * cap;
+    float2 *sq = reinterpret_cast<float2 *>(s_dyn + kWarpsPerBlock * cap) + wib * cap;
+    const int i = blockIdx.x * kWarpsPerBlock + wib;
+    const float rc2 = (float)p.rc2;
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+    float m_e = 0.f, m_t = 0.f, m_w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    unsigned lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+
+    auto triplet = [&](unsigned e, float C, bool valid) {
+        if (!valid) return;
+        const int a = (int)(e & 0xffffu), b = (int)(e >> 16);
+        const float4 ea = se[a], eb = se[b];
+        const float2 qa = sq[a], qb = sq[b];
+        const float A = qa.x, B = qb.x;
+        const float wc = rsqrtf(C);
+        const float sv = rsqrtf(A) * rsqrtf(B) * wc;       // 1/(abc)
+        const float s2 = sv * sv;
+        const float s5 = s2 * s2 * sv;
+        const float t1 = A + B - C, t2 = A - B + C, t3 = B + C - A;
+        const float u = t2 * t3, v = t1 * t3, w = t1 * t2;
+        const float P = t1 * u;
+        const float vA = s5 * (-1.5f * B * C + 0.375f * (u + v - w) - 0.9375f * P * qa.y);
+        const float vB = s5 * (-1.5f * A * C + 0.375f * (u - v + w) - 0.9375f * P * qb.y);
+        gx += vA * ea.x + vB * eb.x;
+        gy += vA * ea.y + vB * eb.y;
+        gz += vA * ea.z + vB * eb.z;
+        if (MEASURE) {
+            const float vC = s5 * (-1.5f * A * B + 0.375f * (-u + v + w) - 0.9375f * P * (wc * wc));
+            m_e += s2 * sv * (1.0f + 0.375f * P * s2) * (1.0f / 3.0f);
+            m_t += 1.0f / 3.0f;
+            float wt;
+            if (p.virial_compat) {
+                const int ca = __float_as_int(ea.w), cb = __float_as_int(eb.w);
+                const int k = 1 + ((ca & 32) ? 0 : 1) + ((cb & 32) ? 0 : 1);
+                wt = p.atm_direct ? 0.0f : 1.0f / (float)k;
+            } else {
+                wt = 1.0f / 3.0f;
+            }
+            const float pa = -2.0f * vA * wt, pb = -2.0f * vB * wt, pc = -2.0f * vC * wt;
+            const float cx = eb.x - ea.x, cy = eb.y - ea.y, cz = eb.z - ea.z;
+            m_w[0] += pa * ea.x * ea.x + pb * eb.x * eb.x + pc * cx * cx;
+            m_w[1] += pa * ea.x * ea.y + pb * eb.x * eb.y + pc * cx * cy;
+            m_w[2] += pa * ea.y * ea.y + pb * eb.y * eb.y + pc * cy * cy;
+            m_w[3] += pa * ea.x * ea.z + pb * eb.x * eb.z + pc * cx * cz;
+            m_w[4] += pa * ea.y * ea.z + pb * eb.y * eb.z + pc * cy * cz;
+            if (!p.virial_compat) m_w[5] += pa * ea.z * ea.z + pb * eb.z * eb.z + pc * cz * cz;
+        }
+    };
+
+    if (i < p.n) {
+        const int ni = p.nl_count[i];
+        for (int k = lane; k < ni; k += 32) {
+            const float4 e = p.nl[(size_t)i * cap + k];
+            const float A = e.x * e.x + e.y * e.y + e.z * e.z;
+            se[k] = e;
+            sq[k] = make_float2(A, 1.0f / A);
+        }
+        __syncwarp();
+        int qn = 0;
+        const int half = ni / 2;
+        for (int a0 = 0; a0 < ni; a0 += 32) {
+            const int a = a0 + lane;
+            const bool av = a < ni;
+            float4 ea = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (av) ea = se[a];
+            for (int d = 1; d <= half; d++) {
+                bool hit = false;
+                int b = 0;
+                float C = 0.f;
+                if (av && !(2 * d == ni && a >= d)) {
+                    b = a + d;
+                    if (b >= ni) b -= ni;
+                    const float4 eb = se[b];
+                    bool ok = true;
+                    if (COMPAT) {
+                        const int nba = __float_as_int(ea.w) & 31, nbb = __float_as_int(eb.w) & 31;
+                        ok = (nba == 13 && nbb == 13) || (nba != 13 && nbb != 13 && nba != nbb);
+                    }
+                    const float cx = eb.x - ea.x, cy = eb.y - ea.y, cz = eb.z - ea.z;
+                    C = cx * cx + cy * cy + cz * cz;
+                    hit = ok && C <= rc2;
+                }
+                const unsigned m = __ballot_sync(0xffffffffu, hit);
+                if (hit) {
+                    const int pos = qn + __popc(m & lt);
+                    s_q[wib][pos] = (unsigned)a | ((unsigned)b << 16);
+                    s_qc[wib][pos] = C;
+                }
+                qn += __popc(m);
+                if (qn >= 32) {
+                    __syncwarp();
+                    const unsigned e = s_q[wib][lane];
+                    const float ce = s_qc[wib][lane];
+                    const bool mv = lane < qn - 32;
+                    const unsigned te = mv ? s_q[wib][lane + 32] : 0u;
+                    const float tc = mv ? s_qc[wib][lane + 32] : 0.f;
+                    __syncwarp();
+                    if (mv) { s_q[wib][lane] = te; s_qc[wib][lane] = tc; }
+                    __syncwarp();
+                    qn -= 32;
+                    triplet(e, ce, true);
+                }
+            }
+        }
+        __syncwarp();
+        if (qn > 0) {
+            const bool v = lane < qn;
+            const unsigned e = v ? s_q[wib][lane] : 0u;
+            const float ce = v ? s_qc[wib][lane] : 1.f;
+            triplet(e, ce, v);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            gx += __shfl_xor_sync(0xffffffffu, gx, o);
+            gy += __shfl_xor_sync(0xffffffffu, gy, o);
+            gz += __shfl_xor_sync(0xffffffffu, gz, o);
+        }
+        if (lane == 0) {
+            const int site = p.slot_site[i];
+            const double sc = 2.0 * p.sign * p.nu;   // reference: +2 nu (...); physical: -2 nu (...)
+            p.f[3 * site] += sc * (double)gx;
+            p.f[3 * site + 1] += sc * (double)gy;
+            p.f[3 * site + 2] += sc * (double)gz;
+        }
+    }
+    if (MEASURE) {
+        double vals[8] = {m_e, m_t, m_w[0], m_w[1], m_w[2], m_w[3], m_w[4], m_w[5]};
+        for (int k = 0; k < 8; k++) {
+            double x = vals[k];
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            vals[k] = x;
+        }
+        if (lane == 0) for (int k = 0; k < 8; k++) s_part[wib][k] = vals[k];
+        __syncthreads();
+        if (threadIdx.x < R_NSLOTS) {
+            const int t = threadIdx.x;
+            double sum = 0.0;
+            int src = -1;
+            if (t == R_UATM) src = 0;
+            else if (t == R_TRIPS) src = 1;
+            else if (t >= R_W0 && t <= R_W5) src = 2 + (t - R_W0);
+            if (src >= 0)
+                for (int w = 0; w < kWarpsPerBlock; w++) sum += s_part[w][src];
+            if (t == R_UATM || (t >= R_W0 && t <= R_W5)) sum *= p.nu;
+            p.partials[(size_t)blockIdx.x * R_NSLOTS + t] = sum;
+        }
+    }
+}
+
 // ===========================================================================
 // bonded terms (no reference counterpart): harmonic bond and angle, FP32
 // arithmetic on FP64 differences, FP64 atomic accumulation into f.
@@ -749,12 +911,14 @@ __global__ void k_rdf_all(Grid g, int n_mol, const double *__restrict__ com, dou
         if (o != k) rdf_pair(com + 3 * k, com + 3 * o, g, max_r, dr, nbins, bins);
 }
 
+// Sums the per-block partial rows: one warp per slot, fixed lane-to-block
+// mapping and a fixed shuffle tree, so the result is deterministic.
 __global__ void k_sum_partials(int nblocks, const double *__restrict__ partials, double *__restrict__ out) {
-    const int t = threadIdx.x;   // one thread per slot, sequential over blocks (deterministic)
-    if (t >= R_NSLOTS) return;
+    const int slot = blockIdx.x, lane = threadIdx.x;
     double s = 0.0;
-    for (int b = 0; b < nblocks; b++) s += partials[(size_t)b * R_NSLOTS + t];
-    out[t] += s;
+    for (int b = lane; b < nblocks; b += 32) s += partials[(size_t)b * R_NSLOTS + slot];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) out[slot] += s;
 }
 
 // ===========================================================================
@@ -889,6 +1053,17 @@ static void atm_dispatch(AtmParams &p, bool measure, bool compat, int grid, size
     }
 }
 
+template <>
+void atm_dispatch<float>(AtmParams &p, bool measure, bool compat, int grid, size_t sm, cudaStream_t st) {
+    if (measure) {
+        if (compat) k_atm_q<true, true><<<grid, kBlock, sm, st>>>(p);
+        else k_atm_q<true, false><<<grid, kBlock, sm, st>>>(p);
+    } else {
+        if (compat) k_atm_q<false, true><<<grid, kBlock, sm, st>>>(p);
+        else k_atm_q<false, false><<<grid, kBlock, sm, st>>>(p);
+    }
+}
+
 void launch_atm(Engine &e, cudaStream_t st, bool measure) {
     AtmParams p;
     p.n = (int)e.n;
@@ -923,7 +1098,7 @@ void launch_kinetic(Engine &e, cudaStream_t st, int n_terms) {
 }
 
 void launch_sum_partials(cudaStream_t st, int nblocks, const double *partials, double *out) {
-    k_sum_partials<<<1, 32, 0, st>>>(nblocks, partials, out);
+    k_sum_partials<<<R_NSLOTS, 32, 0, st>>>(nblocks, partials, out);
 }
 
 void launch_rdf(Engine &e, cudaStream_t st, double *bins, bool cells) {
@@ -938,10 +1113,10 @@ void launch_rdf(Engine &e, cudaStream_t st, double *bins, bool cells) {
 void set_kernel_attributes(Engine &e) {
     const int sm = (int)atm_smem(e);
     if (sm > 48 * 1024) {
-        cudaFuncSetAttribute(k_atm<float, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-        cudaFuncSetAttribute(k_atm<float, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-        cudaFuncSetAttribute(k_atm<float, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-        cudaFuncSetAttribute(k_atm<float, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        cudaFuncSetAttribute(k_atm_q<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        cudaFuncSetAttribute(k_atm_q<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        cudaFuncSetAttribute(k_atm_q<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        cudaFuncSetAttribute(k_atm_q<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
         cudaFuncSetAttribute(k_atm<double, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
         cudaFuncSetAttribute(k_atm<double, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
         cudaFuncSetAttribute(k_atm<double, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);

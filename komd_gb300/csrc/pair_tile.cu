@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(kTileThreads) k_pair_tile(PairParams p) {
     const int hs = s_nbs[13], hn = s_nbn[13];
     const float rc2 = (float)p.rc2, rc3sq = (float)p.rc3sq, scan2 = (float)p.scan2;
     float4 *nl = p.nl;
-    double a_u = 0.0, a_pairs = 0.0, a_w[6] = {0, 0, 0, 0, 0, 0};
+    float m_u = 0.f, m_pairs = 0.f, m_w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};   // per-lane partials (MEASURE)
 
     for (int hb = 0; hb < hn; hb += kHome) {
         const int hc = min(kHome, hn - hb);
@@ -123,7 +123,11 @@ __global__ void __launch_bounds__(kTileThreads) k_pair_tile(PairParams p) {
             }
             __syncthreads();
 
-            // process one queued pair per lane (valid = lane holds an entry)
+            // Process one queued pair per lane (valid = lane holds an entry).
+            // Entries of one home site occupy contiguous lanes (the queue is
+            // filled site by site), and a site belongs to exactly one warp:
+            // its force is reduced over its lane group and added by the
+            // group's first lane with a plain read-modify-write.
             auto process = [&](unsigned e, bool valid) {
                 const int i = valid ? (int)(e >> 16) : 0;
                 const int j = valid ? (int)(e & 0xffffu) : 0;
@@ -132,6 +136,9 @@ __global__ void __launch_bounds__(kTileThreads) k_pair_tile(PairParams p) {
                 const int4 a = s_aux[j];
                 const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
                 const float r2 = dx * dx + dy * dy + dz * dz;
+                const unsigned grp = __match_any_sync(0xffffffffu, valid ? i : (0x10000 | lane));
+                const int first = __ffs(grp) - 1, last = 31 - __clz(grp);
+                float fx = 0.f, fy = 0.f, fz = 0.f;
                 if (p.use_lj && valid && r2 <= rc2 && s_haux[i].x != a.y) {
                     const float inv = rcp_approx(r2);
                     const float sg = pi.w + pj.w;
@@ -140,38 +147,43 @@ __global__ void __launch_bounds__(kTileThreads) k_pair_tile(PairParams p) {
                     const float ee = __int_as_float(s_haux[i].y) * __int_as_float(a.w);
                     const float ljd = 24.0f * ee * (2.0f * lj6 * lj6 - lj6);
                     const float fac = ljd * inv;
-                    atomicAdd(&s_f[3 * i], dx * fac);
-                    atomicAdd(&s_f[3 * i + 1], dy * fac);
-                    atomicAdd(&s_f[3 * i + 2], dz * fac);
+                    fx = dx * fac; fy = dy * fac; fz = dz * fac;
                     if (MEASURE) {
-                        const double wt = (p.virial_compat && (a.z & 32)) ? 1.0 : 0.5;
-                        const double gx = (double)dx * fac, gy = (double)dy * fac, gz = (double)dz * fac;
-                        a_u += 0.5 * (double)(4.0f * ee * (lj6 * lj6 - lj6));
-                        a_pairs += 0.5;
-                        a_w[0] += wt * (dx * gx);
-                        a_w[1] += wt * 0.5 * (dx * gy + dy * gx);
-                        a_w[2] += wt * (dy * gy);
-                        a_w[3] += wt * 0.5 * (dx * gz + dz * gx);
-                        a_w[4] += wt * 0.5 * (dy * gz + dz * gy);
-                        a_w[5] += wt * (dz * gz);
+                        const float wt = (p.virial_compat && (a.z & 32)) ? 1.0f : 0.5f;
+                        m_u += 2.0f * ee * (lj6 * lj6 - lj6);       // half of 4 eps (s12 - s6) per visit
+                        m_pairs += 0.5f;
+                        m_w[0] += wt * dx * fx;
+                        m_w[1] += wt * 0.5f * (dx * fy + dy * fx);
+                        m_w[2] += wt * dy * fy;
+                        m_w[3] += wt * 0.5f * (dx * fz + dz * fx);
+                        m_w[4] += wt * 0.5f * (dy * fz + dz * fy);
+                        m_w[5] += wt * dz * fz;
                     }
                 }
-                if (EMIT) {
-                    const bool emit = valid && r2 <= rc3sq;
-                    const unsigned grp = __match_any_sync(0xffffffffu, valid ? i : (0x10000 | lane));
-                    const unsigned em = __ballot_sync(0xffffffffu, emit) & grp;
-                    int base = 0;
-                    if (emit) base = s_cnt[i];
-                    __syncwarp();
-                    if (valid && lane == __ffs(grp) - 1) s_cnt[i] += __popc(em);
-                    if (emit) {
-                        const int c = base + __popc(em & lanemask_lt());
-                        const int slot_i = hs + hb + i;
-                        if (c < p.nl_cap)
-                            nl[(size_t)slot_i * p.nl_cap + c] = make_float4(dx, dy, dz, __int_as_float(a.z | (a.x << 6)));
-                    }
-                    __syncwarp();
+                for (int o = 1; o < 32; o <<= 1) {
+                    const float yx = __shfl_down_sync(0xffffffffu, fx, o);
+                    const float yy = __shfl_down_sync(0xffffffffu, fy, o);
+                    const float yz = __shfl_down_sync(0xffffffffu, fz, o);
+                    if (lane + o <= last) { fx += yx; fy += yy; fz += yz; }
                 }
+                const bool emit = EMIT && valid && r2 <= rc3sq;
+                const unsigned em = __ballot_sync(0xffffffffu, emit) & grp;
+                int base = 0;
+                if (EMIT && valid && lane == first) base = s_cnt[i];
+                base = __shfl_sync(0xffffffffu, base, first);
+                if (valid && lane == first) {
+                    s_f[3 * i] += fx;
+                    s_f[3 * i + 1] += fy;
+                    s_f[3 * i + 2] += fz;
+                    if (EMIT) s_cnt[i] = base + __popc(em);
+                }
+                if (emit) {
+                    const int c = base + __popc(em & lanemask_lt());
+                    const int slot_i = hs + hb + i;
+                    if (c < p.nl_cap)
+                        nl[(size_t)slot_i * p.nl_cap + c] = make_float4(dx, dy, dz, __int_as_float(a.z | (a.x << 6)));
+                }
+                __syncwarp();
             };
 
             int qn = 0;
@@ -224,7 +236,7 @@ __global__ void __launch_bounds__(kTileThreads) k_pair_tile(PairParams p) {
         __syncthreads();
     }
     if (MEASURE) {
-        double vals[8] = {a_u, a_w[0], a_w[1], a_w[2], a_w[3], a_w[4], a_w[5], a_pairs};
+        double vals[8] = {m_u, m_w[0], m_w[1], m_w[2], m_w[3], m_w[4], m_w[5], m_pairs};
         for (int k = 0; k < 8; k++) {
             double x = vals[k];
             for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
