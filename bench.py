@@ -300,8 +300,8 @@ def run_ours(args, w, name):
         t_launch = atm_ms / atm_launches / 1e3
         achieved = FLOP_PER_TRIPLET * triplets / t_launch / 1e12
         peak = fp32_simt_peak_tflops(torch)
-        traffic = committed_traffic("k_atm", name)
-        roof = {"bound": "fp32", "kernel": "k_atm (ATM triplets, FULL)", "achieved": achieved, "peak": peak,
+        traffic = committed_traffic("k_atm_q", name)
+        roof = {"bound": "fp32", "kernel": "k_atm_q (ATM triplets, FULL)", "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                 "peak_source": "measured here: cuBLAS SGEMM 8192^3, TF32 off (FP32 SIMT pipe; not in MEASURED_PEAKS.json)",
                 "work": f"{FLOP_PER_TRIPLET:.0f} FLOP x {triplets} in-cutoff triplets per launch",
@@ -331,7 +331,7 @@ def run_ours(args, w, name):
             "gpu_launches": kernels * args.steps,
             "graph_ms_per_step": graph_ms / args.steps,
             "kernel_ms": {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()},
-            "roofline": roof, "peak_kind": peak_kind,
+            "roofline": roof, "peak_kind": peak_kind, "traffic_note": "traffic from the committed ncu capture (profiles/traffic.json), lattice state, per launch",
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * s.n * 24, "d2h_bytes_per_step": 3 * s.n * 24},
             "clocks": clk.summary(),
             "energy": {"u_lj_per_atom": obs0["u_lj"] / s.n, "u_atm_per_atom": obs0["u_atm"] / s.n}}
