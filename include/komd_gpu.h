@@ -180,6 +180,29 @@ int  komd_gpu_profile(komd_gpu *h, int max_families, int64_t *launches, double *
 /* Number of kernels one komd_gpu_step launches per step (for accounting). */
 int  komd_gpu_kernels_per_step(komd_gpu *h);
 
+/* ---- allocation-free variant ------------------------------------------- */
+/* No counterpart in the reference.  ATM forces (FULL triplet set) of one
+ * small periodic system for callers that can pass device pointers but must
+ * not allocate device memory: for instance code embedded in a host
+ * application whose caching allocator has reserved the device, or a time-
+ * step loop that must not call cudaMalloc/cudaFree because both implicitly
+ * synchronise the device.  r (n*3 doubles) and f (n*3 doubles, overwritten)
+ * are device-accessible pointers; the neighbour list the kernels need lives
+ * in a fixed static device array inside the library (about 6.3 MB, held on
+ * every GPU that loads the library until the process exits), so this call
+ * allocates nothing.  Limits: n <= KOMD_NOALLOC_MAX_SITES and at most
+ * KOMD_NOALLOC_NL_CAP neighbours inside cutoff_3b per site (KOMD_ERR_ARG /
+ * KOMD_ERR_OVERFLOW otherwise); every box edge >= 2 * cutoff_3b.  The first
+ * call on a device resolves the array's device address (set-up) and should
+ * come before any stream capture on that device.  All calls share the one
+ * array: calls whose GPU work overlaps race and must be serialised by the
+ * caller.  Synchronous on cuda_stream (NULL = legacy default stream). */
+#define KOMD_NOALLOC_MAX_SITES 4096
+#define KOMD_NOALLOC_NL_CAP 96
+int  komd_gpu_atm_forces_noalloc(int64_t n, const double *r, double *f, const double domain_low[3],
+                                 const double domain_high[3], double cutoff_3b, double nu, int32_t atm_sign,
+                                 void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -72,6 +72,11 @@ enum Fam { F_CONTAINER = 0, F_PAIR, F_BONDED, F_LIMIT, F_ATM, F_INTEGRATE, F_MEA
 
 }  // namespace
 
+namespace komd {
+// lets other translation units of the library report through komd_gpu_last_error()
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+}  // namespace komd
+
 struct komd_gpu {
     Engine e;
     double *f_scratch = nullptr;

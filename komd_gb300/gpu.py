@@ -31,7 +31,7 @@ EXPORTS = [
     "komd_gpu_download", "komd_gpu_num_sites", "komd_gpu_update_container", "komd_gpu_forces",
     "komd_gpu_integrate0", "komd_gpu_integrate1", "komd_gpu_step", "komd_gpu_step_host", "komd_gpu_measure",
     "komd_gpu_rdf_bins", "komd_gpu_get_cells", "komd_gpu_neighbour_counts", "komd_gpu_set_profiling",
-    "komd_gpu_profile", "komd_gpu_kernels_per_step",
+    "komd_gpu_profile", "komd_gpu_kernels_per_step", "komd_gpu_atm_forces_noalloc",
 ]
 
 
@@ -101,6 +101,7 @@ def load() -> C.CDLL:
     L.komd_gpu_set_profiling.argtypes = [P, I32]
     L.komd_gpu_profile.argtypes = [P, I32, P, P, C.c_char_p, I32]
     L.komd_gpu_kernels_per_step.argtypes = [P]
+    L.komd_gpu_atm_forces_noalloc.argtypes = [I64, P, P, P, P, C.c_double, C.c_double, C.c_int32, P]
     _lib = L
     return L
 
