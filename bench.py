@@ -3,9 +3,10 @@
 Workload (default): LJ + Axilrod-Teller-Muto argon, 256,000 atoms on an FCC
 lattice (40^3 unit cells) at rho* = 0.8442, T* = 0.722 (seeded Maxwell-
 Boltzmann, zero momentum), LJ cutoff 2.5, ATM cutoff 2.0, nu* = 0.073, cell
-edge 2.5 (26^3 cells), dt* = 0.005.  One step = one full velocity-Verlet MD
-step: integrate0, COM/wrap/counting-sort binning, LJ pair kernel (which also
-writes the ATM neighbour list), ATM triplet kernel, integrate1.  Forces are
+edge >= 2.8 (23^3 cells), Verlet skin 0.3, dt* = 0.005.  One step = one full
+velocity-Verlet MD step: integrate0 (with the skin test), COM/wrap, binning
+and neighbour-list build when the skin test fired, LJ from the list (which
+also writes the ATM neighbour list), ATM triplet kernel, integrate1.  Forces are
 FP32 arithmetic, integration and reductions FP64, the ATM term is the FULL
 triplet set with F = -grad V (the physical form).
 
@@ -35,9 +36,12 @@ UNIT = "atom-steps/s"
 
 WORKLOADS = {
     # name: (fcc cells, rho, T*, cell size, rc_lj, rc_atm, nu*, dt)
-    "lj_atm_argon_256k": dict(ncell=40, rho=0.8442, t=0.722, cell=2.5, rc=2.5, rc3=2.0, nu=0.073, dt=0.005, atm=True),
-    "lj_atm_argon_32k": dict(ncell=20, rho=0.8442, t=0.722, cell=2.5, rc=2.5, rc3=2.0, nu=0.073, dt=0.005, atm=True),
-    "lj_argon_4k": dict(ncell=10, rho=0.8442, t=0.722, cell=2.5, rc=2.5, rc3=2.5, nu=0.0, dt=0.005, atm=False),
+    "lj_atm_argon_256k": dict(ncell=40, rho=0.8442, t=0.722, cell=2.8, rc=2.5, rc3=2.0, nu=0.073, dt=0.005, atm=True,
+                              skin=0.3),
+    "lj_atm_argon_32k": dict(ncell=20, rho=0.8442, t=0.722, cell=2.8, rc=2.5, rc3=2.0, nu=0.073, dt=0.005, atm=True,
+                             skin=0.3),
+    "lj_argon_4k": dict(ncell=10, rho=0.8442, t=0.722, cell=2.8, rc=2.5, rc3=2.5, nu=0.0, dt=0.005, atm=False,
+                        skin=0.3),
 }
 # algorithmic work per unit (frozen constants): the exact ATM
 # term costs 200 FLOP per in-cutoff triplet in the reference's formulation
@@ -213,7 +217,7 @@ def run_ours(args, w, name):
     terms = gpu.TERM_LJ | (gpu.TERM_ATM if w["atm"] else 0)
     cfg = gpu.make_config(s.low, s.high, w["cell"], cutoff=w["rc"], cutoff_3b=w["rc3"], nu=w["nu"], dt=w["dt"],
                           terms=terms, precision=gpu.FP32, atm_sign=gpu.ATM_SIGN_PHYSICAL,
-                          atm_enum=gpu.ATM_ENUM_FULL, virial_mode=gpu.VIRIAL_CORRECT)
+                          atm_enum=gpu.ATM_ENUM_FULL, virial_mode=gpu.VIRIAL_CORRECT, skin=w["skin"])
     g = gpu.GpuSystem(s, cfg, device=local)
     # the engine runs on a torch-created stream so that torch's CUDA events
     # time exactly the engine's launches (the legacy default stream would not
@@ -325,6 +329,7 @@ def run_ours(args, w, name):
             "config": {"workload": name, "form": "exact FP32 (LJ + FULL ATM, F = -grad V)", "sites": s.n,
                        "equilibration_steps": args.equil, "temperature_K_at_timing": obs0["temperature"],
                        "rc_lj": w["rc"], "rc_atm": w["rc3"], "nu_star": w["nu"], "cell": w["cell"], "dt": w["dt"],
+                       "verlet_skin": w["skin"],
                        "triplets_per_step": triplets, "parallelism": f"replicas x{world}",
                        "l2": "no flush: the per-step working set exceeds L2 (the ATM neighbour list alone, "
                              "16 B x capacity per site, is written and re-read every step)"},

@@ -84,7 +84,11 @@ typedef struct komd_config {
     int32_t virial_mode;       /* KOMD_VIRIAL_*                                      */
     int32_t atm_direct;        /* 1: ATM_NOLIST semantics (no ATM virial in COMPAT)  */
     int32_t lj_bins;           /* sensor_lj_bins                                     */
-    int32_t atm_list_cap;      /* per-site neighbour capacity inside cutoff_3b (0 = 64) */
+    int32_t atm_list_cap;      /* per-site neighbour capacity inside cutoff_3b (0 = from density) */
+    double skin;               /* Verlet skin: > 0 keeps a neighbour list inside cutoff + skin and
+                                  rebuilds cells and list only when a site has moved more than
+                                  skin/2 (FP32, no FENE, FULL ATM, CORRECT virial); 0 rebuilds
+                                  every step like LinkedCells::updateContainer */
 } komd_config;
 
 typedef struct komd_observables {

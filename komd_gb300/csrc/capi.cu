@@ -232,6 +232,36 @@ int ensure_posd(komd_gpu *h) {
     return KOMD_OK;
 }
 
+int alloc_verlet(komd_gpu *h, int cap) {
+    Engine &e = h->e;
+    e.vl_cap = cap;
+    CK(dalloc(e.img, e.n));
+    CK(dalloc(e.ref, 3 * (size_t)e.n));
+    CK(dalloc(e.slot_cell, e.n));
+    CK(dalloc(e.vl, (size_t)cap * (size_t)e.n));
+    CK(dalloc(e.vl_count, e.n));
+    CK(cudaMemset(e.img, 0, sizeof(char4) * e.n));
+    if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+    e.graph_valid = false;
+    return KOMD_OK;
+}
+
+// forces a rebuild of cells (and, on the Verlet path, of the list) now
+void launch_rebuild(komd_gpu *h) {
+    Engine &e = h->e;
+    if (e.verlet) cudaMemsetAsync(e.rebuild, 0x01, sizeof(int), e.stream);
+    launch_container(e, e.stream);
+    if (e.verlet) cudaMemsetAsync(e.rebuild, 0, sizeof(int), e.stream);
+}
+
+// The Verlet path keeps a neighbour list across steps; it is used only where
+// the results do not depend on the cells of the current step: FP32 forces,
+// no FENE (same-cell semantics), the FULL triplet set and the CORRECT virial.
+bool uses_verlet(const komd_config &c) {
+    return c.skin > 0 && c.precision == KOMD_FP32 && !(c.terms & KOMD_TERM_FENE) &&
+           (!(c.terms & KOMD_TERM_ATM) || c.atm_enum == KOMD_ATM_ENUM_FULL) && c.virial_mode == KOMD_VIRIAL_CORRECT;
+}
+
 int validate(const komd_config *c, Grid &g) {
     if (!c) return fail(KOMD_ERR_ARG, "null config");
     if (!(c->cell_size > 0)) return fail(KOMD_ERR_ARG, "cell_size must be > 0");
@@ -243,6 +273,12 @@ int validate(const komd_config *c, Grid &g) {
         return fail(KOMD_ERR_ARG, "cutoff_3b must be > 0 and <= cell_size");
     if (!(c->delta_t > 0)) return fail(KOMD_ERR_ARG, "delta_t must be > 0");
     if (c->precision != KOMD_FP32 && c->precision != KOMD_FP64) return fail(KOMD_ERR_ARG, "bad precision");
+    if (c->skin < 0) return fail(KOMD_ERR_ARG, "skin must be >= 0");
+    if (uses_verlet(*c)) {
+        const double rl = std::max(lj ? c->cutoff : 0.0, atm ? c->cutoff_3b : 0.0) + c->skin;
+        if (c->cell_size < rl)
+            return fail(KOMD_ERR_ARG, "with a Verlet skin the cell size must be >= cutoff + skin");
+    }
     g.cs = c->cell_size;
     g.ncell = 1;
     for (int d = 0; d < 3; d++) {
@@ -315,6 +351,35 @@ int komd_gpu_create(const komd_config *cfg, int device, komd_gpu **out) {
             return fail(KOMD_ERR_NOMEM, "offset table");
         }
     }
+    e.verlet = uses_verlet(e.cfg);
+    if (e.verlet) {
+        // per cell and neighbour: home-relative centre offset (FP64 -> FP32), w = periodic image
+        std::vector<float4> nb((size_t)g.ncell * 27);
+        for (int c = 0; c < g.ncell; c++) {
+            int cx, cy, cz;
+            cell_coords(g, c, cx, cy, cz);
+            const int cc[3] = {cx, cy, cz};
+            for (int k = 0; k < 27; k++) {
+                const int dd[3] = {k % 3 - 1, (k / 3) % 3 - 1, k / 9 - 1};
+                double o[3];
+                bool img = false;
+                for (int d = 0; d < 3; d++) {
+                    int q = cc[d] + dd[d];
+                    double shift = 0.0;
+                    if (q < 0) { q += g.nd[d]; shift = -g.L[d]; img = true; }
+                    else if (q >= g.nd[d]) { q -= g.nd[d]; shift = g.L[d]; img = true; }
+                    o[d] = (cell_centre(g, d, q) + shift) - cell_centre(g, d, cc[d]);
+                }
+                nb[(size_t)c * 27 + k] = make_float4((float)o[0], (float)o[1], (float)o[2], img ? 1.f : 0.f);
+            }
+        }
+        if (dalloc(e.nboff, nb.size()) || dalloc(e.rebuild, 1) ||
+            cudaMemcpy(e.nboff, nb.data(), sizeof(float4) * nb.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemset(e.rebuild, 0, sizeof(int)) != cudaSuccess) {
+            komd_gpu_destroy(h);
+            return fail(KOMD_ERR_NOMEM, "Verlet tables");
+        }
+    }
     h->want_posd = e.cfg.precision == KOMD_FP64;
     *out = h;
     return KOMD_OK;
@@ -333,6 +398,7 @@ int komd_gpu_destroy(komd_gpu *h) {
     dfree(e.slot_site); dfree(e.skey); dfree(e.pos4); dfree(e.seps); dfree(e.posd); dfree(e.seps_d); dfree(e.sig_d);
     dfree(e.nl); dfree(e.nl_count); dfree(e.bonds); dfree(e.angles); dfree(e.partials); dfree(e.err);
     dfree(e.rdf); dfree(e.lj_hist); dfree(e.counts); dfree(h->f_scratch); dfree(h->acc); dfree(e.offtab);
+    dfree(e.nboff); dfree(e.rebuild); dfree(e.img); dfree(e.ref); dfree(e.slot_cell); dfree(e.vl); dfree(e.vl_count);
     for (auto &p : h->pending) { h->pool.push_back(p.second.first); h->pool.push_back(p.second.second); }
     for (auto ev : h->pool) cudaEventDestroy(ev);
     if (e.own_stream && e.stream) cudaStreamDestroy(e.stream);
@@ -419,6 +485,15 @@ int komd_gpu_upload_sites(komd_gpu *h, int64_t n, const double *r, const double 
     }
     int rc = alloc_atm_list(h, cap);
     if (rc) return rc;
+    if (e.verlet) {
+        if (n > kMaxVerletSlot) return fail(KOMD_ERR_ARG, "the Verlet path supports at most 2^26 - 1 sites");
+        const double vol = e.g.L[0] * e.g.L[1] * e.g.L[2];
+        const bool lj = (e.cfg.terms & KOMD_TERM_LJ) != 0, atm = (e.cfg.terms & KOMD_TERM_ATM) != 0;
+        const double rl = std::max(lj ? e.cfg.cutoff : 0.0, atm ? e.cfg.cutoff_3b : 0.0) + e.cfg.skin;
+        const double mean = (double)n / vol * 4.18879 * rl * rl * rl;
+        rc = alloc_verlet(h, std::max(64, std::min(2048, ((int)std::ceil(1.5 * mean + 32) + 31) / 32 * 32)));
+        if (rc) return rc;
+    }
     rc = ensure_partials(h);
     if (rc) return rc;
     e.have_sites = true;
@@ -475,14 +550,23 @@ int komd_gpu_download(komd_gpu *h, double *r, double *v, double *f) {
 int komd_gpu_update_container(komd_gpu *h) {
     if (!h || !h->e.have_sites) return fail(KOMD_ERR_STATE, "no sites uploaded");
     Engine &e = h->e;
-    {
-        ProfScope ps(h, F_CONTAINER);
-        launch_container(e, e.stream);
+    for (int attempt = 0; attempt < 6; attempt++) {
+        {
+            ProfScope ps(h, F_CONTAINER);
+            launch_rebuild(h);
+        }
+        CK(cudaMemsetAsync(e.f, 0, sizeof(double) * 3 * e.n, e.stream));   // FReset_Kernel
+        int rc = check_launch("update_container");
+        if (rc) return rc;
+        int flags[E_NFLAGS];
+        rc = read_flags(h, flags, false);
+        if (rc) return rc;
+        if (!flags[E_VL_OVERFLOW]) break;
+        CK(cudaMemsetAsync(e.err, 0, sizeof(int) * E_NFLAGS, e.stream));
+        if (e.vl_cap >= 2048) return fail(KOMD_ERR_OVERFLOW, "Verlet list exceeds 2048 entries per site");
+        rc = alloc_verlet(h, std::min(2048, e.vl_cap * 2));   // grow and rebuild
+        if (rc) return rc;
     }
-    CK(cudaMemsetAsync(e.f, 0, sizeof(double) * 3 * e.n, e.stream));   // FReset_Kernel
-    int rc = check_launch("update_container");
-    if (rc) return rc;
-    CK(cudaStreamSynchronize(e.stream));
     e.have_cells = true;
     e.have_forces = false;
     return KOMD_OK;
@@ -540,6 +624,8 @@ static int finish_steps(komd_gpu *h) {
     if (rc) return rc;
     if (flags[E_ATM_OVERFLOW])
         return fail(KOMD_ERR_OVERFLOW, "ATM neighbour list overflowed during the steps (raise atm_list_cap)");
+    if (flags[E_VL_OVERFLOW])
+        return fail(KOMD_ERR_OVERFLOW, "Verlet list overflowed during the steps (density rose; call update_container)");
     if (flags[E_NONFINITE]) return fail(KOMD_ERR_NONFINITE, "non-finite velocity after a step");
     return KOMD_OK;
 }
@@ -606,6 +692,7 @@ int komd_gpu_measure(komd_gpu *h, uint32_t mask, komd_observables *obs, double *
     launch_kinetic(e, st, n_terms);
     launch_sum_partials(st, kinetic_grid(e), e.partials, h->acc);
     if ((mask & KOMD_MEASURE_RDF) && e.rdf_bins > 0) {
+        if (e.verlet) launch_rebuild(h);   // the cells of the last rebuild may be stale
         CK(cudaMemsetAsync(e.rdf, 0, sizeof(double) * e.rdf_bins, st));
         double minw = 1e300;
         for (int d = 0; d < 3; d++) minw = std::min(minw, e.cfg.cell_size);
@@ -677,8 +764,8 @@ int komd_gpu_neighbour_counts(komd_gpu *h, int64_t *counts) {
         h->want_posd = true;
         int rc = ensure_posd(h);
         if (rc) return rc;
-        launch_container(e, e.stream);   // idempotent: positions are already wrapped
     }
+    launch_rebuild(h);   // cells and FP64 positions of the current state (positions are already wrapped)
     launch_counts(e, e.stream);
     int rc = check_launch("neighbour_counts");
     if (rc) return rc;
@@ -716,6 +803,7 @@ int komd_gpu_kernels_per_step(komd_gpu *h) {
     if (!h) return -1;
     const Engine &e = h->e;
     int k = 2 /* integrate */ + 4 /* com/wrap/bin, scan, scatter, cell sort */ + 1 /* pair */;
+    if (e.verlet) k += 2;   /* refresh, list build (each exits at once when its step does not need it) */
     if ((e.cfg.terms & KOMD_TERM_BONDED) && e.n_bonds > 0) k++;
     if ((e.cfg.terms & KOMD_TERM_BONDED) && e.n_angles > 0) k++;
     if (e.cfg.terms & KOMD_TERM_LIMIT) k++;

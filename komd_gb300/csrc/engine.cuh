@@ -44,7 +44,7 @@ enum RedSlot {
 };
 
 // device error flags
-enum ErrFlag { E_ATM_OVERFLOW = 0, E_NONFINITE = 1, E_NFLAGS = 4 };
+enum ErrFlag { E_ATM_OVERFLOW = 0, E_NONFINITE = 1, E_VL_OVERFLOW = 2, E_NFLAGS = 4 };
 
 // ---------------------------------------------------------------------------
 // exact FP64 helpers: the reference is built without FMA contraction, so the
@@ -129,6 +129,14 @@ struct PairParams {
     int use_lj;
     int virial_compat;
     const float *offtab;       // per dimension nd*3 FP32 offsets centre(k+d) + shift - centre(k)
+    // Verlet path
+    const int *rebuild;
+    unsigned *vl;
+    int *vl_count;
+    int vl_cap;
+    double rl2;                // (cutoff + skin)^2
+    const int *slot_cell;
+    const float4 *nboff;
 };
 
 struct AtmParams {
@@ -191,6 +199,18 @@ struct Engine {
     bool graph_valid = false;
     // profiling
     bool profiling = false;
+    // Verlet list of the physics path (FP32, no FENE, FULL ATM, CORRECT virial, skin > 0)
+    bool verlet = false;
+    int *rebuild = nullptr;      // device flag: rebuild cells and list in this step
+    char4 *img = nullptr;        // per site: periodic wraps since the last rebuild
+    double *ref = nullptr;       // per site: position at the last rebuild (3 doubles)
+    int *slot_cell = nullptr;    // per slot: its cell at the last rebuild
+    float4 *nboff = nullptr;     // per cell x 27: home-relative neighbour-cell offset, w = 1 for an image
+    unsigned *vl = nullptr;      // vl_cap entries per slot: same-molecule bit 31 | nb << 26 | slot
+    int *vl_count = nullptr;
+    int vl_cap = 0;
 };
+
+constexpr int kMaxVerletSlot = (1 << 26) - 1;
 
 }  // namespace komd

@@ -5,6 +5,7 @@
 // [limit] -> [ATM triplets] -> integrate1.
 //
 // Citations are to Snapex2409/KoMD, src/.
+#include <algorithm>
 #include <cfloat>
 #include <climits>
 
@@ -19,7 +20,8 @@ namespace komd {
 // ===========================================================================
 __global__ void k_com_wrap_bin(Grid g, int n_mol, const int *__restrict__ mol_off, double *__restrict__ r,
                                const double *__restrict__ m, double *__restrict__ com, int *__restrict__ mol_cell,
-                               int *__restrict__ mol_rank, int *__restrict__ cell_count, int *__restrict__ cell_mcount) {
+                               int *__restrict__ mol_rank, int *__restrict__ cell_count, int *__restrict__ cell_mcount,
+                               char4 *__restrict__ img, const int *__restrict__ rebuild) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n_mol) return;
     const int s0 = mol_off[k], s1 = mol_off[k + 1];
@@ -49,9 +51,19 @@ __global__ void k_com_wrap_bin(Grid g, int n_mol, const int *__restrict__ mol_of
                 r[3 * s + d] = x;
                 c2[d] = dadd(c2[d], dmul(x, ms));
             }
+            if (img) {
+                // continuous position r - img * L is unchanged by the wrap
+                char4 q = img[s];
+                q.x += (off[0] > 0.0) - (off[0] < 0.0);
+                q.y += (off[1] > 0.0) - (off[1] < 0.0);
+                q.z += (off[2] > 0.0) - (off[2] < 0.0);
+                img[s] = q;
+            }
         }
         for (int d = 0; d < 3; d++) c[d] = ddiv(c2[d], tm);
     }
+    for (int d = 0; d < 3; d++) com[3 * k + d] = c[d];
+    if (rebuild && !*rebuild) return;   // no rebuild in this step: cells stay as built
     // writeIndices: (int64)((com - low) / cs) clamped to [0, nd-1]
     int b[3];
     for (int d = 0; d < 3; d++) {
@@ -60,7 +72,6 @@ __global__ void k_com_wrap_bin(Grid g, int n_mol, const int *__restrict__ mol_of
         if (q < 0) q = 0;
         if (q > g.nd[d] - 1) q = g.nd[d] - 1;
         b[d] = (int)q;
-        com[3 * k + d] = c[d];
     }
     const int cell = b[0] + g.nd[0] * (b[1] + g.nd[1] * b[2]);
     mol_cell[k] = cell;
@@ -71,8 +82,10 @@ __global__ void k_com_wrap_bin(Grid g, int n_mol, const int *__restrict__ mol_of
 // exclusive scan of two count arrays of length nc (one block of 1024 threads,
 // each owning a contiguous chunk)
 __global__ void __launch_bounds__(1024) k_scan2(int nc, const int *__restrict__ a, int *__restrict__ sa,
-                                                const int *__restrict__ b, int *__restrict__ sb) {
+                                                const int *__restrict__ b, int *__restrict__ sb,
+                                                const int *__restrict__ rebuild) {
     __shared__ int wa[32], wb[32];
+    if (rebuild && !*rebuild) return;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     const int per = (nc + 1023) / 1024;
     const int lo = min(t * per, nc), hi = min(lo + per, nc);
@@ -105,9 +118,10 @@ __global__ void __launch_bounds__(1024) k_scan2(int nc, const int *__restrict__ 
 }
 
 __global__ void k_scatter_mol(int n_mol, const int *__restrict__ mol_cell, const int *__restrict__ mol_rank,
-                              const int *__restrict__ cell_mstart, int *__restrict__ cell_mols) {
+                              const int *__restrict__ cell_mstart, int *__restrict__ cell_mols,
+                              const int *__restrict__ rebuild) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n_mol) return;
+    if (k >= n_mol || (rebuild && !*rebuild)) return;
     cell_mols[cell_mstart[mol_cell[k]] + mol_rank[k]] = k;
 }
 
@@ -123,10 +137,12 @@ __global__ void __launch_bounds__(kBlock) k_cell_sort(Grid g, const int *__restr
                                                       int *__restrict__ site_slot, float4 *__restrict__ pos4,
                                                       int *__restrict__ skey, float *__restrict__ seps,
                                                       double *__restrict__ posd, double *__restrict__ seps_d,
-                                                      double *__restrict__ sig_d) {
+                                                      double *__restrict__ sig_d, char4 *__restrict__ img,
+                                                      double *__restrict__ ref, int *__restrict__ slot_cell,
+                                                      const int *__restrict__ rebuild) {
     const int lane = threadIdx.x & 31;
     const int cell = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
-    if (cell >= g.ncell) return;
+    if (cell >= g.ncell || (rebuild && !*rebuild)) return;
     int cx, cy, cz;
     cell_coords(g, cell, cx, cy, cz);
     const double cen[3] = {cell_centre(g, 0, cx), cell_centre(g, 1, cy), cell_centre(g, 2, cz)};
@@ -151,6 +167,11 @@ __global__ void __launch_bounds__(kBlock) k_cell_sort(Grid g, const int *__restr
                                          __double2float_rn(z - cen[2]), __double2float_rn(0.5 * sig[s]));
                 skey[slot] = key[s];
                 seps[slot] = __double2float_rn(sqrt(eps[s]));
+                if (img) {
+                    img[s] = make_char4(0, 0, 0, 0);
+                    ref[3 * s] = x; ref[3 * s + 1] = y; ref[3 * s + 2] = z;
+                    slot_cell[slot] = cell;
+                }
                 if (posd) {
                     posd[3 * slot] = x; posd[3 * slot + 1] = y; posd[3 * slot + 2] = z;
                     seps_d[slot] = eps[s];
@@ -801,21 +822,35 @@ __global__ void k_limit(int n, const double *__restrict__ eps, const double *__r
 // ===========================================================================
 // velocity Verlet (Integrator.cpp:28-37), FP64 without contraction
 // ===========================================================================
+// With a Verlet list (ref != nullptr) it also flags a rebuild when a site's
+// continuous position r - img*L has moved more than skin/2 since the build.
 __global__ void k_step0(int n, double *__restrict__ r, double *__restrict__ v, const double *__restrict__ f,
-                        const double *__restrict__ m, double dt_half, double dt) {
+                        const double *__restrict__ m, double dt_half, double dt, Grid g,
+                        const char4 *__restrict__ img, const double *__restrict__ ref, float half_skin2,
+                        int *__restrict__ rebuild) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const double c = ddiv(dt_half, m[s]);
+    double x[3];
     for (int d = 0; d < 3; d++) {
         const double vv = dadd(v[3 * s + d], dmul(f[3 * s + d], c));
         v[3 * s + d] = vv;
-        r[3 * s + d] = dadd(r[3 * s + d], dmul(vv, dt));
+        x[d] = dadd(r[3 * s + d], dmul(vv, dt));
+        r[3 * s + d] = x[d];
+    }
+    if (ref) {
+        const char4 q = img[s];
+        const float dx = (float)(x[0] - ref[3 * s]) - (float)q.x * (float)g.L[0];
+        const float dy = (float)(x[1] - ref[3 * s + 1]) - (float)q.y * (float)g.L[1];
+        const float dz = (float)(x[2] - ref[3 * s + 2]) - (float)q.z * (float)g.L[2];
+        if (dx * dx + dy * dy + dz * dz > half_skin2) *rebuild = 1;
     }
 }
 
 __global__ void k_step1(int n, double *__restrict__ v, const double *__restrict__ f, const double *__restrict__ m,
-                        double dt_half, int *err) {
+                        double dt_half, int *err, int *rebuild) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (rebuild && s == 0) *rebuild = 0;   // every consumer of this step's flag has run
     if (s >= n) return;
     const double c = ddiv(dt_half, m[s]);
     bool bad = false;
@@ -825,6 +860,24 @@ __global__ void k_step1(int n, double *__restrict__ v, const double *__restrict_
         bad |= !isfinite(vv);
     }
     if (bad) atomicOr(&err[E_NONFINITE], 1);
+}
+
+// Verlet path, steps without rebuild: cell-local FP32 coordinates of the
+// continuous positions r - img*L relative to each slot's build cell.
+__global__ void k_refresh(Grid g, int n, const int *__restrict__ slot_site, const int *__restrict__ slot_cell,
+                          const double *__restrict__ r, const char4 *__restrict__ img, float4 *__restrict__ pos4,
+                          const int *__restrict__ rebuild) {
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= n || *rebuild) return;
+    const int s = slot_site[slot];
+    int cx, cy, cz;
+    cell_coords(g, slot_cell[slot], cx, cy, cz);
+    const char4 q = img[s];
+    float4 p = pos4[slot];
+    p.x = (float)((r[3 * s] - (double)q.x * g.L[0]) - cell_centre(g, 0, cx));
+    p.y = (float)((r[3 * s + 1] - (double)q.y * g.L[1]) - cell_centre(g, 1, cy));
+    p.z = (float)((r[3 * s + 2] - (double)q.z * g.L[2]) - cell_centre(g, 2, cz));
+    pos4[slot] = p;
 }
 
 // ===========================================================================
@@ -928,20 +981,26 @@ static inline int nblk(long long n, int b) { return (int)((n + b - 1) / b); }
 
 void launch_container(Engine &e, cudaStream_t st) {
     const Grid &g = e.g;
+    const int *rb = e.verlet ? e.rebuild : nullptr;   // nullptr: rebuild unconditionally
     cudaMemsetAsync(e.cell_count, 0, sizeof(int) * g.ncell, st);
     cudaMemsetAsync(e.cell_mcount, 0, sizeof(int) * g.ncell, st);
     k_com_wrap_bin<<<nblk(e.n_mol, 256), 256, 0, st>>>(g, (int)e.n_mol, e.mol_off, e.r, e.m, e.com, e.mol_cell,
-                                                         e.mol_rank, e.cell_count, e.cell_mcount);
-    k_scan2<<<1, 1024, 0, st>>>(g.ncell, e.cell_count, e.cell_start, e.cell_mcount, e.cell_mstart);
+                                                         e.mol_rank, e.cell_count, e.cell_mcount,
+                                                         e.verlet ? e.img : nullptr, rb);
+    k_scan2<<<1, 1024, 0, st>>>(g.ncell, e.cell_count, e.cell_start, e.cell_mcount, e.cell_mstart, rb);
     k_scatter_mol<<<nblk(e.n_mol, 256), 256, 0, st>>>((int)e.n_mol, e.mol_cell, e.mol_rank, e.cell_mstart,
-                                                        e.cell_mols);
-    const bool fp64 = e.cfg.precision == KOMD_FP64 || e.posd != nullptr;
+                                                        e.cell_mols, rb);
     k_cell_sort<<<nblk(g.ncell, kWarpsPerBlock), kBlock, 0, st>>>(
         g, e.mol_off, e.cell_mstart, e.cell_start, e.cell_mols, e.r, e.eps, e.sig, e.key, e.slot_site, e.site_slot,
-        e.pos4, e.skey, e.seps, fp64 ? e.posd : nullptr, e.seps_d, e.sig_d);
+        e.pos4, e.skey, e.seps, e.posd, e.seps_d, e.sig_d, e.verlet ? e.img : nullptr, e.verlet ? e.ref : nullptr,
+        e.verlet ? e.slot_cell : nullptr, rb);
+    if (e.verlet) {
+        k_refresh<<<nblk(e.n, 256), 256, 0, st>>>(g, (int)e.n, e.slot_site, e.slot_cell, e.r, e.img, e.pos4, e.rebuild);
+        launch_vlist_build(e, st);
+    }
 }
 
-static PairParams pair_params(Engine &e) {
+PairParams pair_params(Engine &e) {
     PairParams p;
     p.g = e.g;
     p.cell_start = e.cell_start;
@@ -973,6 +1032,14 @@ static PairParams pair_params(Engine &e) {
     p.use_lj = lj ? 1 : 0;
     p.virial_compat = e.cfg.virial_mode == KOMD_VIRIAL_COMPAT;
     p.offtab = e.offtab;
+    p.rebuild = e.rebuild;
+    p.vl = e.vl;
+    p.vl_count = e.vl_count;
+    p.vl_cap = e.vl_cap;
+    const double rl = std::max(lj ? e.cfg.cutoff : 0.0, atm ? e.cfg.cutoff_3b : 0.0) + e.cfg.skin;
+    p.rl2 = rl * rl;
+    p.slot_cell = e.slot_cell;
+    p.nboff = e.nboff;
     return p;
 }
 
@@ -1006,6 +1073,7 @@ int launch_pair(Engine &e, cudaStream_t st, bool measure, double *lj_hist) {
     p.lj_hist = lj_hist;
     const bool emit = (e.cfg.terms & KOMD_TERM_ATM) != 0;
     const bool fene = (e.cfg.terms & KOMD_TERM_FENE) != 0;
+    if (e.verlet && !lj_hist) return launch_lj_vlist(e, p, measure, emit, st);
     if (e.cfg.precision == KOMD_FP32 && !fene && !lj_hist) {
         launch_pair_tile(p, e.g.ncell, measure, emit, st);
         return e.g.ncell;
@@ -1084,11 +1152,15 @@ void launch_atm(Engine &e, cudaStream_t st, bool measure) {
 }
 
 void launch_step0(Engine &e, cudaStream_t st) {
-    k_step0<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.r, e.v, e.f, e.m, e.cfg.delta_t * 0.5, e.cfg.delta_t);
+    const float hs = (float)(0.5 * e.cfg.skin);
+    k_step0<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.r, e.v, e.f, e.m, e.cfg.delta_t * 0.5, e.cfg.delta_t, e.g,
+                                              e.verlet ? e.img : nullptr, e.verlet ? e.ref : nullptr, hs * hs,
+                                              e.rebuild);
 }
 
 void launch_step1(Engine &e, cudaStream_t st) {
-    k_step1<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.v, e.f, e.m, e.cfg.delta_t * 0.5, e.err);
+    k_step1<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.v, e.f, e.m, e.cfg.delta_t * 0.5, e.err,
+                                              e.verlet ? e.rebuild : nullptr);
 }
 
 int kinetic_grid(const Engine &e) { return nblk(e.n, kBlock); }

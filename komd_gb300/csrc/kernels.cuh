@@ -6,6 +6,10 @@ namespace komd {
 void launch_container(Engine &e, cudaStream_t st);
 int launch_pair(Engine &e, cudaStream_t st, bool measure, double *lj_hist);
 void launch_pair_tile(PairParams &p, int ncell, bool measure, bool emit, cudaStream_t st);
+PairParams pair_params(Engine &e);
+void launch_vlist_build(Engine &e, cudaStream_t st);
+int launch_lj_vlist(Engine &e, PairParams &p, bool measure, bool emit, cudaStream_t st);
+int vlist_grid(const Engine &e);
 void launch_counts(Engine &e, cudaStream_t st);
 void launch_bonded(Engine &e, cudaStream_t st, bool measure, double *acc);
 void launch_limit(Engine &e, cudaStream_t st);

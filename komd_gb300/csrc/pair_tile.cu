@@ -257,6 +257,244 @@ __global__ void __launch_bounds__(kTileThreads) k_pair_tile(PairParams p) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Verlet list build (rebuild steps only): the same staged neighbourhood, every
+// pair inside cutoff + skin appended to the home site's row in candidate
+// order (deterministic); bit 31 marks a same-molecule pair (no LJ).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kTileThreads) k_vlist_build(PairParams p) {
+    __shared__ float4 s_pos[kStage];
+    __shared__ int4 s_aux[kStage];
+    __shared__ float4 s_hpos[kHome];
+    __shared__ int s_hkey[kHome];
+    __shared__ int s_cnt[kHome];
+    __shared__ int s_nbs[27], s_nbn[27], s_nbpre[28];
+    __shared__ float s_nbo[27][3];
+    if (!*p.rebuild) return;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int cell = blockIdx.x;
+    int cx, cy, cz;
+    cell_coords(p.g, cell, cx, cy, cz);
+    if (tid < 27) {
+        int kx, ky, kz;
+        bool cr;
+        const int c = nb_cell(p.g, cx, cy, cz, tid, kx, ky, kz, cr);
+        const int s0 = p.cell_start[c];
+        s_nbs[tid] = s0;
+        s_nbn[tid] = p.cell_start[c + 1] - s0;
+        s_nbo[tid][0] = p.offtab[cx * 3 + tid % 3];
+        s_nbo[tid][1] = p.offtab[p.g.nd[0] * 3 + cy * 3 + (tid / 3) % 3];
+        s_nbo[tid][2] = p.offtab[(p.g.nd[0] + p.g.nd[1]) * 3 + cz * 3 + tid / 9];
+    }
+    __syncthreads();
+    if (tid == 0) {
+        int acc = 0;
+        for (int k = 0; k < 27; k++) { s_nbpre[k] = acc; acc += s_nbn[k]; }
+        s_nbpre[27] = acc;
+    }
+    __syncthreads();
+    const int Nn = s_nbpre[27];
+    const int hs = s_nbs[13], hn = s_nbn[13];
+    const float rl2 = (float)p.rl2;
+    unsigned lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+    for (int hb = 0; hb < hn; hb += kHome) {
+        const int hc = min(kHome, hn - hb);
+        for (int t = tid; t < hc; t += kTileThreads) {
+            s_hpos[t] = p.pos4[hs + hb + t];
+            s_hkey[t] = p.skey[hs + hb + t];
+            s_cnt[t] = 0;
+        }
+        const int self_base = s_nbpre[13] + hb;
+        for (int sb = 0; sb < Nn; sb += kStage) {
+            const int ns = min(kStage, Nn - sb);
+            __syncthreads();
+            for (int t = tid; t < ns; t += kTileThreads) {
+                const int gi = sb + t;
+                int lo = 0, hi = 27;
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (s_nbpre[mid] <= gi) lo = mid; else hi = mid;
+                }
+                const int nb = lo;
+                const int j = s_nbs[nb] + (gi - s_nbpre[nb]);
+                float4 q = p.pos4[j];
+                q.x += s_nbo[nb][0];
+                q.y += s_nbo[nb][1];
+                q.z += s_nbo[nb][2];
+                s_pos[t] = q;
+                s_aux[t] = make_int4(j, p.skey[j], nb, 0);
+            }
+            __syncthreads();
+            for (int i = w; i < hc; i += kTileWarps) {
+                const float4 pi = s_hpos[i];
+                const int ki = s_hkey[i];
+                const int self = self_base + i - sb;
+                const int slot_i = hs + hb + i;
+                int cnt = s_cnt[i];
+                for (int j0 = 0; j0 < ns; j0 += 32) {
+                    const int j = j0 + lane;
+                    bool hit = false;
+                    int4 a = make_int4(0, 0, 0, 0);
+                    if (j < ns && j != self) {
+                        const float4 pj = s_pos[j];
+                        const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                        hit = dx * dx + dy * dy + dz * dz <= rl2;
+                        a = s_aux[j];
+                    }
+                    const unsigned m = __ballot_sync(0xffffffffu, hit);
+                    if (hit) {
+                        const int pos = cnt + __popc(m & lt);
+                        if (pos < p.vl_cap)
+                            p.vl[(size_t)slot_i * p.vl_cap + pos] =
+                                (a.y == ki ? 0x80000000u : 0u) | ((unsigned)a.z << 26) | (unsigned)a.x;
+                    }
+                    cnt += __popc(m);
+                }
+                if (lane == 0) s_cnt[i] = cnt;
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+        for (int t = tid; t < hc; t += kTileThreads) {
+            const int c = s_cnt[t];
+            p.vl_count[hs + hb + t] = min(c, p.vl_cap);
+            if (c > p.vl_cap) atomicOr(&p.err[E_VL_OVERFLOW], 1);
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// LJ forces from the Verlet list (every step of the Verlet path): one warp
+// per site, one list entry per lane; the neighbour's position is its FP32
+// cell-local position plus the build-cell offset of the entry's neighbour
+// cell.  Inside cutoff_3b the pair is appended to the ATM list in list
+// order.  No atomics: the warp owns its site.
+// ---------------------------------------------------------------------------
+template <bool MEASURE, bool EMIT>
+__global__ void __launch_bounds__(256) k_lj_vlist(PairParams p, int n) {
+    __shared__ double s_part[8][8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int i = blockIdx.x * 8 + w;
+    const float rc2 = (float)p.rc2, rc3sq = (float)p.rc3sq;
+    unsigned lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+    float m_u = 0.f, m_pairs = 0.f, m_w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (i < n) {
+        const int cnt = p.vl_count[i];
+        const float4 pi = p.pos4[i];
+        const float sei = p.seps[i];
+        const float4 *off = p.nboff + (size_t)p.slot_cell[i] * 27;
+        const unsigned *row = p.vl + (size_t)i * p.vl_cap;
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+        int c_atm = 0;
+        for (int k0 = 0; k0 < cnt; k0 += 32) {
+            const int k = k0 + lane;
+            bool emit = false;
+            float dx = 0.f, dy = 0.f, dz = 0.f;
+            int code = 0;
+            if (k < cnt) {
+                const unsigned e = row[k];
+                const int j = (int)(e & 0x3ffffffu);
+                const int nb = (int)((e >> 26) & 31u);
+                const float4 o = off[nb];
+                const float4 pj = p.pos4[j];
+                dx = pi.x - (pj.x + o.x);
+                dy = pi.y - (pj.y + o.y);
+                dz = pi.z - (pj.z + o.z);
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                if (p.use_lj && r2 <= rc2 && !(e >> 31)) {
+                    const float inv = rcp_approx(r2);
+                    const float sg = pi.w + pj.w;
+                    const float x = sg * sg * inv;
+                    const float lj6 = x * x * x;
+                    const float ee = sei * p.seps[j];
+                    const float fac = 24.0f * ee * (2.0f * lj6 * lj6 - lj6) * inv;
+                    fx += dx * fac; fy += dy * fac; fz += dz * fac;
+                    if (MEASURE) {
+                        const float gx = dx * fac, gy = dy * fac, gz = dz * fac;
+                        m_u += 2.0f * ee * (lj6 * lj6 - lj6);
+                        m_pairs += 0.5f;
+                        m_w[0] += 0.5f * dx * gx;
+                        m_w[1] += 0.25f * (dx * gy + dy * gx);
+                        m_w[2] += 0.5f * dy * gy;
+                        m_w[3] += 0.25f * (dx * gz + dz * gx);
+                        m_w[4] += 0.25f * (dy * gz + dz * gy);
+                        m_w[5] += 0.5f * dz * gz;
+                    }
+                }
+                emit = EMIT && r2 <= rc3sq;
+                code = nb | (o.w != 0.f ? 32 : 0) | (j << 6);
+            }
+            if (EMIT) {
+                const unsigned m = __ballot_sync(0xffffffffu, emit);
+                if (emit) {
+                    const int pos = c_atm + __popc(m & lt);
+                    if (pos < p.nl_cap) p.nl[(size_t)i * p.nl_cap + pos] = make_float4(dx, dy, dz, __int_as_float(code));
+                }
+                c_atm += __popc(m);
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            fx += __shfl_xor_sync(0xffffffffu, fx, o);
+            fy += __shfl_xor_sync(0xffffffffu, fy, o);
+            fz += __shfl_xor_sync(0xffffffffu, fz, o);
+        }
+        if (lane == 0) {
+            const int site = p.slot_site[i];
+            p.f[3 * site] = (double)fx;
+            p.f[3 * site + 1] = (double)fy;
+            p.f[3 * site + 2] = (double)fz;
+            if (EMIT) {
+                p.nl_count[i] = min(c_atm, p.nl_cap);
+                if (c_atm > p.nl_cap) atomicOr(&p.err[E_ATM_OVERFLOW], 1);
+            }
+        }
+    }
+    if (MEASURE) {
+        double vals[8] = {m_u, m_w[0], m_w[1], m_w[2], m_w[3], m_w[4], m_w[5], m_pairs};
+        for (int k = 0; k < 8; k++) {
+            double x = vals[k];
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            vals[k] = x;
+        }
+        if (lane == 0) for (int k = 0; k < 8; k++) s_part[w][k] = vals[k];
+        __syncthreads();
+        const int tid = threadIdx.x;
+        if (tid < R_NSLOTS) {
+            double s = 0.0;
+            int src = -1;
+            if (tid == R_ULJ) src = 0;
+            else if (tid >= R_W0 && tid <= R_W5) src = 1 + tid - R_W0;
+            else if (tid == R_PAIRS) src = 7;
+            if (src >= 0)
+                for (int k = 0; k < 8; k++) s += s_part[k][src];
+            p.partials[(size_t)blockIdx.x * R_NSLOTS + tid] = s;
+        }
+    }
+}
+
+int vlist_grid(const Engine &e) { return (int)((e.n + 7) / 8); }
+
+void launch_vlist_build(Engine &e, cudaStream_t st) {
+    PairParams p = pair_params(e);
+    k_vlist_build<<<e.g.ncell, kTileThreads, 0, st>>>(p);
+}
+
+int launch_lj_vlist(Engine &e, PairParams &p, bool measure, bool emit, cudaStream_t st) {
+    const int grid = vlist_grid(e);
+    const int n = (int)e.n;
+    if (measure) {
+        if (emit) k_lj_vlist<true, true><<<grid, 256, 0, st>>>(p, n);
+        else k_lj_vlist<true, false><<<grid, 256, 0, st>>>(p, n);
+    } else {
+        if (emit) k_lj_vlist<false, true><<<grid, 256, 0, st>>>(p, n);
+        else k_lj_vlist<false, false><<<grid, 256, 0, st>>>(p, n);
+    }
+    return grid;
+}
+
 void launch_pair_tile(PairParams &p, int ncell, bool measure, bool emit, cudaStream_t st) {
     if (measure) {
         if (emit) k_pair_tile<true, true><<<ncell, kTileThreads, 0, st>>>(p);

@@ -266,3 +266,54 @@ def test_full_size_binning_and_momentum():
     assert obs["n_in_box"] == s.n
     assert obs["triplets"] > 15 * s.n     # thermalised FCC: 18 neighbours inside 2.0
     g.close()
+
+
+def _physics_cfg(s, skin, cell):
+    from komd_gb300 import gpu
+    return gpu.make_config(s.low, s.high, cell, cutoff=2.5, cutoff_3b=2.0, nu=0.073, dt=0.005,
+                           terms=gpu.TERM_LJ | gpu.TERM_ATM, atm_sign=gpu.ATM_SIGN_PHYSICAL,
+                           atm_enum=gpu.ATM_ENUM_FULL, virial_mode=gpu.VIRIAL_CORRECT, skin=skin)
+
+
+def test_verlet_path_matches_rebuild_every_step(oracle_lib):
+    """The Verlet list (skin 0.3, rebuilt on demand inside the graph) gives the
+    forces of a per-step rebuild: same trajectory over 60 steps, and forces at
+    the end equal a fresh rebuild's and the oracle's."""
+    from komd_gb300 import gpu, lattice
+    s = lattice.argon_fcc(10, rho=0.8442, t_star=1.2, seed=41, jitter=0.05)    # 4000 sites, L = 16.8
+    a = gpu.GpuSystem(s, _physics_cfg(s, 0.3, 2.8))
+    b = gpu.GpuSystem(s, _physics_cfg(s, 0.0, 2.8))
+    for g in (a, b):
+        g.update_container()
+        g.forces()
+    for _ in range(6):
+        a.step(10)
+        b.step(10)
+    ra, va, fa = a.download()
+    rb, vb, fb = b.download()
+    assert np.abs(ra - rb).max() < 1e-4
+    assert rel_rmse(fa, fb) < 1e-4
+    # list-based forces of the last step == forces after a fresh rebuild
+    a.update_container()
+    a.forces()
+    _, _, fresh = a.download()
+    assert rel_rmse(fa, fresh) < 2e-6
+    sim = oracle_lib.OracleSim(lattice.System(r=ra, v=va, m=s.m, eps=s.eps, sig=s.sig, mol_id=s.mol_id, low=s.low,
+                                              high=s.high), 2.8, 2.5, nu=0.073, cutoff_atm=2.0, atm=True,
+                               atm_mode="full", atm_sign=oracle_lib.ATM_SIGN_PHYSICAL,
+                               virial_mode=oracle_lib.VIRIAL_CORRECT)
+    sim.update_container()
+    sim.forces()
+    assert rel_rmse(fresh, sim.f) < FP32_FORCE_RMSE
+    obs = a.measure(gpu.MEASURE_ENERGY | gpu.MEASURE_PRESSURE)
+    assert obs["u_lj"] == pytest.approx(sim.lj_out.u_total, rel=1e-5)
+    assert obs["u_atm"] == pytest.approx(sim.atm_out.energy, rel=1e-5)
+    a.close()
+    b.close()
+
+
+def test_verlet_requires_cell_for_skin():
+    from komd_gb300 import gpu, lattice
+    s = lattice.argon_fcc(10, seed=1)
+    with pytest.raises(gpu.KomdError, match="cutoff \\+ skin"):
+        gpu.GpuSystem(s, _physics_cfg(s, 0.3, 2.5))
