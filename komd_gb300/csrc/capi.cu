@@ -66,8 +66,8 @@ double temperature_from(double mv2, double n_in_box) {
 // ---------------------------------------------------------------------------
 // profiling: event pairs per kernel family
 // ---------------------------------------------------------------------------
-const char *kFamilies[] = {"container", "pair", "bonded", "limit", "atm", "integrate", "measure"};
-constexpr int kNumFamilies = 7;
+const char *kFamilies[] = {"container", "pair", "bonded", "limit", "atm", "integrate", "measure", "list_rebuilds"};
+constexpr int kNumFamilies = 8;   // the last is a counter (launches = Verlet-list builds), not timed
 enum Fam { F_CONTAINER = 0, F_PAIR, F_BONDED, F_LIMIT, F_ATM, F_INTEGRATE, F_MEASURE };
 
 }  // namespace
@@ -373,7 +373,8 @@ int komd_gpu_create(const komd_config *cfg, int device, komd_gpu **out) {
                 nb[(size_t)c * 27 + k] = make_float4((float)o[0], (float)o[1], (float)o[2], img ? 1.f : 0.f);
             }
         }
-        if (dalloc(e.nboff, nb.size()) || dalloc(e.rebuild, 1) ||
+        if (dalloc(e.nboff, nb.size()) || dalloc(e.rebuild, 1) || dalloc(e.rebuild_count, 1) ||
+            cudaMemset(e.rebuild_count, 0, sizeof(int)) != cudaSuccess ||
             cudaMemcpy(e.nboff, nb.data(), sizeof(float4) * nb.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
             cudaMemset(e.rebuild, 0, sizeof(int)) != cudaSuccess) {
             komd_gpu_destroy(h);
@@ -399,6 +400,7 @@ int komd_gpu_destroy(komd_gpu *h) {
     dfree(e.nl); dfree(e.nl_count); dfree(e.bonds); dfree(e.angles); dfree(e.partials); dfree(e.err);
     dfree(e.rdf); dfree(e.lj_hist); dfree(e.counts); dfree(h->f_scratch); dfree(h->acc); dfree(e.offtab);
     dfree(e.nboff); dfree(e.rebuild); dfree(e.img); dfree(e.ref); dfree(e.slot_cell); dfree(e.vl); dfree(e.vl_count);
+    dfree(e.rebuild_count); dfree(e.hdtm); dfree(e.exact_com);
     for (auto &p : h->pending) { h->pool.push_back(p.second.first); h->pool.push_back(p.second.second); }
     for (auto ev : h->pool) cudaEventDestroy(ev);
     if (e.own_stream && e.stream) cudaStreamDestroy(e.stream);
@@ -474,6 +476,26 @@ int komd_gpu_upload_sites(komd_gpu *h, int64_t n, const double *r, const double 
     CK(cudaMemcpy(e.key, key.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(e.site_mol, site_mol.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(e.mol_off, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice));
+    {
+        // (dt * 0.5) / m per site, the reference's dtInv2m, and the exact-COM flags
+        std::vector<double> hdtm(n);
+        const double dt_half = e.cfg.delta_t * 0.5;
+        for (int64_t s = 0; s < n; s++) hdtm[s] = dt_half / m[s];
+        std::vector<unsigned char> exact(e.n_mol);
+        for (int64_t k = 0; k < e.n_mol; k++) {
+            int ex = 0;
+            const double mk = m[off[k]];
+            exact[k] = (off[k + 1] - off[k] == 1 && std::frexp(mk, &ex) == 0.5) ? 1 : 0;
+        }
+        CK(dalloc(e.hdtm, n));
+        CK(dalloc(e.exact_com, e.n_mol));
+        CK(cudaMemcpy(e.hdtm, hdtm.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(e.exact_com, exact.data(), e.n_mol, cudaMemcpyHostToDevice));
+        e.uniform = true;
+        for (int64_t s = 1; s < n && e.uniform; s++) e.uniform = eps[s] == eps[0] && sig[s] == sig[0];
+        e.eps0 = (float)eps[0];
+        e.sig0 = (float)sig[0];
+    }
     // ATM list capacity: 1.6x the mean neighbour count inside cutoff_3b + 16
     int cap = e.cfg.atm_list_cap;
     if (cap <= 0) {
@@ -777,6 +799,7 @@ int komd_gpu_neighbour_counts(komd_gpu *h, int64_t *counts) {
 int komd_gpu_set_profiling(komd_gpu *h, int on) {
     if (!h) return fail(KOMD_ERR_ARG, "null handle");
     collect_profile(h);
+    if (h->e.rebuild_count) cudaMemsetAsync(h->e.rebuild_count, 0, sizeof(int), h->e.stream);
     h->e.profiling = on != 0;
     for (int k = 0; k < kNumFamilies; k++) { h->launches[k] = 0; h->ms[k] = 0.0; }
     return KOMD_OK;
@@ -785,6 +808,11 @@ int komd_gpu_set_profiling(komd_gpu *h, int on) {
 int komd_gpu_profile(komd_gpu *h, int max_families, int64_t *launches, double *ms, char *names, int cap) {
     if (!h) return fail(KOMD_ERR_ARG, "null handle");
     collect_profile(h);
+    if (h->e.rebuild_count) {
+        int rb = 0;
+        CK(cudaMemcpy(&rb, h->e.rebuild_count, sizeof(int), cudaMemcpyDeviceToHost));
+        h->launches[kNumFamilies - 1] = rb;
+    }
     std::string s;
     for (int k = 0; k < kNumFamilies && k < max_families; k++) {
         if (launches) launches[k] = h->launches[k];

@@ -137,6 +137,8 @@ struct PairParams {
     double rl2;                // (cutoff + skin)^2
     const int *slot_cell;
     const float4 *nboff;
+    int *rebuild_count;
+    float eps0, sig0;
 };
 
 struct AtmParams {
@@ -209,6 +211,13 @@ struct Engine {
     unsigned *vl = nullptr;      // vl_cap entries per slot: same-molecule bit 31 | nb << 26 | slot
     int *vl_count = nullptr;
     int vl_cap = 0;
+    int *rebuild_count = nullptr;    // list builds since the last profile reset
+    // per-site (dt/2)/m and per-molecule exact-COM flags (single site, power-of-two mass)
+    double *hdtm = nullptr;
+    unsigned char *exact_com = nullptr;
+    // all sites share eps and sigma: the list kernel uses constants
+    bool uniform = false;
+    float eps0 = 1.f, sig0 = 1.f;
 };
 
 constexpr int kMaxVerletSlot = (1 << 26) - 1;

@@ -21,18 +21,26 @@ namespace komd {
 __global__ void k_com_wrap_bin(Grid g, int n_mol, const int *__restrict__ mol_off, double *__restrict__ r,
                                const double *__restrict__ m, double *__restrict__ com, int *__restrict__ mol_cell,
                                int *__restrict__ mol_rank, int *__restrict__ cell_count, int *__restrict__ cell_mcount,
-                               char4 *__restrict__ img, const int *__restrict__ rebuild) {
+                               char4 *__restrict__ img, const int *__restrict__ rebuild,
+                               const unsigned char *__restrict__ exact_com) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n_mol) return;
     const int s0 = mol_off[k], s1 = mol_off[k + 1];
-    // com += r * m ; M += m ; com /= M   (updateCOM, no FMA)
+    // com += r * m ; M += m ; com /= M   (updateCOM, no FMA).  For a single
+    // site of power-of-two mass the scaling is exact and the result is r
+    // itself (up to the sign of a zero), so the FP64 division is skipped.
     double c[3] = {0.0, 0.0, 0.0}, tm = 0.0;
-    for (int s = s0; s < s1; s++) {
-        const double ms = m[s];
-        for (int d = 0; d < 3; d++) c[d] = dadd(c[d], dmul(r[3 * s + d], ms));
-        tm = dadd(tm, ms);
+    if (s1 - s0 == 1 && exact_com && exact_com[k]) {
+        tm = m[s0];
+        for (int d = 0; d < 3; d++) c[d] = r[3 * s0 + d];
+    } else {
+        for (int s = s0; s < s1; s++) {
+            const double ms = m[s];
+            for (int d = 0; d < 3; d++) c[d] = dadd(c[d], dmul(r[3 * s + d], ms));
+            tm = dadd(tm, ms);
+        }
+        for (int d = 0; d < 3; d++) c[d] = ddiv(c[d], tm);
     }
-    for (int d = 0; d < 3; d++) c[d] = ddiv(c[d], tm);
     // Periodic_Kernel: strict comparisons against the domain bounds
     double off[3];
     bool moved = false;
@@ -60,7 +68,11 @@ __global__ void k_com_wrap_bin(Grid g, int n_mol, const int *__restrict__ mol_of
                 img[s] = q;
             }
         }
-        for (int d = 0; d < 3; d++) c[d] = ddiv(c2[d], tm);
+        if (s1 - s0 == 1 && exact_com && exact_com[k]) {
+            for (int d = 0; d < 3; d++) c[d] = r[3 * s0 + d];
+        } else {
+            for (int d = 0; d < 3; d++) c[d] = ddiv(c2[d], tm);
+        }
     }
     for (int d = 0; d < 3; d++) com[3 * k + d] = c[d];
     if (rebuild && !*rebuild) return;   // no rebuild in this step: cells stay as built
@@ -576,7 +588,7 @@ __global__ void __launch_bounds__(kBlock) k_atm_q(AtmParams p) {
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int cap = p.nl_cap;
     float4 *se = s_dyn + wib * cap;
-    float2 *sq = reinterpret_cast<float2 *>(s_dyn + kWarpsPerBlock * cap) + wib * cap;
+    float4 *sq = s_dyn + kWarpsPerBlock * cap + wib * cap;   // (A, 1/A, 1/sqrt(A), -) per entry
     const int i = blockIdx.x * kWarpsPerBlock + wib;
     const float rc2 = (float)p.rc2;
     float gx = 0.f, gy = 0.f, gz = 0.f;
@@ -588,10 +600,10 @@ __global__ void __launch_bounds__(kBlock) k_atm_q(AtmParams p) {
         if (!valid) return;
         const int a = (int)(e & 0xffffu), b = (int)(e >> 16);
         const float4 ea = se[a], eb = se[b];
-        const float2 qa = sq[a], qb = sq[b];
+        const float4 qa = sq[a], qb = sq[b];
         const float A = qa.x, B = qb.x;
         const float wc = rsqrtf(C);
-        const float sv = rsqrtf(A) * rsqrtf(B) * wc;       // 1/(abc)
+        const float sv = qa.z * qb.z * wc;                  // 1/(abc)
         const float s2 = sv * sv;
         const float s5 = s2 * s2 * sv;
         const float t1 = A + B - C, t2 = A - B + C, t3 = B + C - A;
@@ -631,7 +643,7 @@ __global__ void __launch_bounds__(kBlock) k_atm_q(AtmParams p) {
             const float4 e = p.nl[(size_t)i * cap + k];
             const float A = e.x * e.x + e.y * e.y + e.z * e.z;
             se[k] = e;
-            sq[k] = make_float2(A, 1.0f / A);
+            sq[k] = make_float4(A, 1.0f / A, rsqrtf(A), 0.f);
         }
         __syncwarp();
         int qn = 0;
@@ -824,13 +836,15 @@ __global__ void k_limit(int n, const double *__restrict__ eps, const double *__r
 // ===========================================================================
 // With a Verlet list (ref != nullptr) it also flags a rebuild when a site's
 // continuous position r - img*L has moved more than skin/2 since the build.
+// hdtm[s] = (dt * 0.5) / m[s], the reference's dtInv2m (Integrator.cpp:29), computed
+// once at upload with the same IEEE division
 __global__ void k_step0(int n, double *__restrict__ r, double *__restrict__ v, const double *__restrict__ f,
-                        const double *__restrict__ m, double dt_half, double dt, Grid g,
+                        const double *__restrict__ hdtm, double dt, Grid g,
                         const char4 *__restrict__ img, const double *__restrict__ ref, float half_skin2,
                         int *__restrict__ rebuild) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
-    const double c = ddiv(dt_half, m[s]);
+    const double c = hdtm[s];
     double x[3];
     for (int d = 0; d < 3; d++) {
         const double vv = dadd(v[3 * s + d], dmul(f[3 * s + d], c));
@@ -847,12 +861,12 @@ __global__ void k_step0(int n, double *__restrict__ r, double *__restrict__ v, c
     }
 }
 
-__global__ void k_step1(int n, double *__restrict__ v, const double *__restrict__ f, const double *__restrict__ m,
-                        double dt_half, int *err, int *rebuild) {
+__global__ void k_step1(int n, double *__restrict__ v, const double *__restrict__ f, const double *__restrict__ hdtm,
+                        int *err, int *rebuild) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (rebuild && s == 0) *rebuild = 0;   // every consumer of this step's flag has run
     if (s >= n) return;
-    const double c = ddiv(dt_half, m[s]);
+    const double c = hdtm[s];
     bool bad = false;
     for (int d = 0; d < 3; d++) {
         const double vv = dadd(v[3 * s + d], dmul(f[3 * s + d], c));
@@ -986,7 +1000,7 @@ void launch_container(Engine &e, cudaStream_t st) {
     cudaMemsetAsync(e.cell_mcount, 0, sizeof(int) * g.ncell, st);
     k_com_wrap_bin<<<nblk(e.n_mol, 256), 256, 0, st>>>(g, (int)e.n_mol, e.mol_off, e.r, e.m, e.com, e.mol_cell,
                                                          e.mol_rank, e.cell_count, e.cell_mcount,
-                                                         e.verlet ? e.img : nullptr, rb);
+                                                         e.verlet ? e.img : nullptr, rb, e.exact_com);
     k_scan2<<<1, 1024, 0, st>>>(g.ncell, e.cell_count, e.cell_start, e.cell_mcount, e.cell_mstart, rb);
     k_scatter_mol<<<nblk(e.n_mol, 256), 256, 0, st>>>((int)e.n_mol, e.mol_cell, e.mol_rank, e.cell_mstart,
                                                         e.cell_mols, rb);
@@ -1040,6 +1054,9 @@ PairParams pair_params(Engine &e) {
     p.rl2 = rl * rl;
     p.slot_cell = e.slot_cell;
     p.nboff = e.nboff;
+    p.rebuild_count = e.rebuild_count;
+    p.eps0 = e.eps0;
+    p.sig0 = e.sig0;
     return p;
 }
 
@@ -1106,7 +1123,7 @@ void launch_limit(Engine &e, cudaStream_t st) {
 
 size_t atm_smem(const Engine &e) {
     const size_t per = e.cfg.precision == KOMD_FP64 ? (sizeof(AtmEntryD) + 2 * sizeof(double))
-                                                    : (sizeof(float4) + 2 * sizeof(float));
+                                                    : (2 * sizeof(float4));
     return (size_t)kWarpsPerBlock * e.nl_cap * per;
 }
 
@@ -1153,13 +1170,13 @@ void launch_atm(Engine &e, cudaStream_t st, bool measure) {
 
 void launch_step0(Engine &e, cudaStream_t st) {
     const float hs = (float)(0.5 * e.cfg.skin);
-    k_step0<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.r, e.v, e.f, e.m, e.cfg.delta_t * 0.5, e.cfg.delta_t, e.g,
+    k_step0<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.r, e.v, e.f, e.hdtm, e.cfg.delta_t, e.g,
                                               e.verlet ? e.img : nullptr, e.verlet ? e.ref : nullptr, hs * hs,
                                               e.rebuild);
 }
 
 void launch_step1(Engine &e, cudaStream_t st) {
-    k_step1<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.v, e.f, e.m, e.cfg.delta_t * 0.5, e.err,
+    k_step1<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.v, e.f, e.hdtm, e.err,
                                               e.verlet ? e.rebuild : nullptr);
 }
 

@@ -273,6 +273,7 @@ __global__ void __launch_bounds__(kTileThreads) k_vlist_build(PairParams p) {
     if (!*p.rebuild) return;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int cell = blockIdx.x;
+    if (cell == 0 && tid == 0 && p.rebuild_count) atomicAdd(p.rebuild_count, 1);
     int cx, cy, cz;
     cell_coords(p.g, cell, cx, cy, cz);
     if (tid < 27) {
@@ -372,9 +373,10 @@ __global__ void __launch_bounds__(kTileThreads) k_vlist_build(PairParams p) {
 // cell.  Inside cutoff_3b the pair is appended to the ATM list in list
 // order.  No atomics: the warp owns its site.
 // ---------------------------------------------------------------------------
-template <bool MEASURE, bool EMIT>
+template <bool MEASURE, bool EMIT, bool UNIFORM>
 __global__ void __launch_bounds__(256) k_lj_vlist(PairParams p, int n) {
     __shared__ double s_part[8][8];
+    constexpr int U = 4;   // list entries per lane in flight: independent loads for latency hiding
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int i = blockIdx.x * 8 + w;
     const float rc2 = (float)p.rc2, rc3sq = (float)p.rc3sq;
@@ -384,56 +386,77 @@ __global__ void __launch_bounds__(256) k_lj_vlist(PairParams p, int n) {
     if (i < n) {
         const int cnt = p.vl_count[i];
         const float4 pi = p.pos4[i];
-        const float sei = p.seps[i];
+        const float sei = UNIFORM ? 0.f : p.seps[i];
         const float4 *off = p.nboff + (size_t)p.slot_cell[i] * 27;
         const unsigned *row = p.vl + (size_t)i * p.vl_cap;
+        const float sg2u = p.sig0 * p.sig0, eeu = p.eps0;
         float fx = 0.f, fy = 0.f, fz = 0.f;
         int c_atm = 0;
-        for (int k0 = 0; k0 < cnt; k0 += 32) {
-            const int k = k0 + lane;
-            bool emit = false;
-            float dx = 0.f, dy = 0.f, dz = 0.f;
-            int code = 0;
-            if (k < cnt) {
-                const unsigned e = row[k];
-                const int j = (int)(e & 0x3ffffffu);
-                const int nb = (int)((e >> 26) & 31u);
-                const float4 o = off[nb];
-                const float4 pj = p.pos4[j];
-                dx = pi.x - (pj.x + o.x);
-                dy = pi.y - (pj.y + o.y);
-                dz = pi.z - (pj.z + o.z);
-                const float r2 = dx * dx + dy * dy + dz * dz;
-                if (p.use_lj && r2 <= rc2 && !(e >> 31)) {
-                    const float inv = rcp_approx(r2);
-                    const float sg = pi.w + pj.w;
-                    const float x = sg * sg * inv;
-                    const float lj6 = x * x * x;
-                    const float ee = sei * p.seps[j];
-                    const float fac = 24.0f * ee * (2.0f * lj6 * lj6 - lj6) * inv;
-                    fx += dx * fac; fy += dy * fac; fz += dz * fac;
-                    if (MEASURE) {
-                        const float gx = dx * fac, gy = dy * fac, gz = dz * fac;
-                        m_u += 2.0f * ee * (lj6 * lj6 - lj6);
-                        m_pairs += 0.5f;
-                        m_w[0] += 0.5f * dx * gx;
-                        m_w[1] += 0.25f * (dx * gy + dy * gx);
-                        m_w[2] += 0.5f * dy * gy;
-                        m_w[3] += 0.25f * (dx * gz + dz * gx);
-                        m_w[4] += 0.25f * (dy * gz + dz * gy);
-                        m_w[5] += 0.5f * dz * gz;
+        for (int k0 = 0; k0 < cnt; k0 += 32 * U) {
+            unsigned e[U];
+            float4 o[U], pj[U];
+            float sej[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int k = k0 + u * 32 + lane;
+                e[u] = k < cnt ? row[k] : 0xffffffffu;
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                if (e[u] != 0xffffffffu) {
+                    o[u] = off[(e[u] >> 26) & 31u];
+                    pj[u] = p.pos4[e[u] & 0x3ffffffu];
+                    if (!UNIFORM) sej[u] = p.seps[e[u] & 0x3ffffffu];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const bool valid = e[u] != 0xffffffffu;
+                float dx = 0.f, dy = 0.f, dz = 0.f, r2 = 1e30f;
+                if (valid) {
+                    dx = pi.x - (pj[u].x + o[u].x);
+                    dy = pi.y - (pj[u].y + o[u].y);
+                    dz = pi.z - (pj[u].z + o[u].z);
+                    r2 = dx * dx + dy * dy + dz * dz;
+                    if (p.use_lj && r2 <= rc2 && !(e[u] >> 31)) {
+                        const float inv = rcp_approx(r2);
+                        float x, ee;
+                        if (UNIFORM) {
+                            x = sg2u * inv;
+                            ee = eeu;
+                        } else {
+                            const float sg = pi.w + pj[u].w;
+                            x = sg * sg * inv;
+                            ee = sei * sej[u];
+                        }
+                        const float lj6 = x * x * x;
+                        const float fac = 24.0f * ee * (2.0f * lj6 * lj6 - lj6) * inv;
+                        fx += dx * fac; fy += dy * fac; fz += dz * fac;
+                        if (MEASURE) {
+                            const float gx = dx * fac, gy = dy * fac, gz = dz * fac;
+                            m_u += 2.0f * ee * (lj6 * lj6 - lj6);
+                            m_pairs += 0.5f;
+                            m_w[0] += 0.5f * dx * gx;
+                            m_w[1] += 0.25f * (dx * gy + dy * gx);
+                            m_w[2] += 0.5f * dy * gy;
+                            m_w[3] += 0.25f * (dx * gz + dz * gx);
+                            m_w[4] += 0.25f * (dy * gz + dz * gy);
+                            m_w[5] += 0.5f * dz * gz;
+                        }
                     }
                 }
-                emit = EMIT && r2 <= rc3sq;
-                code = nb | (o.w != 0.f ? 32 : 0) | (j << 6);
-            }
-            if (EMIT) {
-                const unsigned m = __ballot_sync(0xffffffffu, emit);
-                if (emit) {
-                    const int pos = c_atm + __popc(m & lt);
-                    if (pos < p.nl_cap) p.nl[(size_t)i * p.nl_cap + pos] = make_float4(dx, dy, dz, __int_as_float(code));
+                if (EMIT) {
+                    const bool emit = valid && r2 <= rc3sq;
+                    const unsigned m = __ballot_sync(0xffffffffu, emit);
+                    if (emit) {
+                        const int pos = c_atm + __popc(m & lt);
+                        const int nb = (int)((e[u] >> 26) & 31u), j = (int)(e[u] & 0x3ffffffu);
+                        const int code = nb | (o[u].w != 0.f ? 32 : 0) | (j << 6);
+                        if (pos < p.nl_cap)
+                            p.nl[(size_t)i * p.nl_cap + pos] = make_float4(dx, dy, dz, __int_as_float(code));
+                    }
+                    c_atm += __popc(m);
                 }
-                c_atm += __popc(m);
             }
         }
         for (int o = 16; o > 0; o >>= 1) {
@@ -482,16 +505,21 @@ void launch_vlist_build(Engine &e, cudaStream_t st) {
     k_vlist_build<<<e.g.ncell, kTileThreads, 0, st>>>(p);
 }
 
+template <bool UNIFORM>
+static void lj_vlist_dispatch(PairParams &p, int n, int grid, bool measure, bool emit, cudaStream_t st) {
+    if (measure) {
+        if (emit) k_lj_vlist<true, true, UNIFORM><<<grid, 256, 0, st>>>(p, n);
+        else k_lj_vlist<true, false, UNIFORM><<<grid, 256, 0, st>>>(p, n);
+    } else {
+        if (emit) k_lj_vlist<false, true, UNIFORM><<<grid, 256, 0, st>>>(p, n);
+        else k_lj_vlist<false, false, UNIFORM><<<grid, 256, 0, st>>>(p, n);
+    }
+}
+
 int launch_lj_vlist(Engine &e, PairParams &p, bool measure, bool emit, cudaStream_t st) {
     const int grid = vlist_grid(e);
-    const int n = (int)e.n;
-    if (measure) {
-        if (emit) k_lj_vlist<true, true><<<grid, 256, 0, st>>>(p, n);
-        else k_lj_vlist<true, false><<<grid, 256, 0, st>>>(p, n);
-    } else {
-        if (emit) k_lj_vlist<false, true><<<grid, 256, 0, st>>>(p, n);
-        else k_lj_vlist<false, false><<<grid, 256, 0, st>>>(p, n);
-    }
+    if (e.uniform) lj_vlist_dispatch<true>(p, (int)e.n, grid, measure, emit, st);
+    else lj_vlist_dispatch<false>(p, (int)e.n, grid, measure, emit, st);
     return grid;
 }
 
