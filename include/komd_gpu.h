@@ -55,6 +55,9 @@ enum { KOMD_VIRIAL_COMPAT = 0, KOMD_VIRIAL_CORRECT = 1 };
 #define KOMD_TERM_LIMIT   0x04u  /* potentials/Limit.cpp:19-25                  */
 #define KOMD_TERM_ATM     0x08u  /* potentials/ATM.cpp / ATM_NOLIST.cpp         */
 #define KOMD_TERM_BONDED  0x10u  /* harmonic bond + angle (no reference counterpart) */
+/* with KOMD_TERM_ATM: the learned three-body form (no reference counterpart)
+ * replaces the exact triplet sum once komd_gpu_surrogate_load has run */
+#define KOMD_TERM_ATM_SURROGATE 0x20u
 
 /* measurements (bit mask) */
 #define KOMD_MEASURE_TEMPERATURE 0x01u  /* sensors/TemperatureSensor.cpp:27-48   */
@@ -173,6 +176,45 @@ int  komd_gpu_get_cells(komd_gpu *h, int64_t *count, int64_t ncell, int64_t *idx
  * molecule ID, evaluated in FP64 with the reference's arithmetic
  * (LJ12_6.cpp:23-28), so counts are bit-exact. */
 int  komd_gpu_neighbour_counts(komd_gpu *h, int64_t *counts);
+
+/* ---- learned three-body term (no reference counterpart) ----------------- */
+/* A 32-64-64-1 tanh MLP on per-site descriptors inside cutoff_3b (16 radial
+ * Gaussians, 16 moment-tensor invariants) gives per-site three-body energies;
+ * forces are the analytic gradient.  Inference runs the MLP on the tensor
+ * cores (BF16 weights, FP32 accumulation). */
+#define KOMD_SUR_NFEAT 32
+#define KOMD_SUR_NPARAM 6337   /* W1 64x32, b1 64, W2 64x64, b2 64, w3 64, b3 1 */
+typedef struct komd_surrogate_status {
+    int64_t steps;             /* steps run with the learned form                 */
+    int64_t probes;            /* exact-ATM probes run                            */
+    double last_rmse;          /* last probe: |F_learned - F_exact| RMS / |F_exact| RMS */
+    double max_rmse;
+    int32_t fallback;          /* 1: a probe breached the threshold, exact ATM is used */
+    int64_t fallback_step;
+} komd_surrogate_status;
+/* Loads weights (FP32, KOMD_SUR_NPARAM, converted to BF16), feature
+ * standardisation (mean, std per feature) and energy scaling
+ * (E_i = e_scale * MLP + e_shift).  Every probe_every steps of komd_gpu_step
+ * the exact ATM forces are computed as well; a relative force RMSE above
+ * probe_threshold switches the engine to the exact form for good. */
+int  komd_gpu_surrogate_load(komd_gpu *h, const float *params, const float *fmean, const float *fstd,
+                             double e_scale, double e_shift, int32_t probe_every, double probe_threshold);
+/* Training sample of the current state (after update_container): raw
+ * features (n*32 floats), exact per-site ATM energies V/3 per vertex (n) and
+ * exact ATM forces (n*3), site order, with the configured sign and triplet set. */
+int  komd_gpu_surrogate_sample(komd_gpu *h, float *features, double *e3, double *f3);
+/* Learned three-body forces (n*3) and per-site energies (n) of the current state. */
+int  komd_gpu_surrogate_forces(komd_gpu *h, double *f3, double *e3);
+int  komd_gpu_surrogate_status(komd_gpu *h, komd_surrogate_status *st);
+/* Trains the MLP on the current device by per-site energy regression
+ * (mean squared error, Adam, mini-batches sampled with replacement):
+ * X n*32 standardised features, y n scaled targets; params in/out;
+ * loss (epochs floats, may be NULL) gets each epoch's mean batch loss. */
+int  komd_mlp_train(const float *X, const float *y, int64_t n, float *params, int32_t epochs, int32_t batch,
+                    float lr, uint64_t seed, float *loss);
+/* Gradient of the mean squared error over all n samples (one batch) with
+ * respect to the parameters, from the same kernels komd_mlp_train runs. */
+int  komd_mlp_loss_grad(const float *X, const float *y, int64_t n, const float *params, float *grad, float *loss);
 
 /* ---- profiling ---------------------------------------------------------- */
 /* When enabled, every kernel launch outside komd_gpu_step's graph is

@@ -9,6 +9,7 @@
 
 #include "engine.cuh"
 #include "kernels.cuh"
+#include "surrogate.cuh"
 
 using namespace komd;
 
@@ -66,9 +67,10 @@ double temperature_from(double mv2, double n_in_box) {
 // ---------------------------------------------------------------------------
 // profiling: event pairs per kernel family
 // ---------------------------------------------------------------------------
-const char *kFamilies[] = {"container", "pair", "bonded", "limit", "atm", "integrate", "measure", "list_rebuilds"};
-constexpr int kNumFamilies = 8;   // the last is a counter (launches = Verlet-list builds), not timed
-enum Fam { F_CONTAINER = 0, F_PAIR, F_BONDED, F_LIMIT, F_ATM, F_INTEGRATE, F_MEASURE };
+const char *kFamilies[] = {"container", "pair", "bonded", "limit", "atm", "integrate", "measure", "surrogate",
+                           "probe", "list_rebuilds"};
+constexpr int kNumFamilies = 10;   // the last is a counter (launches = Verlet-list builds), not timed
+enum Fam { F_CONTAINER = 0, F_PAIR, F_BONDED, F_LIMIT, F_ATM, F_INTEGRATE, F_MEASURE, F_SURROGATE, F_PROBE };
 
 }  // namespace
 
@@ -77,8 +79,22 @@ namespace komd {
 void set_last_error(const std::string &msg) { g_last_error = msg; }
 }  // namespace komd
 
+// learned three-body term (surrogate.cu)
+struct Surrogate {
+    bool loaded = false, fallback = false;
+    float *x = nullptr, *mom = nullptr, *dedx = nullptr, *esite = nullptr, *fsur = nullptr;
+    __nv_bfloat16 *w1 = nullptr, *w1t = nullptr, *w2 = nullptr, *w2t = nullptr;
+    float *b1 = nullptr, *b2 = nullptr, *w3 = nullptr, *fmean = nullptr, *fstd = nullptr;
+    float b3 = 0.f, e_scale = 1.f, e_shift = 0.f;
+    int probe_every = 0;
+    double probe_threshold = 0.0, last_rmse = -1.0, max_rmse = 0.0;
+    int64_t probes = 0, steps = 0, fallback_step = -1;
+    double *fprobe = nullptr, *fsur_d = nullptr, *probe_acc = nullptr;
+};
+
 struct komd_gpu {
     Engine e;
+    Surrogate sur;
     double *f_scratch = nullptr;
     double *acc = nullptr;            // R_NSLOTS
     int partial_cap = 0;
@@ -153,8 +169,44 @@ int ensure_partials(komd_gpu *h) {
     return KOMD_OK;
 }
 
+SurParams sur_params(komd_gpu *h) {
+    Engine &e = h->e;
+    Surrogate &u = h->sur;
+    SurParams p;
+    p.n = (int)e.n;
+    p.rc = (float)e.cfg.cutoff_3b;
+    p.nl = e.nl;
+    p.nl_count = e.nl_count;
+    p.nl_cap = e.nl_cap;
+    p.fmean = u.fmean;
+    p.fstd = u.fstd;
+    p.x = u.x;
+    p.mom = u.mom;
+    p.dedx = u.dedx;
+    p.e_site = u.esite;
+    p.fsur = u.fsur;
+    p.w1 = u.w1; p.w1t = u.w1t; p.w2 = u.w2; p.w2t = u.w2t;
+    p.b1 = u.b1; p.b2 = u.b2; p.w3 = u.w3;
+    p.b3 = u.b3; p.e_scale = u.e_scale; p.e_shift = u.e_shift;
+    return p;
+}
+
+bool surrogate_on(komd_gpu *h) {
+    return (h->e.cfg.terms & KOMD_TERM_ATM_SURROGATE) && h->sur.loaded && !h->sur.fallback;
+}
+
+// surrogate three-body forces: into f (fout == nullptr) or written to fout
+void enqueue_surrogate(komd_gpu *h, double *fout) {
+    Engine &e = h->e;
+    SurParams p = sur_params(h);
+    launch_sur_desc(p, e.stream);
+    launch_sur_mlp(p, e.stream);
+    launch_sur_force(p, e.stream);
+    launch_sur_apply(p, e.slot_site, e.f, fout, e.stream);
+}
+
 // the force sequence of Simulation::run: 2-body functors (LJ / FENE, bonded,
-// Limit), then the 3-body functor (ATM)
+// Limit), then the 3-body functor (ATM, exact or learned)
 void enqueue_forces(komd_gpu *h, bool measure, double *lj_hist) {
     Engine &e = h->e;
     cudaStream_t st = e.stream;
@@ -172,11 +224,19 @@ void enqueue_forces(komd_gpu *h, bool measure, double *lj_hist) {
         ProfScope ps(h, F_LIMIT);
         launch_limit(e, st);
     }
-    if (e.cfg.terms & KOMD_TERM_ATM) {
-        ProfScope ps(h, F_ATM);
-        launch_atm(e, st, measure);
+    if (surrogate_on(h)) {
+        {
+            ProfScope ps(h, F_SURROGATE);
+            enqueue_surrogate(h, nullptr);
+        }
+        if (measure) launch_sum_sites((int)e.n, h->sur.esite, h->acc + R_UATM, st);
+    } else if (e.cfg.terms & KOMD_TERM_ATM) {
+        {
+            ProfScope ps(h, F_ATM);
+            launch_atm(e, st, measure);
+        }
+        if (measure) launch_sum_partials(st, atm_grid(e), e.partials, h->acc);
     }
-    if (measure && (e.cfg.terms & KOMD_TERM_ATM)) launch_sum_partials(st, atm_grid(e), e.partials, h->acc);
 }
 
 void enqueue_step(komd_gpu *h) {
@@ -401,6 +461,12 @@ int komd_gpu_destroy(komd_gpu *h) {
     dfree(e.rdf); dfree(e.lj_hist); dfree(e.counts); dfree(h->f_scratch); dfree(h->acc); dfree(e.offtab);
     dfree(e.nboff); dfree(e.rebuild); dfree(e.img); dfree(e.ref); dfree(e.slot_cell); dfree(e.vl); dfree(e.vl_count);
     dfree(e.rebuild_count); dfree(e.hdtm); dfree(e.exact_com);
+    {
+        Surrogate &u = h->sur;
+        dfree(u.x); dfree(u.mom); dfree(u.dedx); dfree(u.esite); dfree(u.fsur); dfree(u.w1); dfree(u.w1t);
+        dfree(u.w2); dfree(u.w2t); dfree(u.b1); dfree(u.b2); dfree(u.w3); dfree(u.fmean); dfree(u.fstd);
+        dfree(u.fprobe); dfree(u.fsur_d); dfree(u.probe_acc);
+    }
     for (auto &p : h->pending) { h->pool.push_back(p.second.first); h->pool.push_back(p.second.second); }
     for (auto ev : h->pool) cudaEventDestroy(ev);
     if (e.own_stream && e.stream) cudaStreamDestroy(e.stream);
@@ -652,16 +718,40 @@ static int finish_steps(komd_gpu *h) {
     return KOMD_OK;
 }
 
-int komd_gpu_step(komd_gpu *h, int64_t n_steps) {
-    if (!h || !h->e.have_sites) return fail(KOMD_ERR_STATE, "no sites uploaded");
+// exact-ATM probe of the learned term at the current state (the ATM list of
+// this step is current): relative force RMSE; a breach switches to exact ATM
+static int run_probe(komd_gpu *h) {
     Engine &e = h->e;
-    if (!e.have_forces) return fail(KOMD_ERR_STATE, "call update_container and forces before step");
-    if (n_steps <= 0) return KOMD_OK;
+    Surrogate &u = h->sur;
+    ProfScope ps(h, F_PROBE);
+    double *keep = e.f;
+    CK(cudaMemsetAsync(u.fprobe, 0, sizeof(double) * 3 * e.n, e.stream));
+    e.f = u.fprobe;
+    launch_atm(e, e.stream, false);
+    e.f = keep;
+    enqueue_surrogate(h, u.fsur_d);
+    CK(cudaMemsetAsync(u.probe_acc, 0, 2 * sizeof(double), e.stream));
+    launch_sur_probe((int)e.n, u.fsur_d, u.fprobe, u.probe_acc, e.stream);
+    double acc[2];
+    CK(cudaMemcpyAsync(acc, u.probe_acc, sizeof(acc), cudaMemcpyDeviceToHost, e.stream));
+    CK(cudaStreamSynchronize(e.stream));
+    u.probes++;
+    u.last_rmse = acc[1] > 0 ? std::sqrt(acc[0] / acc[1]) : 0.0;
+    u.max_rmse = std::max(u.max_rmse, u.last_rmse);
+    if (!(u.last_rmse <= u.probe_threshold)) {
+        u.fallback = true;
+        u.fallback_step = u.steps;
+        if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+        e.graph_valid = false;
+    }
+    return KOMD_OK;
+}
+
+static int run_steps(komd_gpu *h, int64_t n_steps) {
+    Engine &e = h->e;
     if (e.profiling) {
         for (int64_t k = 0; k < n_steps; k++) enqueue_step(h);
-        int rc = check_launch("step");
-        if (rc) return rc;
-        return finish_steps(h);
+        return check_launch("step");
     }
     if (!e.graph_valid) {
         cudaGraph_t graph;
@@ -676,6 +766,30 @@ int komd_gpu_step(komd_gpu *h, int64_t n_steps) {
     }
     for (int64_t k = 0; k < n_steps; k++) CK(cudaGraphLaunch(e.graph, e.stream));
     h->graph_steps += n_steps;
+    return KOMD_OK;
+}
+
+int komd_gpu_step(komd_gpu *h, int64_t n_steps) {
+    if (!h || !h->e.have_sites) return fail(KOMD_ERR_STATE, "no sites uploaded");
+    Engine &e = h->e;
+    if (!e.have_forces) return fail(KOMD_ERR_STATE, "call update_container and forces before step");
+    if (n_steps <= 0) return KOMD_OK;
+    Surrogate &u = h->sur;
+    int64_t done = 0;
+    while (done < n_steps) {
+        int64_t chunk = n_steps - done;
+        const bool probing = surrogate_on(h) && u.probe_every > 0;
+        if (probing) chunk = std::min<int64_t>(chunk, u.probe_every - (u.steps % u.probe_every));
+        const bool learned = surrogate_on(h);
+        int rc = run_steps(h, chunk);
+        if (rc) return rc;
+        done += chunk;
+        if (learned) u.steps += chunk;
+        if (probing && u.steps % u.probe_every == 0) {
+            rc = run_probe(h);
+            if (rc) return rc;
+        }
+    }
     return finish_steps(h);
 }
 
@@ -793,6 +907,208 @@ int komd_gpu_neighbour_counts(komd_gpu *h, int64_t *counts) {
     if (rc) return rc;
     CK(cudaMemcpyAsync(counts, e.counts, sizeof(int64_t) * e.n, cudaMemcpyDeviceToHost, e.stream));
     CK(cudaStreamSynchronize(e.stream));
+    return KOMD_OK;
+}
+
+int komd_gpu_surrogate_load(komd_gpu *h, const float *params, const float *fmean, const float *fstd,
+                            double e_scale, double e_shift, int32_t probe_every, double probe_threshold) {
+    if (!h || !params || !fmean || !fstd) return fail(KOMD_ERR_ARG, "null argument");
+    Engine &e = h->e;
+    if (!e.have_sites) return fail(KOMD_ERR_STATE, "no sites uploaded");
+    if (!(e.cfg.terms & KOMD_TERM_ATM)) return fail(KOMD_ERR_ARG, "the learned three-body term needs KOMD_TERM_ATM");
+    if (e.cfg.precision != KOMD_FP32) return fail(KOMD_ERR_ARG, "the learned three-body term runs in FP32 mode");
+    Surrogate &u = h->sur;
+    const int H = kSurH, F = kSurNF;
+    const float *W1 = params, *b1 = W1 + H * F, *W2 = b1 + H, *b2 = W2 + H * H, *w3 = b2 + H, *b3 = w3 + H;
+    std::vector<__nv_bfloat16> w1(H * F), w1t(F * H), w2(H * H), w2t(H * H);
+    for (int o = 0; o < H; o++)
+        for (int i = 0; i < F; i++) { w1[o * F + i] = __float2bfloat16(W1[o * F + i]); w1t[i * H + o] = w1[o * F + i]; }
+    for (int o = 0; o < H; o++)
+        for (int i = 0; i < H; i++) { w2[o * H + i] = __float2bfloat16(W2[o * H + i]); w2t[i * H + o] = w2[o * H + i]; }
+    CK(dalloc(u.w1, w1.size())); CK(dalloc(u.w1t, w1t.size())); CK(dalloc(u.w2, w2.size())); CK(dalloc(u.w2t, w2t.size()));
+    CK(dalloc(u.b1, H)); CK(dalloc(u.b2, H)); CK(dalloc(u.w3, H)); CK(dalloc(u.fmean, F)); CK(dalloc(u.fstd, F));
+    CK(cudaMemcpy(u.w1, w1.data(), sizeof(__nv_bfloat16) * w1.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(u.w1t, w1t.data(), sizeof(__nv_bfloat16) * w1t.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(u.w2, w2.data(), sizeof(__nv_bfloat16) * w2.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(u.w2t, w2t.data(), sizeof(__nv_bfloat16) * w2t.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(u.b1, b1, sizeof(float) * H, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(u.b2, b2, sizeof(float) * H, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(u.w3, w3, sizeof(float) * H, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(u.fmean, fmean, sizeof(float) * F, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(u.fstd, fstd, sizeof(float) * F, cudaMemcpyHostToDevice));
+    u.b3 = b3[0];
+    u.e_scale = (float)e_scale;
+    u.e_shift = (float)e_shift;
+    CK(dalloc(u.x, (size_t)e.n * kSurNF)); CK(dalloc(u.mom, (size_t)e.n * kSurNC * 9));
+    CK(dalloc(u.dedx, (size_t)e.n * kSurNF)); CK(dalloc(u.esite, e.n)); CK(dalloc(u.fsur, 3 * (size_t)e.n));
+    CK(dalloc(u.fprobe, 3 * (size_t)e.n)); CK(dalloc(u.fsur_d, 3 * (size_t)e.n)); CK(dalloc(u.probe_acc, 2));
+    CK(cudaMemset(u.fsur, 0, sizeof(float) * 3 * e.n));
+    u.probe_every = probe_every;
+    u.probe_threshold = probe_threshold;
+    u.loaded = true;
+    u.fallback = false;
+    u.steps = u.probes = 0;
+    u.last_rmse = -1.0;
+    u.max_rmse = 0.0;
+    u.fallback_step = -1;
+    if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+    e.graph_valid = false;
+    return KOMD_OK;
+}
+
+int komd_gpu_surrogate_sample(komd_gpu *h, float *features, double *e3, double *f3) {
+    if (!h) return fail(KOMD_ERR_ARG, "null handle");
+    Engine &e = h->e;
+    if (!e.have_cells) return fail(KOMD_ERR_STATE, "update_container must run first");
+    if (!(e.cfg.terms & KOMD_TERM_ATM) || e.cfg.precision != KOMD_FP32)
+        return fail(KOMD_ERR_ARG, "samples need KOMD_TERM_ATM in FP32 mode");
+    Surrogate &u = h->sur;
+    if (!u.x) {
+        CK(dalloc(u.x, (size_t)e.n * kSurNF)); CK(dalloc(u.mom, (size_t)e.n * kSurNC * 9));
+        CK(dalloc(u.fprobe, 3 * (size_t)e.n));
+    }
+    double *e3d = nullptr;
+    CK(dalloc(e3d, e.n));
+    CK(cudaMemsetAsync(e3d, 0, sizeof(double) * e.n, e.stream));
+    double *keep = e.f;
+    e.f = u.fprobe;
+    launch_pair(e, e.stream, false, nullptr);                  // ATM neighbour list of this state
+    CK(cudaMemsetAsync(u.fprobe, 0, sizeof(double) * 3 * e.n, e.stream));
+    e.atm_esite = e3d;
+    launch_atm(e, e.stream, true);                             // exact forces and per-site energies
+    e.atm_esite = nullptr;
+    e.f = keep;
+    SurParams p = sur_params(h);
+    p.fmean = nullptr;
+    p.fstd = nullptr;                                          // raw features
+    launch_sur_desc(p, e.stream);
+    int rc = check_launch("surrogate_sample");
+    if (rc) { dfree(e3d); return rc; }
+    std::vector<float> xs((size_t)e.n * kSurNF);
+    std::vector<int> slot_site(e.n);
+    CK(cudaMemcpyAsync(xs.data(), u.x, sizeof(float) * xs.size(), cudaMemcpyDeviceToHost, e.stream));
+    CK(cudaMemcpyAsync(slot_site.data(), e.slot_site, sizeof(int) * e.n, cudaMemcpyDeviceToHost, e.stream));
+    if (e3) CK(cudaMemcpyAsync(e3, e3d, sizeof(double) * e.n, cudaMemcpyDeviceToHost, e.stream));
+    if (f3) CK(cudaMemcpyAsync(f3, u.fprobe, sizeof(double) * 3 * e.n, cudaMemcpyDeviceToHost, e.stream));
+    CK(cudaStreamSynchronize(e.stream));
+    dfree(e3d);
+    if (features)
+        for (int64_t slot = 0; slot < e.n; slot++)
+            std::memcpy(features + (size_t)slot_site[slot] * kSurNF, xs.data() + (size_t)slot * kSurNF,
+                        sizeof(float) * kSurNF);
+    int flags[E_NFLAGS];
+    rc = read_flags(h, flags, true);
+    if (rc) return rc;
+    if (flags[E_ATM_OVERFLOW]) return fail(KOMD_ERR_OVERFLOW, "ATM neighbour list overflow");
+    return KOMD_OK;
+}
+
+int komd_gpu_surrogate_forces(komd_gpu *h, double *f3, double *e3) {
+    if (!h) return fail(KOMD_ERR_ARG, "null handle");
+    Engine &e = h->e;
+    Surrogate &u = h->sur;
+    if (!u.loaded) return fail(KOMD_ERR_STATE, "komd_gpu_surrogate_load first");
+    if (!e.have_cells) return fail(KOMD_ERR_STATE, "update_container must run first");
+    double *keep = e.f;
+    e.f = u.fprobe;
+    launch_pair(e, e.stream, false, nullptr);                  // ATM neighbour list of this state
+    e.f = keep;
+    CK(cudaMemsetAsync(u.fsur_d, 0, sizeof(double) * 3 * e.n, e.stream));
+    enqueue_surrogate(h, u.fsur_d);
+    int rc = check_launch("surrogate_forces");
+    if (rc) return rc;
+    std::vector<float> es(e.n);
+    std::vector<int> slot_site(e.n);
+    if (f3) CK(cudaMemcpyAsync(f3, u.fsur_d, sizeof(double) * 3 * e.n, cudaMemcpyDeviceToHost, e.stream));
+    CK(cudaMemcpyAsync(es.data(), u.esite, sizeof(float) * e.n, cudaMemcpyDeviceToHost, e.stream));
+    CK(cudaMemcpyAsync(slot_site.data(), e.slot_site, sizeof(int) * e.n, cudaMemcpyDeviceToHost, e.stream));
+    CK(cudaStreamSynchronize(e.stream));
+    if (e3)
+        for (int64_t slot = 0; slot < e.n; slot++) e3[slot_site[slot]] = es[slot];
+    return KOMD_OK;
+}
+
+int komd_gpu_surrogate_status(komd_gpu *h, komd_surrogate_status *st) {
+    if (!h || !st) return fail(KOMD_ERR_ARG, "null argument");
+    const Surrogate &u = h->sur;
+    st->steps = u.steps;
+    st->probes = u.probes;
+    st->last_rmse = u.last_rmse;
+    st->max_rmse = u.max_rmse;
+    st->fallback = u.fallback ? 1 : 0;
+    st->fallback_step = u.fallback_step;
+    return KOMD_OK;
+}
+
+namespace {
+struct TrainBuffers {
+    float *X = nullptr, *y = nullptr, *params = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr, *work = nullptr;
+    ~TrainBuffers() { dfree(X); dfree(y); dfree(params); dfree(grad); dfree(m); dfree(v); dfree(work); }
+};
+
+int train_setup(TrainBuffers &b, TrainParams &t, const float *X, const float *y, int64_t n, const float *params,
+                int batch) {
+    if (n <= 0 || n > (1LL << 31) - 1 || batch <= 0) return fail(KOMD_ERR_ARG, "bad sample or batch count");
+    const int stride = kSurNF + 4 * kSurH + 2;
+    CK(dalloc(b.X, (size_t)n * kSurNF)); CK(dalloc(b.y, n)); CK(dalloc(b.params, kSurNParam));
+    CK(dalloc(b.grad, kSurNParam + 1)); CK(dalloc(b.m, kSurNParam)); CK(dalloc(b.v, kSurNParam));
+    CK(dalloc(b.work, (size_t)batch * stride));
+    CK(cudaMemcpy(b.X, X, sizeof(float) * (size_t)n * kSurNF, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(b.y, y, sizeof(float) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(b.params, params, sizeof(float) * kSurNParam, cudaMemcpyHostToDevice));
+    CK(cudaMemset(b.m, 0, sizeof(float) * kSurNParam));
+    CK(cudaMemset(b.v, 0, sizeof(float) * kSurNParam));
+    t.X = b.X; t.y = b.y; t.n = (int)n; t.batch = batch; t.params = b.params; t.grad = b.grad;
+    t.m = b.m; t.v = b.v; t.work = b.work; t.lr = 0.f; t.seed = 0; t.fixed_batch = 0; t.grad_only = 0;
+    return KOMD_OK;
+}
+}  // namespace
+
+int komd_mlp_train(const float *X, const float *y, int64_t n, float *params, int32_t epochs, int32_t batch, float lr,
+                   uint64_t seed, float *loss) {
+    if (!X || !y || !params || epochs < 0) return fail(KOMD_ERR_ARG, "null argument");
+    TrainBuffers b;
+    TrainParams t;
+    int rc = train_setup(b, t, X, y, n, params, batch);
+    if (rc) return rc;
+    t.lr = lr;
+    t.seed = (uint32_t)(seed ^ (seed >> 32));
+    const int64_t steps_per_epoch = std::max<int64_t>(1, n / batch);
+    int step = 0;
+    for (int ep = 0; ep < epochs; ep++) {
+        double sq = 0.0;
+        for (int64_t k = 0; k < steps_per_epoch; k++) {
+            launch_train_step(t, step++, nullptr);
+            if (loss && k == steps_per_epoch - 1) {
+                // the last batch's squared error stands for the epoch (one readback per epoch)
+                float s2 = 0.f;
+                CK(cudaMemcpy(&s2, b.grad + kSurNParam, sizeof(float), cudaMemcpyDeviceToHost));
+                sq = s2;
+            }
+        }
+        rc = check_launch("mlp_train");
+        if (rc) return rc;
+        if (loss) loss[ep] = (float)(sq / batch);
+    }
+    CK(cudaMemcpy(params, b.params, sizeof(float) * kSurNParam, cudaMemcpyDeviceToHost));
+    return KOMD_OK;
+}
+
+int komd_mlp_loss_grad(const float *X, const float *y, int64_t n, const float *params, float *grad, float *loss) {
+    if (!X || !y || !params || !grad) return fail(KOMD_ERR_ARG, "null argument");
+    TrainBuffers b;
+    TrainParams t;
+    int rc = train_setup(b, t, X, y, n, params, (int)n);
+    if (rc) return rc;
+    t.fixed_batch = 1;
+    t.grad_only = 1;
+    launch_train_step(t, 0, nullptr);
+    rc = check_launch("mlp_loss_grad");
+    if (rc) return rc;
+    std::vector<float> g(kSurNParam + 1);
+    CK(cudaMemcpy(g.data(), b.grad, sizeof(float) * g.size(), cudaMemcpyDeviceToHost));
+    std::memcpy(grad, g.data(), sizeof(float) * kSurNParam);
+    if (loss) *loss = g[kSurNParam] / (float)n;
     return KOMD_OK;
 }
 

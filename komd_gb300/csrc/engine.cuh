@@ -154,6 +154,7 @@ struct AtmParams {
     double sign;               // +1 reference (+grad V), -1 physical
     int virial_compat;         // weights and missing ZZ of ATM_Pressure
     int atm_direct;            // COMPAT + direct: no virial contribution
+    double *e_site;            // measure: per-site V/3 sums (site order), optional
 };
 
 struct Engine {
@@ -218,6 +219,7 @@ struct Engine {
     // all sites share eps and sigma: the list kernel uses constants
     bool uniform = false;
     float eps0 = 1.f, sig0 = 1.f;
+    double *atm_esite = nullptr;     // when set, measure-mode ATM writes per-site energies here
 };
 
 constexpr int kMaxVerletSlot = (1 << 26) - 1;

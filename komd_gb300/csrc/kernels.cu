@@ -704,12 +704,16 @@ __global__ void __launch_bounds__(kBlock) k_atm_q(AtmParams p) {
             gy += __shfl_xor_sync(0xffffffffu, gy, o);
             gz += __shfl_xor_sync(0xffffffffu, gz, o);
         }
+        float ev = m_e;
+        if (MEASURE && p.e_site)
+            for (int o = 16; o > 0; o >>= 1) ev += __shfl_xor_sync(0xffffffffu, ev, o);
         if (lane == 0) {
             const int site = p.slot_site[i];
             const double sc = 2.0 * p.sign * p.nu;   // reference: +2 nu (...); physical: -2 nu (...)
             p.f[3 * site] += sc * (double)gx;
             p.f[3 * site + 1] += sc * (double)gy;
             p.f[3 * site + 2] += sc * (double)gz;
+            if (MEASURE && p.e_site) p.e_site[site] = p.nu * (double)ev;
         }
     }
     if (MEASURE) {
@@ -1163,6 +1167,7 @@ void launch_atm(Engine &e, cudaStream_t st, bool measure) {
     p.sign = e.cfg.atm_sign == KOMD_ATM_SIGN_REFERENCE ? 1.0 : -1.0;
     p.virial_compat = e.cfg.virial_mode == KOMD_VIRIAL_COMPAT;
     p.atm_direct = e.cfg.atm_direct;
+    p.e_site = e.atm_esite;
     const bool compat = e.cfg.atm_enum == KOMD_ATM_ENUM_COMPAT;
     if (e.cfg.precision == KOMD_FP64) atm_dispatch<double>(p, measure, compat, atm_grid(e), atm_smem(e), st);
     else atm_dispatch<float>(p, measure, compat, atm_grid(e), atm_smem(e), st);

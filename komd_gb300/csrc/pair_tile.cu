@@ -374,9 +374,9 @@ __global__ void __launch_bounds__(kTileThreads) k_vlist_build(PairParams p) {
 // order.  No atomics: the warp owns its site.
 // ---------------------------------------------------------------------------
 template <bool MEASURE, bool EMIT, bool UNIFORM>
-__global__ void __launch_bounds__(256) k_lj_vlist(PairParams p, int n) {
+__global__ void __launch_bounds__(256, 5) k_lj_vlist(PairParams p, int n) {
     __shared__ double s_part[8][8];
-    constexpr int U = 4;   // list entries per lane in flight: independent loads for latency hiding
+    constexpr int U = 2;   // list entries per lane in flight: independent loads for latency hiding
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int i = blockIdx.x * 8 + w;
     const float rc2 = (float)p.rc2, rc3sq = (float)p.rc3sq;
@@ -396,11 +396,16 @@ __global__ void __launch_bounds__(256) k_lj_vlist(PairParams p, int n) {
             unsigned e[U];
             float4 o[U], pj[U];
             float sej[U];
+            // rows hold vl_cap entries: load speculatively up to the capacity so the
+            // row load does not wait for the count, then mask
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 const int k = k0 + u * 32 + lane;
-                e[u] = k < cnt ? row[k] : 0xffffffffu;
+                e[u] = k < p.vl_cap ? row[k] : 0xffffffffu;
             }
+#pragma unroll
+            for (int u = 0; u < U; u++)
+                if (k0 + u * 32 + lane >= cnt) e[u] = 0xffffffffu;
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 if (e[u] != 0xffffffffu) {

@@ -1,0 +1,523 @@
+// surrogate.cu -- learned three-body term (no reference counterpart): a
+// 32-64-64-1 tanh MLP on per-site descriptors stands in for the ATM triplet
+// sum; forces are the analytic gradient of the learned energy.
+//
+// Descriptors of site i from its neighbours d_j = r_j - r_i inside cutoff_3b
+// (the ATM neighbour list the LJ kernel writes), with fc = (cos(pi r/rc)+1)/2:
+//   G_k  = sum_j exp(-eta_r (r - mu_k)^2) fc            k = 0..15
+//   per channel c = 0..3, g_c = exp(-eta_a (r - mu_c)^2) fc:
+//   M1_c = sum g_c u,  M2_c = sum g_c u u^T,
+//   I1 = |M1|^2, I2 = M2:M2, I3 = M1.M2.M1, I4 = tr(M2^3)
+// x = (raw - mean) / std;  E_i = e_scale * MLP(x) + e_shift.
+// The oracle (oracle/komd_oracle.c, kor_sur_*) states the same definition in FP64.
+//
+// Kernels per step: k_sur_desc (features + moments), k_sur_mlp (tensor cores:
+// mma.sync m16n8k16 BF16 -> FP32, forward and input-gradient backward with the
+// activations kept in registers), k_sur_force (chain rule to the pair vectors,
+// neighbour forces scattered with FP32 atomics), k_sur_apply.
+// Training: k_train_fwdbwd / k_train_grad / k_train_adam (FP32 SIMT).
+#include <cstdint>
+
+#include "engine.cuh"
+#include "kernels.cuh"
+#include "surrogate.cuh"
+
+namespace komd {
+
+__constant__ float c_mu_a[kSurNC] = {1.05f, 1.30f, 1.55f, 1.80f};
+
+__device__ __forceinline__ float sur_mu_r(int k) { return 0.85f + (float)k * (1.15f / 15.0f); }
+
+// radial Gaussians by the product recurrence exp(-eta (t - D)^2) = exp(-eta t^2) exp(2 eta D t) exp(-eta D^2)
+__device__ __forceinline__ void radial_basis(float r, float fc, float dfc, float *G, float *dG) {
+    const float D = 1.15f / 15.0f;
+    float t = r - 0.85f;
+    float gk = __expf(-kSurEtaR * t * t);
+    float up = __expf(2.0f * kSurEtaR * D * t);
+    const float c1 = __expf(-kSurEtaR * D * D), c2 = c1 * c1;
+#pragma unroll
+    for (int k = 0; k < kSurNR; k++) {
+        G[k] = gk * fc;
+        if (dG) dG[k] = gk * (-2.0f * kSurEtaR * t * fc + dfc);
+        gk = gk * up * c1;
+        up = up * c2;
+        t -= D;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// descriptors: one warp per slot (cell order)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_sur_desc(SurParams p) {
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (i >= p.n) return;
+    const int ni = p.nl_count[i];
+    float acc[kSurNR + kSurNC * 9];   // G (16), then per channel M1 (3) + M2 (6: xx xy xz yy yz zz)
+#pragma unroll
+    for (int k = 0; k < kSurNR + kSurNC * 9; k++) acc[k] = 0.f;
+    const float rc = p.rc, pi_rc = 3.14159265358979f / p.rc;
+    for (int k = lane; k < ni; k += 32) {
+        const float4 e = p.nl[(size_t)i * p.nl_cap + k];
+        const float dx = -e.x, dy = -e.y, dz = -e.z;    // d = r_j - r_i
+        const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+        if (!(r < rc) || r == 0.f) continue;
+        float sn, cs;
+        __sincosf(pi_rc * r, &sn, &cs);
+        const float fc = 0.5f * (cs + 1.0f);
+        const float ir = 1.0f / r, ux = dx * ir, uy = dy * ir, uz = dz * ir;
+        float G[kSurNR];
+        radial_basis(r, fc, 0.f, G, nullptr);
+#pragma unroll
+        for (int q = 0; q < kSurNR; q++) acc[q] += G[q];
+#pragma unroll
+        for (int c = 0; c < kSurNC; c++) {
+            const float t = r - c_mu_a[c];
+            const float g = __expf(-kSurEtaA * t * t) * fc;
+            float *m = acc + kSurNR + 9 * c;
+            m[0] += g * ux; m[1] += g * uy; m[2] += g * uz;
+            m[3] += g * ux * ux; m[4] += g * ux * uy; m[5] += g * ux * uz;
+            m[6] += g * uy * uy; m[7] += g * uy * uz; m[8] += g * uz * uz;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kSurNR + kSurNC * 9; k++)
+        for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+    // invariants (every lane holds the totals)
+    float raw[kSurNF];
+#pragma unroll
+    for (int k = 0; k < kSurNR; k++) raw[k] = acc[k];
+#pragma unroll
+    for (int c = 0; c < kSurNC; c++) {
+        const float *m = acc + kSurNR + 9 * c;
+        const float M[3][3] = {{m[3], m[4], m[5]}, {m[4], m[6], m[7]}, {m[5], m[7], m[8]}};
+        const float v[3] = {m[0], m[1], m[2]};
+        float Mv[3], M2[3][3];
+        for (int a = 0; a < 3; a++) Mv[a] = M[a][0] * v[0] + M[a][1] * v[1] + M[a][2] * v[2];
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) M2[a][b] = M[a][0] * M[0][b] + M[a][1] * M[1][b] + M[a][2] * M[2][b];
+        float i2 = 0.f, i4 = 0.f;
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) { i2 += M[a][b] * M[a][b]; i4 += M2[a][b] * M[b][a]; }
+        raw[kSurNR + c] = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+        raw[kSurNR + kSurNC + c] = i2;
+        raw[kSurNR + 2 * kSurNC + c] = v[0] * Mv[0] + v[1] * Mv[1] + v[2] * Mv[2];
+        raw[kSurNR + 3 * kSurNC + c] = i4;
+    }
+    // lane k writes feature k (standardised, or raw when fstd is null) and moment k
+    float xk = 0.f;
+#pragma unroll
+    for (int k = 0; k < kSurNF; k++)
+        if (lane == k) xk = raw[k];
+    if (p.fstd) xk = (xk - p.fmean[lane]) / p.fstd[lane];
+    p.x[(size_t)i * kSurNF + lane] = xk;
+    if (p.mom) {
+        float mk = 0.f, mk2 = 0.f;
+#pragma unroll
+        for (int k = 0; k < kSurNC * 9; k++) {
+            if (lane == k) mk = acc[kSurNR + k];
+            if (lane + 32 == k) mk2 = acc[kSurNR + k];
+        }
+        p.mom[(size_t)i * kSurNC * 9 + lane] = mk;
+        if (lane + 32 < kSurNC * 9) p.mom[(size_t)i * kSurNC * 9 + lane + 32] = mk2;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// MLP on the tensor cores: one warp per 16 sites (m16n8k16, BF16 in, FP32 acc)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    uint32_t r;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+    return r;
+}
+
+__device__ __forceinline__ void mma16816(float *c, const uint32_t *a, uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// B fragment of W stored row-major [n][k] (bf16, ld = K): rows n, k pair at k0 + tig*2 (+8)
+__device__ __forceinline__ void load_b(const __nv_bfloat16 *W, int ld, int n0, int k0, int g, int tig, uint32_t &b0,
+                                       uint32_t &b1) {
+    const uint32_t *row = reinterpret_cast<const uint32_t *>(W + (n0 + g) * ld + k0);
+    b0 = row[tig];
+    b1 = row[tig + 4];
+}
+
+__global__ void __launch_bounds__(128) k_sur_mlp(SurParams p) {
+    __shared__ __align__(16) __nv_bfloat16 sW1[kSurH * kSurNF], sW1T[kSurNF * kSurH], sW2[kSurH * kSurH],
+        sW2T[kSurH * kSurH];
+    __shared__ float sb1[kSurH], sb2[kSurH], sw3[kSurH];
+    for (int t = threadIdx.x; t < kSurH * kSurNF; t += blockDim.x) { sW1[t] = p.w1[t]; sW1T[t] = p.w1t[t]; }
+    for (int t = threadIdx.x; t < kSurH * kSurH; t += blockDim.x) { sW2[t] = p.w2[t]; sW2T[t] = p.w2t[t]; }
+    for (int t = threadIdx.x; t < kSurH; t += blockDim.x) { sb1[t] = p.b1[t]; sb2[t] = p.b2[t]; sw3[t] = p.w3[t]; }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
+    const int warp = blockIdx.x * 4 + (threadIdx.x >> 5);
+    const int nwarps = gridDim.x * 4;
+    const int ntiles = (p.n + 15) / 16;
+    for (int tile = warp; tile < ntiles; tile += nwarps) {
+        const int r0 = tile * 16 + g, r1 = r0 + 8;
+        const bool v0 = r0 < p.n, v1 = r1 < p.n;
+        // layer 1: Z1 = X W1^T  (X 16x32 -> 2 k-steps)
+        uint32_t ax[2][4];
+#pragma unroll
+        for (int s = 0; s < 2; s++) {
+            const int k = 16 * s + tig * 2;
+            const float2 x00 = v0 ? *reinterpret_cast<const float2 *>(p.x + (size_t)r0 * kSurNF + k) : make_float2(0.f, 0.f);
+            const float2 x10 = v1 ? *reinterpret_cast<const float2 *>(p.x + (size_t)r1 * kSurNF + k) : make_float2(0.f, 0.f);
+            const float2 x01 = v0 ? *reinterpret_cast<const float2 *>(p.x + (size_t)r0 * kSurNF + k + 8) : make_float2(0.f, 0.f);
+            const float2 x11 = v1 ? *reinterpret_cast<const float2 *>(p.x + (size_t)r1 * kSurNF + k + 8) : make_float2(0.f, 0.f);
+            ax[s][0] = pack_bf16(x00.x, x00.y);
+            ax[s][1] = pack_bf16(x10.x, x10.y);
+            ax[s][2] = pack_bf16(x01.x, x01.y);
+            ax[s][3] = pack_bf16(x11.x, x11.y);
+        }
+        float h1[8][4];
+#pragma unroll
+        for (int t = 0; t < 8; t++) {
+            const int c = t * 8 + tig * 2;
+            float acc[4] = {sb1[c], sb1[c + 1], sb1[c], sb1[c + 1]};
+#pragma unroll
+            for (int s = 0; s < 2; s++) {
+                uint32_t b0, b1;
+                load_b(sW1, kSurNF, t * 8, 16 * s, g, tig, b0, b1);
+                mma16816(acc, ax[s], b0, b1);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) h1[t][q] = tanhf(acc[q]);
+        }
+        // layer 2: Z2 = H1 W2^T (4 k-steps from the h1 fragments)
+        uint32_t ah[4][4];
+#pragma unroll
+        for (int s = 0; s < 4; s++) {
+            ah[s][0] = pack_bf16(h1[2 * s][0], h1[2 * s][1]);
+            ah[s][1] = pack_bf16(h1[2 * s][2], h1[2 * s][3]);
+            ah[s][2] = pack_bf16(h1[2 * s + 1][0], h1[2 * s + 1][1]);
+            ah[s][3] = pack_bf16(h1[2 * s + 1][2], h1[2 * s + 1][3]);
+        }
+        float h2[8][4];
+#pragma unroll
+        for (int t = 0; t < 8; t++) {
+            const int c = t * 8 + tig * 2;
+            float acc[4] = {sb2[c], sb2[c + 1], sb2[c], sb2[c + 1]};
+#pragma unroll
+            for (int s = 0; s < 4; s++) {
+                uint32_t b0, b1;
+                load_b(sW2, kSurH, t * 8, 16 * s, g, tig, b0, b1);
+                mma16816(acc, ah[s], b0, b1);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) h2[t][q] = tanhf(acc[q]);
+        }
+        // layer 3 and dE/dz2 = w3 (1 - h2^2)
+        float e0 = 0.f, e1 = 0.f;
+        uint32_t ad[4][4];
+        float dz2[8][4];
+#pragma unroll
+        for (int t = 0; t < 8; t++) {
+            const int c = t * 8 + tig * 2;
+            e0 += sw3[c] * h2[t][0] + sw3[c + 1] * h2[t][1];
+            e1 += sw3[c] * h2[t][2] + sw3[c + 1] * h2[t][3];
+            dz2[t][0] = sw3[c] * (1.f - h2[t][0] * h2[t][0]);
+            dz2[t][1] = sw3[c + 1] * (1.f - h2[t][1] * h2[t][1]);
+            dz2[t][2] = sw3[c] * (1.f - h2[t][2] * h2[t][2]);
+            dz2[t][3] = sw3[c + 1] * (1.f - h2[t][3] * h2[t][3]);
+        }
+        e0 += __shfl_xor_sync(0xffffffffu, e0, 1);
+        e0 += __shfl_xor_sync(0xffffffffu, e0, 2);
+        e1 += __shfl_xor_sync(0xffffffffu, e1, 1);
+        e1 += __shfl_xor_sync(0xffffffffu, e1, 2);
+        if (tig == 0) {
+            if (v0) p.e_site[r0] = p.e_scale * (e0 + p.b3) + p.e_shift;
+            if (v1) p.e_site[r1] = p.e_scale * (e1 + p.b3) + p.e_shift;
+        }
+#pragma unroll
+        for (int s = 0; s < 4; s++) {
+            ad[s][0] = pack_bf16(dz2[2 * s][0], dz2[2 * s][1]);
+            ad[s][1] = pack_bf16(dz2[2 * s][2], dz2[2 * s][3]);
+            ad[s][2] = pack_bf16(dz2[2 * s + 1][0], dz2[2 * s + 1][1]);
+            ad[s][3] = pack_bf16(dz2[2 * s + 1][2], dz2[2 * s + 1][3]);
+        }
+        // dH1 = dZ2 W2  (B = W2^T rows), dZ1 = dH1 (1 - h1^2)
+        uint32_t az[4][4];
+        float dz1[8][4];
+#pragma unroll
+        for (int t = 0; t < 8; t++) {
+            float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int s = 0; s < 4; s++) {
+                uint32_t b0, b1;
+                load_b(sW2T, kSurH, t * 8, 16 * s, g, tig, b0, b1);
+                mma16816(acc, ad[s], b0, b1);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) dz1[t][q] = acc[q] * (1.f - h1[t][q] * h1[t][q]);
+        }
+#pragma unroll
+        for (int s = 0; s < 4; s++) {
+            az[s][0] = pack_bf16(dz1[2 * s][0], dz1[2 * s][1]);
+            az[s][1] = pack_bf16(dz1[2 * s][2], dz1[2 * s][3]);
+            az[s][2] = pack_bf16(dz1[2 * s + 1][0], dz1[2 * s + 1][1]);
+            az[s][3] = pack_bf16(dz1[2 * s + 1][2], dz1[2 * s + 1][3]);
+        }
+        // dX = dZ1 W1  (B = W1^T rows, n = feature)
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int s = 0; s < 4; s++) {
+                uint32_t b0, b1;
+                load_b(sW1T, kSurH, t * 8, 16 * s, g, tig, b0, b1);
+                mma16816(acc, az[s], b0, b1);
+            }
+            const int c = t * 8 + tig * 2;
+            if (v0) *reinterpret_cast<float2 *>(p.dedx + (size_t)r0 * kSurNF + c) = make_float2(acc[0], acc[1]);
+            if (v1) *reinterpret_cast<float2 *>(p.dedx + (size_t)r1 * kSurNF + c) = make_float2(acc[2], acc[3]);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// forces: chain rule to the pair vectors; one warp per slot, one neighbour
+// entry per lane; the centre's force is warp-reduced, the neighbour's is
+// scattered with FP32 atomics into fsur (slot order)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_sur_force(SurParams p) {
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (i >= p.n) return;
+    // dE_i / d raw = e_scale * dE/dx / std  (lane k holds feature k)
+    const float drk = p.e_scale * p.dedx[(size_t)i * kSurNF + lane] / p.fstd[lane];
+    float dr[kSurNF];
+#pragma unroll
+    for (int k = 0; k < kSurNF; k++) dr[k] = __shfl_sync(0xffffffffu, drk, k);
+    // angular coefficients a_c = dE/dM1_c, B_c = dE/dM2_c
+    float a[kSurNC][3], B[kSurNC][6];
+    const float *mom = p.mom + (size_t)i * kSurNC * 9;
+#pragma unroll
+    for (int c = 0; c < kSurNC; c++) {
+        const float v[3] = {mom[9 * c], mom[9 * c + 1], mom[9 * c + 2]};
+        const float m[6] = {mom[9 * c + 3], mom[9 * c + 4], mom[9 * c + 5], mom[9 * c + 6], mom[9 * c + 7], mom[9 * c + 8]};
+        const float M[3][3] = {{m[0], m[1], m[2]}, {m[1], m[3], m[4]}, {m[2], m[4], m[5]}};
+        const float e1 = dr[kSurNR + c], e2 = dr[kSurNR + kSurNC + c], e3 = dr[kSurNR + 2 * kSurNC + c],
+                    e4 = dr[kSurNR + 3 * kSurNC + c];
+        float Mv[3], M2[3][3];
+        for (int x = 0; x < 3; x++) Mv[x] = M[x][0] * v[0] + M[x][1] * v[1] + M[x][2] * v[2];
+        for (int x = 0; x < 3; x++)
+            for (int y = 0; y < 3; y++) M2[x][y] = M[x][0] * M[0][y] + M[x][1] * M[1][y] + M[x][2] * M[2][y];
+        for (int x = 0; x < 3; x++) a[c][x] = 2.f * e1 * v[x] + 2.f * e3 * Mv[x];
+        const int ix[6][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
+        for (int q = 0; q < 6; q++) {
+            const int x = ix[q][0], y = ix[q][1];
+            B[c][q] = 2.f * e2 * M[x][y] + e3 * v[x] * v[y] + 3.f * e4 * M2[x][y];
+        }
+    }
+    const float rc = p.rc, pi_rc = 3.14159265358979f / p.rc;
+    const int ni = p.nl_count[i];
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    for (int k = lane; k < ni; k += 32) {
+        const float4 e = p.nl[(size_t)i * p.nl_cap + k];
+        const float dx = -e.x, dy = -e.y, dz = -e.z;
+        const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+        if (!(r < rc) || r == 0.f) continue;
+        float sn, cs;
+        __sincosf(pi_rc * r, &sn, &cs);
+        const float fc = 0.5f * (cs + 1.0f), dfc = -0.5f * pi_rc * sn;
+        const float ir = 1.0f / r, u[3] = {dx * ir, dy * ir, dz * ir};
+        float G[kSurNR], dG[kSurNR];
+        radial_basis(r, fc, dfc, G, dG);
+        float sr = 0.f;
+#pragma unroll
+        for (int q = 0; q < kSurNR; q++) sr += dr[q] * dG[q];
+        float h[3] = {sr * u[0], sr * u[1], sr * u[2]};
+#pragma unroll
+        for (int c = 0; c < kSurNC; c++) {
+            const float t = r - c_mu_a[c];
+            const float ex = __expf(-kSurEtaA * t * t);
+            const float gg = ex * fc, gp = ex * (-2.f * kSurEtaA * t * fc + dfc);
+            const float ua = u[0] * a[c][0] + u[1] * a[c][1] + u[2] * a[c][2];
+            const float Bu[3] = {B[c][0] * u[0] + B[c][1] * u[1] + B[c][2] * u[2],
+                                 B[c][1] * u[0] + B[c][3] * u[1] + B[c][4] * u[2],
+                                 B[c][2] * u[0] + B[c][4] * u[1] + B[c][5] * u[2]};
+            const float uBu = u[0] * Bu[0] + u[1] * Bu[1] + u[2] * Bu[2];
+            const float s1 = gp * (ua + uBu) - (gg * ir) * (ua + 2.f * uBu);
+            for (int x = 0; x < 3; x++) h[x] += s1 * u[x] + (gg * ir) * (a[c][x] + 2.f * Bu[x]);
+        }
+        // dE_i/dd_ij = h:  F_j -= h, F_i += h
+        const int j = __float_as_int(e.w) >> 6;
+        atomicAdd(&p.fsur[3 * j], -h[0]);
+        atomicAdd(&p.fsur[3 * j + 1], -h[1]);
+        atomicAdd(&p.fsur[3 * j + 2], -h[2]);
+        fx += h[0]; fy += h[1]; fz += h[2];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        fx += __shfl_xor_sync(0xffffffffu, fx, o);
+        fy += __shfl_xor_sync(0xffffffffu, fy, o);
+        fz += __shfl_xor_sync(0xffffffffu, fz, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&p.fsur[3 * i], fx);
+        atomicAdd(&p.fsur[3 * i + 1], fy);
+        atomicAdd(&p.fsur[3 * i + 2], fz);
+    }
+}
+
+// f[site] += fsur[slot] (then fsur = 0); with fout, the surrogate force is
+// written there instead (probe comparisons)
+__global__ void k_sur_apply(int n, const int *__restrict__ slot_site, float *__restrict__ fsur, double *__restrict__ f,
+                            double *__restrict__ fout) {
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= n) return;
+    const int s = slot_site[slot];
+    for (int d = 0; d < 3; d++) {
+        const float v = fsur[3 * slot + d];
+        fsur[3 * slot + d] = 0.f;
+        if (fout) fout[3 * s + d] = (double)v;
+        else f[3 * s + d] += (double)v;
+    }
+}
+
+// probe: sums of |f_a - f_b|^2 and |f_b|^2 over sites
+__global__ void k_sur_probe(int n, const double *__restrict__ fa, const double *__restrict__ fb, double *out2) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    double d2 = 0.0, b2 = 0.0;
+    if (s < n) {
+        for (int d = 0; d < 3; d++) {
+            const double x = fa[3 * s + d] - fb[3 * s + d];
+            d2 += x * x;
+            b2 += fb[3 * s + d] * fb[3 * s + d];
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        d2 += __shfl_xor_sync(0xffffffffu, d2, o);
+        b2 += __shfl_xor_sync(0xffffffffu, b2, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&out2[0], d2);
+        atomicAdd(&out2[1], b2);
+    }
+}
+
+__global__ void k_sum_sites(int n, const float *__restrict__ e, double *out) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    double v = s < n ? (double)e[s] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, v);
+}
+
+// ---------------------------------------------------------------------------
+// training (FP32 SIMT): per-site energy regression, mini-batch Adam
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t hash32(uint32_t x) {
+    x ^= x >> 16; x *= 0x7feb352du; x ^= x >> 15; x *= 0x846ca68bu; x ^= x >> 16;
+    return x;
+}
+
+// one thread per batch sample: forward, loss gradient, backward to dz1, dz2
+__global__ void k_train_fwdbwd(TrainParams t, int step) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= t.batch) return;
+    const int idx = t.fixed_batch ? b : (int)(hash32((uint32_t)(t.seed * 2654435761u) ^ hash32(step * 977 + b)) % (uint32_t)t.n);
+    const float *x = t.X + (size_t)idx * kSurNF;
+    const float *W1 = t.params, *b1 = W1 + kSurH * kSurNF, *W2 = b1 + kSurH, *b2 = W2 + kSurH * kSurH,
+                *w3 = b2 + kSurH, *b3 = w3 + kSurH;
+    float xl[kSurNF], h1[kSurH], h2[kSurH];
+    for (int k = 0; k < kSurNF; k++) xl[k] = x[k];
+    for (int o = 0; o < kSurH; o++) {
+        float z = b1[o];
+        for (int k = 0; k < kSurNF; k++) z += W1[o * kSurNF + k] * xl[k];
+        h1[o] = tanhf(z);
+    }
+    for (int o = 0; o < kSurH; o++) {
+        float z = b2[o];
+        for (int k = 0; k < kSurH; k++) z += W2[o * kSurH + k] * h1[k];
+        h2[o] = tanhf(z);
+    }
+    float E = b3[0];
+    for (int k = 0; k < kSurH; k++) E += w3[k] * h2[k];
+    const float err = E - t.y[idx];
+    const float gE = 2.f * err / (float)t.batch;      // d(mean squared error)/dE
+    float *rec = t.work + (size_t)b * (kSurNF + 4 * kSurH + 2);
+    float *rx = rec, *rh1 = rx + kSurNF, *rdz1 = rh1 + kSurH, *rh2 = rdz1 + kSurH, *rdz2 = rh2 + kSurH;
+    for (int k = 0; k < kSurNF; k++) rx[k] = xl[k];
+    float dz2[kSurH];
+    for (int o = 0; o < kSurH; o++) {
+        dz2[o] = gE * w3[o] * (1.f - h2[o] * h2[o]);
+        rh2[o] = h2[o];
+        rdz2[o] = dz2[o];
+        rh1[o] = h1[o];
+    }
+    for (int k = 0; k < kSurH; k++) {
+        float s = 0.f;
+        for (int o = 0; o < kSurH; o++) s += W2[o * kSurH + k] * dz2[o];
+        rdz1[k] = s * (1.f - h1[k] * h1[k]);
+    }
+    rec[kSurNF + 4 * kSurH] = gE;
+    rec[kSurNF + 4 * kSurH + 1] = err * err;
+}
+
+// one thread per parameter: gradient summed over the batch records
+__global__ void k_train_grad(TrainParams t) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q > kSurNParam) return;
+    const int stride = kSurNF + 4 * kSurH + 2;
+    const int oW1 = 0, ob1 = kSurH * kSurNF, oW2 = ob1 + kSurH, ob2 = oW2 + kSurH * kSurH, ow3 = ob2 + kSurH,
+              ob3 = ow3 + kSurH;
+    float s = 0.f;
+    for (int b = 0; b < t.batch; b++) {
+        const float *rec = t.work + (size_t)b * stride;
+        const float *rx = rec, *rh1 = rx + kSurNF, *rdz1 = rh1 + kSurH, *rh2 = rdz1 + kSurH, *rdz2 = rh2 + kSurH;
+        if (q < ob1) s += rdz1[q / kSurNF] * rx[q % kSurNF];
+        else if (q < oW2) s += rdz1[q - ob1];
+        else if (q < ob2) s += rdz2[(q - oW2) / kSurH] * rh1[(q - oW2) % kSurH];
+        else if (q < ow3) s += rdz2[q - ob2];
+        else if (q < ob3) s += rec[kSurNF + 4 * kSurH] * rh2[q - ow3];
+        else if (q == ob3) s += rec[kSurNF + 4 * kSurH];
+        else s += rec[kSurNF + 4 * kSurH + 1];   // q == kSurNParam: the batch's summed squared error
+    }
+    t.grad[q] = s;
+}
+
+__global__ void k_train_adam(TrainParams t, int step) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= kSurNParam) return;
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    const float g = t.grad[q];
+    const float m = t.m[q] = b1 * t.m[q] + (1.f - b1) * g;
+    const float v = t.v[q] = b2 * t.v[q] + (1.f - b2) * g * g;
+    const float mh = m / (1.f - powf(b1, (float)(step + 1))), vh = v / (1.f - powf(b2, (float)(step + 1)));
+    t.params[q] -= t.lr * mh / (sqrtf(vh) + eps);
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+void launch_sur_desc(SurParams &p, cudaStream_t st) { k_sur_desc<<<(p.n + 7) / 8, 256, 0, st>>>(p); }
+void launch_sur_mlp(SurParams &p, cudaStream_t st) {
+    const int tiles = (p.n + 15) / 16;
+    int blocks = (tiles + 3) / 4;
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    k_sur_mlp<<<blocks, 128, 0, st>>>(p);
+}
+void launch_sur_force(SurParams &p, cudaStream_t st) { k_sur_force<<<(p.n + 7) / 8, 256, 0, st>>>(p); }
+void launch_sur_apply(SurParams &p, const int *slot_site, double *f, double *fout, cudaStream_t st) {
+    k_sur_apply<<<(p.n + 255) / 256, 256, 0, st>>>(p.n, slot_site, p.fsur, f, fout);
+}
+void launch_sur_probe(int n, const double *fa, const double *fb, double *out2, cudaStream_t st) {
+    k_sur_probe<<<(n + 255) / 256, 256, 0, st>>>(n, fa, fb, out2);
+}
+void launch_sum_sites(int n, const float *e, double *out, cudaStream_t st) {
+    k_sum_sites<<<(n + 255) / 256, 256, 0, st>>>(n, e, out);
+}
+void launch_train_step(TrainParams &t, int step, cudaStream_t st) {
+    k_train_fwdbwd<<<(t.batch + 127) / 128, 128, 0, st>>>(t, step);
+    k_train_grad<<<(kSurNParam + 1 + 127) / 128, 128, 0, st>>>(t);
+    if (!t.grad_only) k_train_adam<<<(kSurNParam + 127) / 128, 128, 0, st>>>(t, step);
+}
+
+}  // namespace komd

@@ -1,0 +1,52 @@
+// surrogate.cuh -- parameters of the learned three-body term (surrogate.cu).
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace komd {
+
+constexpr int kSurNR = 16;       // radial Gaussians
+constexpr int kSurNC = 4;        // angular channels (4 invariants each)
+constexpr int kSurNF = 32;       // features
+constexpr int kSurH = 64;        // hidden width
+constexpr int kSurNParam = kSurH * kSurNF + kSurH + kSurH * kSurH + kSurH + kSurH + 1;
+constexpr float kSurEtaR = 50.0f;
+constexpr float kSurEtaA = 22.222222f;   // 1 / (2 * 0.15^2)
+
+struct SurParams {
+    int n;
+    float rc;
+    const float4 *nl;            // ATM neighbour list (r_i - r_j, code)
+    const int *nl_count;
+    int nl_cap;
+    const float *fmean, *fstd;   // fstd == nullptr: raw features (training samples)
+    float *x;                    // n x 32 features
+    float *mom;                  // n x 36 moments (M1 3 + M2 6 per channel)
+    float *dedx;                 // n x 32 dE/dx
+    float *e_site;               // n per-site energies (physical units)
+    float *fsur;                 // n x 3 surrogate forces (slot order, accumulated)
+    const __nv_bfloat16 *w1, *w1t, *w2, *w2t;
+    const float *b1, *b2, *w3;
+    float b3, e_scale, e_shift;
+};
+
+struct TrainParams {
+    const float *X, *y;
+    int n, batch;
+    float *params, *grad, *m, *v, *work;
+    float lr;
+    uint32_t seed;
+    int fixed_batch;             // 1: the batch is samples 0..batch-1 (gradient checks)
+    int grad_only;
+};
+
+void launch_sur_desc(SurParams &p, cudaStream_t st);
+void launch_sur_mlp(SurParams &p, cudaStream_t st);
+void launch_sur_force(SurParams &p, cudaStream_t st);
+void launch_sur_apply(SurParams &p, const int *slot_site, double *f, double *fout, cudaStream_t st);
+void launch_sur_probe(int n, const double *fa, const double *fb, double *out2, cudaStream_t st);
+void launch_sum_sites(int n, const float *e, double *out, cudaStream_t st);
+void launch_train_step(TrainParams &t, int step, cudaStream_t st);
+
+}  // namespace komd

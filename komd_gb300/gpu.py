@@ -22,7 +22,8 @@ ATM_SIGN_REFERENCE, ATM_SIGN_PHYSICAL = 0, 1
 ATM_ENUM_COMPAT, ATM_ENUM_FULL = 0, 1
 VIRIAL_COMPAT, VIRIAL_CORRECT = 0, 1
 
-TERM_LJ, TERM_FENE, TERM_LIMIT, TERM_ATM, TERM_BONDED = 0x01, 0x02, 0x04, 0x08, 0x10
+TERM_LJ, TERM_FENE, TERM_LIMIT, TERM_ATM, TERM_BONDED, TERM_ATM_SURROGATE = 0x01, 0x02, 0x04, 0x08, 0x10, 0x20
+SUR_NFEAT, SUR_NPARAM = 32, 6337
 MEASURE_TEMPERATURE, MEASURE_ENERGY, MEASURE_PRESSURE, MEASURE_RDF, MEASURE_LJ_HIST = 0x01, 0x02, 0x04, 0x08, 0x10
 
 EXPORTS = [
@@ -31,7 +32,9 @@ EXPORTS = [
     "komd_gpu_download", "komd_gpu_num_sites", "komd_gpu_update_container", "komd_gpu_forces",
     "komd_gpu_integrate0", "komd_gpu_integrate1", "komd_gpu_step", "komd_gpu_step_host", "komd_gpu_measure",
     "komd_gpu_rdf_bins", "komd_gpu_get_cells", "komd_gpu_neighbour_counts", "komd_gpu_set_profiling",
-    "komd_gpu_profile", "komd_gpu_kernels_per_step", "komd_gpu_atm_forces_noalloc",
+    "komd_gpu_profile", "komd_gpu_kernels_per_step", "komd_gpu_atm_forces_noalloc", "komd_gpu_surrogate_load",
+    "komd_gpu_surrogate_sample", "komd_gpu_surrogate_forces", "komd_gpu_surrogate_status", "komd_mlp_train",
+    "komd_mlp_loss_grad",
 ]
 
 
@@ -53,6 +56,11 @@ class Observables(C.Structure):
         ("u_atm", C.c_double), ("u_bonded", C.c_double), ("kinetic", C.c_double * 6), ("virial", C.c_double * 6),
         ("pressure", C.c_double * 6), ("pairs_in_cutoff", C.c_int64), ("triplets", C.c_int64),
     ]
+
+
+class SurrogateStatus(C.Structure):
+    _fields_ = [("steps", C.c_int64), ("probes", C.c_int64), ("last_rmse", C.c_double), ("max_rmse", C.c_double),
+                ("fallback", C.c_int32), ("fallback_step", C.c_int64)]
 
 
 class KomdError(RuntimeError):
@@ -102,6 +110,12 @@ def load() -> C.CDLL:
     L.komd_gpu_profile.argtypes = [P, I32, P, P, C.c_char_p, I32]
     L.komd_gpu_kernels_per_step.argtypes = [P]
     L.komd_gpu_atm_forces_noalloc.argtypes = [I64, P, P, P, P, C.c_double, C.c_double, C.c_int32, P]
+    L.komd_gpu_surrogate_load.argtypes = [P, P, P, P, C.c_double, C.c_double, C.c_int32, C.c_double]
+    L.komd_gpu_surrogate_sample.argtypes = [P, P, P, P]
+    L.komd_gpu_surrogate_forces.argtypes = [P, P, P]
+    L.komd_gpu_surrogate_status.argtypes = [P, C.POINTER(SurrogateStatus)]
+    L.komd_mlp_train.argtypes = [P, P, I64, P, C.c_int32, C.c_int32, C.c_float, C.c_uint64, P]
+    L.komd_mlp_loss_grad.argtypes = [P, P, I64, P, P, P]
     _lib = L
     return L
 
@@ -252,3 +266,55 @@ class GpuSystem:
 
     def kernels_per_step(self) -> int:
         return int(self.L.komd_gpu_kernels_per_step(self.h))
+
+    # --- learned three-body term ------------------------------------------
+    def surrogate_load(self, model, probe_every=50, probe_threshold=0.05):
+        p = np.ascontiguousarray(model["params"], np.float32)
+        fm = np.ascontiguousarray(model["fmean"], np.float32)
+        fs = np.ascontiguousarray(model["fstd"], np.float32)
+        self._sur_keep = (p, fm, fs)
+        self._check(self.L.komd_gpu_surrogate_load(self.h, _p(p), _p(fm), _p(fs), float(model["e_scale"]),
+                                                   float(model["e_shift"]), int(probe_every), float(probe_threshold)))
+
+    def surrogate_sample(self):
+        x = np.zeros((self.n, SUR_NFEAT), np.float32)
+        e3 = np.zeros(self.n)
+        f3 = np.zeros((self.n, 3))
+        self._check(self.L.komd_gpu_surrogate_sample(self.h, _p(x), _p(e3), _p(f3)))
+        return x, e3, f3
+
+    def surrogate_forces(self):
+        f3 = np.zeros((self.n, 3))
+        e3 = np.zeros(self.n)
+        self._check(self.L.komd_gpu_surrogate_forces(self.h, _p(f3), _p(e3)))
+        return f3, e3
+
+    def surrogate_status(self):
+        st = SurrogateStatus()
+        self._check(self.L.komd_gpu_surrogate_status(self.h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in SurrogateStatus._fields_}
+
+
+def mlp_train(X, y, params, epochs, batch=1024, lr=2e-3, seed=0):
+    L = load()
+    X = np.ascontiguousarray(X, np.float32)
+    y = np.ascontiguousarray(y, np.float32)
+    p = np.ascontiguousarray(params, np.float32).copy()
+    loss = np.zeros(max(epochs, 1), np.float32)
+    rc = L.komd_mlp_train(_p(X), _p(y), X.shape[0], _p(p), int(epochs), int(batch), float(lr), int(seed), _p(loss))
+    if rc != KOMD_OK:
+        raise KomdError(rc, L.komd_gpu_last_error().decode())
+    return p, loss[:epochs]
+
+
+def mlp_loss_grad(X, y, params):
+    L = load()
+    X = np.ascontiguousarray(X, np.float32)
+    y = np.ascontiguousarray(y, np.float32)
+    p = np.ascontiguousarray(params, np.float32)
+    g = np.zeros(SUR_NPARAM, np.float32)
+    loss = np.zeros(1, np.float32)
+    rc = L.komd_mlp_loss_grad(_p(X), _p(y), X.shape[0], _p(p), _p(g), _p(loss))
+    if rc != KOMD_OK:
+        raise KomdError(rc, L.komd_gpu_last_error().decode())
+    return g, float(loss[0])

@@ -905,3 +905,224 @@ void kor_rdf(int64_t n, const double *com, const double L[3], double max_r, doub
         }
     }
 }
+
+/* ------------------------------------------------------------------------ */
+/* three-body surrogate (no reference counterpart)                          */
+/* ------------------------------------------------------------------------ */
+static const double SUR_PI = 3.14159265358979323846;
+static const double SUR_ETA_R = 50.0;
+static const double SUR_ETA_A = 22.222222222222222;   /* 1 / (2 * 0.15^2) */
+static const double SUR_MU_C[KOR_SUR_NC] = {1.05, 1.30, 1.55, 1.80};
+static double sur_mu_r(int k) { return 0.85 + k * (1.15 / 15.0); }
+
+typedef struct { double G[KOR_SUR_NR]; double M1[KOR_SUR_NC][3]; double M2[KOR_SUR_NC][3][3]; } sur_acc;
+
+static void sur_accumulate(int n_nb, const double *d, double rc, sur_acc *a) {
+    memset(a, 0, sizeof(*a));
+    for (int j = 0; j < n_nb; j++) {
+        const double *dj = d + 3 * j;
+        const double r = sqrt(dj[0] * dj[0] + dj[1] * dj[1] + dj[2] * dj[2]);
+        if (!(r < rc) || r == 0.0) continue;
+        const double fc = 0.5 * (cos(SUR_PI * r / rc) + 1.0);
+        const double u[3] = {dj[0] / r, dj[1] / r, dj[2] / r};
+        for (int k = 0; k < KOR_SUR_NR; k++) {
+            const double t = r - sur_mu_r(k);
+            a->G[k] += exp(-SUR_ETA_R * t * t) * fc;
+        }
+        for (int c = 0; c < KOR_SUR_NC; c++) {
+            const double t = r - SUR_MU_C[c];
+            const double g = exp(-SUR_ETA_A * t * t) * fc;
+            for (int p = 0; p < 3; p++) {
+                a->M1[c][p] += g * u[p];
+                for (int q = 0; q < 3; q++) a->M2[c][p][q] += g * u[p] * u[q];
+            }
+        }
+    }
+}
+
+static void mat3_mul(const double A[3][3], const double B[3][3], double C[3][3]) {
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            double s = 0;
+            for (int k = 0; k < 3; k++) s += A[i][k] * B[k][j];
+            C[i][j] = s;
+        }
+}
+
+static void sur_invariants(const sur_acc *a, double *raw) {
+    for (int k = 0; k < KOR_SUR_NR; k++) raw[k] = a->G[k];
+    for (int c = 0; c < KOR_SUR_NC; c++) {
+        const double *m1 = a->M1[c];
+        double M2m1[3], M22[3][3], M23[3][3];
+        for (int p = 0; p < 3; p++) M2m1[p] = a->M2[c][p][0] * m1[0] + a->M2[c][p][1] * m1[1] + a->M2[c][p][2] * m1[2];
+        mat3_mul(a->M2[c], a->M2[c], M22);
+        mat3_mul(M22, a->M2[c], M23);
+        double i2 = 0;
+        for (int p = 0; p < 3; p++) for (int q = 0; q < 3; q++) i2 += a->M2[c][p][q] * a->M2[c][p][q];
+        raw[KOR_SUR_NR + c] = m1[0] * m1[0] + m1[1] * m1[1] + m1[2] * m1[2];
+        raw[KOR_SUR_NR + KOR_SUR_NC + c] = i2;
+        raw[KOR_SUR_NR + 2 * KOR_SUR_NC + c] = m1[0] * M2m1[0] + m1[1] * M2m1[1] + m1[2] * M2m1[2];
+        raw[KOR_SUR_NR + 3 * KOR_SUR_NC + c] = M23[0][0] + M23[1][1] + M23[2][2];
+    }
+}
+
+void kor_sur_features(int n_nb, const double *d, double rc, double *raw) {
+    sur_acc a;
+    sur_accumulate(n_nb, d, rc, &a);
+    sur_invariants(&a, raw);
+}
+
+double kor_sur_mlp(const double *P, const double *x, double *dE_dx) {
+    const int H = KOR_SUR_H, F = KOR_SUR_NF;
+    const double *W1 = P, *b1 = W1 + H * F, *W2 = b1 + H, *b2 = W2 + H * H, *w3 = b2 + H, *b3 = w3 + H;
+    double h1[KOR_SUR_H], h2[KOR_SUR_H];
+    for (int o = 0; o < H; o++) {
+        double z = b1[o];
+        for (int i = 0; i < F; i++) z += W1[o * F + i] * x[i];
+        h1[o] = tanh(z);
+    }
+    for (int o = 0; o < H; o++) {
+        double z = b2[o];
+        for (int i = 0; i < H; i++) z += W2[o * H + i] * h1[i];
+        h2[o] = tanh(z);
+    }
+    double E = b3[0];
+    for (int i = 0; i < H; i++) E += w3[i] * h2[i];
+    if (dE_dx) {
+        double dz2[KOR_SUR_H], dz1[KOR_SUR_H];
+        for (int o = 0; o < H; o++) dz2[o] = w3[o] * (1.0 - h2[o] * h2[o]);
+        for (int i = 0; i < H; i++) {
+            double s = 0;
+            for (int o = 0; o < H; o++) s += W2[o * H + i] * dz2[o];
+            dz1[i] = s * (1.0 - h1[i] * h1[i]);
+        }
+        for (int i = 0; i < F; i++) {
+            double s = 0;
+            for (int o = 0; o < H; o++) s += W1[o * F + i] * dz1[o];
+            dE_dx[i] = s;
+        }
+    }
+    return E;
+}
+
+void kor_sur_mlp_param_grad(const double *P, const double *x, double *G) {
+    const int H = KOR_SUR_H, F = KOR_SUR_NF;
+    const double *W1 = P, *b1 = W1 + H * F, *W2 = b1 + H, *b2 = W2 + H * H, *w3 = b2 + H;
+    double *gW1 = G, *gb1 = gW1 + H * F, *gW2 = gb1 + H, *gb2 = gW2 + H * H, *gw3 = gb2 + H, *gb3 = gw3 + H;
+    double h1[KOR_SUR_H], h2[KOR_SUR_H], dz1[KOR_SUR_H], dz2[KOR_SUR_H];
+    for (int o = 0; o < H; o++) {
+        double z = b1[o];
+        for (int i = 0; i < F; i++) z += W1[o * F + i] * x[i];
+        h1[o] = tanh(z);
+    }
+    for (int o = 0; o < H; o++) {
+        double z = b2[o];
+        for (int i = 0; i < H; i++) z += W2[o * H + i] * h1[i];
+        h2[o] = tanh(z);
+    }
+    for (int o = 0; o < H; o++) dz2[o] = w3[o] * (1.0 - h2[o] * h2[o]);
+    for (int i = 0; i < H; i++) {
+        double s = 0;
+        for (int o = 0; o < H; o++) s += W2[o * H + i] * dz2[o];
+        dz1[i] = s * (1.0 - h1[i] * h1[i]);
+    }
+    for (int o = 0; o < H; o++) {
+        for (int i = 0; i < F; i++) gW1[o * F + i] = dz1[o] * x[i];
+        gb1[o] = dz1[o];
+        for (int i = 0; i < H; i++) gW2[o * H + i] = dz2[o] * h1[i];
+        gb2[o] = dz2[o];
+        gw3[o] = h2[o];
+    }
+    gb3[0] = 1.0;
+}
+
+double kor_sur_energy_forces(int64_t n, const double *r, const double L[3], double rc, const double *params,
+                             const double *fmean, const double *fstd, double e_scale, double e_shift,
+                             double *e_site, double *f) {
+    double etot = 0;
+    int cap = 256;
+    double *d = (double *)malloc(sizeof(double) * 3 * (size_t)cap);
+    int64_t *jj = (int64_t *)malloc(sizeof(int64_t) * (size_t)cap);
+    memset(f, 0, sizeof(double) * 3 * (size_t)n);
+    for (int64_t i = 0; i < n; i++) {
+        int nn = 0;
+        for (int64_t j = 0; j < n; j++) {
+            if (j == i) continue;
+            double v[3];
+            for (int k = 0; k < 3; k++) {
+                v[k] = r[3 * j + k] - r[3 * i + k];
+                v[k] -= L[k] * round(v[k] / L[k]);
+            }
+            const double q = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+            if (!(q < rc * rc)) continue;
+            if (nn == cap) {
+                cap *= 2;
+                d = (double *)realloc(d, sizeof(double) * 3 * (size_t)cap);
+                jj = (int64_t *)realloc(jj, sizeof(int64_t) * (size_t)cap);
+            }
+            memcpy(d + 3 * nn, v, sizeof(v));
+            jj[nn++] = j;
+        }
+        sur_acc a;
+        sur_accumulate(nn, d, rc, &a);
+        double raw[KOR_SUR_NF], x[KOR_SUR_NF], dx[KOR_SUR_NF];
+        sur_invariants(&a, raw);
+        for (int k = 0; k < KOR_SUR_NF; k++) x[k] = (raw[k] - fmean[k]) / fstd[k];
+        const double e = e_scale * kor_sur_mlp(params, x, dx) + e_shift;
+        if (e_site) e_site[i] = e;
+        etot += e;
+        double dr[KOR_SUR_NF];   /* dE_i / d raw */
+        for (int k = 0; k < KOR_SUR_NF; k++) dr[k] = e_scale * dx[k] / fstd[k];
+        /* coefficients of the angular chain: a_c = dE/dM1_c, B_c = dE/dM2_c */
+        double ac[KOR_SUR_NC][3], Bc[KOR_SUR_NC][3][3];
+        for (int c = 0; c < KOR_SUR_NC; c++) {
+            const double e1 = dr[KOR_SUR_NR + c], e2 = dr[KOR_SUR_NR + KOR_SUR_NC + c];
+            const double e3 = dr[KOR_SUR_NR + 2 * KOR_SUR_NC + c], e4 = dr[KOR_SUR_NR + 3 * KOR_SUR_NC + c];
+            double M22[3][3];
+            mat3_mul(a.M2[c], a.M2[c], M22);
+            for (int p = 0; p < 3; p++) {
+                double m2m1 = 0;
+                for (int q = 0; q < 3; q++) m2m1 += a.M2[c][p][q] * a.M1[c][q];
+                ac[c][p] = 2.0 * e1 * a.M1[c][p] + 2.0 * e3 * m2m1;
+                for (int q = 0; q < 3; q++)
+                    Bc[c][p][q] = 2.0 * e2 * a.M2[c][p][q] + e3 * a.M1[c][p] * a.M1[c][q] + 3.0 * e4 * M22[p][q];
+            }
+        }
+        for (int t = 0; t < nn; t++) {
+            const double *dj = d + 3 * t;
+            const double rr = sqrt(dj[0] * dj[0] + dj[1] * dj[1] + dj[2] * dj[2]);
+            if (!(rr < rc) || rr == 0.0) continue;
+            const double u[3] = {dj[0] / rr, dj[1] / rr, dj[2] / rr};
+            const double fc = 0.5 * (cos(SUR_PI * rr / rc) + 1.0);
+            const double dfc = -0.5 * (SUR_PI / rc) * sin(SUR_PI * rr / rc);
+            double hvec[3] = {0, 0, 0};   /* dE_i / d d_ij */
+            double sr = 0;
+            for (int k = 0; k < KOR_SUR_NR; k++) {
+                const double tt = rr - sur_mu_r(k);
+                const double ex = exp(-SUR_ETA_R * tt * tt);
+                sr += dr[k] * ex * (-2.0 * SUR_ETA_R * tt * fc + dfc);
+            }
+            for (int p = 0; p < 3; p++) hvec[p] += sr * u[p];
+            for (int c = 0; c < KOR_SUR_NC; c++) {
+                const double tt = rr - SUR_MU_C[c];
+                const double ex = exp(-SUR_ETA_A * tt * tt);
+                const double g = ex * fc, gp = ex * (-2.0 * SUR_ETA_A * tt * fc + dfc);
+                const double ua = u[0] * ac[c][0] + u[1] * ac[c][1] + u[2] * ac[c][2];
+                double Bu[3];
+                for (int p = 0; p < 3; p++) Bu[p] = Bc[c][p][0] * u[0] + Bc[c][p][1] * u[1] + Bc[c][p][2] * u[2];
+                const double uBu = u[0] * Bu[0] + u[1] * Bu[1] + u[2] * Bu[2];
+                for (int p = 0; p < 3; p++)
+                    hvec[p] += gp * ua * u[p] + (g / rr) * (ac[c][p] - ua * u[p]) + gp * uBu * u[p] +
+                               (2.0 * g / rr) * (Bu[p] - uBu * u[p]);
+            }
+            const int64_t j = jj[t];
+            for (int p = 0; p < 3; p++) {
+                f[3 * j + p] -= hvec[p];
+                f[3 * i + p] += hvec[p];
+            }
+        }
+    }
+    free(d);
+    free(jj);
+    return etot;
+}

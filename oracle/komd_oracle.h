@@ -180,6 +180,39 @@ void kor_rdf(int64_t n_mol, const double *com_mol, const double L[3], double max
 /* Pressure-to-Pa conversion factor of PressureSensor::write (PressureSensor.cpp:49-51). */
 double kor_pressure_factor(void);
 
+
+/* ------------------------------------------------------------------------ */
+/* Three-body surrogate (no reference counterpart): per-site descriptors, the */
+/* 32-64-64-1 tanh MLP and the analytic forces, all in FP64.  Restates the   */
+/* definition the CUDA kernels implement; parity is against this code and   */
+/* finite differences (the reference has no surrogate).                      */
+/* ------------------------------------------------------------------------ */
+#define KOR_SUR_NR 16      /* radial Gaussians                       */
+#define KOR_SUR_NC 4       /* angular channels (x4 invariants)       */
+#define KOR_SUR_NF 32      /* features                               */
+#define KOR_SUR_H 64       /* hidden width                           */
+/* number of MLP parameters: W1 (64x32) b1 (64) W2 (64x64) b2 (64) w3 (64) b3 (1) */
+#define KOR_SUR_NPARAM (KOR_SUR_H * KOR_SUR_NF + KOR_SUR_H + KOR_SUR_H * KOR_SUR_H + KOR_SUR_H + KOR_SUR_H + 1)
+
+/* Raw features of one site from its neighbour vectors d_j = r_j - r_i
+ * (n_nb x 3) inside rc: G_k = sum_j exp(-eta_r (r - mu_k)^2) fc(r), and per
+ * channel c with g_c = exp(-eta_a (r - mu_c)^2) fc(r), M1 = sum g u,
+ * M2 = sum g u u^T: I1 = |M1|^2, I2 = M2:M2, I3 = M1.M2.M1, I4 = tr(M2^3).
+ * fc(r) = (cos(pi r / rc) + 1) / 2.  Feature order: G_0..15, I1_0..3,
+ * I2_0..3, I3_0..3, I4_0..3. */
+void kor_sur_features(int n_nb, const double *d, double rc, double *raw);
+/* MLP on standardised features x = (raw - mean) / std: returns E (scaled
+ * units) and, if dE_dx != NULL, dE/dx.  params layout as KOR_SUR_NPARAM. */
+double kor_sur_mlp(const double *params, const double *x, double *dE_dx);
+/* Gradient of the MLP output with respect to the parameters (same layout). */
+void kor_sur_mlp_param_grad(const double *params, const double *x, double *grad);
+/* Per-site energy E_i = e_scale * MLP(x_i) + e_shift and forces
+ * F = -grad sum_i E_i for a periodic system, neighbour lists by all pairs
+ * with the minimum image (small systems).  Returns the total energy. */
+double kor_sur_energy_forces(int64_t n, const double *r, const double L[3], double rc, const double *params,
+                             const double *fmean, const double *fstd, double e_scale, double e_shift,
+                             double *e_site, double *f);
+
 /* Threads used by the OpenMP loops (1 when built without OpenMP). */
 int kor_num_threads(void);
 void kor_set_num_threads(int n);

@@ -272,3 +272,56 @@ def atm_energy(nu, a, b, c):
 
 def pressure_factor():
     return lib().kor_pressure_factor()
+
+
+# --- three-body surrogate (no reference counterpart) ------------------------
+SUR_NF, SUR_H = 32, 64
+SUR_NPARAM = SUR_H * SUR_NF + SUR_H + SUR_H * SUR_H + SUR_H + SUR_H + 1
+
+
+def _sur_lib():
+    L = lib()
+    if not getattr(L, "_sur", False):
+        L.kor_sur_features.argtypes = [C.c_int, P, D, P]
+        L.kor_sur_mlp.argtypes = [P, P, P]
+        L.kor_sur_mlp.restype = D
+        L.kor_sur_mlp_param_grad.argtypes = [P, P, P]
+        L.kor_sur_energy_forces.argtypes = [I64, P, P, D, P, P, P, D, D, P, P]
+        L.kor_sur_energy_forces.restype = D
+        L._sur = True
+    return L
+
+
+def sur_features(d, rc=2.0):
+    d = np.ascontiguousarray(d, np.float64).reshape(-1, 3)
+    raw = np.zeros(SUR_NF)
+    _sur_lib().kor_sur_features(d.shape[0], _p(d), rc, _p(raw))
+    return raw
+
+
+def sur_mlp(params, x):
+    params = np.ascontiguousarray(params, np.float64)
+    x = np.ascontiguousarray(x, np.float64)
+    dx = np.zeros(SUR_NF)
+    e = _sur_lib().kor_sur_mlp(_p(params), _p(x), _p(dx))
+    return e, dx
+
+
+def sur_mlp_param_grad(params, x):
+    params = np.ascontiguousarray(params, np.float64)
+    x = np.ascontiguousarray(x, np.float64)
+    g = np.zeros(SUR_NPARAM)
+    _sur_lib().kor_sur_mlp_param_grad(_p(params), _p(x), _p(g))
+    return g
+
+
+def sur_energy_forces(r, box, params, fmean, fstd, e_scale, e_shift, rc=2.0):
+    r = np.ascontiguousarray(r, np.float64)
+    n = r.shape[0]
+    box = np.ascontiguousarray(box, np.float64)
+    e = np.zeros(n)
+    f = np.zeros((n, 3))
+    et = _sur_lib().kor_sur_energy_forces(n, _p(r), _p(box), rc, _p(np.ascontiguousarray(params, np.float64)),
+                                          _p(np.ascontiguousarray(fmean, np.float64)),
+                                          _p(np.ascontiguousarray(fstd, np.float64)), e_scale, e_shift, _p(e), _p(f))
+    return et, e, f

@@ -134,3 +134,33 @@ def test_oracle_atm_force_is_gradient(oracle_lib, sign):
             grad = (e[0] - e[1]) / (2 * h)
             expect = -grad if sign == "physical" else grad
             assert o.f[atom, d] == pytest.approx(expect, rel=1e-6, abs=1e-9)
+
+
+def test_oracle_surrogate_is_consistent(oracle_lib):
+    """The FP64 surrogate restatement: forces are -grad of its energy, the
+    parameter gradient matches finite differences, and forces sum to zero."""
+    from komd_gb300 import lattice
+    rng = np.random.default_rng(0)
+    params = rng.normal(0, 0.3, oracle_lib.SUR_NPARAM)
+    s = lattice.argon_fcc(3, rho=0.8442, seed=2, jitter=0.1)
+    fm, fs = np.zeros(32), np.ones(32)
+    et, e, f = oracle_lib.sur_energy_forces(s.r, s.box, params, fm, fs, 0.1, 0.2)
+    assert et == pytest.approx(e.sum())
+    h = 1e-6
+    for a, d in ((0, 0), (5, 1), (17, 2)):
+        rp, rm = s.r.copy(), s.r.copy()
+        rp[a, d] += h
+        rm[a, d] -= h
+        fd = -(oracle_lib.sur_energy_forces(rp, s.box, params, fm, fs, 0.1, 0.2)[0] -
+               oracle_lib.sur_energy_forces(rm, s.box, params, fm, fs, 0.1, 0.2)[0]) / (2 * h)
+        assert f[a, d] == pytest.approx(fd, rel=1e-6, abs=1e-9)
+    assert np.abs(f.sum(0)).max() < 1e-12
+    x = rng.normal(0, 1, 32)
+    g = oracle_lib.sur_mlp_param_grad(params, x)
+    for k in (0, 100, 2100, 6300, oracle_lib.SUR_NPARAM - 1):
+        p2 = params.copy()
+        p2[k] += 1e-6
+        e1, _ = oracle_lib.sur_mlp(p2, x)
+        p2[k] -= 2e-6
+        e2, _ = oracle_lib.sur_mlp(p2, x)
+        assert g[k] == pytest.approx((e1 - e2) / 2e-6, rel=1e-5, abs=1e-8)
