@@ -216,6 +216,40 @@ int  komd_mlp_train(const float *X, const float *y, int64_t n, float *params, in
  * respect to the parameters, from the same kernels komd_mlp_train runs. */
 int  komd_mlp_loss_grad(const float *X, const float *y, int64_t n, const float *params, float *grad, float *loss);
 
+/* Force-matched training.  A dataset on the device holds snapshots that
+ * the exact kernel produced: per site the ATM neighbour list, raw features,
+ * moments, exact per-site energy and exact three-body force (slot order of
+ * the capturing engine, all snapshots with one site count and one
+ * cutoff_3b).  nl_cap bounds the neighbours kept per site. */
+typedef struct komd_sur_data komd_sur_data;
+int     komd_sur_data_create(int32_t device, int32_t nl_cap, komd_sur_data **out);
+void    komd_sur_data_destroy(komd_sur_data *d);
+/* Appends the engine's current state (after update_container) as a snapshot. */
+int     komd_gpu_surrogate_capture(komd_gpu *h, komd_sur_data *d);
+int64_t komd_sur_data_snapshots(const komd_sur_data *d);
+int32_t komd_sur_data_sites(const komd_sur_data *d);   /* sites per snapshot */
+/* Host copies of one snapshot (snap >= 0) or of all (snap < 0), slot order:
+ * raw features (32 per site), energies, forces (3 per site), site ids. */
+int     komd_sur_data_get(komd_sur_data *d, int64_t snap, float *features, float *e3, float *f3, int32_t *site);
+typedef struct komd_sur_fit_opts {
+    int32_t epochs;            /* passes over the snapshots                         */
+    int32_t snaps_per_batch;   /* snapshots per Adam step                           */
+    float lr, lr_end;          /* learning rate, decayed geometrically to lr_end    */
+    float lam_e, lam_f;        /* weights of the energy and force terms             */
+    uint64_t seed;             /* snapshot shuffling                                */
+} komd_sur_fit_opts;
+/* Minimises lam_e * mean (E - (e3 - e_shift)/e_scale)^2
+ *         + lam_f * mean |F - F_exact|^2 / f2      (per site, f2 = <|F_exact|^2>)
+ * over the parameters (in/out) with Adam; loss (2*epochs floats, may be
+ * NULL) gets each epoch's mean energy and force terms. */
+int     komd_sur_fit(komd_sur_data *d, float *params, const float *fmean, const float *fstd, double e_scale,
+                     double e_shift, double f2, const komd_sur_fit_opts *opts, float *loss);
+/* Gradient (and the two loss terms) over all snapshots as one batch, from
+ * the kernels komd_sur_fit runs. */
+int     komd_sur_fit_grad(komd_sur_data *d, const float *params, const float *fmean, const float *fstd,
+                          double e_scale, double e_shift, double f2, float lam_e, float lam_f, float *grad,
+                          double *loss);
+
 /* ---- profiling ---------------------------------------------------------- */
 /* When enabled, every kernel launch outside komd_gpu_step's graph is
  * bracketed by CUDA events; komd_gpu_profile reports per kernel family the

@@ -26,7 +26,7 @@ INC = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-I" + INC, "-I" + CSRC]
-GPU_SOURCES = ["kernels.cu", "pair_tile.cu", "surrogate.cu", "capi.cu", "noalloc.cu"]
+GPU_SOURCES = ["kernels.cu", "pair_tile.cu", "surrogate.cu", "sur_train.cu", "capi.cu", "noalloc.cu"]
 
 LIB_GPU = os.path.join(OUT, "libkomd_gpu.so")
 LIB_HOST = os.path.join(OUT, "libkomd_host.so")

@@ -1,5 +1,6 @@
 // capi.cu -- the C ABI of include/komd_gpu.h: engine lifetime, buffers,
 // the per-step launch sequence, CUDA-graph replay, sensors and parity dumps.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1109,6 +1110,253 @@ int komd_mlp_loss_grad(const float *X, const float *y, int64_t n, const float *p
     CK(cudaMemcpy(g.data(), b.grad, sizeof(float) * g.size(), cudaMemcpyDeviceToHost));
     std::memcpy(grad, g.data(), sizeof(float) * kSurNParam);
     if (loss) *loss = g[kSurNParam] / (float)n;
+    return KOMD_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// force-matched training: snapshot dataset on the device (sur_train.cu)
+// ---------------------------------------------------------------------------
+struct komd_sur_data {
+    int device = 0;
+    int cap = 0, n_site = 0;
+    float rc = 0.f;
+    int64_t n_snap = 0, snap_cap = 0;
+    float4 *nl = nullptr;
+    int *count = nullptr, *site = nullptr, *err = nullptr;
+    float *x = nullptr, *mom = nullptr, *e3 = nullptr, *f3 = nullptr;
+    ~komd_sur_data() {
+        cudaSetDevice(device);
+        dfree(nl); dfree(count); dfree(site); dfree(err); dfree(x); dfree(mom); dfree(e3); dfree(f3);
+    }
+};
+
+namespace {
+template <typename T>
+cudaError_t dgrow(T *&p, size_t old_count, size_t new_count) {
+    T *q = nullptr;
+    cudaError_t rc = cudaMalloc(reinterpret_cast<void **>(&q), sizeof(T) * new_count);
+    if (rc != cudaSuccess) return rc;
+    if (p && old_count) rc = cudaMemcpy(q, p, sizeof(T) * old_count, cudaMemcpyDeviceToDevice);
+    if (p) cudaFree(p);
+    p = q;
+    return rc;
+}
+
+int data_reserve(komd_sur_data *d, int64_t snaps) {
+    if (snaps <= d->snap_cap) return KOMD_OK;
+    const int64_t cap = std::max<int64_t>(snaps, 2 * d->snap_cap);
+    const size_t o = (size_t)d->snap_cap * d->n_site, n = (size_t)cap * d->n_site;
+    CK(dgrow(d->nl, o * d->cap, n * d->cap));
+    CK(dgrow(d->count, o, n)); CK(dgrow(d->site, o, n));
+    CK(dgrow(d->x, o * kSurNF, n * kSurNF)); CK(dgrow(d->mom, o * kSurNC * 9, n * kSurNC * 9));
+    CK(dgrow(d->e3, o, n)); CK(dgrow(d->f3, 3 * o, 3 * n));
+    d->snap_cap = cap;
+    return KOMD_OK;
+}
+
+struct FitBuffers {
+    int *snaps = nullptr;
+    float *params = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr, *fmean = nullptr, *fstd = nullptr;
+    float *E = nullptr, *g = nullptr, *fs = nullptr, *w = nullptr, *rec = nullptr;
+    double *loss = nullptr;
+    ~FitBuffers() {
+        dfree(snaps); dfree(params); dfree(grad); dfree(m); dfree(v); dfree(fmean); dfree(fstd);
+        dfree(E); dfree(g); dfree(fs); dfree(w); dfree(rec); dfree(loss);
+    }
+};
+
+int fit_setup(komd_sur_data *d, FitBuffers &b, FitParams &p, const float *params, const float *fmean,
+              const float *fstd, double e_scale, double e_shift, double f2, float lam_e, float lam_f, int64_t n_snaps,
+              int batch_snaps) {
+    if (!d || !params || !fmean || !fstd) return fail(KOMD_ERR_ARG, "null argument");
+    if (d->n_snap <= 0) return fail(KOMD_ERR_STATE, "the dataset holds no snapshots");
+    if (!(e_scale > 0.0) || !(f2 > 0.0)) return fail(KOMD_ERR_ARG, "e_scale and f2 must be positive");
+    CK(cudaSetDevice(d->device));
+    const int64_t nb = (int64_t)batch_snaps * d->n_site;
+    if (nb > (1LL << 30)) return fail(KOMD_ERR_ARG, "batch too large");
+    CK(dalloc(b.snaps, n_snaps)); CK(dalloc(b.params, kSurNParam)); CK(dalloc(b.grad, kSurNParam));
+    CK(dalloc(b.m, kSurNParam)); CK(dalloc(b.v, kSurNParam)); CK(dalloc(b.fmean, kSurNF)); CK(dalloc(b.fstd, kSurNF));
+    CK(dalloc(b.E, nb)); CK(dalloc(b.g, nb * kSurNF)); CK(dalloc(b.fs, 3 * nb)); CK(dalloc(b.w, nb * kSurNF));
+    CK(dalloc(b.rec, nb * kFitRec)); CK(dalloc(b.loss, 2));
+    CK(cudaMemcpy(b.params, params, sizeof(float) * kSurNParam, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(b.fmean, fmean, sizeof(float) * kSurNF, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(b.fstd, fstd, sizeof(float) * kSurNF, cudaMemcpyHostToDevice));
+    CK(cudaMemset(b.m, 0, sizeof(float) * kSurNParam));
+    CK(cudaMemset(b.v, 0, sizeof(float) * kSurNParam));
+    CK(cudaMemset(b.loss, 0, sizeof(double) * 2));
+    p.nl = d->nl; p.nl_count = d->count; p.cap = d->cap; p.n_site = d->n_site; p.nb = (int)nb; p.rc = d->rc;
+    p.x = d->x; p.mom = d->mom; p.e3 = d->e3; p.f3 = d->f3; p.snaps = b.snaps;
+    p.params = b.params; p.fmean = b.fmean; p.fstd = b.fstd;
+    p.e_scale = (float)e_scale; p.e_shift = (float)e_shift;
+    p.lam_e = lam_e; p.lam_f = lam_f; p.inv_f2 = (float)(1.0 / f2);
+    p.E = b.E; p.g = b.g; p.fs = b.fs; p.w = b.w; p.rec = b.rec; p.loss = b.loss;
+    return KOMD_OK;
+}
+
+uint64_t splitmix(uint64_t &s) {
+    uint64_t z = (s += 0x9e3779b97f4a7c15ull);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+}  // namespace
+
+extern "C" {
+
+int komd_sur_data_create(int32_t device, int32_t nl_cap, komd_sur_data **out) {
+    if (!out || nl_cap <= 0 || nl_cap > 4096) return fail(KOMD_ERR_ARG, "bad argument");
+    CK(cudaSetDevice(device));
+    komd_sur_data *d = new komd_sur_data();
+    d->device = device;
+    d->cap = nl_cap;
+    if (cudaMalloc(reinterpret_cast<void **>(&d->err), sizeof(int)) != cudaSuccess) {
+        delete d;
+        return fail(KOMD_ERR_NOMEM, "device allocation failed");
+    }
+    cudaMemset(d->err, 0, sizeof(int));
+    *out = d;
+    return KOMD_OK;
+}
+
+void komd_sur_data_destroy(komd_sur_data *d) { delete d; }
+
+int64_t komd_sur_data_snapshots(const komd_sur_data *d) { return d ? d->n_snap : -1; }
+int32_t komd_sur_data_sites(const komd_sur_data *d) { return d ? d->n_site : -1; }
+
+int komd_gpu_surrogate_capture(komd_gpu *h, komd_sur_data *d) {
+    if (!h || !d) return fail(KOMD_ERR_ARG, "null argument");
+    Engine &e = h->e;
+    if (!e.have_cells) return fail(KOMD_ERR_STATE, "update_container must run first");
+    if (!(e.cfg.terms & KOMD_TERM_ATM) || e.cfg.precision != KOMD_FP32)
+        return fail(KOMD_ERR_ARG, "captures need KOMD_TERM_ATM in FP32 mode");
+    if (e.device != d->device) return fail(KOMD_ERR_ARG, "dataset and engine live on different devices");
+    if (e.n > (1 << 24)) return fail(KOMD_ERR_ARG, "snapshots are limited to 2^24 sites");
+    if (d->n_snap == 0) {
+        d->n_site = (int)e.n;
+        d->rc = (float)e.cfg.cutoff_3b;
+    } else if (d->n_site != (int)e.n || d->rc != (float)e.cfg.cutoff_3b) {
+        return fail(KOMD_ERR_ARG, "all snapshots of a dataset need the same site count and three-body cutoff");
+    }
+    int rc = data_reserve(d, d->n_snap + 1);
+    if (rc) return rc;
+    Surrogate &u = h->sur;
+    if (!u.x) {
+        CK(dalloc(u.x, (size_t)e.n * kSurNF)); CK(dalloc(u.mom, (size_t)e.n * kSurNC * 9));
+        CK(dalloc(u.fprobe, 3 * (size_t)e.n));
+    }
+    double *e3d = nullptr;
+    CK(dalloc(e3d, e.n));
+    CK(cudaMemsetAsync(e3d, 0, sizeof(double) * e.n, e.stream));
+    double *keep = e.f;
+    e.f = u.fprobe;
+    launch_pair(e, e.stream, false, nullptr);                  // ATM neighbour list of this state
+    CK(cudaMemsetAsync(u.fprobe, 0, sizeof(double) * 3 * e.n, e.stream));
+    e.atm_esite = e3d;
+    launch_atm(e, e.stream, true);                             // exact forces and per-site energies
+    e.atm_esite = nullptr;
+    e.f = keep;
+    SurParams p = sur_params(h);
+    p.fmean = nullptr;
+    p.fstd = nullptr;
+    launch_sur_desc(p, e.stream);
+    const size_t o = (size_t)d->n_snap * d->n_site;
+    launch_fit_capture((int)e.n, e.nl, e.nl_count, e.nl_cap, u.x, u.mom, e3d, u.fprobe, e.slot_site,
+                       d->nl + o * d->cap, d->count + o, d->cap, d->x + o * kSurNF, d->mom + o * kSurNC * 9,
+                       d->e3 + o, d->f3 + 3 * o, d->site + o, d->err, e.stream);
+    rc = check_launch("surrogate_capture");
+    int derr = 0;
+    if (!rc) {
+        CK(cudaMemcpyAsync(&derr, d->err, sizeof(int), cudaMemcpyDeviceToHost, e.stream));
+        CK(cudaStreamSynchronize(e.stream));
+    }
+    dfree(e3d);
+    if (rc) return rc;
+    int flags[E_NFLAGS];
+    rc = read_flags(h, flags, true);
+    if (rc) return rc;
+    if (flags[E_ATM_OVERFLOW]) return fail(KOMD_ERR_OVERFLOW, "ATM neighbour list overflow");
+    if (derr) {
+        cudaMemset(d->err, 0, sizeof(int));
+        return fail(KOMD_ERR_OVERFLOW, "a site has more neighbours than the dataset's nl_cap");
+    }
+    d->n_snap++;
+    return KOMD_OK;
+}
+
+int komd_sur_data_get(komd_sur_data *d, int64_t snap, float *features, float *e3, float *f3, int32_t *site) {
+    if (!d) return fail(KOMD_ERR_ARG, "null dataset");
+    if (snap >= d->n_snap) return fail(KOMD_ERR_ARG, "snapshot index out of range");
+    CK(cudaSetDevice(d->device));
+    const size_t o = snap < 0 ? 0 : (size_t)snap * d->n_site;
+    const size_t n = snap < 0 ? (size_t)d->n_snap * d->n_site : (size_t)d->n_site;
+    if (features) CK(cudaMemcpy(features, d->x + o * kSurNF, sizeof(float) * n * kSurNF, cudaMemcpyDeviceToHost));
+    if (e3) CK(cudaMemcpy(e3, d->e3 + o, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    if (f3) CK(cudaMemcpy(f3, d->f3 + 3 * o, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost));
+    if (site) CK(cudaMemcpy(site, d->site + o, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    return KOMD_OK;
+}
+
+int komd_sur_fit_grad(komd_sur_data *d, const float *params, const float *fmean, const float *fstd, double e_scale,
+                      double e_shift, double f2, float lam_e, float lam_f, float *grad, double *loss) {
+    if (!grad) return fail(KOMD_ERR_ARG, "null argument");
+    FitBuffers b;
+    FitParams p;
+    int rc = fit_setup(d, b, p, params, fmean, fstd, e_scale, e_shift, f2, lam_e, lam_f, d ? d->n_snap : 0,
+                       d ? (int)d->n_snap : 0);
+    if (rc) return rc;
+    std::vector<int> ids((size_t)d->n_snap);
+    for (int64_t k = 0; k < d->n_snap; k++) ids[k] = (int)k;
+    CK(cudaMemcpy(b.snaps, ids.data(), sizeof(int) * ids.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemset(b.fs, 0, sizeof(float) * 3 * (size_t)p.nb));
+    CK(cudaMemset(b.grad, 0, sizeof(float) * kSurNParam));
+    launch_fit_step(p, b.grad, nullptr);
+    rc = check_launch("sur_fit_grad");
+    if (rc) return rc;
+    CK(cudaMemcpy(grad, b.grad, sizeof(float) * kSurNParam, cudaMemcpyDeviceToHost));
+    if (loss) CK(cudaMemcpy(loss, b.loss, sizeof(double) * 2, cudaMemcpyDeviceToHost));
+    return KOMD_OK;
+}
+
+int komd_sur_fit(komd_sur_data *d, float *params, const float *fmean, const float *fstd, double e_scale,
+                 double e_shift, double f2, const komd_sur_fit_opts *o, float *loss) {
+    if (!o || o->epochs < 0 || o->snaps_per_batch <= 0 || !(o->lr > 0.f) || !(o->lr_end > 0.f))
+        return fail(KOMD_ERR_ARG, "bad training options");
+    if (!d) return fail(KOMD_ERR_ARG, "null dataset");
+    const int bs = (int)std::min<int64_t>(o->snaps_per_batch, std::max<int64_t>(d->n_snap, 1));
+    FitBuffers b;
+    FitParams p;
+    int rc = fit_setup(d, b, p, params, fmean, fstd, e_scale, e_shift, f2, o->lam_e, o->lam_f, d->n_snap, bs);
+    if (rc) return rc;
+    const int64_t per_epoch = d->n_snap / bs;
+    const int64_t total = per_epoch * o->epochs;
+    uint64_t rng = o->seed;
+    std::vector<int> perm((size_t)d->n_snap);
+    int64_t step = 0;
+    for (int ep = 0; ep < o->epochs; ep++) {
+        for (int64_t k = 0; k < d->n_snap; k++) perm[k] = (int)k;
+        for (int64_t k = d->n_snap - 1; k > 0; k--) std::swap(perm[k], perm[splitmix(rng) % (uint64_t)(k + 1)]);
+        CK(cudaMemcpy(b.snaps, perm.data(), sizeof(int) * perm.size(), cudaMemcpyHostToDevice));
+        CK(cudaMemset(b.loss, 0, sizeof(double) * 2));
+        for (int64_t k = 0; k < per_epoch; k++, step++) {
+            p.snaps = b.snaps + k * bs;
+            const float lr = o->lr * std::pow(o->lr_end / o->lr, total > 1 ? (float)step / (float)(total - 1) : 0.f);
+            CK(cudaMemsetAsync(b.fs, 0, sizeof(float) * 3 * (size_t)p.nb, nullptr));
+            CK(cudaMemsetAsync(b.grad, 0, sizeof(float) * kSurNParam, nullptr));
+            launch_fit_step(p, b.grad, nullptr);
+            launch_fit_adam(b.params, b.grad, b.m, b.v, lr, (int)step, nullptr);
+        }
+        rc = check_launch("sur_fit");
+        if (rc) return rc;
+        double l2[2];
+        CK(cudaMemcpy(l2, b.loss, sizeof(l2), cudaMemcpyDeviceToHost));
+        if (loss) {
+            loss[2 * ep] = (float)(l2[0] / std::max<int64_t>(per_epoch, 1));
+            loss[2 * ep + 1] = (float)(l2[1] / std::max<int64_t>(per_epoch, 1));
+        }
+    }
+    CK(cudaMemcpy(params, b.params, sizeof(float) * kSurNParam, cudaMemcpyDeviceToHost));
     return KOMD_OK;
 }
 

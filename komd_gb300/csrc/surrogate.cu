@@ -20,30 +20,10 @@
 
 #include "engine.cuh"
 #include "kernels.cuh"
+#include "sur_device.cuh"
 #include "surrogate.cuh"
 
 namespace komd {
-
-__constant__ float c_mu_a[kSurNC] = {1.05f, 1.30f, 1.55f, 1.80f};
-
-__device__ __forceinline__ float sur_mu_r(int k) { return 0.85f + (float)k * (1.15f / 15.0f); }
-
-// radial Gaussians by the product recurrence exp(-eta (t - D)^2) = exp(-eta t^2) exp(2 eta D t) exp(-eta D^2)
-__device__ __forceinline__ void radial_basis(float r, float fc, float dfc, float *G, float *dG) {
-    const float D = 1.15f / 15.0f;
-    float t = r - 0.85f;
-    float gk = __expf(-kSurEtaR * t * t);
-    float up = __expf(2.0f * kSurEtaR * D * t);
-    const float c1 = __expf(-kSurEtaR * D * D), c2 = c1 * c1;
-#pragma unroll
-    for (int k = 0; k < kSurNR; k++) {
-        G[k] = gk * fc;
-        if (dG) dG[k] = gk * (-2.0f * kSurEtaR * t * fc + dfc);
-        gk = gk * up * c1;
-        up = up * c2;
-        t -= D;
-    }
-}
 
 // ---------------------------------------------------------------------------
 // descriptors: one warp per slot (cell order)
@@ -56,25 +36,19 @@ __global__ void __launch_bounds__(256) k_sur_desc(SurParams p) {
     float acc[kSurNR + kSurNC * 9];   // G (16), then per channel M1 (3) + M2 (6: xx xy xz yy yz zz)
 #pragma unroll
     for (int k = 0; k < kSurNR + kSurNC * 9; k++) acc[k] = 0.f;
-    const float rc = p.rc, pi_rc = 3.14159265358979f / p.rc;
     for (int k = lane; k < ni; k += 32) {
-        const float4 e = p.nl[(size_t)i * p.nl_cap + k];
-        const float dx = -e.x, dy = -e.y, dz = -e.z;    // d = r_j - r_i
-        const float r = sqrtf(dx * dx + dy * dy + dz * dz);
-        if (!(r < rc) || r == 0.f) continue;
-        float sn, cs;
-        __sincosf(pi_rc * r, &sn, &cs);
-        const float fc = 0.5f * (cs + 1.0f);
-        const float ir = 1.0f / r, ux = dx * ir, uy = dy * ir, uz = dz * ir;
+        SurNb q;
+        if (!sur_nb(p.nl[(size_t)i * p.nl_cap + k], p.rc, q)) continue;
         float G[kSurNR];
-        radial_basis(r, fc, 0.f, G, nullptr);
+        radial_basis(q.r, q.fc, 0.f, G, nullptr);
 #pragma unroll
-        for (int q = 0; q < kSurNR; q++) acc[q] += G[q];
+        for (int c = 0; c < kSurNR; c++) acc[c] += G[c];
 #pragma unroll
         for (int c = 0; c < kSurNC; c++) {
-            const float t = r - c_mu_a[c];
-            const float g = __expf(-kSurEtaA * t * t) * fc;
+            const float t = q.r - sur_mu_a(c);
+            const float g = __expf(-kSurEtaA * t * t) * q.fc;
             float *m = acc + kSurNR + 9 * c;
+            const float ux = q.u[0], uy = q.u[1], uz = q.u[2];
             m[0] += g * ux; m[1] += g * uy; m[2] += g * uz;
             m[3] += g * ux * ux; m[4] += g * ux * uy; m[5] += g * ux * uz;
             m[6] += g * uy * uy; m[7] += g * uy * uz; m[8] += g * uz * uz;
@@ -300,54 +274,17 @@ __global__ void __launch_bounds__(256) k_sur_force(SurParams p) {
     float a[kSurNC][3], B[kSurNC][6];
     const float *mom = p.mom + (size_t)i * kSurNC * 9;
 #pragma unroll
-    for (int c = 0; c < kSurNC; c++) {
-        const float v[3] = {mom[9 * c], mom[9 * c + 1], mom[9 * c + 2]};
-        const float m[6] = {mom[9 * c + 3], mom[9 * c + 4], mom[9 * c + 5], mom[9 * c + 6], mom[9 * c + 7], mom[9 * c + 8]};
-        const float M[3][3] = {{m[0], m[1], m[2]}, {m[1], m[3], m[4]}, {m[2], m[4], m[5]}};
-        const float e1 = dr[kSurNR + c], e2 = dr[kSurNR + kSurNC + c], e3 = dr[kSurNR + 2 * kSurNC + c],
-                    e4 = dr[kSurNR + 3 * kSurNC + c];
-        float Mv[3], M2[3][3];
-        for (int x = 0; x < 3; x++) Mv[x] = M[x][0] * v[0] + M[x][1] * v[1] + M[x][2] * v[2];
-        for (int x = 0; x < 3; x++)
-            for (int y = 0; y < 3; y++) M2[x][y] = M[x][0] * M[0][y] + M[x][1] * M[1][y] + M[x][2] * M[2][y];
-        for (int x = 0; x < 3; x++) a[c][x] = 2.f * e1 * v[x] + 2.f * e3 * Mv[x];
-        const int ix[6][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
-        for (int q = 0; q < 6; q++) {
-            const int x = ix[q][0], y = ix[q][1];
-            B[c][q] = 2.f * e2 * M[x][y] + e3 * v[x] * v[y] + 3.f * e4 * M2[x][y];
-        }
-    }
-    const float rc = p.rc, pi_rc = 3.14159265358979f / p.rc;
+    for (int c = 0; c < kSurNC; c++)
+        sur_channel_coeffs(mom + 9 * c, mom + 9 * c + 3, dr[kSurNR + c], dr[kSurNR + kSurNC + c],
+                           dr[kSurNR + 2 * kSurNC + c], dr[kSurNR + 3 * kSurNC + c], a[c], B[c]);
     const int ni = p.nl_count[i];
     float fx = 0.f, fy = 0.f, fz = 0.f;
     for (int k = lane; k < ni; k += 32) {
         const float4 e = p.nl[(size_t)i * p.nl_cap + k];
-        const float dx = -e.x, dy = -e.y, dz = -e.z;
-        const float r = sqrtf(dx * dx + dy * dy + dz * dz);
-        if (!(r < rc) || r == 0.f) continue;
-        float sn, cs;
-        __sincosf(pi_rc * r, &sn, &cs);
-        const float fc = 0.5f * (cs + 1.0f), dfc = -0.5f * pi_rc * sn;
-        const float ir = 1.0f / r, u[3] = {dx * ir, dy * ir, dz * ir};
-        float G[kSurNR], dG[kSurNR];
-        radial_basis(r, fc, dfc, G, dG);
-        float sr = 0.f;
-#pragma unroll
-        for (int q = 0; q < kSurNR; q++) sr += dr[q] * dG[q];
-        float h[3] = {sr * u[0], sr * u[1], sr * u[2]};
-#pragma unroll
-        for (int c = 0; c < kSurNC; c++) {
-            const float t = r - c_mu_a[c];
-            const float ex = __expf(-kSurEtaA * t * t);
-            const float gg = ex * fc, gp = ex * (-2.f * kSurEtaA * t * fc + dfc);
-            const float ua = u[0] * a[c][0] + u[1] * a[c][1] + u[2] * a[c][2];
-            const float Bu[3] = {B[c][0] * u[0] + B[c][1] * u[1] + B[c][2] * u[2],
-                                 B[c][1] * u[0] + B[c][3] * u[1] + B[c][4] * u[2],
-                                 B[c][2] * u[0] + B[c][4] * u[1] + B[c][5] * u[2]};
-            const float uBu = u[0] * Bu[0] + u[1] * Bu[1] + u[2] * Bu[2];
-            const float s1 = gp * (ua + uBu) - (gg * ir) * (ua + 2.f * uBu);
-            for (int x = 0; x < 3; x++) h[x] += s1 * u[x] + (gg * ir) * (a[c][x] + 2.f * Bu[x]);
-        }
+        SurNb q;
+        if (!sur_nb(e, p.rc, q)) continue;
+        float h[3];
+        sur_pair_grad(q, dr, a, B, h);
         // dE_i/dd_ij = h:  F_j -= h, F_i += h
         const int j = __float_as_int(e.w) >> 6;
         atomicAdd(&p.fsur[3 * j], -h[0]);

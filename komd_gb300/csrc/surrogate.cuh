@@ -41,6 +41,34 @@ struct TrainParams {
     int grad_only;
 };
 
+// force-matched training on captured snapshots (sur_train.cu).  A dataset
+// holds snapshots of n_site sites each, in the cell (slot) order of the
+// engine that captured them; neighbour entries are the engine's ATM list
+// entries (r_i - r_j, code) whose code >> 6 is the neighbour's slot within
+// the same snapshot.  A batch is a list of snapshot ids; batch site b is
+// site b % n_site of snapshot snaps[b / n_site].
+struct FitParams {
+    const float4 *nl;
+    const int *nl_count;
+    int cap, n_site, nb;
+    float rc;
+    const float *x, *mom, *e3, *f3;      // raw features, moments, exact energies and forces (dataset order)
+    const int *snaps;
+    const float *params, *fmean, *fstd;
+    float e_scale, e_shift;
+    float lam_e, lam_f, inv_f2;          // loss weights; 1 / <|F_exact|^2> per site
+    float *E, *g, *fs, *w, *rec;         // per batch site: energy, dE/dx, learned force, tangent, record
+    double *loss;                        // [0] energy term, [1] force term (accumulated)
+};
+constexpr int kFitRec = 580;             // record stride (floats)
+
+void launch_fit_capture(int n, const float4 *nl, const int *nl_count, int nl_cap, const float *x, const float *mom,
+                        const double *e3_site, const double *f3_site, const int *slot_site, float4 *dnl,
+                        int *dcount, int dcap, float *dx, float *dmom, float *de3, float *df3, int *dsite, int *err,
+                        cudaStream_t st);
+void launch_fit_step(FitParams &p, float *grad, cudaStream_t st);
+void launch_fit_adam(float *params, const float *grad, float *m, float *v, float lr, int step, cudaStream_t st);
+
 void launch_sur_desc(SurParams &p, cudaStream_t st);
 void launch_sur_mlp(SurParams &p, cudaStream_t st);
 void launch_sur_force(SurParams &p, cudaStream_t st);

@@ -34,7 +34,8 @@ EXPORTS = [
     "komd_gpu_rdf_bins", "komd_gpu_get_cells", "komd_gpu_neighbour_counts", "komd_gpu_set_profiling",
     "komd_gpu_profile", "komd_gpu_kernels_per_step", "komd_gpu_atm_forces_noalloc", "komd_gpu_surrogate_load",
     "komd_gpu_surrogate_sample", "komd_gpu_surrogate_forces", "komd_gpu_surrogate_status", "komd_mlp_train",
-    "komd_mlp_loss_grad",
+    "komd_mlp_loss_grad", "komd_sur_data_create", "komd_sur_data_destroy", "komd_gpu_surrogate_capture",
+    "komd_sur_data_snapshots", "komd_sur_data_sites", "komd_sur_data_get", "komd_sur_fit", "komd_sur_fit_grad",
 ]
 
 
@@ -61,6 +62,11 @@ class Observables(C.Structure):
 class SurrogateStatus(C.Structure):
     _fields_ = [("steps", C.c_int64), ("probes", C.c_int64), ("last_rmse", C.c_double), ("max_rmse", C.c_double),
                 ("fallback", C.c_int32), ("fallback_step", C.c_int64)]
+
+
+class SurFitOpts(C.Structure):
+    _fields_ = [("epochs", C.c_int32), ("snaps_per_batch", C.c_int32), ("lr", C.c_float), ("lr_end", C.c_float),
+                ("lam_e", C.c_float), ("lam_f", C.c_float), ("seed", C.c_uint64)]
 
 
 class KomdError(RuntimeError):
@@ -116,6 +122,16 @@ def load() -> C.CDLL:
     L.komd_gpu_surrogate_status.argtypes = [P, C.POINTER(SurrogateStatus)]
     L.komd_mlp_train.argtypes = [P, P, I64, P, C.c_int32, C.c_int32, C.c_float, C.c_uint64, P]
     L.komd_mlp_loss_grad.argtypes = [P, P, I64, P, P, P]
+    L.komd_sur_data_create.argtypes = [I32, I32, C.POINTER(P)]
+    L.komd_sur_data_destroy.argtypes = [P]
+    L.komd_sur_data_destroy.restype = None
+    L.komd_gpu_surrogate_capture.argtypes = [P, P]
+    L.komd_sur_data_snapshots.argtypes = [P]
+    L.komd_sur_data_snapshots.restype = I64
+    L.komd_sur_data_sites.argtypes = [P]
+    L.komd_sur_data_get.argtypes = [P, I64, P, P, P, P]
+    L.komd_sur_fit.argtypes = [P, P, P, P, C.c_double, C.c_double, C.c_double, C.POINTER(SurFitOpts), P]
+    L.komd_sur_fit_grad.argtypes = [P, P, P, P, C.c_double, C.c_double, C.c_double, C.c_float, C.c_float, P, P]
     _lib = L
     return L
 
@@ -283,6 +299,10 @@ class GpuSystem:
         self._check(self.L.komd_gpu_surrogate_sample(self.h, _p(x), _p(e3), _p(f3)))
         return x, e3, f3
 
+    def surrogate_capture(self, data: "SurData"):
+        """Appends the current state to a force-matching dataset."""
+        self._check(self.L.komd_gpu_surrogate_capture(self.h, data.h))
+
     def surrogate_forces(self):
         f3 = np.zeros((self.n, 3))
         e3 = np.zeros(self.n)
@@ -318,3 +338,69 @@ def mlp_loss_grad(X, y, params):
     if rc != KOMD_OK:
         raise KomdError(rc, L.komd_gpu_last_error().decode())
     return g, float(loss[0])
+
+
+class SurData:
+    """Snapshots for force-matched training, resident on the device."""
+
+    def __init__(self, device=0, nl_cap=80):
+        self.L = load()
+        self.h = C.c_void_p()
+        rc = self.L.komd_sur_data_create(int(device), int(nl_cap), C.byref(self.h))
+        if rc != KOMD_OK:
+            raise KomdError(rc, self.L.komd_gpu_last_error().decode())
+
+    def _check(self, rc):
+        if rc != KOMD_OK:
+            raise KomdError(rc, self.L.komd_gpu_last_error().decode())
+
+    @property
+    def snapshots(self) -> int:
+        return int(self.L.komd_sur_data_snapshots(self.h))
+
+    @property
+    def sites(self) -> int:
+        return int(self.L.komd_sur_data_sites(self.h))
+
+    def get(self, snap=-1):
+        """(features, e3, f3, site) of one snapshot or of all (snap < 0), slot order."""
+        n = self.sites * (self.snapshots if snap < 0 else 1)
+        x = np.zeros((n, SUR_NFEAT), np.float32)
+        e3 = np.zeros(n, np.float32)
+        f3 = np.zeros((n, 3), np.float32)
+        site = np.zeros(n, np.int32)
+        self._check(self.L.komd_sur_data_get(self.h, int(snap), _p(x), _p(e3), _p(f3), _p(site)))
+        return x, e3, f3, site
+
+    def fit(self, params, fmean, fstd, e_scale, e_shift, f2, epochs, snaps_per_batch=4, lr=2e-3, lr_end=1e-4,
+            lam_e=0.1, lam_f=1.0, seed=0):
+        o = SurFitOpts(int(epochs), int(snaps_per_batch), float(lr), float(lr_end), float(lam_e), float(lam_f),
+                       int(seed))
+        p = np.ascontiguousarray(params, np.float32).copy()
+        fm = np.ascontiguousarray(fmean, np.float32)
+        fs = np.ascontiguousarray(fstd, np.float32)
+        loss = np.zeros(2 * max(int(epochs), 1), np.float32)
+        self._check(self.L.komd_sur_fit(self.h, _p(p), _p(fm), _p(fs), float(e_scale), float(e_shift), float(f2),
+                                        C.byref(o), _p(loss)))
+        return p, loss[:2 * int(epochs)].reshape(-1, 2)
+
+    def fit_grad(self, params, fmean, fstd, e_scale, e_shift, f2, lam_e=0.1, lam_f=1.0):
+        p = np.ascontiguousarray(params, np.float32)
+        fm = np.ascontiguousarray(fmean, np.float32)
+        fs = np.ascontiguousarray(fstd, np.float32)
+        g = np.zeros(SUR_NPARAM, np.float32)
+        loss = np.zeros(2)
+        self._check(self.L.komd_sur_fit_grad(self.h, _p(p), _p(fm), _p(fs), float(e_scale), float(e_shift), float(f2),
+                                             float(lam_e), float(lam_f), _p(g), _p(loss)))
+        return g, loss
+
+    def close(self):
+        if self.h:
+            self.L.komd_sur_data_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -38,7 +38,8 @@ def test_descriptors_and_labels_match_oracle(oracle_lib):
     r, _, _ = g.download()
     ref = np.array([oracle_lib.sur_features(_min_image_neighbours(r, s.box, i, 2.0)) for i in range(s.n)])
     scale = np.abs(ref).max(0) + 1e-12
-    np.testing.assert_allclose(x, ref, rtol=2e-4, atol=2e-4 * scale)
+    dev = (np.abs(x - ref) / (2e-4 * np.abs(ref) + 2e-4 * scale)).max(0)
+    assert dev.max() < 1.0, f"feature deviations in units of the tolerance: {np.round(dev, 2).tolist()}"
     # exact per-site ATM energies sum to the oracle's ATM energy; forces match
     sim = oracle_lib.OracleSim(s, 2.2, 2.0, nu=0.073, lj=False, atm=True, atm_mode="full",
                                atm_sign=oracle_lib.ATM_SIGN_PHYSICAL, virial_mode=oracle_lib.VIRIAL_CORRECT)
@@ -67,6 +68,58 @@ def test_training_gradient_matches_oracle(oracle_lib):
         ref_loss += (e - y[k]) ** 2 / len(y)
     assert loss == pytest.approx(ref_loss, rel=1e-4)
     assert np.abs(g - ref).max() < 1e-4 * np.abs(ref).max() + 1e-7
+
+
+def test_force_matching_gradient_matches_oracle(oracle_lib):
+    """komd_sur_fit's gradient (energy + force residuals through the
+    descriptor Jacobian and the network's tangent pass) against central
+    differences of the same loss evaluated by the FP64 oracle."""
+    from komd_gb300 import gpu, surrogate
+    s = _small_system(seed=53)
+    g = _gpu(s)
+    data = gpu.SurData(nl_cap=80)
+    g.surrogate_capture(data)
+    r, _, _ = g.download()
+    g.close()
+    x, e3, f3, site = data.get(0)
+    e3s = np.zeros(s.n)
+    f3s = np.zeros((s.n, 3))
+    e3s[site] = e3
+    f3s[site] = f3
+    fmean = x.mean(0).astype(np.float32)
+    fstd = (x.std(0) + 1e-6).astype(np.float32)
+    e_scale, e_shift = float(e3.std()), float(e3.mean())
+    f2 = float((f3.astype(np.float64) ** 2).sum(1).mean())
+    rng = np.random.default_rng(4)
+    params = surrogate.init_params(8)
+    params[64 * 32:64 * 32 + 64] = rng.normal(0, 0.1, 64)
+    params[64 * 32 + 64 + 64 * 64:64 * 32 + 64 + 64 * 64 + 64] = rng.normal(0, 0.1, 64)
+    lam_e, lam_f = 0.3, 1.0
+    grad, loss = data.fit_grad(params, fmean, fstd, e_scale, e_shift, f2, lam_e=lam_e, lam_f=lam_f)
+    fm64, fs64 = fmean.astype(np.float64), fstd.astype(np.float64)
+    y = (e3s - e_shift) / e_scale
+
+    def oracle_loss(p64):
+        _, e, f = oracle_lib.sur_energy_forces(r, s.box, p64, fm64, fs64, e_scale, e_shift)
+        return (lam_e * np.mean(((e - e_shift) / e_scale - y) ** 2), lam_f * np.mean(((f - f3s) ** 2).sum(1)) / f2)
+
+    p64 = params.astype(np.float64)
+    le, lf = oracle_loss(p64)
+    assert loss[0] == pytest.approx(le, rel=2e-3)
+    assert loss[1] == pytest.approx(lf, rel=2e-3)
+    blocks = [(0, 2048), (2048, 2112), (2112, 6208), (6208, 6272), (6272, 6336), (6336, 6337)]
+    idx = np.concatenate([rng.choice(np.arange(a, b), min(4, b - a), replace=False) for a, b in blocks])
+    h = 1e-4
+    num = []
+    for q in idx:
+        pp, pm = p64.copy(), p64.copy()
+        pp[q] += h
+        pm[q] -= h
+        num.append((sum(oracle_loss(pp)) - sum(oracle_loss(pm))) / (2 * h))
+    num = np.array(num)
+    scale = max(np.abs(num).max(), np.abs(grad).max())
+    assert np.abs(grad[idx] - num).max() < 3e-3 * scale, (grad[idx], num)
+    data.close()
 
 
 def _model_from_sample(x, params, e3):
@@ -100,26 +153,33 @@ def test_inference_forces_match_oracle(oracle_lib):
 @pytest.fixture(scope="module")
 def trained():
     from komd_gb300 import surrogate
-    data = surrogate.generate(n_points=8, snaps_per_point=10, ncell=5, equil=40, every=10, seed=99)
-    model = surrogate.fit(data, epochs=30, batch=512, lr=3e-3, seed=3)
-    return data, model
+    data = surrogate.capture(n_points=8, snaps_per_point=10, ncell=5, equil=40, every=10, seed=99)
+    model = surrogate.fit_forces(data, epochs=40, snaps_per_batch=4, lr=3e-3, seed=3)
+    data.close()
+    return None, model
 
 
 def test_trained_surrogate_gains_over_no_threebody(trained):
-    """On a held-out configuration the trained network's three-body forces
-    sit far closer to the exact ones than the method without the learned term
-    (three-body forces left out: relative error 1), and the per-site energy
-    regression explains most of the variance."""
-    from komd_gb300 import surrogate
-    data, model = trained
-    assert model["loss"][-1] < 0.5 * model["loss"][0]
-    s = _small_system(seed=777, jitter=0.1)
-    g = _gpu(s)
+    """On a held-out configuration (another seed and state point, run with
+    the exact forces) the trained network's three-body forces sit far closer
+    to the exact ones than the method without the learned term (three-body
+    forces left out: relative error 1), and the per-site energies explain
+    most of the variance."""
+    from komd_gb300 import gpu, lattice, surrogate
+    _, model = trained
+    assert model["loss"][-1].sum() < 0.5 * model["loss"][0].sum()
+    s = lattice.argon_fcc(5, rho=0.82, t_star=0.9, seed=777, jitter=0.02)
+    cell = float(s.high[0]) / np.floor(float(s.high[0]) / 2.5)
+    g = gpu.GpuSystem(s, surrogate.physics_config(s, cell))
+    g.update_container()
+    g.forces()
+    g.step(150)
+    g.update_container()
     _, e3, f3 = g.surrogate_sample()
     g.surrogate_load(model, probe_every=0)
     f, e = g.surrogate_forces()
     err = surrogate.force_rmse(f, f3)
-    assert err < 0.5, f"surrogate three-body force RMSE {err:.3f}"
+    assert err < 0.35, f"surrogate three-body force RMSE {err:.3f}"
     r2 = 1.0 - ((e - e3) ** 2).sum() / ((e3 - e3.mean()) ** 2).sum()
     assert r2 > 0.8
     g.close()
