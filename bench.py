@@ -202,6 +202,61 @@ def run_reference(args, w, name):
     return 0
 
 
+def surrogate_leg(args, g, s, stream, local, dist, exact_value, world):
+    """FP32 + learned three-body form of the same workload: training set from
+    the exact kernel (2000 snapshots of 500 atoms over T* in [0.6, 1.2],
+    rho* in [0.75, 0.9]), force-matched training on the GPU, then K timed
+    steps with an exact-ATM probe every probe_every steps (fallback to the
+    exact form on a breach).  The probes' cost is inside the timed steps."""
+    import torch
+    from komd_gb300 import surrogate
+    t0 = time.perf_counter()
+    data = surrogate.capture(n_points=40, snaps_per_point=50, ncell=5, equil=100, every=10, seed=2026, device=local)
+    t1 = time.perf_counter()
+    model = surrogate.fit_forces(data, epochs=args.sur_epochs, snaps_per_batch=4, lr=3e-3, seed=7)
+    snaps, sites = data.snapshots, data.sites
+    data.close()
+    # accuracy on the benchmark state itself, before the timed steps
+    g.update_container()
+    _, e3, f3 = g.surrogate_sample()
+    g.surrogate_load(model, probe_every=args.sur_probe, probe_threshold=args.sur_threshold)
+    f_l, e_l = g.surrogate_forces()
+    rmse0 = surrogate.force_rmse(f_l, f3)
+    g.forces()
+    g.step(max(args.warmup, 3))
+    torch.cuda.synchronize()
+    g.set_profiling(True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    g.step(args.steps)
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    prof = g.profile()
+    g.set_profiling(False)
+    if dist:
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    st = g.surrogate_status()
+    value = world * s.n * args.steps / (ms / 1e3)
+    return {"value": value, "unit": UNIT, "ms_per_step": ms / args.steps, "speedup_vs_exact": value / exact_value,
+            "form": "FP32 LJ + learned three-body term (32-64-64-1 MLP, BF16 tensor-core inference)",
+            "force_rmse_3body": {"at_start": rmse0, "probe_last": st["last_rmse"], "probe_max": st["max_rmse"],
+                                 "definition": "|F_learned - F_exact| RMS / |F_exact| RMS over sites, three-body term"},
+            "energy_r2_3body": float(1.0 - ((e_l - e3) ** 2).sum() / ((e3 - e3.mean()) ** 2).sum()),
+            "probe_every": args.sur_probe, "probe_threshold": args.sur_threshold, "probes": st["probes"],
+            "fallback": bool(st["fallback"]), "fallback_step": st["fallback_step"],
+            "training": {"snapshots": snaps, "sites_per_snapshot": sites, "capture_s": t1 - t0,
+                         "train_s": model["train_s"], "epochs": args.sur_epochs,
+                         "final_loss_energy_force": [float(x) for x in model["loss"][-1]]},
+            "kernel_ms": {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()}}
+
+
 def run_ours(args, w, name):
     import torch
     from komd_gb300 import gpu
@@ -214,7 +269,7 @@ def run_ours(args, w, name):
         dist.init_process_group("nccl")
 
     s = make_system(w, seed=1 + rank)
-    terms = gpu.TERM_LJ | (gpu.TERM_ATM if w["atm"] else 0)
+    terms = gpu.TERM_LJ | (gpu.TERM_ATM | gpu.TERM_ATM_SURROGATE if w["atm"] else 0)   # learned form off until loaded
     cfg = gpu.make_config(s.low, s.high, w["cell"], cutoff=w["rc"], cutoff_3b=w["rc3"], nu=w["nu"], dt=w["dt"],
                           terms=terms, precision=gpu.FP32, atm_sign=gpu.ATM_SIGN_PHYSICAL,
                           atm_enum=gpu.ATM_ENUM_FULL, virial_mode=gpu.VIRIAL_CORRECT, skin=w["skin"])
@@ -291,6 +346,10 @@ def run_ours(args, w, name):
         e_s = float(tt.item())
     e2e = world * s.n * args.steps / e_s
 
+    sur = None
+    if w["atm"] and not args.no_surrogate:
+        sur = surrogate_leg(args, g, s, stream, local, dist, value, world)
+
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -342,6 +401,8 @@ def run_ours(args, w, name):
             "energy": {"u_lj_per_atom": obs0["u_lj"] / s.n, "u_atm_per_atom": obs0["u_atm"] / s.n}}
     if cb:
         line["cpu_baseline"] = cb
+    if sur:
+        line["surrogate"] = sur
     print(json.dumps(line), flush=True)
     g.close()
     if dist:
@@ -360,6 +421,11 @@ def main():
     ap.add_argument("--equil", type=int, default=400,
                     help="untimed NVE steps from the lattice before the warm-up (thermalises the crystal)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-surrogate", action="store_true", help="skip the learned three-body leg")
+    ap.add_argument("--sur-epochs", type=int, default=30)
+    ap.add_argument("--sur-probe", type=int, default=50, help="exact-ATM probe interval of the learned form")
+    ap.add_argument("--sur-threshold", type=float, default=0.2,
+                    help="probe breach (relative three-body force RMSE) that switches back to exact ATM")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -921,11 +921,27 @@ int komd_gpu_surrogate_load(komd_gpu *h, const float *params, const float *fmean
     Surrogate &u = h->sur;
     const int H = kSurH, F = kSurNF;
     const float *W1 = params, *b1 = W1 + H * F, *W2 = b1 + H, *b2 = W2 + H * H, *w3 = b2 + H, *b3 = w3 + H;
-    std::vector<__nv_bfloat16> w1(H * F), w1t(F * H), w2(H * H), w2t(H * H);
-    for (int o = 0; o < H; o++)
-        for (int i = 0; i < F; i++) { w1[o * F + i] = __float2bfloat16(W1[o * F + i]); w1t[i * H + o] = w1[o * F + i]; }
-    for (int o = 0; o < H; o++)
-        for (int i = 0; i < H; i++) { w2[o * H + i] = __float2bfloat16(W2[o * H + i]); w2t[i * H + o] = w2[o * H + i]; }
+    // BF16 weights in the MMA B-fragment order of surrogate.cu (load_frag):
+    // element (n, k) of an N x K matrix given by at(n, k)
+    auto frag = [](int N, int K, auto at) {
+        std::vector<__nv_bfloat16> out((size_t)N * K);
+        const int S = K / 16;
+        for (int t = 0; t < N / 8; t++)
+            for (int s = 0; s < S; s++)
+                for (int lane = 0; lane < 32; lane++) {
+                    const int n = 8 * t + lane / 4, k0 = 16 * s + 2 * (lane % 4);
+                    __nv_bfloat16 *o = out.data() + ((size_t)(t * S + s) * 32 + lane) * 4;
+                    o[0] = __float2bfloat16(at(n, k0));
+                    o[1] = __float2bfloat16(at(n, k0 + 1));
+                    o[2] = __float2bfloat16(at(n, k0 + 8));
+                    o[3] = __float2bfloat16(at(n, k0 + 9));
+                }
+        return out;
+    };
+    const std::vector<__nv_bfloat16> w1 = frag(H, F, [&](int n, int k) { return W1[n * F + k]; });
+    const std::vector<__nv_bfloat16> w1t = frag(F, H, [&](int n, int k) { return W1[k * F + n]; });
+    const std::vector<__nv_bfloat16> w2 = frag(H, H, [&](int n, int k) { return W2[n * H + k]; });
+    const std::vector<__nv_bfloat16> w2t = frag(H, H, [&](int n, int k) { return W2[k * H + n]; });
     CK(dalloc(u.w1, w1.size())); CK(dalloc(u.w1t, w1t.size())); CK(dalloc(u.w2, w2.size())); CK(dalloc(u.w2t, w2t.size()));
     CK(dalloc(u.b1, H)); CK(dalloc(u.b2, H)); CK(dalloc(u.w3, H)); CK(dalloc(u.fmean, F)); CK(dalloc(u.fstd, F));
     CK(cudaMemcpy(u.w1, w1.data(), sizeof(__nv_bfloat16) * w1.size(), cudaMemcpyHostToDevice));
@@ -941,9 +957,9 @@ int komd_gpu_surrogate_load(komd_gpu *h, const float *params, const float *fmean
     u.e_scale = (float)e_scale;
     u.e_shift = (float)e_shift;
     CK(dalloc(u.x, (size_t)e.n * kSurNF)); CK(dalloc(u.mom, (size_t)e.n * kSurNC * 9));
-    CK(dalloc(u.dedx, (size_t)e.n * kSurNF)); CK(dalloc(u.esite, e.n)); CK(dalloc(u.fsur, 3 * (size_t)e.n));
+    CK(dalloc(u.dedx, (size_t)e.n * kSurNF)); CK(dalloc(u.esite, e.n)); CK(dalloc(u.fsur, 4 * (size_t)e.n));
     CK(dalloc(u.fprobe, 3 * (size_t)e.n)); CK(dalloc(u.fsur_d, 3 * (size_t)e.n)); CK(dalloc(u.probe_acc, 2));
-    CK(cudaMemset(u.fsur, 0, sizeof(float) * 3 * e.n));
+    CK(cudaMemset(u.fsur, 0, sizeof(float) * 4 * e.n));
     u.probe_every = probe_every;
     u.probe_threshold = probe_threshold;
     u.loaded = true;
@@ -1399,7 +1415,8 @@ int komd_gpu_kernels_per_step(komd_gpu *h) {
     if ((e.cfg.terms & KOMD_TERM_BONDED) && e.n_bonds > 0) k++;
     if ((e.cfg.terms & KOMD_TERM_BONDED) && e.n_angles > 0) k++;
     if (e.cfg.terms & KOMD_TERM_LIMIT) k++;
-    if (e.cfg.terms & KOMD_TERM_ATM) k++;
+    if (surrogate_on(h)) k += 4;   /* descriptors, MLP, forces, apply */
+    else if (e.cfg.terms & KOMD_TERM_ATM) k++;
     return k;
 }
 

@@ -26,19 +26,19 @@
 namespace komd {
 
 // ---------------------------------------------------------------------------
-// descriptors: one warp per slot (cell order)
+// descriptors: one thread per slot (cell order), the 52 sums in registers
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_sur_desc(SurParams p) {
-    const int lane = threadIdx.x & 31;
-    const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
+__global__ void __launch_bounds__(128) k_sur_desc(SurParams p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
-    const int ni = p.nl_count[i];
+    const int ni = min(p.nl_count[i], p.nl_cap);
     float acc[kSurNR + kSurNC * 9];   // G (16), then per channel M1 (3) + M2 (6: xx xy xz yy yz zz)
 #pragma unroll
     for (int k = 0; k < kSurNR + kSurNC * 9; k++) acc[k] = 0.f;
-    for (int k = lane; k < ni; k += 32) {
+    const float4 *row = p.nl + (size_t)i * p.nl_cap;
+    for (int k = 0; k < ni; k++) {
         SurNb q;
-        if (!sur_nb(p.nl[(size_t)i * p.nl_cap + k], p.rc, q)) continue;
+        if (!sur_nb(row[k], p.rc, q)) continue;
         float G[kSurNR];
         radial_basis(q.r, q.fc, 0.f, G, nullptr);
 #pragma unroll
@@ -48,52 +48,49 @@ __global__ void __launch_bounds__(256) k_sur_desc(SurParams p) {
             const float t = q.r - sur_mu_a(c);
             const float g = __expf(-kSurEtaA * t * t) * q.fc;
             float *m = acc + kSurNR + 9 * c;
-            const float ux = q.u[0], uy = q.u[1], uz = q.u[2];
-            m[0] += g * ux; m[1] += g * uy; m[2] += g * uz;
-            m[3] += g * ux * ux; m[4] += g * ux * uy; m[5] += g * ux * uz;
-            m[6] += g * uy * uy; m[7] += g * uy * uz; m[8] += g * uz * uz;
+            const float gx = g * q.u[0], gy = g * q.u[1], gz = g * q.u[2];
+            m[0] += gx; m[1] += gy; m[2] += gz;
+            m[3] += gx * q.u[0]; m[4] += gx * q.u[1]; m[5] += gx * q.u[2];
+            m[6] += gy * q.u[1]; m[7] += gy * q.u[2]; m[8] += gz * q.u[2];
         }
     }
-#pragma unroll
-    for (int k = 0; k < kSurNR + kSurNC * 9; k++)
-        for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
-    // invariants (every lane holds the totals)
     float raw[kSurNF];
 #pragma unroll
     for (int k = 0; k < kSurNR; k++) raw[k] = acc[k];
 #pragma unroll
     for (int c = 0; c < kSurNC; c++) {
-        const float *m = acc + kSurNR + 9 * c;
-        const float M[3][3] = {{m[3], m[4], m[5]}, {m[4], m[6], m[7]}, {m[5], m[7], m[8]}};
-        const float v[3] = {m[0], m[1], m[2]};
-        float Mv[3], M2[3][3];
-        for (int a = 0; a < 3; a++) Mv[a] = M[a][0] * v[0] + M[a][1] * v[1] + M[a][2] * v[2];
-        for (int a = 0; a < 3; a++)
-            for (int b = 0; b < 3; b++) M2[a][b] = M[a][0] * M[0][b] + M[a][1] * M[1][b] + M[a][2] * M[2][b];
+        const float *v = acc + kSurNR + 9 * c, *m = v + 3;
+        float M[3][3], Mv[3], M2[3][3];
+        sym_full(m, M);
+#pragma unroll
+        for (int x = 0; x < 3; x++) Mv[x] = M[x][0] * v[0] + M[x][1] * v[1] + M[x][2] * v[2];
+#pragma unroll
+        for (int x = 0; x < 3; x++)
+#pragma unroll
+            for (int y = 0; y < 3; y++) M2[x][y] = M[x][0] * M[0][y] + M[x][1] * M[1][y] + M[x][2] * M[2][y];
         float i2 = 0.f, i4 = 0.f;
-        for (int a = 0; a < 3; a++)
-            for (int b = 0; b < 3; b++) { i2 += M[a][b] * M[a][b]; i4 += M2[a][b] * M[b][a]; }
+#pragma unroll
+        for (int x = 0; x < 3; x++)
+#pragma unroll
+            for (int y = 0; y < 3; y++) { i2 += M[x][y] * M[x][y]; i4 += M2[x][y] * M[y][x]; }
         raw[kSurNR + c] = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
         raw[kSurNR + kSurNC + c] = i2;
         raw[kSurNR + 2 * kSurNC + c] = v[0] * Mv[0] + v[1] * Mv[1] + v[2] * Mv[2];
         raw[kSurNR + 3 * kSurNC + c] = i4;
     }
-    // lane k writes feature k (standardised, or raw when fstd is null) and moment k
-    float xk = 0.f;
+    if (p.fstd) {
 #pragma unroll
-    for (int k = 0; k < kSurNF; k++)
-        if (lane == k) xk = raw[k];
-    if (p.fstd) xk = (xk - p.fmean[lane]) / p.fstd[lane];
-    p.x[(size_t)i * kSurNF + lane] = xk;
+        for (int k = 0; k < kSurNF; k++) raw[k] = (raw[k] - p.fmean[k]) / p.fstd[k];
+    }
+    float4 *xo = reinterpret_cast<float4 *>(p.x + (size_t)i * kSurNF);
+#pragma unroll
+    for (int k = 0; k < kSurNF / 4; k++) xo[k] = make_float4(raw[4 * k], raw[4 * k + 1], raw[4 * k + 2], raw[4 * k + 3]);
     if (p.mom) {
-        float mk = 0.f, mk2 = 0.f;
+        float4 *mo = reinterpret_cast<float4 *>(p.mom + (size_t)i * kSurNC * 9);
 #pragma unroll
-        for (int k = 0; k < kSurNC * 9; k++) {
-            if (lane == k) mk = acc[kSurNR + k];
-            if (lane + 32 == k) mk2 = acc[kSurNR + k];
-        }
-        p.mom[(size_t)i * kSurNC * 9 + lane] = mk;
-        if (lane + 32 < kSurNC * 9) p.mom[(size_t)i * kSurNC * 9 + lane + 32] = mk2;
+        for (int k = 0; k < kSurNC * 9 / 4; k++)
+            mo[k] = make_float4(acc[kSurNR + 4 * k], acc[kSurNR + 4 * k + 1], acc[kSurNR + 4 * k + 2],
+                                acc[kSurNR + 4 * k + 3]);
     }
 }
 
@@ -106,6 +103,14 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     return r;
 }
 
+// hardware tanh (PTX tanh.approx.f32, max relative error about 2^-11: below
+// the BF16 rounding of the activations that follow)
+__device__ __forceinline__ float tanh_fast(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 __device__ __forceinline__ void mma16816(float *c, const uint32_t *a, uint32_t b0, uint32_t b1) {
     asm volatile(
         "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
@@ -114,20 +119,29 @@ __device__ __forceinline__ void mma16816(float *c, const uint32_t *a, uint32_t b
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-// B fragment of W stored row-major [n][k] (bf16, ld = K): rows n, k pair at k0 + tig*2 (+8)
-__device__ __forceinline__ void load_b(const __nv_bfloat16 *W, int ld, int n0, int k0, int g, int tig, uint32_t &b0,
-                                       uint32_t &b1) {
-    const uint32_t *row = reinterpret_cast<const uint32_t *>(W + (n0 + g) * ld + k0);
-    b0 = row[tig];
-    b1 = row[tig + 4];
+// B fragment (m16n8k16) of an N x K weight matrix stored in fragment order:
+// for n-tile t, k-step s and lane (g = lane/4, tig = lane%4) one uint2 holding
+// W[8t+g][16s+2tig .. +1] and W[8t+g][16s+8+2tig .. +1] (S = K/16 k-steps).
+// One conflict-free 8-byte shared load per MMA.
+__device__ __forceinline__ void load_frag(const __nv_bfloat16 *F, int S, int t, int s, int lane, uint32_t &b0,
+                                          uint32_t &b1) {
+    const uint2 v = reinterpret_cast<const uint2 *>(F)[(t * S + s) * 32 + lane];
+    b0 = v.x;
+    b1 = v.y;
 }
 
 __global__ void __launch_bounds__(128) k_sur_mlp(SurParams p) {
     __shared__ __align__(16) __nv_bfloat16 sW1[kSurH * kSurNF], sW1T[kSurNF * kSurH], sW2[kSurH * kSurH],
         sW2T[kSurH * kSurH];
     __shared__ float sb1[kSurH], sb2[kSurH], sw3[kSurH];
-    for (int t = threadIdx.x; t < kSurH * kSurNF; t += blockDim.x) { sW1[t] = p.w1[t]; sW1T[t] = p.w1t[t]; }
-    for (int t = threadIdx.x; t < kSurH * kSurH; t += blockDim.x) { sW2[t] = p.w2[t]; sW2T[t] = p.w2t[t]; }
+    {   // 16-byte staging of the BF16 weights
+        const uint4 *g1 = reinterpret_cast<const uint4 *>(p.w1), *g1t = reinterpret_cast<const uint4 *>(p.w1t);
+        const uint4 *g2 = reinterpret_cast<const uint4 *>(p.w2), *g2t = reinterpret_cast<const uint4 *>(p.w2t);
+        uint4 *s1 = reinterpret_cast<uint4 *>(sW1), *s1t = reinterpret_cast<uint4 *>(sW1T);
+        uint4 *s2 = reinterpret_cast<uint4 *>(sW2), *s2t = reinterpret_cast<uint4 *>(sW2T);
+        for (int t = threadIdx.x; t < kSurH * kSurNF / 8; t += blockDim.x) { s1[t] = g1[t]; s1t[t] = g1t[t]; }
+        for (int t = threadIdx.x; t < kSurH * kSurH / 8; t += blockDim.x) { s2[t] = g2[t]; s2t[t] = g2t[t]; }
+    }
     for (int t = threadIdx.x; t < kSurH; t += blockDim.x) { sb1[t] = p.b1[t]; sb2[t] = p.b2[t]; sw3[t] = p.w3[t]; }
     __syncthreads();
     const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
@@ -159,11 +173,11 @@ __global__ void __launch_bounds__(128) k_sur_mlp(SurParams p) {
 #pragma unroll
             for (int s = 0; s < 2; s++) {
                 uint32_t b0, b1;
-                load_b(sW1, kSurNF, t * 8, 16 * s, g, tig, b0, b1);
+                load_frag(sW1, kSurNF / 16, t, s, lane, b0, b1);
                 mma16816(acc, ax[s], b0, b1);
             }
 #pragma unroll
-            for (int q = 0; q < 4; q++) h1[t][q] = tanhf(acc[q]);
+            for (int q = 0; q < 4; q++) h1[t][q] = tanh_fast(acc[q]);
         }
         // layer 2: Z2 = H1 W2^T (4 k-steps from the h1 fragments)
         uint32_t ah[4][4];
@@ -182,11 +196,11 @@ __global__ void __launch_bounds__(128) k_sur_mlp(SurParams p) {
 #pragma unroll
             for (int s = 0; s < 4; s++) {
                 uint32_t b0, b1;
-                load_b(sW2, kSurH, t * 8, 16 * s, g, tig, b0, b1);
+                load_frag(sW2, kSurH / 16, t, s, lane, b0, b1);
                 mma16816(acc, ah[s], b0, b1);
             }
 #pragma unroll
-            for (int q = 0; q < 4; q++) h2[t][q] = tanhf(acc[q]);
+            for (int q = 0; q < 4; q++) h2[t][q] = tanh_fast(acc[q]);
         }
         // layer 3 and dE/dz2 = w3 (1 - h2^2)
         float e0 = 0.f, e1 = 0.f;
@@ -226,7 +240,7 @@ __global__ void __launch_bounds__(128) k_sur_mlp(SurParams p) {
 #pragma unroll
             for (int s = 0; s < 4; s++) {
                 uint32_t b0, b1;
-                load_b(sW2T, kSurH, t * 8, 16 * s, g, tig, b0, b1);
+                load_frag(sW2T, kSurH / 16, t, s, lane, b0, b1);
                 mma16816(acc, ad[s], b0, b1);
             }
 #pragma unroll
@@ -246,7 +260,7 @@ __global__ void __launch_bounds__(128) k_sur_mlp(SurParams p) {
 #pragma unroll
             for (int s = 0; s < 4; s++) {
                 uint32_t b0, b1;
-                load_b(sW1T, kSurH, t * 8, 16 * s, g, tig, b0, b1);
+                load_frag(sW1T, kSurH / 16, t, s, lane, b0, b1);
                 mma16816(acc, az[s], b0, b1);
             }
             const int c = t * 8 + tig * 2;
@@ -257,51 +271,51 @@ __global__ void __launch_bounds__(128) k_sur_mlp(SurParams p) {
 }
 
 // ---------------------------------------------------------------------------
-// forces: chain rule to the pair vectors; one warp per slot, one neighbour
-// entry per lane; the centre's force is warp-reduced, the neighbour's is
-// scattered with FP32 atomics into fsur (slot order)
+// forces: chain rule to the pair vectors, one thread per slot; the
+// neighbour's share is scattered with float4 atomics into fsur (slot order,
+// xyz + pad), the centre's share is summed in registers
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_sur_force(SurParams p) {
-    const int lane = threadIdx.x & 31;
-    const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
+__global__ void __launch_bounds__(128) k_sur_force(SurParams p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
-    // dE_i / d raw = e_scale * dE/dx / std  (lane k holds feature k)
-    const float drk = p.e_scale * p.dedx[(size_t)i * kSurNF + lane] / p.fstd[lane];
+    // dE_i / d raw = e_scale * dE/dx / std
     float dr[kSurNF];
+    const float4 *dx = reinterpret_cast<const float4 *>(p.dedx + (size_t)i * kSurNF);
 #pragma unroll
-    for (int k = 0; k < kSurNF; k++) dr[k] = __shfl_sync(0xffffffffu, drk, k);
-    // angular coefficients a_c = dE/dM1_c, B_c = dE/dM2_c
+    for (int k = 0; k < kSurNF / 4; k++) {
+        const float4 t = dx[k];
+        dr[4 * k] = t.x; dr[4 * k + 1] = t.y; dr[4 * k + 2] = t.z; dr[4 * k + 3] = t.w;
+    }
+#pragma unroll
+    for (int k = 0; k < kSurNF; k++) dr[k] *= p.e_scale / p.fstd[k];
     float a[kSurNC][3], B[kSurNC][6];
-    const float *mom = p.mom + (size_t)i * kSurNC * 9;
+    float mom[kSurNC * 9];
+    const float4 *mo = reinterpret_cast<const float4 *>(p.mom + (size_t)i * kSurNC * 9);
+#pragma unroll
+    for (int k = 0; k < kSurNC * 9 / 4; k++) {
+        const float4 t = mo[k];
+        mom[4 * k] = t.x; mom[4 * k + 1] = t.y; mom[4 * k + 2] = t.z; mom[4 * k + 3] = t.w;
+    }
 #pragma unroll
     for (int c = 0; c < kSurNC; c++)
         sur_channel_coeffs(mom + 9 * c, mom + 9 * c + 3, dr[kSurNR + c], dr[kSurNR + kSurNC + c],
                            dr[kSurNR + 2 * kSurNC + c], dr[kSurNR + 3 * kSurNC + c], a[c], B[c]);
-    const int ni = p.nl_count[i];
+    const int ni = min(p.nl_count[i], p.nl_cap);
+    const float4 *row = p.nl + (size_t)i * p.nl_cap;
+    float4 *fs = reinterpret_cast<float4 *>(p.fsur);
     float fx = 0.f, fy = 0.f, fz = 0.f;
-    for (int k = lane; k < ni; k += 32) {
-        const float4 e = p.nl[(size_t)i * p.nl_cap + k];
+    for (int k = 0; k < ni; k++) {
+        const float4 e = row[k];
         SurNb q;
         if (!sur_nb(e, p.rc, q)) continue;
         float h[3];
         sur_pair_grad(q, dr, a, B, h);
         // dE_i/dd_ij = h:  F_j -= h, F_i += h
         const int j = __float_as_int(e.w) >> 6;
-        atomicAdd(&p.fsur[3 * j], -h[0]);
-        atomicAdd(&p.fsur[3 * j + 1], -h[1]);
-        atomicAdd(&p.fsur[3 * j + 2], -h[2]);
+        atomicAdd(&fs[j], make_float4(-h[0], -h[1], -h[2], 0.f));
         fx += h[0]; fy += h[1]; fz += h[2];
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        fx += __shfl_xor_sync(0xffffffffu, fx, o);
-        fy += __shfl_xor_sync(0xffffffffu, fy, o);
-        fz += __shfl_xor_sync(0xffffffffu, fz, o);
-    }
-    if (lane == 0) {
-        atomicAdd(&p.fsur[3 * i], fx);
-        atomicAdd(&p.fsur[3 * i + 1], fy);
-        atomicAdd(&p.fsur[3 * i + 2], fz);
-    }
+    atomicAdd(&fs[i], make_float4(fx, fy, fz, 0.f));
 }
 
 // f[site] += fsur[slot] (then fsur = 0); with fout, the surrogate force is
@@ -311,11 +325,13 @@ __global__ void k_sur_apply(int n, const int *__restrict__ slot_site, float *__r
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= n) return;
     const int s = slot_site[slot];
+    float4 *f4 = reinterpret_cast<float4 *>(fsur);
+    const float4 v = f4[slot];
+    f4[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const double w[3] = {(double)v.x, (double)v.y, (double)v.z};
     for (int d = 0; d < 3; d++) {
-        const float v = fsur[3 * slot + d];
-        fsur[3 * slot + d] = 0.f;
-        if (fout) fout[3 * s + d] = (double)v;
-        else f[3 * s + d] += (double)v;
+        if (fout) fout[3 * s + d] = w[d];
+        else f[3 * s + d] += w[d];
     }
 }
 
@@ -434,14 +450,14 @@ __global__ void k_train_adam(TrainParams t, int step) {
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-void launch_sur_desc(SurParams &p, cudaStream_t st) { k_sur_desc<<<(p.n + 7) / 8, 256, 0, st>>>(p); }
+void launch_sur_desc(SurParams &p, cudaStream_t st) { k_sur_desc<<<(p.n + 127) / 128, 128, 0, st>>>(p); }
 void launch_sur_mlp(SurParams &p, cudaStream_t st) {
     const int tiles = (p.n + 15) / 16;
     int blocks = (tiles + 3) / 4;
-    if (blocks > 152 * 8) blocks = 152 * 8;
+    if (blocks > 152 * 4) blocks = 152 * 4;   // persistent: weights staged once per block
     k_sur_mlp<<<blocks, 128, 0, st>>>(p);
 }
-void launch_sur_force(SurParams &p, cudaStream_t st) { k_sur_force<<<(p.n + 7) / 8, 256, 0, st>>>(p); }
+void launch_sur_force(SurParams &p, cudaStream_t st) { k_sur_force<<<(p.n + 127) / 128, 128, 0, st>>>(p); }
 void launch_sur_apply(SurParams &p, const int *slot_site, double *f, double *fout, cudaStream_t st) {
     k_sur_apply<<<(p.n + 255) / 256, 256, 0, st>>>(p.n, slot_site, p.fsur, f, fout);
 }

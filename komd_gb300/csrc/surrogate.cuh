@@ -25,7 +25,7 @@ struct SurParams {
     float *mom;                  // n x 36 moments (M1 3 + M2 6 per channel)
     float *dedx;                 // n x 32 dE/dx
     float *e_site;               // n per-site energies (physical units)
-    float *fsur;                 // n x 3 surrogate forces (slot order, accumulated)
+    float *fsur;                 // n x 4 surrogate forces (slot order, xyz + pad, accumulated; 16-byte aligned)
     const __nv_bfloat16 *w1, *w1t, *w2, *w2t;
     const float *b1, *b2, *w3;
     float b3, e_scale, e_shift;
