@@ -202,6 +202,95 @@ def run_reference(args, w, name):
     return 0
 
 
+REPLICAS = dict(count=512, n_min=2000, n_max=20000, rho=(0.70, 0.90), t=(0.6, 1.5), seed=2027, rc=2.5, rc3=2.0,
+                nu=0.073, dt=0.005, skin=0.3, cell_min=2.8, rdf_max=2.5, rdf_bins=200)
+
+
+def replica_specs(count, seed):
+    rng = np.random.default_rng(seed)
+    return [(int(rng.integers(1 << 30)), int(rng.integers(REPLICAS["n_min"], REPLICAS["n_max"] + 1)),
+             float(rng.uniform(*REPLICAS["rho"])), float(rng.uniform(*REPLICAS["t"]))) for _ in range(count)]
+
+
+def replicas_leg(args, stream, local):
+    """Batched replicas: 512 periodic LJ + ATM argon boxes, N ~ U[2000, 20000]
+    (FCC filled, trimmed at random by seed), rho* ~ U[0.70, 0.90],
+    T* ~ U[0.6, 1.5], FP32 forces / FP64 integration; all replicas advance
+    in one CUDA-graph launch per graph (komd_batch).  Compared with the same
+    replicas stepped one after another through the single-system path; then
+    per-replica RDF (200 bins to 2.5) and virial pressure."""
+    import torch
+    from komd_gb300 import gpu, komd_io, lattice
+    R = REPLICAS
+    t0 = time.perf_counter()
+    reps, n_atoms, vols, sizes = [], 0, [], []
+    for seed, n, rho, t_star in replica_specs(args.replicas, R["seed"]):
+        s = lattice.trimmed_fcc(n, rho, t_star, seed)
+        L = float(s.high[0])
+        cell = L / np.floor(L / R["cell_min"])
+        cfg = gpu.make_config(s.low, s.high, cell, cutoff=R["rc"], cutoff_3b=R["rc3"], nu=R["nu"], dt=R["dt"],
+                              terms=gpu.TERM_LJ | gpu.TERM_ATM, precision=gpu.FP32, atm_sign=gpu.ATM_SIGN_PHYSICAL,
+                              atm_enum=gpu.ATM_ENUM_FULL, virial_mode=gpu.VIRIAL_CORRECT, skin=R["skin"],
+                              rdf_max=R["rdf_max"], rdf_dr=R["rdf_max"] / R["rdf_bins"])
+        g = gpu.GpuSystem(s, cfg, device=local)
+        g.update_container()
+        g.forces()
+        reps.append(g)
+        sizes.append(s.n)
+        n_atoms += s.n
+        vols.append(float(np.prod(s.high - s.low)))
+    setup_s = time.perf_counter() - t0
+    k = args.replica_steps
+    # sequential: each replica through komd_gpu_step (its own graph), one after another
+    for g in reps:
+        g.step(3)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for g in reps:
+        g.step(k)
+    torch.cuda.synchronize()
+    seq_s = time.perf_counter() - t1
+    # batched: one graph per steps_per_graph steps of all replicas
+    spg = args.replica_graph_steps
+    t2 = time.perf_counter()
+    batch = gpu.Batch(reps, n_streams=args.replica_streams, steps_per_graph=spg, stream=stream.cuda_stream)
+    capture_s = time.perf_counter() - t2
+    batch.step(max(1, 3 // spg))
+    torch.cuda.synchronize()
+    n_graphs = max(1, k // spg)
+    with ClockSampler(local) as clk:
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        batch.launch(n_graphs)
+        b.record(stream)
+        batch.check()
+    ms = a.elapsed_time(b)
+    steps = n_graphs * spg
+    value = n_atoms * steps / (ms / 1e3)
+    seq_value = n_atoms * k / seq_s
+    batch.close()
+    # per-replica observables after the run
+    pres, peaks, temps = [], [], []
+    dr = R["rdf_max"] / R["rdf_bins"]
+    for g, vol, n in zip(reps, vols, sizes):
+        o = g.measure(gpu.MEASURE_PRESSURE | gpu.MEASURE_RDF | gpu.MEASURE_TEMPERATURE)
+        pres.append((o["pressure"][0] + o["pressure"][2] + o["pressure"][5]) / (3.0 * vol))
+        r, gr = komd_io.rdf_normalise(o["rdf"], 1, dr, vol, n)
+        peaks.append(float(r[int(np.argmax(gr))]))
+        temps.append(o["temperature"])
+        g.close()
+    return {"value": value, "unit": UNIT, "replicas": len(reps), "atoms": n_atoms, "steps": steps,
+            "ms_per_step": ms / steps, "sequential": {"value": seq_value, "steps": k, "s": seq_s},
+            "speedup_vs_sequential": value / seq_value, "streams": args.replica_streams,
+            "steps_per_graph": spg, "setup_s": setup_s, "capture_s": capture_s, "clocks": clk.summary(),
+            "pressure_star": {"min": float(np.min(pres)), "median": float(np.median(pres)), "max": float(np.max(pres))},
+            "rdf_first_peak_r": {"min": float(np.nanmin(peaks)), "median": float(np.nanmedian(peaks)),
+                                 "max": float(np.nanmax(peaks))},
+            "config": "512 LJ+ATM argon boxes, N~U[2000,20000] FCC-trimmed, rho*~U[0.70,0.90], T*~U[0.6,1.5], "
+                      "rc 2.5 / 2.0, nu* 0.073, dt* 0.005, skin 0.3; RDF 200 bins to 2.5, virial pressure per replica"}
+
+
 def surrogate_leg(args, g, s, stream, local, dist, exact_value, world):
     """FP32 + learned three-body form of the same workload: training set from
     the exact kernel (2000 snapshots of 500 atoms over T* in [0.6, 1.2],
@@ -349,6 +438,9 @@ def run_ours(args, w, name):
     sur = None
     if w["atm"] and not args.no_surrogate:
         sur = surrogate_leg(args, g, s, stream, local, dist, value, world)
+    reps = None
+    if args.replicas > 0:
+        reps = replicas_leg(args, stream, local)
 
     if rank != 0:
         if dist:
@@ -403,6 +495,8 @@ def run_ours(args, w, name):
         line["cpu_baseline"] = cb
     if sur:
         line["surrogate"] = sur
+    if reps:
+        line["replicas"] = reps
     print(json.dumps(line), flush=True)
     g.close()
     if dist:
@@ -423,6 +517,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the learned three-body leg")
     ap.add_argument("--sur-epochs", type=int, default=30)
+    ap.add_argument("--replicas", type=int, default=512, help="batched-replica leg (0 = skip)")
+    ap.add_argument("--replica-steps", type=int, default=20)
+    ap.add_argument("--replica-streams", type=int, default=32)
+    ap.add_argument("--replica-graph-steps", type=int, default=5)
     ap.add_argument("--sur-probe", type=int, default=50, help="exact-ATM probe interval of the learned form")
     ap.add_argument("--sur-threshold", type=float, default=0.2,
                     help="probe breach (relative three-body force RMSE) that switches back to exact ATM")

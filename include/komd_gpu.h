@@ -250,6 +250,24 @@ int     komd_sur_fit_grad(komd_sur_data *d, const float *params, const float *fm
                           double e_scale, double e_shift, double f2, float lam_e, float lam_f, float *grad,
                           double *loss);
 
+/* ---- batched replicas (no reference counterpart) ----------------------- */
+/* Independent engines (replicas of uneven sizes, each created, uploaded and
+ * past update_container + forces) advance together: one CUDA graph holds
+ * steps_per_graph steps of every replica, spread over n_streams parallel
+ * branches.  stream (may be NULL) is the stream the graph is launched on.
+ * Replicas must not be modified (upload, set_state, update_container) while
+ * the batch exists; the exact forces run (no learned-term probes). */
+typedef struct komd_batch komd_batch;
+int  komd_batch_create(komd_gpu *const *replicas, int32_t n, int32_t n_streams, int32_t steps_per_graph,
+                       void *stream, komd_batch **out);
+void komd_batch_destroy(komd_batch *b);
+/* n_graphs launches of the graph (n_graphs * steps_per_graph steps), then a
+ * synchronisation and every replica's error-flag check. */
+int  komd_batch_step(komd_batch *b, int64_t n_graphs);
+/* Launches only (asynchronous); komd_batch_check synchronises and checks. */
+int  komd_batch_launch(komd_batch *b, int64_t n_graphs);
+int  komd_batch_check(komd_batch *b);
+
 /* ---- profiling ---------------------------------------------------------- */
 /* When enabled, every kernel launch outside komd_gpu_step's graph is
  * bracketed by CUDA events; komd_gpu_profile reports per kernel family the

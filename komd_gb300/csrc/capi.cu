@@ -1407,6 +1407,148 @@ int komd_gpu_profile(komd_gpu *h, int max_families, int64_t *launches, double *m
     return kNumFamilies;
 }
 
+// ---------------------------------------------------------------------------
+// batched replicas: one CUDA graph advances every replica by steps_per_graph
+// steps; replicas are spread over n_streams parallel branches of the graph
+// (fork/join through events), each replica's steps in order on its branch
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+struct komd_batch {
+    std::vector<komd_gpu *> reps;
+    int n_streams = 1, steps_per_graph = 1, device = 0;
+    cudaStream_t origin = nullptr;
+    bool own_origin = false;
+    std::vector<cudaStream_t> branch;
+    std::vector<cudaEvent_t> ev;          // [0] fork, [1..n_streams] joins
+    cudaGraphExec_t graph = nullptr;
+    int64_t steps = 0;
+    ~komd_batch() {
+        cudaSetDevice(device);
+        if (graph) cudaGraphExecDestroy(graph);
+        for (auto s : branch) cudaStreamDestroy(s);
+        for (auto e : ev) cudaEventDestroy(e);
+        if (own_origin && origin) cudaStreamDestroy(origin);
+    }
+};
+
+namespace {
+int batch_capture(komd_batch *b) {
+    CK(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal));
+    cudaError_t ce = cudaEventRecord(b->ev[0], b->origin);
+    for (int k = 0; k < b->n_streams && ce == cudaSuccess; k++) ce = cudaStreamWaitEvent(b->branch[k], b->ev[0], 0);
+    if (ce == cudaSuccess) {
+        for (size_t r = 0; r < b->reps.size(); r++) {
+            Engine &e = b->reps[r]->e;
+            cudaStream_t keep = e.stream;
+            e.stream = b->branch[r % b->n_streams];
+            for (int k = 0; k < b->steps_per_graph; k++) enqueue_step(b->reps[r]);
+            e.stream = keep;
+        }
+        for (int k = 0; k < b->n_streams && ce == cudaSuccess; k++) {
+            ce = cudaEventRecord(b->ev[1 + k], b->branch[k]);
+            if (ce == cudaSuccess) ce = cudaStreamWaitEvent(b->origin, b->ev[1 + k], 0);
+        }
+    }
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(b->origin, &graph);
+    if (ce != cudaSuccess || ee != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return fail(KOMD_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(ce != cudaSuccess ? ce : ee));
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&b->graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) return fail(KOMD_ERR_CUDA, std::string("batch graph instantiate: ") + cudaGetErrorString(ie));
+    return KOMD_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int komd_batch_create(komd_gpu *const *replicas, int32_t n, int32_t n_streams, int32_t steps_per_graph,
+                      void *stream, komd_batch **out) {
+    if (!replicas || !out || n <= 0 || n_streams <= 0 || n_streams > 128 || steps_per_graph <= 0 ||
+        steps_per_graph > 1000)
+        return fail(KOMD_ERR_ARG, "bad batch arguments");
+    const int dev = replicas[0] ? replicas[0]->e.device : 0;
+    for (int r = 0; r < n; r++) {
+        komd_gpu *h = replicas[r];
+        if (!h) return fail(KOMD_ERR_ARG, "null replica");
+        if (h->e.device != dev) return fail(KOMD_ERR_ARG, "replicas on different devices");
+        if (!h->e.have_forces) return fail(KOMD_ERR_STATE, "every replica needs update_container and forces first");
+        if (surrogate_on(h)) return fail(KOMD_ERR_ARG, "replicas run the exact forces (no host-side probes)");
+        if (h->e.profiling) return fail(KOMD_ERR_STATE, "switch profiling off before batching");
+        for (int q = 0; q < r; q++)
+            if (replicas[q] == h) return fail(KOMD_ERR_ARG, "a replica appears twice");
+    }
+    CK(cudaSetDevice(dev));
+    komd_batch *b = new komd_batch();
+    b->device = dev;
+    b->reps.assign(replicas, replicas + n);
+    b->n_streams = std::min<int>(n_streams, n);
+    b->steps_per_graph = steps_per_graph;
+    auto bail = [&](int rc) { delete b; return rc; };
+    if (stream) {
+        b->origin = (cudaStream_t)stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking) != cudaSuccess)
+            return bail(fail(KOMD_ERR_CUDA, "stream creation failed"));
+        b->own_origin = true;
+    }
+    for (int k = 0; k < b->n_streams; k++) {
+        cudaStream_t s;
+        if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
+            return bail(fail(KOMD_ERR_CUDA, "stream creation failed"));
+        b->branch.push_back(s);
+    }
+    for (int k = 0; k <= b->n_streams; k++) {
+        cudaEvent_t e;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+            return bail(fail(KOMD_ERR_CUDA, "event creation failed"));
+        b->ev.push_back(e);
+    }
+    // the replicas' own queues must be drained before the batch graph runs
+    for (auto h : b->reps)
+        if (cudaStreamSynchronize(h->e.stream) != cudaSuccess) return bail(fail(KOMD_ERR_CUDA, "replica stream"));
+    int rc = batch_capture(b);
+    if (rc) return bail(rc);
+    *out = b;
+    return KOMD_OK;
+}
+
+void komd_batch_destroy(komd_batch *b) { delete b; }
+
+int komd_batch_step(komd_batch *b, int64_t n_graphs) {
+    if (!b) return fail(KOMD_ERR_ARG, "null batch");
+    CK(cudaSetDevice(b->device));
+    for (int64_t k = 0; k < n_graphs; k++) CK(cudaGraphLaunch(b->graph, b->origin));
+    CK(cudaStreamSynchronize(b->origin));
+    b->steps += n_graphs * b->steps_per_graph;
+    for (size_t r = 0; r < b->reps.size(); r++) {
+        int rc = finish_steps(b->reps[r]);
+        if (rc) return fail(rc, "replica " + std::to_string(r) + ": " + g_last_error);
+    }
+    return KOMD_OK;
+}
+
+// enqueue only (no synchronisation, no flag check): for timing with events on the origin stream
+int komd_batch_launch(komd_batch *b, int64_t n_graphs) {
+    if (!b) return fail(KOMD_ERR_ARG, "null batch");
+    for (int64_t k = 0; k < n_graphs; k++) CK(cudaGraphLaunch(b->graph, b->origin));
+    b->steps += n_graphs * b->steps_per_graph;
+    return KOMD_OK;
+}
+
+int komd_batch_check(komd_batch *b) {
+    if (!b) return fail(KOMD_ERR_ARG, "null batch");
+    CK(cudaStreamSynchronize(b->origin));
+    for (size_t r = 0; r < b->reps.size(); r++) {
+        int rc = finish_steps(b->reps[r]);
+        if (rc) return fail(rc, "replica " + std::to_string(r) + ": " + g_last_error);
+    }
+    return KOMD_OK;
+}
+
 int komd_gpu_kernels_per_step(komd_gpu *h) {
     if (!h) return -1;
     const Engine &e = h->e;

@@ -36,6 +36,7 @@ EXPORTS = [
     "komd_gpu_surrogate_sample", "komd_gpu_surrogate_forces", "komd_gpu_surrogate_status", "komd_mlp_train",
     "komd_mlp_loss_grad", "komd_sur_data_create", "komd_sur_data_destroy", "komd_gpu_surrogate_capture",
     "komd_sur_data_snapshots", "komd_sur_data_sites", "komd_sur_data_get", "komd_sur_fit", "komd_sur_fit_grad",
+    "komd_batch_create", "komd_batch_destroy", "komd_batch_step", "komd_batch_launch", "komd_batch_check",
 ]
 
 
@@ -131,6 +132,12 @@ def load() -> C.CDLL:
     L.komd_sur_data_sites.argtypes = [P]
     L.komd_sur_data_get.argtypes = [P, I64, P, P, P, P]
     L.komd_sur_fit.argtypes = [P, P, P, P, C.c_double, C.c_double, C.c_double, C.POINTER(SurFitOpts), P]
+    L.komd_batch_create.argtypes = [P, I32, I32, I32, P, C.POINTER(P)]
+    L.komd_batch_destroy.argtypes = [P]
+    L.komd_batch_destroy.restype = None
+    L.komd_batch_step.argtypes = [P, I64]
+    L.komd_batch_launch.argtypes = [P, I64]
+    L.komd_batch_check.argtypes = [P]
     L.komd_sur_fit_grad.argtypes = [P, P, P, P, C.c_double, C.c_double, C.c_double, C.c_float, C.c_float, P, P]
     _lib = L
     return L
@@ -397,6 +404,47 @@ class SurData:
     def close(self):
         if self.h:
             self.L.komd_sur_data_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Replicas (GpuSystem objects, each past update_container + forces)
+    advanced together by one CUDA graph of steps_per_graph steps each."""
+
+    def __init__(self, systems, n_streams=16, steps_per_graph=1, stream=None):
+        self.L = load()
+        self.systems = list(systems)
+        arr = (C.c_void_p * len(self.systems))(*[g.h.value if isinstance(g.h, C.c_void_p) else g.h
+                                                 for g in self.systems])
+        self.h = C.c_void_p()
+        self.steps_per_graph = int(steps_per_graph)
+        rc = self.L.komd_batch_create(arr, len(self.systems), int(n_streams), self.steps_per_graph, stream,
+                                      C.byref(self.h))
+        if rc != KOMD_OK:
+            raise KomdError(rc, self.L.komd_gpu_last_error().decode())
+
+    def _check(self, rc):
+        if rc != KOMD_OK:
+            raise KomdError(rc, self.L.komd_gpu_last_error().decode())
+
+    def step(self, n_graphs=1):
+        self._check(self.L.komd_batch_step(self.h, int(n_graphs)))
+
+    def launch(self, n_graphs=1):
+        self._check(self.L.komd_batch_launch(self.h, int(n_graphs)))
+
+    def check(self):
+        self._check(self.L.komd_batch_check(self.h))
+
+    def close(self):
+        if self.h:
+            self.L.komd_batch_destroy(self.h)
             self.h = C.c_void_p()
 
     def __del__(self):

@@ -163,3 +163,13 @@ def read_checkpoint(path: str, low=(0, 0, 0), high=(10, 10, 10), offset=(0.0, 0.
 def rdf_nbins(max_r: float, dr: float) -> int:
     """(uint64)(max_r / dr), RDFSensor.cpp:18."""
     return int(math.trunc(max_r / dr))
+
+
+def rdf_normalise(bins: np.ndarray, samples: int, dr: float, volume: float, n: int):
+    """(r, g(r)) from a raw histogram of ordered molecule pairs, as
+    RDFSensor::write (RDFSensor.cpp:45-60): bin centres r = (k + 1/2) dr,
+    g = (bins/samples) V / (shell volume * n (n - 1))."""
+    b = np.asarray(bins, np.float64) / max(samples, 1)
+    r = (np.arange(b.size) + 0.5) * dr
+    v_bin = 4.0 / 3.0 * math.pi * ((r + 0.5 * dr) ** 3 - (r - 0.5 * dr) ** 3)
+    return r, b * volume / (v_bin * n * (n - 1.0))
