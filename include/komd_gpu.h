@@ -58,6 +58,11 @@ enum { KOMD_VIRIAL_COMPAT = 0, KOMD_VIRIAL_CORRECT = 1 };
 /* with KOMD_TERM_ATM: the learned three-body form (no reference counterpart)
  * replaces the exact triplet sum once komd_gpu_surrogate_load has run */
 #define KOMD_TERM_ATM_SURROGATE 0x20u
+/* with KOMD_TERM_LJ: ATM2B effective pair force (potentials/ATM2B.cpp:9-56,
+ * main.cpp:57-58 enable_3b_approx): LJ forces times 1 - 2 nu rho / (3 eps sigma^6),
+ * rho = molecules / domain volume, eps and sigma of the first uploaded site;
+ * the LJ energy and virial sensors stay unscaled as in the reference */
+#define KOMD_TERM_ATM2B 0x40u
 
 /* measurements (bit mask) */
 #define KOMD_MEASURE_TEMPERATURE 0x01u  /* sensors/TemperatureSensor.cpp:27-48   */
@@ -92,6 +97,10 @@ typedef struct komd_config {
                                   rebuilds cells and list only when a site has moved more than
                                   skin/2 (FP32, no FENE, FULL ATM, CORRECT virial); 0 rebuilds
                                   every step like LinkedCells::updateContainer */
+    double temperature_target; /* VelocityScaling target in K (configuration()->temperature)   */
+    int32_t thermostat;        /* 1: each step of komd_gpu_step ends with v *= sqrt(T_target / T),
+                                  T measured on the device as TemperatureSensor does
+                                  (VelocityScaling.cpp:12-25, Simulation.cpp:72) */
 } komd_config;
 
 typedef struct komd_observables {
@@ -176,6 +185,10 @@ int  komd_gpu_get_cells(komd_gpu *h, int64_t *count, int64_t ncell, int64_t *idx
  * molecule ID, evaluated in FP64 with the reference's arithmetic
  * (LJ12_6.cpp:23-28), so counts are bit-exact. */
 int  komd_gpu_neighbour_counts(komd_gpu *h, int64_t *counts);
+
+/* VelocityScaling::apply (VelocityScaling.cpp:12-25) with the caller's
+ * beta = sqrt(T_target / T_sensor): v *= beta for every site. */
+int  komd_gpu_scale_velocities(komd_gpu *h, double beta);
 
 /* ---- learned three-body term (no reference counterpart) ----------------- */
 /* A 32-64-64-1 tanh MLP on per-site descriptors inside cutoff_3b (16 radial

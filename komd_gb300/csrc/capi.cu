@@ -44,26 +44,8 @@ cudaError_t dalloc(T *&p, size_t count) {
     return cudaMalloc(reinterpret_cast<void **>(&p), sizeof(T) * count);
 }
 
-// SciValue arithmetic (math/SciValue.{h,cpp}): mantissa normalised into
-// (0.1, 10) by repeated /10, *10; converted as m * pow(10, e).
-struct Sci { double m; long long e; };
-Sci sci_norm(double m, long long e) {
-    double a = std::fabs(m);
-    while (a >= 10.0) { m /= 10.0; e += 1; a = std::fabs(m); }
-    while (a <= 0.1) { m *= 10.0; e -= 1; a = std::fabs(m); }
-    return {m, e};
-}
-Sci sci_from(double v) { return v == 0.0 ? Sci{0.0, 0} : sci_norm(v, 0); }
-Sci sci_mul(Sci a, Sci b) { return sci_norm(a.m * b.m, a.e + b.e); }
-Sci sci_div(Sci a, Sci b) { return sci_norm(a.m / b.m, a.e - b.e); }
-double sci_val(Sci a) { return a.m * std::pow(10.0, (double)a.e); }
-
-// TemperatureSensor's conversion (TemperatureSensor.cpp:44-47)
-double temperature_from(double mv2, double n_in_box) {
-    const Sci kB = sci_norm(1.380649, -23), da = sci_norm(1.66053906892, -27), aps = sci_norm(1.0, 2);
-    const Sci factor = sci_mul(sci_mul(aps, aps), sci_div(da, kB));
-    return sci_val(sci_mul(factor, sci_from(mv2 / (n_in_box * 3))));
-}
+// TemperatureSensor's conversion (TemperatureSensor.cpp:44-47), restated in engine.cuh
+double temperature_from(double mv2, double n_in_box) { return sci_temperature(mv2, n_in_box); }
 
 // ---------------------------------------------------------------------------
 // profiling: event pairs per kernel family
@@ -98,6 +80,7 @@ struct komd_gpu {
     Surrogate sur;
     double *f_scratch = nullptr;
     double *acc = nullptr;            // R_NSLOTS
+    double *thermo_acc = nullptr;     // R_NSLOTS, the device thermostat's kinetic sums
     int partial_cap = 0;
     bool want_posd = false;
     // profiling
@@ -255,6 +238,13 @@ void enqueue_step(komd_gpu *h) {
         ProfScope ps(h, F_INTEGRATE);
         launch_step1(e, e.stream);
     }
+    if (e.cfg.thermostat) {   // Simulation.cpp:72, after the step's sensors
+        ProfScope ps(h, F_INTEGRATE);
+        cudaMemsetAsync(h->thermo_acc, 0, sizeof(double) * R_NSLOTS, e.stream);
+        launch_kinetic(e, e.stream, 0);
+        launch_sum_partials(e.stream, kinetic_grid(e), e.partials, h->thermo_acc);
+        launch_velocity_scale(e, e.stream, h->thermo_acc, 1.0);
+    }
 }
 
 int read_flags(komd_gpu *h, int flags[E_NFLAGS], bool clear) {
@@ -328,6 +318,8 @@ int validate(const komd_config *c, Grid &g) {
     if (!(c->cell_size > 0)) return fail(KOMD_ERR_ARG, "cell_size must be > 0");
     const bool lj = (c->terms & KOMD_TERM_LJ) != 0, atm = (c->terms & KOMD_TERM_ATM) != 0;
     if (lj && !(c->cutoff > 0)) return fail(KOMD_ERR_ARG, "cutoff must be > 0");
+    if (c->thermostat && !(c->temperature_target > 0)) return fail(KOMD_ERR_ARG, "thermostat needs temperature_target > 0");
+    if ((c->terms & KOMD_TERM_ATM2B) && !lj) return fail(KOMD_ERR_ARG, "KOMD_TERM_ATM2B scales the LJ term: set KOMD_TERM_LJ");
     if (c->cell_size < c->cutoff)
         return fail(KOMD_ERR_ARG, "cell size must be larger or equal to cutoff radius");
     if (atm && (!(c->cutoff_3b > 0) || c->cell_size < c->cutoff_3b))
@@ -383,7 +375,7 @@ int komd_gpu_create(const komd_config *cfg, int device, komd_gpu **out) {
     }
     e.own_stream = true;
     if (dalloc(e.cell_count, g.ncell) || dalloc(e.cell_start, g.ncell + 1) || dalloc(e.cell_mcount, g.ncell) ||
-        dalloc(e.cell_mstart, g.ncell + 1) || dalloc(e.err, E_NFLAGS) || dalloc(h->acc, R_NSLOTS)) {
+        dalloc(e.cell_mstart, g.ncell + 1) || dalloc(e.err, E_NFLAGS) || dalloc(h->acc, R_NSLOTS) || dalloc(h->thermo_acc, R_NSLOTS)) {
         komd_gpu_destroy(h);
         return fail(KOMD_ERR_NOMEM, "device allocation failed");
     }
@@ -459,7 +451,7 @@ int komd_gpu_destroy(komd_gpu *h) {
     dfree(e.cell_count); dfree(e.cell_start); dfree(e.cell_mcount); dfree(e.cell_mstart); dfree(e.cell_mols);
     dfree(e.slot_site); dfree(e.skey); dfree(e.pos4); dfree(e.seps); dfree(e.posd); dfree(e.seps_d); dfree(e.sig_d);
     dfree(e.nl); dfree(e.nl_count); dfree(e.bonds); dfree(e.angles); dfree(e.partials); dfree(e.err);
-    dfree(e.rdf); dfree(e.lj_hist); dfree(e.counts); dfree(h->f_scratch); dfree(h->acc); dfree(e.offtab);
+    dfree(e.rdf); dfree(e.lj_hist); dfree(e.counts); dfree(h->f_scratch); dfree(h->acc); dfree(h->thermo_acc); dfree(e.offtab);
     dfree(e.nboff); dfree(e.rebuild); dfree(e.img); dfree(e.ref); dfree(e.slot_cell); dfree(e.vl); dfree(e.vl_count);
     dfree(e.rebuild_count); dfree(e.hdtm); dfree(e.exact_com);
     {
@@ -562,6 +554,13 @@ int komd_gpu_upload_sites(komd_gpu *h, int64_t n, const double *r, const double 
         for (int64_t s = 1; s < n && e.uniform; s++) e.uniform = eps[s] == eps[0] && sig[s] == sig[0];
         e.eps0 = (float)eps[0];
         e.sig0 = (float)sig[0];
+        e.lj_fscale = 1.0;
+        if (e.cfg.terms & KOMD_TERM_ATM2B) {
+            // ATM2B::ATM2B (ATM2B.cpp:9-20): 1 - 2 nu rho / (3 eps sigma^6), number density of molecules
+            const double rho = (double)e.n_mol / (e.g.L[0] * e.g.L[1] * e.g.L[2]);
+            const double sig6 = std::pow(sig[0], 6);
+            e.lj_fscale = 1.0 - ((2 * e.cfg.nu * rho) / (3 * eps[0] * sig6));
+        }
     }
     // ATM list capacity: 1.6x the mean neighbour count inside cutoff_3b + 16
     int cap = e.cfg.atm_list_cap;
@@ -802,6 +801,16 @@ int komd_gpu_step_host(komd_gpu *h, int64_t n_steps, double *r, double *v, doubl
     int rc = komd_gpu_step(h, n_steps);
     if (rc) return rc;
     return komd_gpu_download(h, r, v, f);
+}
+
+int komd_gpu_scale_velocities(komd_gpu *h, double beta) {
+    if (!h || !h->e.have_sites) return fail(KOMD_ERR_STATE, "no sites uploaded");
+    if (!std::isfinite(beta)) return fail(KOMD_ERR_ARG, "non-finite scaling factor");
+    launch_velocity_scale(h->e, h->e.stream, nullptr, beta);
+    int rc = check_launch("scale_velocities");
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(h->e.stream));
+    return KOMD_OK;
 }
 
 int64_t komd_gpu_rdf_bins(komd_gpu *h) { return h ? h->e.rdf_bins : -1; }
@@ -1557,6 +1566,7 @@ int komd_gpu_kernels_per_step(komd_gpu *h) {
     if ((e.cfg.terms & KOMD_TERM_BONDED) && e.n_bonds > 0) k++;
     if ((e.cfg.terms & KOMD_TERM_BONDED) && e.n_angles > 0) k++;
     if (e.cfg.terms & KOMD_TERM_LIMIT) k++;
+    if (e.cfg.thermostat) k += 3;  /* kinetic sums, partial reduction, velocity scaling */
     if (surrogate_on(h)) k += 4;   /* descriptors, MLP, forces, apply */
     else if (e.cfg.terms & KOMD_TERM_ATM) k++;
     return k;

@@ -139,6 +139,8 @@ struct PairParams {
     const float4 *nboff;
     int *rebuild_count;
     float eps0, sig0;
+    float lj_fscalef;          // ATM2B force factor (1 without ATM2B), force path only
+    double lj_fscale;
 };
 
 struct AtmParams {
@@ -156,6 +158,37 @@ struct AtmParams {
     int atm_direct;            // COMPAT + direct: no virial contribution
     double *e_site;            // measure: per-site V/3 sums (site order), optional
 };
+
+// TemperatureSensor's conversion (TemperatureSensor.cpp:44-47) in SciValue
+// arithmetic (math/SciValue.{h,cpp}): mantissas normalised into (0.1, 10) by
+// repeated /10 and *10, converted as m * 10^e.  10^e is exact for 0 <= e <= 22
+// and 1 / 10^-e (one correctly rounded division) below; host and device
+// evaluate the same IEEE operations, so both give the same temperature.
+struct SciNum { double m; int e; };
+__host__ __device__ inline SciNum sci_norm(double m, int e) {
+    double a = fabs(m);
+    while (a >= 10.0) { m = m / 10.0; e += 1; a = fabs(m); }
+    while (a <= 0.1 && a > 0.0) { m = m * 10.0; e -= 1; a = fabs(m); }
+    return {m, e};
+}
+__host__ __device__ inline double sci_pow10(int e) {
+    double p = 1.0;
+    const int k = e < 0 ? -e : e;
+    for (int i = 0; i < k && i < 22; i++) p = p * 10.0;
+    for (int i = 22; i < k; i++) p = p * 10.0;   // beyond 1e22 no longer exact (not reached here)
+    return e < 0 ? 1.0 / p : p;
+}
+__host__ __device__ inline double sci_temperature(double mv2, double n_in_box) {
+    if (!(n_in_box > 0.0)) return 0.0;
+    const SciNum kB = sci_norm(1.380649, -23), da = sci_norm(1.66053906892, -27), aps = sci_norm(1.0, 2);
+    SciNum f = sci_norm(aps.m * aps.m, aps.e + aps.e);
+    const SciNum q = sci_norm(da.m / kB.m, da.e - kB.e);
+    f = sci_norm(f.m * q.m, f.e + q.e);
+    const double x = mv2 / (n_in_box * 3);
+    const SciNum v = x == 0.0 ? SciNum{0.0, 0} : sci_norm(x, 0);
+    const SciNum t = sci_norm(f.m * v.m, f.e + v.e);
+    return t.m * sci_pow10(t.e);
+}
 
 struct Engine {
     komd_config cfg;
@@ -219,6 +252,7 @@ struct Engine {
     // all sites share eps and sigma: the list kernel uses constants
     bool uniform = false;
     float eps0 = 1.f, sig0 = 1.f;
+    double lj_fscale = 1.0;         // ATM2B factor (KOMD_TERM_ATM2B), else 1
     double *atm_esite = nullptr;     // when set, measure-mode ATM writes per-site energies here
 };
 

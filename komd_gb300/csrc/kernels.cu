@@ -345,6 +345,7 @@ __global__ void __launch_bounds__(kBlock) k_pair(PairParams p) {
                         fac = ljd * inv;
                         u = 4.0f * e * (lj12 - lj6);
                     }
+                    if (!MEASURE) fac *= (Real)p.lj_fscale;   // ATM2B (1 otherwise); sensors stay unscaled
                     fx += dx * fac; fy += dy * fac; fz += dz * fac;
                     if (MEASURE) {
                         const double wt = vir_full ? 1.0 : 0.5;
@@ -992,6 +993,26 @@ __global__ void k_sum_partials(int nblocks, const double *__restrict__ partials,
     if (lane == 0) out[slot] += s;
 }
 
+// VelocityScaling (VelocityScaling.cpp:12-25): v *= beta; beta from the
+// caller, or (acc != nullptr) sqrt(T_target / T) with T from the summed
+// kinetic slots as TemperatureSensor computes it
+__global__ void k_velocity_scale(int n, double *__restrict__ v, const double *__restrict__ acc, double t_target,
+                                 double beta_in) {
+    __shared__ double s_beta;
+    if (threadIdx.x == 0) {
+        double beta = beta_in;
+        if (acc) {
+            const double t = sci_temperature(acc[R_MV2], acc[R_NBOX]);
+            beta = t > 0.0 ? __dsqrt_rn(__ddiv_rn(t_target, t)) : 1.0;
+        }
+        s_beta = beta;
+    }
+    __syncthreads();
+    const double beta = s_beta;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < 3 * n; k += gridDim.x * blockDim.x)
+        v[k] = __dmul_rn(v[k], beta);
+}
+
 // ===========================================================================
 // launchers
 // ===========================================================================
@@ -1048,6 +1069,8 @@ PairParams pair_params(Engine &e) {
     if (atm && p.rc3sq > p.scan2) p.scan2 = p.rc3sq;
     p.stiffness = e.cfg.stiffness;
     p.use_lj = lj ? 1 : 0;
+    p.lj_fscale = e.lj_fscale;
+    p.lj_fscalef = (float)e.lj_fscale;
     p.virial_compat = e.cfg.virial_mode == KOMD_VIRIAL_COMPAT;
     p.offtab = e.offtab;
     p.rebuild = e.rebuild;
@@ -1186,6 +1209,11 @@ void launch_step1(Engine &e, cudaStream_t st) {
 }
 
 int kinetic_grid(const Engine &e) { return nblk(e.n, kBlock); }
+
+void launch_velocity_scale(Engine &e, cudaStream_t st, const double *acc, double beta) {
+    const int blocks = std::min(nblk(3 * e.n, 256), 152 * 8);
+    k_velocity_scale<<<blocks, 256, 0, st>>>((int)e.n, e.v, acc, e.cfg.temperature_target, beta);
+}
 
 void launch_kinetic(Engine &e, cudaStream_t st, int n_terms) {
     k_kinetic<<<kinetic_grid(e), kBlock, 0, st>>>(e.g, (int)e.n, n_terms, e.r, e.v, e.m, e.partials);

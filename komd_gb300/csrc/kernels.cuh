@@ -17,6 +17,7 @@ void launch_atm(Engine &e, cudaStream_t st, bool measure);
 void launch_step0(Engine &e, cudaStream_t st);
 void launch_step1(Engine &e, cudaStream_t st);
 void launch_kinetic(Engine &e, cudaStream_t st, int n_terms);
+void launch_velocity_scale(Engine &e, cudaStream_t st, const double *acc, double beta);
 void launch_sum_partials(cudaStream_t st, int nblocks, const double *partials, double *out);
 void launch_rdf(Engine &e, cudaStream_t st, double *bins, bool cells);
 void set_kernel_attributes(Engine &e);

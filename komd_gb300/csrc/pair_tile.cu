@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(kTileThreads) k_pair_tile(PairParams p) {
                     const float lj6 = x * x * x;
                     const float ee = __int_as_float(s_haux[i].y) * __int_as_float(a.w);
                     const float ljd = 24.0f * ee * (2.0f * lj6 * lj6 - lj6);
-                    const float fac = ljd * inv;
+                    const float fac = MEASURE ? ljd * inv : ljd * inv * p.lj_fscalef;   // ATM2B factor
                     fx = dx * fac; fy = dy * fac; fz = dz * fac;
                     if (MEASURE) {
                         const float wt = (p.virial_compat && (a.z & 32)) ? 1.0f : 0.5f;
@@ -435,7 +435,8 @@ __global__ void __launch_bounds__(256, 5) k_lj_vlist(PairParams p, int n) {
                             ee = sei * sej[u];
                         }
                         const float lj6 = x * x * x;
-                        const float fac = 24.0f * ee * (2.0f * lj6 * lj6 - lj6) * inv;
+                        const float fac0 = 24.0f * ee * (2.0f * lj6 * lj6 - lj6) * inv;
+                        const float fac = MEASURE ? fac0 : fac0 * p.lj_fscalef;   // ATM2B factor
                         fx += dx * fac; fy += dy * fac; fz += dz * fac;
                         if (MEASURE) {
                             const float gx = dx * fac, gy = dy * fac, gz = dz * fac;

@@ -23,6 +23,7 @@ ATM_ENUM_COMPAT, ATM_ENUM_FULL = 0, 1
 VIRIAL_COMPAT, VIRIAL_CORRECT = 0, 1
 
 TERM_LJ, TERM_FENE, TERM_LIMIT, TERM_ATM, TERM_BONDED, TERM_ATM_SURROGATE = 0x01, 0x02, 0x04, 0x08, 0x10, 0x20
+TERM_ATM2B = 0x40
 SUR_NFEAT, SUR_NPARAM = 32, 6337
 MEASURE_TEMPERATURE, MEASURE_ENERGY, MEASURE_PRESSURE, MEASURE_RDF, MEASURE_LJ_HIST = 0x01, 0x02, 0x04, 0x08, 0x10
 
@@ -36,7 +37,7 @@ EXPORTS = [
     "komd_gpu_surrogate_sample", "komd_gpu_surrogate_forces", "komd_gpu_surrogate_status", "komd_mlp_train",
     "komd_mlp_loss_grad", "komd_sur_data_create", "komd_sur_data_destroy", "komd_gpu_surrogate_capture",
     "komd_sur_data_snapshots", "komd_sur_data_sites", "komd_sur_data_get", "komd_sur_fit", "komd_sur_fit_grad",
-    "komd_batch_create", "komd_batch_destroy", "komd_batch_step", "komd_batch_launch", "komd_batch_check",
+    "komd_gpu_scale_velocities", "komd_batch_create", "komd_batch_destroy", "komd_batch_step", "komd_batch_launch", "komd_batch_check",
 ]
 
 
@@ -48,7 +49,8 @@ class KomdConfig(C.Structure):
         ("angle_k", C.c_double), ("angle_theta0", C.c_double), ("max_sigma", C.c_double), ("rdf_max", C.c_double),
         ("rdf_dr", C.c_double), ("terms", C.c_uint32), ("precision", C.c_int32), ("atm_sign", C.c_int32),
         ("atm_enum", C.c_int32), ("virial_mode", C.c_int32), ("atm_direct", C.c_int32), ("lj_bins", C.c_int32),
-        ("atm_list_cap", C.c_int32), ("skin", C.c_double),
+        ("atm_list_cap", C.c_int32), ("skin", C.c_double), ("temperature_target", C.c_double),
+        ("thermostat", C.c_int32),
     ]
 
 
@@ -132,6 +134,7 @@ def load() -> C.CDLL:
     L.komd_sur_data_sites.argtypes = [P]
     L.komd_sur_data_get.argtypes = [P, I64, P, P, P, P]
     L.komd_sur_fit.argtypes = [P, P, P, P, C.c_double, C.c_double, C.c_double, C.POINTER(SurFitOpts), P]
+    L.komd_gpu_scale_velocities.argtypes = [P, C.c_double]
     L.komd_batch_create.argtypes = [P, I32, I32, I32, P, C.POINTER(P)]
     L.komd_batch_destroy.argtypes = [P]
     L.komd_batch_destroy.restype = None
@@ -150,7 +153,8 @@ def _p(a: Optional[np.ndarray]):
 def make_config(low, high, cell_size, cutoff=2.5, cutoff_3b=None, nu=0.0, dt=0.005, terms=TERM_LJ,
                 precision=FP32, atm_sign=ATM_SIGN_REFERENCE, atm_enum=ATM_ENUM_COMPAT, virial_mode=VIRIAL_COMPAT,
                 atm_direct=1, stiffness=30.0, limit=1e30, bond_k=0.0, bond_r0=1.0, angle_k=0.0, angle_theta0=0.0,
-                max_sigma=1.0, rdf_max=0.0, rdf_dr=0.0, lj_bins=100, atm_list_cap=0, skin=0.0) -> KomdConfig:
+                max_sigma=1.0, rdf_max=0.0, rdf_dr=0.0, lj_bins=100, atm_list_cap=0, skin=0.0,
+                thermostat=0, temperature_target=0.0) -> KomdConfig:
     c = KomdConfig()
     for d in range(3):
         c.domain_low[d] = float(low[d])
@@ -164,6 +168,7 @@ def make_config(low, high, cell_size, cutoff=2.5, cutoff_3b=None, nu=0.0, dt=0.0
     c.terms, c.precision, c.atm_sign, c.atm_enum = int(terms), int(precision), int(atm_sign), int(atm_enum)
     c.virial_mode, c.atm_direct, c.lj_bins, c.atm_list_cap = int(virial_mode), int(atm_direct), int(lj_bins), int(atm_list_cap)
     c.skin = float(skin)
+    c.thermostat, c.temperature_target = int(thermostat), float(temperature_target)
     return c
 
 
@@ -305,6 +310,10 @@ class GpuSystem:
         f3 = np.zeros((self.n, 3))
         self._check(self.L.komd_gpu_surrogate_sample(self.h, _p(x), _p(e3), _p(f3)))
         return x, e3, f3
+
+    def scale_velocities(self, beta: float):
+        """VelocityScaling::apply with the caller's beta (v *= beta)."""
+        self._check(self.L.komd_gpu_scale_velocities(self.h, float(beta)))
 
     def surrogate_capture(self, data: "SurData"):
         """Appends the current state to a force-matching dataset."""

@@ -348,6 +348,21 @@ static inline uint64_t pot_bin(double r, double sigma, uint64_t bins) {
     return b;
 }
 
+/* ATM2B (potentials/ATM2B.cpp:22-47) is LJ12_6_Force with the force vector
+ * multiplied by potential_factor: force = dr * fac * potential_factor.  The
+ * factor applies to kor_lj and kor_lj_cells while set (1 = plain LJ). */
+static double g_lj_fscale = 1.0;
+void kor_set_lj_force_scale(double s) { g_lj_fscale = s; }
+
+/* ATM2B::ATM2B (ATM2B.cpp:9-20): 1 - (2 nu rho) / (3 eps sig^6) with rho =
+ * molecules / volume and eps, sig of the first site of component 0 (all
+ * internal units). */
+double kor_atm2b_factor(double nu, double n_mol, double volume, double eps, double sig) {
+    const double rho = n_mol / volume;
+    const double sig6 = pow(sig, 6);
+    return 1.0 - ((2 * nu * rho) / (3 * eps * sig6));
+}
+
 void kor_lj(const kor_grid *g, int64_t n_pairs, const int64_t *pairs, const double *shifts,
             const double *r, const double *eps, const double *sig, const uint64_t *id,
             double cutoff, int virial_mode, double *f, int64_t *ncount, kor_lj_out *out,
@@ -375,7 +390,9 @@ void kor_lj(const kor_grid *g, int64_t n_pairs, const int64_t *pairs, const doub
         const double lj6 = pow(sig2 * invdr2, 3.0);
         const double lj12 = pow(lj6, 2.0);
         const double fac = 24.0 * epsilon * (2.0 * lj12 - lj6) * invdr2;
-        const double fo[3] = {dr[0] * fac, dr[1] * fac, dr[2] * fac};
+        double fo[3] = {dr[0] * fac, dr[1] * fac, dr[2] * fac};
+        if (g_lj_fscale != 1.0)
+            for (int d = 0; d < 3; d++) fo[d] = fo[d] * g_lj_fscale;
         const int dom0 = !shift_nonzero(sh0), dom1 = !shift_nonzero(sh1);
         if (dom0) for (int d = 0; d < 3; d++) atomic_addd(&f[3 * s0 + d], fo[d]);
         if (dom1) for (int d = 0; d < 3; d++) atomic_addd(&f[3 * s1 + d], -fo[d]);
@@ -482,8 +499,11 @@ void kor_lj_cells(const kor_grid *g, const kor_cells *c, const double *r, const 
             const double lj6 = pow(sig2 * invdr2, 3.0);
             const double lj12 = pow(lj6, 2.0);
             const double fac = 24.0 * epsilon * (2.0 * lj12 - lj6) * invdr2;
-            if (dom0) for (int d = 0; d < 3; d++) atomic_addd(&f[3 * s0 + d], dr[d] * fac);
-            if (dom1) for (int d = 0; d < 3; d++) atomic_addd(&f[3 * s1 + d], -(dr[d] * fac));
+            double fo[3] = {dr[0] * fac, dr[1] * fac, dr[2] * fac};
+            if (g_lj_fscale != 1.0)
+                for (int d = 0; d < 3; d++) fo[d] = fo[d] * g_lj_fscale;
+            if (dom0) for (int d = 0; d < 3; d++) atomic_addd(&f[3 * s0 + d], fo[d]);
+            if (dom1) for (int d = 0; d < 3; d++) atomic_addd(&f[3 * s1 + d], -fo[d]);
             if (dom1) u_total += 4.0 * epsilon * (lj12 - lj6);
         }
     }

@@ -113,6 +113,9 @@ typedef struct {
     int64_t triplets;      /* triplets inside the cutoff that were counted */
 } kor_atm_out;
 
+/* ATM2B: the force factor applied by kor_lj / kor_lj_cells while set (1 = LJ12_6) */
+void kor_set_lj_force_scale(double s);
+double kor_atm2b_factor(double nu, double n_mol, double volume, double eps, double sig);
 /* kor_lj without a materialised pair list: the same entries in C08 order,
  * generated from the cells (no virial, no histograms). */
 void kor_lj_cells(const kor_grid *g, const kor_cells *c, const double *r, const double *eps, const double *sig,

@@ -88,6 +88,10 @@ def lib():
         L.kor_step0.argtypes = [I64, P, P, P, P, D]
         L.kor_step1.argtypes = [I64, P, P, P, D]
         L.kor_temperature.argtypes = [I64, P, P, P, P, P]
+        L.kor_set_lj_force_scale.argtypes = [D]
+        L.kor_set_lj_force_scale.restype = None
+        L.kor_atm2b_factor.argtypes = [D, D, D, D, D]
+        L.kor_atm2b_factor.restype = D
         L.kor_temperature.restype = D
         L.kor_momentum.argtypes = [I64, P, P, P]
         L.kor_rdf_nbins.argtypes = [D, D]
@@ -117,7 +121,7 @@ class OracleSim:
 
     def __init__(self, sysm, cell_size, cutoff, dt=0.005, nu=0.0, cutoff_atm=None, limit=1e30,
                  stiffness=30.0, lj=True, atm=False, atm_mode="compat", atm_sign=ATM_SIGN_REFERENCE,
-                 fene=False, bonded=None, virial_mode=VIRIAL_COMPAT):
+                 fene=False, bonded=None, virial_mode=VIRIAL_COMPAT, lj_force_scale=1.0):
         self.L = lib()
         self.r = np.ascontiguousarray(sysm.r, dtype=np.float64).copy()
         self.v = np.ascontiguousarray(sysm.v, dtype=np.float64).copy()
@@ -141,6 +145,7 @@ class OracleSim:
         self.use_lj, self.use_atm, self.use_fene = lj, atm, fene
         self.atm_mode, self.atm_sign, self.virial_mode = atm_mode, atm_sign, virial_mode
         self.bonded = bonded
+        self.lj_force_scale = float(lj_force_scale)   # ATM2B potential_factor (1 = LJ12_6)
         self.lj_out, self.atm_out = LJOut(), ATMOut()
         self.e_bonded = 0.0
         self.ncount = None
@@ -182,6 +187,20 @@ class OracleSim:
 
     # --- forces ------------------------------------------------------------
     def forces(self, nbins=0, max_sigma=1.0, with_atm_virial=False, ncount=False, listless=False):
+        self.L.kor_set_lj_force_scale(self.lj_force_scale)
+        try:
+            self._forces(nbins, max_sigma, with_atm_virial, ncount, listless)
+        finally:
+            self.L.kor_set_lj_force_scale(1.0)
+
+    def thermostat(self, t_target):
+        """VelocityScaling::apply (VelocityScaling.cpp:12-25) after a
+        temperature measure: v *= sqrt(T_target / T)."""
+        beta = np.sqrt(t_target / self.temperature())
+        self.v *= beta
+        return beta
+
+    def _forces(self, nbins, max_sigma, with_atm_virial, ncount, listless):
         if listless:
             # large systems: LJ straight from the cells, no materialised pair list
             if self.use_fene or self.bonded is not None or nbins or ncount:
@@ -325,3 +344,8 @@ def sur_energy_forces(r, box, params, fmean, fstd, e_scale, e_shift, rc=2.0):
                                           _p(np.ascontiguousarray(fmean, np.float64)),
                                           _p(np.ascontiguousarray(fstd, np.float64)), e_scale, e_shift, _p(e), _p(f))
     return et, e, f
+
+
+def atm2b_factor(nu, n_mol, volume, eps, sig):
+    """ATM2B::ATM2B's potential_factor (kor_atm2b_factor)."""
+    return lib().kor_atm2b_factor(float(nu), float(n_mol), float(volume), float(eps), float(sig))

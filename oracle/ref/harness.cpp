@@ -7,10 +7,11 @@
 // sources where they lie; the binary goes to oracle/_ref/ and is never part
 // of the product.
 //
-// It mirrors Simulation::run (src/Simulation.cpp:10-80) without the always-on
-// velocity-scaling thermostat and without plugins, so that dynamics are NVE:
-//   step 0 : updateContainer, forces
-//   step k : integrate0, updateContainer, forces, integrate1
+// It mirrors Simulation::run (src/Simulation.cpp:10-80) without plugins and,
+// unless KOMD_HARNESS_THERMOSTAT=1, without the always-on velocity-scaling
+// thermostat, so that dynamics are NVE:
+//   step 0 : updateContainer, forces            [+ temperature, VelocityScaling]
+//   step k : integrate0, updateContainer, forces, integrate1   [+ the same]
 // and after every requested step writes
 //   R / V / F      per-site positions, velocities, forces   (%.17g)
 //   CELLS          every cell of the (nd+2)^3 grid incl. halo copies
@@ -36,6 +37,8 @@
 #include "potentials/Limit.h"
 #include "potentials/ATM.h"
 #include "potentials/ATM_NOLIST.h"
+#include "potentials/ATM2B.h"
+#include "thermostats/VelocityScaling.h"
 #include "sensors/PressureSensor.h"
 #include "sensors/LJ12_6_Sensor.h"
 #include "sensors/RDFSensor.h"
@@ -63,8 +66,8 @@ int main(int argc, char** argv) {
         auto config = Registry::instance->configuration();
         Registry::instance->moleculeContainer_ptr() = std::make_shared<LinkedCells>();
 
-        // force functors as src/main.cpp:57-66 (ATM2B is out of scope here)
-        Registry::instance->forceFunctors().push_back(std::make_shared<LJ12_6>());
+        // force functors as src/main.cpp:57-66
+        const bool atm2b = config->enable_3b_approx;
         Registry::instance->forceFunctors().push_back(std::make_shared<FENE>());
         Registry::instance->forceFunctors().push_back(std::make_shared<Limit>());
         if (config->enable_3b) {
@@ -73,8 +76,24 @@ int main(int argc, char** argv) {
         }
         Registry::instance->integrators().push_back(std::make_unique<Integrator>());
         CheckpointIO::loadCheckpoint();
+        // ATM2B reads the molecule count in its constructor.  main.cpp:57 builds
+        // it before CheckpointIO::loadCheckpoint (main.cpp:70), where the count is
+        // still 0 and the factor comes out as exactly 1; here it is built after the
+        // checkpoint is loaded so that the factor formula itself is exercised.  It
+        // goes first in the functor list as in main.cpp:57-58.
+        Registry::instance->forceFunctors().insert(Registry::instance->forceFunctors().begin(),
+            atm2b ? std::shared_ptr<ForceFunctor>(std::make_shared<ATM2B>())
+                  : std::shared_ptr<ForceFunctor>(std::make_shared<LJ12_6>()));
 
         auto temp = std::make_shared<TemperatureSensor>();
+        // KOMD_HARNESS_THERMOSTAT=1: the always-on VelocityScaling of main.cpp:95
+        // and Simulation.cpp:42,72 (after the initial forces and after every step)
+        const char* th = getenv("KOMD_HARNESS_THERMOSTAT");
+        std::unique_ptr<VelocityScaling> thermostat;
+        if (th && atoi(th) != 0) {
+            Registry::instance->temperature_sensor_ptr() = temp;
+            thermostat = std::make_unique<VelocityScaling>();
+        }
         std::shared_ptr<LJ12_6_Sensor> pot;
         std::shared_ptr<PressureSensor> pres;
         std::shared_ptr<RDFSensor> rdf;
@@ -99,6 +118,7 @@ int main(int argc, char** argv) {
             for (auto& p : Registry::instance->forceFunctors()) (*p)();
             if (config->enable_3b) for (auto& p : Registry::instance->forceFunctors3b()) (*p)();
             if (step > 0) for (auto& it : Registry::instance->integrators()) it->integrate1();
+            if (thermostat) { temp->measure(); thermostat->apply(); }
             if (!dumps.count(step)) continue;
 
             SOA& soa = container->getSOA();

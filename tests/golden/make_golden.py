@@ -9,7 +9,7 @@ compressed .npz files together with the inputs that produced them.
 
 Run from the repo root in a container where the reference is present:
 
-    make -C oracle/ref -j8 && python tests/golden/make_golden.py
+    make -C oracle/ref -j8 && python tests/golden/make_golden.py [case ...]
 
 The fixtures are then read by the tests without the reference.
 """
@@ -75,7 +75,7 @@ def parse_dump(path):
     return steps
 
 
-def run_case(name, sysm, values, steps, dumps, comps=None):
+def run_case(name, sysm, values, steps, dumps, comps=None, thermostat=False):
     tmp = tempfile.mkdtemp(prefix=f"komd_golden_{name}_")
     try:
         ps = os.path.join(tmp, "in.ps")
@@ -83,19 +83,22 @@ def run_case(name, sysm, values, steps, dumps, comps=None):
         comps = comps or [(0, EPS_J, 1.0, 1.0)]
         with open(os.path.join(tmp, "in.dat"), "w") as fh:
             fh.write(komd_io.format_input(values, ps, comps))
+        env = dict(os.environ, KOMD_HARNESS_THERMOSTAT="1" if thermostat else "0")
         res = subprocess.run([HARNESS, "in.dat", "out.txt", str(steps)] + [str(d) for d in dumps], cwd=tmp,
-                             capture_output=True, text=True)
+                             capture_output=True, text=True, env=env)
         if res.returncode != 0:
             raise RuntimeError(f"{name}: harness failed\n{res.stdout}\n{res.stderr}")
         dump = parse_dump(os.path.join(tmp, "out.txt"))
         arrays = dict(r0=sysm.r, v0=sysm.v, m=sysm.m, eps=sysm.eps, sig=sysm.sig, mol_id=sysm.mol_id,
                       low=np.asarray(values["domain_low"], float), high=np.asarray(values["domain_high"], float),
                       dumps=np.array(dumps, np.int64))
+        arrays["p_thermostat"] = np.int64(1 if thermostat else 0)
         for k in ("cutoff", "cell_size", "delta_t", "limit", "energy_3b", "stiffness", "sensor_rdf_max",
-                  "sensor_rdf_dr"):
+                  "sensor_rdf_dr", "temperature"):
             if k in values:
                 arrays["p_" + k] = np.float64(values[k])
-        for k in ("enable_3b", "enable_3b_direct", "enable_sensor_rdf", "enable_sensor_lj", "enable_sensor_pres"):
+        for k in ("enable_3b", "enable_3b_direct", "enable_sensor_rdf", "enable_sensor_lj", "enable_sensor_pres",
+                  "enable_3b_approx"):
             if k in values:
                 arrays["p_" + k] = np.int64(values[k])
         for s, d in dump.items():
@@ -120,44 +123,67 @@ def base_values(sysm, cutoff, cell, dt, steps, **kw):
     return v
 
 
-def main():
+def main(selected):
     if not os.path.exists(HARNESS):
         raise SystemExit("build the reference harness first: make -C oracle/ref -j8")
-
-    # 1. plain LJ argon, 864 atoms, jittered FCC, rc = cell = 2.5, RDF 200 bins
-    s = lattice.argon_fcc(6, rho=0.8442, t_star=0.722, seed=11, jitter=0.05)
-    run_case("lj864", s, base_values(s, 2.5, 2.5, 0.005, 100, enable_sensor_rdf=1, sensor_rdf_max=2.5,
-                                      sensor_rdf_dr=0.0125), 100, [0, 1, 100])
-
-    # 2. LJ + ATM (direct enumeration), single cutoff 2.0 (the reference has one cutoff)
-    s = lattice.argon_fcc(6, rho=0.8442, t_star=0.722, seed=12, jitter=0.05)
     e3b = lattice.nu_star_to_energy_3b(0.073)
-    run_case("ljatm864", s, base_values(s, 2.0, 2.0, 0.005, 20, enable_3b=1, enable_3b_direct=1, energy_3b=e3b),
-             20, [0, 1, 20])
 
-    # 3. ATM via the triplet list (ATM + ATM_Pressure), 500 atoms, stretched last cell
-    s = lattice.argon_fcc(5, rho=0.8442, t_star=0.722, seed=13, jitter=0.05)
-    run_case("atmlist500", s, base_values(s, 2.0, 2.0, 0.005, 5, enable_3b=1, enable_3b_direct=0, energy_3b=e3b),
-             5, [0, 1, 5])
+    def lj864():
+        # plain LJ argon, 864 atoms, jittered FCC, rc = cell = 2.5, RDF 200 bins
+        s = lattice.argon_fcc(6, rho=0.8442, t_star=0.722, seed=11, jitter=0.05)
+        run_case("lj864", s, base_values(s, 2.5, 2.5, 0.005, 100, enable_sensor_rdf=1, sensor_rdf_max=2.5,
+                                          sensor_rdf_dr=0.0125), 100, [0, 1, 100])
 
-    # 4. three-site molecules with FENE (all same-molecule pairs) and intermolecular LJ
-    s = lattice.triatomic_sc(5, rho_site=0.25, t_star=0.5, seed=14, r0=0.97, theta0_deg=90.0)
-    run_case("fene375", s, base_values(s, 2.5, 2.5, 0.002, 20, stiffness=30.0), 20, [0, 1, 20])
+    def ljatm864():
+        # LJ + ATM (direct enumeration), single cutoff 2.0 (the reference has one cutoff)
+        s = lattice.argon_fcc(6, rho=0.8442, t_star=0.722, seed=12, jitter=0.05)
+        run_case("ljatm864", s, base_values(s, 2.0, 2.0, 0.005, 20, enable_3b=1, enable_3b_direct=1,
+                                             energy_3b=e3b), 20, [0, 1, 20])
 
-    # 5. non-cubic box, non-zero domain_low, atoms on the domain faces, hot gas so
-    #    that sites cross the periodic boundary; small force clamp (Limit)
-    rng = np.random.default_rng(15)
-    low = np.array([-2.0, 0.5, 1.0])
-    box = np.array([10.3, 11.1, 9.7])
-    g = np.stack(np.meshgrid(*(np.arange(int(b // 1.15)) for b in box), indexing="ij"), -1).reshape(-1, 3)
-    r = low + (g + 0.5) * (box / np.floor(box / 1.15)) + rng.normal(0, 0.04, g.shape)
-    r[0] = low                  # exactly on the low corner
-    r[1] = low + box * np.array([1.0, 0.5, 0.5])   # exactly on the high x face
-    n = r.shape[0]
-    s = lattice.System(r=r, v=lattice.maxwell_boltzmann(n, 2.0, np.ones(n), rng), m=np.ones(n), eps=np.ones(n),
-                       sig=np.ones(n), mol_id=np.arange(1, n + 1, dtype=np.uint64), low=low, high=low + box)
-    run_case("edge_box", s, base_values(s, 2.5, 2.5, 0.004, 50, limit=40.0), 50, [0, 1, 50])
+    def atmlist500():
+        # ATM via the triplet list (ATM + ATM_Pressure), 500 atoms, stretched last cell
+        s = lattice.argon_fcc(5, rho=0.8442, t_star=0.722, seed=13, jitter=0.05)
+        run_case("atmlist500", s, base_values(s, 2.0, 2.0, 0.005, 5, enable_3b=1, enable_3b_direct=0,
+                                               energy_3b=e3b), 5, [0, 1, 5])
+
+    def fene375():
+        # three-site molecules with FENE (all same-molecule pairs) and intermolecular LJ
+        s = lattice.triatomic_sc(5, rho_site=0.25, t_star=0.5, seed=14, r0=0.97, theta0_deg=90.0)
+        run_case("fene375", s, base_values(s, 2.5, 2.5, 0.002, 20, stiffness=30.0), 20, [0, 1, 20])
+
+    def edge_box():
+        # non-cubic box, non-zero domain_low, atoms on the domain faces, hot gas so
+        # that sites cross the periodic boundary; small force clamp (Limit)
+        rng = np.random.default_rng(15)
+        low = np.array([-2.0, 0.5, 1.0])
+        box = np.array([10.3, 11.1, 9.7])
+        g = np.stack(np.meshgrid(*(np.arange(int(b // 1.15)) for b in box), indexing="ij"), -1).reshape(-1, 3)
+        r = low + (g + 0.5) * (box / np.floor(box / 1.15)) + rng.normal(0, 0.04, g.shape)
+        r[0] = low                  # exactly on the low corner
+        r[1] = low + box * np.array([1.0, 0.5, 0.5])   # exactly on the high x face
+        n = r.shape[0]
+        s = lattice.System(r=r, v=lattice.maxwell_boltzmann(n, 2.0, np.ones(n), rng), m=np.ones(n),
+                           eps=np.ones(n), sig=np.ones(n), mol_id=np.arange(1, n + 1, dtype=np.uint64), low=low,
+                           high=low + box)
+        run_case("edge_box", s, base_values(s, 2.5, 2.5, 0.004, 50, limit=40.0), 50, [0, 1, 50])
+
+    def atm2b864():
+        # ATM2B effective pair force (enable_3b_approx) in place of LJ12_6, nu* = 0.073
+        s = lattice.argon_fcc(6, rho=0.8442, t_star=0.722, seed=16, jitter=0.05)
+        run_case("atm2b864", s, base_values(s, 2.5, 2.5, 0.005, 20, enable_3b_approx=1, energy_3b=e3b),
+                 20, [0, 1, 20])
+
+    def thermo864():
+        # the always-on VelocityScaling thermostat: target 1.2 K (T* ~ 1.0) from T* = 0.722
+        s = lattice.argon_fcc(6, rho=0.8442, t_star=0.722, seed=17, jitter=0.05)
+        run_case("thermo864", s, base_values(s, 2.5, 2.5, 0.005, 50, temperature=1.2), 50, [0, 1, 50],
+                 thermostat=True)
+
+    cases = dict(lj864=lj864, ljatm864=ljatm864, atmlist500=atmlist500, fene375=fene375, edge_box=edge_box,
+                 atm2b864=atm2b864, thermo864=thermo864)
+    for name in (selected or list(cases)):
+        cases[name]()
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -29,11 +29,14 @@ def gpu_for_case(z, precision=None, **over):
     terms = gpu.TERM_LJ | gpu.TERM_FENE | gpu.TERM_LIMIT
     if int(z["p_enable_3b"]):
         terms |= gpu.TERM_ATM
+    if int(z.get("p_enable_3b_approx", 0)):
+        terms |= gpu.TERM_ATM2B
     kw = dict(cutoff=float(z["p_cutoff"]), cutoff_3b=float(z["p_cutoff"]), nu=lattice.energy_3b_to_nu(float(z["p_energy_3b"])),
               dt=float(z["p_delta_t"]), terms=terms, precision=gpu.FP32 if precision is None else precision,
               atm_direct=int(z["p_enable_3b_direct"]), stiffness=float(z.get("p_stiffness", 30.0)),
               limit=float(z["p_limit"]), rdf_max=float(z.get("p_sensor_rdf_max", 0.0)),
-              rdf_dr=float(z.get("p_sensor_rdf_dr", 0.0)))
+              rdf_dr=float(z.get("p_sensor_rdf_dr", 0.0)), thermostat=int(z.get("p_thermostat", 0)),
+              temperature_target=float(z.get("p_temperature", 0.0)))
     kw.update(over)
     cfg = gpu.make_config(z["low"], z["high"], float(z["p_cell_size"]), **kw)
     return gpu.GpuSystem(s, cfg), s
@@ -117,6 +120,50 @@ def test_fp64_trajectory_follows_reference():
     r, v, f = g.download()
     assert np.abs(r - z["s100_R"]).max() < 1e-8
     assert rel_rmse(f, z["s100_F"]) < 1e-6
+    g.close()
+
+
+def test_atm2b_trajectory_follows_reference():
+    """ATM2B (enable_3b_approx) in FP64: the engine's factor and scaled LJ
+    forces keep the reference's trajectory for 20 steps."""
+    from komd_gb300 import gpu
+    z = load_case("atm2b864")
+    g, _ = gpu_for_case(z, precision=gpu.FP64)
+    g.update_container()
+    g.forces()
+    _, _, f0 = g.download()
+    assert rel_rmse(f0, z["s0_F"]) < 1e-12
+    g.step(20)
+    r, v, f = g.download()
+    assert np.abs(r - z["s20_R"]).max() < 1e-8
+    assert rel_rmse(f, z["s20_F"]) < 1e-6
+    g.close()
+
+
+def test_thermostat_trajectory_follows_reference():
+    """The always-on VelocityScaling thermostat: the initial application
+    through komd_gpu_scale_velocities (Simulation.cpp:42) and the per-step
+    device-side application inside the step graph follow the reference's
+    thermostatted trajectory for 50 steps (FP64)."""
+    from komd_gb300 import gpu
+    z = load_case("thermo864")
+    t_target = float(z["p_temperature"])
+    g, _ = gpu_for_case(z, precision=gpu.FP64)
+    g.update_container()
+    g.forces()
+    t0 = g.measure(gpu.MEASURE_TEMPERATURE)["temperature"]
+    g.scale_velocities(np.sqrt(t_target / t0))
+    _, v0, _ = g.download()
+    assert np.abs(v0 - z["s0_V"]).max() < 1e-13
+    g.step(1)
+    r1, v1, _ = g.download()
+    assert np.abs(r1 - z["s1_R"]).max() < 1e-12
+    assert np.abs(v1 - z["s1_V"]).max() < 1e-12
+    g.step(49)
+    r, v, _ = g.download()
+    assert np.abs(r - z["s50_R"]).max() < 1e-8
+    assert np.abs(v - z["s50_V"]).max() < 1e-7
+    assert g.measure(gpu.MEASURE_TEMPERATURE)["temperature"] == pytest.approx(t_target, rel=1e-10)
     g.close()
 
 

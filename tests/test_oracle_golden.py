@@ -13,13 +13,26 @@ import pytest
 from conftest import CASES, case_system, load_case
 
 
+def atm2b_factor(oracle_lib, z, s):
+    """The ATM2B factor as the reference's constructor forms it from the COMP
+    line (epsilon in J times conv_J_Ei) and the loaded molecule count."""
+    from komd_gb300 import lattice
+    if not int(z.get("p_enable_3b_approx", 0)):
+        return 1.0
+    nu = float(z["p_energy_3b"]) * 1e+9 * lattice.CONV_J_EI
+    eps = (1.0 / lattice.CONV_J_EI) * lattice.CONV_J_EI      # COMP epsilon of the fixtures, J -> internal
+    vol = float(np.prod(z["high"] - z["low"]))
+    return oracle_lib.atm2b_factor(nu, len(np.unique(z["mol_id"])), vol, eps, 1.0)
+
+
 def _sim(oracle_lib, z, **kw):
     from komd_gb300 import lattice
     s = case_system(z)
     nu = lattice.energy_3b_to_nu(float(z["p_energy_3b"]))
     return oracle_lib.OracleSim(s, float(z["p_cell_size"]), float(z["p_cutoff"]), dt=float(z["p_delta_t"]), nu=nu,
                                 limit=float(z["p_limit"]), stiffness=float(z.get("p_stiffness", 30.0)),
-                                atm=bool(z["p_enable_3b"]), fene=True, **kw)
+                                atm=bool(z["p_enable_3b"]), fene=True, lj_force_scale=atm2b_factor(oracle_lib, z, s),
+                                **kw)
 
 
 @pytest.mark.parametrize("name", CASES)
@@ -37,6 +50,8 @@ def test_oracle_matches_reference_bitwise(oracle_lib, name):
         sim.forces(ncount=True, with_atm_virial=list_atm)
         if step > 0:
             sim.integrate1()
+        if int(z.get("p_thermostat", 0)):
+            sim.thermostat(float(z["p_temperature"]))
         if step not in dumps:
             continue
         p = f"s{step}_"
