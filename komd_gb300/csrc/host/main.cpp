@@ -1,0 +1,71 @@
+// main.cpp -- the `komd` executable: KoMD's stock main (src/main.cpp:37-99)
+// on the GB300 engine.  Usage: komd <input file> [--fused]
+//   --fused   advance write_freq steps per engine call (CUDA graph replay with
+//             the thermostat on the device); log lines at write steps only
+// Input files are KoMD's; the phase space comes from checkpoint_file entries
+// (ps_gen_region inputs are rejected: the phase-space generator is not part of
+// this engine).  Plugins (IBI, AdResS) and the FENE, displacement and
+// viscosity sensors are not available and are reported, not silently skipped.
+#include <cstring>
+#include <iostream>
+#include <stdexcept>
+
+#include "gpu_adapters.h"
+
+using namespace komd;
+
+int main(int argc, char **argv) {
+    if (argc <= 1) {
+        std::cout << "Run program with: komd <input file> [--fused]" << std::endl;
+        return 0;
+    }
+    bool fused = false;
+    for (int a = 2; a < argc; a++)
+        if (std::strcmp(argv[a], "--fused") == 0) fused = true;
+    try {
+        Registry::instance = std::make_unique<Registry>();
+        Registry::instance->configuration_ptr() = std::make_shared<Configuration>();
+        if (!FileInput::readFile(argv[1])) return 0;
+        auto cfg = Registry::instance->configuration();
+        if (cfg->enable_one_cell) throw std::runtime_error("not supported anymore");
+        if (!cfg->phasespace_gen_regions.empty())
+            throw std::runtime_error("ps_gen_region: the phase-space generator is not available; use checkpoint_file");
+        if (cfg->IBI_enable || cfg->IBI_reload_enable || cfg->ADR_enable)
+            throw std::runtime_error("the IBI and AdResS plugins are not available in this engine");
+        auto container = std::make_shared<GpuLinkedCells>();
+        container->device_thermostat = fused;
+        Registry::instance->moleculeContainer_ptr() = container;
+        Registry::instance->simulation_ptr() = std::make_shared<Simulation>();
+
+        // force functors (main.cpp:57-66): LJ12_6 or ATM2B, FENE, Limit and ATM
+        // are terms of one engine call
+        Registry::instance->forceFunctors().push_back(std::make_shared<GpuForces>());
+        if (cfg->enable_3b) Registry::instance->forceFunctors3b().push_back(std::make_shared<GpuATM>());
+        Registry::instance->integrators().push_back(std::make_unique<GpuIntegrator>());
+        if (!CheckpointIO::loadCheckpoint()) return 0;
+        container->init();
+
+        // measurements (main.cpp:74-85)
+        auto temp = std::make_shared<GpuTemperatureSensor>();
+        Registry::instance->temperature_sensor_ptr() = temp;
+        Registry::instance->sensors().push_back(temp);
+        if (cfg->enable_sensor_lj) {
+            auto pot = std::make_shared<GpuLJSensor>();
+            Registry::instance->potential_sensor_ptr() = pot;
+            Registry::instance->sensors().push_back(pot);
+        }
+        if (cfg->enable_sensor_rdf) Registry::instance->sensors().push_back(std::make_shared<GpuRDFSensor>());
+        if (cfg->enable_sensor_pres) Registry::instance->sensors().push_back(std::make_shared<GpuPressureSensor>());
+        if (cfg->enable_sensor_fene || cfg->enable_sensor_disp || cfg->enable_sensor_visc)
+            std::cerr << "note: the FENE, displacement and viscosity sensors are not available" << std::endl;
+        Registry::instance->thermostats().push_back(std::make_unique<GpuVelocityScaling>());
+
+        Registry::instance->simulation()->run(fused);
+    } catch (const std::exception &e) {
+        std::cerr << "komd: " << e.what() << std::endl;
+        Registry::instance = nullptr;
+        return 1;
+    }
+    Registry::instance = nullptr;
+    return 0;
+}

@@ -1,0 +1,79 @@
+"""The C++ host layer and the `komd` executable (komd_gb300/csrc/host/):
+KoMD's input parser, checkpoint IO, Registry and Simulation::run over the
+engine.  CPU tests cover the parser's checks (they fail before any GPU use);
+the GPU test runs a reference fixture's input end to end and lands on the
+reference's thermostatted trajectory."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, case_system, load_case
+
+EXE = os.path.join(ROOT, "komd_gb300", "_build", "komd")
+
+
+@pytest.fixture(scope="module")
+def komd_exe():
+    from komd_gb300 import build
+    build.build()
+    assert os.path.exists(EXE)
+    return EXE
+
+
+def _write_case(tmp_path, z, extra=None, steps=None):
+    from komd_gb300 import komd_io, lattice
+    s = case_system(z)
+    ps = str(tmp_path / "in.ps")
+    komd_io.write_checkpoint(ps, s)
+    values = dict(temperature=float(z["p_temperature"]), delta_t=float(z["p_delta_t"]),
+                  cutoff=float(z["p_cutoff"]), cell_size=float(z["p_cell_size"]),
+                  timesteps=int(steps if steps is not None else max(z["dumps"])), limit=float(z["p_limit"]),
+                  energy_3b=float(z["p_energy_3b"]), domain_low=tuple(z["low"]), domain_high=tuple(z["high"]),
+                  write_freq=100000000, enable_3b=int(z["p_enable_3b"]), store_checkpoint=1)
+    values.update(extra or {})
+    inp = tmp_path / "in.dat"
+    inp.write_text(komd_io.format_input(values, ps, [(0, 1.0 / lattice.CONV_J_EI, 1.0, 1.0)]))
+    return str(inp)
+
+
+def test_usage_and_parser_checks(komd_exe, tmp_path):
+    out = subprocess.run([komd_exe], capture_output=True, text=True)
+    assert out.returncode == 0 and "Run program with" in out.stdout
+    bad = tmp_path / "bad.dat"
+    bad.write_text("temperature 100\ncutoff 2.5\ncell_size 2.5")
+    out = subprocess.run([komd_exe, str(bad)], capture_output=True, text=True)
+    assert out.returncode == 0 and "no components defined" in out.stderr
+    bad.write_text("cutoff 2.5\ncell_size 2.0\ncheckpoint_file x.ps 0 0 0\nCOMP 0 1e-21 1.0 1.0 0 0 0")
+    out = subprocess.run([komd_exe, str(bad)], capture_output=True, text=True)
+    assert "cell size must be larger or equal to cutoff radius" in out.stderr
+    bad.write_text("cutoff 2.5\ncell_size 2.5\nCOMP 0 1e-21 1.0 1.0 0 0 0")
+    out = subprocess.run([komd_exe, str(bad)], capture_output=True, text=True)
+    assert "No phasespace data specified" in out.stderr
+    bad.write_text("cutoff 2.5\ncell_size 2.5\ncheckpoint_file x.ps 0 0 0\nCOMP 0 1e-21 1.0 1.0 0 0 0\n"
+                   "gpu_precision fp16")
+    out = subprocess.run([komd_exe, str(bad)], capture_output=True, text=True)
+    assert "invalid value for gpu_precision" in out.stderr
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fused", [False, True])
+def test_komd_executable_follows_reference(komd_exe, tmp_path, fused):
+    """thermo864: 50 thermostatted steps through FileInput, CheckpointIO,
+    the adapters and Simulation::run (per-call or fused) end on the
+    reference's positions (the checkpoint is written with the reference's
+    6-digit stream format)."""
+    from komd_gb300 import komd_io
+    z = load_case("thermo864")
+    inp = _write_case(tmp_path, z, extra=dict(gpu_precision="fp64"))
+    cmd = [komd_exe, inp] + (["--fused"] if fused else [])
+    out = subprocess.run(cmd, capture_output=True, text=True, cwd=tmp_path, timeout=300)
+    assert out.returncode == 0, out.stderr
+    assert "Initial temperature T=" in out.stdout
+    ck = tmp_path / "ckpt_50.ps"
+    assert ck.exists()
+    assert not ck.read_text().endswith("\n")
+    s = komd_io.read_checkpoint(str(ck), low=z["low"], high=z["high"])
+    ref = z["s50_R"]
+    assert np.abs(s.r - ref).max() <= 1e-5 * max(1.0, np.abs(ref).max())
