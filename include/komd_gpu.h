@@ -63,6 +63,10 @@ enum { KOMD_VIRIAL_COMPAT = 0, KOMD_VIRIAL_CORRECT = 1 };
  * rho = molecules / domain volume, eps and sigma of the first uploaded site;
  * the LJ energy and virial sensors stay unscaled as in the reference */
 #define KOMD_TERM_ATM2B 0x40u
+/* tabulated pair force (plugins/IBI/IBI_ForceFunctor.cpp:18-37): every site pair
+ * inside cutoff gets F(r) from komd_gpu_set_pair_table, FP64, in the LJ
+ * functor's place before Limit (set it instead of, or with, KOMD_TERM_LJ) */
+#define KOMD_TERM_TABULATED 0x80u
 
 /* measurements (bit mask) */
 #define KOMD_MEASURE_TEMPERATURE 0x01u  /* sensors/TemperatureSensor.cpp:27-48   */
@@ -185,6 +189,16 @@ int  komd_gpu_get_cells(komd_gpu *h, int64_t *count, int64_t ncell, int64_t *idx
  * molecule ID, evaluated in FP64 with the reference's arithmetic
  * (LJ12_6.cpp:23-28), so counts are bit-exact. */
 int  komd_gpu_neighbour_counts(komd_gpu *h, int64_t *counts);
+
+/* The tabulated pair force F(r) (FunctionPL::evaluateAt, plugins/IBI/IBI_Math.h:30-44):
+ * piecewise linear on n >= 2 strictly ascending nodes x with values y,
+ * `below` for r < x[0], `above` for r > x[n-1].  May be replaced between
+ * steps (the IBI iteration's force update, IBI.cpp:172-178). */
+int  komd_gpu_set_pair_table(komd_gpu *h, int32_t n, const double *x, const double *y, double below, double above);
+/* RDF_Profiler::measure / getRDF (plugins/IBI/RDF_Profiler.cpp:18-55): ordered
+ * molecule-COM pair histogram with nbins bins of max_r / nbins up to max_r
+ * (added to bins, nbins doubles). */
+int  komd_gpu_rdf_profile(komd_gpu *h, double max_r, int32_t nbins, double *bins);
 
 /* VelocityScaling::apply (VelocityScaling.cpp:12-25) with the caller's
  * beta = sqrt(T_target / T_sensor): v *= beta for every site. */

@@ -200,6 +200,10 @@ void enqueue_forces(komd_gpu *h, bool measure, double *lj_hist) {
         pair_blocks = launch_pair(e, st, measure, lj_hist);
     }
     if (measure) launch_sum_partials(st, pair_blocks, e.partials, h->acc);
+    if (e.cfg.terms & KOMD_TERM_TABULATED) {   // in the LJ functor's place (IBI.cpp:52-54), before Limit
+        ProfScope ps(h, F_PAIR);
+        launch_pair_table(e, st);
+    }
     if ((e.cfg.terms & KOMD_TERM_BONDED) && (e.n_bonds > 0 || e.n_angles > 0)) {
         ProfScope ps(h, F_BONDED);
         launch_bonded(e, st, measure, h->acc);
@@ -320,6 +324,8 @@ int validate(const komd_config *c, Grid &g) {
     if (lj && !(c->cutoff > 0)) return fail(KOMD_ERR_ARG, "cutoff must be > 0");
     if (c->thermostat && !(c->temperature_target > 0)) return fail(KOMD_ERR_ARG, "thermostat needs temperature_target > 0");
     if ((c->terms & KOMD_TERM_ATM2B) && !lj) return fail(KOMD_ERR_ARG, "KOMD_TERM_ATM2B scales the LJ term: set KOMD_TERM_LJ");
+    if ((c->terms & KOMD_TERM_TABULATED) && c->skin > 0)
+        return fail(KOMD_ERR_ARG, "the tabulated pair term runs on per-step cell lists (skin 0)");
     if (c->cell_size < c->cutoff)
         return fail(KOMD_ERR_ARG, "cell size must be larger or equal to cutoff radius");
     if (atm && (!(c->cutoff_3b > 0) || c->cell_size < c->cutoff_3b))
@@ -434,7 +440,7 @@ int komd_gpu_create(const komd_config *cfg, int device, komd_gpu **out) {
             return fail(KOMD_ERR_NOMEM, "Verlet tables");
         }
     }
-    h->want_posd = e.cfg.precision == KOMD_FP64;
+    h->want_posd = e.cfg.precision == KOMD_FP64 || (e.cfg.terms & KOMD_TERM_TABULATED);
     *out = h;
     return KOMD_OK;
 }
@@ -451,6 +457,7 @@ int komd_gpu_destroy(komd_gpu *h) {
     dfree(e.cell_count); dfree(e.cell_start); dfree(e.cell_mcount); dfree(e.cell_mstart); dfree(e.cell_mols);
     dfree(e.slot_site); dfree(e.skey); dfree(e.pos4); dfree(e.seps); dfree(e.posd); dfree(e.seps_d); dfree(e.sig_d);
     dfree(e.nl); dfree(e.nl_count); dfree(e.bonds); dfree(e.angles); dfree(e.partials); dfree(e.err);
+    dfree(e.tab_x); dfree(e.tab_y);
     dfree(e.rdf); dfree(e.lj_hist); dfree(e.counts); dfree(h->f_scratch); dfree(h->acc); dfree(h->thermo_acc); dfree(e.offtab);
     dfree(e.nboff); dfree(e.rebuild); dfree(e.img); dfree(e.ref); dfree(e.slot_cell); dfree(e.vl); dfree(e.vl_count);
     dfree(e.rebuild_count); dfree(e.hdtm); dfree(e.exact_com);
@@ -801,6 +808,58 @@ int komd_gpu_step_host(komd_gpu *h, int64_t n_steps, double *r, double *v, doubl
     int rc = komd_gpu_step(h, n_steps);
     if (rc) return rc;
     return komd_gpu_download(h, r, v, f);
+}
+
+int komd_gpu_set_pair_table(komd_gpu *h, int32_t n, const double *x, const double *y, double below,
+                            double above) {
+    if (!h || !x || !y) return fail(KOMD_ERR_ARG, "null argument");
+    Engine &e = h->e;
+    if (!(e.cfg.terms & KOMD_TERM_TABULATED)) return fail(KOMD_ERR_ARG, "the engine was created without KOMD_TERM_TABULATED");
+    if (n < 2) return fail(KOMD_ERR_ARG, "a table needs at least two nodes");
+    for (int32_t k = 1; k < n; k++)
+        if (!(x[k] > x[k - 1])) return fail(KOMD_ERR_ARG, "table nodes must be strictly ascending");
+    CK(cudaStreamSynchronize(e.stream));
+    if (n != e.tab_n) {
+        CK(dalloc(e.tab_x, n));
+        CK(dalloc(e.tab_y, n));
+        e.tab_n = n;
+        if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+        e.graph_valid = false;
+    }
+    // same-size tables are replaced in place: graphs already captured read the new values
+    CK(cudaMemcpy(e.tab_x, x, sizeof(double) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e.tab_y, y, sizeof(double) * n, cudaMemcpyHostToDevice));
+    if (e.tab_lo != below || e.tab_hi != above) {
+        e.tab_lo = below;
+        e.tab_hi = above;
+        if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+        e.graph_valid = false;
+    }
+    return KOMD_OK;
+}
+
+int komd_gpu_rdf_profile(komd_gpu *h, double max_r, int32_t nbins, double *bins) {
+    if (!h || !bins || nbins <= 0 || !(max_r > 0)) return fail(KOMD_ERR_ARG, "bad argument");
+    Engine &e = h->e;
+    if (!e.have_cells) return fail(KOMD_ERR_STATE, "update_container must run first");
+    cudaStream_t st = e.stream;
+    if (e.verlet) launch_rebuild(h);   // the cells of the last rebuild may be stale
+    double *d = nullptr;
+    CK(dalloc(d, nbins));
+    CK(cudaMemsetAsync(d, 0, sizeof(double) * nbins, st));
+    const double dr = max_r / (double)nbins;   // RDF_Profiler.cpp:8
+    launch_rdf_bins(e, st, d, max_r <= e.cfg.cell_size, max_r, dr, nbins);
+    int rc = check_launch("rdf_profile");
+    std::vector<double> hb(nbins);
+    if (!rc) {
+        const cudaError_t ce = cudaMemcpyAsync(hb.data(), d, sizeof(double) * nbins, cudaMemcpyDeviceToHost, st);
+        const cudaError_t se = cudaStreamSynchronize(st);
+        if (ce != cudaSuccess || se != cudaSuccess) rc = fail(KOMD_ERR_CUDA, "rdf_profile copy");
+    }
+    dfree(d);
+    if (rc) return rc;
+    for (int32_t k = 0; k < nbins; k++) bins[k] += hb[k];
+    return KOMD_OK;
 }
 
 int komd_gpu_scale_velocities(komd_gpu *h, double beta) {

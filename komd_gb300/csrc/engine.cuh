@@ -253,6 +253,11 @@ struct Engine {
     bool uniform = false;
     float eps0 = 1.f, sig0 = 1.f;
     double lj_fscale = 1.0;         // ATM2B factor (KOMD_TERM_ATM2B), else 1
+    // tabulated pair force (KOMD_TERM_TABULATED): F(r) piecewise linear on
+    // ascending nodes tab_x, values tab_y, tab_lo below / tab_hi above the nodes
+    double *tab_x = nullptr, *tab_y = nullptr;
+    int tab_n = 0;
+    double tab_lo = 0.0, tab_hi = 0.0;
     double *atm_esite = nullptr;     // when set, measure-mode ATM writes per-site energies here
 };
 

@@ -993,6 +993,68 @@ __global__ void k_sum_partials(int nblocks, const double *__restrict__ partials,
     if (lane == 0) out[slot] += s;
 }
 
+// Tabulated pair force (IBI_ForceFunctor<IBI_Default>::IBI_Force,
+// plugins/IBI/IBI_ForceFunctor.cpp:18-37, FunctionPL::evaluateAt,
+// plugins/IBI/IBI_Math.h:30-44): for every pair inside the cutoff (no
+// same-molecule exclusion) F = table(r), force = (dr / r) * F on the site.
+// FP64 with the reference's operation order; the upper node is the first
+// node >= r (binary search, the same node the reference's linear scan finds).
+// At r == x[0] the reference reads x[-1]; here the first segment is used.
+__device__ __forceinline__ double table_eval(double x, int n, const double *__restrict__ xs,
+                                             const double *__restrict__ ys, double lo, double hi) {
+    if (x > xs[n - 1]) return hi;
+    if (x < xs[0]) return lo;
+    int a = 0, b = n - 1;           // lower_bound: first index with xs[i] >= x
+    while (a < b) {
+        const int m = (a + b) >> 1;
+        if (x > xs[m]) a = m + 1;
+        else b = m;
+    }
+    const int ub = a < 1 ? 1 : a, lb = ub - 1;
+    const double ya = ys[lb], yb = ys[ub], xa = xs[lb], xb = xs[ub];
+    return dadd(ya, dmul(ddiv(dsub(yb, ya), dsub(xb, xa)), dsub(x, xa)));
+}
+
+__global__ void __launch_bounds__(kBlock) k_pair_table(Grid g, const int *__restrict__ cell_start,
+                                                      const int *__restrict__ slot_site,
+                                                      const double *__restrict__ posd, double rc2, int n,
+                                                      const double *__restrict__ xs, const double *__restrict__ ys,
+                                                      double lo, double hi, double *f) {
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int cell = blockIdx.x * kWarpsPerBlock + wib;
+    if (cell >= g.ncell) return;
+    int cx, cy, cz;
+    cell_coords(g, cell, cx, cy, cz);
+    const int hs = cell_start[cell], hn = cell_start[cell + 1] - hs;
+    for (int k = lane; k < hn; k += 32) {
+        const int is = hs + k;
+        const double xi = posd[3 * is], yi = posd[3 * is + 1], zi = posd[3 * is + 2];
+        double fx = 0.0, fy = 0.0, fz = 0.0;
+        for (int nb = 0; nb < 27; nb++) {
+            const NbCell q = neighbour_cell(g, cx, cy, cz, nb);
+            const int js = cell_start[q.cell], jn = cell_start[q.cell + 1] - js;
+            for (int j = js; j < js + jn; j++) {
+                if (j == is) continue;
+                const double *pj = posd + 3 * j;
+                const double dx = dsub(xi, dadd(pj[0], q.shift[0]));
+                const double dy = dsub(yi, dadd(pj[1], q.shift[1]));
+                const double dz = dsub(zi, dadd(pj[2], q.shift[2]));
+                const double r2 = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
+                if (r2 > rc2) continue;
+                const double r = __dsqrt_rn(r2);
+                const double F = table_eval(r, n, xs, ys, lo, hi);
+                fx = dadd(fx, dmul(ddiv(dx, r), F));
+                fy = dadd(fy, dmul(ddiv(dy, r), F));
+                fz = dadd(fz, dmul(ddiv(dz, r), F));
+            }
+        }
+        const int site = slot_site[is];
+        f[3 * site] = dadd(f[3 * site], fx);
+        f[3 * site + 1] = dadd(f[3 * site + 1], fy);
+        f[3 * site + 2] = dadd(f[3 * site + 2], fz);
+    }
+}
+
 // VelocityScaling (VelocityScaling.cpp:12-25): v *= beta; beta from the
 // caller, or (acc != nullptr) sqrt(T_target / T) with T from the summed
 // kinetic slots as TemperatureSensor computes it
@@ -1210,6 +1272,13 @@ void launch_step1(Engine &e, cudaStream_t st) {
 
 int kinetic_grid(const Engine &e) { return nblk(e.n, kBlock); }
 
+void launch_pair_table(Engine &e, cudaStream_t st) {
+    if (!e.tab_x || e.tab_n < 2) return;
+    k_pair_table<<<nblk(e.g.ncell, kWarpsPerBlock), kBlock, 0, st>>>(e.g, e.cell_start, e.slot_site, e.posd, e.cfg.cutoff *
+                                                                   e.cfg.cutoff, e.tab_n, e.tab_x, e.tab_y, e.tab_lo,
+                                                                   e.tab_hi, e.f);
+}
+
 void launch_velocity_scale(Engine &e, cudaStream_t st, const double *acc, double beta) {
     const int blocks = std::min(nblk(3 * e.n, 256), 152 * 8);
     k_velocity_scale<<<blocks, 256, 0, st>>>((int)e.n, e.v, acc, e.cfg.temperature_target, beta);
@@ -1224,12 +1293,15 @@ void launch_sum_partials(cudaStream_t st, int nblocks, const double *partials, d
 }
 
 void launch_rdf(Engine &e, cudaStream_t st, double *bins, bool cells) {
+    launch_rdf_bins(e, st, bins, cells, e.cfg.rdf_max, e.cfg.rdf_dr, e.rdf_bins);
+}
+
+void launch_rdf_bins(Engine &e, cudaStream_t st, double *bins, bool cells, double max_r, double dr, int64_t nbins) {
     if (cells)
         k_rdf_cells<<<nblk(e.n_mol, 128), 128, 0, st>>>(e.g, (int)e.n_mol, e.com, e.mol_cell, e.cell_mstart,
-                                                          e.cell_mols, e.cfg.rdf_max, e.cfg.rdf_dr, e.rdf_bins, bins);
+                                                          e.cell_mols, max_r, dr, nbins, bins);
     else
-        k_rdf_all<<<nblk(e.n_mol, 128), 128, 0, st>>>(e.g, (int)e.n_mol, e.com, e.cfg.rdf_max, e.cfg.rdf_dr,
-                                                        e.rdf_bins, bins);
+        k_rdf_all<<<nblk(e.n_mol, 128), 128, 0, st>>>(e.g, (int)e.n_mol, e.com, max_r, dr, nbins, bins);
 }
 
 void set_kernel_attributes(Engine &e) {

@@ -18,8 +18,10 @@ void launch_step0(Engine &e, cudaStream_t st);
 void launch_step1(Engine &e, cudaStream_t st);
 void launch_kinetic(Engine &e, cudaStream_t st, int n_terms);
 void launch_velocity_scale(Engine &e, cudaStream_t st, const double *acc, double beta);
+void launch_pair_table(Engine &e, cudaStream_t st);
 void launch_sum_partials(cudaStream_t st, int nblocks, const double *partials, double *out);
 void launch_rdf(Engine &e, cudaStream_t st, double *bins, bool cells);
+void launch_rdf_bins(Engine &e, cudaStream_t st, double *bins, bool cells, double max_r, double dr, int64_t nbins);
 void set_kernel_attributes(Engine &e);
 int atm_grid(const Engine &e);
 int kinetic_grid(const Engine &e);

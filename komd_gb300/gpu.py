@@ -23,7 +23,7 @@ ATM_ENUM_COMPAT, ATM_ENUM_FULL = 0, 1
 VIRIAL_COMPAT, VIRIAL_CORRECT = 0, 1
 
 TERM_LJ, TERM_FENE, TERM_LIMIT, TERM_ATM, TERM_BONDED, TERM_ATM_SURROGATE = 0x01, 0x02, 0x04, 0x08, 0x10, 0x20
-TERM_ATM2B = 0x40
+TERM_ATM2B, TERM_TABULATED = 0x40, 0x80
 SUR_NFEAT, SUR_NPARAM = 32, 6337
 MEASURE_TEMPERATURE, MEASURE_ENERGY, MEASURE_PRESSURE, MEASURE_RDF, MEASURE_LJ_HIST = 0x01, 0x02, 0x04, 0x08, 0x10
 
@@ -37,7 +37,7 @@ EXPORTS = [
     "komd_gpu_surrogate_sample", "komd_gpu_surrogate_forces", "komd_gpu_surrogate_status", "komd_mlp_train",
     "komd_mlp_loss_grad", "komd_sur_data_create", "komd_sur_data_destroy", "komd_gpu_surrogate_capture",
     "komd_sur_data_snapshots", "komd_sur_data_sites", "komd_sur_data_get", "komd_sur_fit", "komd_sur_fit_grad",
-    "komd_gpu_scale_velocities", "komd_batch_create", "komd_batch_destroy", "komd_batch_step", "komd_batch_launch", "komd_batch_check",
+    "komd_gpu_scale_velocities", "komd_gpu_set_pair_table", "komd_gpu_rdf_profile", "komd_batch_create", "komd_batch_destroy", "komd_batch_step", "komd_batch_launch", "komd_batch_check",
 ]
 
 
@@ -135,6 +135,8 @@ def load() -> C.CDLL:
     L.komd_sur_data_get.argtypes = [P, I64, P, P, P, P]
     L.komd_sur_fit.argtypes = [P, P, P, P, C.c_double, C.c_double, C.c_double, C.POINTER(SurFitOpts), P]
     L.komd_gpu_scale_velocities.argtypes = [P, C.c_double]
+    L.komd_gpu_set_pair_table.argtypes = [P, I32, P, P, C.c_double, C.c_double]
+    L.komd_gpu_rdf_profile.argtypes = [P, C.c_double, I32, P]
     L.komd_batch_create.argtypes = [P, I32, I32, I32, P, C.POINTER(P)]
     L.komd_batch_destroy.argtypes = [P]
     L.komd_batch_destroy.restype = None
@@ -314,6 +316,18 @@ class GpuSystem:
     def scale_velocities(self, beta: float):
         """VelocityScaling::apply with the caller's beta (v *= beta)."""
         self._check(self.L.komd_gpu_scale_velocities(self.h, float(beta)))
+
+    def set_pair_table(self, x, y, below=1e6, above=0.0):
+        """Tabulated pair force F(r) (KOMD_TERM_TABULATED), piecewise linear."""
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.ascontiguousarray(y, np.float64)
+        self._check(self.L.komd_gpu_set_pair_table(self.h, x.size, _p(x), _p(y), float(below), float(above)))
+
+    def rdf_profile(self, max_r, nbins):
+        """RDF_Profiler histogram (ordered COM pairs, nbins bins up to max_r)."""
+        b = np.zeros(int(nbins))
+        self._check(self.L.komd_gpu_rdf_profile(self.h, float(max_r), int(nbins), _p(b)))
+        return b
 
     def surrogate_capture(self, data: "SurData"):
         """Appends the current state to a force-matching dataset."""

@@ -348,6 +348,47 @@ static inline uint64_t pot_bin(double r, double sigma, uint64_t bins) {
     return b;
 }
 
+/* FunctionPL::evaluateAt (plugins/IBI/IBI_Math.h:30-44): linear scan for the
+ * first node >= x, then ya + (yb - ya) / (xb - xa) * (x - xa).  At x == x[0]
+ * the reference would read x[-1]; the first segment is used instead. */
+static double table_eval(double x, int64_t n, const double *xs, const double *ys, double lo, double hi) {
+    if (x > xs[n - 1]) return hi;
+    if (x < xs[0]) return lo;
+    int64_t i = 0;
+    while (x > xs[i]) {
+        i++;
+        if (i == n) break;
+    }
+    if (i < 1) i = 1;
+    const double ya = ys[i - 1], yb = ys[i], xa = xs[i - 1], xb = xs[i];
+    return ya + (yb - ya) / (xb - xa) * (x - xa);
+}
+
+/* IBI_ForceFunctor<IBI_Default>::IBI_Force (plugins/IBI/IBI_ForceFunctor.cpp:18-37):
+ * every listed pair inside the cutoff (no same-molecule test), force =
+ * (dr / r) * F(r), added to the unshifted sides in list order. */
+void kor_pair_table(int64_t n_pairs, const int64_t *pairs, const double *shifts, const double *r, double cutoff,
+                    int64_t n_nodes, const double *xs, const double *ys, double lo, double hi, double *f) {
+    const double cutoff2 = pow(cutoff, 2);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int64_t p = 0; p < n_pairs; p++) {
+        const int64_t s0 = pairs[2 * p], s1 = pairs[2 * p + 1];
+        const double *sh0 = shifts + 6 * p, *sh1 = shifts + 6 * p + 3;
+        double dr[3];
+        for (int d = 0; d < 3; d++) dr[d] = (r[3 * s0 + d] + sh0[d]) - (r[3 * s1 + d] + sh1[d]);
+        const double dr2 = dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2];
+        if (dr2 > cutoff2) continue;
+        const double rr = sqrt(dr2);
+        const double F = table_eval(rr, n_nodes, xs, ys, lo, hi);
+        double fo[3];
+        for (int d = 0; d < 3; d++) fo[d] = (dr[d] / rr) * F;
+        if (!shift_nonzero(sh0)) for (int d = 0; d < 3; d++) atomic_addd(&f[3 * s0 + d], fo[d]);
+        if (!shift_nonzero(sh1)) for (int d = 0; d < 3; d++) atomic_addd(&f[3 * s1 + d], -fo[d]);
+    }
+}
+
 /* ATM2B (potentials/ATM2B.cpp:22-47) is LJ12_6_Force with the force vector
  * multiplied by potential_factor: force = dr * fac * potential_factor.  The
  * factor applies to kor_lj and kor_lj_cells while set (1 = plain LJ). */

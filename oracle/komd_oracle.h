@@ -113,6 +113,10 @@ typedef struct {
     int64_t triplets;      /* triplets inside the cutoff that were counted */
 } kor_atm_out;
 
+/* tabulated pair force (IBI_ForceFunctor): F(r) piecewise linear on ascending
+ * nodes xs with values ys, lo below / hi above */
+void kor_pair_table(int64_t n_pairs, const int64_t *pairs, const double *shifts, const double *r, double cutoff,
+                    int64_t n_nodes, const double *xs, const double *ys, double lo, double hi, double *f);
 /* ATM2B: the force factor applied by kor_lj / kor_lj_cells while set (1 = LJ12_6) */
 void kor_set_lj_force_scale(double s);
 double kor_atm2b_factor(double nu, double n_mol, double volume, double eps, double sig);

@@ -88,6 +88,8 @@ def lib():
         L.kor_step0.argtypes = [I64, P, P, P, P, D]
         L.kor_step1.argtypes = [I64, P, P, P, D]
         L.kor_temperature.argtypes = [I64, P, P, P, P, P]
+        L.kor_pair_table.argtypes = [I64, P, P, P, D, I64, P, P, D, D, P]
+        L.kor_pair_table.restype = None
         L.kor_set_lj_force_scale.argtypes = [D]
         L.kor_set_lj_force_scale.restype = None
         L.kor_atm2b_factor.argtypes = [D, D, D, D, D]
@@ -121,7 +123,7 @@ class OracleSim:
 
     def __init__(self, sysm, cell_size, cutoff, dt=0.005, nu=0.0, cutoff_atm=None, limit=1e30,
                  stiffness=30.0, lj=True, atm=False, atm_mode="compat", atm_sign=ATM_SIGN_REFERENCE,
-                 fene=False, bonded=None, virial_mode=VIRIAL_COMPAT, lj_force_scale=1.0):
+                 fene=False, bonded=None, virial_mode=VIRIAL_COMPAT, lj_force_scale=1.0, table=None):
         self.L = lib()
         self.r = np.ascontiguousarray(sysm.r, dtype=np.float64).copy()
         self.v = np.ascontiguousarray(sysm.v, dtype=np.float64).copy()
@@ -146,6 +148,10 @@ class OracleSim:
         self.atm_mode, self.atm_sign, self.virial_mode = atm_mode, atm_sign, virial_mode
         self.bonded = bonded
         self.lj_force_scale = float(lj_force_scale)   # ATM2B potential_factor (1 = LJ12_6)
+        # tabulated pair force (x, y, below, above) in place of / after LJ
+        self.table = None if table is None else (np.ascontiguousarray(table[0], np.float64),
+                                                 np.ascontiguousarray(table[1], np.float64),
+                                                 float(table[2]), float(table[3]))
         self.lj_out, self.atm_out = LJOut(), ATMOut()
         self.e_bonded = 0.0
         self.ncount = None
@@ -224,6 +230,10 @@ class OracleSim:
                           _p(self.ncount) if ncount else None, C.byref(self.lj_out), nbins, max_sigma,
                           _p(h[0]) if h else None, _p(h[1]) if h else None, _p(h[2]) if h else None,
                           _p(h[3]) if h else None)
+        if self.table is not None:
+            tx, ty, lo, hi = self.table
+            self.L.kor_pair_table(pairs.shape[0], _p(pairs), _p(shifts), _p(self.r), self.cutoff, tx.size, _p(tx),
+                                  _p(ty), lo, hi, _p(self.f))
         if self.use_fene:
             self.L.kor_fene(pairs.shape[0], _p(pairs), _p(shifts), _p(self.r), _p(self.eps), _p(self.sig),
                             _p(self.id), self.stiffness, _p(self.f))
@@ -270,6 +280,17 @@ class OracleSim:
         acc = np.zeros(6)
         self.L.kor_momentum(self.n_mol if n_terms is None else n_terms, _p(self.v), _p(self.m), _p(acc))
         return acc
+
+    def rdf_profile(self, max_r, nbins):
+        """RDF_Profiler::measure + getRDF for one sample (plugins/IBI/RDF_Profiler.cpp:18-55):
+        raw histogram with dr = max_r / nbins, then the normalised g(r)."""
+        bins = np.zeros(nbins)
+        com = np.zeros((self.n_mol, 3))
+        self.L.kor_com(self.n_mol, _p(self.mol_off), _p(self.r), _p(self.m), _p(com))
+        box = (self.high - self.low).copy()
+        dr = max_r / nbins
+        self.L.kor_rdf(self.n_mol, _p(com), _p(box), max_r, dr, nbins, _p(bins))
+        return bins, rdf_profile_normalise(bins, 1, max_r, nbins, self.n_mol, float(np.prod(box)))
 
     def rdf(self, max_r, dr):
         nb = int(self.L.kor_rdf_nbins(max_r, dr))
@@ -349,3 +370,15 @@ def sur_energy_forces(r, box, params, fmean, fstd, e_scale, e_shift, rc=2.0):
 def atm2b_factor(nu, n_mol, volume, eps, sig):
     """ATM2B::ATM2B's potential_factor (kor_atm2b_factor)."""
     return lib().kor_atm2b_factor(float(nu), float(n_mol), float(volume), float(eps), float(sig))
+
+
+def rdf_profile_normalise(bins, samples, max_r, nbins, n, volume):
+    """RDF_Profiler::getRDF (RDF_Profiler.cpp:34-52): bins / samples / (N (N-1) V_bin / V)."""
+    dr = max_r / nbins
+    out = np.zeros(nbins)
+    for b in range(nbins):
+        rmin, rmax = b * dr, (b + 1) * dr
+        binvol = (4.0 / 3.0) * np.pi * (rmax * rmax * rmax - rmin * rmin * rmin)
+        den = n * (n - 1.0) * binvol / volume
+        out[b] = bins[b] / samples / den
+    return out

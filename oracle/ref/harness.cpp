@@ -39,6 +39,8 @@
 #include "potentials/ATM_NOLIST.h"
 #include "potentials/ATM2B.h"
 #include "thermostats/VelocityScaling.h"
+#include "plugins/IBI/IBI_ForceFunctor.h"
+#include "plugins/IBI/RDF_Profiler.h"
 #include "sensors/PressureSensor.h"
 #include "sensors/LJ12_6_Sensor.h"
 #include "sensors/RDFSensor.h"
@@ -81,9 +83,27 @@ int main(int argc, char** argv) {
         // still 0 and the factor comes out as exactly 1; here it is built after the
         // checkpoint is loaded so that the factor formula itself is exercised.  It
         // goes first in the functor list as in main.cpp:57-58.
-        Registry::instance->forceFunctors().insert(Registry::instance->forceFunctors().begin(),
-            atm2b ? std::shared_ptr<ForceFunctor>(std::make_shared<ATM2B>())
-                  : std::shared_ptr<ForceFunctor>(std::make_shared<LJ12_6>()));
+        // KOMD_HARNESS_IBI_TABLE=<file>: IBI_ForceFunctor<IBI_Default> with that
+        // force table (FunctionPL::read; defaults 1e6 below, 0 above as
+        // IBI::derivativeOfPotential sets them) takes the LJ functor's place, as
+        // the IBI plugin swaps it in (IBI.cpp:52-54); the RDF_Profiler histogram
+        // is dumped as IBIRDF
+        const char* ibi_table = getenv("KOMD_HARNESS_IBI_TABLE");
+        std::shared_ptr<ForceFunctor> first;
+        if (ibi_table && *ibi_table) {
+            auto ibi = std::make_shared<IBI_ForceFunctor<IBI_Default>>();
+            ibi->getForceFunction().read(ibi_table);
+            ibi->getForceFunction().setLowerDefault(1e+6);
+            ibi->getForceFunction().setUpperDefault(0.0);
+            first = ibi;
+        } else if (atm2b) {
+            first = std::make_shared<ATM2B>();
+        } else {
+            first = std::make_shared<LJ12_6>();
+        }
+        Registry::instance->forceFunctors().insert(Registry::instance->forceFunctors().begin(), first);
+        std::unique_ptr<RDF_Profiler> profiler;
+        if (ibi_table && *ibi_table) profiler = std::make_unique<RDF_Profiler>();
 
         auto temp = std::make_shared<TemperatureSensor>();
         // KOMD_HARNESS_THERMOSTAT=1: the always-on VelocityScaling of main.cpp:95
@@ -165,6 +185,14 @@ int main(int argc, char** argv) {
                 const auto& t = pres->getPressureTensor();
                 fprintf(out, "PRESSURE 6\n");
                 for (int k = 0; k < 6; k++) fprintf(out, "%.17g\n", t[k]);
+            }
+            if (profiler) {
+                profiler->reset();
+                profiler->measure();
+                KW::vec_t<double> g("IBIRDF", profiler->getBufferSize());
+                profiler->getRDF(g);
+                fprintf(out, "IBIRDF %llu\n", (unsigned long long)profiler->getBufferSize());
+                for (uint64_t k = 0; k < profiler->getBufferSize(); k++) fprintf(out, "%.17g\n", g[k]);
             }
             if (rdf) {
                 rdf->measure();

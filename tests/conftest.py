@@ -8,7 +8,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-CASES = ["lj864", "ljatm864", "atmlist500", "fene375", "edge_box", "atm2b864", "thermo864"]
+CASES = ["lj864", "ljatm864", "atmlist500", "fene375", "edge_box", "atm2b864", "thermo864", "ibi864"]
 
 
 def pytest_configure(config):

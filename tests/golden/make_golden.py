@@ -68,6 +68,10 @@ def parse_dump(path):
         elif key == "PRESSURE":
             cur["pressure"] = np.array([float(lines[i + k]) for k in range(6)])
             i += 6
+        elif key == "IBIRDF":
+            n = int(ln[1])
+            cur["ibirdf"] = np.array([float(lines[i + k]) for k in range(n)])
+            i += n
         elif key in ("TEMP", "UPOT"):
             cur[key.lower()] = float(ln[1])
         elif key == "NPAIRS":
@@ -75,7 +79,7 @@ def parse_dump(path):
     return steps
 
 
-def run_case(name, sysm, values, steps, dumps, comps=None, thermostat=False):
+def run_case(name, sysm, values, steps, dumps, comps=None, thermostat=False, table=None):
     tmp = tempfile.mkdtemp(prefix=f"komd_golden_{name}_")
     try:
         ps = os.path.join(tmp, "in.ps")
@@ -84,6 +88,11 @@ def run_case(name, sysm, values, steps, dumps, comps=None, thermostat=False):
         with open(os.path.join(tmp, "in.dat"), "w") as fh:
             fh.write(komd_io.format_input(values, ps, comps))
         env = dict(os.environ, KOMD_HARNESS_THERMOSTAT="1" if thermostat else "0")
+        if table is not None:
+            tab = os.path.join(tmp, "force.txt")
+            with open(tab, "w") as fh:   # FunctionPL::write layout: "x\ty" per line
+                fh.write("\n".join("%.17g\t%.17g" % (x, y) for x, y in zip(*table)))
+            env["KOMD_HARNESS_IBI_TABLE"] = tab
         res = subprocess.run([HARNESS, "in.dat", "out.txt", str(steps)] + [str(d) for d in dumps], cwd=tmp,
                              capture_output=True, text=True, env=env)
         if res.returncode != 0:
@@ -93,6 +102,8 @@ def run_case(name, sysm, values, steps, dumps, comps=None, thermostat=False):
                       low=np.asarray(values["domain_low"], float), high=np.asarray(values["domain_high"], float),
                       dumps=np.array(dumps, np.int64))
         arrays["p_thermostat"] = np.int64(1 if thermostat else 0)
+        if table is not None:
+            arrays["table_x"], arrays["table_y"] = np.asarray(table[0]), np.asarray(table[1])
         for k in ("cutoff", "cell_size", "delta_t", "limit", "energy_3b", "stiffness", "sensor_rdf_max",
                   "sensor_rdf_dr", "temperature"):
             if k in values:
@@ -179,7 +190,16 @@ def main(selected):
         run_case("thermo864", s, base_values(s, 2.5, 2.5, 0.005, 50, temperature=1.2), 50, [0, 1, 50],
                  thermostat=True)
 
-    cases = dict(lj864=lj864, ljatm864=ljatm864, atmlist500=atmlist500, fene375=fene375, edge_box=edge_box,
+    def ibi864():
+        # tabulated pair force (IBI_ForceFunctor) in place of LJ: the LJ force
+        # sampled on IBI_bins = 100 nodes (i + 1/2) * 2.5/100, linear in between;
+        # plus the RDF_Profiler histogram (100 bins to the cutoff)
+        s = lattice.argon_fcc(6, rho=0.8442, t_star=0.722, seed=18, jitter=0.05)
+        x = (np.arange(100) + 0.5) * 2.5 / 100
+        y = 24.0 * (2.0 * x ** -13 - x ** -7)
+        run_case("ibi864", s, base_values(s, 2.5, 2.5, 0.005, 20), 20, [0, 1, 20], table=(x, y))
+
+    cases = dict(ibi864=ibi864, lj864=lj864, ljatm864=ljatm864, atmlist500=atmlist500, fene375=fene375, edge_box=edge_box,
                  atm2b864=atm2b864, thermo864=thermo864)
     for name in (selected or list(cases)):
         cases[name]()

@@ -31,6 +31,8 @@ def gpu_for_case(z, precision=None, **over):
         terms |= gpu.TERM_ATM
     if int(z.get("p_enable_3b_approx", 0)):
         terms |= gpu.TERM_ATM2B
+    if "table_x" in z:   # the tabulated force in LJ12_6's place
+        terms = (terms & ~gpu.TERM_LJ) | gpu.TERM_TABULATED
     kw = dict(cutoff=float(z["p_cutoff"]), cutoff_3b=float(z["p_cutoff"]), nu=lattice.energy_3b_to_nu(float(z["p_energy_3b"])),
               dt=float(z["p_delta_t"]), terms=terms, precision=gpu.FP32 if precision is None else precision,
               atm_direct=int(z["p_enable_3b_direct"]), stiffness=float(z.get("p_stiffness", 30.0)),
@@ -39,7 +41,10 @@ def gpu_for_case(z, precision=None, **over):
               temperature_target=float(z.get("p_temperature", 0.0)))
     kw.update(over)
     cfg = gpu.make_config(z["low"], z["high"], float(z["p_cell_size"]), **kw)
-    return gpu.GpuSystem(s, cfg), s
+    g = gpu.GpuSystem(s, cfg)
+    if "table_x" in z:
+        g.set_pair_table(z["table_x"], z["table_y"], 1e6, 0.0)
+    return g, s
 
 
 def _state_at(z, step):
@@ -137,6 +142,37 @@ def test_atm2b_trajectory_follows_reference():
     r, v, f = g.download()
     assert np.abs(r - z["s20_R"]).max() < 1e-8
     assert rel_rmse(f, z["s20_F"]) < 1e-6
+    g.close()
+
+
+def test_tabulated_force_and_rdf_profiler_follow_reference(oracle_lib):
+    """ibi864: the tabulated pair force (IBI_ForceFunctor with a 100-node
+    table) keeps the reference's trajectory for 20 steps in FP64, and the
+    RDF_Profiler histogram matches it; replacing the table between steps
+    reaches the captured step graph."""
+    from komd_gb300 import gpu
+    z = load_case("ibi864")
+    g, s = gpu_for_case(z, precision=gpu.FP64)
+    g.update_container()
+    g.forces()
+    _, _, f0 = g.download()
+    assert rel_rmse(f0, z["s0_F"]) < 1e-13
+    g.step(1)
+    r1, _, _ = g.download()
+    assert np.abs(r1 - z["s1_R"]).max() < 1e-12
+    nb = z["s1_ibirdf"].size
+    bins = g.rdf_profile(float(z["p_cutoff"]), nb)
+    gr = oracle_lib.rdf_profile_normalise(bins, 1, float(z["p_cutoff"]), nb, s.n, float(np.prod(z["high"] - z["low"])))
+    np.testing.assert_allclose(gr, z["s1_ibirdf"], rtol=1e-14, atol=0)
+    g.step(19)
+    r, _, f = g.download()
+    assert np.abs(r - z["s20_R"]).max() < 1e-8
+    assert rel_rmse(f, z["s20_F"]) < 1e-6
+    # a zero table switches the pair force off inside the same graph
+    g.set_pair_table(z["table_x"], np.zeros_like(z["table_y"]), 1e6, 0.0)
+    g.step(1)
+    _, _, fz = g.download()
+    assert np.abs(fz).max() == 0.0
     g.close()
 
 
