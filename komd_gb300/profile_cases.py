@@ -1,0 +1,82 @@
+"""Small fixed workloads for kernel profiling (ncu) and quick timing.
+
+    python -m komd_gb300.profile_cases exact      [--ncell 40] [--steps 3] [--equil 0]
+    python -m komd_gb300.profile_cases surrogate  [--ncell 40] [--steps 3]
+    python -m komd_gb300.profile_cases replicas   [--count 64] [--steps 2]
+
+`exact`: LJ + FULL ATM argon (rho* 0.8442, T* 0.722, rc 2.5 / 2.0, nu* 0.073,
+cell 2.8, skin 0.3), the benchmark's engine configuration.  `surrogate`: the
+same with the learned three-body term on Glorot-initialised weights (kernel
+cost does not depend on the weights).  `replicas`: `count` uneven replicas
+(2000-20000 atoms) advanced by one batched graph.  Each prints its mean step
+time; the launches before the measured steps are few, so that a profiler can
+skip to them.
+"""
+from __future__ import annotations
+
+import argparse
+import time
+
+import numpy as np
+
+from . import gpu, lattice, surrogate
+
+
+def exact(ncell, steps, equil, learned=False):
+    s = lattice.argon_fcc(ncell, rho=0.8442, t_star=0.722, seed=1)
+    terms = gpu.TERM_LJ | gpu.TERM_ATM | (gpu.TERM_ATM_SURROGATE if learned else 0)
+    g = gpu.GpuSystem(s, surrogate.physics_config(s, 2.8, skin=0.3, terms=terms))
+    g.update_container()
+    g.forces()
+    if learned:
+        x, e3, _ = g.surrogate_sample()
+        model = dict(params=surrogate.init_params(1), fmean=x.mean(0).astype(np.float32),
+                     fstd=(x.std(0) + 1e-6).astype(np.float32), e_scale=float(e3.std()), e_shift=float(e3.mean()))
+        g.surrogate_load(model, probe_every=0)
+        g.forces()
+    if equil:
+        g.step(equil)
+    t0 = time.perf_counter()
+    g.step(steps)
+    dt = (time.perf_counter() - t0) / steps
+    print(f"{'surrogate' if learned else 'exact'} n={s.n}: {dt * 1e3:.3f} ms/step (host clock)")
+    g.close()
+
+
+def replicas(count, steps):
+    rng = np.random.default_rng(2027)
+    reps = []
+    for _ in range(count):
+        s = lattice.trimmed_fcc(int(rng.integers(2000, 20001)), float(rng.uniform(0.7, 0.9)),
+                                float(rng.uniform(0.6, 1.5)), int(rng.integers(1 << 30)))
+        L = float(s.high[0])
+        g = gpu.GpuSystem(s, surrogate.physics_config(s, L / np.floor(L / 2.8), skin=0.3))
+        g.update_container()
+        g.forces()
+        reps.append(g)
+    b = gpu.Batch(reps, n_streams=32, steps_per_graph=1)
+    t0 = time.perf_counter()
+    b.step(steps)
+    dt = (time.perf_counter() - t0) / steps
+    print(f"replicas x{count}: {dt * 1e3:.3f} ms/step (host clock)")
+    b.close()
+    for g in reps:
+        g.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("case", choices=["exact", "surrogate", "replicas"])
+    ap.add_argument("--ncell", type=int, default=40)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--equil", type=int, default=0)
+    ap.add_argument("--count", type=int, default=64)
+    a = ap.parse_args()
+    if a.case == "replicas":
+        replicas(a.count, a.steps)
+    else:
+        exact(a.ncell, a.steps, a.equil, learned=a.case == "surrogate")
+
+
+if __name__ == "__main__":
+    main()
