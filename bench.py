@@ -48,6 +48,14 @@ WORKLOADS = {
 FLOP_PER_TRIPLET = 200.0
 
 
+def max_over_ranks(x, dist, device):
+    """The largest value of x over all ranks (the timed region's max over ranks)."""
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
@@ -328,9 +336,7 @@ def surrogate_leg(args, g, s, stream, local, dist, exact_value, world):
     prof = g.profile()
     g.set_profiling(False)
     if dist:
-        tt = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+        ms = max_over_ranks(ms, dist, "cuda")
     st = g.surrogate_status()
     value = world * s.n * args.steps / (ms / 1e3)
     return {"value": value, "unit": UNIT, "ms_per_step": ms / args.steps, "speedup_vs_exact": value / exact_value,
@@ -399,9 +405,7 @@ def run_ours(args, w, name):
     prof = g.profile()
     g.set_profiling(False)
     if dist:
-        tt = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+        ms = max_over_ranks(ms, dist, "cuda")
         dist.barrier()
     value = world * s.n * args.steps / (ms / 1e3)
 
@@ -430,9 +434,7 @@ def run_ours(args, w, name):
         g.step_host(1, r_h.numpy(), v_h.numpy(), f_h.numpy())
     e_s = time.perf_counter() - e0
     if dist:
-        tt = torch.tensor([e_s], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e_s = float(tt.item())
+        e_s = max_over_ranks(e_s, dist, "cuda")
     e2e = world * s.n * args.steps / e_s
 
     sur = None

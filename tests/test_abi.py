@@ -10,7 +10,7 @@ from conftest import ROOT
 def declared_symbols():
     with open(os.path.join(ROOT, "include", "komd_gpu.h")) as fh:
         text = fh.read()
-    return sorted(set(re.findall(r"\b(komd_gpu_\w+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(komd_\w+)\s*\(", text)))
 
 
 def test_library_exports_every_declared_symbol():
@@ -38,3 +38,14 @@ def test_abi_version_and_error_reporting_without_gpu():
     cfg = gpu.make_config([0, 0, 0], [20, 20, 20], 2.0, cutoff=2.5)  # cell smaller than cutoff
     assert lib.komd_gpu_create(ctypes.byref(cfg), 0, ctypes.byref(h)) == 1
     assert b"cell size" in lib.komd_gpu_last_error()
+    cfg = gpu.make_config([0, 0, 0], [20, 20, 20], 2.5, cutoff=2.5, thermostat=1)   # no target temperature
+    assert lib.komd_gpu_create(ctypes.byref(cfg), 0, ctypes.byref(h)) == 1
+    assert b"temperature_target" in lib.komd_gpu_last_error()
+    cfg = gpu.make_config([0, 0, 0], [20, 20, 20], 2.8, cutoff=2.5, terms=gpu.TERM_TABULATED, skin=0.3)
+    assert lib.komd_gpu_create(ctypes.byref(cfg), 0, ctypes.byref(h)) == 1
+    assert b"tabulated" in lib.komd_gpu_last_error()
+    cfg = gpu.make_config([0, 0, 0], [20, 20, 20], 2.5, cutoff=2.5, terms=gpu.TERM_ATM2B)   # ATM2B without LJ
+    assert lib.komd_gpu_create(ctypes.byref(cfg), 0, ctypes.byref(h)) == 1
+    assert b"ATM2B" in lib.komd_gpu_last_error()
+    b = ctypes.c_void_p()
+    assert lib.komd_batch_create(None, 0, 1, 1, None, ctypes.byref(b)) == 1   # no replicas
