@@ -299,6 +299,51 @@ def replicas_leg(args, stream, local):
                       "rc 2.5 / 2.0, nu* 0.073, dt* 0.005, skin 0.3; RDF 200 bins to 2.5, virial pressure per replica"}
 
 
+def drift_leg(args, local, model=None):
+    """NVE energy drift: 32,000 LJ + ATM argon atoms (FCC 20^3, rho* 0.8442,
+    T* 0.722), rc 2.5 / 2.0, nu* 0.073, dt* 0.005, 1000 steps of
+    equilibration, then 10^4 steps with the total energy (kinetic + LJ + ATM,
+    reduced units) sampled every 500 steps; the drift is the fitted slope per
+    atom per 10^4 steps.  Forms: exact FP32 forces, exact FP64 forces, and
+    the learned three-body term when a trained model is given."""
+    from komd_gb300 import gpu, lattice, surrogate
+    out = {}
+    forms = [("fp32_exact", gpu.FP32, False), ("fp64_exact", gpu.FP64, False)]
+    if model is not None:
+        forms.append(("fp32_learned", gpu.FP32, True))
+    for name, prec, learned in forms:
+        s = lattice.argon_fcc(20, rho=0.8442, t_star=0.722, seed=3)
+        terms = gpu.TERM_LJ | gpu.TERM_ATM | (gpu.TERM_ATM_SURROGATE if learned else 0)
+        skin = 0.3 if prec == gpu.FP32 else 0.0
+        cfg = gpu.make_config(s.low, s.high, 2.8, cutoff=2.5, cutoff_3b=2.0, nu=0.073, dt=0.005, terms=terms,
+                              precision=prec, atm_sign=gpu.ATM_SIGN_PHYSICAL, atm_enum=gpu.ATM_ENUM_FULL,
+                              virial_mode=gpu.VIRIAL_CORRECT, skin=skin)
+        g = gpu.GpuSystem(s, cfg, device=local)
+        if learned:
+            g.surrogate_load(model, probe_every=0)
+        g.update_container()
+        g.forces()
+        t0 = time.perf_counter()
+        g.step(1000)
+        steps, energy = [], []
+        for k in range(21):
+            o = g.measure(gpu.MEASURE_ENERGY | gpu.MEASURE_TEMPERATURE)
+            steps.append(500 * k)
+            energy.append(0.5 * o["mv2"] + o["u_lj"] + o["u_atm"])
+            if k < 20:
+                g.step(500)
+        wall = time.perf_counter() - t0
+        e = np.asarray(energy) / s.n
+        slope = float(np.polyfit(np.asarray(steps, float), e, 1)[0])
+        out[name] = {"drift_per_atom_per_1e4_steps": slope * 1e4, "max_abs_dev_per_atom": float(np.abs(e - e[0]).max()),
+                     "e_per_atom_start": float(e[0]), "wall_s": wall}
+        g.close()
+    out["system"] = ("32,000 atoms FCC 20^3, rho* 0.8442, T* 0.722, LJ rc 2.5 + ATM rc 2.0 (FULL, -grad V), "
+                     "nu* 0.073, dt* 0.005, 1000 steps equilibration + 10^4 steps, energy every 500 steps")
+    out["target"] = "<= 1e-4 epsilon per atom per 10^4 steps"
+    return out
+
+
 def surrogate_leg(args, g, s, stream, local, dist, exact_value, world):
     """FP32 + learned three-body form of the same workload: training set from
     the exact kernel (2000 snapshots of 500 atoms over T* in [0.6, 1.2],
@@ -339,6 +384,7 @@ def surrogate_leg(args, g, s, stream, local, dist, exact_value, world):
         ms = max_over_ranks(ms, dist, "cuda")
     st = g.surrogate_status()
     value = world * s.n * args.steps / (ms / 1e3)
+    g.last_model = model
     return {"value": value, "unit": UNIT, "ms_per_step": ms / args.steps, "speedup_vs_exact": value / exact_value,
             "form": "FP32 LJ + learned three-body term (32-64-64-1 MLP, BF16 tensor-core inference)",
             "force_rmse_3body": {"at_start": rmse0, "probe_last": st["last_rmse"], "probe_max": st["max_rmse"],
@@ -443,6 +489,9 @@ def run_ours(args, w, name):
     reps = None
     if args.replicas > 0:
         reps = replicas_leg(args, stream, local)
+    drift = None
+    if w["atm"] and not args.no_drift and rank == 0:
+        drift = drift_leg(args, local, getattr(g, "last_model", None))
 
     if rank != 0:
         if dist:
@@ -499,6 +548,8 @@ def run_ours(args, w, name):
         line["surrogate"] = sur
     if reps:
         line["replicas"] = reps
+    if drift:
+        line["nve_drift"] = drift
     print(json.dumps(line), flush=True)
     g.close()
     if dist:
@@ -520,6 +571,7 @@ def main():
     ap.add_argument("--no-surrogate", action="store_true", help="skip the learned three-body leg")
     ap.add_argument("--sur-epochs", type=int, default=30)
     ap.add_argument("--replicas", type=int, default=512, help="batched-replica leg (0 = skip)")
+    ap.add_argument("--no-drift", action="store_true", help="skip the NVE energy-drift leg")
     ap.add_argument("--replica-steps", type=int, default=20)
     ap.add_argument("--replica-streams", type=int, default=32)
     ap.add_argument("--replica-graph-steps", type=int, default=5)
