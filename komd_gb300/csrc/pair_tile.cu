@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(kTileThreads) k_pair_tile(PairParams p) {
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kTileThreads) k_vlist_build(PairParams p) {
     __shared__ float4 s_pos[kStage];
-    __shared__ int4 s_aux[kStage];
+    __shared__ int2 s_aux[kStage];      // (list entry without the same-molecule bit, molecule key)
     __shared__ float4 s_hpos[kHome];
     __shared__ int s_hkey[kHome];
     __shared__ int s_cnt[kHome];
@@ -324,35 +324,52 @@ __global__ void __launch_bounds__(kTileThreads) k_vlist_build(PairParams p) {
                 q.y += s_nbo[nb][1];
                 q.z += s_nbo[nb][2];
                 s_pos[t] = q;
-                s_aux[t] = make_int4(j, p.skey[j], nb, 0);
+                s_aux[t] = make_int2((int)(((unsigned)nb << 26) | (unsigned)j), p.skey[j]);
             }
             __syncthreads();
-            for (int i = w; i < hc; i += kTileWarps) {
-                const float4 pi = s_hpos[i];
-                const int ki = s_hkey[i];
-                const int self = self_base + i - sb;
-                const int slot_i = hs + hb + i;
-                int cnt = s_cnt[i];
+            // two home sites per warp pass: one staged position load serves both
+            // tests; the list word is read only for hits
+            for (int ia = w; ia < hc; ia += 2 * kTileWarps) {
+                const int ib = ia + kTileWarps;
+                const bool two = ib < hc;
+                const float4 pa = s_hpos[ia];
+                const float4 pb = two ? s_hpos[ib] : pa;
+                const int ka = s_hkey[ia], kb = two ? s_hkey[ib] : 0;
+                const int selfa = self_base + ia - sb, selfb = self_base + ib - sb;
+                const size_t rowa = (size_t)(hs + hb + ia) * p.vl_cap, rowb = (size_t)(hs + hb + ib) * p.vl_cap;
+                int ca = s_cnt[ia], cb = two ? s_cnt[ib] : 0;
                 for (int j0 = 0; j0 < ns; j0 += 32) {
                     const int j = j0 + lane;
-                    bool hit = false;
-                    int4 a = make_int4(0, 0, 0, 0);
-                    if (j < ns && j != self) {
+                    bool ha = false, hbb = false;
+                    if (j < ns) {
                         const float4 pj = s_pos[j];
-                        const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-                        hit = dx * dx + dy * dy + dz * dz <= rl2;
-                        a = s_aux[j];
+                        const float ax = pa.x - pj.x, ay = pa.y - pj.y, az = pa.z - pj.z;
+                        ha = j != selfa && ax * ax + ay * ay + az * az <= rl2;
+                        if (two) {
+                            const float bx = pb.x - pj.x, by = pb.y - pj.y, bz = pb.z - pj.z;
+                            hbb = j != selfb && bx * bx + by * by + bz * bz <= rl2;
+                        }
                     }
-                    const unsigned m = __ballot_sync(0xffffffffu, hit);
-                    if (hit) {
-                        const int pos = cnt + __popc(m & lt);
-                        if (pos < p.vl_cap)
-                            p.vl[(size_t)slot_i * p.vl_cap + pos] =
-                                (a.y == ki ? 0x80000000u : 0u) | ((unsigned)a.z << 26) | (unsigned)a.x;
+                    const unsigned ma = __ballot_sync(0xffffffffu, ha);
+                    const unsigned mb = __ballot_sync(0xffffffffu, hbb);
+                    if (ha || hbb) {
+                        const int2 a = s_aux[j];
+                        if (ha) {
+                            const int pos = ca + __popc(ma & lt);
+                            if (pos < p.vl_cap) p.vl[rowa + pos] = (a.y == ka ? 0x80000000u : 0u) | (unsigned)a.x;
+                        }
+                        if (hbb) {
+                            const int pos = cb + __popc(mb & lt);
+                            if (pos < p.vl_cap) p.vl[rowb + pos] = (a.y == kb ? 0x80000000u : 0u) | (unsigned)a.x;
+                        }
                     }
-                    cnt += __popc(m);
+                    ca += __popc(ma);
+                    cb += __popc(mb);
                 }
-                if (lane == 0) s_cnt[i] = cnt;
+                if (lane == 0) {
+                    s_cnt[ia] = ca;
+                    if (two) s_cnt[ib] = cb;
+                }
                 __syncwarp();
             }
         }
