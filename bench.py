@@ -259,9 +259,14 @@ def replicas_leg(args, stream, local):
     torch.cuda.synchronize()
     seq_s = time.perf_counter() - t1
     # batched: one graph per steps_per_graph steps of all replicas
-    spg = args.replica_graph_steps
+    spg, nstr = args.replica_graph_steps, args.replica_streams
+    tuned = None
+    if not args.replica_fixed:
+        from komd_gb300 import autotune
+        tuned = autotune.tune_batch(reps, streams=(16, 32, 64), graph_steps=(1, 5, 10), steps=10)
+        spg, nstr = tuned["best"]["steps_per_graph"], tuned["best"]["streams"]
     t2 = time.perf_counter()
-    batch = gpu.Batch(reps, n_streams=args.replica_streams, steps_per_graph=spg, stream=stream.cuda_stream)
+    batch = gpu.Batch(reps, n_streams=nstr, steps_per_graph=spg, stream=stream.cuda_stream)
     capture_s = time.perf_counter() - t2
     batch.step(max(1, 3 // spg))
     torch.cuda.synchronize()
@@ -290,7 +295,7 @@ def replicas_leg(args, stream, local):
         g.close()
     return {"value": value, "unit": UNIT, "replicas": len(reps), "atoms": n_atoms, "steps": steps,
             "ms_per_step": ms / steps, "sequential": {"value": seq_value, "steps": k, "s": seq_s},
-            "speedup_vs_sequential": value / seq_value, "streams": args.replica_streams,
+            "speedup_vs_sequential": value / seq_value, "streams": nstr, "autotune": tuned,
             "steps_per_graph": spg, "setup_s": setup_s, "capture_s": capture_s, "clocks": clk.summary(),
             "pressure_star": {"min": float(np.min(pres)), "median": float(np.median(pres)), "max": float(np.max(pres))},
             "rdf_first_peak_r": {"min": float(np.nanmin(peaks)), "median": float(np.nanmedian(peaks)),
@@ -413,7 +418,8 @@ def run_ours(args, w, name):
     terms = gpu.TERM_LJ | (gpu.TERM_ATM | gpu.TERM_ATM_SURROGATE if w["atm"] else 0)   # learned form off until loaded
     cfg = gpu.make_config(s.low, s.high, w["cell"], cutoff=w["rc"], cutoff_3b=w["rc3"], nu=w["nu"], dt=w["dt"],
                           terms=terms, precision=gpu.FP32, atm_sign=gpu.ATM_SIGN_PHYSICAL,
-                          atm_enum=gpu.ATM_ENUM_FULL, virial_mode=gpu.VIRIAL_CORRECT, skin=w["skin"])
+                          atm_enum=gpu.ATM_ENUM_FULL, virial_mode=gpu.VIRIAL_CORRECT,
+                          skin=w["skin"] if args.skin is None else args.skin)
     g = gpu.GpuSystem(s, cfg, device=local)
     # the engine runs on a torch-created stream so that torch's CUDA events
     # time exactly the engine's launches (the legacy default stream would not
@@ -430,6 +436,28 @@ def run_ours(args, w, name):
     # also capture the CUDA graph); the triplet count is taken after both
     if args.equil > 0:
         g.step(args.equil)
+    tuned = None
+    if args.skin is None and w.get("skin", 0) > 0:
+        # measured choice of the Verlet skin (and cell edge) on the equilibrated state
+        from komd_gb300 import autotune, lattice
+        r_eq, v_eq, _ = g.download()
+        s_eq = lattice.System(r=r_eq, v=v_eq, m=s.m, eps=s.eps, sig=s.sig, mol_id=s.mol_id, low=s.low, high=s.high)
+
+        def make_cfg(skin, cell):
+            return gpu.make_config(s.low, s.high, cell, cutoff=w["rc"], cutoff_3b=w["rc3"], nu=w["nu"], dt=w["dt"],
+                                   terms=terms, precision=gpu.FP32, atm_sign=gpu.ATM_SIGN_PHYSICAL,
+                                   atm_enum=gpu.ATM_ENUM_FULL, virial_mode=gpu.VIRIAL_CORRECT, skin=skin)
+        tuned = autotune.tune_skin(s_eq, make_cfg, (0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 1.0), max(w["rc"], w["rc3"]), device=local)
+        best = tuned["best"]
+        g.close()
+        cfg = make_cfg(best["skin"], best["cell"])
+        s = s_eq
+        g = gpu.GpuSystem(s, cfg, device=local)
+        g.set_stream(stream.cuda_stream)
+        g.update_container()
+        g.forces()
+    elif args.skin is not None:
+        tuned = {"best": {"skin": args.skin, "cell": w["cell"]}, "table": "fixed by --skin"}
     g.step(max(args.warmup, 3))
     torch.cuda.synchronize()
     obs0 = g.measure(gpu.MEASURE_ENERGY | gpu.MEASURE_TEMPERATURE)
@@ -531,7 +559,9 @@ def run_ours(args, w, name):
             "config": {"workload": name, "form": "exact FP32 (LJ + FULL ATM, F = -grad V)", "sites": s.n,
                        "equilibration_steps": args.equil, "temperature_K_at_timing": obs0["temperature"],
                        "rc_lj": w["rc"], "rc_atm": w["rc3"], "nu_star": w["nu"], "cell": w["cell"], "dt": w["dt"],
-                       "verlet_skin": w["skin"],
+                       "verlet_skin": tuned["best"]["skin"] if tuned else w["skin"],
+                       "cell_edge": tuned["best"]["cell"] if tuned else w["cell"],
+                       "autotune": tuned,
                        "triplets_per_step": triplets, "parallelism": f"replicas x{world}",
                        "l2": "no flush: the per-step working set exceeds L2 (the ATM neighbour list alone, "
                              "16 B x capacity per site, is written and re-read every step)"},
@@ -572,9 +602,11 @@ def main():
     ap.add_argument("--sur-epochs", type=int, default=30)
     ap.add_argument("--replicas", type=int, default=512, help="batched-replica leg (0 = skip)")
     ap.add_argument("--no-drift", action="store_true", help="skip the NVE energy-drift leg")
+    ap.add_argument("--skin", type=float, default=None, help="fixed Verlet skin (default: chosen by the autotuner)")
     ap.add_argument("--replica-steps", type=int, default=20)
     ap.add_argument("--replica-streams", type=int, default=32)
     ap.add_argument("--replica-graph-steps", type=int, default=5)
+    ap.add_argument("--replica-fixed", action="store_true", help="use --replica-streams/--replica-graph-steps as given")
     ap.add_argument("--sur-probe", type=int, default=50, help="exact-ATM probe interval of the learned form")
     ap.add_argument("--sur-threshold", type=float, default=0.2,
                     help="probe breach (relative three-body force RMSE) that switches back to exact ATM")

@@ -45,3 +45,20 @@ def test_batch_rejects_bad_input():
     with pytest.raises(gpu.KomdError):
         gpu.Batch([g, g])                           # the same replica twice
     g.close()
+
+
+def test_autotuner_picks_a_measured_shape():
+    from komd_gb300 import autotune, gpu, lattice, surrogate
+    reps = [_replica(*sp) for sp in SPECS[:3]]
+    t = autotune.tune_batch(reps, streams=(2, 3), graph_steps=(1, 2), steps=4)
+    assert len(t["table"]) == 4
+    assert t["best"]["ms_per_step"] == min(r["ms_per_step"] for r in t["table"])
+    for g in reps:
+        g.close()
+    s = lattice.argon_fcc(8, rho=0.8442, t_star=0.722, seed=5)          # 2048 atoms, L = 13.4
+
+    def make_cfg(skin, cell):
+        return surrogate.physics_config(s, cell, skin=skin)
+    t = autotune.tune_skin(s, make_cfg, (0.2, 0.4), 2.5, steps=20, warmup=5)
+    assert [r["skin"] for r in sorted(t["table"], key=lambda r: r["skin"])] == [0.2, 0.4]
+    assert all(r["cell"] >= 2.5 + r["skin"] for r in t["table"])

@@ -61,3 +61,11 @@ def test_parse_rejects_like_reference():
 def test_unit_mapping():
     assert lattice.energy_3b_to_nu(lattice.nu_star_to_energy_3b(0.073)) == pytest.approx(0.073, rel=1e-15)
     assert komd_io.rdf_nbins(2.5, 0.0125) in (199, 200)
+
+
+def test_autotune_cell_edge():
+    from komd_gb300 import autotune
+    assert autotune.cell_for(67.184, 2.8) == pytest.approx(67.184 / 23)
+    assert autotune.cell_for(10.0, 2.5) == pytest.approx(2.5)
+    with pytest.raises(ValueError):
+        autotune.cell_for(7.0, 2.5)
