@@ -457,7 +457,7 @@ int komd_gpu_destroy(komd_gpu *h) {
     dfree(e.cell_count); dfree(e.cell_start); dfree(e.cell_mcount); dfree(e.cell_mstart); dfree(e.cell_mols);
     dfree(e.slot_site); dfree(e.skey); dfree(e.pos4); dfree(e.seps); dfree(e.posd); dfree(e.seps_d); dfree(e.sig_d);
     dfree(e.nl); dfree(e.nl_count); dfree(e.bonds); dfree(e.angles); dfree(e.partials); dfree(e.err);
-    dfree(e.tab_x); dfree(e.tab_y);
+    dfree(e.tab_x); dfree(e.tab_y); dfree(e.atm_acc);
     dfree(e.rdf); dfree(e.lj_hist); dfree(e.counts); dfree(h->f_scratch); dfree(h->acc); dfree(h->thermo_acc); dfree(e.offtab);
     dfree(e.nboff); dfree(e.rebuild); dfree(e.img); dfree(e.ref); dfree(e.slot_cell); dfree(e.vl); dfree(e.vl_count);
     dfree(e.rebuild_count); dfree(e.hdtm); dfree(e.exact_com);
@@ -580,6 +580,12 @@ int komd_gpu_upload_sites(komd_gpu *h, int64_t n, const double *r, const double 
     }
     int rc = alloc_atm_list(h, cap);
     if (rc) return rc;
+    dfree(e.atm_acc);
+    if ((e.cfg.terms & KOMD_TERM_ATM) && e.cfg.precision == KOMD_FP32 && e.cfg.atm_enum == KOMD_ATM_ENUM_FULL) {
+        // fixed-point force sums of the once-per-triplet kernel (kept at zero between launches)
+        CK(dalloc(e.atm_acc, 3 * (size_t)n));
+        CK(cudaMemset(e.atm_acc, 0, sizeof(unsigned long long) * 3 * n));
+    }
     if (e.verlet) {
         if (n > kMaxVerletSlot) return fail(KOMD_ERR_ARG, "the Verlet path supports at most 2^26 - 1 sites");
         const double vol = e.g.L[0] * e.g.L[1] * e.g.L[2];
@@ -1627,7 +1633,8 @@ int komd_gpu_kernels_per_step(komd_gpu *h) {
     if (e.cfg.terms & KOMD_TERM_LIMIT) k++;
     if (e.cfg.thermostat) k += 3;  /* kinetic sums, partial reduction, velocity scaling */
     if (surrogate_on(h)) k += 4;   /* descriptors, MLP, forces, apply */
-    else if (e.cfg.terms & KOMD_TERM_ATM) k++;
+    else if (e.cfg.terms & KOMD_TERM_ATM)   /* once-per-triplet kernel + flush in FP32 FULL mode */
+        k += (e.atm_acc != nullptr) ? 2 : 1;
     return k;
 }
 

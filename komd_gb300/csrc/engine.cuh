@@ -157,6 +157,7 @@ struct AtmParams {
     int virial_compat;         // weights and missing ZZ of ATM_Pressure
     int atm_direct;            // COMPAT + direct: no virial contribution
     double *e_site;            // measure: per-site V/3 sums (site order), optional
+    unsigned long long *acc;   // k_atm_s: 3 fixed-point force sums per slot (2^-32 units)
 };
 
 // TemperatureSensor's conversion (TemperatureSensor.cpp:44-47) in SciValue
@@ -253,6 +254,7 @@ struct Engine {
     bool uniform = false;
     float eps0 = 1.f, sig0 = 1.f;
     double lj_fscale = 1.0;         // ATM2B factor (KOMD_TERM_ATM2B), else 1
+    unsigned long long *atm_acc = nullptr;   // 3 per slot, fixed-point force sums of k_atm_s (zero between steps)
     // tabulated pair force (KOMD_TERM_TABULATED): F(r) piecewise linear on
     // ascending nodes tab_x, values tab_y, tab_lo below / tab_hi above the nodes
     double *tab_x = nullptr, *tab_y = nullptr;

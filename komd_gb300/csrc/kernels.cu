@@ -1216,6 +1216,192 @@ size_t atm_smem(const Engine &e) {
     return (size_t)kWarpsPerBlock * e.nl_cap * per;
 }
 
+// FP32 ATM, FULL triplet set, forces only: every triplet once, from its
+// lowest slot i (the other two members are neighbours of i with larger
+// slots).  One warp per vertex; lane a owns staged neighbour a (a < m, the
+// neighbours above i) and evaluates the round-robin pairs (a, a+d mod m),
+// d = 1 .. m/2, directly.  Per triplet with A = |e_a|^2, B = |e_b|^2,
+// C = |e_b - e_a|^2 (e = r_i - r_x) and v_X = dV/dX / nu, the forces in units
+// of 2 sign nu are
+//   g_i = vA e_a + vB e_b,  g_a = -vA e_a + vC (e_b - e_a),  g_b = -vB e_b - vC (e_b - e_a).
+// g_i and g_a stay in the lane's registers; g_b reaches lane b by one warp
+// shuffle per component (lane r pulls from lane r - d mod m).  At the end the
+// per-neighbour and per-vertex sums go to 64-bit fixed-point accumulators by
+// integer atomics (order-independent: the forces are bitwise reproducible);
+// k_atm_flush adds them to f.
+constexpr double kAtmFix = 4294967296.0;   // 2^32 fixed-point units
+
+__device__ __forceinline__ void atm_fix_add(unsigned long long *acc, float x) {
+    // x * 2^32 is exact in FP32 (a power-of-two scale); one FP32 -> int64 conversion
+    const long long q = __float2ll_rn(x * 4294967296.0f);
+    if (q != 0) atomicAdd(acc, (unsigned long long)q);
+}
+
+struct AtmV {
+    float vA, vB, vC;
+};
+// dV/dA, dV/dB, dV/dC over nu from the squared sides and the staged (A, 1/A, 1/sqrt(A))
+__device__ __forceinline__ AtmV atm_derivs(float4 qa, float4 qb, float C) {
+    const float A = qa.x, B = qb.x;
+    const float wc = rsqrtf(C);
+    const float sv = qa.z * qb.z * wc;                  // 1/(abc)
+    const float s2 = sv * sv;
+    const float s5 = s2 * s2 * sv;
+    const float t1 = A + B - C, t2 = A - B + C, t3 = B + C - A;
+    const float u = t2 * t3, v = t1 * t3, w = t1 * t2;
+    const float P = t1 * u;
+    AtmV r;
+    r.vA = s5 * (-1.5f * B * C + 0.375f * (u + v - w) - 0.9375f * P * qa.y);
+    r.vB = s5 * (-1.5f * A * C + 0.375f * (u - v + w) - 0.9375f * P * qb.y);
+    r.vC = s5 * (-1.5f * A * B + 0.375f * (-u + v + w) - 0.9375f * P * (wc * wc));
+    return r;
+}
+
+// stage vertex i's neighbours above i (ballot compaction); returns their count
+__device__ __forceinline__ int atm_stage(const AtmParams &p, int i, float4 *se, float4 *sq, int lane, unsigned lt) {
+    const int ni = min(p.nl_count[i], p.nl_cap);
+    int m = 0;
+    for (int k0 = 0; k0 < ni; k0 += 32) {
+        const int k = k0 + lane;
+        float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
+        bool up = false;
+        if (k < ni) {
+            e = p.nl[(size_t)i * p.nl_cap + k];
+            up = (__float_as_int(e.w) >> 6) > i;
+        }
+        const unsigned bm = __ballot_sync(0xffffffffu, up);
+        if (up) {
+            const int pos = m + __popc(bm & lt);
+            const float A = e.x * e.x + e.y * e.y + e.z * e.z;
+            se[pos] = e;
+            sq[pos] = make_float4(A, 1.0f / A, rsqrtf(A), 0.f);
+        }
+        m += __popc(bm);
+    }
+    return m;
+}
+
+// the round-robin sweep of one vertex over the lanes of a warp from base gb:
+// lane li = lane - gb owns staged neighbour li < m; rounds d = 1 .. dmax
+// (m/2 <= dmax <= m; rounds past m/2 do nothing)
+__device__ __forceinline__ void atm_sweep(const AtmParams &p, const float4 *se, const float4 *sq, int m, int li,
+                                          int gb, int dmax, float rc2, float &gx, float &gy, float &gz) {
+    const bool own = li < m;
+    const float4 ea = own ? se[li] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 qa = own ? sq[li] : make_float4(1.f, 1.f, 1.f, 0.f);
+    float ax = 0.f, ay = 0.f, az = 0.f;    // neighbour li
+    const int half = m / 2;
+    for (int d = 1; d <= dmax; d++) {
+        float bx = 0.f, by = 0.f, bz = 0.f;
+        if (own && d <= half && !(2 * d == m && li >= d)) {
+            int b = li + d;
+            if (b >= m) b -= m;
+            const float4 eb = se[b];
+            const float cx = eb.x - ea.x, cy = eb.y - ea.y, cz = eb.z - ea.z;
+            const float C = cx * cx + cy * cy + cz * cz;
+            if (C <= rc2) {
+                const AtmV t = atm_derivs(qa, sq[b], C);
+                gx += t.vA * ea.x + t.vB * eb.x;
+                gy += t.vA * ea.y + t.vB * eb.y;
+                gz += t.vA * ea.z + t.vB * eb.z;
+                ax += t.vC * cx - t.vA * ea.x;
+                ay += t.vC * cy - t.vA * ea.y;
+                az += t.vC * cz - t.vA * ea.z;
+                bx = -t.vC * cx - t.vB * eb.x;
+                by = -t.vC * cy - t.vB * eb.y;
+                bz = -t.vC * cz - t.vB * eb.z;
+            }
+        }
+        // lane li pulls the share computed by the lane whose partner it was
+        int src = li;               // lanes without an entry pull from themselves
+        if (own) {
+            src = li - d;           // d <= dmax <= m: one wrap at most
+            if (src < 0) src += m;
+        }
+        src += gb;
+        const float rx = __shfl_sync(0xffffffffu, bx, src);
+        const float ry = __shfl_sync(0xffffffffu, by, src);
+        const float rz = __shfl_sync(0xffffffffu, bz, src);
+        if (own && d <= half) { ax += rx; ay += ry; az += rz; }
+    }
+    if (own) {
+        unsigned long long *acc = p.acc + 3 * (size_t)(__float_as_int(ea.w) >> 6);
+        atm_fix_add(acc, ax);
+        atm_fix_add(acc + 1, ay);
+        atm_fix_add(acc + 2, az);
+    }
+}
+
+// vertices with more than 32 neighbours above them: a plain pair loop with a
+// fixed-point atomic per contribution (rare at liquid densities)
+__device__ void atm_pairs_slow(const AtmParams &p, const float4 *se, const float4 *sq, int m, int lane, float rc2,
+                               float &gx, float &gy, float &gz) {
+    for (int a = lane; a < m; a += 32) {
+        const float4 ea = se[a], qa = sq[a];
+        unsigned long long *acca = p.acc + 3 * (size_t)(__float_as_int(ea.w) >> 6);
+        for (int b = a + 1; b < m; b++) {
+            const float4 eb = se[b];
+            const float cx = eb.x - ea.x, cy = eb.y - ea.y, cz = eb.z - ea.z;
+            const float C = cx * cx + cy * cy + cz * cz;
+            if (C > rc2) continue;
+            const AtmV t = atm_derivs(qa, sq[b], C);
+            gx += t.vA * ea.x + t.vB * eb.x;
+            gy += t.vA * ea.y + t.vB * eb.y;
+            gz += t.vA * ea.z + t.vB * eb.z;
+            unsigned long long *accb = p.acc + 3 * (size_t)(__float_as_int(eb.w) >> 6);
+            atm_fix_add(acca, t.vC * cx - t.vA * ea.x);
+            atm_fix_add(acca + 1, t.vC * cy - t.vA * ea.y);
+            atm_fix_add(acca + 2, t.vC * cz - t.vA * ea.z);
+            atm_fix_add(accb, -t.vC * cx - t.vB * eb.x);
+            atm_fix_add(accb + 1, -t.vC * cy - t.vB * eb.y);
+            atm_fix_add(accb + 2, -t.vC * cz - t.vB * eb.z);
+        }
+    }
+}
+
+__device__ __forceinline__ void atm_vertex_out(const AtmParams &p, int i, float gx, float gy, float gz) {
+    atm_fix_add(p.acc + 3 * (size_t)i, gx);
+    atm_fix_add(p.acc + 3 * (size_t)i + 1, gy);
+    atm_fix_add(p.acc + 3 * (size_t)i + 2, gz);
+}
+
+// one warp per vertex
+__global__ void __launch_bounds__(kBlock) k_atm_s(AtmParams p) {
+    extern __shared__ float4 s_dyn[];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int cap = p.nl_cap;
+    float4 *se = s_dyn + wib * 2 * cap, *sq = se + cap;
+    const int i = blockIdx.x * kWarpsPerBlock + wib;
+    if (i >= p.n) return;
+    const float rc2 = (float)p.rc2;
+    unsigned lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+    const int m = atm_stage(p, i, se, sq, lane, lt);
+    __syncwarp();
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+    if (m <= 32) atm_sweep(p, se, sq, m, lane, 0, m / 2, rc2, gx, gy, gz);
+    else atm_pairs_slow(p, se, sq, m, lane, rc2, gx, gy, gz);
+    for (int o = 16; o > 0; o >>= 1) {
+        gx += __shfl_xor_sync(0xffffffffu, gx, o);
+        gy += __shfl_xor_sync(0xffffffffu, gy, o);
+        gz += __shfl_xor_sync(0xffffffffu, gz, o);
+    }
+    if (lane == 0) atm_vertex_out(p, i, gx, gy, gz);
+}
+
+// f[site] += 2 sign nu g (fixed point -> FP64) and the accumulators back to 0
+__global__ void k_atm_flush(int n, const int *__restrict__ slot_site, unsigned long long *acc, double *f,
+                            double scale) {
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= n) return;
+    const int site = slot_site[slot];
+    for (int d = 0; d < 3; d++) {
+        const long long q = (long long)acc[3 * slot + d];
+        acc[3 * slot + d] = 0ull;
+        f[3 * site + d] += scale * ((double)q * (1.0 / kAtmFix));
+    }
+}
+
 template <typename Real>
 static void atm_dispatch(AtmParams &p, bool measure, bool compat, int grid, size_t sm, cudaStream_t st) {
     if (measure) {
@@ -1253,7 +1439,14 @@ void launch_atm(Engine &e, cudaStream_t st, bool measure) {
     p.virial_compat = e.cfg.virial_mode == KOMD_VIRIAL_COMPAT;
     p.atm_direct = e.cfg.atm_direct;
     p.e_site = e.atm_esite;
+    p.acc = e.atm_acc;
     const bool compat = e.cfg.atm_enum == KOMD_ATM_ENUM_COMPAT;
+    if (!measure && !compat && e.cfg.precision == KOMD_FP32 && e.atm_acc) {
+        // every triplet once (lowest slot), fixed-point scatter, then the flush into f
+        k_atm_s<<<atm_grid(e), kBlock, atm_smem(e), st>>>(p);
+        k_atm_flush<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.slot_site, e.atm_acc, e.f, 2.0 * p.sign * p.nu);
+        return;
+    }
     if (e.cfg.precision == KOMD_FP64) atm_dispatch<double>(p, measure, compat, atm_grid(e), atm_smem(e), st);
     else atm_dispatch<float>(p, measure, compat, atm_grid(e), atm_smem(e), st);
 }
@@ -1306,6 +1499,7 @@ void launch_rdf_bins(Engine &e, cudaStream_t st, double *bins, bool cells, doubl
 
 void set_kernel_attributes(Engine &e) {
     const int sm = (int)atm_smem(e);
+    if (sm > 48 * 1024) cudaFuncSetAttribute(k_atm_s, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     if (sm > 48 * 1024) {
         cudaFuncSetAttribute(k_atm_q<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
         cudaFuncSetAttribute(k_atm_q<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);

@@ -418,7 +418,7 @@ __global__ void __launch_bounds__(256, 5) k_lj_vlist(PairParams p, int n) {
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 const int k = k0 + u * 32 + lane;
-                e[u] = k < p.vl_cap ? row[k] : 0xffffffffu;
+                e[u] = k < p.vl_cap ? __ldcs(row + k) : 0xffffffffu;   // read once per step: evict first
             }
 #pragma unroll
             for (int u = 0; u < U; u++)
