@@ -1281,54 +1281,51 @@ __device__ __forceinline__ int atm_stage(const AtmParams &p, int i, float4 *se, 
     return m;
 }
 
-// the round-robin sweep of one vertex over the lanes of a warp from base gb:
-// lane li = lane - gb owns staged neighbour li < m; rounds d = 1 .. dmax
-// (m/2 <= dmax <= m; rounds past m/2 do nothing)
-__device__ __forceinline__ void atm_sweep(const AtmParams &p, const float4 *se, const float4 *sq, int m, int li,
-                                          int gb, int dmax, float rc2, float &gx, float &gy, float &gz) {
+// the round-robin sweep of one vertex: lane li = lane - gb owns staged
+// neighbour li < m and plays rounds d = d_first .. d_last (at most m/2) over
+// `rounds` loop trips (rounds past d_last do nothing); the lane's partial sum
+// for its neighbour is returned in (ax, ay, az)
+__device__ __forceinline__ void atm_sweep(const float4 *se, const float4 *sq, int m, int li, int gb, int d_first,
+                                          int d_last, int rounds, float rc2, float &gx, float &gy, float &gz,
+                                          float &ax, float &ay, float &az, float4 &ea_out) {
     const bool own = li < m;
     const float4 ea = own ? se[li] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 qa = own ? sq[li] : make_float4(1.f, 1.f, 1.f, 0.f);
-    float ax = 0.f, ay = 0.f, az = 0.f;    // neighbour li
-    const int half = m / 2;
-    for (int d = 1; d <= dmax; d++) {
+    ea_out = ea;
+    for (int t = 0; t < rounds; t++) {
+        const int d = d_first + t;
+        const bool act = own && d <= d_last;
         float bx = 0.f, by = 0.f, bz = 0.f;
-        if (own && d <= half && !(2 * d == m && li >= d)) {
+        if (act && !(2 * d == m && li >= d)) {
             int b = li + d;
             if (b >= m) b -= m;
             const float4 eb = se[b];
             const float cx = eb.x - ea.x, cy = eb.y - ea.y, cz = eb.z - ea.z;
             const float C = cx * cx + cy * cy + cz * cz;
             if (C <= rc2) {
-                const AtmV t = atm_derivs(qa, sq[b], C);
-                gx += t.vA * ea.x + t.vB * eb.x;
-                gy += t.vA * ea.y + t.vB * eb.y;
-                gz += t.vA * ea.z + t.vB * eb.z;
-                ax += t.vC * cx - t.vA * ea.x;
-                ay += t.vC * cy - t.vA * ea.y;
-                az += t.vC * cz - t.vA * ea.z;
-                bx = -t.vC * cx - t.vB * eb.x;
-                by = -t.vC * cy - t.vB * eb.y;
-                bz = -t.vC * cz - t.vB * eb.z;
+                const AtmV v = atm_derivs(qa, sq[b], C);
+                gx += v.vA * ea.x + v.vB * eb.x;
+                gy += v.vA * ea.y + v.vB * eb.y;
+                gz += v.vA * ea.z + v.vB * eb.z;
+                ax += v.vC * cx - v.vA * ea.x;
+                ay += v.vC * cy - v.vA * ea.y;
+                az += v.vC * cz - v.vA * ea.z;
+                bx = -v.vC * cx - v.vB * eb.x;
+                by = -v.vC * cy - v.vB * eb.y;
+                bz = -v.vC * cz - v.vB * eb.z;
             }
         }
-        // lane li pulls the share computed by the lane whose partner it was
-        int src = li;               // lanes without an entry pull from themselves
-        if (own) {
-            src = li - d;           // d <= dmax <= m: one wrap at most
+        // lane li pulls the share computed, in this lane group, by the lane whose partner it was
+        int src = li;               // lanes without a round pull from themselves
+        if (act) {
+            src = li - d;           // d <= m/2: one wrap at most
             if (src < 0) src += m;
         }
         src += gb;
         const float rx = __shfl_sync(0xffffffffu, bx, src);
         const float ry = __shfl_sync(0xffffffffu, by, src);
         const float rz = __shfl_sync(0xffffffffu, bz, src);
-        if (own && d <= half) { ax += rx; ay += ry; az += rz; }
-    }
-    if (own) {
-        unsigned long long *acc = p.acc + 3 * (size_t)(__float_as_int(ea.w) >> 6);
-        atm_fix_add(acc, ax);
-        atm_fix_add(acc + 1, ay);
-        atm_fix_add(acc + 2, az);
+        if (act) { ax += rx; ay += ry; az += rz; }
     }
 }
 
@@ -1365,7 +1362,9 @@ __device__ __forceinline__ void atm_vertex_out(const AtmParams &p, int i, float 
     atm_fix_add(p.acc + 3 * (size_t)i + 2, gz);
 }
 
-// one warp per vertex
+// one warp per vertex; with at most 16 neighbours above the vertex the two
+// half-warps split the rounds (lower and upper half of d), each delivering
+// shares within itself, and their partial sums per neighbour are added
 __global__ void __launch_bounds__(kBlock) k_atm_s(AtmParams p) {
     extern __shared__ float4 s_dyn[];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1379,8 +1378,36 @@ __global__ void __launch_bounds__(kBlock) k_atm_s(AtmParams p) {
     const int m = atm_stage(p, i, se, sq, lane, lt);
     __syncwarp();
     float gx = 0.f, gy = 0.f, gz = 0.f;
-    if (m <= 32) atm_sweep(p, se, sq, m, lane, 0, m / 2, rc2, gx, gy, gz);
-    else atm_pairs_slow(p, se, sq, m, lane, rc2, gx, gy, gz);
+    const int half = m / 2;
+    if (m <= 32) {
+        float ax = 0.f, ay = 0.f, az = 0.f;
+        float4 ea;
+        if (m <= 16) {
+            const int g = lane >> 4, li = lane & 15;
+            const int h1 = (half + 1) / 2;                     // rounds of the lower half-warp
+            const int d_first = g ? h1 + 1 : 1, d_last = g ? half : h1;
+            atm_sweep(se, sq, m, li, 16 * g, d_first, d_last, h1, rc2, gx, gy, gz, ax, ay, az, ea);
+            ax += __shfl_xor_sync(0xffffffffu, ax, 16);
+            ay += __shfl_xor_sync(0xffffffffu, ay, 16);
+            az += __shfl_xor_sync(0xffffffffu, az, 16);
+            if (lane < m) {
+                unsigned long long *acc = p.acc + 3 * (size_t)(__float_as_int(ea.w) >> 6);
+                atm_fix_add(acc, ax);
+                atm_fix_add(acc + 1, ay);
+                atm_fix_add(acc + 2, az);
+            }
+        } else {
+            atm_sweep(se, sq, m, lane, 0, 1, half, half, rc2, gx, gy, gz, ax, ay, az, ea);
+            if (lane < m) {
+                unsigned long long *acc = p.acc + 3 * (size_t)(__float_as_int(ea.w) >> 6);
+                atm_fix_add(acc, ax);
+                atm_fix_add(acc + 1, ay);
+                atm_fix_add(acc + 2, az);
+            }
+        }
+    } else {
+        atm_pairs_slow(p, se, sq, m, lane, rc2, gx, gy, gz);
+    }
     for (int o = 16; o > 0; o >>= 1) {
         gx += __shfl_xor_sync(0xffffffffu, gx, o);
         gy += __shfl_xor_sync(0xffffffffu, gy, o);
