@@ -191,9 +191,11 @@ void enqueue_surrogate(komd_gpu *h, double *fout) {
 
 // the force sequence of Simulation::run: 2-body functors (LJ / FENE, bonded,
 // Limit), then the 3-body functor (ATM, exact or learned)
-void enqueue_forces(komd_gpu *h, bool measure, double *lj_hist) {
+// returns true when integrate1 was fused into the last force kernel (with_step1)
+bool enqueue_forces(komd_gpu *h, bool measure, double *lj_hist, bool with_step1 = false) {
     Engine &e = h->e;
     cudaStream_t st = e.stream;
+    bool fused = false;
     int pair_blocks;
     {
         ProfScope ps(h, F_PAIR);
@@ -221,24 +223,25 @@ void enqueue_forces(komd_gpu *h, bool measure, double *lj_hist) {
     } else if (e.cfg.terms & KOMD_TERM_ATM) {
         {
             ProfScope ps(h, F_ATM);
-            launch_atm(e, st, measure);
+            fused = launch_atm(e, st, measure, with_step1);
         }
         if (measure) launch_sum_partials(st, atm_grid(e), e.partials, h->acc);
     }
+    return fused;
 }
 
 void enqueue_step(komd_gpu *h) {
     Engine &e = h->e;
     {
         ProfScope ps(h, F_INTEGRATE);
-        launch_step0(e, e.stream);
+        launch_step0(e, e.stream, true);
     }
     {
         ProfScope ps(h, F_CONTAINER);
         launch_container(e, e.stream);
     }
-    enqueue_forces(h, false, nullptr);
-    {
+    // the step's integrate1 rides on the ATM flush when the once-per-triplet path runs
+    if (!enqueue_forces(h, false, nullptr, true)) {
         ProfScope ps(h, F_INTEGRATE);
         launch_step1(e, e.stream);
     }
@@ -557,6 +560,8 @@ int komd_gpu_upload_sites(komd_gpu *h, int64_t n, const double *r, const double 
         CK(dalloc(e.exact_com, e.n_mol));
         CK(cudaMemcpy(e.hdtm, hdtm.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(e.exact_com, exact.data(), e.n_mol, cudaMemcpyHostToDevice));
+        e.fused_drift = e.verlet && e.n_mol == n;
+        for (int64_t k = 0; k < e.n_mol && e.fused_drift; k++) e.fused_drift = exact[k] != 0;
         e.uniform = true;
         for (int64_t s = 1; s < n && e.uniform; s++) e.uniform = eps[s] == eps[0] && sig[s] == sig[0];
         e.eps0 = (float)eps[0];
@@ -1627,7 +1632,8 @@ int komd_gpu_kernels_per_step(komd_gpu *h) {
     if (!h) return -1;
     const Engine &e = h->e;
     int k = 2 /* integrate */ + 4 /* com/wrap/bin, scan, scatter, cell sort */ + 1 /* pair */;
-    if (e.verlet) k += 2;   /* refresh, list build (each exits at once when its step does not need it) */
+    if (!surrogate_on(h) && (e.cfg.terms & KOMD_TERM_ATM) && e.atm_acc) k--;   /* integrate1 fused into the ATM flush */
+    if (e.verlet) k += e.fused_drift ? 1 : 2;   /* (refresh,) list build; the fused drift does the refresh */
     if ((e.cfg.terms & KOMD_TERM_BONDED) && e.n_bonds > 0) k++;
     if ((e.cfg.terms & KOMD_TERM_BONDED) && e.n_angles > 0) k++;
     if (e.cfg.terms & KOMD_TERM_LIMIT) k++;

@@ -254,6 +254,7 @@ struct Engine {
     bool uniform = false;
     float eps0 = 1.f, sig0 = 1.f;
     double lj_fscale = 1.0;         // ATM2B factor (KOMD_TERM_ATM2B), else 1
+    bool fused_drift = false;       // Verlet path, single-site molecules with exact COM: k_step0_fused
     unsigned long long *atm_acc = nullptr;   // 3 per slot, fixed-point force sums of k_atm_s (zero between steps)
     // tabulated pair force (KOMD_TERM_TABULATED): F(r) piecewise linear on
     // ascending nodes tab_x, values tab_y, tab_lo below / tab_hi above the nodes

@@ -22,9 +22,10 @@ __global__ void k_com_wrap_bin(Grid g, int n_mol, const int *__restrict__ mol_of
                                const double *__restrict__ m, double *__restrict__ com, int *__restrict__ mol_cell,
                                int *__restrict__ mol_rank, int *__restrict__ cell_count, int *__restrict__ cell_mcount,
                                char4 *__restrict__ img, const int *__restrict__ rebuild,
-                               const unsigned char *__restrict__ exact_com) {
+                               const unsigned char *__restrict__ exact_com, int wrapped) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n_mol) return;
+    if (wrapped && rebuild && !*rebuild) return;   // k_step0_fused wrapped this step; no rebuild
     const int s0 = mol_off[k], s1 = mol_off[k + 1];
     // com += r * m ; M += m ; com /= M   (updateCOM, no FMA).  For a single
     // site of power-of-two mass the scaling is exact and the result is r
@@ -866,6 +867,63 @@ __global__ void k_step0(int n, double *__restrict__ r, double *__restrict__ v, c
     }
 }
 
+// Verlet path with single-site molecules whose COM is exactly the position
+// (power-of-two masses): integrate0, the skin test, the periodic wrap with
+// its image counters and COM (k_com_wrap_bin's operations) and the FP32
+// cell-local refresh (k_refresh's) in one pass over the sites.  The
+// results are those of the separate kernels; on a rebuild step the cell sort
+// rewrites pos4 afterwards.
+__global__ void k_step0_fused(int n, double *__restrict__ r, double *__restrict__ v, const double *__restrict__ f,
+                              const double *__restrict__ hdtm, double dt, Grid g, char4 *__restrict__ img,
+                              const double *__restrict__ ref, float half_skin2, int *__restrict__ rebuild,
+                              double *__restrict__ com, const int *__restrict__ site_slot,
+                              const int *__restrict__ slot_cell, float4 *__restrict__ pos4) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const double c = hdtm[s];
+    double x[3];
+    for (int d = 0; d < 3; d++) {
+        const double vv = dadd(v[3 * s + d], dmul(f[3 * s + d], c));
+        v[3 * s + d] = vv;
+        x[d] = dadd(r[3 * s + d], dmul(vv, dt));
+    }
+    char4 q = img[s];
+    {
+        const float dx = (float)(x[0] - ref[3 * s]) - (float)q.x * (float)g.L[0];
+        const float dy = (float)(x[1] - ref[3 * s + 1]) - (float)q.y * (float)g.L[1];
+        const float dz = (float)(x[2] - ref[3 * s + 2]) - (float)q.z * (float)g.L[2];
+        if (dx * dx + dy * dy + dz * dz > half_skin2) *rebuild = 1;
+    }
+    // Periodic_Kernel on the COM (= the position): strict comparisons
+    double off[3];
+    bool moved = false;
+    for (int d = 0; d < 3; d++) {
+        off[d] = 0.0;
+        if (x[d] < g.low[d]) off[d] = g.L[d];
+        if (x[d] > g.high[d]) off[d] = -g.L[d];
+        moved |= (off[d] != 0.0);
+    }
+    if (moved) {
+        for (int d = 0; d < 3; d++) x[d] = dadd(x[d], off[d]);
+        q.x += (off[0] > 0.0) - (off[0] < 0.0);
+        q.y += (off[1] > 0.0) - (off[1] < 0.0);
+        q.z += (off[2] > 0.0) - (off[2] < 0.0);
+        img[s] = q;
+    }
+    for (int d = 0; d < 3; d++) {
+        r[3 * s + d] = x[d];
+        com[3 * s + d] = x[d];
+    }
+    const int slot = site_slot[s];
+    int cx, cy, cz;
+    cell_coords(g, slot_cell[slot], cx, cy, cz);
+    float4 p = pos4[slot];
+    p.x = (float)((x[0] - (double)q.x * g.L[0]) - cell_centre(g, 0, cx));
+    p.y = (float)((x[1] - (double)q.y * g.L[1]) - cell_centre(g, 1, cy));
+    p.z = (float)((x[2] - (double)q.z * g.L[2]) - cell_centre(g, 2, cz));
+    pos4[slot] = p;
+}
+
 __global__ void k_step1(int n, double *__restrict__ v, const double *__restrict__ f, const double *__restrict__ hdtm,
                         int *err, int *rebuild) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1087,7 +1145,8 @@ void launch_container(Engine &e, cudaStream_t st) {
     cudaMemsetAsync(e.cell_mcount, 0, sizeof(int) * g.ncell, st);
     k_com_wrap_bin<<<nblk(e.n_mol, 256), 256, 0, st>>>(g, (int)e.n_mol, e.mol_off, e.r, e.m, e.com, e.mol_cell,
                                                          e.mol_rank, e.cell_count, e.cell_mcount,
-                                                         e.verlet ? e.img : nullptr, rb, e.exact_com);
+                                                         e.verlet ? e.img : nullptr, rb, e.exact_com,
+                                                         e.fused_drift ? 1 : 0);
     k_scan2<<<1, 1024, 0, st>>>(g.ncell, e.cell_count, e.cell_start, e.cell_mcount, e.cell_mstart, rb);
     k_scatter_mol<<<nblk(e.n_mol, 256), 256, 0, st>>>((int)e.n_mol, e.mol_cell, e.mol_rank, e.cell_mstart,
                                                         e.cell_mols, rb);
@@ -1096,7 +1155,9 @@ void launch_container(Engine &e, cudaStream_t st) {
         e.pos4, e.skey, e.seps, e.posd, e.seps_d, e.sig_d, e.verlet ? e.img : nullptr, e.verlet ? e.ref : nullptr,
         e.verlet ? e.slot_cell : nullptr, rb);
     if (e.verlet) {
-        k_refresh<<<nblk(e.n, 256), 256, 0, st>>>(g, (int)e.n, e.slot_site, e.slot_cell, e.r, e.img, e.pos4, e.rebuild);
+        if (!e.fused_drift)
+            k_refresh<<<nblk(e.n, 256), 256, 0, st>>>(g, (int)e.n, e.slot_site, e.slot_cell, e.r, e.img, e.pos4,
+                                                        e.rebuild);
         launch_vlist_build(e, st);
     }
 }
@@ -1416,6 +1477,30 @@ __global__ void __launch_bounds__(kBlock) k_atm_s(AtmParams p) {
     if (lane == 0) atm_vertex_out(p, i, gx, gy, gz);
 }
 
+// the same flush fused with Integrator::integrate1 of the step (ATM is the
+// last force term): f[site] += ..., then v[site] += f[site] * dt/(2m) with
+// k_step1's operations, its non-finite check and the rebuild-flag reset
+__global__ void k_atm_flush_step1(int n, const int *__restrict__ slot_site, unsigned long long *acc, double *f,
+                                  double scale, double *__restrict__ v, const double *__restrict__ hdtm, int *err,
+                                  int *rebuild) {
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (rebuild && slot == 0) *rebuild = 0;   // every consumer of this step's flag has run
+    if (slot >= n) return;
+    const int site = slot_site[slot];
+    const double c = hdtm[site];
+    bool bad = false;
+    for (int d = 0; d < 3; d++) {
+        const long long q = (long long)acc[3 * slot + d];
+        acc[3 * slot + d] = 0ull;
+        const double fd = f[3 * site + d] + scale * ((double)q * (1.0 / kAtmFix));
+        f[3 * site + d] = fd;
+        const double vv = dadd(v[3 * site + d], dmul(fd, c));
+        v[3 * site + d] = vv;
+        bad |= !isfinite(vv);
+    }
+    if (bad) atomicOr(&err[E_NONFINITE], 1);
+}
+
 // f[site] += 2 sign nu g (fixed point -> FP64) and the accumulators back to 0
 __global__ void k_atm_flush(int n, const int *__restrict__ slot_site, unsigned long long *acc, double *f,
                             double scale) {
@@ -1451,7 +1536,7 @@ void atm_dispatch<float>(AtmParams &p, bool measure, bool compat, int grid, size
     }
 }
 
-void launch_atm(Engine &e, cudaStream_t st, bool measure) {
+bool launch_atm(Engine &e, cudaStream_t st, bool measure, bool with_step1) {
     AtmParams p;
     p.n = (int)e.n;
     p.slot_site = e.slot_site;
@@ -1471,15 +1556,28 @@ void launch_atm(Engine &e, cudaStream_t st, bool measure) {
     if (!measure && !compat && e.cfg.precision == KOMD_FP32 && e.atm_acc) {
         // every triplet once (lowest slot), fixed-point scatter, then the flush into f
         k_atm_s<<<atm_grid(e), kBlock, atm_smem(e), st>>>(p);
+        if (with_step1) {
+            k_atm_flush_step1<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.slot_site, e.atm_acc, e.f,
+                                                                2.0 * p.sign * p.nu, e.v, e.hdtm, e.err,
+                                                                e.verlet ? e.rebuild : nullptr);
+            return true;
+        }
         k_atm_flush<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.slot_site, e.atm_acc, e.f, 2.0 * p.sign * p.nu);
-        return;
+        return false;
     }
     if (e.cfg.precision == KOMD_FP64) atm_dispatch<double>(p, measure, compat, atm_grid(e), atm_smem(e), st);
     else atm_dispatch<float>(p, measure, compat, atm_grid(e), atm_smem(e), st);
+    return false;
 }
 
-void launch_step0(Engine &e, cudaStream_t st) {
+void launch_step0(Engine &e, cudaStream_t st, bool in_step) {
     const float hs = (float)(0.5 * e.cfg.skin);
+    if (in_step && e.fused_drift) {
+        k_step0_fused<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.r, e.v, e.f, e.hdtm, e.cfg.delta_t, e.g, e.img,
+                                                       e.ref, hs * hs, e.rebuild, e.com, e.site_slot, e.slot_cell,
+                                                       e.pos4);
+        return;
+    }
     k_step0<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.r, e.v, e.f, e.hdtm, e.cfg.delta_t, e.g,
                                               e.verlet ? e.img : nullptr, e.verlet ? e.ref : nullptr, hs * hs,
                                               e.rebuild);

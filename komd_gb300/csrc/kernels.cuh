@@ -13,8 +13,11 @@ int vlist_grid(const Engine &e);
 void launch_counts(Engine &e, cudaStream_t st);
 void launch_bonded(Engine &e, cudaStream_t st, bool measure, double *acc);
 void launch_limit(Engine &e, cudaStream_t st);
-void launch_atm(Engine &e, cudaStream_t st, bool measure);
-void launch_step0(Engine &e, cudaStream_t st);
+// ATM forces; with_step1 (step graphs only) lets the FULL FP32 path fuse
+// integrate1 into its flush: returns true when it did
+bool launch_atm(Engine &e, cudaStream_t st, bool measure, bool with_step1 = false);
+// in_step (step graphs only): the fused drift path when the engine qualifies
+void launch_step0(Engine &e, cudaStream_t st, bool in_step = false);
 void launch_step1(Engine &e, cudaStream_t st);
 void launch_kinetic(Engine &e, cudaStream_t st, int n_terms);
 void launch_velocity_scale(Engine &e, cudaStream_t st, const double *acc, double beta);
