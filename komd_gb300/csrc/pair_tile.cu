@@ -413,12 +413,13 @@ __global__ void __launch_bounds__(256, 5) k_lj_vlist(PairParams p, int n) {
             unsigned e[U];
             float4 o[U], pj[U];
             float sej[U];
-            // rows hold vl_cap entries: load speculatively up to the capacity so the
-            // row load does not wait for the count, then mask
+            // rows hold vl_cap entries: the first pass loads speculatively up to the
+            // capacity so that it does not wait for the count; later passes stop at it
+            const int lim = k0 == 0 ? p.vl_cap : cnt;
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 const int k = k0 + u * 32 + lane;
-                e[u] = k < p.vl_cap ? __ldcs(row + k) : 0xffffffffu;   // read once per step: evict first
+                e[u] = k < lim ? __ldcs(row + k) : 0xffffffffu;   // read once per step: evict first
             }
 #pragma unroll
             for (int u = 0; u < U; u++)
