@@ -211,6 +211,80 @@ void GpuPressureSensor::write(uint64_t simstep) {
     }
 }
 
+void GpuViscositySensor::measure() {
+    komd_observables o{};
+    gpu_check(komd_gpu_measure(engine(), KOMD_MEASURE_PRESSURE, &o, nullptr, nullptr));
+    const double vol = volume();
+    for (int k = 0; k < 6; k++) series_[k].push_back(o.pressure[k] / vol);   // TensorEvaluator::eval
+}
+
+double GpuViscositySensor::integrate(const std::vector<std::vector<double>> &series, const int *dims, int ndims,
+                                     double dt, bool origin_free) {
+    // TensorEvaluator::integrate (ViscositySensor.cpp:118-149): per component the
+    // autocorrelation c(k) = mean over origins of (p(t) - s)(p(t + k) - s), with
+    // s the mean of p when origin_free, then (c(0) + c(n-1) + sum of the inner
+    // c(k)) * dt / 2, and the mean over the components
+    double sum = 0.0;
+    for (int q = 0; q < ndims; q++) {
+        const std::vector<double> &p = series[dims[q]];
+        const int n = (int)p.size();
+        if (n == 0) continue;
+        double shift = 0.0;
+        if (origin_free) {
+            for (double x : p) shift += x;
+            shift /= n;
+        }
+        std::vector<double> c(n, 0.0);
+        for (int k = 0; k < n; k++) {
+            double t = 0.0;
+            for (int o = 0; o < n - k; o++) t += (p[o] - shift) * (p[o + k] - shift);
+            c[k] = t / (n - k);
+        }
+        double integral = c[0] + c[n - 1];
+        for (int k = 1; k < n - 1; k++) integral += c[k];
+        sum += integral * (dt / 2.0);
+    }
+    return sum / ndims;
+}
+
+namespace {
+// SciValue (math/SciValue.{h,cpp}): mantissa normalised into (0.1, 10) by /10
+// and *10 steps, products renormalised, converted as m * pow(10, e)
+struct Sci {
+    double m;
+    long long e;
+    Sci(double mm, long long ee) : m(mm), e(ee) { norm(); }
+    explicit Sci(double v) : m(v), e(0) { if (v != 0.0) norm(); }
+    void norm() {
+        double a = std::fabs(m);
+        while (a >= 10.0) { m /= 10.0; e += 1; a = std::fabs(m); }
+        while (a <= 0.1) { m *= 10.0; e -= 1; a = std::fabs(m); }
+    }
+    Sci operator*(const Sci &o) const { return Sci(m * o.m, e + o.e); }
+    Sci operator/(const Sci &o) const { return Sci(m / o.m, e - o.e); }
+    Sci operator*(double o) const { return *this * Sci(o); }
+    double value() const { return m * std::pow(10, e); }
+};
+}  // namespace
+
+void GpuViscositySensor::write(uint64_t simstep) {
+    // ViscositySensor::write (ViscositySensor.cpp:37-89): factor =
+    // (Da_kg^2 * A_m / ps_s^3) * (V / (kB * T)) in SciValue arithmetic
+    const auto cfg = Registry::instance->configuration();
+    const Sci da(1.66053906892, -27), a_m(1.0, -10), ps_s(1.0, -12), kB(1.380649, -23);
+    const Sci conv = (da * da * a_m) / (ps_s * ps_s * ps_s);
+    const double V = volume();
+    const double kBT = (kB * cfg->temperature).value();
+    const double factor = (conv * (V / kBT)).value();
+    static const int bulk[3] = {0, 2, 5}, shear[3] = {1, 3, 4};   // XX YY ZZ, XY XZ YZ
+    std::stringstream name;
+    name << "viscosity_" << simstep << ".txt";
+    std::ofstream file(name.str());
+    if (!file.is_open()) { std::cerr << "Could not write file: " << name.str() << std::endl; return; }
+    file << "b: " << integrate(series_, bulk, 3, cfg->delta_t, cfg->sensor_visc_no_orig) * factor << std::endl;
+    file << "s: " << integrate(series_, shear, 3, cfg->delta_t, cfg->sensor_visc_no_orig) * factor << std::endl;
+}
+
 void GpuVelocityScaling::apply() {
     const double target = Registry::instance->configuration()->temperature;
     const double current = Registry::instance->temperature_sensor()->getTemperature();

@@ -91,6 +91,21 @@ private:
     double p_[6] = {0, 0, 0, 0, 0, 0};
 };
 
+// ViscositySensor (sensors/ViscositySensor.cpp): the pressure tensor / V of
+// every measure; at write, Green-Kubo integrals of the bulk (XX YY ZZ) and
+// shear (XY XZ YZ) autocorrelations, averaged over the components
+class GpuViscositySensor : public Sensor {
+public:
+    GpuViscositySensor() : Sensor("Viscosity") {}
+    void measure() override;
+    void write(uint64_t simstep) override;     // viscosity_<step>.txt
+    // TensorEvaluator::integrate for the components `dims` of the recorded series
+    static double integrate(const std::vector<std::vector<double>> &series, const int *dims, int ndims, double dt,
+                            bool origin_free);
+private:
+    std::vector<std::vector<double>> series_ = std::vector<std::vector<double>>(6);
+};
+
 // VelocityScaling (thermostats/VelocityScaling.cpp:12-25)
 class GpuVelocityScaling : public Thermostat {
 public:

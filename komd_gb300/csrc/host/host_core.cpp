@@ -102,6 +102,8 @@ bool FileInput::readFile(const std::string &filename) {
         else if (var == "sensor_fene_bins") rd(file, c.sensor_fene_bins);
         else if (var == "sensor_rdf_max") rd(file, c.sensor_rdf_max);
         else if (var == "sensor_rdf_dr") rd(file, c.sensor_rdf_dr);
+        else if (var == "sensor_visc_window") rd(file, c.sensor_visc_window);
+        else if (var == "sensor_visc_no_orig") rdb(file, c.sensor_visc_no_orig);
         else if (var == "store_checkpoint") rdb(file, c.storeCheckpoint);
         else if (var == "ADR_enable") rdb(file, c.ADR_enable);
         else if (var == "IBI_enable") rdb(file, c.IBI_enable);

@@ -65,6 +65,8 @@ struct Configuration {
     uint64_t sensor_fene_bins = 100;
     double sensor_rdf_max = 5.0;
     double sensor_rdf_dr = 0.1;
+    int sensor_visc_window = 1000;
+    bool sensor_visc_no_orig = false;
     bool IBI_enable = false;
     bool ADR_enable = false;
     bool IBI_reload_enable = false;

@@ -4,8 +4,8 @@
 //             the thermostat on the device); log lines at write steps only
 // Input files are KoMD's; the phase space comes from checkpoint_file entries
 // (ps_gen_region inputs are rejected: the phase-space generator is not part of
-// this engine).  Plugins (IBI, AdResS) and the FENE, displacement and
-// viscosity sensors are not available and are reported, not silently skipped.
+// this engine).  Plugins (IBI, AdResS) and the FENE and displacement sensors
+// are not available and are reported, not silently skipped.
 #include <cstring>
 #include <iostream>
 #include <stdexcept>
@@ -56,8 +56,9 @@ int main(int argc, char **argv) {
         }
         if (cfg->enable_sensor_rdf) Registry::instance->sensors().push_back(std::make_shared<GpuRDFSensor>());
         if (cfg->enable_sensor_pres) Registry::instance->sensors().push_back(std::make_shared<GpuPressureSensor>());
-        if (cfg->enable_sensor_fene || cfg->enable_sensor_disp || cfg->enable_sensor_visc)
-            std::cerr << "note: the FENE, displacement and viscosity sensors are not available" << std::endl;
+        if (cfg->enable_sensor_visc) Registry::instance->sensors().push_back(std::make_shared<GpuViscositySensor>());
+        if (cfg->enable_sensor_fene || cfg->enable_sensor_disp)
+            std::cerr << "note: the FENE and displacement sensors are not available" << std::endl;
         Registry::instance->thermostats().push_back(std::make_unique<GpuVelocityScaling>());
 
         Registry::instance->simulation()->run(fused);

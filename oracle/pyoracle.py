@@ -382,3 +382,29 @@ def rdf_profile_normalise(bins, samples, max_r, nbins, n, volume):
         den = n * (n - 1.0) * binvol / volume
         out[b] = bins[b] / samples / den
     return out
+
+
+def visc_green_kubo(series, dt, origin_free):
+    """ViscositySensor::TensorEvaluator::integrate (sensors/ViscositySensor.cpp:118-159)
+    for the bulk (XX YY ZZ) and shear (XY XZ YZ) components of a series of
+    pressure tensors / V (rows in the order XX XY YY XZ YZ ZZ): per component
+    c(k) = mean_t (p(t) - s)(p(t+k) - s) (s = mean p when origin_free), the
+    integral (c(0) + c(n-1) + sum of the inner c(k)) dt / 2, averaged."""
+    p_all = np.asarray(series, np.float64)
+    out = []
+    for dims in ((0, 2, 5), (1, 3, 4)):
+        acc = 0.0
+        for d in dims:
+            p = p_all[:, d]
+            n = p.size
+            s = p.mean() if origin_free else 0.0
+            q = p - s
+            c = np.array([np.dot(q[:n - k], q[k:]) / (n - k) for k in range(n)])
+            acc += (c[0] + c[-1] + c[1:-1].sum()) * dt / 2.0
+        out.append(acc / len(dims))
+    return tuple(out)
+
+
+def visc_factor(volume, temperature):
+    """ViscositySensor::write's unit factor (Da_kg^2 A_m / ps_s^3) * V / (kB T)."""
+    return (1.66053906892e-27 ** 2 * 1e-10 / 1e-36) * volume / (1.380649e-23 * temperature)

@@ -77,3 +77,40 @@ def test_komd_executable_follows_reference(komd_exe, tmp_path, fused):
     s = komd_io.read_checkpoint(str(ck), low=z["low"], high=z["high"])
     ref = z["s50_R"]
     assert np.abs(s.r - ref).max() <= 1e-5 * max(1.0, np.abs(ref).max())
+
+
+@pytest.mark.gpu
+def test_viscosity_sensor_matches_restatement(komd_exe, tmp_path, oracle_lib):
+    """The host layer's Green-Kubo viscosity sensor against the oracle's
+    restatement applied to the same per-step pressure tensors (taken through
+    the C ABI along the same thermostatted FP64 trajectory)."""
+    from komd_gb300 import gpu
+    z = load_case("thermo864")
+    steps = 30
+    inp = _write_case(tmp_path, z, extra=dict(gpu_precision="fp64", enable_sensor_visc=1, sensor_visc_no_orig=1),
+                      steps=steps)
+    out = subprocess.run([komd_exe, inp], capture_output=True, text=True, cwd=tmp_path, timeout=300)
+    assert out.returncode == 0, out.stderr
+    vals = dict(ln.split(": ") for ln in (tmp_path / f"viscosity_{steps}.txt").read_text().split("\n") if ln)
+    # the same loop through the Python binding
+    from test_gpu_parity import gpu_for_case
+    g, _ = gpu_for_case(z, precision=gpu.FP64, thermostat=0)
+    t_target = float(z["p_temperature"])
+    g.update_container()
+    g.forces()
+    g.scale_velocities(np.sqrt(t_target / g.measure(gpu.MEASURE_TEMPERATURE)["temperature"]))
+    vol = float(np.prod(z["high"] - z["low"]))
+    series = []
+    for _ in range(steps):
+        g.integrate0()
+        g.update_container()
+        g.forces()
+        g.integrate1()
+        o = g.measure(gpu.MEASURE_PRESSURE | gpu.MEASURE_TEMPERATURE)
+        series.append(np.asarray(o["pressure"]) / vol)
+        g.scale_velocities(np.sqrt(t_target / o["temperature"]))
+    g.close()
+    b, s = oracle_lib.visc_green_kubo(series, float(z["p_delta_t"]), True)
+    f = oracle_lib.visc_factor(vol, t_target)
+    assert float(vals["b"]) == pytest.approx(b * f, rel=1e-4)
+    assert float(vals["s"]) == pytest.approx(s * f, rel=1e-4)
