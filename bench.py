@@ -43,7 +43,7 @@ WORKLOADS = {
     "lj_argon_4k": dict(ncell=10, rho=0.8442, t=0.722, cell=2.8, rc=2.5, rc3=2.5, nu=0.0, dt=0.005, atm=False,
                         skin=0.3),
 }
-# algorithmic work per unit (frozen constants, see DESIGN.md): the exact ATM
+# algorithmic work per unit (frozen constants): the exact ATM
 # term costs 200 FLOP per in-cutoff triplet in the reference's formulation
 FLOP_PER_TRIPLET = 200.0
 
