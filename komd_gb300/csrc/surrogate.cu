@@ -28,9 +28,9 @@ namespace komd {
 // ---------------------------------------------------------------------------
 // descriptors: one thread per slot (cell order), the 52 sums in registers
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_sur_desc(SurParams p) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
+// features of slot i (standardised when p.fstd is set) to xo[0..31] and its
+// moments to mo[0..35] (both 16-byte aligned; mo may be null)
+__device__ __forceinline__ void sur_site_desc(const SurParams &p, int i, float *xo, float *mo) {
     const int ni = min(p.nl_count[i], p.nl_cap);
     float acc[kSurNR + kSurNC * 9];   // G (16), then per channel M1 (3) + M2 (6: xx xy xz yy yz zz)
 #pragma unroll
@@ -82,16 +82,22 @@ __global__ void __launch_bounds__(128) k_sur_desc(SurParams p) {
 #pragma unroll
         for (int k = 0; k < kSurNF; k++) raw[k] = (raw[k] - p.fmean[k]) / p.fstd[k];
     }
-    float4 *xo = reinterpret_cast<float4 *>(p.x + (size_t)i * kSurNF);
+    float4 *x4 = reinterpret_cast<float4 *>(xo);
 #pragma unroll
-    for (int k = 0; k < kSurNF / 4; k++) xo[k] = make_float4(raw[4 * k], raw[4 * k + 1], raw[4 * k + 2], raw[4 * k + 3]);
-    if (p.mom) {
-        float4 *mo = reinterpret_cast<float4 *>(p.mom + (size_t)i * kSurNC * 9);
+    for (int k = 0; k < kSurNF / 4; k++) x4[k] = make_float4(raw[4 * k], raw[4 * k + 1], raw[4 * k + 2], raw[4 * k + 3]);
+    if (mo) {
+        float4 *m4 = reinterpret_cast<float4 *>(mo);
 #pragma unroll
         for (int k = 0; k < kSurNC * 9 / 4; k++)
-            mo[k] = make_float4(acc[kSurNR + 4 * k], acc[kSurNR + 4 * k + 1], acc[kSurNR + 4 * k + 2],
+            m4[k] = make_float4(acc[kSurNR + 4 * k], acc[kSurNR + 4 * k + 1], acc[kSurNR + 4 * k + 2],
                                 acc[kSurNR + 4 * k + 3]);
     }
+}
+
+__global__ void __launch_bounds__(128) k_sur_desc(SurParams p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    sur_site_desc(p, i, p.x + (size_t)i * kSurNF, p.mom ? p.mom + (size_t)i * kSurNC * 9 : nullptr);
 }
 
 // ---------------------------------------------------------------------------
@@ -130,20 +136,156 @@ __device__ __forceinline__ void load_frag(const __nv_bfloat16 *F, int S, int t, 
     b1 = v.y;
 }
 
+// BF16 weights and FP32 biases staged in shared memory
+struct SurW {
+    const __nv_bfloat16 *w1, *w1t, *w2, *w2t;
+    const float *b1, *b2, *w3;
+};
+
+// one 16-site tile on the tensor cores: thread (g = lane/4, tig = lane%4)
+// reads its rows g and g + 8 of the features (xr0, xr1) and writes the same
+// rows of dE/dx (dr0, dr1, which may alias xr0, xr1); E0, E1 return the MLP
+// outputs (before b3 and scaling) of those rows, complete in the tig == 0 lanes
+__device__ __forceinline__ void sur_mlp_tile(const SurW &W, const float *xr0, const float *xr1, bool v0, bool v1,
+                                             float *dr0, float *dr1, float &E0, float &E1, int lane) {
+    const int tig = lane & 3;
+    // layer 1: Z1 = X W1^T  (X 16x32 -> 2 k-steps)
+    uint32_t ax[2][4];
+#pragma unroll
+    for (int s = 0; s < 2; s++) {
+        const int k = 16 * s + tig * 2;
+        const float2 x00 = v0 ? *reinterpret_cast<const float2 *>(xr0 + k) : make_float2(0.f, 0.f);
+        const float2 x10 = v1 ? *reinterpret_cast<const float2 *>(xr1 + k) : make_float2(0.f, 0.f);
+        const float2 x01 = v0 ? *reinterpret_cast<const float2 *>(xr0 + k + 8) : make_float2(0.f, 0.f);
+        const float2 x11 = v1 ? *reinterpret_cast<const float2 *>(xr1 + k + 8) : make_float2(0.f, 0.f);
+        ax[s][0] = pack_bf16(x00.x, x00.y);
+        ax[s][1] = pack_bf16(x10.x, x10.y);
+        ax[s][2] = pack_bf16(x01.x, x01.y);
+        ax[s][3] = pack_bf16(x11.x, x11.y);
+    }
+    float h1[8][4];
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+        const int c = t * 8 + tig * 2;
+        float acc[4] = {W.b1[c], W.b1[c + 1], W.b1[c], W.b1[c + 1]};
+#pragma unroll
+        for (int s = 0; s < 2; s++) {
+            uint32_t b0, b1;
+            load_frag(W.w1, kSurNF / 16, t, s, lane, b0, b1);
+            mma16816(acc, ax[s], b0, b1);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) h1[t][q] = tanh_fast(acc[q]);
+    }
+    // layer 2: Z2 = H1 W2^T (4 k-steps from the h1 fragments)
+    uint32_t ah[4][4];
+#pragma unroll
+    for (int s = 0; s < 4; s++) {
+        ah[s][0] = pack_bf16(h1[2 * s][0], h1[2 * s][1]);
+        ah[s][1] = pack_bf16(h1[2 * s][2], h1[2 * s][3]);
+        ah[s][2] = pack_bf16(h1[2 * s + 1][0], h1[2 * s + 1][1]);
+        ah[s][3] = pack_bf16(h1[2 * s + 1][2], h1[2 * s + 1][3]);
+    }
+    float h2[8][4];
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+        const int c = t * 8 + tig * 2;
+        float acc[4] = {W.b2[c], W.b2[c + 1], W.b2[c], W.b2[c + 1]};
+#pragma unroll
+        for (int s = 0; s < 4; s++) {
+            uint32_t b0, b1;
+            load_frag(W.w2, kSurH / 16, t, s, lane, b0, b1);
+            mma16816(acc, ah[s], b0, b1);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) h2[t][q] = tanh_fast(acc[q]);
+    }
+    // layer 3 and dE/dz2 = w3 (1 - h2^2)
+    float e0 = 0.f, e1 = 0.f;
+    uint32_t ad[4][4];
+    float dz2[8][4];
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+        const int c = t * 8 + tig * 2;
+        e0 += W.w3[c] * h2[t][0] + W.w3[c + 1] * h2[t][1];
+        e1 += W.w3[c] * h2[t][2] + W.w3[c + 1] * h2[t][3];
+        dz2[t][0] = W.w3[c] * (1.f - h2[t][0] * h2[t][0]);
+        dz2[t][1] = W.w3[c + 1] * (1.f - h2[t][1] * h2[t][1]);
+        dz2[t][2] = W.w3[c] * (1.f - h2[t][2] * h2[t][2]);
+        dz2[t][3] = W.w3[c + 1] * (1.f - h2[t][3] * h2[t][3]);
+    }
+    e0 += __shfl_xor_sync(0xffffffffu, e0, 1);
+    e0 += __shfl_xor_sync(0xffffffffu, e0, 2);
+    e1 += __shfl_xor_sync(0xffffffffu, e1, 1);
+    e1 += __shfl_xor_sync(0xffffffffu, e1, 2);
+    E0 = e0;
+    E1 = e1;
+#pragma unroll
+    for (int s = 0; s < 4; s++) {
+        ad[s][0] = pack_bf16(dz2[2 * s][0], dz2[2 * s][1]);
+        ad[s][1] = pack_bf16(dz2[2 * s][2], dz2[2 * s][3]);
+        ad[s][2] = pack_bf16(dz2[2 * s + 1][0], dz2[2 * s + 1][1]);
+        ad[s][3] = pack_bf16(dz2[2 * s + 1][2], dz2[2 * s + 1][3]);
+    }
+    // dH1 = dZ2 W2  (B = W2^T rows), dZ1 = dH1 (1 - h1^2)
+    uint32_t az[4][4];
+    float dz1[8][4];
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int s = 0; s < 4; s++) {
+            uint32_t b0, b1;
+            load_frag(W.w2t, kSurH / 16, t, s, lane, b0, b1);
+            mma16816(acc, ad[s], b0, b1);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) dz1[t][q] = acc[q] * (1.f - h1[t][q] * h1[t][q]);
+    }
+#pragma unroll
+    for (int s = 0; s < 4; s++) {
+        az[s][0] = pack_bf16(dz1[2 * s][0], dz1[2 * s][1]);
+        az[s][1] = pack_bf16(dz1[2 * s][2], dz1[2 * s][3]);
+        az[s][2] = pack_bf16(dz1[2 * s + 1][0], dz1[2 * s + 1][1]);
+        az[s][3] = pack_bf16(dz1[2 * s + 1][2], dz1[2 * s + 1][3]);
+    }
+    // dX = dZ1 W1  (B = W1^T rows, n = feature); the rows may alias the input rows
+    __syncwarp();
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int s = 0; s < 4; s++) {
+            uint32_t b0, b1;
+            load_frag(W.w1t, kSurH / 16, t, s, lane, b0, b1);
+            mma16816(acc, az[s], b0, b1);
+        }
+        const int c = t * 8 + tig * 2;
+        if (v0) *reinterpret_cast<float2 *>(dr0 + c) = make_float2(acc[0], acc[1]);
+        if (v1) *reinterpret_cast<float2 *>(dr1 + c) = make_float2(acc[2], acc[3]);
+    }
+}
+
+__device__ __forceinline__ void sur_stage_weights(const SurParams &p, __nv_bfloat16 *sW1, __nv_bfloat16 *sW1T,
+                                                  __nv_bfloat16 *sW2, __nv_bfloat16 *sW2T, float *sb1, float *sb2,
+                                                  float *sw3) {
+    // 16-byte staging of the BF16 weights
+    const uint4 *g1 = reinterpret_cast<const uint4 *>(p.w1), *g1t = reinterpret_cast<const uint4 *>(p.w1t);
+    const uint4 *g2 = reinterpret_cast<const uint4 *>(p.w2), *g2t = reinterpret_cast<const uint4 *>(p.w2t);
+    uint4 *s1 = reinterpret_cast<uint4 *>(sW1), *s1t = reinterpret_cast<uint4 *>(sW1T);
+    uint4 *s2 = reinterpret_cast<uint4 *>(sW2), *s2t = reinterpret_cast<uint4 *>(sW2T);
+    for (int t = threadIdx.x; t < kSurH * kSurNF / 8; t += blockDim.x) { s1[t] = g1[t]; s1t[t] = g1t[t]; }
+    for (int t = threadIdx.x; t < kSurH * kSurH / 8; t += blockDim.x) { s2[t] = g2[t]; s2t[t] = g2t[t]; }
+    for (int t = threadIdx.x; t < kSurH; t += blockDim.x) { sb1[t] = p.b1[t]; sb2[t] = p.b2[t]; sw3[t] = p.w3[t]; }
+}
+
 __global__ void __launch_bounds__(128) k_sur_mlp(SurParams p) {
     __shared__ __align__(16) __nv_bfloat16 sW1[kSurH * kSurNF], sW1T[kSurNF * kSurH], sW2[kSurH * kSurH],
         sW2T[kSurH * kSurH];
     __shared__ float sb1[kSurH], sb2[kSurH], sw3[kSurH];
-    {   // 16-byte staging of the BF16 weights
-        const uint4 *g1 = reinterpret_cast<const uint4 *>(p.w1), *g1t = reinterpret_cast<const uint4 *>(p.w1t);
-        const uint4 *g2 = reinterpret_cast<const uint4 *>(p.w2), *g2t = reinterpret_cast<const uint4 *>(p.w2t);
-        uint4 *s1 = reinterpret_cast<uint4 *>(sW1), *s1t = reinterpret_cast<uint4 *>(sW1T);
-        uint4 *s2 = reinterpret_cast<uint4 *>(sW2), *s2t = reinterpret_cast<uint4 *>(sW2T);
-        for (int t = threadIdx.x; t < kSurH * kSurNF / 8; t += blockDim.x) { s1[t] = g1[t]; s1t[t] = g1t[t]; }
-        for (int t = threadIdx.x; t < kSurH * kSurH / 8; t += blockDim.x) { s2[t] = g2[t]; s2t[t] = g2t[t]; }
-    }
-    for (int t = threadIdx.x; t < kSurH; t += blockDim.x) { sb1[t] = p.b1[t]; sb2[t] = p.b2[t]; sw3[t] = p.w3[t]; }
+    sur_stage_weights(p, sW1, sW1T, sW2, sW2T, sb1, sb2, sw3);
     __syncthreads();
+    const SurW W{sW1, sW1T, sW2, sW2T, sb1, sb2, sw3};
     const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
     const int warp = blockIdx.x * 4 + (threadIdx.x >> 5);
     const int nwarps = gridDim.x * 4;
@@ -151,121 +293,12 @@ __global__ void __launch_bounds__(128) k_sur_mlp(SurParams p) {
     for (int tile = warp; tile < ntiles; tile += nwarps) {
         const int r0 = tile * 16 + g, r1 = r0 + 8;
         const bool v0 = r0 < p.n, v1 = r1 < p.n;
-        // layer 1: Z1 = X W1^T  (X 16x32 -> 2 k-steps)
-        uint32_t ax[2][4];
-#pragma unroll
-        for (int s = 0; s < 2; s++) {
-            const int k = 16 * s + tig * 2;
-            const float2 x00 = v0 ? *reinterpret_cast<const float2 *>(p.x + (size_t)r0 * kSurNF + k) : make_float2(0.f, 0.f);
-            const float2 x10 = v1 ? *reinterpret_cast<const float2 *>(p.x + (size_t)r1 * kSurNF + k) : make_float2(0.f, 0.f);
-            const float2 x01 = v0 ? *reinterpret_cast<const float2 *>(p.x + (size_t)r0 * kSurNF + k + 8) : make_float2(0.f, 0.f);
-            const float2 x11 = v1 ? *reinterpret_cast<const float2 *>(p.x + (size_t)r1 * kSurNF + k + 8) : make_float2(0.f, 0.f);
-            ax[s][0] = pack_bf16(x00.x, x00.y);
-            ax[s][1] = pack_bf16(x10.x, x10.y);
-            ax[s][2] = pack_bf16(x01.x, x01.y);
-            ax[s][3] = pack_bf16(x11.x, x11.y);
-        }
-        float h1[8][4];
-#pragma unroll
-        for (int t = 0; t < 8; t++) {
-            const int c = t * 8 + tig * 2;
-            float acc[4] = {sb1[c], sb1[c + 1], sb1[c], sb1[c + 1]};
-#pragma unroll
-            for (int s = 0; s < 2; s++) {
-                uint32_t b0, b1;
-                load_frag(sW1, kSurNF / 16, t, s, lane, b0, b1);
-                mma16816(acc, ax[s], b0, b1);
-            }
-#pragma unroll
-            for (int q = 0; q < 4; q++) h1[t][q] = tanh_fast(acc[q]);
-        }
-        // layer 2: Z2 = H1 W2^T (4 k-steps from the h1 fragments)
-        uint32_t ah[4][4];
-#pragma unroll
-        for (int s = 0; s < 4; s++) {
-            ah[s][0] = pack_bf16(h1[2 * s][0], h1[2 * s][1]);
-            ah[s][1] = pack_bf16(h1[2 * s][2], h1[2 * s][3]);
-            ah[s][2] = pack_bf16(h1[2 * s + 1][0], h1[2 * s + 1][1]);
-            ah[s][3] = pack_bf16(h1[2 * s + 1][2], h1[2 * s + 1][3]);
-        }
-        float h2[8][4];
-#pragma unroll
-        for (int t = 0; t < 8; t++) {
-            const int c = t * 8 + tig * 2;
-            float acc[4] = {sb2[c], sb2[c + 1], sb2[c], sb2[c + 1]};
-#pragma unroll
-            for (int s = 0; s < 4; s++) {
-                uint32_t b0, b1;
-                load_frag(sW2, kSurH / 16, t, s, lane, b0, b1);
-                mma16816(acc, ah[s], b0, b1);
-            }
-#pragma unroll
-            for (int q = 0; q < 4; q++) h2[t][q] = tanh_fast(acc[q]);
-        }
-        // layer 3 and dE/dz2 = w3 (1 - h2^2)
-        float e0 = 0.f, e1 = 0.f;
-        uint32_t ad[4][4];
-        float dz2[8][4];
-#pragma unroll
-        for (int t = 0; t < 8; t++) {
-            const int c = t * 8 + tig * 2;
-            e0 += sw3[c] * h2[t][0] + sw3[c + 1] * h2[t][1];
-            e1 += sw3[c] * h2[t][2] + sw3[c + 1] * h2[t][3];
-            dz2[t][0] = sw3[c] * (1.f - h2[t][0] * h2[t][0]);
-            dz2[t][1] = sw3[c + 1] * (1.f - h2[t][1] * h2[t][1]);
-            dz2[t][2] = sw3[c] * (1.f - h2[t][2] * h2[t][2]);
-            dz2[t][3] = sw3[c + 1] * (1.f - h2[t][3] * h2[t][3]);
-        }
-        e0 += __shfl_xor_sync(0xffffffffu, e0, 1);
-        e0 += __shfl_xor_sync(0xffffffffu, e0, 2);
-        e1 += __shfl_xor_sync(0xffffffffu, e1, 1);
-        e1 += __shfl_xor_sync(0xffffffffu, e1, 2);
+        float e0, e1;
+        sur_mlp_tile(W, p.x + (size_t)r0 * kSurNF, p.x + (size_t)r1 * kSurNF, v0, v1, p.dedx + (size_t)r0 * kSurNF,
+                     p.dedx + (size_t)r1 * kSurNF, e0, e1, lane);
         if (tig == 0) {
             if (v0) p.e_site[r0] = p.e_scale * (e0 + p.b3) + p.e_shift;
             if (v1) p.e_site[r1] = p.e_scale * (e1 + p.b3) + p.e_shift;
-        }
-#pragma unroll
-        for (int s = 0; s < 4; s++) {
-            ad[s][0] = pack_bf16(dz2[2 * s][0], dz2[2 * s][1]);
-            ad[s][1] = pack_bf16(dz2[2 * s][2], dz2[2 * s][3]);
-            ad[s][2] = pack_bf16(dz2[2 * s + 1][0], dz2[2 * s + 1][1]);
-            ad[s][3] = pack_bf16(dz2[2 * s + 1][2], dz2[2 * s + 1][3]);
-        }
-        // dH1 = dZ2 W2  (B = W2^T rows), dZ1 = dH1 (1 - h1^2)
-        uint32_t az[4][4];
-        float dz1[8][4];
-#pragma unroll
-        for (int t = 0; t < 8; t++) {
-            float acc[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-            for (int s = 0; s < 4; s++) {
-                uint32_t b0, b1;
-                load_frag(sW2T, kSurH / 16, t, s, lane, b0, b1);
-                mma16816(acc, ad[s], b0, b1);
-            }
-#pragma unroll
-            for (int q = 0; q < 4; q++) dz1[t][q] = acc[q] * (1.f - h1[t][q] * h1[t][q]);
-        }
-#pragma unroll
-        for (int s = 0; s < 4; s++) {
-            az[s][0] = pack_bf16(dz1[2 * s][0], dz1[2 * s][1]);
-            az[s][1] = pack_bf16(dz1[2 * s][2], dz1[2 * s][3]);
-            az[s][2] = pack_bf16(dz1[2 * s + 1][0], dz1[2 * s + 1][1]);
-            az[s][3] = pack_bf16(dz1[2 * s + 1][2], dz1[2 * s + 1][3]);
-        }
-        // dX = dZ1 W1  (B = W1^T rows, n = feature)
-#pragma unroll
-        for (int t = 0; t < 4; t++) {
-            float acc[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-            for (int s = 0; s < 4; s++) {
-                uint32_t b0, b1;
-                load_frag(sW1T, kSurH / 16, t, s, lane, b0, b1);
-                mma16816(acc, az[s], b0, b1);
-            }
-            const int c = t * 8 + tig * 2;
-            if (v0) *reinterpret_cast<float2 *>(p.dedx + (size_t)r0 * kSurNF + c) = make_float2(acc[0], acc[1]);
-            if (v1) *reinterpret_cast<float2 *>(p.dedx + (size_t)r1 * kSurNF + c) = make_float2(acc[2], acc[3]);
         }
     }
 }
@@ -275,12 +308,11 @@ __global__ void __launch_bounds__(128) k_sur_mlp(SurParams p) {
 // neighbour's share is scattered with float4 atomics into fsur (slot order,
 // xyz + pad), the centre's share is summed in registers
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_sur_force(SurParams p) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
+// forces of slot i from its dE/dx row and moment row (16-byte aligned)
+__device__ __forceinline__ void sur_site_force(const SurParams &p, int i, const float *dxr, const float *mor) {
     // dE_i / d raw = e_scale * dE/dx / std
     float dr[kSurNF];
-    const float4 *dx = reinterpret_cast<const float4 *>(p.dedx + (size_t)i * kSurNF);
+    const float4 *dx = reinterpret_cast<const float4 *>(dxr);
 #pragma unroll
     for (int k = 0; k < kSurNF / 4; k++) {
         const float4 t = dx[k];
@@ -290,7 +322,7 @@ __global__ void __launch_bounds__(128) k_sur_force(SurParams p) {
     for (int k = 0; k < kSurNF; k++) dr[k] *= p.e_scale / p.fstd[k];
     float a[kSurNC][3], B[kSurNC][6];
     float mom[kSurNC * 9];
-    const float4 *mo = reinterpret_cast<const float4 *>(p.mom + (size_t)i * kSurNC * 9);
+    const float4 *mo = reinterpret_cast<const float4 *>(mor);
 #pragma unroll
     for (int k = 0; k < kSurNC * 9 / 4; k++) {
         const float4 t = mo[k];
@@ -316,6 +348,12 @@ __global__ void __launch_bounds__(128) k_sur_force(SurParams p) {
         fx += h[0]; fy += h[1]; fz += h[2];
     }
     atomicAdd(&fs[i], make_float4(fx, fy, fz, 0.f));
+}
+
+__global__ void __launch_bounds__(128) k_sur_force(SurParams p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    sur_site_force(p, i, p.dedx + (size_t)i * kSurNF, p.mom + (size_t)i * kSurNC * 9);
 }
 
 // f[site] += fsur[slot] (then fsur = 0); with fout, the surrogate force is
@@ -419,7 +457,7 @@ __global__ void k_train_grad(TrainParams t) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q > kSurNParam) return;
     const int stride = kSurNF + 4 * kSurH + 2;
-    const int oW1 = 0, ob1 = kSurH * kSurNF, oW2 = ob1 + kSurH, ob2 = oW2 + kSurH * kSurH, ow3 = ob2 + kSurH,
+    const int ob1 = kSurH * kSurNF, oW2 = ob1 + kSurH, ob2 = oW2 + kSurH * kSurH, ow3 = ob2 + kSurH,
               ob3 = ow3 + kSurH;
     float s = 0.f;
     for (int b = 0; b < t.batch; b++) {
