@@ -197,10 +197,14 @@ bool enqueue_forces(komd_gpu *h, bool measure, double *lj_hist, bool with_step1 
     cudaStream_t st = e.stream;
     bool fused = false;
     int pair_blocks;
+    // a force-only pass whose ATM list goes only to the once-per-triplet kernel
+    // needs the neighbours above each site only
+    e.atm_up = !measure && !surrogate_on(h) && e.atm_acc != nullptr && e.verlet;
     {
         ProfScope ps(h, F_PAIR);
         pair_blocks = launch_pair(e, st, measure, lj_hist);
     }
+    e.atm_up = false;
     if (measure) launch_sum_partials(st, pair_blocks, e.partials, h->acc);
     if (e.cfg.terms & KOMD_TERM_TABULATED) {   // in the LJ functor's place (IBI.cpp:52-54), before Limit
         ProfScope ps(h, F_PAIR);

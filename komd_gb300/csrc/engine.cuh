@@ -141,6 +141,7 @@ struct PairParams {
     float eps0, sig0;
     float lj_fscalef;          // ATM2B force factor (1 without ATM2B), force path only
     double lj_fscale;
+    int atm_up;                // Verlet LJ kernel: emit only ATM neighbours with a larger slot
 };
 
 struct AtmParams {
@@ -255,6 +256,7 @@ struct Engine {
     float eps0 = 1.f, sig0 = 1.f;
     double lj_fscale = 1.0;         // ATM2B factor (KOMD_TERM_ATM2B), else 1
     bool fused_drift = false;       // Verlet path, single-site molecules with exact COM: k_step0_fused
+    bool atm_up = false;            // this force pass feeds k_atm_s only: ATM lists hold neighbours above
     unsigned long long *atm_acc = nullptr;   // 3 per slot, fixed-point force sums of k_atm_s (zero between steps)
     // tabulated pair force (KOMD_TERM_TABULATED): F(r) piecewise linear on
     // ascending nodes tab_x, values tab_y, tab_lo below / tab_hi above the nodes

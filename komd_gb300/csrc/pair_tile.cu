@@ -470,7 +470,8 @@ __global__ void __launch_bounds__(256, 5) k_lj_vlist(PairParams p, int n) {
                     }
                 }
                 if (EMIT) {
-                    const bool emit = valid && r2 <= rc3sq;
+                    // with atm_up the once-per-triplet kernel reads the list: neighbours above i only
+                    const bool emit = valid && r2 <= rc3sq && (!p.atm_up || (int)(e[u] & 0x3ffffffu) > i);
                     const unsigned m = __ballot_sync(0xffffffffu, emit);
                     if (emit) {
                         const int pos = c_atm + __popc(m & lt);
