@@ -195,6 +195,14 @@ int  komd_gpu_neighbour_counts(komd_gpu *h, int64_t *counts);
  * `below` for r < x[0], `above` for r > x[n-1].  May be replaced between
  * steps (the IBI iteration's force update, IBI.cpp:172-178). */
 int  komd_gpu_set_pair_table(komd_gpu *h, int32_t n, const double *x, const double *y, double below, double above);
+/* Replace the step's force terms between steps, as a plugin replaces the
+ * Registry's functors (plugins/IBI/IBI.cpp:50-54 swaps LJ, FENE, Limit and
+ * ATM for the tabulated force; IBI_ReloadForce.cpp:33-49).  `terms` may drop
+ * any term given at creation and may add KOMD_TERM_TABULATED (per-step cell
+ * lists only: skin 0); nothing else can be added.  The sensors
+ * (komd_gpu_measure) keep evaluating the terms given at creation, as the
+ * reference's sensors do not go through the functor list. */
+int  komd_gpu_set_terms(komd_gpu *h, uint32_t terms);
 /* RDF_Profiler::measure / getRDF (plugins/IBI/RDF_Profiler.cpp:18-55): ordered
  * molecule-COM pair histogram with nbins bins of max_r / nbins up to max_r
  * (added to bins, nbins doubles). */

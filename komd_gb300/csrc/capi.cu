@@ -83,6 +83,11 @@ struct komd_gpu {
     double *thermo_acc = nullptr;     // R_NSLOTS, the device thermostat's kinetic sums
     int partial_cap = 0;
     bool want_posd = false;
+    // the terms given at creation: the sensors evaluate these whatever the step's
+    // force terms are (the reference's sensors do not go through the functor list)
+    uint32_t sensor_terms = 0;
+    double *prof = nullptr;           // komd_gpu_rdf_profile's device histogram
+    int prof_cap = 0;
     // profiling
     std::vector<cudaEvent_t> pool;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
@@ -200,9 +205,12 @@ bool enqueue_forces(komd_gpu *h, bool measure, double *lj_hist, bool with_step1 
     // a force-only pass whose ATM list goes only to the once-per-triplet kernel
     // needs the neighbours above each site only
     e.atm_up = !measure && !surrogate_on(h) && e.atm_acc != nullptr && e.verlet;
-    {
+    if (measure || (e.cfg.terms & (KOMD_TERM_LJ | KOMD_TERM_FENE | KOMD_TERM_ATM))) {
         ProfScope ps(h, F_PAIR);
-        pair_blocks = launch_pair(e, st, measure, lj_hist);
+        pair_blocks = launch_pair(e, st, measure, lj_hist);   // the pair pass writes f (first writer)
+    } else {
+        pair_blocks = 0;
+        cudaMemsetAsync(e.f, 0, sizeof(double) * 3 * e.n, st);
     }
     e.atm_up = false;
     if (measure) launch_sum_partials(st, pair_blocks, e.partials, h->acc);
@@ -378,6 +386,7 @@ int komd_gpu_create(const komd_config *cfg, int device, komd_gpu **out) {
     komd_gpu *h = new komd_gpu();
     Engine &e = h->e;
     e.cfg = *cfg;
+    h->sensor_terms = cfg->terms;
     if (e.cfg.lj_bins <= 0) e.cfg.lj_bins = 100;
     if (!(e.cfg.max_sigma > 0)) e.cfg.max_sigma = 1.0;
     e.g = g;
@@ -465,7 +474,7 @@ int komd_gpu_destroy(komd_gpu *h) {
     dfree(e.slot_site); dfree(e.skey); dfree(e.pos4); dfree(e.seps); dfree(e.posd); dfree(e.seps_d); dfree(e.sig_d);
     dfree(e.nl); dfree(e.nl_count); dfree(e.bonds); dfree(e.angles); dfree(e.partials); dfree(e.err);
     dfree(e.tab_x); dfree(e.tab_y); dfree(e.atm_acc);
-    dfree(e.rdf); dfree(e.lj_hist); dfree(e.counts); dfree(h->f_scratch); dfree(h->acc); dfree(h->thermo_acc); dfree(e.offtab);
+    dfree(e.rdf); dfree(e.lj_hist); dfree(e.counts); dfree(h->f_scratch); dfree(h->prof); dfree(h->acc); dfree(h->thermo_acc); dfree(e.offtab);
     dfree(e.nboff); dfree(e.rebuild); dfree(e.img); dfree(e.ref); dfree(e.slot_cell); dfree(e.vl); dfree(e.vl_count);
     dfree(e.rebuild_count); dfree(e.hdtm); dfree(e.exact_com);
     {
@@ -853,14 +862,52 @@ int komd_gpu_set_pair_table(komd_gpu *h, int32_t n, const double *x, const doubl
     return KOMD_OK;
 }
 
+int komd_gpu_set_terms(komd_gpu *h, uint32_t terms) {
+    if (!h) return fail(KOMD_ERR_ARG, "null handle");
+    Engine &e = h->e;
+    if (terms & ~(h->sensor_terms | KOMD_TERM_TABULATED))
+        return fail(KOMD_ERR_ARG, "only KOMD_TERM_TABULATED can be added to the terms given at creation");
+    if ((terms & KOMD_TERM_TABULATED) && e.verlet)
+        return fail(KOMD_ERR_ARG, "the tabulated pair term runs on per-step cell lists (skin 0)");
+    if ((terms & KOMD_TERM_ATM2B) && !(terms & KOMD_TERM_LJ))
+        return fail(KOMD_ERR_ARG, "KOMD_TERM_ATM2B scales the LJ term: set KOMD_TERM_LJ");
+    if ((terms & KOMD_TERM_ATM_SURROGATE) && !(terms & KOMD_TERM_ATM))
+        return fail(KOMD_ERR_ARG, "the learned three-body term needs KOMD_TERM_ATM");
+    if (terms == e.cfg.terms) return KOMD_OK;
+    CK(cudaStreamSynchronize(e.stream));
+    if ((terms & KOMD_TERM_TABULATED) && !e.posd) {
+        h->want_posd = true;
+        if (e.have_sites) {
+            int rc = ensure_posd(h);
+            if (rc) return rc;
+            // fill the FP64 slot-ordered positions of the current cells; the
+            // container pass is idempotent on wrapped positions and leaves f alone
+            if (e.have_cells) launch_rebuild(h);
+            rc = check_launch("set_terms");
+            if (rc) return rc;
+        }
+    }
+    e.cfg.terms = terms;
+    if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+    e.graph_valid = false;
+    return KOMD_OK;
+}
+
 int komd_gpu_rdf_profile(komd_gpu *h, double max_r, int32_t nbins, double *bins) {
     if (!h || !bins || nbins <= 0 || !(max_r > 0)) return fail(KOMD_ERR_ARG, "bad argument");
     Engine &e = h->e;
     if (!e.have_cells) return fail(KOMD_ERR_STATE, "update_container must run first");
     cudaStream_t st = e.stream;
     if (e.verlet) launch_rebuild(h);   // the cells of the last rebuild may be stale
-    double *d = nullptr;
-    CK(dalloc(d, nbins));
+    if (nbins > h->prof_cap) {   // kept across calls: a profiler samples every step
+        h->prof_cap = 0;
+        if (dalloc(h->prof, nbins) != cudaSuccess) {
+            h->prof = nullptr;
+            return fail(KOMD_ERR_NOMEM, "rdf_profile histogram");
+        }
+        h->prof_cap = nbins;
+    }
+    double *d = h->prof;
     CK(cudaMemsetAsync(d, 0, sizeof(double) * nbins, st));
     const double dr = max_r / (double)nbins;   // RDF_Profiler.cpp:8
     launch_rdf_bins(e, st, d, max_r <= e.cfg.cell_size, max_r, dr, nbins);
@@ -871,7 +918,6 @@ int komd_gpu_rdf_profile(komd_gpu *h, double max_r, int32_t nbins, double *bins)
         const cudaError_t se = cudaStreamSynchronize(st);
         if (ce != cudaSuccess || se != cudaSuccess) rc = fail(KOMD_ERR_CUDA, "rdf_profile copy");
     }
-    dfree(d);
     if (rc) return rc;
     for (int32_t k = 0; k < nbins; k++) bins[k] += hb[k];
     return KOMD_OK;
@@ -903,9 +949,12 @@ int komd_gpu_measure(komd_gpu *h, uint32_t mask, komd_observables *obs, double *
         // the reference re-run their functors as well); f itself is untouched
         if (mask & KOMD_MEASURE_LJ_HIST) CK(cudaMemsetAsync(e.lj_hist, 0, sizeof(double) * 4 * e.cfg.lj_bins, st));
         double *keep = e.f;
+        const uint32_t force_terms = e.cfg.terms;
         CK(cudaMemsetAsync(h->f_scratch, 0, sizeof(double) * 3 * e.n, st));
         e.f = h->f_scratch;
+        e.cfg.terms = h->sensor_terms;
         enqueue_forces(h, true, (mask & KOMD_MEASURE_LJ_HIST) ? e.lj_hist : nullptr);
+        e.cfg.terms = force_terms;
         e.f = keep;
     }
     const int n_terms = e.cfg.virial_mode == KOMD_VIRIAL_COMPAT ? (int)e.n_mol : (int)e.n;
@@ -1635,7 +1684,9 @@ int komd_batch_check(komd_batch *b) {
 int komd_gpu_kernels_per_step(komd_gpu *h) {
     if (!h) return -1;
     const Engine &e = h->e;
-    int k = 2 /* integrate */ + 4 /* com/wrap/bin, scan, scatter, cell sort */ + 1 /* pair */;
+    int k = 2 /* integrate */ + 4 /* com/wrap/bin, scan, scatter, cell sort */;
+    if (e.cfg.terms & (KOMD_TERM_LJ | KOMD_TERM_FENE | KOMD_TERM_ATM)) k++;   /* pair pass (else a memset) */
+    if (e.cfg.terms & KOMD_TERM_TABULATED) k++;
     if (!surrogate_on(h) && (e.cfg.terms & KOMD_TERM_ATM) && e.atm_acc) k--;   /* integrate1 fused into the ATM flush */
     if (e.verlet) k += e.fused_drift ? 1 : 2;   /* (refresh,) list build; the fused drift does the refresh */
     if ((e.cfg.terms & KOMD_TERM_BONDED) && e.n_bonds > 0) k++;

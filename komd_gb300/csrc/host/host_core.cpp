@@ -107,7 +107,19 @@ bool FileInput::readFile(const std::string &filename) {
         else if (var == "store_checkpoint") rdb(file, c.storeCheckpoint);
         else if (var == "ADR_enable") rdb(file, c.ADR_enable);
         else if (var == "IBI_enable") rdb(file, c.IBI_enable);
+        else if (var == "IBI_bins") rd(file, c.IBI_bins);
+        else if (var == "IBI_alpha") rd(file, c.IBI_alpha);
+        else if (var == "IBI_steps_equil") { double t = 0; file >> t; c.IBI_steps_equil = (int)t; }
+        else if (var == "IBI_steps_measure") { double t = 0; file >> t; c.IBI_steps_measure = (int)t; }
+        else if (var == "IBI_conv_threshold") rd(file, c.IBI_conv_threshold);
+        else if (var == "IBI_conv_mode") rd(file, c.IBI_conv_mode);
+        else if (var == "IBI_conv_stop") rd(file, c.IBI_conv_stop);
+        else if (var == "IBI_conv_window") rd(file, c.IBI_conv_window);
         else if (var == "IBI_reload") rdb(file, c.IBI_reload_enable);
+        else if (var == "IBI_reload_fpath") rd(file, c.IBI_reload_fpath);
+        else if (var == "IBI_reload_ppath") rd(file, c.IBI_reload_ppath);
+        else if (var == "IBI_exclusion_low") rd3(file, c.IBI_exclusion_low);
+        else if (var == "IBI_exclusion_high") rd3(file, c.IBI_exclusion_high);
         else if (var == "enable_one_cell") rdb(file, c.enable_one_cell);
         else if (var == "ps_gen_region") {
             d3 b, e;

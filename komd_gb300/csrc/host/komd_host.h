@@ -68,8 +68,19 @@ struct Configuration {
     int sensor_visc_window = 1000;
     bool sensor_visc_no_orig = false;
     bool IBI_enable = false;
-    bool ADR_enable = false;
+    uint64_t IBI_bins = 100;
+    double IBI_alpha = 0.2;
+    int IBI_steps_equil = 1000000;
+    int IBI_steps_measure = 100000;
+    double IBI_conv_threshold = 0.99;
+    std::string IBI_conv_mode = "integral";
+    std::string IBI_conv_stop = "worse";
+    int IBI_conv_window = 10;
     bool IBI_reload_enable = false;
+    std::string IBI_reload_fpath, IBI_reload_ppath;
+    d3 IBI_exclusion_low{0, 0, 0};
+    d3 IBI_exclusion_high{0, 0, 0};
+    bool ADR_enable = false;
     bool enable_one_cell = false;
     // engine keys (no reference counterpart)
     int gpu_precision = KOMD_FP32;                  // gpu_precision fp32|fp64

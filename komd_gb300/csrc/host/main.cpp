@@ -4,13 +4,15 @@
 //             the thermostat on the device); log lines at write steps only
 // Input files are KoMD's; the phase space comes from checkpoint_file entries
 // (ps_gen_region inputs are rejected: the phase-space generator is not part of
-// this engine).  Plugins (IBI, AdResS) and the FENE and displacement sensors
-// are not available and are reported, not silently skipped.
+// this engine).  The IBI and IBI_Reload plugins run (ibi.h); AdResS and the
+// FENE and displacement sensors are not available and are reported, not
+// silently skipped.
 #include <cstring>
 #include <iostream>
 #include <stdexcept>
 
 #include "gpu_adapters.h"
+#include "ibi.h"
 
 using namespace komd;
 
@@ -30,8 +32,13 @@ int main(int argc, char **argv) {
         if (cfg->enable_one_cell) throw std::runtime_error("not supported anymore");
         if (!cfg->phasespace_gen_regions.empty())
             throw std::runtime_error("ps_gen_region: the phase-space generator is not available; use checkpoint_file");
-        if (cfg->IBI_enable || cfg->IBI_reload_enable || cfg->ADR_enable)
-            throw std::runtime_error("the IBI and AdResS plugins are not available in this engine");
+        if (cfg->ADR_enable) throw std::runtime_error("the AdResS plugin is not available in this engine");
+        const bool plugins = cfg->IBI_enable || cfg->IBI_reload_enable;
+        if (plugins && fused)
+            throw std::runtime_error("--fused advances whole write intervals on the device; the IBI plugins need "
+                                     "their per-step hooks");
+        if (plugins && cfg->gpu_skin > 0)
+            throw std::runtime_error("the IBI plugins' tabulated force runs on per-step cell lists: set gpu_skin 0");
         auto container = std::make_shared<GpuLinkedCells>();
         container->device_thermostat = fused;
         Registry::instance->moleculeContainer_ptr() = container;
@@ -59,6 +66,9 @@ int main(int argc, char **argv) {
         if (cfg->enable_sensor_visc) Registry::instance->sensors().push_back(std::make_shared<GpuViscositySensor>());
         if (cfg->enable_sensor_fene || cfg->enable_sensor_disp)
             std::cerr << "note: the FENE and displacement sensors are not available" << std::endl;
+        // plugins (main.cpp:89-91)
+        if (cfg->IBI_enable) Registry::instance->plugins().push_back(std::make_unique<GpuIBI>());
+        if (cfg->IBI_reload_enable) Registry::instance->plugins().push_back(std::make_unique<GpuIBIReload>());
         Registry::instance->thermostats().push_back(std::make_unique<GpuVelocityScaling>());
 
         Registry::instance->simulation()->run(fused);

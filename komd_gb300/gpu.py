@@ -37,7 +37,7 @@ EXPORTS = [
     "komd_gpu_surrogate_sample", "komd_gpu_surrogate_forces", "komd_gpu_surrogate_status", "komd_mlp_train",
     "komd_mlp_loss_grad", "komd_sur_data_create", "komd_sur_data_destroy", "komd_gpu_surrogate_capture",
     "komd_sur_data_snapshots", "komd_sur_data_sites", "komd_sur_data_get", "komd_sur_fit", "komd_sur_fit_grad",
-    "komd_gpu_scale_velocities", "komd_gpu_set_pair_table", "komd_gpu_rdf_profile", "komd_batch_create", "komd_batch_destroy", "komd_batch_step", "komd_batch_launch", "komd_batch_check",
+    "komd_gpu_scale_velocities", "komd_gpu_set_pair_table", "komd_gpu_rdf_profile", "komd_gpu_set_terms", "komd_batch_create", "komd_batch_destroy", "komd_batch_step", "komd_batch_launch", "komd_batch_check",
 ]
 
 
@@ -137,6 +137,7 @@ def load() -> C.CDLL:
     L.komd_gpu_scale_velocities.argtypes = [P, C.c_double]
     L.komd_gpu_set_pair_table.argtypes = [P, I32, P, P, C.c_double, C.c_double]
     L.komd_gpu_rdf_profile.argtypes = [P, C.c_double, I32, P]
+    L.komd_gpu_set_terms.argtypes = [P, C.c_uint32]
     L.komd_batch_create.argtypes = [P, I32, I32, I32, P, C.POINTER(P)]
     L.komd_batch_destroy.argtypes = [P]
     L.komd_batch_destroy.restype = None
@@ -322,6 +323,10 @@ class GpuSystem:
         x = np.ascontiguousarray(x, np.float64)
         y = np.ascontiguousarray(y, np.float64)
         self._check(self.L.komd_gpu_set_pair_table(self.h, x.size, _p(x), _p(y), float(below), float(above)))
+
+    def set_terms(self, terms: int):
+        """Replaces the step's force terms (a plugin swapping the functors)."""
+        self._check(self.L.komd_gpu_set_terms(self.h, int(terms)))
 
     def rdf_profile(self, max_r, nbins):
         """RDF_Profiler histogram (ordered COM pairs, nbins bins up to max_r)."""

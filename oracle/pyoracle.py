@@ -408,3 +408,166 @@ def visc_green_kubo(series, dt, origin_free):
 def visc_factor(volume, temperature):
     """ViscositySensor::write's unit factor (Da_kg^2 A_m / ps_s^3) * V / (kB T)."""
     return (1.66053906892e-27 ** 2 * 1e-10 / 1e-36) * volume / (1.380649e-23 * temperature)
+
+
+# --- IBI plugin (plugins/IBI/*.cpp) under the stock main's loop ---------------
+
+def ibi_continue_below(y, k0):
+    """Linear continuation below node k0 with the slope of (k0, k0 + 1)
+    (IBI.cpp:140-150 and 170-180)."""
+    if k0 < 0:
+        return
+    dy = y[k0 + 1] - y[k0] if k0 + 1 < y.size else 0.0
+    v = y[k0]
+    for k in range(k0, -1, -1):
+        y[k] = v
+        v -= dy
+
+
+def ibi_initial_potential(g0, temperature):
+    """IBI::initializePotentialValues (IBI.cpp:130-153): U0 = -T ln g0, continued
+    linearly below the first finite value."""
+    with np.errstate(divide="ignore", invalid="ignore"):
+        u = -temperature * np.log(np.asarray(g0, np.float64))
+    fin = np.flatnonzero(np.isfinite(u))
+    ibi_continue_below(u, int(fin[0]) if fin.size else -1)
+    return u
+
+
+def ibi_correction(pot, g_i, g0, alpha, temperature):
+    """IBI::addPotentialCorrection (IBI.cpp:155-182): (new potential, update)."""
+    pot = np.asarray(pot, np.float64).copy()
+    with np.errstate(divide="ignore", invalid="ignore"):
+        d = alpha * temperature * np.log(np.asarray(g_i) / np.asarray(g0))
+    ok = np.isfinite(d)
+    pot[ok] += d[ok]
+    update = np.where(ok, d, 0.0)
+    nz = np.flatnonzero(np.asarray(g0) != 0.0)
+    ibi_continue_below(pot, int(nz[0]) if nz.size else -1)
+    return pot, update
+
+
+def ibi_force(x, pot):
+    """IBI::derivativeOfPotential (IBI.cpp:184-191) with FunctionPL::derivative
+    (IBI_Math.cpp:21-33): F = -dU/dr, one-sided at the ends, central inside."""
+    x, y = np.asarray(x, np.float64), np.asarray(pot, np.float64)
+    d = np.empty_like(y)
+    d[0] = (y[1] - y[0]) / (x[1] - x[0])
+    d[-1] = (y[-1] - y[-2]) / (x[-1] - x[-2])
+    d[1:-1] = (y[2:] - y[:-2]) / (x[2:] - x[:-2])
+    return -d
+
+
+def ibi_convergence(mode, x, g0, g_i):
+    """IBI::Convergence::integral / l2 (IBI.cpp:210-253)."""
+    g0, g_i = np.asarray(g0, np.float64), np.asarray(g_i, np.float64)
+    if mode == "l2":
+        return float(np.sum((g0 - g_i) ** 2))
+    dx = np.diff(np.asarray(x, np.float64))
+    a, b = np.abs(g_i - g0), np.abs(g_i + g0)
+    diff = float(np.sum(dx * (a[1:] + a[:-1]) / 2.0))
+    tot = float(np.sum(dx * (b[1:] + b[:-1]) / 2.0))
+    return 1.0 - diff / (tot if tot != 0 else 1e-15)
+
+
+def ibi_should_stop(values, mode, stop, threshold, window):
+    """IBI::Convergence::shouldStop (IBI.cpp:262-281)."""
+    n = len(values)
+    if stop == "worse":
+        if n < 2:
+            return False
+        prev, last = values[-2], values[-1]
+        if mode == "l2":
+            return not (prev > threshold) and not (prev >= last)
+        return not (prev < threshold) and not (prev <= last)
+    if n < window:
+        return False
+    tail = values[n - window:]
+    return all((v <= threshold) if mode == "l2" else (v >= threshold) for v in tail)
+
+
+def run_ibi(sim, temperature, steps, bins, alpha, steps_equil, steps_measure, conv_mode="integral",
+            conv_stop="worse", conv_threshold=0.99, conv_window=10):
+    """The stock main's Simulation::run (Simulation.cpp:10-80) with the
+    VelocityScaling thermostat and the IBI plugin's post_forces state machine
+    (IBI.cpp:28-118) on an OracleSim (LJ until the first RDF is complete, then
+    the tabulated force alone).  Returns the files IBI writes ({name: (x, y)}),
+    the convergence values, whether the plugin stopped the run and the final
+    step count."""
+    max_r = sim.cutoff
+    nodes = (np.arange(bins) + 0.5) * (max_r / bins)
+    volume = float(np.prod(sim.high - sim.low))
+    st = dict(phase="init", cur=0, it=0, acc=np.zeros(bins), samples=0.0, g0=None, pot=None, conv=[],
+              max_step=steps, stop=False)
+    files = {}
+
+    def rdf():
+        return rdf_profile_normalise(st["acc"], st["samples"], max_r, bins, sim.n_mol, volume)
+
+    def measure():
+        b, _ = sim.rdf_profile(max_r, bins)
+        st["acc"] += b
+        st["samples"] += 1.0
+
+    def set_force():
+        f = ibi_force(nodes, st["pot"])
+        files[f"force_{st['it']}"] = (nodes, f)
+        # IBI.cpp:50-54: the tabulated force replaces every functor (LJ, FENE, Limit)
+        sim.use_lj = sim.use_fene = sim.use_atm = False
+        sim.limit = np.inf
+        sim.table = (nodes.copy(), f, 1e6, 0.0)
+
+    def post_forces(simstep):
+        st["cur"] += 1
+        if st["phase"] == "init":
+            if st["cur"] < steps_measure:
+                measure()
+                return
+            st.update(phase="equil", cur=0, it=0)
+            st["g0"] = rdf()
+            files["rdf_0"] = (nodes, st["g0"])
+            st["acc"][:] = 0.0
+            st["samples"] = 0.0
+            st["pot"] = ibi_initial_potential(st["g0"], temperature)
+            files["pot_0"] = (nodes, st["pot"].copy())
+            set_force()
+        elif st["phase"] == "equil":
+            if st["cur"] < steps_equil:
+                return
+            st.update(phase="measure", cur=0)
+        else:
+            if st["cur"] < steps_measure:
+                measure()
+                return
+            st.update(phase="equil", cur=0)
+            g_i = rdf()
+            st["pot"], upd = ibi_correction(st["pot"], g_i, st["g0"], alpha, temperature)
+            files[f"update_{st['it']}"] = (nodes, upd)
+            st["it"] += 1
+            files[f"pot_{st['it']}"] = (nodes, st["pot"].copy())
+            set_force()
+            files[f"rdf_{st['it']}"] = (nodes, g_i)
+            st["conv"].append(ibi_convergence(conv_mode, nodes, st["g0"], g_i))
+            if ibi_should_stop(st["conv"], conv_mode, conv_stop, conv_threshold, conv_window):
+                st["max_step"] = simstep
+                st["stop"] = True
+                return
+            st["acc"][:] = 0.0
+            st["samples"] = 0.0
+
+    sim.update_container()
+    sim.forces()
+    post_forces(0)
+    sim.thermostat(temperature)
+    simstep = 0
+    while simstep < st["max_step"]:
+        sim.integrate0()
+        sim.update_container()
+        sim.forces()
+        post_forces(simstep)
+        sim.integrate1()
+        simstep += 1
+        sim.thermostat(temperature)
+    if st["pot"] is not None:
+        files["final_pot"] = (nodes, st["pot"].copy())
+    return files, st["conv"], st["stop"], simstep

@@ -2,7 +2,9 @@
 
 The reference harness (oracle/ref/harness.cpp, built by oracle/ref/Makefile
 from the reference's own sources into oracle/_ref/) is fed seeded synthetic
-inputs in KoMD's own input and checkpoint formats; its dumps (positions,
+inputs in KoMD's own input and checkpoint formats (the plugin cases run the
+reference's unmodified stock main, oracle/_ref/komd_ref_main, on whole input
+files); its dumps (positions,
 velocities, forces, cell lists incl. halo copies, neighbour counts,
 temperature, LJ potential, pressure tensor, RDF histogram) are stored as
 compressed .npz files together with the inputs that produced them.
@@ -29,6 +31,7 @@ sys.path.insert(0, ROOT)
 from komd_gb300 import lattice, komd_io  # noqa: E402
 
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "komd_ref_harness")
+STOCK = os.path.join(ROOT, "oracle", "_ref", "komd_ref_main")
 OUT = os.path.dirname(os.path.abspath(__file__))
 EPS_J = 1.0 / lattice.CONV_J_EI          # eps* = 1 as the COMP line's Joule value
 
@@ -125,6 +128,50 @@ def run_case(name, sysm, values, steps, dumps, comps=None, thermostat=False, tab
         shutil.rmtree(tmp, ignore_errors=True)
 
 
+def run_stock(name, sysm, values, comps=None, tables=None):
+    """Runs the reference's unmodified stock main (oracle/_ref/komd_ref_main)
+    on a whole input file (plugins included) and stores every text file it
+    writes (IBI's rdf_/pot_/force_/update_<iteration>.txt, final_pot.txt), the
+    final checkpoint and the IBI convergence log lines."""
+    tmp = tempfile.mkdtemp(prefix=f"komd_golden_{name}_")
+    try:
+        ps = os.path.join(tmp, "in.ps")
+        komd_io.write_checkpoint(ps, sysm)
+        comps = comps or [(0, EPS_J, 1.0, 1.0)]
+        arrays = dict(r0=sysm.r, v0=sysm.v, m=sysm.m, eps=sysm.eps, sig=sysm.sig, mol_id=sysm.mol_id,
+                      low=np.asarray(values["domain_low"], float), high=np.asarray(values["domain_high"], float))
+        for fname, (x, y) in (tables or {}).items():   # FunctionPL files read by the run
+            with open(os.path.join(tmp, fname), "w") as fh:
+                fh.write("\n".join("%.17g\t%.17g" % (a, b) for a, b in zip(x, y)))
+            arrays["in_" + fname.replace(".txt", "")] = np.stack([np.asarray(x), np.asarray(y)], 1)
+        with open(os.path.join(tmp, "in.dat"), "w") as fh:
+            fh.write(komd_io.format_input(values, ps, comps))
+        res = subprocess.run([STOCK, "in.dat"], cwd=tmp, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"{name}: stock main failed\n{res.stdout[-2000:]}\n{res.stderr[-2000:]}")
+        for k, v in values.items():
+            if isinstance(v, (tuple, list)):
+                continue
+            arrays["p_" + k] = np.asarray(v) if not isinstance(v, str) else np.asarray(v)
+        conv = [float(ln.split("value=")[1]) for ln in res.stdout.splitlines() if "[IBI] Convergence: target" in ln]
+        arrays["conv"] = np.asarray(conv, float)
+        arrays["stopped"] = np.int64("stopping criterion reached" in res.stdout)
+        names = sorted(f for f in os.listdir(tmp) if f.endswith(".txt") and f not in (tables or {}))
+        arrays["files"] = np.asarray(names)
+        for f in names:
+            arrays["file_" + f[:-4]] = np.atleast_2d(np.loadtxt(os.path.join(tmp, f)))
+        ck = [f for f in os.listdir(tmp) if f.startswith("ckpt_") and f.endswith(".ps")]
+        if len(ck) != 1:
+            raise RuntimeError(f"{name}: expected one checkpoint, found {ck}")
+        arrays["ckpt_step"] = np.int64(int(ck[0][5:-3]))
+        arrays["ckpt_R"] = komd_io.read_checkpoint(os.path.join(tmp, ck[0]), low=values["domain_low"],
+                                                   high=values["domain_high"]).r
+        np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **arrays)
+        print(f"{name}: n={sysm.n} files={names} ckpt={ck[0]} conv={conv} -> {name}.npz")
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+
+
 def base_values(sysm, cutoff, cell, dt, steps, **kw):
     v = dict(temperature=100.0, delta_t=dt, cutoff=cutoff, cell_size=cell, timesteps=steps, density=0.8,
              limit=1e30, energy_3b=0.0, domain_low=tuple(sysm.low), domain_high=tuple(sysm.high),
@@ -135,8 +182,8 @@ def base_values(sysm, cutoff, cell, dt, steps, **kw):
 
 
 def main(selected):
-    if not os.path.exists(HARNESS):
-        raise SystemExit("build the reference harness first: make -C oracle/ref -j8")
+    if not os.path.exists(HARNESS) or not os.path.exists(STOCK):
+        raise SystemExit("build the reference harness and stock main first: make -C oracle/ref -j8")
     e3b = lattice.nu_star_to_energy_3b(0.073)
 
     def lj864():
@@ -199,7 +246,41 @@ def main(selected):
         y = 24.0 * (2.0 * x ** -13 - x ** -7)
         run_case("ibi864", s, base_values(s, 2.5, 2.5, 0.005, 20), 20, [0, 1, 20], table=(x, y))
 
-    cases = dict(ibi864=ibi864, lj864=lj864, ljatm864=ljatm864, atmlist500=atmlist500, fene375=fene375, edge_box=edge_box,
+    def ibi_values(s, steps, **kw):
+        v = dict(temperature=1.2, delta_t=0.005, cutoff=2.5, cell_size=2.5, timesteps=steps, density=0.8,
+                 limit=1e30, energy_3b=0.0, domain_low=tuple(s.low), domain_high=tuple(s.high), pair_steps=1,
+                 triple_steps=1, write_freq=100000000, enable_3b=0, enable_3b_direct=1, store_checkpoint=1)
+        v.update(kw)
+        return v
+
+    def ibirun864():
+        # the IBI plugin under the stock main: 9 RDF samples with LJ, then
+        # U0 = -T ln g0 as a tabulated force and three correction iterations
+        # (5 equilibration + 10 measurement steps each); integral criterion
+        s = lattice.argon_fcc(6, rho=0.8442, t_star=0.722, seed=19, jitter=0.05)
+        run_stock("ibirun864", s, ibi_values(s, 60, IBI_enable=1, IBI_bins=50, IBI_alpha=0.2, IBI_steps_equil=5,
+                                             IBI_steps_measure=10))
+
+    def ibistop864():
+        # l2 criterion with a 2-iteration window under a loose threshold: the
+        # plugin stops the run after the second iteration (Simulation::stop)
+        s = lattice.argon_fcc(6, rho=0.8442, t_star=0.722, seed=20, jitter=0.05)
+        run_stock("ibistop864", s, ibi_values(s, 80, IBI_enable=1, IBI_bins=40, IBI_alpha=0.3, IBI_steps_equil=4,
+                                              IBI_steps_measure=8, IBI_conv_mode="l2", IBI_conv_stop="window",
+                                              IBI_conv_window=2, IBI_conv_threshold=1e6))
+
+    def ibireload864():
+        # IBI_reload: a tabulated force and potential read from files replace
+        # every functor from the first step (no exclusion zone)
+        s = lattice.argon_fcc(6, rho=0.8442, t_star=0.722, seed=21, jitter=0.05)
+        x = (np.arange(60) + 0.5) * 2.5 / 60
+        f = 24.0 * (2.0 * x ** -13 - x ** -7)
+        u = 4.0 * (x ** -12 - x ** -6)
+        run_stock("ibireload864", s, ibi_values(s, 30, IBI_reload=1, IBI_bins=60, IBI_reload_fpath="force.txt",
+                                                IBI_reload_ppath="pot.txt"),
+                  tables={"force.txt": (x, f), "pot.txt": (x, u)})
+
+    cases = dict(ibirun864=ibirun864, ibistop864=ibistop864, ibireload864=ibireload864, ibi864=ibi864, lj864=lj864, ljatm864=ljatm864, atmlist500=atmlist500, fene375=fene375, edge_box=edge_box,
                  atm2b864=atm2b864, thermo864=thermo864)
     for name in (selected or list(cases)):
         cases[name]()

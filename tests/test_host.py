@@ -114,3 +114,62 @@ def test_viscosity_sensor_matches_restatement(komd_exe, tmp_path, oracle_lib):
     f = oracle_lib.visc_factor(vol, t_target)
     assert float(vals["b"]) == pytest.approx(b * f, rel=1e-4)
     assert float(vals["s"]) == pytest.approx(s * f, rel=1e-4)
+
+
+def _write_stock_case(tmp_path, z, extra=None):
+    """The input file of a stock-main fixture (its p_* keys), the checkpoint and
+    any FunctionPL files the run reads."""
+    from komd_gb300 import komd_io, lattice
+    ps = str(tmp_path / "in.ps")
+    komd_io.write_checkpoint(ps, case_system(z))
+    values = {k[2:]: z[k].item() for k in z if k.startswith("p_")}
+    values.update(domain_low=tuple(z["low"]), domain_high=tuple(z["high"]))
+    values.update(extra or {})
+    for k in z:
+        if k.startswith("in_"):   # "x\ty" per line, no trailing newline
+            (tmp_path / (k[3:] + ".txt")).write_text("\n".join("%.17g\t%.17g" % (a, b) for a, b in z[k]))
+    inp = tmp_path / "in.dat"
+    inp.write_text(komd_io.format_input(values, ps, [(0, 1.0 / lattice.CONV_J_EI, 1.0, 1.0)]))
+    return str(inp)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["ibirun864", "ibistop864", "ibireload864"])
+def test_komd_ibi_plugins_follow_reference(komd_exe, tmp_path, name):
+    """The IBI plugin (RDF sampling on the engine, the tabulated force swapped in
+    through komd_gpu_set_terms / komd_gpu_set_pair_table, corrections and the
+    convergence stop) and IBI_reload, run by `komd` on the stock-main
+    fixtures' inputs: every file IBI writes, the convergence log and the final
+    checkpoint match the reference's (files carry 6 significant digits)."""
+    from komd_gb300 import komd_io
+    z = load_case(name)
+    inp = _write_stock_case(tmp_path, z, extra=dict(gpu_precision="fp64"))
+    out = subprocess.run([komd_exe, inp], capture_output=True, text=True, cwd=tmp_path, timeout=300)
+    assert out.returncode == 0, out.stderr
+    for f in z["files"]:
+        f = str(f)
+        got = np.atleast_2d(np.loadtxt(tmp_path / f))
+        np.testing.assert_allclose(got, z["file_" + f[:-4]], rtol=1e-5, atol=1e-9, err_msg=f)
+        assert not (tmp_path / f).read_text().endswith("\n")
+    conv = [float(ln.split("value=")[1]) for ln in out.stdout.splitlines() if "[IBI] Convergence: target" in ln]
+    np.testing.assert_allclose(conv, z["conv"], rtol=1e-5)
+    assert ("stopping criterion reached" in out.stdout) == bool(z["stopped"])
+    ck = tmp_path / f"ckpt_{int(z['ckpt_step'])}.ps"
+    assert ck.exists()
+    s = komd_io.read_checkpoint(str(ck), low=z["low"], high=z["high"])
+    assert np.abs(s.r - z["ckpt_R"]).max() <= 1e-5 * max(1.0, np.abs(z["ckpt_R"]).max())
+
+
+def test_ibi_parser_checks(komd_exe, tmp_path):
+    """IBI input errors are reported before any GPU use."""
+    base = "cutoff 2.5\ncell_size 2.5\ncheckpoint_file x.ps 0 0 0\nCOMP 0 1e-21 1.0 1.0 0 0 0\n"
+    bad = tmp_path / "bad.dat"
+    bad.write_text(base + "IBI_enable 1\ngpu_skin 0.3")
+    out = subprocess.run([komd_exe, str(bad)], capture_output=True, text=True)
+    assert out.returncode == 1 and "gpu_skin 0" in out.stderr
+    bad.write_text(base + "IBI_enable 1")
+    out = subprocess.run([komd_exe, str(bad), "--fused"], capture_output=True, text=True)
+    assert out.returncode == 1 and "per-step hooks" in out.stderr
+    bad.write_text(base + "ADR_enable 1")
+    out = subprocess.run([komd_exe, str(bad)], capture_output=True, text=True)
+    assert out.returncode == 1 and "AdResS" in out.stderr

@@ -186,3 +186,55 @@ def test_oracle_surrogate_is_consistent(oracle_lib):
         p2[k] -= 2e-6
         e2, _ = oracle_lib.sur_mlp(p2, x)
         assert g[k] == pytest.approx((e1 - e2) / 2e-6, rel=1e-5, abs=1e-8)
+
+
+def _file_close(got, want, name):
+    """IBI's files carry 6 significant digits (FunctionPL::write, default stream format)."""
+    got, want = np.asarray(got, np.float64), np.asarray(want, np.float64)
+    assert got.shape == want.shape, name
+    np.testing.assert_allclose(got, want, rtol=1e-5, atol=1e-9, err_msg=name)
+
+
+@pytest.mark.parametrize("name", ["ibirun864", "ibistop864"])
+def test_oracle_ibi_plugin_matches_stock_main(oracle_lib, name):
+    """The oracle's restatement of the IBI plugin (RDF sampling, U0 = -T ln g0,
+    corrections, F = -dU/dr, convergence and stopping) under the stock main's
+    loop with the VelocityScaling thermostat, against the files, the
+    convergence log and the final checkpoint of the reference's own stock main."""
+    z = load_case(name)
+    sim = _sim(oracle_lib, z)
+    gs = lambda k, d: z[k].item() if k in z else d   # noqa: E731
+    files, conv, stopped, steps = oracle_lib.run_ibi(
+        sim, float(z["p_temperature"]), int(z["p_timesteps"]), int(z["p_IBI_bins"]), float(z["p_IBI_alpha"]),
+        int(z["p_IBI_steps_equil"]), int(z["p_IBI_steps_measure"]), conv_mode=str(gs("p_IBI_conv_mode", "integral")),
+        conv_stop=str(gs("p_IBI_conv_stop", "worse")), conv_threshold=float(gs("p_IBI_conv_threshold", 0.99)),
+        conv_window=int(gs("p_IBI_conv_window", 10)))
+    assert sorted(files) == sorted(str(f)[:-4] for f in z["files"])
+    for k, (x, y) in files.items():
+        _file_close(np.stack([x, y], 1), z["file_" + k], f"{name}: {k}.txt")
+    np.testing.assert_allclose(conv, z["conv"], rtol=1e-5)
+    assert bool(stopped) == bool(z["stopped"])
+    assert steps == int(z["ckpt_step"])
+    assert np.abs(sim.r - z["ckpt_R"]).max() <= 1e-5 * max(1.0, np.abs(z["ckpt_R"]).max())
+
+
+def test_oracle_ibi_reload_matches_stock_main(oracle_lib):
+    """IBI_reload: the tabulated force read from a file replaces every functor."""
+    z = load_case("ibireload864")
+    sim = _sim(oracle_lib, z)
+    f = z["in_force"]
+    sim.use_lj = sim.use_fene = False
+    sim.limit = np.inf
+    sim.table = (f[:, 0].copy(), f[:, 1].copy(), 1e6, 0.0)
+    t = float(z["p_temperature"])
+    sim.update_container()
+    sim.forces()
+    sim.thermostat(t)
+    for _ in range(int(z["p_timesteps"])):
+        sim.integrate0()
+        sim.update_container()
+        sim.forces()
+        sim.integrate1()
+        sim.thermostat(t)
+    assert int(z["ckpt_step"]) == int(z["p_timesteps"])
+    assert np.abs(sim.r - z["ckpt_R"]).max() <= 1e-5 * max(1.0, np.abs(z["ckpt_R"]).max())
