@@ -2,6 +2,7 @@
 // the host layer (komd_host.h), restated from the reference's behaviour.
 #include <cmath>
 #include <fstream>
+#include <iomanip>
 #include <iostream>
 #include <sstream>
 #include <stdexcept>
@@ -156,6 +157,7 @@ bool FileInput::readFile(const std::string &filename) {
             else if (var == "gpu_atm2b") c.gpu_atm2b_physical = mode(v, "compat", 0, "physical", 1, ok) != 0;
             else if (var == "gpu_skin") c.gpu_skin = std::stod(v);
             else if (var == "gpu_device") c.gpu_device = std::stoi(v);
+            else if (var == "gpu_vtk") c.gpu_vtk = std::stoi(v) != 0;
             if (!ok) { std::cerr << "invalid value for " << var << ": " << v << std::endl; return false; }
         }
         // unknown tokens are skipped, as in the reference
@@ -202,6 +204,54 @@ void CheckpointIO::writeCheckpoint(uint64_t simstep) {
             file << m.id << "\t" << r[0] << " " << r[1] << " " << r[2] << "\t" << v[0] << " " << v[1] << " " << v[2]
                  << "\t" << m.mass[q] << " " << m.eps[q] << " " << m.sig[q];
         }
+}
+
+void VTKWriter::write(const std::string &filename, uint64_t iteration) {
+    if (!Registry::instance->configuration()->gpu_vtk) return;
+    auto container = Registry::instance->moleculeContainer();
+    container->syncHost();
+    std::stringstream name;
+    name << filename << "_" << std::setfill('0') << std::setw(4) << iteration << ".vtu";
+    std::ofstream file(name.str());
+    if (!file.is_open()) {
+        std::cerr << "Could not write VTK file: " << name.str() << std::endl;
+        return;
+    }
+    const auto &mols = container->molecules();
+    const uint64_t n = container->getNumSites();
+    file << std::setprecision(std::numeric_limits<float>::max_digits10);
+    auto array = [&](const char *type, const char *nm, int comps, auto &&emit) {
+        file << "      <DataArray type=\"" << type << "\" Name=\"" << nm << "\" NumberOfComponents=\"" << comps
+             << "\" format=\"ascii\">";
+        emit();
+        file << "</DataArray>\n";
+    };
+    auto sites3 = [&](const std::vector<d3> &a) {
+        for (uint64_t i = 0; i < n; i++) file << (float)a[i][0] << " " << (float)a[i][1] << " " << (float)a[i][2] << " ";
+    };
+    file << "<?xml version=\"1.0\" encoding=\"UTF-8\"?>\n"
+         << "<VTKFile type=\"UnstructuredGrid\" version=\"0.1\" byte_order=\"LittleEndian\">\n"
+         << "  <UnstructuredGrid>\n"
+         << "    <Piece NumberOfPoints=\"" << n << "\" NumberOfCells=\"0\">\n"
+         << "    <PointData>\n";
+    array("Float32", "mass", 1, [&]() {
+        for (const Molecule &m : mols)
+            for (double q : m.mass) file << (float)q << " ";
+    });
+    array("Float32", "velocity", 3, [&]() { sites3(container->v); });
+    array("Float32", "force", 3, [&]() { sites3(container->f); });
+    array("Int32", "id", 1, [&]() {
+        for (const Molecule &m : mols)
+            for (size_t q = 0; q < m.r.size(); q++) file << (int32_t)m.id << " ";
+    });
+    array("Int32", "cid", 1, [&]() {   // checkpoint-loaded molecules carry no component id
+        for (uint64_t i = 0; i < n; i++) file << 0 << " ";
+    });
+    file << "    </PointData>\n    <CellData/>\n    <Points>\n";
+    array("Float32", "points", 3, [&]() { sites3(container->r); });
+    file << "    </Points>\n    <Cells>\n";
+    array("Float32", "types", 0, [&]() {});
+    file << "    </Cells>\n    </Piece>\n  </UnstructuredGrid>\n</VTKFile>\n";
 }
 
 bool CheckpointIO::loadCheckpoint() {
@@ -256,6 +306,7 @@ void Simulation::run(bool fused) {
     for (auto &p : plugins) p->pre_container_update();
     container->updateContainer();
     for (auto &p : plugins) p->post_container_update();
+    VTKWriter::write("VTK_Output", 0);
     for (auto &f : R.forceFunctors()) (*f)();
     if (config->enable_3b)
         for (auto &f : R.forceFunctors3b()) (*f)();
@@ -283,6 +334,7 @@ void Simulation::run(bool fused) {
             std::cout << "Simstep=" << simstep_ - 1 << " t=" << t - dt << " T=" << temp->getTemperature();
             if (pot) std::cout << " u=" << pot->getCurrentPotential();
             std::cout << std::endl;
+            if (simstep_ % write_freq == 0) VTKWriter::write("VTK_Output", simstep_);
             if (simstep_ % write_freq == 0)
                 for (auto &s : R.sensors()) s->write(simstep_);
         }
@@ -304,6 +356,7 @@ void Simulation::run(bool fused) {
             std::cout << std::endl;
             t += dt;
             simstep_++;
+            if (simstep_ % write_freq == 0) VTKWriter::write("VTK_Output", simstep_);
             if (simstep_ % write_freq == 0)
                 for (auto &s : R.sensors()) s->write(simstep_);
             for (auto &th : R.thermostats()) th->apply();

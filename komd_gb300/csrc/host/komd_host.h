@@ -90,6 +90,7 @@ struct Configuration {
     double gpu_skin = 0.0;                          // gpu_skin <float>
     int gpu_device = 0;                             // gpu_device <int>
     bool gpu_atm2b_physical = false;                // gpu_atm2b physical: ATM2B factor from the loaded density
+    bool gpu_vtk = false;                           // gpu_vtk 1: VTK_Output_<step>.vtu as a USE_VTK build writes
 };
 
 struct SiteDesc {
@@ -254,6 +255,14 @@ private:
 namespace FileInput {
 // IO/FileInput.cpp:13-121: the same keys, checks and messages; false on error
 bool readFile(const std::string &filename);
+}
+
+namespace VTKWriter {
+// IO/VTKWriter.cpp:21-123: one .vtu per call (<name>_<4-digit iteration>.vtu),
+// sites in molecule order with mass, velocity, force, id, cid as Float32 /
+// Int32 point data; the reference writes only when built with USE_VTK, here
+// only with gpu_vtk 1
+void write(const std::string &filename, uint64_t iteration);
 }
 
 namespace CheckpointIO {

@@ -173,3 +173,52 @@ def rdf_normalise(bins: np.ndarray, samples: int, dr: float, volume: float, n: i
     r = (np.arange(b.size) + 0.5) * dr
     v_bin = 4.0 / 3.0 * math.pi * ((r + 0.5 * dr) ** 3 - (r - 0.5 * dr) ** 3)
     return r, b * volume / (v_bin * n * (n - 1.0))
+
+
+_VTU_ARRAYS = (("mass", "Float32", 1), ("velocity", "Float32", 3), ("force", "Float32", 3), ("id", "Int32", 1),
+               ("cid", "Int32", 1))
+
+
+def write_vtu(path: str, sysm: System, f=None, cid=None) -> None:
+    """VTK UnstructuredGrid (.vtu, ASCII) of a snapshot with the arrays of
+    KoMD's VTKWriter (IO/VTKWriter.cpp:44-123): points, and per site mass,
+    velocity, force (Float32) and molecule id and component id (Int32).  The
+    same layout as the `komd` executable's VTK_Output_<step>.vtu."""
+    n = sysm.n
+    f = np.zeros((n, 3)) if f is None else np.asarray(f)
+    cid = np.zeros(n, np.int64) if cid is None else np.asarray(cid)
+    cols = dict(mass=sysm.m, velocity=sysm.v, force=f, id=sysm.mol_id.astype(np.int64), cid=cid)
+
+    def arr(name, typ, comps, data):
+        a = np.asarray(data).reshape(-1)
+        body = " ".join(repr(float(np.float32(x))) if typ == "Float32" else str(int(x)) for x in a)
+        return (f'      <DataArray type="{typ}" Name="{name}" NumberOfComponents="{comps}" format="ascii">'
+                f"{body + ' ' if body else ''}</DataArray>\n")
+
+    out = ['<?xml version="1.0" encoding="UTF-8"?>\n',
+           '<VTKFile type="UnstructuredGrid" version="0.1" byte_order="LittleEndian">\n',
+           "  <UnstructuredGrid>\n", f'    <Piece NumberOfPoints="{n}" NumberOfCells="0">\n', "    <PointData>\n"]
+    out += [arr(nm, t, c, cols[nm]) for nm, t, c in _VTU_ARRAYS]
+    out += ["    </PointData>\n    <CellData/>\n    <Points>\n", arr("points", "Float32", 3, sysm.r),
+            "    </Points>\n    <Cells>\n", arr("types", "Float32", 0, []),
+            "    </Cells>\n    </Piece>\n  </UnstructuredGrid>\n</VTKFile>\n"]
+    with open(path, "w") as fh:
+        fh.write("".join(out))
+
+
+def read_vtu(path: str) -> Dict[str, np.ndarray]:
+    """The point arrays of an ASCII .vtu written by write_vtu or `komd`
+    ({"points": (n, 3), "mass": (n,), "velocity": (n, 3), ...})."""
+    import xml.etree.ElementTree as ET
+    root = ET.parse(path).getroot()
+    piece = root.find("UnstructuredGrid/Piece")
+    n = int(piece.get("NumberOfPoints"))
+    out = {}
+    for da in piece.iter("DataArray"):
+        comps = int(da.get("NumberOfComponents"))
+        if comps == 0:
+            continue
+        dt = np.float32 if da.get("type") == "Float32" else np.int64
+        vals = np.array((da.text or "").split(), dtype=np.float64).astype(dt)
+        out[da.get("Name")] = vals.reshape(n, comps) if comps > 1 else vals.reshape(n)
+    return out

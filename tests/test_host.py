@@ -173,3 +173,26 @@ def test_ibi_parser_checks(komd_exe, tmp_path):
     bad.write_text(base + "ADR_enable 1")
     out = subprocess.run([komd_exe, str(bad)], capture_output=True, text=True)
     assert out.returncode == 1 and "AdResS" in out.stderr
+
+
+@pytest.mark.gpu
+def test_komd_vtk_output(komd_exe, tmp_path):
+    """gpu_vtk 1: VTK_Output_<step>.vtu at step 0 (after the first container
+    update, forces still zero) and every write_freq steps, sites in molecule
+    order; the last one holds the final checkpoint's state in Float32."""
+    from komd_gb300 import komd_io
+    z = load_case("thermo864")
+    inp = _write_case(tmp_path, z, extra=dict(gpu_precision="fp64", gpu_vtk=1, write_freq=25))
+    out = subprocess.run([komd_exe, inp], capture_output=True, text=True, cwd=tmp_path, timeout=300)
+    assert out.returncode == 0, out.stderr
+    assert sorted(p.name for p in tmp_path.glob("VTK_Output_*.vtu")) == [
+        "VTK_Output_0000.vtu", "VTK_Output_0025.vtu", "VTK_Output_0050.vtu"]
+    d0 = komd_io.read_vtu(str(tmp_path / "VTK_Output_0000.vtu"))
+    assert np.array_equal(d0["points"], z["r0"].astype(np.float32))
+    assert np.array_equal(d0["velocity"], z["v0"].astype(np.float32))
+    assert not d0["force"].any()
+    assert np.array_equal(d0["id"], z["mol_id"].astype(np.int64))
+    d50 = komd_io.read_vtu(str(tmp_path / "VTK_Output_0050.vtu"))
+    ck = komd_io.read_checkpoint(str(tmp_path / "ckpt_50.ps"), low=z["low"], high=z["high"])
+    np.testing.assert_allclose(d50["points"], ck.r, rtol=1e-5, atol=1e-5)
+    assert np.isfinite(d50["force"]).all() and np.abs(d50["force"]).max() > 0

@@ -69,3 +69,19 @@ def test_autotune_cell_edge():
     assert autotune.cell_for(10.0, 2.5) == pytest.approx(2.5)
     with pytest.raises(ValueError):
         autotune.cell_for(7.0, 2.5)
+
+
+def test_vtu_round_trip(tmp_path):
+    """write_vtu / read_vtu: KoMD's VTKWriter arrays as Float32 / Int32."""
+    from komd_gb300 import komd_io, lattice
+    s = lattice.argon_fcc(2, seed=3)
+    f = np.random.default_rng(0).normal(size=(s.n, 3))
+    p = tmp_path / "VTK_Output_0007.vtu"
+    komd_io.write_vtu(str(p), s, f=f)
+    d = komd_io.read_vtu(str(p))
+    assert np.array_equal(d["points"], s.r.astype(np.float32))
+    assert np.array_equal(d["velocity"], s.v.astype(np.float32))
+    assert np.array_equal(d["force"], f.astype(np.float32))
+    assert np.array_equal(d["mass"], s.m.astype(np.float32))
+    assert np.array_equal(d["id"], s.mol_id.astype(np.int64))
+    assert not d["cid"].any()
