@@ -1346,48 +1346,48 @@ __device__ __forceinline__ int atm_stage(const AtmParams &p, int i, float4 *se, 
 // the round-robin sweep of one vertex: lane li = lane - gb owns staged
 // neighbour li < m and plays rounds d = d_first .. d_last (at most m/2) over
 // `rounds` loop trips (rounds past d_last do nothing); the lane's partial sum
-// for its neighbour is returned in (ax, ay, az)
+// for its neighbour is returned in (ax, ay, az).  The vertex's own share is
+// not summed here: per triplet g_i = -(g_a + g_b), so the vertex force is
+// minus the sum of its neighbours' shares.
 __device__ __forceinline__ void atm_sweep(const float4 *se, const float4 *sq, int m, int li, int gb, int d_first,
-                                          int d_last, int rounds, float rc2, float &gx, float &gy, float &gz,
-                                          float &ax, float &ay, float &az, float4 &ea_out) {
+                                          int d_last, int rounds, float rc2, float &ax, float &ay, float &az,
+                                          float4 &ea_out) {
     const bool own = li < m;
     const float4 ea = own ? se[li] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 qa = own ? sq[li] : make_float4(1.f, 1.f, 1.f, 0.f);
     ea_out = ea;
+    // partner b = li + d and share source li - d (mod m), stepped per round;
+    // d <= m/2 keeps both within one wrap
+    int b = li + d_first, src = li - d_first;
+    if (b >= m) b -= m;
+    if (src < 0) src += m;
     for (int t = 0; t < rounds; t++) {
         const int d = d_first + t;
         const bool act = own && d <= d_last;
         float bx = 0.f, by = 0.f, bz = 0.f;
         if (act && !(2 * d == m && li >= d)) {
-            int b = li + d;
-            if (b >= m) b -= m;
             const float4 eb = se[b];
             const float cx = eb.x - ea.x, cy = eb.y - ea.y, cz = eb.z - ea.z;
             const float C = cx * cx + cy * cy + cz * cz;
             if (C <= rc2) {
                 const AtmV v = atm_derivs(qa, sq[b], C);
-                gx += v.vA * ea.x + v.vB * eb.x;
-                gy += v.vA * ea.y + v.vB * eb.y;
-                gz += v.vA * ea.z + v.vB * eb.z;
-                ax += v.vC * cx - v.vA * ea.x;
-                ay += v.vC * cy - v.vA * ea.y;
-                az += v.vC * cz - v.vA * ea.z;
-                bx = -v.vC * cx - v.vB * eb.x;
-                by = -v.vC * cy - v.vB * eb.y;
-                bz = -v.vC * cz - v.vB * eb.z;
+                const float tx = v.vC * cx, ty = v.vC * cy, tz = v.vC * cz;
+                ax += tx - v.vA * ea.x;
+                ay += ty - v.vA * ea.y;
+                az += tz - v.vA * ea.z;
+                bx = -tx - v.vB * eb.x;
+                by = -ty - v.vB * eb.y;
+                bz = -tz - v.vB * eb.z;
             }
         }
         // lane li pulls the share computed, in this lane group, by the lane whose partner it was
-        int src = li;               // lanes without a round pull from themselves
-        if (act) {
-            src = li - d;           // d <= m/2: one wrap at most
-            if (src < 0) src += m;
-        }
-        src += gb;
-        const float rx = __shfl_sync(0xffffffffu, bx, src);
-        const float ry = __shfl_sync(0xffffffffu, by, src);
-        const float rz = __shfl_sync(0xffffffffu, bz, src);
+        const int s = (act ? src : li) + gb;   // lanes without a round pull from themselves
+        const float rx = __shfl_sync(0xffffffffu, bx, s);
+        const float ry = __shfl_sync(0xffffffffu, by, s);
+        const float rz = __shfl_sync(0xffffffffu, bz, s);
         if (act) { ax += rx; ay += ry; az += rz; }
+        b = b + 1 == m ? 0 : b + 1;
+        src = src == 0 ? m - 1 : src - 1;
     }
 }
 
@@ -1448,24 +1448,21 @@ __global__ void __launch_bounds__(kBlock) k_atm_s(AtmParams p) {
             const int g = lane >> 4, li = lane & 15;
             const int h1 = (half + 1) / 2;                     // rounds of the lower half-warp
             const int d_first = g ? h1 + 1 : 1, d_last = g ? half : h1;
-            atm_sweep(se, sq, m, li, 16 * g, d_first, d_last, h1, rc2, gx, gy, gz, ax, ay, az, ea);
+            atm_sweep(se, sq, m, li, 16 * g, d_first, d_last, h1, rc2, ax, ay, az, ea);
             ax += __shfl_xor_sync(0xffffffffu, ax, 16);
             ay += __shfl_xor_sync(0xffffffffu, ay, 16);
             az += __shfl_xor_sync(0xffffffffu, az, 16);
-            if (lane < m) {
-                unsigned long long *acc = p.acc + 3 * (size_t)(__float_as_int(ea.w) >> 6);
-                atm_fix_add(acc, ax);
-                atm_fix_add(acc + 1, ay);
-                atm_fix_add(acc + 2, az);
-            }
         } else {
-            atm_sweep(se, sq, m, lane, 0, 1, half, half, rc2, gx, gy, gz, ax, ay, az, ea);
-            if (lane < m) {
-                unsigned long long *acc = p.acc + 3 * (size_t)(__float_as_int(ea.w) >> 6);
-                atm_fix_add(acc, ax);
-                atm_fix_add(acc + 1, ay);
-                atm_fix_add(acc + 2, az);
-            }
+            atm_sweep(se, sq, m, lane, 0, 1, half, half, rc2, ax, ay, az, ea);
+        }
+        if (lane < m) {
+            unsigned long long *acc = p.acc + 3 * (size_t)(__float_as_int(ea.w) >> 6);
+            atm_fix_add(acc, ax);
+            atm_fix_add(acc + 1, ay);
+            atm_fix_add(acc + 2, az);
+            gx = -ax;
+            gy = -ay;
+            gz = -az;
         }
     } else {
         atm_pairs_slow(p, se, sq, m, lane, rc2, gx, gy, gz);

@@ -391,15 +391,18 @@ __global__ void __launch_bounds__(kTileThreads) k_vlist_build(PairParams p) {
 // order.  No atomics: the warp owns its site.
 // ---------------------------------------------------------------------------
 template <bool MEASURE, bool EMIT, bool UNIFORM>
-__global__ void __launch_bounds__(256, 5) k_lj_vlist(PairParams p, int n) {
+__global__ void __launch_bounds__(256, 5) k_lj_vlist(PairParams p, int n, int per) {
     __shared__ double s_part[8][8];
     constexpr int U = 2;   // list entries per lane in flight: independent loads for latency hiding
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int i = blockIdx.x * 8 + w;
     const float rc2 = (float)p.rc2, rc3sq = (float)p.rc3sq;
     unsigned lt;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
     float m_u = 0.f, m_pairs = 0.f, m_w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    // each block walks `per` consecutive groups of 8 slots: neighbouring slots share
+    // most of their neighbours, so the gathers of one group hit L1 lines of the last
+    for (int it = 0; it < per; it++) {
+    const int i = (blockIdx.x * per + it) * 8 + w;
     if (i < n) {
         const int cnt = p.vl_count[i];
         const float4 pi = p.pos4[i];
@@ -500,6 +503,7 @@ __global__ void __launch_bounds__(256, 5) k_lj_vlist(PairParams p, int n) {
             }
         }
     }
+    }
     if (MEASURE) {
         double vals[8] = {m_u, m_w[0], m_w[1], m_w[2], m_w[3], m_w[4], m_w[5], m_pairs};
         for (int k = 0; k < 8; k++) {
@@ -525,26 +529,36 @@ __global__ void __launch_bounds__(256, 5) k_lj_vlist(PairParams p, int n) {
 
 int vlist_grid(const Engine &e) { return (int)((e.n + 7) / 8); }
 
+// groups of 8 slots per block of the force pass: about eight resident waves of
+// blocks (5 per SM), each over a contiguous range of slots
+int vlist_per(const Engine &e) {
+    const int groups = vlist_grid(e);
+    const int target = 152 * 5 * 8;
+    return groups <= target ? 1 : (groups + target - 1) / target;
+}
+
 void launch_vlist_build(Engine &e, cudaStream_t st) {
     PairParams p = pair_params(e);
     k_vlist_build<<<e.g.ncell, kTileThreads, 0, st>>>(p);
 }
 
 template <bool UNIFORM>
-static void lj_vlist_dispatch(PairParams &p, int n, int grid, bool measure, bool emit, cudaStream_t st) {
+static void lj_vlist_dispatch(PairParams &p, int n, int grid, int per, bool measure, bool emit, cudaStream_t st) {
     if (measure) {
-        if (emit) k_lj_vlist<true, true, UNIFORM><<<grid, 256, 0, st>>>(p, n);
-        else k_lj_vlist<true, false, UNIFORM><<<grid, 256, 0, st>>>(p, n);
+        if (emit) k_lj_vlist<true, true, UNIFORM><<<grid, 256, 0, st>>>(p, n, per);
+        else k_lj_vlist<true, false, UNIFORM><<<grid, 256, 0, st>>>(p, n, per);
     } else {
-        if (emit) k_lj_vlist<false, true, UNIFORM><<<grid, 256, 0, st>>>(p, n);
-        else k_lj_vlist<false, false, UNIFORM><<<grid, 256, 0, st>>>(p, n);
+        if (emit) k_lj_vlist<false, true, UNIFORM><<<grid, 256, 0, st>>>(p, n, per);
+        else k_lj_vlist<false, false, UNIFORM><<<grid, 256, 0, st>>>(p, n, per);
     }
 }
 
 int launch_lj_vlist(Engine &e, PairParams &p, bool measure, bool emit, cudaStream_t st) {
-    const int grid = vlist_grid(e);
-    if (e.uniform) lj_vlist_dispatch<true>(p, (int)e.n, grid, measure, emit, st);
-    else lj_vlist_dispatch<false>(p, (int)e.n, grid, measure, emit, st);
+    // the measure pass keeps one group per block (its partial sums are per block)
+    const int per = measure ? 1 : vlist_per(e);
+    const int grid = (vlist_grid(e) + per - 1) / per;
+    if (e.uniform) lj_vlist_dispatch<true>(p, (int)e.n, grid, per, measure, emit, st);
+    else lj_vlist_dispatch<false>(p, (int)e.n, grid, per, measure, emit, st);
     return grid;
 }
 
