@@ -305,12 +305,11 @@ int ensure_posd(komd_gpu *h) {
 int alloc_verlet(komd_gpu *h, int cap) {
     Engine &e = h->e;
     e.vl_cap = cap;
-    CK(dalloc(e.img, e.n));
-    CK(dalloc(e.ref, 3 * (size_t)e.n));
+    CK(dalloc(e.bias, 3 * (size_t)e.n));
+    CK(dalloc(e.ref4, e.n));
     CK(dalloc(e.slot_cell, e.n));
     CK(dalloc(e.vl, (size_t)cap * (size_t)e.n));
     CK(dalloc(e.vl_count, e.n));
-    CK(cudaMemset(e.img, 0, sizeof(char4) * e.n));
     if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
     e.graph_valid = false;
     return KOMD_OK;
@@ -475,7 +474,7 @@ int komd_gpu_destroy(komd_gpu *h) {
     dfree(e.nl); dfree(e.nl_count); dfree(e.bonds); dfree(e.angles); dfree(e.partials); dfree(e.err);
     dfree(e.tab_x); dfree(e.tab_y); dfree(e.atm_acc);
     dfree(e.rdf); dfree(e.lj_hist); dfree(e.counts); dfree(h->f_scratch); dfree(h->prof); dfree(h->acc); dfree(h->thermo_acc); dfree(e.offtab);
-    dfree(e.nboff); dfree(e.rebuild); dfree(e.img); dfree(e.ref); dfree(e.slot_cell); dfree(e.vl); dfree(e.vl_count);
+    dfree(e.nboff); dfree(e.rebuild); dfree(e.bias); dfree(e.ref4); dfree(e.slot_cell); dfree(e.vl); dfree(e.vl_count);
     dfree(e.rebuild_count); dfree(e.hdtm); dfree(e.exact_com);
     {
         Surrogate &u = h->sur;

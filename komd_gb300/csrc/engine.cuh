@@ -240,8 +240,11 @@ struct Engine {
     // Verlet list of the physics path (FP32, no FENE, FULL ATM, CORRECT virial, skin > 0)
     bool verlet = false;
     int *rebuild = nullptr;      // device flag: rebuild cells and list in this step
-    char4 *img = nullptr;        // per site: periodic wraps since the last rebuild
-    double *ref = nullptr;       // per site: position at the last rebuild (3 doubles)
+    // per site: bias such that (float)(r - bias) is the FP32 position relative to
+    // the centre of the slot's build cell (the build cell centre plus the periodic
+    // shifts applied since the build; 3 doubles)
+    double *bias = nullptr;
+    float4 *ref4 = nullptr;      // per site: that FP32 position at the last rebuild
     int *slot_cell = nullptr;    // per slot: its cell at the last rebuild
     float4 *nboff = nullptr;     // per cell x 27: home-relative neighbour-cell offset, w = 1 for an image
     unsigned *vl = nullptr;      // vl_cap entries per slot: same-molecule bit 31 | nb << 26 | slot

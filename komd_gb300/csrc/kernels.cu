@@ -21,7 +21,7 @@ namespace komd {
 __global__ void k_com_wrap_bin(Grid g, int n_mol, const int *__restrict__ mol_off, double *__restrict__ r,
                                const double *__restrict__ m, double *__restrict__ com, int *__restrict__ mol_cell,
                                int *__restrict__ mol_rank, int *__restrict__ cell_count, int *__restrict__ cell_mcount,
-                               char4 *__restrict__ img, const int *__restrict__ rebuild,
+                               double *__restrict__ bias, const int *__restrict__ rebuild,
                                const unsigned char *__restrict__ exact_com, int wrapped) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n_mol) return;
@@ -60,14 +60,9 @@ __global__ void k_com_wrap_bin(Grid g, int n_mol, const int *__restrict__ mol_of
                 r[3 * s + d] = x;
                 c2[d] = dadd(c2[d], dmul(x, ms));
             }
-            if (img) {
-                // continuous position r - img * L is unchanged by the wrap
-                char4 q = img[s];
-                q.x += (off[0] > 0.0) - (off[0] < 0.0);
-                q.y += (off[1] > 0.0) - (off[1] < 0.0);
-                q.z += (off[2] > 0.0) - (off[2] < 0.0);
-                img[s] = q;
-            }
+            if (bias)   // the cell-local position r - bias is unchanged by the wrap
+                for (int d = 0; d < 3; d++)
+                    if (off[d] != 0.0) bias[3 * s + d] = dadd(bias[3 * s + d], off[d]);
         }
         if (s1 - s0 == 1 && exact_com && exact_com[k]) {
             for (int d = 0; d < 3; d++) c[d] = r[3 * s0 + d];
@@ -150,8 +145,8 @@ __global__ void __launch_bounds__(kBlock) k_cell_sort(Grid g, const int *__restr
                                                       int *__restrict__ site_slot, float4 *__restrict__ pos4,
                                                       int *__restrict__ skey, float *__restrict__ seps,
                                                       double *__restrict__ posd, double *__restrict__ seps_d,
-                                                      double *__restrict__ sig_d, char4 *__restrict__ img,
-                                                      double *__restrict__ ref, int *__restrict__ slot_cell,
+                                                      double *__restrict__ sig_d, double *__restrict__ bias,
+                                                      float4 *__restrict__ ref4, int *__restrict__ slot_cell,
                                                       const int *__restrict__ rebuild) {
     const int lane = threadIdx.x & 31;
     const int cell = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
@@ -176,13 +171,14 @@ __global__ void __launch_bounds__(kBlock) k_cell_sort(Grid g, const int *__restr
                 slot_site[slot] = s;
                 site_slot[s] = slot;
                 const double x = r[3 * s], y = r[3 * s + 1], z = r[3 * s + 2];
-                pos4[slot] = make_float4(__double2float_rn(x - cen[0]), __double2float_rn(y - cen[1]),
-                                         __double2float_rn(z - cen[2]), __double2float_rn(0.5 * sig[s]));
+                const float4 p4 = make_float4(__double2float_rn(x - cen[0]), __double2float_rn(y - cen[1]),
+                                              __double2float_rn(z - cen[2]), __double2float_rn(0.5 * sig[s]));
+                pos4[slot] = p4;
                 skey[slot] = key[s];
                 seps[slot] = __double2float_rn(sqrt(eps[s]));
-                if (img) {
-                    img[s] = make_char4(0, 0, 0, 0);
-                    ref[3 * s] = x; ref[3 * s + 1] = y; ref[3 * s + 2] = z;
+                if (bias) {
+                    bias[3 * s] = cen[0]; bias[3 * s + 1] = cen[1]; bias[3 * s + 2] = cen[2];
+                    ref4[s] = p4;
                     slot_cell[slot] = cell;
                 }
                 if (posd) {
@@ -840,13 +836,13 @@ __global__ void k_limit(int n, const double *__restrict__ eps, const double *__r
 // ===========================================================================
 // velocity Verlet (Integrator.cpp:28-37), FP64 without contraction
 // ===========================================================================
-// With a Verlet list (ref != nullptr) it also flags a rebuild when a site's
-// continuous position r - img*L has moved more than skin/2 since the build.
+// With a Verlet list (bias != nullptr) it also flags a rebuild when a site's
+// cell-local position r - bias has moved more than skin/2 since the build.
 // hdtm[s] = (dt * 0.5) / m[s], the reference's dtInv2m (Integrator.cpp:29), computed
 // once at upload with the same IEEE division
 __global__ void k_step0(int n, double *__restrict__ r, double *__restrict__ v, const double *__restrict__ f,
                         const double *__restrict__ hdtm, double dt, Grid g,
-                        const char4 *__restrict__ img, const double *__restrict__ ref, float half_skin2,
+                        const double *__restrict__ bias, const float4 *__restrict__ ref4, float half_skin2,
                         int *__restrict__ rebuild) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
@@ -858,43 +854,38 @@ __global__ void k_step0(int n, double *__restrict__ r, double *__restrict__ v, c
         x[d] = dadd(r[3 * s + d], dmul(vv, dt));
         r[3 * s + d] = x[d];
     }
-    if (ref) {
-        const char4 q = img[s];
-        const float dx = (float)(x[0] - ref[3 * s]) - (float)q.x * (float)g.L[0];
-        const float dy = (float)(x[1] - ref[3 * s + 1]) - (float)q.y * (float)g.L[1];
-        const float dz = (float)(x[2] - ref[3 * s + 2]) - (float)q.z * (float)g.L[2];
+    if (bias) {
+        const float4 q = ref4[s];
+        const float dx = __double2float_rn(dsub(x[0], bias[3 * s])) - q.x;
+        const float dy = __double2float_rn(dsub(x[1], bias[3 * s + 1])) - q.y;
+        const float dz = __double2float_rn(dsub(x[2], bias[3 * s + 2])) - q.z;
         if (dx * dx + dy * dy + dz * dz > half_skin2) *rebuild = 1;
     }
 }
 
 // Verlet path with single-site molecules whose COM is exactly the position
 // (power-of-two masses): integrate0, the skin test, the periodic wrap with
-// its image counters and COM (k_com_wrap_bin's operations) and the FP32
+// its bias update and COM (k_com_wrap_bin's operations) and the FP32
 // cell-local refresh (k_refresh's) in one pass over the sites.  The
 // results are those of the separate kernels; on a rebuild step the cell sort
 // rewrites pos4 afterwards.
 __global__ void k_step0_fused(int n, double *__restrict__ r, double *__restrict__ v, const double *__restrict__ f,
-                              const double *__restrict__ hdtm, double dt, Grid g, char4 *__restrict__ img,
-                              const double *__restrict__ ref, float half_skin2, int *__restrict__ rebuild,
+                              const double *__restrict__ hdtm, double dt, Grid g, double *__restrict__ bias,
+                              const float4 *__restrict__ ref4, float half_skin2, int *__restrict__ rebuild,
                               double *__restrict__ com, const int *__restrict__ site_slot,
-                              const int *__restrict__ slot_cell, float4 *__restrict__ pos4) {
+                              float4 *__restrict__ pos4) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const double c = hdtm[s];
-    double x[3];
+    double x[3], b[3];
     for (int d = 0; d < 3; d++) {
         const double vv = dadd(v[3 * s + d], dmul(f[3 * s + d], c));
         v[3 * s + d] = vv;
         x[d] = dadd(r[3 * s + d], dmul(vv, dt));
+        b[d] = bias[3 * s + d];
     }
-    char4 q = img[s];
-    {
-        const float dx = (float)(x[0] - ref[3 * s]) - (float)q.x * (float)g.L[0];
-        const float dy = (float)(x[1] - ref[3 * s + 1]) - (float)q.y * (float)g.L[1];
-        const float dz = (float)(x[2] - ref[3 * s + 2]) - (float)q.z * (float)g.L[2];
-        if (dx * dx + dy * dy + dz * dz > half_skin2) *rebuild = 1;
-    }
-    // Periodic_Kernel on the COM (= the position): strict comparisons
+    // Periodic_Kernel on the COM (= the position): strict comparisons; the
+    // cell-local position x - bias is unchanged by a wrap
     double off[3];
     bool moved = false;
     for (int d = 0; d < 3; d++) {
@@ -903,25 +894,27 @@ __global__ void k_step0_fused(int n, double *__restrict__ r, double *__restrict_
         if (x[d] > g.high[d]) off[d] = -g.L[d];
         moved |= (off[d] != 0.0);
     }
-    if (moved) {
-        for (int d = 0; d < 3; d++) x[d] = dadd(x[d], off[d]);
-        q.x += (off[0] > 0.0) - (off[0] < 0.0);
-        q.y += (off[1] > 0.0) - (off[1] < 0.0);
-        q.z += (off[2] > 0.0) - (off[2] < 0.0);
-        img[s] = q;
+    if (moved) {   // r += shift over all three components, as Periodic_Kernel
+        for (int d = 0; d < 3; d++) {
+            x[d] = dadd(x[d], off[d]);
+            b[d] = dadd(b[d], off[d]);
+            bias[3 * s + d] = b[d];
+        }
+    }
+    float4 p = pos4[site_slot[s]];
+    p.x = __double2float_rn(dsub(x[0], b[0]));
+    p.y = __double2float_rn(dsub(x[1], b[1]));
+    p.z = __double2float_rn(dsub(x[2], b[2]));
+    pos4[site_slot[s]] = p;
+    {
+        const float4 q = ref4[s];
+        const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+        if (dx * dx + dy * dy + dz * dz > half_skin2) *rebuild = 1;
     }
     for (int d = 0; d < 3; d++) {
         r[3 * s + d] = x[d];
         com[3 * s + d] = x[d];
     }
-    const int slot = site_slot[s];
-    int cx, cy, cz;
-    cell_coords(g, slot_cell[slot], cx, cy, cz);
-    float4 p = pos4[slot];
-    p.x = (float)((x[0] - (double)q.x * g.L[0]) - cell_centre(g, 0, cx));
-    p.y = (float)((x[1] - (double)q.y * g.L[1]) - cell_centre(g, 1, cy));
-    p.z = (float)((x[2] - (double)q.z * g.L[2]) - cell_centre(g, 2, cz));
-    pos4[slot] = p;
 }
 
 __global__ void k_step1(int n, double *__restrict__ v, const double *__restrict__ f, const double *__restrict__ hdtm,
@@ -941,19 +934,15 @@ __global__ void k_step1(int n, double *__restrict__ v, const double *__restrict_
 
 // Verlet path, steps without rebuild: cell-local FP32 coordinates of the
 // continuous positions r - img*L relative to each slot's build cell.
-__global__ void k_refresh(Grid g, int n, const int *__restrict__ slot_site, const int *__restrict__ slot_cell,
-                          const double *__restrict__ r, const char4 *__restrict__ img, float4 *__restrict__ pos4,
-                          const int *__restrict__ rebuild) {
+__global__ void k_refresh(int n, const int *__restrict__ slot_site, const double *__restrict__ r,
+                          const double *__restrict__ bias, float4 *__restrict__ pos4, const int *__restrict__ rebuild) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= n || *rebuild) return;
     const int s = slot_site[slot];
-    int cx, cy, cz;
-    cell_coords(g, slot_cell[slot], cx, cy, cz);
-    const char4 q = img[s];
     float4 p = pos4[slot];
-    p.x = (float)((r[3 * s] - (double)q.x * g.L[0]) - cell_centre(g, 0, cx));
-    p.y = (float)((r[3 * s + 1] - (double)q.y * g.L[1]) - cell_centre(g, 1, cy));
-    p.z = (float)((r[3 * s + 2] - (double)q.z * g.L[2]) - cell_centre(g, 2, cz));
+    p.x = __double2float_rn(dsub(r[3 * s], bias[3 * s]));
+    p.y = __double2float_rn(dsub(r[3 * s + 1], bias[3 * s + 1]));
+    p.z = __double2float_rn(dsub(r[3 * s + 2], bias[3 * s + 2]));
     pos4[slot] = p;
 }
 
@@ -1145,19 +1134,18 @@ void launch_container(Engine &e, cudaStream_t st) {
     cudaMemsetAsync(e.cell_mcount, 0, sizeof(int) * g.ncell, st);
     k_com_wrap_bin<<<nblk(e.n_mol, 256), 256, 0, st>>>(g, (int)e.n_mol, e.mol_off, e.r, e.m, e.com, e.mol_cell,
                                                          e.mol_rank, e.cell_count, e.cell_mcount,
-                                                         e.verlet ? e.img : nullptr, rb, e.exact_com,
+                                                         e.verlet ? e.bias : nullptr, rb, e.exact_com,
                                                          e.fused_drift ? 1 : 0);
     k_scan2<<<1, 1024, 0, st>>>(g.ncell, e.cell_count, e.cell_start, e.cell_mcount, e.cell_mstart, rb);
     k_scatter_mol<<<nblk(e.n_mol, 256), 256, 0, st>>>((int)e.n_mol, e.mol_cell, e.mol_rank, e.cell_mstart,
                                                         e.cell_mols, rb);
     k_cell_sort<<<nblk(g.ncell, kWarpsPerBlock), kBlock, 0, st>>>(
         g, e.mol_off, e.cell_mstart, e.cell_start, e.cell_mols, e.r, e.eps, e.sig, e.key, e.slot_site, e.site_slot,
-        e.pos4, e.skey, e.seps, e.posd, e.seps_d, e.sig_d, e.verlet ? e.img : nullptr, e.verlet ? e.ref : nullptr,
+        e.pos4, e.skey, e.seps, e.posd, e.seps_d, e.sig_d, e.verlet ? e.bias : nullptr, e.verlet ? e.ref4 : nullptr,
         e.verlet ? e.slot_cell : nullptr, rb);
     if (e.verlet) {
         if (!e.fused_drift)
-            k_refresh<<<nblk(e.n, 256), 256, 0, st>>>(g, (int)e.n, e.slot_site, e.slot_cell, e.r, e.img, e.pos4,
-                                                        e.rebuild);
+            k_refresh<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.slot_site, e.r, e.bias, e.pos4, e.rebuild);
         launch_vlist_build(e, st);
     }
 }
@@ -1479,7 +1467,7 @@ __global__ void __launch_bounds__(kBlock) k_atm_s(AtmParams p) {
 // last force term): f[site] += ..., then v[site] += f[site] * dt/(2m) with
 // k_step1's operations, its non-finite check and the rebuild-flag reset
 __global__ void k_atm_flush_step1(int n, const int *__restrict__ slot_site, unsigned long long *acc, double *f,
-                                  double scale, double *__restrict__ v, const double *__restrict__ hdtm, int *err,
+                                  double scale_fix, double *__restrict__ v, const double *__restrict__ hdtm, int *err,
                                   int *rebuild) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (rebuild && slot == 0) *rebuild = 0;   // every consumer of this step's flag has run
@@ -1490,7 +1478,8 @@ __global__ void k_atm_flush_step1(int n, const int *__restrict__ slot_site, unsi
     for (int d = 0; d < 3; d++) {
         const long long q = (long long)acc[3 * slot + d];
         acc[3 * slot + d] = 0ull;
-        const double fd = f[3 * site + d] + scale * ((double)q * (1.0 / kAtmFix));
+        // scale_fix = scale / 2^32 exactly: the same product as scale * (q / 2^32)
+        const double fd = f[3 * site + d] + scale_fix * (double)q;
         f[3 * site + d] = fd;
         const double vv = dadd(v[3 * site + d], dmul(fd, c));
         v[3 * site + d] = vv;
@@ -1501,14 +1490,14 @@ __global__ void k_atm_flush_step1(int n, const int *__restrict__ slot_site, unsi
 
 // f[site] += 2 sign nu g (fixed point -> FP64) and the accumulators back to 0
 __global__ void k_atm_flush(int n, const int *__restrict__ slot_site, unsigned long long *acc, double *f,
-                            double scale) {
+                            double scale_fix) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= n) return;
     const int site = slot_site[slot];
     for (int d = 0; d < 3; d++) {
         const long long q = (long long)acc[3 * slot + d];
         acc[3 * slot + d] = 0ull;
-        f[3 * site + d] += scale * ((double)q * (1.0 / kAtmFix));
+        f[3 * site + d] += scale_fix * (double)q;
     }
 }
 
@@ -1556,11 +1545,12 @@ bool launch_atm(Engine &e, cudaStream_t st, bool measure, bool with_step1) {
         k_atm_s<<<atm_grid(e), kBlock, atm_smem(e), st>>>(p);
         if (with_step1) {
             k_atm_flush_step1<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.slot_site, e.atm_acc, e.f,
-                                                                2.0 * p.sign * p.nu, e.v, e.hdtm, e.err,
+                                                                2.0 * p.sign * p.nu / kAtmFix, e.v, e.hdtm, e.err,
                                                                 e.verlet ? e.rebuild : nullptr);
             return true;
         }
-        k_atm_flush<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.slot_site, e.atm_acc, e.f, 2.0 * p.sign * p.nu);
+        k_atm_flush<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.slot_site, e.atm_acc, e.f,
+                                                      2.0 * p.sign * p.nu / kAtmFix);
         return false;
     }
     if (e.cfg.precision == KOMD_FP64) atm_dispatch<double>(p, measure, compat, atm_grid(e), atm_smem(e), st);
@@ -1571,13 +1561,12 @@ bool launch_atm(Engine &e, cudaStream_t st, bool measure, bool with_step1) {
 void launch_step0(Engine &e, cudaStream_t st, bool in_step) {
     const float hs = (float)(0.5 * e.cfg.skin);
     if (in_step && e.fused_drift) {
-        k_step0_fused<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.r, e.v, e.f, e.hdtm, e.cfg.delta_t, e.g, e.img,
-                                                       e.ref, hs * hs, e.rebuild, e.com, e.site_slot, e.slot_cell,
-                                                       e.pos4);
+        k_step0_fused<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.r, e.v, e.f, e.hdtm, e.cfg.delta_t, e.g, e.bias,
+                                                       e.ref4, hs * hs, e.rebuild, e.com, e.site_slot, e.pos4);
         return;
     }
     k_step0<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.r, e.v, e.f, e.hdtm, e.cfg.delta_t, e.g,
-                                              e.verlet ? e.img : nullptr, e.verlet ? e.ref : nullptr, hs * hs,
+                                              e.verlet ? e.bias : nullptr, e.verlet ? e.ref4 : nullptr, hs * hs,
                                               e.rebuild);
 }
 
