@@ -869,6 +869,17 @@ __global__ void k_step0(int n, double *__restrict__ r, double *__restrict__ v, c
 // cell-local refresh (k_refresh's) in one pass over the sites.  The
 // results are those of the separate kernels; on a rebuild step the cell sort
 // rewrites pos4 afterwards.
+// integer key with key(x) < key(y) exactly when x < y for non-NaN doubles
+// (-0.0 and +0.0 share the key 0)
+__device__ __forceinline__ long long dkey(double x) {
+    const long long b = __double_as_longlong(x);
+    const long long m = b & 0x7fffffffffffffffLL;
+    return b < 0 ? -m : m;
+}
+__device__ __forceinline__ bool dkey_nan(double x) {
+    return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+}
+
 __global__ void k_step0_fused(int n, double *__restrict__ r, double *__restrict__ v, const double *__restrict__ f,
                               const double *__restrict__ hdtm, double dt, Grid g, double *__restrict__ bias,
                               const float4 *__restrict__ ref4, float half_skin2, int *__restrict__ rebuild,
@@ -884,14 +895,18 @@ __global__ void k_step0_fused(int n, double *__restrict__ r, double *__restrict_
         x[d] = dadd(r[3 * s + d], dmul(vv, dt));
         b[d] = bias[3 * s + d];
     }
-    // Periodic_Kernel on the COM (= the position): strict comparisons; the
-    // cell-local position x - bias is unchanged by a wrap
+    // Periodic_Kernel on the COM (= the position): strict comparisons, made on
+    // order-preserving integer keys (the FP64 pipe is the bottleneck here);
+    // the cell-local position x - bias is unchanged by a wrap
     double off[3];
     bool moved = false;
     for (int d = 0; d < 3; d++) {
         off[d] = 0.0;
-        if (x[d] < g.low[d]) off[d] = g.L[d];
-        if (x[d] > g.high[d]) off[d] = -g.L[d];
+        const long long kx = dkey(x[d]);
+        if (!dkey_nan(x[d])) {
+            if (kx < dkey(g.low[d])) off[d] = g.L[d];
+            if (kx > dkey(g.high[d])) off[d] = -g.L[d];
+        }
         moved |= (off[d] != 0.0);
     }
     if (moved) {   // r += shift over all three components, as Periodic_Kernel
@@ -918,7 +933,7 @@ __global__ void k_step0_fused(int n, double *__restrict__ r, double *__restrict_
 }
 
 __global__ void k_step1(int n, double *__restrict__ v, const double *__restrict__ f, const double *__restrict__ hdtm,
-                        int *err, int *rebuild) {
+                        int *__restrict__ err, int *__restrict__ rebuild) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (rebuild && s == 0) *rebuild = 0;   // every consumer of this step's flag has run
     if (s >= n) return;
@@ -1466,22 +1481,29 @@ __global__ void __launch_bounds__(kBlock) k_atm_s(AtmParams p) {
 // the same flush fused with Integrator::integrate1 of the step (ATM is the
 // last force term): f[site] += ..., then v[site] += f[site] * dt/(2m) with
 // k_step1's operations, its non-finite check and the rebuild-flag reset
-__global__ void k_atm_flush_step1(int n, const int *__restrict__ slot_site, unsigned long long *acc, double *f,
-                                  double scale_fix, double *__restrict__ v, const double *__restrict__ hdtm, int *err,
-                                  int *rebuild) {
+__global__ void k_atm_flush_step1(int n, const int *__restrict__ slot_site, unsigned long long *__restrict__ acc,
+                                  double *__restrict__ f, double scale_fix, double *__restrict__ v,
+                                  const double *__restrict__ hdtm, int *__restrict__ err, int *__restrict__ rebuild) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (rebuild && slot == 0) *rebuild = 0;   // every consumer of this step's flag has run
     if (slot >= n) return;
+    // every load first (independent requests in flight), then the arithmetic
     const int site = slot_site[slot];
+    long long q[3];
+    double fo[3], vo[3];
+    for (int d = 0; d < 3; d++) q[d] = (long long)acc[3 * slot + d];
+    for (int d = 0; d < 3; d++) {
+        fo[d] = f[3 * site + d];
+        vo[d] = v[3 * site + d];
+    }
     const double c = hdtm[site];
     bool bad = false;
     for (int d = 0; d < 3; d++) {
-        const long long q = (long long)acc[3 * slot + d];
         acc[3 * slot + d] = 0ull;
         // scale_fix = scale / 2^32 exactly: the same product as scale * (q / 2^32)
-        const double fd = f[3 * site + d] + scale_fix * (double)q;
+        const double fd = fo[d] + scale_fix * (double)q[d];
         f[3 * site + d] = fd;
-        const double vv = dadd(v[3 * site + d], dmul(fd, c));
+        const double vv = dadd(vo[d], dmul(fd, c));
         v[3 * site + d] = vv;
         bad |= !isfinite(vv);
     }
@@ -1489,15 +1511,18 @@ __global__ void k_atm_flush_step1(int n, const int *__restrict__ slot_site, unsi
 }
 
 // f[site] += 2 sign nu g (fixed point -> FP64) and the accumulators back to 0
-__global__ void k_atm_flush(int n, const int *__restrict__ slot_site, unsigned long long *acc, double *f,
-                            double scale_fix) {
+__global__ void k_atm_flush(int n, const int *__restrict__ slot_site, unsigned long long *__restrict__ acc,
+                            double *__restrict__ f, double scale_fix) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= n) return;
     const int site = slot_site[slot];
+    long long q[3];
+    double fo[3];
+    for (int d = 0; d < 3; d++) q[d] = (long long)acc[3 * slot + d];
+    for (int d = 0; d < 3; d++) fo[d] = f[3 * site + d];
     for (int d = 0; d < 3; d++) {
-        const long long q = (long long)acc[3 * slot + d];
         acc[3 * slot + d] = 0ull;
-        f[3 * site + d] += scale_fix * (double)q;
+        f[3 * site + d] = fo[d] + scale_fix * (double)q[d];
     }
 }
 

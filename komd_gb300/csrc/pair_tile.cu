@@ -390,10 +390,11 @@ __global__ void __launch_bounds__(kTileThreads) k_vlist_build(PairParams p) {
 // cell.  Inside cutoff_3b the pair is appended to the ATM list in list
 // order.  No atomics: the warp owns its site.
 // ---------------------------------------------------------------------------
-template <bool MEASURE, bool EMIT, bool UNIFORM>
-__global__ void __launch_bounds__(256, 5) k_lj_vlist(PairParams p, int n, int per) {
+// U = list entries per lane in flight (independent loads for latency hiding):
+// a warp covers 32 U entries of a row per pass
+template <bool MEASURE, bool EMIT, bool UNIFORM, int U>
+__global__ void __launch_bounds__(256, U == 3 ? 4 : 5) k_lj_vlist(PairParams p, int n, int per) {
     __shared__ double s_part[8][8];
-    constexpr int U = 2;   // list entries per lane in flight: independent loads for latency hiding
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const float rc2 = (float)p.rc2, rc3sq = (float)p.rc3sq;
     unsigned lt;
@@ -543,22 +544,36 @@ void launch_vlist_build(Engine &e, cudaStream_t st) {
 }
 
 template <bool UNIFORM>
-static void lj_vlist_dispatch(PairParams &p, int n, int grid, int per, bool measure, bool emit, cudaStream_t st) {
+static void lj_vlist_dispatch(PairParams &p, int n, int grid, int per, bool measure, bool emit, bool u3,
+                              cudaStream_t st) {
     if (measure) {
-        if (emit) k_lj_vlist<true, true, UNIFORM><<<grid, 256, 0, st>>>(p, n, per);
-        else k_lj_vlist<true, false, UNIFORM><<<grid, 256, 0, st>>>(p, n, per);
+        if (emit) k_lj_vlist<true, true, UNIFORM, 2><<<grid, 256, 0, st>>>(p, n, per);
+        else k_lj_vlist<true, false, UNIFORM, 2><<<grid, 256, 0, st>>>(p, n, per);
+    } else if (u3) {
+        if (emit) k_lj_vlist<false, true, UNIFORM, 3><<<grid, 256, 0, st>>>(p, n, per);
+        else k_lj_vlist<false, false, UNIFORM, 3><<<grid, 256, 0, st>>>(p, n, per);
     } else {
-        if (emit) k_lj_vlist<false, true, UNIFORM><<<grid, 256, 0, st>>>(p, n, per);
-        else k_lj_vlist<false, false, UNIFORM><<<grid, 256, 0, st>>>(p, n, per);
+        if (emit) k_lj_vlist<false, true, UNIFORM, 2><<<grid, 256, 0, st>>>(p, n, per);
+        else k_lj_vlist<false, false, UNIFORM, 2><<<grid, 256, 0, st>>>(p, n, per);
     }
+}
+
+// rows of at most 96 entries on average: one pass of 3 entries per lane
+// instead of two of 2 (the row length is the number of sites within the
+// list range, about density * 4/3 pi (cutoff + skin)^3)
+bool vlist_u3(const Engine &e) {
+    const double reach = std::max(e.cfg.cutoff, (e.cfg.terms & KOMD_TERM_ATM) ? e.cfg.cutoff_3b : 0.0) + e.cfg.skin;
+    const double rho = (double)e.n / (e.g.L[0] * e.g.L[1] * e.g.L[2]);
+    return rho * 4.18879020478639 * reach * reach * reach <= 88.0;
 }
 
 int launch_lj_vlist(Engine &e, PairParams &p, bool measure, bool emit, cudaStream_t st) {
     // the measure pass keeps one group per block (its partial sums are per block)
     const int per = measure ? 1 : vlist_per(e);
     const int grid = (vlist_grid(e) + per - 1) / per;
-    if (e.uniform) lj_vlist_dispatch<true>(p, (int)e.n, grid, per, measure, emit, st);
-    else lj_vlist_dispatch<false>(p, (int)e.n, grid, per, measure, emit, st);
+    const bool u3 = vlist_u3(e);
+    if (e.uniform) lj_vlist_dispatch<true>(p, (int)e.n, grid, per, measure, emit, u3, st);
+    else lj_vlist_dispatch<false>(p, (int)e.n, grid, per, measure, emit, u3, st);
     return grid;
 }
 
