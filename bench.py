@@ -372,7 +372,6 @@ def surrogate_leg(args, g, s, stream, local, dist, exact_value, world):
     g.forces()
     g.step(max(args.warmup, 3))
     torch.cuda.synchronize()
-    g.set_profiling(True)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -383,10 +382,14 @@ def surrogate_leg(args, g, s, stream, local, dist, exact_value, world):
     b.record(stream)
     torch.cuda.synchronize()
     ms = a.elapsed_time(b)
-    prof = g.profile()
-    g.set_profiling(False)
     if dist:
         ms = max_over_ranks(ms, dist, "cuda")
+    # per-kernel breakdown over K more steps (events around each family)
+    g.set_profiling(True)
+    g.step(args.steps)
+    torch.cuda.synchronize()
+    prof = g.profile()
+    g.set_profiling(False)
     st = g.surrogate_status()
     value = world * s.n * args.steps / (ms / 1e3)
     g.last_model = model
@@ -467,8 +470,9 @@ def run_ours(args, w, name):
     obs0 = g.measure(gpu.MEASURE_ENERGY | gpu.MEASURE_TEMPERATURE)
     triplets = int(obs0["triplets"])
 
-    # ---- timed region: K steps, per-kernel CUDA events on the launching stream
-    g.set_profiling(True)
+    # ---- timed region: K steps replayed from the step graph (komd_gpu_step, the
+    # production path), CUDA events on the launching stream
+    g.set_profiling(False)   # zeroes the list-rebuild counter read after the region
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -480,14 +484,15 @@ def run_ours(args, w, name):
         t1.record(stream)
         torch.cuda.synchronize()
     ms = t0.elapsed_time(t1)
-    prof = g.profile()
-    g.set_profiling(False)
     if dist:
         ms = max_over_ranks(ms, dist, "cuda")
         dist.barrier()
     value = world * s.n * args.steps / (ms / 1e3)
+    rebuilds_timed = g.profile().get("list_rebuilds", (0, 0.0))[0]
 
-    # graph-replay timing of the same K steps (no per-kernel events)
+    # per-kernel breakdown: K more steps launched kernel by kernel with CUDA
+    # events around each kernel family (slower than the graph by the events)
+    g.set_profiling(True)
     torch.cuda.synchronize()
     a = torch.cuda.Event(enable_timing=True)
     b = torch.cuda.Event(enable_timing=True)
@@ -495,7 +500,9 @@ def run_ours(args, w, name):
     g.step(args.steps)
     b.record(stream)
     torch.cuda.synchronize()
-    graph_ms = a.elapsed_time(b)
+    events_ms = a.elapsed_time(b)
+    prof = g.profile()
+    g.set_profiling(False)
 
     # ---- end to end through the C ABI from pinned host buffers
     r_h = torch.empty((s.n, 3), dtype=torch.float64).pin_memory()
@@ -556,7 +563,7 @@ def run_ours(args, w, name):
     cb = None
     if not args.no_cpu_baseline:
         cb = cpu_baseline(w, seed=1, budget_s=args.cpu_budget)
-    kernels = g.kernels_per_step()
+    kernels = g.kernels_per_step() * args.steps + g.kernels_per_rebuild() * rebuilds_timed
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp32 forces / fp64 integration",
@@ -570,8 +577,8 @@ def run_ours(args, w, name):
                        "triplets_per_step": triplets, "parallelism": f"replicas x{world}",
                        "l2": "no flush: the per-step working set exceeds L2 (the ATM neighbour list alone, "
                              "16 B x capacity per site, is written and re-read every step)"},
-            "gpu_launches": kernels * args.steps,
-            "graph_ms_per_step": graph_ms / args.steps,
+            "gpu_launches": kernels, "list_rebuilds_timed": rebuilds_timed,
+            "events_ms_per_step": events_ms / args.steps,
             "kernel_ms": {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()},
             "roofline": roof, "peak_kind": peak_kind, "traffic_note": "traffic from the committed ncu capture (profiles/traffic.json), lattice state, per launch",
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * s.n * 24, "d2h_bytes_per_step": 3 * s.n * 24},
