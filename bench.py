@@ -563,7 +563,7 @@ def run_ours(args, w, name):
     cb = None
     if not args.no_cpu_baseline:
         cb = cpu_baseline(w, seed=1, budget_s=args.cpu_budget)
-    kernels = g.kernels_per_step() * args.steps + g.kernels_per_rebuild() * rebuilds_timed
+    kernels = g.kernels_per_step() * args.steps
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp32 forces / fp64 integration",

@@ -310,11 +310,8 @@ int  komd_batch_check(komd_batch *b);
  * reset.  names is a '\n'-separated list of families (<= cap bytes). */
 int  komd_gpu_set_profiling(komd_gpu *h, int on);
 int  komd_gpu_profile(komd_gpu *h, int max_families, int64_t *launches, double *ms, char *names, int cap);
-/* Number of kernels one komd_gpu_step launches per step without a Verlet-list
- * rebuild, and the number a rebuild step adds (for accounting; the rebuilds
- * are counted by komd_gpu_profile's "list_rebuilds"). */
+/* Number of kernels one komd_gpu_step launches per step (for accounting). */
 int  komd_gpu_kernels_per_step(komd_gpu *h);
-int  komd_gpu_kernels_per_rebuild(komd_gpu *h);
 
 /* ---- allocation-free variant ------------------------------------------- */
 /* No counterpart in the reference.  ATM forces (FULL triplet set) of one

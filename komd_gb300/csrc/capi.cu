@@ -88,7 +88,6 @@ struct komd_gpu {
     uint32_t sensor_terms = 0;
     double *prof = nullptr;           // komd_gpu_rdf_profile's device histogram
     int prof_cap = 0;
-    cudaStream_t cap_stream = nullptr;   // captures the conditional container body
     // profiling
     std::vector<cudaEvent_t> pool;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
@@ -243,49 +242,7 @@ bool enqueue_forces(komd_gpu *h, bool measure, double *lj_hist, bool with_step1 
     return fused;
 }
 
-// Inside a stream capture of the single-system step graph: the container pass
-// (on the fused-drift Verlet path every kernel of it is a no-op unless a site
-// moved more than skin/2) becomes the body of a conditional IF node that one
-// small kernel sets from the device rebuild flag, so that steps without a
-// rebuild skip its launches.  Returns false (nothing enqueued) when the capture
-// cannot take the node; the caller then enqueues the plain pass.
-bool enqueue_container_if_rebuild(komd_gpu *h) {
-    Engine &e = h->e;
-    cudaStreamCaptureStatus cs;
-    cudaGraph_t cg;
-    const cudaGraphNode_t *deps = nullptr;
-    const cudaGraphEdgeData *edges = nullptr;
-    size_t nd = 0;
-    if (cudaStreamGetCaptureInfo(e.stream, &cs, nullptr, &cg, &deps, &edges, &nd) != cudaSuccess ||
-        cs != cudaStreamCaptureStatusActive)
-        return false;
-    if (!h->cap_stream && cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
-        h->cap_stream = nullptr;
-        return false;
-    }
-    cudaGraphConditionalHandle hnd;
-    if (cudaGraphConditionalHandleCreate(&hnd, cg, 0, cudaGraphCondAssignDefault) != cudaSuccess) return false;
-    launch_rebuild_cond(hnd, e.rebuild, e.stream);
-    if (cudaStreamGetCaptureInfo(e.stream, &cs, nullptr, &cg, &deps, &edges, &nd) != cudaSuccess) return false;
-    cudaGraphNodeParams cp{};
-    cp.type = cudaGraphNodeTypeConditional;
-    cp.conditional.handle = hnd;
-    cp.conditional.type = cudaGraphCondTypeIf;
-    cp.conditional.size = 1;
-    cudaGraphNode_t node;
-    if (cudaGraphAddNode(&node, cg, deps, edges, nd, &cp) != cudaSuccess) return false;
-    cudaGraph_t body = cp.conditional.phGraph_out[0];
-    if (cudaStreamBeginCaptureToGraph(h->cap_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) !=
-        cudaSuccess)
-        return false;
-    launch_container(e, h->cap_stream);
-    cudaGraph_t done;
-    if (cudaStreamEndCapture(h->cap_stream, &done) != cudaSuccess) return false;
-    return cudaStreamUpdateCaptureDependencies(e.stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies) ==
-           cudaSuccess;
-}
-
-void enqueue_step(komd_gpu *h, bool conditional_container = false) {
+void enqueue_step(komd_gpu *h) {
     Engine &e = h->e;
     {
         ProfScope ps(h, F_INTEGRATE);
@@ -293,8 +250,7 @@ void enqueue_step(komd_gpu *h, bool conditional_container = false) {
     }
     {
         ProfScope ps(h, F_CONTAINER);
-        if (!(conditional_container && e.verlet && e.fused_drift && enqueue_container_if_rebuild(h)))
-            launch_container(e, e.stream);
+        launch_container(e, e.stream);
     }
     // the step's integrate1 rides on the ATM flush when the once-per-triplet path runs
     if (!enqueue_forces(h, false, nullptr, true)) {
@@ -510,7 +466,6 @@ int komd_gpu_destroy(komd_gpu *h) {
     cudaSetDevice(e.device);
     if (e.stream) cudaStreamSynchronize(e.stream);
     if (e.graph) cudaGraphExecDestroy(e.graph);
-    if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
     dfree(e.r); dfree(e.v); dfree(e.f); dfree(e.m); dfree(e.eps); dfree(e.sig);
     dfree(e.key); dfree(e.site_mol); dfree(e.site_slot);
     dfree(e.mol_off); dfree(e.mol_cell); dfree(e.mol_rank); dfree(e.com);
@@ -831,7 +786,7 @@ static int run_steps(komd_gpu *h, int64_t n_steps) {
     if (!e.graph_valid) {
         cudaGraph_t graph;
         CK(cudaStreamBeginCapture(e.stream, cudaStreamCaptureModeThreadLocal));
-        enqueue_step(h, true);
+        enqueue_step(h);
         CK(cudaStreamEndCapture(e.stream, &graph));
         if (e.graph) cudaGraphExecDestroy(e.graph);
         const cudaError_t ie = cudaGraphInstantiate(&e.graph, graph, 0);
@@ -1725,23 +1680,12 @@ int komd_batch_check(komd_batch *b) {
     return KOMD_OK;
 }
 
-// kernels of the container pass: com/wrap/bin, scan, scatter, cell sort, and on
-// the Verlet path the list build (and the FP32 refresh unless the drift does it)
-static int container_kernels(const Engine &e) { return 4 + (e.verlet ? (e.fused_drift ? 1 : 2) : 0); }
-
-// the step graph puts the container pass behind the rebuild condition on this path
-static bool container_conditional(const Engine &e) { return e.verlet && e.fused_drift; }
-
-int komd_gpu_kernels_per_rebuild(komd_gpu *h) {
-    if (!h) return -1;
-    return container_conditional(h->e) ? container_kernels(h->e) : 0;
-}
-
 int komd_gpu_kernels_per_step(komd_gpu *h) {
     if (!h) return -1;
     const Engine &e = h->e;
-    int k = 2 /* integrate */;
-    k += container_conditional(e) ? 1 /* the rebuild condition */ : container_kernels(e);
+    // integrate0/1; the container pass (com/wrap/bin, scan, scatter, cell sort, and
+    // on the Verlet path the list build and the FP32 refresh unless the drift does it)
+    int k = 2 + 4 + (e.verlet ? (e.fused_drift ? 1 : 2) : 0);
     if (e.cfg.terms & (KOMD_TERM_LJ | KOMD_TERM_FENE | KOMD_TERM_ATM)) k++;   /* pair pass (else a memset) */
     if (e.cfg.terms & KOMD_TERM_TABULATED) k++;
     if (!surrogate_on(h) && (e.cfg.terms & KOMD_TERM_ATM) && e.atm_acc) k--;   /* integrate1 fused into the ATM flush */

@@ -1142,16 +1142,6 @@ __global__ void k_velocity_scale(int n, double *__restrict__ v, const double *__
 // ===========================================================================
 static inline int nblk(long long n, int b) { return (int)((n + b - 1) / b); }
 
-// one thread: the step graph's IF node runs the container pass only when some
-// site moved more than skin/2 (the flag k_step0_fused raised this step)
-__global__ void k_rebuild_cond(cudaGraphConditionalHandle hnd, const int *__restrict__ rebuild) {
-    cudaGraphSetConditional(hnd, *rebuild != 0 ? 1u : 0u);
-}
-
-void launch_rebuild_cond(cudaGraphConditionalHandle hnd, const int *rebuild, cudaStream_t st) {
-    k_rebuild_cond<<<1, 1, 0, st>>>(hnd, rebuild);
-}
-
 void launch_container(Engine &e, cudaStream_t st) {
     const Grid &g = e.g;
     const int *rb = e.verlet ? e.rebuild : nullptr;   // nullptr: rebuild unconditionally

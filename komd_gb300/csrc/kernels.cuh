@@ -4,7 +4,6 @@
 
 namespace komd {
 void launch_container(Engine &e, cudaStream_t st);
-void launch_rebuild_cond(cudaGraphConditionalHandle hnd, const int *rebuild, cudaStream_t st);
 int launch_pair(Engine &e, cudaStream_t st, bool measure, double *lj_hist);
 void launch_pair_tile(PairParams &p, int ncell, bool measure, bool emit, cudaStream_t st);
 PairParams pair_params(Engine &e);

@@ -33,7 +33,7 @@ EXPORTS = [
     "komd_gpu_download", "komd_gpu_num_sites", "komd_gpu_update_container", "komd_gpu_forces",
     "komd_gpu_integrate0", "komd_gpu_integrate1", "komd_gpu_step", "komd_gpu_step_host", "komd_gpu_measure",
     "komd_gpu_rdf_bins", "komd_gpu_get_cells", "komd_gpu_neighbour_counts", "komd_gpu_set_profiling",
-    "komd_gpu_profile", "komd_gpu_kernels_per_step", "komd_gpu_kernels_per_rebuild", "komd_gpu_atm_forces_noalloc", "komd_gpu_surrogate_load",
+    "komd_gpu_profile", "komd_gpu_kernels_per_step", "komd_gpu_atm_forces_noalloc", "komd_gpu_surrogate_load",
     "komd_gpu_surrogate_sample", "komd_gpu_surrogate_forces", "komd_gpu_surrogate_status", "komd_mlp_train",
     "komd_mlp_loss_grad", "komd_sur_data_create", "komd_sur_data_destroy", "komd_gpu_surrogate_capture",
     "komd_sur_data_snapshots", "komd_sur_data_sites", "komd_sur_data_get", "komd_sur_fit", "komd_sur_fit_grad",
@@ -118,7 +118,6 @@ def load() -> C.CDLL:
     L.komd_gpu_set_profiling.argtypes = [P, I32]
     L.komd_gpu_profile.argtypes = [P, I32, P, P, C.c_char_p, I32]
     L.komd_gpu_kernels_per_step.argtypes = [P]
-    L.komd_gpu_kernels_per_rebuild.argtypes = [P]
     L.komd_gpu_atm_forces_noalloc.argtypes = [I64, P, P, P, P, C.c_double, C.c_double, C.c_int32, P]
     L.komd_gpu_surrogate_load.argtypes = [P, P, P, P, C.c_double, C.c_double, C.c_int32, C.c_double]
     L.komd_gpu_surrogate_sample.argtypes = [P, P, P, P]
@@ -298,9 +297,6 @@ class GpuSystem:
 
     def kernels_per_step(self) -> int:
         return int(self.L.komd_gpu_kernels_per_step(self.h))
-
-    def kernels_per_rebuild(self) -> int:
-        return int(self.L.komd_gpu_kernels_per_rebuild(self.h))
 
     # --- learned three-body term ------------------------------------------
     def surrogate_load(self, model, probe_every=50, probe_threshold=0.05):
