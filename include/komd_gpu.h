@@ -167,8 +167,14 @@ int  komd_gpu_integrate1(komd_gpu *h);
  * graph.  Requires forces of the current positions (call update_container +
  * forces once before the first step_n). */
 int  komd_gpu_step(komd_gpu *h, int64_t n_steps);
-/* Same as komd_gpu_step, end to end from host buffers: uploads r, v (n*3) from
- * the host, runs n_steps, downloads r, v and f.  Host buffers may be pinned. */
+/* Same as komd_gpu_step, end to end from host buffers: takes r, v (n*3) from
+ * the host, runs n_steps, returns r, v and f.  When the GPU can address the
+ * buffers (pinned memory, or any host memory where the GPU walks the host page
+ * tables, as over NVLink-C2C) and the step is the fused Verlet / FULL FP32 ATM
+ * path without device thermostat or learned term, the first step's drift
+ * kernel reads r, v and writes r back, and the last step's ATM flush writes f
+ * and v, so no separate copies run; otherwise copies frame the steps.  The
+ * results are bitwise those of komd_gpu_step. */
 int  komd_gpu_step_host(komd_gpu *h, int64_t n_steps, double *r, double *v, double *f);
 
 /* ---- sensors ------------------------------------------------------------ */

@@ -83,6 +83,7 @@ struct komd_gpu {
     double *thermo_acc = nullptr;     // R_NSLOTS, the device thermostat's kinetic sums
     int partial_cap = 0;
     bool want_posd = false;
+    bool pageable_access = false;     // kernels may dereference any host pointer (host page tables)
     // the terms given at creation: the sensors evaluate these whatever the step's
     // force terms are (the reference's sensors do not go through the functor list)
     uint32_t sensor_terms = 0;
@@ -390,6 +391,12 @@ int komd_gpu_create(const komd_config *cfg, int device, komd_gpu **out) {
     if (!(e.cfg.max_sigma > 0)) e.cfg.max_sigma = 1.0;
     e.g = g;
     e.device = device;
+    {
+        int pa = 0, pt = 0;
+        cudaDeviceGetAttribute(&pa, cudaDevAttrPageableMemoryAccess, device);
+        cudaDeviceGetAttribute(&pt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device);
+        h->pageable_access = pa != 0 && pt != 0;
+    }
     if (cudaStreamCreateWithFlags(&e.stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete h;
         return fail(KOMD_ERR_CUDA, "stream creation failed");
@@ -823,9 +830,69 @@ int komd_gpu_step(komd_gpu *h, int64_t n_steps) {
     return finish_steps(h);
 }
 
+}  // extern "C"
+
+namespace {
+// the device address of a host buffer, if kernels can reach it: pinned (mapped)
+// memory, or any host memory on a system whose GPU walks the host page tables
+// (NVLink-C2C with address translation, as on Grace)
+const double *device_view(komd_gpu *h, const double *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost && a.devicePointer) return static_cast<const double *>(a.devicePointer);
+    if (a.type == cudaMemoryTypeUnregistered && h->pageable_access) return p;
+    return nullptr;
+}
+
+// komd_gpu_step_host without copy-engine transfers: the step's drift kernel reads
+// r and v from the caller's buffers and writes the new r back, and the flush
+// that ends the step writes f and v, so the host traffic runs inside those
+// kernels (and in both directions at once) instead of before and after the
+// step.  Only for the step graph's fused path (Verlet list, single-site
+// molecules, FULL FP32 ATM ending the step, no device thermostat, no learned
+// term); *applies = false (nothing done) otherwise.
+int step_host_direct(komd_gpu *h, int64_t n_steps, double *r, double *v, double *f, bool *applies) {
+    Engine &e = h->e;
+    *applies = false;
+    if (!(e.verlet && e.fused_drift && e.atm_acc && (e.cfg.terms & KOMD_TERM_ATM) && !e.cfg.thermostat &&
+          !surrogate_on(h) && e.have_forces && r && v && f))
+        return KOMD_OK;
+    const double *rin = device_view(h, r), *vin = device_view(h, v), *fo = device_view(h, f);
+    if (!rin || !vin || !fo) return KOMD_OK;
+    *applies = true;
+    double *rout = const_cast<double *>(rin), *vout = const_cast<double *>(vin), *fout = const_cast<double *>(fo);
+    e.hin_r = rin;
+    e.hin_v = vin;
+    if (n_steps == 1) { e.hout_r = rout; e.hout_v = vout; e.hout_f = fout; }
+    enqueue_step(h);
+    e.hin_r = e.hin_v = nullptr;
+    e.hout_r = e.hout_v = e.hout_f = nullptr;
+    int rc = check_launch("step_host");
+    if (!rc && n_steps > 2) rc = run_steps(h, n_steps - 2);
+    if (!rc && n_steps > 1) {
+        e.hout_r = rout; e.hout_v = vout; e.hout_f = fout;
+        enqueue_step(h);
+        e.hout_r = e.hout_v = e.hout_f = nullptr;
+        rc = check_launch("step_host");
+    }
+    if (rc) return rc;
+    return finish_steps(h);
+}
+}  // namespace
+
+extern "C" {
+
 int komd_gpu_step_host(komd_gpu *h, int64_t n_steps, double *r, double *v, double *f) {
     if (!h || !h->e.have_sites) return fail(KOMD_ERR_STATE, "no sites uploaded");
     Engine &e = h->e;
+    if (n_steps > 0 && !e.profiling) {
+        bool applies = false;
+        const int rc = step_host_direct(h, n_steps, r, v, f, &applies);
+        if (applies) return rc;
+    }
     if (r) CK(cudaMemcpyAsync(e.r, r, sizeof(double) * 3 * e.n, cudaMemcpyHostToDevice, e.stream));
     if (v) CK(cudaMemcpyAsync(e.v, v, sizeof(double) * 3 * e.n, cudaMemcpyHostToDevice, e.stream));
     int rc = komd_gpu_step(h, n_steps);

@@ -260,6 +260,11 @@ struct Engine {
     double lj_fscale = 1.0;         // ATM2B factor (KOMD_TERM_ATM2B), else 1
     bool fused_drift = false;       // Verlet path, single-site molecules with exact COM: k_step0_fused
     bool atm_up = false;            // this force pass feeds k_atm_s only: ATM lists hold neighbours above
+    // device-accessible host buffers of komd_gpu_step_host (site order, 3 doubles
+    // per site), read or written directly by the step's first and last kernels;
+    // nullptr outside such a step
+    const double *hin_r = nullptr, *hin_v = nullptr;
+    double *hout_r = nullptr, *hout_v = nullptr, *hout_f = nullptr;
     unsigned long long *atm_acc = nullptr;   // 3 per slot, fixed-point force sums of k_atm_s (zero between steps)
     // tabulated pair force (KOMD_TERM_TABULATED): F(r) piecewise linear on
     // ascending nodes tab_x, values tab_y, tab_lo below / tab_hi above the nodes

@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <climits>
+#include <cstdint>
 
 #include "engine.cuh"
 #include "kernels.cuh"
@@ -880,55 +881,112 @@ __device__ __forceinline__ bool dkey_nan(double x) {
     return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
 }
 
-__global__ void k_step0_fused(int n, double *__restrict__ r, double *__restrict__ v, const double *__restrict__ f,
-                              const double *__restrict__ hdtm, double dt, Grid g, double *__restrict__ bias,
-                              const float4 *__restrict__ ref4, float half_skin2, int *__restrict__ rebuild,
-                              double *__restrict__ com, const int *__restrict__ site_slot,
-                              float4 *__restrict__ pos4) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    const double c = hdtm[s];
-    double x[3], b[3];
-    for (int d = 0; d < 3; d++) {
-        const double vv = dadd(v[3 * s + d], dmul(f[3 * s + d], c));
-        v[3 * s + d] = vv;
-        x[d] = dadd(r[3 * s + d], dmul(vv, dt));
-        b[d] = bias[3 * s + d];
-    }
-    // Periodic_Kernel on the COM (= the position): strict comparisons, made on
-    // order-preserving integer keys (the FP64 pipe is the bottleneck here);
-    // the cell-local position x - bias is unchanged by a wrap
-    double off[3];
-    bool moved = false;
-    for (int d = 0; d < 3; d++) {
-        off[d] = 0.0;
-        const long long kx = dkey(x[d]);
-        if (!dkey_nan(x[d])) {
-            if (kx < dkey(g.low[d])) off[d] = g.L[d];
-            if (kx > dkey(g.high[d])) off[d] = -g.L[d];
+// Block-cooperative copies of a block's rows (3 doubles per site) between a
+// caller's host buffer and shared memory in 16-byte pieces: over the host link
+// whole contiguous lines move instead of 8-byte pieces strided by 24 bytes.
+constexpr int kIoBlock = 256;   // sites per block of the kernels that do host I/O
+
+__device__ __forceinline__ void rows_in(const double *src, double *dst_s, int base, int cnt) {
+    const double *p = src + 3 * (size_t)base;
+    const int m = 3 * cnt;
+    if ((reinterpret_cast<uintptr_t>(p) & 15u) == 0) {
+        const double2 *p2 = reinterpret_cast<const double2 *>(p);
+        for (int k = threadIdx.x; k < m / 2; k += blockDim.x) {
+            const double2 q = p2[k];
+            dst_s[2 * k] = q.x;
+            dst_s[2 * k + 1] = q.y;
         }
-        moved |= (off[d] != 0.0);
+        if ((m & 1) && threadIdx.x == 0) dst_s[m - 1] = p[m - 1];
+    } else {
+        for (int k = threadIdx.x; k < m; k += blockDim.x) dst_s[k] = p[k];
     }
-    if (moved) {   // r += shift over all three components, as Periodic_Kernel
+}
+
+__device__ __forceinline__ void rows_out(const double *src_s, double *dst, int base, int cnt) {
+    double *p = dst + 3 * (size_t)base;
+    const int m = 3 * cnt;
+    if ((reinterpret_cast<uintptr_t>(p) & 15u) == 0) {
+        double2 *p2 = reinterpret_cast<double2 *>(p);
+        for (int k = threadIdx.x; k < m / 2; k += blockDim.x) p2[k] = make_double2(src_s[2 * k], src_s[2 * k + 1]);
+        if ((m & 1) && threadIdx.x == 0) p[m - 1] = src_s[m - 1];
+    } else {
+        for (int k = threadIdx.x; k < m; k += blockDim.x) p[k] = src_s[k];
+    }
+}
+
+// r_in / v_in: where this step's positions and velocities are read (the
+// engine's own arrays, or a caller's host buffers reached over the host link);
+// r_out: an extra host copy of the new positions (nullptr: none).  Launched
+// with kIoBlock threads per block.
+__global__ void __launch_bounds__(kIoBlock) k_step0_fused(
+    int n, double *r, double *v, const double *__restrict__ f, const double *__restrict__ hdtm, double dt, Grid g,
+    double *__restrict__ bias, const float4 *__restrict__ ref4, float half_skin2, int *__restrict__ rebuild,
+    double *__restrict__ com, const int *__restrict__ site_slot, float4 *__restrict__ pos4, const double *r_in,
+    const double *v_in, double *r_out) {
+    __shared__ double s_r[3 * kIoBlock], s_v[3 * kIoBlock];
+    const int t = threadIdx.x;
+    const int base = blockIdx.x * blockDim.x, s = base + t;
+    const int cnt = min((int)blockDim.x, n - base);
+    const bool host_in = r_in != r;   // uniform: the whole step reads the caller's buffers
+    if (host_in) {
+        rows_in(r_in, s_r, base, cnt);
+        rows_in(v_in, s_v, base, cnt);
+        __syncthreads();
+    }
+    if (s < n) {
+        const double c = hdtm[s];
+        double x[3], b[3], vi[3], ri[3];
         for (int d = 0; d < 3; d++) {
-            x[d] = dadd(x[d], off[d]);
-            b[d] = dadd(b[d], off[d]);
-            bias[3 * s + d] = b[d];
+            vi[d] = host_in ? s_v[3 * t + d] : v[3 * s + d];
+            ri[d] = host_in ? s_r[3 * t + d] : r[3 * s + d];
         }
+        for (int d = 0; d < 3; d++) {
+            const double vv = dadd(vi[d], dmul(f[3 * s + d], c));
+            v[3 * s + d] = vv;
+            x[d] = dadd(ri[d], dmul(vv, dt));
+            b[d] = bias[3 * s + d];
+        }
+        // Periodic_Kernel on the COM (= the position): strict comparisons, made on
+        // order-preserving integer keys (the FP64 pipe is the bottleneck here);
+        // the cell-local position x - bias is unchanged by a wrap
+        double off[3];
+        bool moved = false;
+        for (int d = 0; d < 3; d++) {
+            off[d] = 0.0;
+            const long long kx = dkey(x[d]);
+            if (!dkey_nan(x[d])) {
+                if (kx < dkey(g.low[d])) off[d] = g.L[d];
+                if (kx > dkey(g.high[d])) off[d] = -g.L[d];
+            }
+            moved |= (off[d] != 0.0);
+        }
+        if (moved) {   // r += shift over all three components, as Periodic_Kernel
+            for (int d = 0; d < 3; d++) {
+                x[d] = dadd(x[d], off[d]);
+                b[d] = dadd(b[d], off[d]);
+                bias[3 * s + d] = b[d];
+            }
+        }
+        float4 p = pos4[site_slot[s]];
+        p.x = __double2float_rn(dsub(x[0], b[0]));
+        p.y = __double2float_rn(dsub(x[1], b[1]));
+        p.z = __double2float_rn(dsub(x[2], b[2]));
+        pos4[site_slot[s]] = p;
+        {
+            const float4 q = ref4[s];
+            const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+            if (dx * dx + dy * dy + dz * dz > half_skin2) *rebuild = 1;
+        }
+        for (int d = 0; d < 3; d++) {
+            r[3 * s + d] = x[d];
+            com[3 * s + d] = x[d];
+        }
+        if (r_out)   // each thread overwrites only the entries it read
+            for (int d = 0; d < 3; d++) s_r[3 * t + d] = x[d];
     }
-    float4 p = pos4[site_slot[s]];
-    p.x = __double2float_rn(dsub(x[0], b[0]));
-    p.y = __double2float_rn(dsub(x[1], b[1]));
-    p.z = __double2float_rn(dsub(x[2], b[2]));
-    pos4[site_slot[s]] = p;
-    {
-        const float4 q = ref4[s];
-        const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
-        if (dx * dx + dy * dy + dz * dz > half_skin2) *rebuild = 1;
-    }
-    for (int d = 0; d < 3; d++) {
-        r[3 * s + d] = x[d];
-        com[3 * s + d] = x[d];
+    if (r_out) {
+        __syncthreads();
+        rows_out(s_r, r_out, base, cnt);
     }
 }
 
@@ -1481,33 +1539,46 @@ __global__ void __launch_bounds__(kBlock) k_atm_s(AtmParams p) {
 // the same flush fused with Integrator::integrate1 of the step (ATM is the
 // last force term): f[site] += ..., then v[site] += f[site] * dt/(2m) with
 // k_step1's operations, its non-finite check and the rebuild-flag reset
-__global__ void k_atm_flush_step1(int n, const int *__restrict__ slot_site, unsigned long long *__restrict__ acc,
-                                  double *__restrict__ f, double scale_fix, double *__restrict__ v,
-                                  const double *__restrict__ hdtm, int *__restrict__ err, int *__restrict__ rebuild) {
-    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
-    if (rebuild && slot == 0) *rebuild = 0;   // every consumer of this step's flag has run
-    if (slot >= n) return;
-    // every load first (independent requests in flight), then the arithmetic
-    const int site = slot_site[slot];
-    long long q[3];
-    double fo[3], vo[3];
-    for (int d = 0; d < 3; d++) q[d] = (long long)acc[3 * slot + d];
-    for (int d = 0; d < 3; d++) {
-        fo[d] = f[3 * site + d];
-        vo[d] = v[3 * site + d];
+__global__ void __launch_bounds__(kIoBlock) k_atm_flush_step1(
+    int n, const int *__restrict__ site_slot, unsigned long long *__restrict__ acc, double *__restrict__ f,
+    double scale_fix, double *__restrict__ v, const double *__restrict__ hdtm, int *__restrict__ err,
+    int *__restrict__ rebuild, double *f_out, double *v_out) {
+    __shared__ double s_f[3 * kIoBlock], s_v[3 * kIoBlock];
+    const int t = threadIdx.x;
+    const int base = blockIdx.x * blockDim.x, site = base + t;
+    const int cnt = min((int)blockDim.x, n - base);
+    if (rebuild && site == 0) *rebuild = 0;   // every consumer of this step's flag has run
+    if (site < n) {
+        // one thread per site (f, v, dt/2m coalesced, the accumulators
+        // gathered); every load first, then the arithmetic
+        const int slot = site_slot[site];
+        long long q[3];
+        double fo[3], vo[3];
+        for (int d = 0; d < 3; d++) q[d] = (long long)acc[3 * slot + d];
+        for (int d = 0; d < 3; d++) {
+            fo[d] = f[3 * site + d];
+            vo[d] = v[3 * site + d];
+        }
+        const double c = hdtm[site];
+        bool bad = false;
+        for (int d = 0; d < 3; d++) {
+            acc[3 * slot + d] = 0ull;
+            // scale_fix = scale / 2^32 exactly: the same product as scale * (q / 2^32)
+            const double fd = fo[d] + scale_fix * (double)q[d];
+            f[3 * site + d] = fd;
+            const double vv = dadd(vo[d], dmul(fd, c));
+            v[3 * site + d] = vv;
+            bad |= !isfinite(vv);
+            s_f[3 * t + d] = fd;
+            s_v[3 * t + d] = vv;
+        }
+        if (bad) atomicOr(&err[E_NONFINITE], 1);
     }
-    const double c = hdtm[site];
-    bool bad = false;
-    for (int d = 0; d < 3; d++) {
-        acc[3 * slot + d] = 0ull;
-        // scale_fix = scale / 2^32 exactly: the same product as scale * (q / 2^32)
-        const double fd = fo[d] + scale_fix * (double)q[d];
-        f[3 * site + d] = fd;
-        const double vv = dadd(vo[d], dmul(fd, c));
-        v[3 * site + d] = vv;
-        bad |= !isfinite(vv);
+    if (f_out || v_out) {   // the caller's host buffers, in whole lines
+        __syncthreads();
+        if (f_out) rows_out(s_f, f_out, base, cnt);
+        if (v_out) rows_out(s_v, v_out, base, cnt);
     }
-    if (bad) atomicOr(&err[E_NONFINITE], 1);
 }
 
 // f[site] += 2 sign nu g (fixed point -> FP64) and the accumulators back to 0
@@ -1569,9 +1640,9 @@ bool launch_atm(Engine &e, cudaStream_t st, bool measure, bool with_step1) {
         // every triplet once (lowest slot), fixed-point scatter, then the flush into f
         k_atm_s<<<atm_grid(e), kBlock, atm_smem(e), st>>>(p);
         if (with_step1) {
-            k_atm_flush_step1<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.slot_site, e.atm_acc, e.f,
+            k_atm_flush_step1<<<nblk(e.n, kIoBlock), kIoBlock, 0, st>>>((int)e.n, e.site_slot, e.atm_acc, e.f,
                                                                 2.0 * p.sign * p.nu / kAtmFix, e.v, e.hdtm, e.err,
-                                                                e.verlet ? e.rebuild : nullptr);
+                                                                e.verlet ? e.rebuild : nullptr, e.hout_f, e.hout_v);
             return true;
         }
         k_atm_flush<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.slot_site, e.atm_acc, e.f,
@@ -1586,8 +1657,9 @@ bool launch_atm(Engine &e, cudaStream_t st, bool measure, bool with_step1) {
 void launch_step0(Engine &e, cudaStream_t st, bool in_step) {
     const float hs = (float)(0.5 * e.cfg.skin);
     if (in_step && e.fused_drift) {
-        k_step0_fused<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.r, e.v, e.f, e.hdtm, e.cfg.delta_t, e.g, e.bias,
-                                                       e.ref4, hs * hs, e.rebuild, e.com, e.site_slot, e.pos4);
+        k_step0_fused<<<nblk(e.n, kIoBlock), kIoBlock, 0, st>>>((int)e.n, e.r, e.v, e.f, e.hdtm, e.cfg.delta_t, e.g, e.bias,
+                                                       e.ref4, hs * hs, e.rebuild, e.com, e.site_slot, e.pos4,
+                                                       e.hin_r ? e.hin_r : e.r, e.hin_v ? e.hin_v : e.v, e.hout_r);
         return;
     }
     k_step0<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.r, e.v, e.f, e.hdtm, e.cfg.delta_t, e.g,

@@ -62,3 +62,31 @@ def test_autotuner_picks_a_measured_shape():
     t = autotune.tune_skin(s, make_cfg, (0.2, 0.4), 2.5, steps=20, warmup=5)
     assert [r["skin"] for r in sorted(t["table"], key=lambda r: r["skin"])] == [0.2, 0.4]
     assert all(r["cell"] >= 2.5 + r["skin"] for r in t["table"])
+
+
+@pytest.mark.parametrize("pinned", [True, False])
+def test_step_host_matches_device_path(pinned):
+    """komd_gpu_step_host on the fused path reads r, v from the caller's buffers
+    and writes r, v, f back from inside the step's kernels (pinned buffers, or
+    plain pageable memory where the GPU walks the host page tables); the
+    trajectory is bitwise the one of komd_gpu_step on device-resident state,
+    for one step per call and for several."""
+    import torch
+    a = _replica(*SPECS[1])
+    b = _replica(*SPECS[1])
+    r0, v0, f0 = a.download()
+
+    def buf(x):
+        t = torch.from_numpy(np.ascontiguousarray(x))
+        return (t.pin_memory() if pinned else t.clone()).numpy()
+
+    r, v, f = buf(r0), buf(v0), buf(np.zeros_like(f0))
+    for n in (1, 1, 2, 5, 1):
+        a.step_host(n, r, v, f)
+        b.step(n)
+        rb, vb, fb = b.download()
+        assert np.array_equal(r, rb)
+        assert np.array_equal(v, vb)
+        assert np.array_equal(f, fb)
+    a.close()
+    b.close()
