@@ -1,0 +1,175 @@
+// atm_device.cuh -- device functions of the once-per-triplet ATM sweep,
+// shared by k_atm_s (kernels.cu) and the fused LJ + ATM pass (pair_tile.cu).
+#pragma once
+
+#include "engine.cuh"
+
+namespace komd {
+
+// FP32 ATM, FULL triplet set, forces only: every triplet once, from its
+// lowest slot i (the other two members are neighbours of i with larger
+// slots).  One warp per vertex; lane a owns staged neighbour a (a < m, the
+// neighbours above i) and evaluates the round-robin pairs (a, a+d mod m),
+// d = 1 .. m/2, directly.  Per triplet with A = |e_a|^2, B = |e_b|^2,
+// C = |e_b - e_a|^2 (e = r_i - r_x) and v_X = dV/dX / nu, the forces in units
+// of 2 sign nu are
+//   g_i = vA e_a + vB e_b,  g_a = -vA e_a + vC (e_b - e_a),  g_b = -vB e_b - vC (e_b - e_a).
+// g_i and g_a stay in the lane's registers; g_b reaches lane b by one warp
+// shuffle per component (lane r pulls from lane r - d mod m).  At the end the
+// per-neighbour and per-vertex sums go to 64-bit fixed-point accumulators by
+// integer atomics (order-independent: the forces are bitwise reproducible);
+// k_atm_flush adds them to f.
+constexpr double kAtmFix = 4294967296.0;   // 2^32 fixed-point units
+
+__device__ __forceinline__ void atm_fix_add(unsigned long long *acc, float x) {
+    // x * 2^32 is exact in FP32 (a power-of-two scale); one FP32 -> int64 conversion
+    const long long q = __float2ll_rn(x * 4294967296.0f);
+    if (q != 0) atomicAdd(acc, (unsigned long long)q);
+}
+
+struct AtmV {
+    float vA, vB, vC;
+};
+// dV/dA, dV/dB, dV/dC over nu from the squared sides and the staged (A, 1/A, 1/sqrt(A))
+__device__ __forceinline__ AtmV atm_derivs(float4 qa, float4 qb, float C) {
+    const float A = qa.x, B = qb.x;
+    const float wc = rsqrtf(C);
+    const float sv = qa.z * qb.z * wc;                  // 1/(abc)
+    const float s2 = sv * sv;
+    const float s5 = s2 * s2 * sv;
+    const float t1 = A + B - C, t2 = A - B + C, t3 = B + C - A;
+    const float u = t2 * t3, v = t1 * t3, w = t1 * t2;
+    const float P = t1 * u;
+    AtmV r;
+    r.vA = s5 * (-1.5f * B * C + 0.375f * (u + v - w) - 0.9375f * P * qa.y);
+    r.vB = s5 * (-1.5f * A * C + 0.375f * (u - v + w) - 0.9375f * P * qb.y);
+    r.vC = s5 * (-1.5f * A * B + 0.375f * (-u + v + w) - 0.9375f * P * (wc * wc));
+    return r;
+}
+
+// the round-robin sweep of one vertex: lane li = lane - gb owns staged
+// neighbour li < m and plays rounds d = d_first .. d_last (at most m/2) over
+// `rounds` loop trips (rounds past d_last do nothing); the lane's partial sum
+// for its neighbour is returned in (ax, ay, az).  The vertex's own share is
+// not summed here: per triplet g_i = -(g_a + g_b), so the vertex force is
+// minus the sum of its neighbours' shares.
+__device__ __forceinline__ void atm_sweep(const float4 *se, const float4 *sq, int m, int li, int gb, int d_first,
+                                          int d_last, int rounds, float rc2, float &ax, float &ay, float &az,
+                                          float4 &ea_out) {
+    const bool own = li < m;
+    const float4 ea = own ? se[li] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 qa = own ? sq[li] : make_float4(1.f, 1.f, 1.f, 0.f);
+    ea_out = ea;
+    // partner b = li + d and share source li - d (mod m), stepped per round;
+    // d <= m/2 keeps both within one wrap
+    int b = li + d_first, src = li - d_first;
+    if (b >= m) b -= m;
+    if (src < 0) src += m;
+    for (int t = 0; t < rounds; t++) {
+        const int d = d_first + t;
+        const bool act = own && d <= d_last;
+        float bx = 0.f, by = 0.f, bz = 0.f;
+        if (act && !(2 * d == m && li >= d)) {
+            const float4 eb = se[b];
+            const float cx = eb.x - ea.x, cy = eb.y - ea.y, cz = eb.z - ea.z;
+            const float C = cx * cx + cy * cy + cz * cz;
+            if (C <= rc2) {
+                const AtmV v = atm_derivs(qa, sq[b], C);
+                const float tx = v.vC * cx, ty = v.vC * cy, tz = v.vC * cz;
+                ax += tx - v.vA * ea.x;
+                ay += ty - v.vA * ea.y;
+                az += tz - v.vA * ea.z;
+                bx = -tx - v.vB * eb.x;
+                by = -ty - v.vB * eb.y;
+                bz = -tz - v.vB * eb.z;
+            }
+        }
+        // lane li pulls the share computed, in this lane group, by the lane whose partner it was
+        const int s = (act ? src : li) + gb;   // lanes without a round pull from themselves
+        const float rx = __shfl_sync(0xffffffffu, bx, s);
+        const float ry = __shfl_sync(0xffffffffu, by, s);
+        const float rz = __shfl_sync(0xffffffffu, bz, s);
+        if (act) { ax += rx; ay += ry; az += rz; }
+        b = b + 1 == m ? 0 : b + 1;
+        src = src == 0 ? m - 1 : src - 1;
+    }
+}
+
+// vertices with more than 32 neighbours above them: a plain pair loop with a
+// fixed-point atomic per contribution (rare at liquid densities)
+__device__ __forceinline__ void atm_pairs_slow(const AtmParams &p, const float4 *se, const float4 *sq, int m, int lane, float rc2,
+                               float &gx, float &gy, float &gz) {
+    for (int a = lane; a < m; a += 32) {
+        const float4 ea = se[a], qa = sq[a];
+        unsigned long long *acca = p.acc + 3 * (size_t)(__float_as_int(ea.w) >> 6);
+        for (int b = a + 1; b < m; b++) {
+            const float4 eb = se[b];
+            const float cx = eb.x - ea.x, cy = eb.y - ea.y, cz = eb.z - ea.z;
+            const float C = cx * cx + cy * cy + cz * cz;
+            if (C > rc2) continue;
+            const AtmV t = atm_derivs(qa, sq[b], C);
+            gx += t.vA * ea.x + t.vB * eb.x;
+            gy += t.vA * ea.y + t.vB * eb.y;
+            gz += t.vA * ea.z + t.vB * eb.z;
+            unsigned long long *accb = p.acc + 3 * (size_t)(__float_as_int(eb.w) >> 6);
+            atm_fix_add(acca, t.vC * cx - t.vA * ea.x);
+            atm_fix_add(acca + 1, t.vC * cy - t.vA * ea.y);
+            atm_fix_add(acca + 2, t.vC * cz - t.vA * ea.z);
+            atm_fix_add(accb, -t.vC * cx - t.vB * eb.x);
+            atm_fix_add(accb + 1, -t.vC * cy - t.vB * eb.y);
+            atm_fix_add(accb + 2, -t.vC * cz - t.vB * eb.z);
+        }
+    }
+}
+
+__device__ __forceinline__ void atm_vertex_out(const AtmParams &p, int i, float gx, float gy, float gz) {
+    atm_fix_add(p.acc + 3 * (size_t)i, gx);
+    atm_fix_add(p.acc + 3 * (size_t)i + 1, gy);
+    atm_fix_add(p.acc + 3 * (size_t)i + 2, gz);
+}
+
+// the sweep of one vertex whose m neighbours above it are staged in se / sq
+// (e = r_i - r_x and code; |e|^2, 1/|e|^2, 1/|e|): with at most 16 the two
+// half-warps split the rounds (lower and upper half of d), each delivering
+// shares within itself, and their partial sums per neighbour are added; the
+// neighbours' sums and the vertex's (minus their total) go to the fixed-point
+// accumulators
+__device__ __forceinline__ void atm_vertex(const AtmParams &p, int i, const float4 *se, const float4 *sq, int m,
+                                           int lane, float rc2) {
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+    const int half = m / 2;
+    if (m <= 32) {
+        float ax = 0.f, ay = 0.f, az = 0.f;
+        float4 ea;
+        if (m <= 16) {
+            const int g = lane >> 4, li = lane & 15;
+            const int h1 = (half + 1) / 2;                     // rounds of the lower half-warp
+            const int d_first = g ? h1 + 1 : 1, d_last = g ? half : h1;
+            atm_sweep(se, sq, m, li, 16 * g, d_first, d_last, h1, rc2, ax, ay, az, ea);
+            ax += __shfl_xor_sync(0xffffffffu, ax, 16);
+            ay += __shfl_xor_sync(0xffffffffu, ay, 16);
+            az += __shfl_xor_sync(0xffffffffu, az, 16);
+        } else {
+            atm_sweep(se, sq, m, lane, 0, 1, half, half, rc2, ax, ay, az, ea);
+        }
+        if (lane < m) {
+            unsigned long long *acc = p.acc + 3 * (size_t)(__float_as_int(ea.w) >> 6);
+            atm_fix_add(acc, ax);
+            atm_fix_add(acc + 1, ay);
+            atm_fix_add(acc + 2, az);
+            gx = -ax;
+            gy = -ay;
+            gz = -az;
+        }
+    } else {
+        atm_pairs_slow(p, se, sq, m, lane, rc2, gx, gy, gz);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        gx += __shfl_xor_sync(0xffffffffu, gx, o);
+        gy += __shfl_xor_sync(0xffffffffu, gy, o);
+        gz += __shfl_xor_sync(0xffffffffu, gz, o);
+    }
+    if (lane == 0) atm_vertex_out(p, i, gx, gy, gz);
+}
+
+}  // namespace komd

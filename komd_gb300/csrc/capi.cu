@@ -195,6 +195,11 @@ void enqueue_surrogate(komd_gpu *h, double *fout) {
     launch_sur_apply(p, e.slot_site, e.f, fout, e.stream);
 }
 
+bool fused_lj_atm(komd_gpu *h, bool measure) {
+    const Engine &e = h->e;
+    return !measure && !surrogate_on(h) && e.atm_acc != nullptr && e.verlet && (e.cfg.terms & KOMD_TERM_ATM);
+}
+
 // the force sequence of Simulation::run: 2-body functors (LJ / FENE, bonded,
 // Limit), then the 3-body functor (ATM, exact or learned)
 // returns true when integrate1 was fused into the last force kernel (with_step1)
@@ -205,15 +210,20 @@ bool enqueue_forces(komd_gpu *h, bool measure, double *lj_hist, bool with_step1 
     int pair_blocks;
     // a force-only pass whose ATM list goes only to the once-per-triplet kernel
     // needs the neighbours above each site only
-    e.atm_up = !measure && !surrogate_on(h) && e.atm_acc != nullptr && e.verlet;
-    if (measure || (e.cfg.terms & (KOMD_TERM_LJ | KOMD_TERM_FENE | KOMD_TERM_ATM))) {
+    // force-only FP32 FULL ATM on the Verlet path: the LJ pass sweeps each site's
+    // triplets itself (k_lj_atm) and the ATM list never goes to memory
+    const bool lj_atm = fused_lj_atm(h, measure);
+    if (lj_atm) {
+        ProfScope ps(h, F_PAIR);
+        launch_lj_atm(e, st);   // writes f (first writer); ATM sums to the fixed-point accumulators
+        pair_blocks = 0;
+    } else if (measure || (e.cfg.terms & (KOMD_TERM_LJ | KOMD_TERM_FENE | KOMD_TERM_ATM))) {
         ProfScope ps(h, F_PAIR);
         pair_blocks = launch_pair(e, st, measure, lj_hist);   // the pair pass writes f (first writer)
     } else {
         pair_blocks = 0;
         cudaMemsetAsync(e.f, 0, sizeof(double) * 3 * e.n, st);
     }
-    e.atm_up = false;
     if (measure) launch_sum_partials(st, pair_blocks, e.partials, h->acc);
     if (e.cfg.terms & KOMD_TERM_TABULATED) {   // in the LJ functor's place (IBI.cpp:52-54), before Limit
         ProfScope ps(h, F_PAIR);
@@ -236,7 +246,7 @@ bool enqueue_forces(komd_gpu *h, bool measure, double *lj_hist, bool with_step1 
     } else if (e.cfg.terms & KOMD_TERM_ATM) {
         {
             ProfScope ps(h, F_ATM);
-            fused = launch_atm(e, st, measure, with_step1);
+            fused = lj_atm ? launch_atm_flush(e, st, with_step1) : launch_atm(e, st, measure, with_step1);
         }
         if (measure) launch_sum_partials(st, atm_grid(e), e.partials, h->acc);
     }
@@ -1761,8 +1771,8 @@ int komd_gpu_kernels_per_step(komd_gpu *h) {
     if (e.cfg.terms & KOMD_TERM_LIMIT) k++;
     if (e.cfg.thermostat) k += 3;  /* kinetic sums, partial reduction, velocity scaling */
     if (surrogate_on(h)) k += 4;   /* descriptors, MLP, forces, apply */
-    else if (e.cfg.terms & KOMD_TERM_ATM)   /* once-per-triplet kernel + flush in FP32 FULL mode */
-        k += (e.atm_acc != nullptr) ? 2 : 1;
+    else if (e.cfg.terms & KOMD_TERM_ATM)   /* once-per-triplet kernel (inside the LJ pass on the Verlet path) + flush */
+        k += (e.atm_acc != nullptr) ? (fused_lj_atm(h, false) ? 1 : 2) : 1;
     return k;
 }
 

@@ -12,6 +12,7 @@
 
 #include "engine.cuh"
 #include "kernels.cuh"
+#include "atm_device.cuh"
 
 namespace komd {
 
@@ -1339,47 +1340,6 @@ size_t atm_smem(const Engine &e) {
     return (size_t)kWarpsPerBlock * e.nl_cap * per;
 }
 
-// FP32 ATM, FULL triplet set, forces only: every triplet once, from its
-// lowest slot i (the other two members are neighbours of i with larger
-// slots).  One warp per vertex; lane a owns staged neighbour a (a < m, the
-// neighbours above i) and evaluates the round-robin pairs (a, a+d mod m),
-// d = 1 .. m/2, directly.  Per triplet with A = |e_a|^2, B = |e_b|^2,
-// C = |e_b - e_a|^2 (e = r_i - r_x) and v_X = dV/dX / nu, the forces in units
-// of 2 sign nu are
-//   g_i = vA e_a + vB e_b,  g_a = -vA e_a + vC (e_b - e_a),  g_b = -vB e_b - vC (e_b - e_a).
-// g_i and g_a stay in the lane's registers; g_b reaches lane b by one warp
-// shuffle per component (lane r pulls from lane r - d mod m).  At the end the
-// per-neighbour and per-vertex sums go to 64-bit fixed-point accumulators by
-// integer atomics (order-independent: the forces are bitwise reproducible);
-// k_atm_flush adds them to f.
-constexpr double kAtmFix = 4294967296.0;   // 2^32 fixed-point units
-
-__device__ __forceinline__ void atm_fix_add(unsigned long long *acc, float x) {
-    // x * 2^32 is exact in FP32 (a power-of-two scale); one FP32 -> int64 conversion
-    const long long q = __float2ll_rn(x * 4294967296.0f);
-    if (q != 0) atomicAdd(acc, (unsigned long long)q);
-}
-
-struct AtmV {
-    float vA, vB, vC;
-};
-// dV/dA, dV/dB, dV/dC over nu from the squared sides and the staged (A, 1/A, 1/sqrt(A))
-__device__ __forceinline__ AtmV atm_derivs(float4 qa, float4 qb, float C) {
-    const float A = qa.x, B = qb.x;
-    const float wc = rsqrtf(C);
-    const float sv = qa.z * qb.z * wc;                  // 1/(abc)
-    const float s2 = sv * sv;
-    const float s5 = s2 * s2 * sv;
-    const float t1 = A + B - C, t2 = A - B + C, t3 = B + C - A;
-    const float u = t2 * t3, v = t1 * t3, w = t1 * t2;
-    const float P = t1 * u;
-    AtmV r;
-    r.vA = s5 * (-1.5f * B * C + 0.375f * (u + v - w) - 0.9375f * P * qa.y);
-    r.vB = s5 * (-1.5f * A * C + 0.375f * (u - v + w) - 0.9375f * P * qb.y);
-    r.vC = s5 * (-1.5f * A * B + 0.375f * (-u + v + w) - 0.9375f * P * (wc * wc));
-    return r;
-}
-
 // stage vertex i's neighbours above i (ballot compaction); returns their count
 __device__ __forceinline__ int atm_stage(const AtmParams &p, int i, float4 *se, float4 *sq, int lane, unsigned lt) {
     const int ni = min(p.nl_count[i], p.nl_cap);
@@ -1404,90 +1364,7 @@ __device__ __forceinline__ int atm_stage(const AtmParams &p, int i, float4 *se, 
     return m;
 }
 
-// the round-robin sweep of one vertex: lane li = lane - gb owns staged
-// neighbour li < m and plays rounds d = d_first .. d_last (at most m/2) over
-// `rounds` loop trips (rounds past d_last do nothing); the lane's partial sum
-// for its neighbour is returned in (ax, ay, az).  The vertex's own share is
-// not summed here: per triplet g_i = -(g_a + g_b), so the vertex force is
-// minus the sum of its neighbours' shares.
-__device__ __forceinline__ void atm_sweep(const float4 *se, const float4 *sq, int m, int li, int gb, int d_first,
-                                          int d_last, int rounds, float rc2, float &ax, float &ay, float &az,
-                                          float4 &ea_out) {
-    const bool own = li < m;
-    const float4 ea = own ? se[li] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 qa = own ? sq[li] : make_float4(1.f, 1.f, 1.f, 0.f);
-    ea_out = ea;
-    // partner b = li + d and share source li - d (mod m), stepped per round;
-    // d <= m/2 keeps both within one wrap
-    int b = li + d_first, src = li - d_first;
-    if (b >= m) b -= m;
-    if (src < 0) src += m;
-    for (int t = 0; t < rounds; t++) {
-        const int d = d_first + t;
-        const bool act = own && d <= d_last;
-        float bx = 0.f, by = 0.f, bz = 0.f;
-        if (act && !(2 * d == m && li >= d)) {
-            const float4 eb = se[b];
-            const float cx = eb.x - ea.x, cy = eb.y - ea.y, cz = eb.z - ea.z;
-            const float C = cx * cx + cy * cy + cz * cz;
-            if (C <= rc2) {
-                const AtmV v = atm_derivs(qa, sq[b], C);
-                const float tx = v.vC * cx, ty = v.vC * cy, tz = v.vC * cz;
-                ax += tx - v.vA * ea.x;
-                ay += ty - v.vA * ea.y;
-                az += tz - v.vA * ea.z;
-                bx = -tx - v.vB * eb.x;
-                by = -ty - v.vB * eb.y;
-                bz = -tz - v.vB * eb.z;
-            }
-        }
-        // lane li pulls the share computed, in this lane group, by the lane whose partner it was
-        const int s = (act ? src : li) + gb;   // lanes without a round pull from themselves
-        const float rx = __shfl_sync(0xffffffffu, bx, s);
-        const float ry = __shfl_sync(0xffffffffu, by, s);
-        const float rz = __shfl_sync(0xffffffffu, bz, s);
-        if (act) { ax += rx; ay += ry; az += rz; }
-        b = b + 1 == m ? 0 : b + 1;
-        src = src == 0 ? m - 1 : src - 1;
-    }
-}
-
-// vertices with more than 32 neighbours above them: a plain pair loop with a
-// fixed-point atomic per contribution (rare at liquid densities)
-__device__ void atm_pairs_slow(const AtmParams &p, const float4 *se, const float4 *sq, int m, int lane, float rc2,
-                               float &gx, float &gy, float &gz) {
-    for (int a = lane; a < m; a += 32) {
-        const float4 ea = se[a], qa = sq[a];
-        unsigned long long *acca = p.acc + 3 * (size_t)(__float_as_int(ea.w) >> 6);
-        for (int b = a + 1; b < m; b++) {
-            const float4 eb = se[b];
-            const float cx = eb.x - ea.x, cy = eb.y - ea.y, cz = eb.z - ea.z;
-            const float C = cx * cx + cy * cy + cz * cz;
-            if (C > rc2) continue;
-            const AtmV t = atm_derivs(qa, sq[b], C);
-            gx += t.vA * ea.x + t.vB * eb.x;
-            gy += t.vA * ea.y + t.vB * eb.y;
-            gz += t.vA * ea.z + t.vB * eb.z;
-            unsigned long long *accb = p.acc + 3 * (size_t)(__float_as_int(eb.w) >> 6);
-            atm_fix_add(acca, t.vC * cx - t.vA * ea.x);
-            atm_fix_add(acca + 1, t.vC * cy - t.vA * ea.y);
-            atm_fix_add(acca + 2, t.vC * cz - t.vA * ea.z);
-            atm_fix_add(accb, -t.vC * cx - t.vB * eb.x);
-            atm_fix_add(accb + 1, -t.vC * cy - t.vB * eb.y);
-            atm_fix_add(accb + 2, -t.vC * cz - t.vB * eb.z);
-        }
-    }
-}
-
-__device__ __forceinline__ void atm_vertex_out(const AtmParams &p, int i, float gx, float gy, float gz) {
-    atm_fix_add(p.acc + 3 * (size_t)i, gx);
-    atm_fix_add(p.acc + 3 * (size_t)i + 1, gy);
-    atm_fix_add(p.acc + 3 * (size_t)i + 2, gz);
-}
-
-// one warp per vertex; with at most 16 neighbours above the vertex the two
-// half-warps split the rounds (lower and upper half of d), each delivering
-// shares within itself, and their partial sums per neighbour are added
+// one warp per vertex: stage its neighbours above it, then the sweep
 __global__ void __launch_bounds__(kBlock) k_atm_s(AtmParams p) {
     extern __shared__ float4 s_dyn[];
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1495,45 +1372,11 @@ __global__ void __launch_bounds__(kBlock) k_atm_s(AtmParams p) {
     float4 *se = s_dyn + wib * 2 * cap, *sq = se + cap;
     const int i = blockIdx.x * kWarpsPerBlock + wib;
     if (i >= p.n) return;
-    const float rc2 = (float)p.rc2;
     unsigned lt;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
     const int m = atm_stage(p, i, se, sq, lane, lt);
     __syncwarp();
-    float gx = 0.f, gy = 0.f, gz = 0.f;
-    const int half = m / 2;
-    if (m <= 32) {
-        float ax = 0.f, ay = 0.f, az = 0.f;
-        float4 ea;
-        if (m <= 16) {
-            const int g = lane >> 4, li = lane & 15;
-            const int h1 = (half + 1) / 2;                     // rounds of the lower half-warp
-            const int d_first = g ? h1 + 1 : 1, d_last = g ? half : h1;
-            atm_sweep(se, sq, m, li, 16 * g, d_first, d_last, h1, rc2, ax, ay, az, ea);
-            ax += __shfl_xor_sync(0xffffffffu, ax, 16);
-            ay += __shfl_xor_sync(0xffffffffu, ay, 16);
-            az += __shfl_xor_sync(0xffffffffu, az, 16);
-        } else {
-            atm_sweep(se, sq, m, lane, 0, 1, half, half, rc2, ax, ay, az, ea);
-        }
-        if (lane < m) {
-            unsigned long long *acc = p.acc + 3 * (size_t)(__float_as_int(ea.w) >> 6);
-            atm_fix_add(acc, ax);
-            atm_fix_add(acc + 1, ay);
-            atm_fix_add(acc + 2, az);
-            gx = -ax;
-            gy = -ay;
-            gz = -az;
-        }
-    } else {
-        atm_pairs_slow(p, se, sq, m, lane, rc2, gx, gy, gz);
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        gx += __shfl_xor_sync(0xffffffffu, gx, o);
-        gy += __shfl_xor_sync(0xffffffffu, gy, o);
-        gz += __shfl_xor_sync(0xffffffffu, gz, o);
-    }
-    if (lane == 0) atm_vertex_out(p, i, gx, gy, gz);
+    atm_vertex(p, i, se, sq, m, lane, (float)p.rc2);
 }
 
 // the same flush fused with Integrator::integrate1 of the step (ATM is the
@@ -1619,7 +1462,7 @@ void atm_dispatch<float>(AtmParams &p, bool measure, bool compat, int grid, size
     }
 }
 
-bool launch_atm(Engine &e, cudaStream_t st, bool measure, bool with_step1) {
+AtmParams atm_params(const Engine &e) {
     AtmParams p;
     p.n = (int)e.n;
     p.slot_site = e.slot_site;
@@ -1635,19 +1478,31 @@ bool launch_atm(Engine &e, cudaStream_t st, bool measure, bool with_step1) {
     p.atm_direct = e.cfg.atm_direct;
     p.e_site = e.atm_esite;
     p.acc = e.atm_acc;
+    return p;
+}
+
+// the fixed-point sums of the once-per-triplet sweep into f (and, with_step1,
+// integrate1 of the step); returns with_step1
+bool launch_atm_flush(Engine &e, cudaStream_t st, bool with_step1) {
+    const double sign = e.cfg.atm_sign == KOMD_ATM_SIGN_REFERENCE ? 1.0 : -1.0;
+    const double scale_fix = 2.0 * sign * e.cfg.nu / kAtmFix;
+    if (with_step1) {
+        k_atm_flush_step1<<<nblk(e.n, kIoBlock), kIoBlock, 0, st>>>((int)e.n, e.site_slot, e.atm_acc, e.f, scale_fix,
+                                                                     e.v, e.hdtm, e.err,
+                                                                     e.verlet ? e.rebuild : nullptr, e.hout_f, e.hout_v);
+        return true;
+    }
+    k_atm_flush<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.slot_site, e.atm_acc, e.f, scale_fix);
+    return false;
+}
+
+bool launch_atm(Engine &e, cudaStream_t st, bool measure, bool with_step1) {
+    AtmParams p = atm_params(e);
     const bool compat = e.cfg.atm_enum == KOMD_ATM_ENUM_COMPAT;
     if (!measure && !compat && e.cfg.precision == KOMD_FP32 && e.atm_acc) {
         // every triplet once (lowest slot), fixed-point scatter, then the flush into f
         k_atm_s<<<atm_grid(e), kBlock, atm_smem(e), st>>>(p);
-        if (with_step1) {
-            k_atm_flush_step1<<<nblk(e.n, kIoBlock), kIoBlock, 0, st>>>((int)e.n, e.site_slot, e.atm_acc, e.f,
-                                                                2.0 * p.sign * p.nu / kAtmFix, e.v, e.hdtm, e.err,
-                                                                e.verlet ? e.rebuild : nullptr, e.hout_f, e.hout_v);
-            return true;
-        }
-        k_atm_flush<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.slot_site, e.atm_acc, e.f,
-                                                      2.0 * p.sign * p.nu / kAtmFix);
-        return false;
+        return launch_atm_flush(e, st, with_step1);
     }
     if (e.cfg.precision == KOMD_FP64) atm_dispatch<double>(p, measure, compat, atm_grid(e), atm_smem(e), st);
     else atm_dispatch<float>(p, measure, compat, atm_grid(e), atm_smem(e), st);

@@ -16,6 +16,10 @@ void launch_limit(Engine &e, cudaStream_t st);
 // ATM forces; with_step1 (step graphs only) lets the FULL FP32 path fuse
 // integrate1 into its flush: returns true when it did
 bool launch_atm(Engine &e, cudaStream_t st, bool measure, bool with_step1 = false);
+AtmParams atm_params(const Engine &e);
+bool launch_atm_flush(Engine &e, cudaStream_t st, bool with_step1);
+// LJ forces and the once-per-triplet ATM sweep in one pass (FP32, FULL, Verlet)
+void launch_lj_atm(Engine &e, cudaStream_t st);
 // in_step (step graphs only): the fused drift path when the engine qualifies
 void launch_step0(Engine &e, cudaStream_t st, bool in_step = false);
 void launch_step1(Engine &e, cudaStream_t st);

@@ -16,6 +16,7 @@
 // Full shell: each site's force is summed by its own CTA, no global atomics.
 #include "engine.cuh"
 #include "kernels.cuh"
+#include "atm_device.cuh"
 
 namespace komd {
 
@@ -390,8 +391,126 @@ __global__ void __launch_bounds__(kTileThreads) k_vlist_build(PairParams p) {
 // cell.  Inside cutoff_3b the pair is appended to the ATM list in list
 // order.  No atomics: the warp owns its site.
 // ---------------------------------------------------------------------------
+// The LJ pass over site i's Verlet row (one warp, lanes over the entries):
+// the site's LJ force to f, and inside cutoff_3b the pair appended to the ATM
+// list in list order -- to the global list, or (TO_SMEM) staged in shared
+// memory (se, sq) for the sweep that follows in the same warp.  Returns the
+// number of ATM neighbours kept.
 // U = list entries per lane in flight (independent loads for latency hiding):
 // a warp covers 32 U entries of a row per pass
+template <bool MEASURE, bool EMIT, bool UNIFORM, int U, bool TO_SMEM>
+__device__ __forceinline__ int lj_site(const PairParams &p, int i, int lane, unsigned lt, float rc2, float rc3sq,
+                                       float4 *se, float4 *sq, float &m_u, float &m_pairs, float (&m_w)[6]) {
+    const int cnt = p.vl_count[i];
+    const float4 pi = p.pos4[i];
+    const float sei = UNIFORM ? 0.f : p.seps[i];
+    const float4 *off = p.nboff + (size_t)p.slot_cell[i] * 27;
+    const unsigned *row = p.vl + (size_t)i * p.vl_cap;
+    const float sg2u = p.sig0 * p.sig0, eeu = p.eps0;
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    int c_atm = 0;
+    for (int k0 = 0; k0 < cnt; k0 += 32 * U) {
+        unsigned e[U];
+        float4 o[U], pj[U];
+        float sej[U];
+        // rows hold vl_cap entries: the first pass loads speculatively up to the
+        // capacity so that it does not wait for the count; later passes stop at it
+        const int lim = k0 == 0 ? p.vl_cap : cnt;
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int k = k0 + u * 32 + lane;
+            e[u] = k < lim ? __ldcs(row + k) : 0xffffffffu;   // read once per step: evict first
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++)
+            if (k0 + u * 32 + lane >= cnt) e[u] = 0xffffffffu;
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            if (e[u] != 0xffffffffu) {
+                o[u] = off[(e[u] >> 26) & 31u];
+                pj[u] = p.pos4[e[u] & 0x3ffffffu];
+                if (!UNIFORM) sej[u] = p.seps[e[u] & 0x3ffffffu];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const bool valid = e[u] != 0xffffffffu;
+            float dx = 0.f, dy = 0.f, dz = 0.f, r2 = 1e30f;
+            if (valid) {
+                dx = pi.x - (pj[u].x + o[u].x);
+                dy = pi.y - (pj[u].y + o[u].y);
+                dz = pi.z - (pj[u].z + o[u].z);
+                r2 = dx * dx + dy * dy + dz * dz;
+                if (p.use_lj && r2 <= rc2 && !(e[u] >> 31)) {
+                    const float inv = rcp_approx(r2);
+                    float x, ee;
+                    if (UNIFORM) {
+                        x = sg2u * inv;
+                        ee = eeu;
+                    } else {
+                        const float sg = pi.w + pj[u].w;
+                        x = sg * sg * inv;
+                        ee = sei * sej[u];
+                    }
+                    const float lj6 = x * x * x;
+                    const float fac0 = 24.0f * ee * (2.0f * lj6 * lj6 - lj6) * inv;
+                    const float fac = MEASURE ? fac0 : fac0 * p.lj_fscalef;   // ATM2B factor
+                    fx += dx * fac; fy += dy * fac; fz += dz * fac;
+                    if (MEASURE) {
+                        const float gx = dx * fac, gy = dy * fac, gz = dz * fac;
+                        m_u += 2.0f * ee * (lj6 * lj6 - lj6);
+                        m_pairs += 0.5f;
+                        m_w[0] += 0.5f * dx * gx;
+                        m_w[1] += 0.25f * (dx * gy + dy * gx);
+                        m_w[2] += 0.5f * dy * gy;
+                        m_w[3] += 0.25f * (dx * gz + dz * gx);
+                        m_w[4] += 0.25f * (dy * gz + dz * gy);
+                        m_w[5] += 0.5f * dz * gz;
+                    }
+                }
+            }
+            if (EMIT) {
+                // with atm_up (or into shared memory) the once-per-triplet sweep reads
+                // the list: neighbours above i only
+                const bool emit =
+                    valid && r2 <= rc3sq && ((!TO_SMEM && !p.atm_up) || (int)(e[u] & 0x3ffffffu) > i);
+                const unsigned m = __ballot_sync(0xffffffffu, emit);
+                if (emit) {
+                    const int pos = c_atm + __popc(m & lt);
+                    const int nb = (int)((e[u] >> 26) & 31u), j = (int)(e[u] & 0x3ffffffu);
+                    const int code = nb | (o[u].w != 0.f ? 32 : 0) | (j << 6);
+                    if (pos < p.nl_cap) {
+                        const float4 entry = make_float4(dx, dy, dz, __int_as_float(code));
+                        if (TO_SMEM) {   // staged as the sweep wants it: e and (A, 1/A, 1/sqrt A)
+                            se[pos] = entry;
+                            sq[pos] = make_float4(r2, 1.0f / r2, rsqrtf(r2), 0.f);
+                        } else {
+                            p.nl[(size_t)i * p.nl_cap + pos] = entry;
+                        }
+                    }
+                }
+                c_atm += __popc(m);
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        fx += __shfl_xor_sync(0xffffffffu, fx, o);
+        fy += __shfl_xor_sync(0xffffffffu, fy, o);
+        fz += __shfl_xor_sync(0xffffffffu, fz, o);
+    }
+    if (lane == 0) {
+        const int site = p.slot_site[i];
+        p.f[3 * site] = (double)fx;
+        p.f[3 * site + 1] = (double)fy;
+        p.f[3 * site + 2] = (double)fz;
+        if (EMIT) {
+            if (!TO_SMEM) p.nl_count[i] = min(c_atm, p.nl_cap);
+            if (c_atm > p.nl_cap) atomicOr(&p.err[E_ATM_OVERFLOW], 1);
+        }
+    }
+    return min(c_atm, p.nl_cap);
+}
+
 template <bool MEASURE, bool EMIT, bool UNIFORM, int U>
 __global__ void __launch_bounds__(256, U == 3 ? 4 : 5) k_lj_vlist(PairParams p, int n, int per) {
     __shared__ double s_part[8][8];
@@ -403,107 +522,8 @@ __global__ void __launch_bounds__(256, U == 3 ? 4 : 5) k_lj_vlist(PairParams p, 
     // each block walks `per` consecutive groups of 8 slots: neighbouring slots share
     // most of their neighbours, so the gathers of one group hit L1 lines of the last
     for (int it = 0; it < per; it++) {
-    const int i = (blockIdx.x * per + it) * 8 + w;
-    if (i < n) {
-        const int cnt = p.vl_count[i];
-        const float4 pi = p.pos4[i];
-        const float sei = UNIFORM ? 0.f : p.seps[i];
-        const float4 *off = p.nboff + (size_t)p.slot_cell[i] * 27;
-        const unsigned *row = p.vl + (size_t)i * p.vl_cap;
-        const float sg2u = p.sig0 * p.sig0, eeu = p.eps0;
-        float fx = 0.f, fy = 0.f, fz = 0.f;
-        int c_atm = 0;
-        for (int k0 = 0; k0 < cnt; k0 += 32 * U) {
-            unsigned e[U];
-            float4 o[U], pj[U];
-            float sej[U];
-            // rows hold vl_cap entries: the first pass loads speculatively up to the
-            // capacity so that it does not wait for the count; later passes stop at it
-            const int lim = k0 == 0 ? p.vl_cap : cnt;
-#pragma unroll
-            for (int u = 0; u < U; u++) {
-                const int k = k0 + u * 32 + lane;
-                e[u] = k < lim ? __ldcs(row + k) : 0xffffffffu;   // read once per step: evict first
-            }
-#pragma unroll
-            for (int u = 0; u < U; u++)
-                if (k0 + u * 32 + lane >= cnt) e[u] = 0xffffffffu;
-#pragma unroll
-            for (int u = 0; u < U; u++) {
-                if (e[u] != 0xffffffffu) {
-                    o[u] = off[(e[u] >> 26) & 31u];
-                    pj[u] = p.pos4[e[u] & 0x3ffffffu];
-                    if (!UNIFORM) sej[u] = p.seps[e[u] & 0x3ffffffu];
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < U; u++) {
-                const bool valid = e[u] != 0xffffffffu;
-                float dx = 0.f, dy = 0.f, dz = 0.f, r2 = 1e30f;
-                if (valid) {
-                    dx = pi.x - (pj[u].x + o[u].x);
-                    dy = pi.y - (pj[u].y + o[u].y);
-                    dz = pi.z - (pj[u].z + o[u].z);
-                    r2 = dx * dx + dy * dy + dz * dz;
-                    if (p.use_lj && r2 <= rc2 && !(e[u] >> 31)) {
-                        const float inv = rcp_approx(r2);
-                        float x, ee;
-                        if (UNIFORM) {
-                            x = sg2u * inv;
-                            ee = eeu;
-                        } else {
-                            const float sg = pi.w + pj[u].w;
-                            x = sg * sg * inv;
-                            ee = sei * sej[u];
-                        }
-                        const float lj6 = x * x * x;
-                        const float fac0 = 24.0f * ee * (2.0f * lj6 * lj6 - lj6) * inv;
-                        const float fac = MEASURE ? fac0 : fac0 * p.lj_fscalef;   // ATM2B factor
-                        fx += dx * fac; fy += dy * fac; fz += dz * fac;
-                        if (MEASURE) {
-                            const float gx = dx * fac, gy = dy * fac, gz = dz * fac;
-                            m_u += 2.0f * ee * (lj6 * lj6 - lj6);
-                            m_pairs += 0.5f;
-                            m_w[0] += 0.5f * dx * gx;
-                            m_w[1] += 0.25f * (dx * gy + dy * gx);
-                            m_w[2] += 0.5f * dy * gy;
-                            m_w[3] += 0.25f * (dx * gz + dz * gx);
-                            m_w[4] += 0.25f * (dy * gz + dz * gy);
-                            m_w[5] += 0.5f * dz * gz;
-                        }
-                    }
-                }
-                if (EMIT) {
-                    // with atm_up the once-per-triplet kernel reads the list: neighbours above i only
-                    const bool emit = valid && r2 <= rc3sq && (!p.atm_up || (int)(e[u] & 0x3ffffffu) > i);
-                    const unsigned m = __ballot_sync(0xffffffffu, emit);
-                    if (emit) {
-                        const int pos = c_atm + __popc(m & lt);
-                        const int nb = (int)((e[u] >> 26) & 31u), j = (int)(e[u] & 0x3ffffffu);
-                        const int code = nb | (o[u].w != 0.f ? 32 : 0) | (j << 6);
-                        if (pos < p.nl_cap)
-                            p.nl[(size_t)i * p.nl_cap + pos] = make_float4(dx, dy, dz, __int_as_float(code));
-                    }
-                    c_atm += __popc(m);
-                }
-            }
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            fx += __shfl_xor_sync(0xffffffffu, fx, o);
-            fy += __shfl_xor_sync(0xffffffffu, fy, o);
-            fz += __shfl_xor_sync(0xffffffffu, fz, o);
-        }
-        if (lane == 0) {
-            const int site = p.slot_site[i];
-            p.f[3 * site] = (double)fx;
-            p.f[3 * site + 1] = (double)fy;
-            p.f[3 * site + 2] = (double)fz;
-            if (EMIT) {
-                p.nl_count[i] = min(c_atm, p.nl_cap);
-                if (c_atm > p.nl_cap) atomicOr(&p.err[E_ATM_OVERFLOW], 1);
-            }
-        }
-    }
+        const int i = (blockIdx.x * per + it) * 8 + w;
+        if (i < n) lj_site<MEASURE, EMIT, UNIFORM, U, false>(p, i, lane, lt, rc2, rc3sq, nullptr, nullptr, m_u, m_pairs, m_w);
     }
     if (MEASURE) {
         double vals[8] = {m_u, m_w[0], m_w[1], m_w[2], m_w[3], m_w[4], m_w[5], m_pairs};
@@ -524,6 +544,32 @@ __global__ void __launch_bounds__(256, U == 3 ? 4 : 5) k_lj_vlist(PairParams p, 
             if (src >= 0)
                 for (int k = 0; k < 8; k++) s += s_part[k][src];
             p.partials[(size_t)blockIdx.x * R_NSLOTS + tid] = s;
+        }
+    }
+}
+
+// LJ and ATM in one pass (FP32 forces, FULL triplets, Verlet path): each warp
+// runs the LJ pass of its site, stages the site's ATM neighbours above it in
+// shared memory instead of the global list, and sweeps its triplets at once.
+// Warps in their latency-bound LJ phase and warps in their issue-bound sweep
+// share each SM, and the ATM list never goes to memory.  The arithmetic and
+// the order of every sum are those of k_lj_vlist + k_atm_s.
+template <bool UNIFORM, int U>
+__global__ void __launch_bounds__(256, 4) k_lj_atm(PairParams p, AtmParams a, int n, int per) {
+    extern __shared__ float4 s_dyn[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    float4 *se = s_dyn + w * 2 * p.nl_cap, *sq = se + p.nl_cap;
+    const float rc2 = (float)p.rc2, rc3sq = (float)p.rc3sq, rc3f = (float)a.rc2;
+    unsigned lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+    float m_u = 0.f, m_pairs = 0.f, m_w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int it = 0; it < per; it++) {
+        const int i = (blockIdx.x * per + it) * 8 + w;
+        if (i < n) {
+            const int m = lj_site<false, true, UNIFORM, U, true>(p, i, lane, lt, rc2, rc3sq, se, sq, m_u, m_pairs, m_w);
+            __syncwarp();
+            atm_vertex(a, i, se, sq, m, lane, rc3f);
+            __syncwarp();   // se / sq are refilled by the next site
         }
     }
 }
@@ -575,6 +621,34 @@ int launch_lj_vlist(Engine &e, PairParams &p, bool measure, bool emit, cudaStrea
     if (e.uniform) lj_vlist_dispatch<true>(p, (int)e.n, grid, per, measure, emit, u3, st);
     else lj_vlist_dispatch<false>(p, (int)e.n, grid, per, measure, emit, u3, st);
     return grid;
+}
+
+void launch_lj_atm(Engine &e, cudaStream_t st) {
+    e.atm_up = true;
+    PairParams p = pair_params(e);
+    e.atm_up = false;
+    const AtmParams a = atm_params(e);
+    const int per = vlist_per(e);
+    const int grid = (vlist_grid(e) + per - 1) / per;
+    const size_t sm = (size_t)8 * 2 * sizeof(float4) * (size_t)e.nl_cap;
+    const bool u3 = vlist_u3(e);
+    if (e.uniform) {
+        if (u3) {
+            if (sm > 48 * 1024) cudaFuncSetAttribute(k_lj_atm<true, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            k_lj_atm<true, 3><<<grid, 256, sm, st>>>(p, a, (int)e.n, per);
+        } else {
+            if (sm > 48 * 1024) cudaFuncSetAttribute(k_lj_atm<true, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            k_lj_atm<true, 2><<<grid, 256, sm, st>>>(p, a, (int)e.n, per);
+        }
+    } else {
+        if (u3) {
+            if (sm > 48 * 1024) cudaFuncSetAttribute(k_lj_atm<false, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            k_lj_atm<false, 3><<<grid, 256, sm, st>>>(p, a, (int)e.n, per);
+        } else {
+            if (sm > 48 * 1024) cudaFuncSetAttribute(k_lj_atm<false, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            k_lj_atm<false, 2><<<grid, 256, sm, st>>>(p, a, (int)e.n, per);
+        }
+    }
 }
 
 void launch_pair_tile(PairParams &p, int ncell, bool measure, bool emit, cudaStream_t st) {
