@@ -141,7 +141,6 @@ struct PairParams {
     float eps0, sig0;
     float lj_fscalef;          // ATM2B force factor (1 without ATM2B), force path only
     double lj_fscale;
-    int atm_up;                // Verlet LJ kernel: emit only ATM neighbours with a larger slot
 };
 
 struct AtmParams {
@@ -259,7 +258,6 @@ struct Engine {
     float eps0 = 1.f, sig0 = 1.f;
     double lj_fscale = 1.0;         // ATM2B factor (KOMD_TERM_ATM2B), else 1
     bool fused_drift = false;       // Verlet path, single-site molecules with exact COM: k_step0_fused
-    bool atm_up = false;            // this force pass feeds k_atm_s only: ATM lists hold neighbours above
     // device-accessible host buffers of komd_gpu_step_host (site order, 3 doubles
     // per site), read or written directly by the step's first and last kernels;
     // nullptr outside such a step

@@ -1256,7 +1256,6 @@ PairParams pair_params(Engine &e) {
     p.use_lj = lj ? 1 : 0;
     p.lj_fscale = e.lj_fscale;
     p.lj_fscalef = (float)e.lj_fscale;
-    p.atm_up = e.atm_up ? 1 : 0;
     p.virial_compat = e.cfg.virial_mode == KOMD_VIRIAL_COMPAT;
     p.offtab = e.offtab;
     p.rebuild = e.rebuild;

@@ -470,10 +470,8 @@ __device__ __forceinline__ int lj_site(const PairParams &p, int i, int lane, uns
                 }
             }
             if (EMIT) {
-                // with atm_up (or into shared memory) the once-per-triplet sweep reads
-                // the list: neighbours above i only
-                const bool emit =
-                    valid && r2 <= rc3sq && ((!TO_SMEM && !p.atm_up) || (int)(e[u] & 0x3ffffffu) > i);
+                // staged for the once-per-triplet sweep: neighbours above i only
+                const bool emit = valid && r2 <= rc3sq && (!TO_SMEM || (int)(e[u] & 0x3ffffffu) > i);
                 const unsigned m = __ballot_sync(0xffffffffu, emit);
                 if (emit) {
                     const int pos = c_atm + __popc(m & lt);
@@ -624,9 +622,7 @@ int launch_lj_vlist(Engine &e, PairParams &p, bool measure, bool emit, cudaStrea
 }
 
 void launch_lj_atm(Engine &e, cudaStream_t st) {
-    e.atm_up = true;
     PairParams p = pair_params(e);
-    e.atm_up = false;
     const AtmParams a = atm_params(e);
     const int per = vlist_per(e);
     const int grid = (vlist_grid(e) + per - 1) / per;
