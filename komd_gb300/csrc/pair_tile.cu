@@ -259,128 +259,77 @@ __global__ void __launch_bounds__(kTileThreads) k_pair_tile(PairParams p) {
 }
 
 // ---------------------------------------------------------------------------
-// Verlet list build (rebuild steps only): the same staged neighbourhood, every
-// pair inside cutoff + skin appended to the home site's row in candidate
-// order (deterministic); bit 31 marks a same-molecule pair (no LJ).
+// Verlet list build (rebuild steps only): one warp per home cell, one lane per
+// home site (groups of 32 when a cell holds more).  The warp walks the 27
+// neighbour cells in order and stages each one's sites (position with the
+// cell's periodic offset, list word, molecule key) in warp-private shared
+// memory; every lane tests them all against its site and appends the hits to
+// its row.  Rows hold the pairs inside cutoff + skin by neighbour cell, then
+// by slot (deterministic); bit 31 marks a same-molecule pair (no LJ).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kTileThreads) k_vlist_build(PairParams p) {
-    __shared__ float4 s_pos[kStage];
-    __shared__ int2 s_aux[kStage];      // (list entry without the same-molecule bit, molecule key)
-    __shared__ float4 s_hpos[kHome];
-    __shared__ int s_hkey[kHome];
-    __shared__ int s_cnt[kHome];
-    __shared__ int s_nbs[27], s_nbn[27], s_nbpre[28];
-    __shared__ float s_nbo[27][3];
+constexpr int kVbWarps = 4;   // home cells per block
+
+__global__ void __launch_bounds__(32 * kVbWarps) k_vlist_build(PairParams p) {
+    __shared__ float4 s_q[kVbWarps][32];
+    __shared__ uint2 s_w[kVbWarps][32];   // (list word without the same-molecule bit, molecule key)
     if (!*p.rebuild) return;
-    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const int cell = blockIdx.x;
-    if (cell == 0 && tid == 0 && p.rebuild_count) atomicAdd(p.rebuild_count, 1);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int cell = blockIdx.x * kVbWarps + w;
+    if (cell == 0 && lane == 0 && p.rebuild_count) atomicAdd(p.rebuild_count, 1);
+    if (cell >= p.g.ncell) return;
     int cx, cy, cz;
     cell_coords(p.g, cell, cx, cy, cz);
-    if (tid < 27) {
-        int kx, ky, kz;
-        bool cr;
-        const int c = nb_cell(p.g, cx, cy, cz, tid, kx, ky, kz, cr);
-        const int s0 = p.cell_start[c];
-        s_nbs[tid] = s0;
-        s_nbn[tid] = p.cell_start[c + 1] - s0;
-        s_nbo[tid][0] = p.offtab[cx * 3 + tid % 3];
-        s_nbo[tid][1] = p.offtab[p.g.nd[0] * 3 + cy * 3 + (tid / 3) % 3];
-        s_nbo[tid][2] = p.offtab[(p.g.nd[0] + p.g.nd[1]) * 3 + cz * 3 + tid / 9];
-    }
-    __syncthreads();
-    if (tid == 0) {
-        int acc = 0;
-        for (int k = 0; k < 27; k++) { s_nbpre[k] = acc; acc += s_nbn[k]; }
-        s_nbpre[27] = acc;
-    }
-    __syncthreads();
-    const int Nn = s_nbpre[27];
-    const int hs = s_nbs[13], hn = s_nbn[13];
+    const int hs = p.cell_start[cell], hn = p.cell_start[cell + 1] - hs;
+    const float4 *nbo = p.nboff + (size_t)cell * 27;
     const float rl2 = (float)p.rl2;
-    unsigned lt;
-    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
-    for (int hb = 0; hb < hn; hb += kHome) {
-        const int hc = min(kHome, hn - hb);
-        for (int t = tid; t < hc; t += kTileThreads) {
-            s_hpos[t] = p.pos4[hs + hb + t];
-            s_hkey[t] = p.skey[hs + hb + t];
-            s_cnt[t] = 0;
-        }
-        const int self_base = s_nbpre[13] + hb;
-        for (int sb = 0; sb < Nn; sb += kStage) {
-            const int ns = min(kStage, Nn - sb);
-            __syncthreads();
-            for (int t = tid; t < ns; t += kTileThreads) {
-                const int gi = sb + t;
-                int lo = 0, hi = 27;
-                while (hi - lo > 1) {
-                    const int mid = (lo + hi) >> 1;
-                    if (s_nbpre[mid] <= gi) lo = mid; else hi = mid;
-                }
-                const int nb = lo;
-                const int j = s_nbs[nb] + (gi - s_nbpre[nb]);
-                float4 q = p.pos4[j];
-                q.x += s_nbo[nb][0];
-                q.y += s_nbo[nb][1];
-                q.z += s_nbo[nb][2];
-                s_pos[t] = q;
-                s_aux[t] = make_int2((int)(((unsigned)nb << 26) | (unsigned)j), p.skey[j]);
-            }
-            __syncthreads();
-            // two home sites per warp pass: one staged position load serves both
-            // tests; the list word is read only for hits
-            for (int ia = w; ia < hc; ia += 2 * kTileWarps) {
-                const int ib = ia + kTileWarps;
-                const bool two = ib < hc;
-                const float4 pa = s_hpos[ia];
-                const float4 pb = two ? s_hpos[ib] : pa;
-                const int ka = s_hkey[ia], kb = two ? s_hkey[ib] : 0;
-                const int selfa = self_base + ia - sb, selfb = self_base + ib - sb;
-                const size_t rowa = (size_t)(hs + hb + ia) * p.vl_cap, rowb = (size_t)(hs + hb + ib) * p.vl_cap;
-                int ca = s_cnt[ia], cb = two ? s_cnt[ib] : 0;
-                for (int j0 = 0; j0 < ns; j0 += 32) {
-                    const int j = j0 + lane;
-                    bool ha = false, hbb = false;
-                    if (j < ns) {
-                        const float4 pj = s_pos[j];
-                        const float ax = pa.x - pj.x, ay = pa.y - pj.y, az = pa.z - pj.z;
-                        ha = j != selfa && ax * ax + ay * ay + az * az <= rl2;
-                        if (two) {
-                            const float bx = pb.x - pj.x, by = pb.y - pj.y, bz = pb.z - pj.z;
-                            hbb = j != selfb && bx * bx + by * by + bz * bz <= rl2;
-                        }
-                    }
-                    const unsigned ma = __ballot_sync(0xffffffffu, ha);
-                    const unsigned mb = __ballot_sync(0xffffffffu, hbb);
-                    if (ha || hbb) {
-                        const int2 a = s_aux[j];
-                        if (ha) {
-                            const int pos = ca + __popc(ma & lt);
-                            if (pos < p.vl_cap) p.vl[rowa + pos] = (a.y == ka ? 0x80000000u : 0u) | (unsigned)a.x;
-                        }
-                        if (hbb) {
-                            const int pos = cb + __popc(mb & lt);
-                            if (pos < p.vl_cap) p.vl[rowb + pos] = (a.y == kb ? 0x80000000u : 0u) | (unsigned)a.x;
-                        }
-                    }
-                    ca += __popc(ma);
-                    cb += __popc(mb);
-                }
-                if (lane == 0) {
-                    s_cnt[ia] = ca;
-                    if (two) s_cnt[ib] = cb;
+    for (int hb = 0; hb < hn; hb += 32) {
+        const int h = hb + lane;
+        const bool active = h < hn;
+        const int hslot = hs + min(h, hn - 1);
+        const float4 hp = p.pos4[hslot];
+        const int hkey = p.skey[hslot];
+        const unsigned self = (13u << 26) | (unsigned)hslot;   // the site itself, in the home cell
+        unsigned *row = p.vl + (size_t)hslot * p.vl_cap;
+        int c = 0;
+        for (int nb = 0; nb < 27; nb++) {
+            int kx, ky, kz;
+            bool cr;
+            const int q = nb_cell(p.g, cx, cy, cz, nb, kx, ky, kz, cr);
+            const int qs = p.cell_start[q], qn = p.cell_start[q + 1] - qs;
+            const float4 o = nbo[nb];
+            for (int jb = 0; jb < qn; jb += 32) {
+                const int jc = min(32, qn - jb);
+                __syncwarp();
+                if (lane < jc) {
+                    const int j = qs + jb + lane;
+                    float4 pj = p.pos4[j];
+                    pj.x += o.x;
+                    pj.y += o.y;
+                    pj.z += o.z;
+                    s_q[w][lane] = pj;
+                    s_w[w][lane] = make_uint2(((unsigned)nb << 26) | (unsigned)j, (unsigned)p.skey[j]);
                 }
                 __syncwarp();
+                if (active) {
+#pragma unroll 4
+                    for (int t = 0; t < jc; t++) {
+                        const float4 pj = s_q[w][t];
+                        const float ax = hp.x - pj.x, ay = hp.y - pj.y, az = hp.z - pj.z;
+                        if (ax * ax + ay * ay + az * az <= rl2) {
+                            const uint2 ww = s_w[w][t];
+                            if (ww.x != self) {
+                                if (c < p.vl_cap) row[c] = ((int)ww.y == hkey ? 0x80000000u : 0u) | ww.x;
+                                c++;
+                            }
+                        }
+                    }
+                }
             }
         }
-        __syncthreads();
-        for (int t = tid; t < hc; t += kTileThreads) {
-            const int c = s_cnt[t];
-            p.vl_count[hs + hb + t] = min(c, p.vl_cap);
+        if (active) {
+            p.vl_count[hslot] = min(c, p.vl_cap);
             if (c > p.vl_cap) atomicOr(&p.err[E_VL_OVERFLOW], 1);
         }
-        __syncthreads();
     }
 }
 
@@ -584,7 +533,7 @@ int vlist_per(const Engine &e) {
 
 void launch_vlist_build(Engine &e, cudaStream_t st) {
     PairParams p = pair_params(e);
-    k_vlist_build<<<e.g.ncell, kTileThreads, 0, st>>>(p);
+    k_vlist_build<<<(e.g.ncell + kVbWarps - 1) / kVbWarps, 32 * kVbWarps, 0, st>>>(p);
 }
 
 template <bool UNIFORM>
