@@ -464,7 +464,7 @@ int komd_gpu_create(const komd_config *cfg, int device, komd_gpu **out) {
                 nb[(size_t)c * 27 + k] = make_float4((float)o[0], (float)o[1], (float)o[2], img ? 1.f : 0.f);
             }
         }
-        if (dalloc(e.nboff, nb.size()) || dalloc(e.rebuild, 1) || dalloc(e.rebuild_count, 1) ||
+        if (dalloc(e.nboff, nb.size()) || dalloc(e.rebuild, 1) || dalloc(e.rebuild_count, 1) || dalloc(e.vb_next, 1) ||
             cudaMemset(e.rebuild_count, 0, sizeof(int)) != cudaSuccess ||
             cudaMemcpy(e.nboff, nb.data(), sizeof(float4) * nb.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
             cudaMemset(e.rebuild, 0, sizeof(int)) != cudaSuccess) {
@@ -491,7 +491,7 @@ int komd_gpu_destroy(komd_gpu *h) {
     dfree(e.nl); dfree(e.nl_count); dfree(e.bonds); dfree(e.angles); dfree(e.partials); dfree(e.err);
     dfree(e.tab_x); dfree(e.tab_y); dfree(e.atm_acc);
     dfree(e.rdf); dfree(e.lj_hist); dfree(e.counts); dfree(h->f_scratch); dfree(h->prof); dfree(h->acc); dfree(h->thermo_acc); dfree(e.offtab);
-    dfree(e.nboff); dfree(e.rebuild); dfree(e.bias); dfree(e.ref4); dfree(e.slot_cell); dfree(e.vl); dfree(e.vl_count);
+    dfree(e.nboff); dfree(e.vb_next); dfree(e.rebuild); dfree(e.bias); dfree(e.ref4); dfree(e.slot_cell); dfree(e.vl); dfree(e.vl_count);
     dfree(e.rebuild_count); dfree(e.hdtm); dfree(e.exact_com);
     {
         Surrogate &u = h->sur;

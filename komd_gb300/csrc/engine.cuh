@@ -136,6 +136,7 @@ struct PairParams {
     int vl_cap;
     double rl2;                // (cutoff + skin)^2
     const int *slot_cell;
+    int *vb_next;              // Verlet list build: next home cell to take (reset by the scan)
     const float4 *nboff;
     int *rebuild_count;
     float eps0, sig0;
@@ -245,6 +246,7 @@ struct Engine {
     double *bias = nullptr;
     float4 *ref4 = nullptr;      // per site: that FP32 position at the last rebuild
     int *slot_cell = nullptr;    // per slot: its cell at the last rebuild
+    int *vb_next = nullptr;      // Verlet list build: work counter over home cells
     float4 *nboff = nullptr;     // per cell x 27: home-relative neighbour-cell offset, w = 1 for an image
     unsigned *vl = nullptr;      // vl_cap entries per slot: same-molecule bit 31 | nb << 26 | slot
     int *vl_count = nullptr;

@@ -91,12 +91,14 @@ __global__ void k_com_wrap_bin(Grid g, int n_mol, const int *__restrict__ mol_of
 
 // exclusive scan of two count arrays of length nc (one block of 1024 threads,
 // each owning a contiguous chunk)
+// (work: the Verlet list build's cell counter, reset here for this rebuild)
 __global__ void __launch_bounds__(1024) k_scan2(int nc, const int *__restrict__ a, int *__restrict__ sa,
                                                 const int *__restrict__ b, int *__restrict__ sb,
-                                                const int *__restrict__ rebuild) {
+                                                const int *__restrict__ rebuild, int *__restrict__ work) {
     __shared__ int wa[32], wb[32];
     if (rebuild && !*rebuild) return;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    if (work && t == 0) *work = 0;
     const int per = (nc + 1023) / 1024;
     const int lo = min(t * per, nc), hi = min(lo + per, nc);
     int ta = 0, tb = 0;
@@ -1210,7 +1212,7 @@ void launch_container(Engine &e, cudaStream_t st) {
                                                          e.mol_rank, e.cell_count, e.cell_mcount,
                                                          e.verlet ? e.bias : nullptr, rb, e.exact_com,
                                                          e.fused_drift ? 1 : 0);
-    k_scan2<<<1, 1024, 0, st>>>(g.ncell, e.cell_count, e.cell_start, e.cell_mcount, e.cell_mstart, rb);
+    k_scan2<<<1, 1024, 0, st>>>(g.ncell, e.cell_count, e.cell_start, e.cell_mcount, e.cell_mstart, rb, e.vb_next);
     k_scatter_mol<<<nblk(e.n_mol, 256), 256, 0, st>>>((int)e.n_mol, e.mol_cell, e.mol_rank, e.cell_mstart,
                                                         e.cell_mols, rb);
     k_cell_sort<<<nblk(g.ncell, kWarpsPerBlock), kBlock, 0, st>>>(
@@ -1265,6 +1267,7 @@ PairParams pair_params(Engine &e) {
     const double rl = std::max(lj ? e.cfg.cutoff : 0.0, atm ? e.cfg.cutoff_3b : 0.0) + e.cfg.skin;
     p.rl2 = rl * rl;
     p.slot_cell = e.slot_cell;
+    p.vb_next = e.vb_next;
     p.nboff = e.nboff;
     p.rebuild_count = e.rebuild_count;
     p.eps0 = e.eps0;

@@ -274,9 +274,14 @@ __global__ void __launch_bounds__(32 * kVbWarps) k_vlist_build(PairParams p) {
     __shared__ uint2 s_w[kVbWarps][32];   // (list word without the same-molecule bit, molecule key)
     if (!*p.rebuild) return;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int cell = blockIdx.x * kVbWarps + w;
-    if (cell == 0 && lane == 0 && p.rebuild_count) atomicAdd(p.rebuild_count, 1);
-    if (cell >= p.g.ncell) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && p.rebuild_count) atomicAdd(p.rebuild_count, 1);
+    // warps take home cells from a counter (reset by the scan of this rebuild):
+    // cells differ in cost, and a resident grid keeps every SM busy to the end
+    for (;;) {
+    int cell = 0;
+    if (lane == 0) cell = atomicAdd(p.vb_next, 1);
+    cell = __shfl_sync(0xffffffffu, cell, 0);
+    if (cell < 0 || cell >= p.g.ncell) break;
     int cx, cy, cz;
     cell_coords(p.g, cell, cx, cy, cz);
     const int hs = p.cell_start[cell], hn = p.cell_start[cell + 1] - hs;
@@ -330,6 +335,7 @@ __global__ void __launch_bounds__(32 * kVbWarps) k_vlist_build(PairParams p) {
             p.vl_count[hslot] = min(c, p.vl_cap);
             if (c > p.vl_cap) atomicOr(&p.err[E_VL_OVERFLOW], 1);
         }
+    }
     }
 }
 
@@ -533,7 +539,9 @@ int vlist_per(const Engine &e) {
 
 void launch_vlist_build(Engine &e, cudaStream_t st) {
     PairParams p = pair_params(e);
-    k_vlist_build<<<(e.g.ncell + kVbWarps - 1) / kVbWarps, 32 * kVbWarps, 0, st>>>(p);
+    // a resident grid (12 blocks of 4 warps per SM at this kernel's register count)
+    const int blocks = std::min((e.g.ncell + kVbWarps - 1) / kVbWarps, 152 * 12);
+    k_vlist_build<<<blocks, 32 * kVbWarps, 0, st>>>(p);
 }
 
 template <bool UNIFORM>
