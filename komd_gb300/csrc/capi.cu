@@ -418,6 +418,8 @@ int komd_gpu_create(const komd_config *cfg, int device, komd_gpu **out) {
         return fail(KOMD_ERR_NOMEM, "device allocation failed");
     }
     cudaMemset(e.err, 0, sizeof(int) * E_NFLAGS);
+    cudaMemset(e.cell_count, 0, sizeof(int) * g.ncell);    // the binning's counters start at zero
+    cudaMemset(e.cell_mcount, 0, sizeof(int) * g.ncell);
     if (e.cfg.rdf_dr > 0 && e.cfg.rdf_max > 0) {
         e.rdf_bins = (int64_t)(uint64_t)(e.cfg.rdf_max / e.cfg.rdf_dr);   // RDFSensor.cpp:18
         if (e.rdf_bins > 0 && dalloc(e.rdf, e.rdf_bins)) { komd_gpu_destroy(h); return fail(KOMD_ERR_NOMEM, "rdf"); }

@@ -25,9 +25,9 @@ __global__ void k_com_wrap_bin(Grid g, int n_mol, const int *__restrict__ mol_of
                                int *__restrict__ mol_rank, int *__restrict__ cell_count, int *__restrict__ cell_mcount,
                                double *__restrict__ bias, const int *__restrict__ rebuild,
                                const unsigned char *__restrict__ exact_com, int wrapped) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n_mol) return;
     if (wrapped && rebuild && !*rebuild) return;   // k_step0_fused wrapped this step; no rebuild
+    const bool bin = !(rebuild && !*rebuild);      // no rebuild in this step: cells stay as built
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n_mol; k += gridDim.x * blockDim.x) {
     const int s0 = mol_off[k], s1 = mol_off[k + 1];
     // com += r * m ; M += m ; com /= M   (updateCOM, no FMA).  For a single
     // site of power-of-two mass the scaling is exact and the result is r
@@ -73,7 +73,7 @@ __global__ void k_com_wrap_bin(Grid g, int n_mol, const int *__restrict__ mol_of
         }
     }
     for (int d = 0; d < 3; d++) com[3 * k + d] = c[d];
-    if (rebuild && !*rebuild) return;   // no rebuild in this step: cells stay as built
+    if (!bin) continue;
     // writeIndices: (int64)((com - low) / cs) clamped to [0, nd-1]
     int b[3];
     for (int d = 0; d < 3; d++) {
@@ -87,13 +87,15 @@ __global__ void k_com_wrap_bin(Grid g, int n_mol, const int *__restrict__ mol_of
     mol_cell[k] = cell;
     mol_rank[k] = atomicAdd(&cell_mcount[cell], 1);
     atomicAdd(&cell_count[cell], s1 - s0);
+    }
 }
 
 // exclusive scan of two count arrays of length nc (one block of 1024 threads,
-// each owning a contiguous chunk)
-// (work: the Verlet list build's cell counter, reset here for this rebuild)
-__global__ void __launch_bounds__(1024) k_scan2(int nc, const int *__restrict__ a, int *__restrict__ sa,
-                                                const int *__restrict__ b, int *__restrict__ sb,
+// each owning a contiguous chunk); the counts are zeroed once read, ready for
+// the next binning (work: the Verlet list build's cell counter, reset here for
+// this rebuild)
+__global__ void __launch_bounds__(1024) k_scan2(int nc, int *__restrict__ a, int *__restrict__ sa,
+                                                int *__restrict__ b, int *__restrict__ sb,
                                                 const int *__restrict__ rebuild, int *__restrict__ work) {
     __shared__ int wa[32], wb[32];
     if (rebuild && !*rebuild) return;
@@ -125,6 +127,8 @@ __global__ void __launch_bounds__(1024) k_scan2(int nc, const int *__restrict__ 
     for (int i = lo; i < hi; i++) {
         sa[i] = pa; pa += a[i];
         sb[i] = pb; pb += b[i];
+        a[i] = 0;
+        b[i] = 0;
     }
     if (t == 1023) { sa[nc] = wa[31]; sb[nc] = wb[31]; }
 }
@@ -132,9 +136,9 @@ __global__ void __launch_bounds__(1024) k_scan2(int nc, const int *__restrict__ 
 __global__ void k_scatter_mol(int n_mol, const int *__restrict__ mol_cell, const int *__restrict__ mol_rank,
                               const int *__restrict__ cell_mstart, int *__restrict__ cell_mols,
                               const int *__restrict__ rebuild) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n_mol || (rebuild && !*rebuild)) return;
-    cell_mols[cell_mstart[mol_cell[k]] + mol_rank[k]] = k;
+    if (rebuild && !*rebuild) return;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n_mol; k += gridDim.x * blockDim.x)
+        cell_mols[cell_mstart[mol_cell[k]] + mol_rank[k]] = k;
 }
 
 // One warp per domain cell: order the cell's molecules by index (ascending
@@ -153,8 +157,9 @@ __global__ void __launch_bounds__(kBlock) k_cell_sort(Grid g, const int *__restr
                                                       float4 *__restrict__ ref4, int *__restrict__ slot_cell,
                                                       const int *__restrict__ rebuild) {
     const int lane = threadIdx.x & 31;
-    const int cell = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
-    if (cell >= g.ncell || (rebuild && !*rebuild)) return;
+    if (rebuild && !*rebuild) return;
+    for (int cell = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); cell < g.ncell;
+         cell += gridDim.x * kWarpsPerBlock) {
     int cx, cy, cz;
     cell_coords(g, cell, cx, cy, cz);
     const double cen[3] = {cell_centre(g, 0, cx), cell_centre(g, 1, cy), cell_centre(g, 2, cz)};
@@ -192,6 +197,7 @@ __global__ void __launch_bounds__(kBlock) k_cell_sort(Grid g, const int *__restr
                 }
             }
         }
+    }
     }
 }
 
@@ -1206,16 +1212,18 @@ static inline int nblk(long long n, int b) { return (int)((n + b - 1) / b); }
 void launch_container(Engine &e, cudaStream_t st) {
     const Grid &g = e.g;
     const int *rb = e.verlet ? e.rebuild : nullptr;   // nullptr: rebuild unconditionally
-    cudaMemsetAsync(e.cell_count, 0, sizeof(int) * g.ncell, st);
-    cudaMemsetAsync(e.cell_mcount, 0, sizeof(int) * g.ncell, st);
-    k_com_wrap_bin<<<nblk(e.n_mol, 256), 256, 0, st>>>(g, (int)e.n_mol, e.mol_off, e.r, e.m, e.com, e.mol_cell,
+    // the per-cell counts are zero here: zeroed at allocation, and by the scan
+    // of every binning after reading them
+    // grid-stride kernels on a resident grid: steps without a rebuild launch few blocks
+    const int res = 152 * 8;
+    k_com_wrap_bin<<<std::min(nblk(e.n_mol, 256), res), 256, 0, st>>>(g, (int)e.n_mol, e.mol_off, e.r, e.m, e.com, e.mol_cell,
                                                          e.mol_rank, e.cell_count, e.cell_mcount,
                                                          e.verlet ? e.bias : nullptr, rb, e.exact_com,
                                                          e.fused_drift ? 1 : 0);
     k_scan2<<<1, 1024, 0, st>>>(g.ncell, e.cell_count, e.cell_start, e.cell_mcount, e.cell_mstart, rb, e.vb_next);
-    k_scatter_mol<<<nblk(e.n_mol, 256), 256, 0, st>>>((int)e.n_mol, e.mol_cell, e.mol_rank, e.cell_mstart,
+    k_scatter_mol<<<std::min(nblk(e.n_mol, 256), res), 256, 0, st>>>((int)e.n_mol, e.mol_cell, e.mol_rank, e.cell_mstart,
                                                         e.cell_mols, rb);
-    k_cell_sort<<<nblk(g.ncell, kWarpsPerBlock), kBlock, 0, st>>>(
+    k_cell_sort<<<std::min(nblk(g.ncell, kWarpsPerBlock), res), kBlock, 0, st>>>(
         g, e.mol_off, e.cell_mstart, e.cell_start, e.cell_mols, e.r, e.eps, e.sig, e.key, e.slot_site, e.site_slot,
         e.pos4, e.skey, e.seps, e.posd, e.seps_d, e.sig_d, e.verlet ? e.bias : nullptr, e.verlet ? e.ref4 : nullptr,
         e.verlet ? e.slot_cell : nullptr, rb);
