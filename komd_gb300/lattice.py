@@ -149,6 +149,56 @@ def triatomic_sc(n_mol_side: int, rho_site: float = 0.8, t_star: float = 1.0, se
                   low=np.zeros(3), high=np.full(3, L), bonds=bonds, angles=angles)
 
 
+def triatomic_count(n_mol: int, rho_site: float = 0.8, t_star: float = 1.0, seed: int = 3, r0: float = 1.0,
+                    theta0_deg: float = 109.47, aligned: bool = False) -> System:
+    """Exactly n_mol flexible 3-site molecules at site density rho_site, centred
+    on a seeded random n_mol of the points of the smallest simple-cubic lattice
+    with at least n_mol points.  Orientations: random per molecule, or
+    (aligned) one orientation for all, the seeded candidate (of 4000) that keeps
+    sites of different molecules farthest apart -- at rho_site 0.8 random
+    orientations put sites of neighbouring molecules within a fraction of sigma."""
+    rng = np.random.default_rng(seed)
+    side = int(np.ceil(n_mol ** (1.0 / 3.0) - 1e-9))
+    while side ** 3 < n_mol:
+        side += 1
+    L = (3 * n_mol / rho_site) ** (1.0 / 3.0)
+    a = L / side
+    g = np.stack(np.meshgrid(*(np.arange(side),) * 3, indexing="ij"), -1).reshape(-1, 3)
+    g = g[np.lexsort((g[:, 0], g[:, 1], g[:, 2]))]
+    keep = np.sort(rng.choice(side ** 3, n_mol, replace=False))
+    centres = (g[keep] + 0.5) * a
+    th = np.deg2rad(theta0_deg)
+    body = np.array([[r0 * np.sin(th / 2), r0 * np.cos(th / 2), 0.0], [0, 0, 0],
+                     [-r0 * np.sin(th / 2), r0 * np.cos(th / 2), 0.0]])
+    body -= body.mean(0)
+    if aligned:
+        shifts = np.array([[i, j, k] for i in range(-2, 3) for j in range(-2, 3) for k in range(-2, 3)
+                           if (i, j, k) != (0, 0, 0)], float) * a
+        best, rot = -1.0, None
+        for _ in range(4000):
+            R = _rotation(rng)
+            b = body @ R.T
+            d = (shifts[:, None, None, :] + b[None, None, :, :] - b[None, :, None, :]).reshape(-1, 3)
+            dmin = float(np.sqrt((d * d).sum(1)).min())
+            if dmin > best:
+                best, rot = dmin, R
+        r = (centres[:, None, :] + (body @ rot.T)[None, :, :]).reshape(-1, 3)
+    else:
+        r = np.empty((3 * n_mol, 3))
+        for k in range(n_mol):
+            r[3 * k:3 * k + 3] = centres[k] + body @ _rotation(rng).T
+    n = 3 * n_mol
+    m = np.ones(n)
+    v = maxwell_boltzmann(n, t_star, m, rng)
+    v -= (v * m[:, None]).sum(0) / m.sum()   # no net momentum
+    base = 3 * np.arange(n_mol)
+    bonds = np.concatenate([np.stack([base, base + 1], 1), np.stack([base + 1, base + 2], 1)]).astype(np.int64)
+    angles = np.stack([base, base + 1, base + 2], 1).astype(np.int64)
+    return System(r=r, v=v, m=m, eps=np.ones(n), sig=np.ones(n),
+                  mol_id=np.repeat(np.arange(1, n_mol + 1, dtype=np.uint64), 3), low=np.zeros(3),
+                  high=np.full(3, L), bonds=bonds, angles=angles)
+
+
 def nu_star_to_energy_3b(nu_star: float) -> float:
     """Reduced ATM coefficient -> the input file's energy_3b (J*nm^9), the
     inverse of ATM::ATM's conversion (potentials/ATM.cpp:11-14)."""
