@@ -476,3 +476,76 @@ def test_multisite_300k_full_size(oracle_lib):
     b = np.linalg.norm(r1[s.bonds[:, 0]] - r1[s.bonds[:, 1]], axis=1)
     assert 0.8 < b.min() and b.max() < 1.2
     g.close()
+
+
+def test_plain_lj_4000_fp64_1000_steps(oracle_lib):
+    """The plain LJ workload at its full size and length: 4,000 argon atoms
+    (FCC 10^3, rho* 0.8442, T* 0.722), cutoff 2.5, 1000 NVE steps of dt 0.005,
+    all FP64.  After the 1000 steps the engine's positions follow the oracle's
+    (the reference's pair sweep) to 1e-5 (the FP64 forces agree to ~1e-12 and
+    chaos amplifies that by ~1e4 over this run), and the energy, the virial
+    pressure and the RDF (200 bins to 2.5) agree."""
+    from komd_gb300 import gpu, lattice
+    s = lattice.argon_fcc(10, rho=0.8442, t_star=0.722, seed=51)
+    L = float((s.high - s.low)[0])
+    cell = L / np.floor(L / 2.5)
+    cfg = gpu.make_config(s.low, s.high, cell, cutoff=2.5, dt=0.005, terms=gpu.TERM_LJ, precision=gpu.FP64,
+                          virial_mode=gpu.VIRIAL_CORRECT, rdf_max=2.5, rdf_dr=0.0125)
+    g = gpu.GpuSystem(s, cfg)
+    g.update_container()
+    g.forces()
+    g.step(1000)
+    r, v, f = g.download()
+    sim = oracle_lib.OracleSim(s, cell, 2.5, dt=0.005, limit=1e30, virial_mode=oracle_lib.VIRIAL_CORRECT)
+    sim.update_container()
+    sim.forces()
+    for _ in range(1000):
+        sim.step()
+    assert np.abs(r - sim.r).max() < 1e-5
+    assert np.abs(v - sim.v).max() < 1e-5
+    obs = g.measure(gpu.MEASURE_ENERGY | gpu.MEASURE_PRESSURE | gpu.MEASURE_RDF)
+    sim.update_container()
+    sim.forces()
+    assert obs["u_lj"] == pytest.approx(sim.lj_out.u_total, rel=1e-8)
+    pres = sim.momentum(s.n) + np.array(sim.lj_out.virial[:])
+    np.testing.assert_allclose(obs["pressure"], pres, rtol=1e-6, atol=1e-6 * np.abs(pres).max())
+    rdf = sim.rdf(2.5, 0.0125)
+    assert obs["rdf"].size == rdf.size == 200
+    assert np.abs(obs["rdf"] - rdf).max() <= 4    # a pair or two may sit within 1e-7 of a bin edge
+    assert obs["rdf"].sum() == pytest.approx(rdf.sum(), abs=4)
+    g.close()
+
+
+def test_lj_atm_32k_fp32_against_fp64_oracle(oracle_lib):
+    """The LJ + ATM workload at its full size: 32,000 argon atoms (FCC 20^3),
+    LJ cutoff 2.5, ATM nu* 0.073 with cutoff 2.0 on all sides, FULL triplets
+    and F = -grad V, FP32 forces with FP64 integration.  At the start and
+    after 100 steps the forces, LJ and ATM energies and the virial match the
+    FP64 oracle evaluated at the engine's positions."""
+    from komd_gb300 import gpu, lattice
+    s = lattice.argon_fcc(20, rho=0.8442, t_star=0.722, seed=52, jitter=0.05)   # off the symmetric lattice
+    L = float((s.high - s.low)[0])
+    cell = L / np.floor(L / 2.5)
+    cfg = gpu.make_config(s.low, s.high, cell, cutoff=2.5, cutoff_3b=2.0, nu=0.073, dt=0.005,
+                          terms=gpu.TERM_LJ | gpu.TERM_ATM, atm_sign=gpu.ATM_SIGN_PHYSICAL,
+                          atm_enum=gpu.ATM_ENUM_FULL, virial_mode=gpu.VIRIAL_CORRECT)
+    g = gpu.GpuSystem(s, cfg)
+    g.update_container()
+    g.forces()
+    for steps in (0, 100):
+        if steps:
+            g.step(steps)
+        r, v, f = g.download()
+        at = lattice.System(r=r, v=v, m=s.m, eps=s.eps, sig=s.sig, mol_id=s.mol_id, low=s.low, high=s.high)
+        sim = oracle_lib.OracleSim(at, cell, 2.5, nu=0.073, cutoff_atm=2.0, atm=True, atm_mode="full",
+                                   atm_sign=oracle_lib.ATM_SIGN_PHYSICAL, virial_mode=oracle_lib.VIRIAL_CORRECT)
+        sim.update_container()
+        sim.forces()
+        assert rel_rmse(f, sim.f) < FP32_FORCE_RMSE
+        obs = g.measure(gpu.MEASURE_ENERGY | gpu.MEASURE_PRESSURE)
+        assert obs["u_lj"] == pytest.approx(sim.lj_out.u_total, rel=1e-5)
+        assert obs["u_atm"] == pytest.approx(sim.atm_out.energy, rel=1e-5)
+        assert obs["triplets"] == sim.atm_out.triplets
+        vir = np.array(sim.lj_out.virial[:]) + np.array(sim.atm_out.virial[:])
+        np.testing.assert_allclose(obs["virial"], vir, rtol=0, atol=2e-5 * np.abs(vir).max())
+    g.close()
