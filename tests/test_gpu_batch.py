@@ -90,3 +90,43 @@ def test_step_host_matches_device_path(pinned):
         assert np.array_equal(f, fb)
     a.close()
     b.close()
+
+
+def test_batch_512_replicas_full_size():
+    """The batched-replicas workload at its full size: 512 LJ + ATM boxes,
+    N ~ U[2000, 20000] (FCC filled, trimmed by seed), rho* ~ U[0.70, 0.90],
+    T* ~ U[0.6, 1.5], one graph over 32 branches.  After 10 steps, sampled
+    replicas equal, bit for bit, the same replicas stepped alone, and every
+    replica's RDF (200 bins to 2.5) and virial pressure are finite."""
+    from komd_gb300 import gpu, lattice, surrogate
+    rng = np.random.default_rng(2027)
+    specs = [(int(rng.integers(1 << 30)), int(rng.integers(2000, 20001)), float(rng.uniform(0.70, 0.90)),
+              float(rng.uniform(0.6, 1.5))) for _ in range(512)]
+
+    def make(seed, n, rho, t_star):
+        s = lattice.trimmed_fcc(n, rho, t_star, seed)
+        L = float(s.high[0])
+        cfg = surrogate.physics_config(s, L / np.floor(L / 2.8), skin=0.3)
+        cfg.rdf_max, cfg.rdf_dr = 2.5, 2.5 / 200
+        g = gpu.GpuSystem(s, cfg)
+        g.update_container()
+        g.forces()
+        return g
+
+    reps = [make(*sp) for sp in specs]
+    assert 512 * 2000 <= sum(g.n for g in reps) <= 512 * 20000
+    batch = gpu.Batch(reps, n_streams=32, steps_per_graph=5)
+    batch.step(2)
+    batch.close()
+    for k in (0, 137, 511):
+        alone = make(*specs[k])
+        alone.step(10)
+        ra, va, fa = reps[k].download()
+        rb, vb, fb = alone.download()
+        assert np.array_equal(ra, rb) and np.array_equal(va, vb) and np.array_equal(fa, fb)
+        alone.close()
+    for g in reps:
+        o = g.measure(gpu.MEASURE_PRESSURE | gpu.MEASURE_RDF)
+        assert o["rdf"].size == 200 and np.isfinite(o["rdf"]).all() and o["rdf"].sum() > 0
+        assert np.isfinite(o["pressure"]).all()
+        g.close()
