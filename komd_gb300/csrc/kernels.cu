@@ -2,7 +2,10 @@
 //
 // Per step (komd_gpu_step): integrate0 -> com/wrap/bin -> scan -> scatter ->
 // cell sort+gather -> pair (LJ, FENE, ATM neighbour list) -> [bonded] ->
-// [limit] -> [ATM triplets] -> integrate1.
+// [limit] -> [ATM triplets] -> integrate1.  On the Verlet path with FP32
+// forces the drift is one kernel (k_step0_fused), the container kernels run
+// only on a rebuild, the LJ pass sweeps the triplets itself (k_lj_atm,
+// pair_tile.cu) and integrate1 rides on the ATM flush.
 //
 // Citations are to Snapex2409/KoMD, src/.
 #include <algorithm>
@@ -1014,8 +1017,8 @@ __global__ void k_step1(int n, double *__restrict__ v, const double *__restrict_
     if (bad) atomicOr(&err[E_NONFINITE], 1);
 }
 
-// Verlet path, steps without rebuild: cell-local FP32 coordinates of the
-// continuous positions r - img*L relative to each slot's build cell.
+// Verlet path, steps without rebuild: cell-local FP32 coordinates
+// (float)(r - bias) relative to each slot's build cell.
 __global__ void k_refresh(int n, const int *__restrict__ slot_site, const double *__restrict__ r,
                           const double *__restrict__ bias, float4 *__restrict__ pos4, const int *__restrict__ rebuild) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;

@@ -14,6 +14,11 @@
 //      accumulator and, inside cutoff_3b, appends (r_i - r_j, code) to the
 //      home site's ATM list in queue order (deterministic list order).
 // Full shell: each site's force is summed by its own CTA, no global atomics.
+//
+// The Verlet path (skin > 0) has its own kernels here: the list build
+// (k_vlist_build, rebuild steps only), the LJ pass over each site's list row
+// (k_lj_vlist) and the LJ pass that sweeps each site's ATM triplets from
+// shared memory (k_lj_atm).
 #include "engine.cuh"
 #include "kernels.cuh"
 #include "atm_device.cuh"
