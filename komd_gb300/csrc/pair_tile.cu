@@ -274,73 +274,104 @@ __global__ void __launch_bounds__(kTileThreads) k_pair_tile(PairParams p) {
 // ---------------------------------------------------------------------------
 constexpr int kVbWarps = 4;   // home cells per block
 
+// one lane's home site in the build: position, key, row and hit count
+struct VbHome {
+    float4 p;
+    int key, slot, c;
+    unsigned self;
+    bool active;
+};
+
+__device__ __forceinline__ void vb_home(const PairParams &p, int hs, int hn, int h, VbHome &o) {
+    o.active = h < hn;
+    o.slot = hs + min(h, hn - 1);
+    o.p = p.pos4[o.slot];
+    o.key = p.skey[o.slot];
+    o.self = (13u << 26) | (unsigned)o.slot;   // the site itself, in the home cell
+    o.c = 0;
+}
+
+__device__ __forceinline__ bool vb_hit(const VbHome &o, const float4 &pj, float rl2) {
+    const float ax = o.p.x - pj.x, ay = o.p.y - pj.y, az = o.p.z - pj.z;
+    return ax * ax + ay * ay + az * az <= rl2;
+}
+
+__device__ __forceinline__ void vb_emit(const PairParams &p, VbHome &o, const uint2 &ww) {
+    if (ww.x != o.self) {
+        if (o.c < p.vl_cap) p.vl[(size_t)o.slot * p.vl_cap + o.c] = ((int)ww.y == o.key ? 0x80000000u : 0u) | ww.x;
+        o.c++;
+    }
+}
+
+__device__ __forceinline__ void vb_done(const PairParams &p, const VbHome &o) {
+    if (o.active) {
+        p.vl_count[o.slot] = min(o.c, p.vl_cap);
+        if (o.c > p.vl_cap) atomicOr(&p.err[E_VL_OVERFLOW], 1);
+    }
+}
+
 __global__ void __launch_bounds__(32 * kVbWarps) k_vlist_build(PairParams p) {
     __shared__ float4 s_q[kVbWarps][32];
     __shared__ uint2 s_w[kVbWarps][32];   // (list word without the same-molecule bit, molecule key)
     if (!*p.rebuild) return;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (blockIdx.x == 0 && threadIdx.x == 0 && p.rebuild_count) atomicAdd(p.rebuild_count, 1);
+    const float rl2 = (float)p.rl2;
     // warps take home cells from a counter (reset by the scan of this rebuild):
     // cells differ in cost, and a resident grid keeps every SM busy to the end
     for (;;) {
-    int cell = 0;
-    if (lane == 0) cell = atomicAdd(p.vb_next, 1);
-    cell = __shfl_sync(0xffffffffu, cell, 0);
-    if (cell < 0 || cell >= p.g.ncell) break;
-    int cx, cy, cz;
-    cell_coords(p.g, cell, cx, cy, cz);
-    const int hs = p.cell_start[cell], hn = p.cell_start[cell + 1] - hs;
-    const float4 *nbo = p.nboff + (size_t)cell * 27;
-    const float rl2 = (float)p.rl2;
-    for (int hb = 0; hb < hn; hb += 32) {
-        const int h = hb + lane;
-        const bool active = h < hn;
-        const int hslot = hs + min(h, hn - 1);
-        const float4 hp = p.pos4[hslot];
-        const int hkey = p.skey[hslot];
-        const unsigned self = (13u << 26) | (unsigned)hslot;   // the site itself, in the home cell
-        unsigned *row = p.vl + (size_t)hslot * p.vl_cap;
-        int c = 0;
-        for (int nb = 0; nb < 27; nb++) {
-            int kx, ky, kz;
-            bool cr;
-            const int q = nb_cell(p.g, cx, cy, cz, nb, kx, ky, kz, cr);
-            const int qs = p.cell_start[q], qn = p.cell_start[q + 1] - qs;
-            const float4 o = nbo[nb];
-            for (int jb = 0; jb < qn; jb += 32) {
-                const int jc = min(32, qn - jb);
-                __syncwarp();
-                if (lane < jc) {
-                    const int j = qs + jb + lane;
-                    float4 pj = p.pos4[j];
-                    pj.x += o.x;
-                    pj.y += o.y;
-                    pj.z += o.z;
-                    s_q[w][lane] = pj;
-                    s_w[w][lane] = make_uint2(((unsigned)nb << 26) | (unsigned)j, (unsigned)p.skey[j]);
-                }
-                __syncwarp();
-                if (active) {
-#pragma unroll 4
-                    for (int t = 0; t < jc; t++) {
-                        const float4 pj = s_q[w][t];
-                        const float ax = hp.x - pj.x, ay = hp.y - pj.y, az = hp.z - pj.z;
-                        if (ax * ax + ay * ay + az * az <= rl2) {
-                            const uint2 ww = s_w[w][t];
-                            if (ww.x != self) {
-                                if (c < p.vl_cap) row[c] = ((int)ww.y == hkey ? 0x80000000u : 0u) | ww.x;
-                                c++;
-                            }
+        int cell = 0;
+        if (lane == 0) cell = atomicAdd(p.vb_next, 1);
+        cell = __shfl_sync(0xffffffffu, cell, 0);
+        if (cell < 0 || cell >= p.g.ncell) break;
+        int cx, cy, cz;
+        cell_coords(p.g, cell, cx, cy, cz);
+        const int hs = p.cell_start[cell], hn = p.cell_start[cell + 1] - hs;
+        const float4 *nbo = p.nboff + (size_t)cell * 27;
+        // up to 64 home sites per walk of the neighbourhood: lane l serves homes
+        // hb + l and, in cells of more than 32 sites, hb + 32 + l
+        for (int hb = 0; hb < hn; hb += 64) {
+            const bool two = hn - hb > 32;   // warp-uniform
+            VbHome h0, h1;
+            vb_home(p, hs, hn, hb + lane, h0);
+            if (two) vb_home(p, hs, hn, hb + 32 + lane, h1);
+            for (int nb = 0; nb < 27; nb++) {
+                int kx, ky, kz;
+                bool cr;
+                const int q = nb_cell(p.g, cx, cy, cz, nb, kx, ky, kz, cr);
+                const int qs = p.cell_start[q], qn = p.cell_start[q + 1] - qs;
+                const float4 o = nbo[nb];
+                for (int jb = 0; jb < qn; jb += 32) {
+                    const int jc = min(32, qn - jb);
+                    __syncwarp();
+                    if (lane < jc) {
+                        const int j = qs + jb + lane;
+                        float4 pj = p.pos4[j];
+                        pj.x += o.x;
+                        pj.y += o.y;
+                        pj.z += o.z;
+                        s_q[w][lane] = pj;
+                        s_w[w][lane] = make_uint2(((unsigned)nb << 26) | (unsigned)j, (unsigned)p.skey[j]);
+                    }
+                    __syncwarp();
+                    if (two) {   // h0 is active: hn - hb > 32
+#pragma unroll 2
+                        for (int t = 0; t < jc; t++) {
+                            const float4 pj = s_q[w][t];
+                            const uint2 ww = s_w[w][t];   // one read for both homes
+                            if (vb_hit(h0, pj, rl2)) vb_emit(p, h0, ww);
+                            if (h1.active && vb_hit(h1, pj, rl2)) vb_emit(p, h1, ww);
                         }
+                    } else if (h0.active) {
+#pragma unroll 4
+                        for (int t = 0; t < jc; t++)   // the word is read only for hits
+                            if (vb_hit(h0, s_q[w][t], rl2)) vb_emit(p, h0, s_w[w][t]);
                     }
                 }
             }
+            vb_done(p, h0);
+            if (two) vb_done(p, h1);
         }
-        if (active) {
-            p.vl_count[hslot] = min(c, p.vl_cap);
-            if (c > p.vl_cap) atomicOr(&p.err[E_VL_OVERFLOW], 1);
-        }
-    }
     }
 }
 
