@@ -95,6 +95,13 @@ struct komd_gpu {
     int64_t launches[kNumFamilies] = {0};
     double ms[kNumFamilies] = {0};
     int64_t graph_steps = 0;
+    uint64_t graph_epoch = 0;         // step graphs captured so far
+    int *flags_h = nullptr;           // pinned landing buffer of the error flags
+    // komd_gpu_step_host's one-step graph (the step graph with the caller's
+    // buffers bound), valid for one capture of the step graph and one set of buffers
+    cudaGraphExec_t hgraph = nullptr;
+    uint64_t hgraph_epoch = 0;
+    const void *hkey[3] = {nullptr, nullptr, nullptr};
 };
 
 namespace {
@@ -279,9 +286,11 @@ void enqueue_step(komd_gpu *h) {
 
 int read_flags(komd_gpu *h, int flags[E_NFLAGS], bool clear) {
     Engine &e = h->e;
-    CK(cudaMemcpyAsync(flags, e.err, sizeof(int) * E_NFLAGS, cudaMemcpyDeviceToHost, e.stream));
+    int *land = h->flags_h ? h->flags_h : flags;   // a pinned landing buffer copies without staging
+    CK(cudaMemcpyAsync(land, e.err, sizeof(int) * E_NFLAGS, cudaMemcpyDeviceToHost, e.stream));
     if (clear) CK(cudaMemsetAsync(e.err, 0, sizeof(int) * E_NFLAGS, e.stream));
     CK(cudaStreamSynchronize(e.stream));
+    if (land != flags) std::memcpy(flags, land, sizeof(int) * E_NFLAGS);
     return KOMD_OK;
 }
 
@@ -418,6 +427,10 @@ int komd_gpu_create(const komd_config *cfg, int device, komd_gpu **out) {
         return fail(KOMD_ERR_NOMEM, "device allocation failed");
     }
     cudaMemset(e.err, 0, sizeof(int) * E_NFLAGS);
+    if (cudaHostAlloc(reinterpret_cast<void **>(&h->flags_h), sizeof(int) * E_NFLAGS, cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        h->flags_h = nullptr;   // read_flags then copies into the caller's array
+    }
     cudaMemset(e.cell_count, 0, sizeof(int) * g.ncell);    // the binning's counters start at zero
     cudaMemset(e.cell_mcount, 0, sizeof(int) * g.ncell);
     if (e.cfg.rdf_dr > 0 && e.cfg.rdf_max > 0) {
@@ -485,6 +498,8 @@ int komd_gpu_destroy(komd_gpu *h) {
     cudaSetDevice(e.device);
     if (e.stream) cudaStreamSynchronize(e.stream);
     if (e.graph) cudaGraphExecDestroy(e.graph);
+    if (h->hgraph) cudaGraphExecDestroy(h->hgraph);
+    if (h->flags_h) cudaFreeHost(h->flags_h);
     dfree(e.r); dfree(e.v); dfree(e.f); dfree(e.m); dfree(e.eps); dfree(e.sig);
     dfree(e.key); dfree(e.site_mol); dfree(e.site_slot);
     dfree(e.mol_off); dfree(e.mol_cell); dfree(e.mol_rank); dfree(e.com);
@@ -796,23 +811,44 @@ static int run_probe(komd_gpu *h) {
     return KOMD_OK;
 }
 
+// one step captured into *out (replacing it)
+static int capture_step(komd_gpu *h, cudaGraphExec_t *out) {
+    Engine &e = h->e;
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(e.stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_step(h);
+    CK(cudaStreamEndCapture(e.stream, &graph));
+    if (*out) cudaGraphExecDestroy(*out);
+    *out = nullptr;
+    const cudaError_t ie = cudaGraphInstantiate(out, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) {
+        *out = nullptr;
+        return fail(KOMD_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+    }
+    return KOMD_OK;
+}
+
+// the step graph of the current configuration; every change that invalidates
+// it (buffers, terms, list capacities ...) also retires graphs of its epoch
+static int ensure_graph(komd_gpu *h) {
+    Engine &e = h->e;
+    if (e.graph_valid && e.graph) return KOMD_OK;
+    const int rc = capture_step(h, &e.graph);
+    if (rc) return rc;
+    e.graph_valid = true;
+    h->graph_epoch++;
+    return KOMD_OK;
+}
+
 static int run_steps(komd_gpu *h, int64_t n_steps) {
     Engine &e = h->e;
     if (e.profiling) {
         for (int64_t k = 0; k < n_steps; k++) enqueue_step(h);
         return check_launch("step");
     }
-    if (!e.graph_valid) {
-        cudaGraph_t graph;
-        CK(cudaStreamBeginCapture(e.stream, cudaStreamCaptureModeThreadLocal));
-        enqueue_step(h);
-        CK(cudaStreamEndCapture(e.stream, &graph));
-        if (e.graph) cudaGraphExecDestroy(e.graph);
-        const cudaError_t ie = cudaGraphInstantiate(&e.graph, graph, 0);
-        cudaGraphDestroy(graph);
-        if (ie != cudaSuccess) return fail(KOMD_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
-        e.graph_valid = true;
-    }
+    const int rc = ensure_graph(h);
+    if (rc) return rc;
     for (int64_t k = 0; k < n_steps; k++) CK(cudaGraphLaunch(e.graph, e.stream));
     h->graph_steps += n_steps;
     return KOMD_OK;
@@ -876,9 +912,31 @@ int step_host_direct(komd_gpu *h, int64_t n_steps, double *r, double *v, double 
     if (!rin || !vin || !fo) return KOMD_OK;
     *applies = true;
     double *rout = const_cast<double *>(rin), *vout = const_cast<double *>(vin), *fout = const_cast<double *>(fo);
+    if (n_steps == 1) {
+        // one launch per call: the step with these buffers bound, captured once
+        // per step graph and set of buffers
+        int rc = ensure_graph(h);
+        if (rc) return rc;
+        if (!(h->hgraph && h->hgraph_epoch == h->graph_epoch && h->hkey[0] == rin && h->hkey[1] == vin &&
+              h->hkey[2] == fo)) {
+            e.hin_r = rin;
+            e.hin_v = vin;
+            e.hout_r = rout; e.hout_v = vout; e.hout_f = fout;
+            rc = capture_step(h, &h->hgraph);
+            e.hin_r = e.hin_v = nullptr;
+            e.hout_r = e.hout_v = e.hout_f = nullptr;
+            if (rc) return rc;
+            h->hgraph_epoch = h->graph_epoch;
+            h->hkey[0] = rin;
+            h->hkey[1] = vin;
+            h->hkey[2] = fo;
+        }
+        CK(cudaGraphLaunch(h->hgraph, e.stream));
+        h->graph_steps += 1;
+        return finish_steps(h);
+    }
     e.hin_r = rin;
     e.hin_v = vin;
-    if (n_steps == 1) { e.hout_r = rout; e.hout_v = vout; e.hout_f = fout; }
     enqueue_step(h);
     e.hin_r = e.hin_v = nullptr;
     e.hout_r = e.hout_v = e.hout_f = nullptr;
