@@ -21,6 +21,15 @@ namespace komd {
 // k_atm_flush adds them to f.
 constexpr double kAtmFix = 4294967296.0;   // 2^32 fixed-point units
 
+// staged (A, 1/A, 1/sqrt A) of a neighbour at squared distance A: the
+// hardware reciprocal (about 1 ulp) and reciprocal square root; A is a squared
+// distance of order one, never in the flush-to-zero range
+__device__ __forceinline__ float4 atm_stage_q(float A) {
+    float ia;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(ia) : "f"(A));
+    return make_float4(A, ia, rsqrtf(A), 0.f);
+}
+
 __device__ __forceinline__ void atm_fix_add(unsigned long long *acc, float x) {
     // x * 2^32 is exact in FP32 (a power-of-two scale); one FP32 -> int64 conversion
     const long long q = __float2ll_rn(x * 4294967296.0f);

@@ -1370,7 +1370,7 @@ __device__ __forceinline__ int atm_stage(const AtmParams &p, int i, float4 *se, 
             const int pos = m + __popc(bm & lt);
             const float A = e.x * e.x + e.y * e.y + e.z * e.z;
             se[pos] = e;
-            sq[pos] = make_float4(A, 1.0f / A, rsqrtf(A), 0.f);
+            sq[pos] = atm_stage_q(A);
         }
         m += __popc(bm);
     }

@@ -310,13 +310,49 @@ __device__ __forceinline__ void vb_done(const PairParams &p, const VbHome &o) {
     }
 }
 
+// the 27 cells around a home cell, staged 32 sites at a time in the warp's
+// shared arrays (position in the home cell's frame; list word without the
+// same-molecule bit and molecule key); visit(jc) tests the jc staged sites
+template <typename Visit>
+__device__ __forceinline__ void vb_walk(const PairParams &p, int cx, int cy, int cz, const float4 *nbo, float4 *sq,
+                                        uint2 *sw, int lane, Visit &&visit) {
+    for (int nb = 0; nb < 27; nb++) {
+        int kx, ky, kz;
+        bool cr;
+        const int q = nb_cell(p.g, cx, cy, cz, nb, kx, ky, kz, cr);
+        const int qs = p.cell_start[q], qn = p.cell_start[q + 1] - qs;
+        const float4 o = nbo[nb];
+        for (int jb = 0; jb < qn; jb += 32) {
+            const int jc = min(32, qn - jb);
+            __syncwarp();
+            if (lane < jc) {
+                const int j = qs + jb + lane;
+                float4 pj = p.pos4[j];
+                pj.x += o.x;
+                pj.y += o.y;
+                pj.z += o.z;
+                sq[lane] = pj;
+                sw[lane] = make_uint2(((unsigned)nb << 26) | (unsigned)j, (unsigned)p.skey[j]);
+            }
+            __syncwarp();
+            visit(jc);
+        }
+    }
+}
+
+// TWO = false: a home site per lane, one walk per 32 homes (cells of up to
+// about 26 sites on average); TWO = true: cells of more than 32 sites walk
+// their neighbourhood once per 64 homes.  Both write the same rows.
+template <bool TWO>
 __global__ void __launch_bounds__(32 * kVbWarps) k_vlist_build(PairParams p) {
     __shared__ float4 s_q[kVbWarps][32];
-    __shared__ uint2 s_w[kVbWarps][32];   // (list word without the same-molecule bit, molecule key)
+    __shared__ uint2 s_w[kVbWarps][32];
     if (!*p.rebuild) return;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (blockIdx.x == 0 && threadIdx.x == 0 && p.rebuild_count) atomicAdd(p.rebuild_count, 1);
     const float rl2 = (float)p.rl2;
+    float4 *sq = s_q[w];
+    uint2 *sw = s_w[w];
     // warps take home cells from a counter (reset by the scan of this rebuild):
     // cells differ in cost, and a resident grid keeps every SM busy to the end
     for (;;) {
@@ -328,49 +364,64 @@ __global__ void __launch_bounds__(32 * kVbWarps) k_vlist_build(PairParams p) {
         cell_coords(p.g, cell, cx, cy, cz);
         const int hs = p.cell_start[cell], hn = p.cell_start[cell + 1] - hs;
         const float4 *nbo = p.nboff + (size_t)cell * 27;
-        // up to 64 home sites per walk of the neighbourhood: lane l serves homes
-        // hb + l and, in cells of more than 32 sites, hb + 32 + l
-        for (int hb = 0; hb < hn; hb += 64) {
-            const bool two = hn - hb > 32;   // warp-uniform
-            VbHome h0, h1;
-            vb_home(p, hs, hn, hb + lane, h0);
-            if (two) vb_home(p, hs, hn, hb + 32 + lane, h1);
-            for (int nb = 0; nb < 27; nb++) {
-                int kx, ky, kz;
-                bool cr;
-                const int q = nb_cell(p.g, cx, cy, cz, nb, kx, ky, kz, cr);
-                const int qs = p.cell_start[q], qn = p.cell_start[q + 1] - qs;
-                const float4 o = nbo[nb];
-                for (int jb = 0; jb < qn; jb += 32) {
-                    const int jc = min(32, qn - jb);
-                    __syncwarp();
-                    if (lane < jc) {
-                        const int j = qs + jb + lane;
-                        float4 pj = p.pos4[j];
-                        pj.x += o.x;
-                        pj.y += o.y;
-                        pj.z += o.z;
-                        s_q[w][lane] = pj;
-                        s_w[w][lane] = make_uint2(((unsigned)nb << 26) | (unsigned)j, (unsigned)p.skey[j]);
+        if (!TWO || hn <= 32) {
+          for (int hb = 0; hb < hn; hb += 32) {   // one trip unless TWO is false and hn > 32
+            // a home site per lane
+            const int h = hb + lane;
+            const bool active = h < hn;
+            const int hslot = hs + min(h, hn - 1);
+            const float4 hp = p.pos4[hslot];
+            const int hkey = p.skey[hslot];
+            const unsigned self = (13u << 26) | (unsigned)hslot;   // the site itself, in the home cell
+            unsigned *row = p.vl + (size_t)hslot * p.vl_cap;
+            int c = 0;
+            vb_walk(p, cx, cy, cz, nbo, sq, sw, lane, [&](int jc) {
+                if (active) {
+#pragma unroll 4
+                    for (int t = 0; t < jc; t++) {
+                        const float4 pj = sq[t];
+                        const float ax = hp.x - pj.x, ay = hp.y - pj.y, az = hp.z - pj.z;
+                        if (ax * ax + ay * ay + az * az <= rl2) {   // the word is read only for hits
+                            const uint2 ww = sw[t];
+                            if (ww.x != self) {
+                                if (c < p.vl_cap) row[c] = ((int)ww.y == hkey ? 0x80000000u : 0u) | ww.x;
+                                c++;
+                            }
+                        }
                     }
-                    __syncwarp();
+                }
+            });
+            if (active) {
+                p.vl_count[hslot] = min(c, p.vl_cap);
+                if (c > p.vl_cap) atomicOr(&p.err[E_VL_OVERFLOW], 1);
+            }
+          }
+        } else {
+            // up to 64 home sites per walk of the neighbourhood: lane l serves
+            // homes hb + l and, while more than 32 remain, hb + 32 + l
+            for (int hb = 0; hb < hn; hb += 64) {
+                const bool two = hn - hb > 32;   // warp-uniform
+                VbHome h0, h1;
+                vb_home(p, hs, hn, hb + lane, h0);
+                if (two) vb_home(p, hs, hn, hb + 32 + lane, h1);
+                vb_walk(p, cx, cy, cz, nbo, sq, sw, lane, [&](int jc) {
                     if (two) {   // h0 is active: hn - hb > 32
 #pragma unroll 2
                         for (int t = 0; t < jc; t++) {
-                            const float4 pj = s_q[w][t];
-                            const uint2 ww = s_w[w][t];   // one read for both homes
+                            const float4 pj = sq[t];
+                            const uint2 ww = sw[t];   // one read for both homes
                             if (vb_hit(h0, pj, rl2)) vb_emit(p, h0, ww);
                             if (h1.active && vb_hit(h1, pj, rl2)) vb_emit(p, h1, ww);
                         }
                     } else if (h0.active) {
 #pragma unroll 4
-                        for (int t = 0; t < jc; t++)   // the word is read only for hits
-                            if (vb_hit(h0, s_q[w][t], rl2)) vb_emit(p, h0, s_w[w][t]);
+                        for (int t = 0; t < jc; t++)
+                            if (vb_hit(h0, sq[t], rl2)) vb_emit(p, h0, sw[t]);
                     }
-                }
+                });
+                vb_done(p, h0);
+                if (two) vb_done(p, h1);
             }
-            vb_done(p, h0);
-            if (two) vb_done(p, h1);
         }
     }
 }
@@ -472,7 +523,7 @@ __device__ __forceinline__ int lj_site(const PairParams &p, int i, int lane, uns
                         const float4 entry = make_float4(dx, dy, dz, __int_as_float(code));
                         if (TO_SMEM) {   // staged as the sweep wants it: e and (A, 1/A, 1/sqrt A)
                             se[pos] = entry;
-                            sq[pos] = make_float4(r2, 1.0f / r2, rsqrtf(r2), 0.f);
+                            sq[pos] = atm_stage_q(r2);
                         } else {
                             p.nl[(size_t)i * p.nl_cap + pos] = entry;
                         }
@@ -577,7 +628,10 @@ void launch_vlist_build(Engine &e, cudaStream_t st) {
     PairParams p = pair_params(e);
     // a resident grid (12 blocks of 4 warps per SM at this kernel's register count)
     const int blocks = std::min((e.g.ncell + kVbWarps - 1) / kVbWarps, 152 * 12);
-    k_vlist_build<<<blocks, 32 * kVbWarps, 0, st>>>(p);
+    // the two-home form pays off once many cells hold more than 32 sites
+    const double per_cell = (double)e.n / ((double)e.g.nd[0] * e.g.nd[1] * e.g.nd[2]);
+    if (per_cell > 26.0) k_vlist_build<true><<<blocks, 32 * kVbWarps, 0, st>>>(p);
+    else k_vlist_build<false><<<blocks, 32 * kVbWarps, 0, st>>>(p);
 }
 
 template <bool UNIFORM>
