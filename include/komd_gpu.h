@@ -173,8 +173,10 @@ int  komd_gpu_step(komd_gpu *h, int64_t n_steps);
  * tables, as over NVLink-C2C) and the step is the fused Verlet / FULL FP32 ATM
  * path without device thermostat or learned term, the first step's drift
  * kernel reads r, v and writes r back, and the last step's ATM flush writes f
- * and v, so no separate copies run; otherwise copies frame the steps.  The
- * results are bitwise those of komd_gpu_step. */
+ * and v, so no separate copies run; otherwise copies frame the steps.  A
+ * one-step call on that path launches a graph captured for these buffers
+ * (recaptured when the buffers or the step change).  The results are bitwise
+ * those of komd_gpu_step. */
 int  komd_gpu_step_host(komd_gpu *h, int64_t n_steps, double *r, double *v, double *f);
 
 /* ---- sensors ------------------------------------------------------------ */
