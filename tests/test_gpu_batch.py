@@ -92,6 +92,42 @@ def test_step_host_matches_device_path(pinned):
     b.close()
 
 
+def test_step_host_graph_follows_buffers_and_stream():
+    """A one-step komd_gpu_step_host call replays a graph captured for the
+    caller's buffers.  Calls that alternate between two pinned buffer sets, and
+    calls after set_stream (which retires the step graph), stay bitwise on the
+    trajectory of komd_gpu_step."""
+    import torch
+    a = _replica(*SPECS[1])
+    b = _replica(*SPECS[1])
+    r0, v0, f0 = a.download()
+
+    def pin(x):
+        return torch.from_numpy(np.ascontiguousarray(x)).pin_memory().numpy()
+
+    sets = [(pin(r0), pin(v0), pin(np.zeros_like(f0))), (pin(r0), pin(v0), pin(np.zeros_like(f0)))]
+    side = torch.cuda.Stream()
+    cur = 0
+    for k in range(8):
+        if k == 4:
+            a.set_stream(side.cuda_stream)
+            b.set_stream(side.cuda_stream)
+        r, v, f = sets[cur]
+        a.step_host(1, r, v, f)
+        b.step(1)
+        rb, vb, fb = b.download()
+        assert np.array_equal(r, rb), k
+        assert np.array_equal(v, vb), k
+        assert np.array_equal(f, fb), k
+        if k % 2:   # the next call reads the other buffer set
+            nr, nv, _ = sets[1 - cur]
+            nr[:] = r
+            nv[:] = v
+            cur = 1 - cur
+    a.close()
+    b.close()
+
+
 def test_batch_512_replicas_full_size():
     """The batched-replicas workload at its full size: 512 LJ + ATM boxes,
     N ~ U[2000, 20000] (FCC filled, trimmed by seed), rho* ~ U[0.70, 0.90],
