@@ -265,7 +265,8 @@ __global__ void __launch_bounds__(kTileThreads) k_pair_tile(PairParams p) {
 
 // ---------------------------------------------------------------------------
 // Verlet list build (rebuild steps only): one warp per home cell, one lane per
-// home site (groups of 32 when a cell holds more).  The warp walks the 27
+// home site (groups of 32 when a cell holds more, or two homes per lane in
+// the form for crowded cells).  The warp walks the 27
 // neighbour cells in order and stages each one's sites (position with the
 // cell's periodic offset, list word, molecule key) in warp-private shared
 // memory; every lane tests them all against its site and appends the hits to
