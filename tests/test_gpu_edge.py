@@ -18,8 +18,9 @@ def rel_rmse(a, b):
 
 def _sites(r, v, L):
     from komd_gb300 import lattice
+    r = np.asarray(r, np.float64).reshape(-1, 3)
     n = r.shape[0]
-    return lattice.System(r=np.asarray(r, np.float64), v=np.asarray(v, np.float64), m=np.ones(n), eps=np.ones(n),
+    return lattice.System(r=r, v=np.asarray(v, np.float64).reshape(-1, 3), m=np.ones(n), eps=np.ones(n),
                           sig=np.ones(n), mol_id=np.arange(1, n + 1, dtype=np.uint64), low=np.zeros(3),
                           high=np.asarray(L, np.float64))
 
