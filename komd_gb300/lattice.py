@@ -81,7 +81,7 @@ def maxwell_boltzmann(n: int, t_star: float, m: np.ndarray, rng: np.random.Gener
 
 def argon_fcc(ncell: int | tuple, rho: float = 0.8442, t_star: float = 0.722, seed: int = 1,
               jitter: float = 0.0) -> System:
-    """Single-site LJ argon on an FCC lattice (BASELINE configs 1, 2, 4)."""
+    """Single-site LJ argon on an FCC lattice (the 4k plain-LJ, 32k LJ+ATM and 256k LJ+ATM workloads)."""
     rng = np.random.default_rng(seed)
     r, L = fcc_positions(ncell, rho)
     if jitter > 0:
@@ -122,7 +122,7 @@ def _rotation(rng: np.random.Generator) -> np.ndarray:
 def triatomic_sc(n_mol_side: int, rho_site: float = 0.8, t_star: float = 1.0, seed: int = 3,
                  r0: float = 1.0, theta0_deg: float = 109.47) -> System:
     """Flexible 3-site molecules (bond r0, angle theta0) centred on the sites
-    of a simple-cubic lattice with a random orientation each (BASELINE config 3).
+    of a simple-cubic lattice with a random orientation each (the 300k-site multi-site workload).
     Topology: bonds (0,1), (1,2); angle (0,1,2) with site 1 the vertex."""
     rng = np.random.default_rng(seed)
     n_mol = n_mol_side ** 3
