@@ -39,20 +39,27 @@ __device__ __forceinline__ void atm_fix_add(unsigned long long *acc, float x) {
 struct AtmV {
     float vA, vB, vC;
 };
-// dV/dA, dV/dB, dV/dC over nu from the squared sides and the staged (A, 1/A, 1/sqrt(A))
+// dV/dA, dV/dB, dV/dC over nu from the squared sides and the staged (A, 1/A, 1/sqrt(A)).
+// With t1 = A + B - C, t2 = A - B + C, t3 = B + C - A (= S - 2C, S - 2B, S - 2A for
+// S = A + B + C), u = t2 t3, v = t1 t3, w = t1 t2, P = t1 t2 t3 and s5 = 1/(abc)^5:
+//   dV/dA = s5 (3/8 (u + v - w) - 3/2 B C - 15/16 P / A)   (B with v and A C; C with u and A B),
+// written around K = 3/8 (u + v + w), which the three share.
 __device__ __forceinline__ AtmV atm_derivs(float4 qa, float4 qb, float C) {
     const float A = qa.x, B = qb.x;
     const float wc = rsqrtf(C);
     const float sv = qa.z * qb.z * wc;                  // 1/(abc)
     const float s2 = sv * sv;
     const float s5 = s2 * s2 * sv;
-    const float t1 = A + B - C, t2 = A - B + C, t3 = B + C - A;
+    const float S = A + B + C;
+    const float t1 = fmaf(-2.0f, C, S), t2 = fmaf(-2.0f, B, S), t3 = fmaf(-2.0f, A, S);
     const float u = t2 * t3, v = t1 * t3, w = t1 * t2;
-    const float P = t1 * u;
+    const float K = 0.375f * (u + v + w);
+    const float nP = -0.9375f * (t1 * u);
+    const float a15 = -1.5f * A;
     AtmV r;
-    r.vA = s5 * (-1.5f * B * C + 0.375f * (u + v - w) - 0.9375f * P * qa.y);
-    r.vB = s5 * (-1.5f * A * C + 0.375f * (u - v + w) - 0.9375f * P * qb.y);
-    r.vC = s5 * (-1.5f * A * B + 0.375f * (-u + v + w) - 0.9375f * P * (wc * wc));
+    r.vA = s5 * fmaf(nP, qa.y, fmaf(-0.75f, w, fmaf(-1.5f * B, C, K)));
+    r.vB = s5 * fmaf(nP, qb.y, fmaf(-0.75f, v, fmaf(a15, C, K)));
+    r.vC = s5 * fmaf(nP, wc * wc, fmaf(-0.75f, u, fmaf(a15, B, K)));
     return r;
 }
 
