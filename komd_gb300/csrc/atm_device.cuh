@@ -100,12 +100,14 @@ __device__ __forceinline__ void atm_sweep(const float4 *se, const float4 *sq, in
                 bz = -tz - v.vB * eb.z;
             }
         }
-        // lane li pulls the share computed, in this lane group, by the lane whose partner it was
-        const int s = (act ? src : li) + gb;   // lanes without a round pull from themselves
-        const float rx = __shfl_sync(0xffffffffu, bx, s);
-        const float ry = __shfl_sync(0xffffffffu, by, s);
-        const float rz = __shfl_sync(0xffffffffu, bz, s);
-        if (act) { ax += rx; ay += ry; az += rz; }
+        // lane li pulls the share computed, in this lane group, by the lane whose
+        // partner it was.  In a round past d_last the source lane has no round
+        // either and sends zero; lanes without a neighbour (li >= m) pull
+        // whatever their index gives, and their sums are never used.
+        const int s = src + gb;
+        ax += __shfl_sync(0xffffffffu, bx, s);
+        ay += __shfl_sync(0xffffffffu, by, s);
+        az += __shfl_sync(0xffffffffu, bz, s);
         b = b + 1 == m ? 0 : b + 1;
         src = src == 0 ? m - 1 : src - 1;
     }
