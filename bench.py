@@ -305,6 +305,75 @@ def replicas_leg(args, stream, local):
                       "rc 2.5 / 2.0, nu* 0.073, dt* 0.005, skin 0.3; RDF 200 bins to 2.5, virial pressure per replica"}
 
 
+def next_rows_leg(args, stream, local):
+    """The rows on either side of the hot path, on the 256k argon lattice
+    (jittered FCC 40^3): steps with the IBI tabulated pair force (IBI_ForceFunctor,
+    FP64 on per-step cells, a 200-node table of the LJ force), one RDF_Profiler
+    sample (komd_gpu_rdf_profile, 100 bins to 2.5), ATM2B (the LJ force scaled by
+    the two-body ATM factor, FP32 on the Verlet list) and the LJ + ATM step with
+    the VelocityScaling thermostat inside the step graph.  Each is timed with
+    CUDA events over K steps replayed from its step graph."""
+    import torch
+    from komd_gb300 import autotune, gpu, lattice
+    w = WORKLOADS["lj_atm_argon_256k"]
+    s = lattice.argon_fcc(w["ncell"], rho=w["rho"], t_star=w["t"], seed=3, jitter=0.02)
+    side = float(np.min(s.high - s.low))
+    k = args.next_steps
+    t_kelvin = w["t"] * 1.2027235   # T* in the reference's Kelvin (sigma = 1 A, m = 1 u, eps* = 1)
+
+    def events_ms(fn):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b)
+
+    def run(cfg, table=None):
+        g = gpu.GpuSystem(s, cfg, device=local)
+        try:
+            g.set_stream(stream.cuda_stream)
+            if table is not None:
+                g.set_pair_table(*table)
+            g.update_container()
+            g.forces()
+            g.step(3)
+            torch.cuda.synchronize()
+            ms = events_ms(lambda: g.step(k))
+            extra = {}
+            if table is not None:
+                g.rdf_profile(2.5, 100)
+                extra["rdf_profile_ms"] = events_ms(lambda: g.rdf_profile(2.5, 100))
+            return dict(value=s.n * k / (ms / 1e3), unit=UNIT, ms_per_step=ms / k, steps=k, **extra)
+        finally:
+            g.close()
+
+    out = {}
+    legs = {
+        "ibi_tabulated_fp64": lambda: run(
+            gpu.make_config(s.low, s.high, autotune.cell_for(side, 2.5), cutoff=2.5, terms=gpu.TERM_TABULATED,
+                            precision=gpu.FP64),
+            table=(np.linspace(0.6, 2.5, 200), 24.0 * (2.0 * np.linspace(0.6, 2.5, 200) ** -13
+                                                       - np.linspace(0.6, 2.5, 200) ** -7), 1e6, 0.0)),
+        "atm2b_fp32_verlet": lambda: run(
+            gpu.make_config(s.low, s.high, autotune.cell_for(side, 2.9), cutoff=2.5, nu=w["nu"],
+                            terms=gpu.TERM_LJ | gpu.TERM_ATM2B, virial_mode=gpu.VIRIAL_CORRECT, skin=0.4)),
+        "lj_atm_thermostat": lambda: run(
+            gpu.make_config(s.low, s.high, autotune.cell_for(side, 2.9), cutoff=2.5, cutoff_3b=2.0, nu=w["nu"],
+                            terms=gpu.TERM_LJ | gpu.TERM_ATM, atm_sign=gpu.ATM_SIGN_PHYSICAL,
+                            atm_enum=gpu.ATM_ENUM_FULL, virial_mode=gpu.VIRIAL_CORRECT, skin=0.4, thermostat=1,
+                            temperature_target=t_kelvin)),
+    }
+    for name, fn in legs.items():
+        try:
+            out[name] = fn()
+        except Exception as exc:   # reported in the line; the headline stands on its own
+            out[name] = {"error": f"{type(exc).__name__}: {exc}"}
+    out["system"] = "256,000 argon atoms, FCC 40^3 jittered by 0.02 sigma, rho* 0.8442; K steps from each step graph"
+    return out
+
+
 def drift_leg(args, local, model=None):
     """NVE energy drift: 32,000 LJ + ATM argon atoms (FCC 20^3, rho* 0.8442,
     T* 0.722), rc 2.5 / 2.0, nu* 0.073, dt* 0.005, 1000 steps of
@@ -534,6 +603,9 @@ def run_ours(args, w, name):
     drift = None
     if w["atm"] and not args.no_drift and rank == 0:
         drift = drift_leg(args, local, getattr(g, "last_model", None))
+    nxt = None
+    if w["atm"] and args.next_steps > 0 and rank == 0:
+        nxt = next_rows_leg(args, stream, local)
 
     if rank != 0:
         if dist:
@@ -598,6 +670,8 @@ def run_ours(args, w, name):
         line["replicas"] = reps
     if drift:
         line["nve_drift"] = drift
+    if nxt is not None:
+        line["next_rows"] = nxt
     print(json.dumps(line), flush=True)
     g.close()
     if dist:
@@ -621,6 +695,8 @@ def main():
     ap.add_argument("--replicas", type=int, default=512, help="batched-replica leg (0 = skip)")
     ap.add_argument("--no-drift", action="store_true", help="skip the NVE energy-drift leg")
     ap.add_argument("--skin", type=float, default=None, help="fixed Verlet skin (default: chosen by the autotuner)")
+    ap.add_argument("--next-steps", type=int, default=20,
+                    help="steps timed per configuration of the rows around the path (0 = skip)")
     ap.add_argument("--replica-steps", type=int, default=20)
     ap.add_argument("--replica-streams", type=int, default=32)
     ap.add_argument("--replica-graph-steps", type=int, default=5)
