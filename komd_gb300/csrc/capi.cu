@@ -506,7 +506,7 @@ int komd_gpu_destroy(komd_gpu *h) {
     dfree(e.cell_count); dfree(e.cell_start); dfree(e.cell_mcount); dfree(e.cell_mstart); dfree(e.cell_mols);
     dfree(e.slot_site); dfree(e.skey); dfree(e.pos4); dfree(e.seps); dfree(e.posd); dfree(e.seps_d); dfree(e.sig_d);
     dfree(e.nl); dfree(e.nl_count); dfree(e.bonds); dfree(e.angles); dfree(e.partials); dfree(e.err);
-    dfree(e.tab_x); dfree(e.tab_y); dfree(e.atm_acc);
+    dfree(e.tab_x); dfree(e.tab_y); dfree(e.tab_s); dfree(e.atm_acc);
     dfree(e.rdf); dfree(e.lj_hist); dfree(e.counts); dfree(h->f_scratch); dfree(h->prof); dfree(h->acc); dfree(h->thermo_acc); dfree(e.offtab);
     dfree(e.nboff); dfree(e.vb_next); dfree(e.rebuild); dfree(e.bias); dfree(e.ref4); dfree(e.slot_cell); dfree(e.vl); dfree(e.vl_count);
     dfree(e.rebuild_count); dfree(e.hdtm); dfree(e.exact_com);
@@ -982,6 +982,7 @@ int komd_gpu_set_pair_table(komd_gpu *h, int32_t n, const double *x, const doubl
     if (n != e.tab_n) {
         CK(dalloc(e.tab_x, n));
         CK(dalloc(e.tab_y, n));
+        CK(dalloc(e.tab_s, n));
         e.tab_n = n;
         if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
         e.graph_valid = false;
@@ -989,6 +990,10 @@ int komd_gpu_set_pair_table(komd_gpu *h, int32_t n, const double *x, const doubl
     // same-size tables are replaced in place: graphs already captured read the new values
     CK(cudaMemcpy(e.tab_x, x, sizeof(double) * n, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(e.tab_y, y, sizeof(double) * n, cudaMemcpyHostToDevice));
+    // segment slopes, the quotient FunctionPL::evaluateAt forms (IBI_Math.h:30-44)
+    std::vector<double> sl(n, 0.0);
+    for (int32_t k = 0; k + 1 < n; k++) sl[k] = (y[k + 1] - y[k]) / (x[k + 1] - x[k]);
+    CK(cudaMemcpy(e.tab_s, sl.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
     if (e.tab_lo != below || e.tab_hi != above) {
         e.tab_lo = below;
         e.tab_hi = above;

@@ -268,7 +268,7 @@ struct Engine {
     unsigned long long *atm_acc = nullptr;   // 3 per slot, fixed-point force sums of k_atm_s (zero between steps)
     // tabulated pair force (KOMD_TERM_TABULATED): F(r) piecewise linear on
     // ascending nodes tab_x, values tab_y, tab_lo below / tab_hi above the nodes
-    double *tab_x = nullptr, *tab_y = nullptr;
+    double *tab_x = nullptr, *tab_y = nullptr, *tab_s = nullptr;   // nodes, values, segment slopes
     int tab_n = 0;
     double tab_lo = 0.0, tab_hi = 0.0;
     double *atm_esite = nullptr;     // when set, measure-mode ATM writes per-site energies here

@@ -1129,11 +1129,14 @@ __global__ void k_sum_partials(int nblocks, const double *__restrict__ partials,
 // plugins/IBI/IBI_ForceFunctor.cpp:18-37, FunctionPL::evaluateAt,
 // plugins/IBI/IBI_Math.h:30-44): for every pair inside the cutoff (no
 // same-molecule exclusion) F = table(r), force = (dr / r) * F on the site.
-// FP64 with the reference's operation order; the upper node is the first
-// node >= r (binary search, the same node the reference's linear scan finds).
-// At r == x[0] the reference reads x[-1]; here the first segment is used.
+// FP64 with the reference's operation order per pair; the upper node is the
+// first node >= r (binary search, the same node the reference's linear scan
+// finds), and slope[k] = (y[k+1] - y[k]) / (x[k+1] - x[k]) is the quotient the
+// reference forms, computed once with the same IEEE operations.  At r == x[0]
+// the reference reads x[-1]; here the first segment is used.
 __device__ __forceinline__ double table_eval(double x, int n, const double *__restrict__ xs,
-                                             const double *__restrict__ ys, double lo, double hi) {
+                                             const double *__restrict__ ys, const double *__restrict__ slope,
+                                             double lo, double hi) {
     if (x > xs[n - 1]) return hi;
     if (x < xs[0]) return lo;
     int a = 0, b = n - 1;           // lower_bound: first index with xs[i] >= x
@@ -1142,48 +1145,138 @@ __device__ __forceinline__ double table_eval(double x, int n, const double *__re
         if (x > xs[m]) a = m + 1;
         else b = m;
     }
-    const int ub = a < 1 ? 1 : a, lb = ub - 1;
-    const double ya = ys[lb], yb = ys[ub], xa = xs[lb], xb = xs[ub];
-    return dadd(ya, dmul(ddiv(dsub(yb, ya), dsub(xb, xa)), dsub(x, xa)));
+    const int lb = (a < 1 ? 1 : a) - 1;
+    return dadd(ys[lb], dmul(slope[lb], dsub(x, xs[lb])));
 }
 
-__global__ void __launch_bounds__(kBlock) k_pair_table(Grid g, const int *__restrict__ cell_start,
-                                                      const int *__restrict__ slot_site,
-                                                      const double *__restrict__ posd, double rc2, int n,
-                                                      const double *__restrict__ xs, const double *__restrict__ ys,
-                                                      double lo, double hi, double *f) {
-    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int cell = blockIdx.x * kWarpsPerBlock + wib;
-    if (cell >= g.ncell) return;
+// One warp per home cell.  The 27-cell neighbourhood is staged in shared
+// memory in FP32 home-cell coordinates (cell-local position plus the
+// neighbour cell's centre offset); for each home site the lanes test 32
+// staged sites at a time against the cutoff with a 1e-4 relative margin (the
+// FP32 separation is good to ~1e-7, so the test only drops pairs that are
+// clearly outside), queue the hits by ballot, and evaluate the queue 32 pairs
+// at a time in FP64 from the FP64 positions and the neighbour cell's periodic
+// shift, with the exact cutoff test.  Per home site the lanes' sums are
+// reduced in a fixed tree and added to f.
+constexpr int kTabWarps = 4;
+constexpr int kTabStage = 416;   // staged sites per round (more rounds for a larger neighbourhood)
+
+__global__ void __launch_bounds__(32 * kTabWarps) k_pair_table(
+    Grid g, const int *__restrict__ cell_start, const int *__restrict__ slot_site, const double *__restrict__ posd,
+    const float4 *__restrict__ pos4, const float *__restrict__ offtab, double rc2, int n,
+    const double *__restrict__ xs, const double *__restrict__ ys, const double *__restrict__ slope, double lo,
+    double hi, double *__restrict__ f) {
+    __shared__ float4 s_p[kTabWarps][kTabStage];
+    __shared__ int2 s_j[kTabWarps][kTabStage];   // slot, neighbour-cell index
+    __shared__ double s_sh[kTabWarps][27][3];
+    __shared__ float s_o[kTabWarps][27][3];
+    __shared__ int s_st[kTabWarps][27], s_pre[kTabWarps][28];
+    __shared__ int s_q[kTabWarps][64];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int cell = blockIdx.x * kTabWarps + w;
+    if (cell >= g.ncell) return;   // warp-uniform; the kernel uses no block barrier
+    unsigned lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
     int cx, cy, cz;
     cell_coords(g, cell, cx, cy, cz);
-    const int hs = cell_start[cell], hn = cell_start[cell + 1] - hs;
-    for (int k = lane; k < hn; k += 32) {
-        const int is = hs + k;
-        const double xi = posd[3 * is], yi = posd[3 * is + 1], zi = posd[3 * is + 2];
-        double fx = 0.0, fy = 0.0, fz = 0.0;
-        for (int nb = 0; nb < 27; nb++) {
-            const NbCell q = neighbour_cell(g, cx, cy, cz, nb);
-            const int js = cell_start[q.cell], jn = cell_start[q.cell + 1] - js;
-            for (int j = js; j < js + jn; j++) {
-                if (j == is) continue;
-                const double *pj = posd + 3 * j;
-                const double dx = dsub(xi, dadd(pj[0], q.shift[0]));
-                const double dy = dsub(yi, dadd(pj[1], q.shift[1]));
-                const double dz = dsub(zi, dadd(pj[2], q.shift[2]));
+    int cnt = 0;
+    if (lane < 27) {
+        const NbCell q = neighbour_cell(g, cx, cy, cz, lane);
+        const int s0 = cell_start[q.cell];
+        cnt = cell_start[q.cell + 1] - s0;
+        s_st[w][lane] = s0;
+        for (int d = 0; d < 3; d++) s_sh[w][lane][d] = q.shift[d];
+        s_o[w][lane][0] = offtab[cx * 3 + lane % 3];
+        s_o[w][lane][1] = offtab[g.nd[0] * 3 + cy * 3 + (lane / 3) % 3];
+        s_o[w][lane][2] = offtab[(g.nd[0] + g.nd[1]) * 3 + cz * 3 + lane / 9];
+    }
+    int inc = cnt;   // inclusive prefix of the 27 counts
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane < 27) s_pre[w][lane] = inc - cnt;
+    const int total = __shfl_sync(0xffffffffu, inc, 26);
+    if (lane == 0) s_pre[w][27] = total;
+    __syncwarp();
+    const int hs = s_st[w][13], hn = s_pre[w][14] - s_pre[w][13];   // neighbour 13 is the home cell
+    const float pre2 = (float)(rc2 * (1.0 + 1e-4));
+    for (int sb = 0; sb < total; sb += kTabStage) {
+        const int ns = min(kTabStage, total - sb);
+        __syncwarp();
+        for (int t = lane; t < ns; t += 32) {
+            const int gi = sb + t;
+            int a = 0, b = 27;   // the neighbour cell holding staged site gi
+            while (b - a > 1) {
+                const int mid = (a + b) >> 1;
+                if (s_pre[w][mid] <= gi) a = mid;
+                else b = mid;
+            }
+            const int j = s_st[w][a] + (gi - s_pre[w][a]);
+            float4 q = pos4[j];
+            q.x += s_o[w][a][0];
+            q.y += s_o[w][a][1];
+            q.z += s_o[w][a][2];
+            s_p[w][t] = q;
+            s_j[w][t] = make_int2(j, a);
+        }
+        __syncwarp();
+        for (int h = 0; h < hn; h++) {
+            const int is = hs + h;
+            const float4 hp = pos4[is];
+            const double xi = posd[3 * is], yi = posd[3 * is + 1], zi = posd[3 * is + 2];
+            double fx = 0.0, fy = 0.0, fz = 0.0;
+            auto eval = [&](int c) {
+                if (c < 0) return;
+                const int2 jn = s_j[w][c];
+                const double *pj = posd + 3 * (size_t)jn.x;
+                const double dx = dsub(xi, dadd(pj[0], s_sh[w][jn.y][0]));
+                const double dy = dsub(yi, dadd(pj[1], s_sh[w][jn.y][1]));
+                const double dz = dsub(zi, dadd(pj[2], s_sh[w][jn.y][2]));
                 const double r2 = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
-                if (r2 > rc2) continue;
+                if (r2 > rc2) return;
                 const double r = __dsqrt_rn(r2);
-                const double F = table_eval(r, n, xs, ys, lo, hi);
+                const double F = table_eval(r, n, xs, ys, slope, lo, hi);
                 fx = dadd(fx, dmul(ddiv(dx, r), F));
                 fy = dadd(fy, dmul(ddiv(dy, r), F));
                 fz = dadd(fz, dmul(ddiv(dz, r), F));
+            };
+            int qn = 0;
+            for (int c0 = 0; c0 < ns; c0 += 32) {
+                const int c = c0 + lane;
+                bool hit = false;
+                if (c < ns && s_j[w][c].x != is) {
+                    const float4 pj = s_p[w][c];
+                    const float dx = hp.x - pj.x, dy = hp.y - pj.y, dz = hp.z - pj.z;
+                    hit = dx * dx + dy * dy + dz * dz <= pre2;
+                }
+                const unsigned m = __ballot_sync(0xffffffffu, hit);
+                if (hit) s_q[w][qn + __popc(m & lt)] = c;
+                qn += __popc(m);
+                if (qn >= 32) {   // a full batch: one queued pair per lane
+                    __syncwarp();
+                    eval(s_q[w][lane]);
+                    __syncwarp();
+                    qn -= 32;
+                    if (lane < qn) s_q[w][lane] = s_q[w][32 + lane];
+                    __syncwarp();
+                }
             }
+            __syncwarp();
+            eval(lane < qn ? s_q[w][lane] : -1);
+            for (int o = 16; o > 0; o >>= 1) {
+                fx = dadd(fx, __shfl_xor_sync(0xffffffffu, fx, o));
+                fy = dadd(fy, __shfl_xor_sync(0xffffffffu, fy, o));
+                fz = dadd(fz, __shfl_xor_sync(0xffffffffu, fz, o));
+            }
+            if (lane == 0) {
+                const int site = slot_site[is];
+                f[3 * site] = dadd(f[3 * site], fx);
+                f[3 * site + 1] = dadd(f[3 * site + 1], fy);
+                f[3 * site + 2] = dadd(f[3 * site + 2], fz);
+            }
+            __syncwarp();
         }
-        const int site = slot_site[is];
-        f[3 * site] = dadd(f[3 * site], fx);
-        f[3 * site + 1] = dadd(f[3 * site + 1], fy);
-        f[3 * site + 2] = dadd(f[3 * site + 2], fz);
     }
 }
 
@@ -1543,10 +1636,10 @@ void launch_step1(Engine &e, cudaStream_t st) {
 int kinetic_grid(const Engine &e) { return nblk(e.n, kBlock); }
 
 void launch_pair_table(Engine &e, cudaStream_t st) {
-    if (!e.tab_x || e.tab_n < 2) return;
-    k_pair_table<<<nblk(e.g.ncell, kWarpsPerBlock), kBlock, 0, st>>>(e.g, e.cell_start, e.slot_site, e.posd, e.cfg.cutoff *
-                                                                   e.cfg.cutoff, e.tab_n, e.tab_x, e.tab_y, e.tab_lo,
-                                                                   e.tab_hi, e.f);
+    if (!e.tab_x || !e.tab_s || e.tab_n < 2) return;
+    k_pair_table<<<nblk(e.g.ncell, kTabWarps), 32 * kTabWarps, 0, st>>>(
+        e.g, e.cell_start, e.slot_site, e.posd, e.pos4, e.offtab, e.cfg.cutoff * e.cfg.cutoff, e.tab_n, e.tab_x,
+        e.tab_y, e.tab_s, e.tab_lo, e.tab_hi, e.f);
 }
 
 void launch_velocity_scale(Engine &e, cudaStream_t st, const double *acc, double beta) {
