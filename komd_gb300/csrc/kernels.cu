@@ -1090,20 +1090,141 @@ __device__ __forceinline__ void rdf_pair(const double *ca, const double *cb, Gri
     atomicAdd(&bins[b], 1.0);
 }
 
-__global__ void k_rdf_cells(Grid g, int n_mol, const double *__restrict__ com, const int *__restrict__ mol_cell,
-                            const int *__restrict__ cell_mstart, const int *__restrict__ cell_mols, double max_r,
-                            double dr, long long nbins, double *bins) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n_mol) return;
-    int cx, cy, cz;
-    cell_coords(g, mol_cell[k], cx, cy, cz);
-    for (int nb = 0; nb < 27; nb++) {
-        const NbCell q = neighbour_cell(g, cx, cy, cz, nb);
-        for (int u = cell_mstart[q.cell]; u < cell_mstart[q.cell + 1]; u++) {
-            const int o = cell_mols[u];
-            if (o == k) continue;
-            rdf_pair(com + 3 * k, com + 3 * o, g, max_r, dr, nbins, bins);
+// Cell path (max_r <= cell edge): one warp per home cell.  The molecules of the
+// 27 neighbour cells are staged in shared memory as FP32 COMs relative to the
+// home cell's centre (formed in FP64, then rounded); for each home molecule
+// the lanes test 32 staged molecules at a time against max_r with a 1e-4
+// relative margin and queue the hits, and the queued pairs take rdf_pair's
+// FP64 arithmetic, so the bin of every pair is the reference's.  The counts go
+// to a per-block shared histogram of integers (hist_smem) or straight to bins,
+// and the block adds its integer counts to bins at the end: the sums are
+// exact, whatever the order.
+constexpr int kRdfWarps = 4;
+constexpr int kRdfStage = 320;
+constexpr int kRdfSmemBins = 2048;   // with the staging arrays, under the 48 KB default
+
+__device__ __forceinline__ long long rdf_pair_bin(const double *ca, const double *cb, Grid g, double max_r, double dr,
+                                                  long long nbins) {
+    double q[3];
+    for (int d = 0; d < 3; d++) {
+        const double delta = dsub(ca[d], cb[d]);
+        // round(delta / L) is 0 for |delta| < 0.4 L whatever the quotient's rounding; the
+        // division runs only where the minimum image can move the pair
+        const double img = fabs(delta) < 0.4 * g.L[d] ? 0.0 : (double)(long long)round(ddiv(delta, g.L[d]));
+        q[d] = dsub(delta, dmul(g.L[d], img));
+    }
+    const double rr = sqrt(dadd(dadd(dmul(q[0], q[0]), dmul(q[1], q[1])), dmul(q[2], q[2])));
+    if (rr > max_r) return -1;
+    unsigned long long b = (unsigned long long)ddiv(rr, dr);
+    if (b > (unsigned long long)(nbins - 1)) b = nbins - 1;
+    return (long long)b;
+}
+
+__global__ void __launch_bounds__(32 * kRdfWarps) k_rdf_cells(Grid g, const double *__restrict__ com,
+                                                              const int *__restrict__ cell_mstart,
+                                                              const int *__restrict__ cell_mols, double max_r,
+                                                              double dr, long long nbins, bool hist_smem,
+                                                              double *bins) {
+    extern __shared__ unsigned s_hist[];   // nbins counts when hist_smem
+    __shared__ float4 s_p[kRdfWarps][kRdfStage];
+    __shared__ int2 s_j[kRdfWarps][kRdfStage];   // molecule, neighbour-cell index
+    __shared__ double s_sh[kRdfWarps][27][3];
+    __shared__ int s_st[kRdfWarps][27], s_pre[kRdfWarps][28];
+    __shared__ int s_q[kRdfWarps][64];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (hist_smem)
+        for (int b = threadIdx.x; b < nbins; b += blockDim.x) s_hist[b] = 0u;
+    __syncthreads();
+    const int cell = blockIdx.x * kRdfWarps + w;
+    if (cell < g.ncell) {
+        unsigned lt;
+        asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+        int cx, cy, cz;
+        cell_coords(g, cell, cx, cy, cz);
+        const double ctr[3] = {cell_centre(g, 0, cx), cell_centre(g, 1, cy), cell_centre(g, 2, cz)};
+        int cnt = 0;
+        if (lane < 27) {
+            const NbCell q = neighbour_cell(g, cx, cy, cz, lane);
+            const int s0 = cell_mstart[q.cell];
+            cnt = cell_mstart[q.cell + 1] - s0;
+            s_st[w][lane] = s0;
+            for (int d = 0; d < 3; d++) s_sh[w][lane][d] = q.shift[d];
         }
+        int inc = cnt;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        if (lane < 27) s_pre[w][lane] = inc - cnt;
+        const int total = __shfl_sync(0xffffffffu, inc, 26);
+        if (lane == 0) s_pre[w][27] = total;
+        __syncwarp();
+        const int hs = s_st[w][13], hn = s_pre[w][14] - s_pre[w][13];
+        const float pre2 = (float)(max_r * max_r * (1.0 + 1e-4));
+        auto rel = [&](int o, int nb) {   // FP32 COM relative to the home centre, through the periodic shift
+            const double *c = com + 3 * (size_t)o;
+            return make_float4((float)dsub(dadd(c[0], s_sh[w][nb][0]), ctr[0]),
+                               (float)dsub(dadd(c[1], s_sh[w][nb][1]), ctr[1]),
+                               (float)dsub(dadd(c[2], s_sh[w][nb][2]), ctr[2]), 0.f);
+        };
+        for (int sb = 0; sb < total; sb += kRdfStage) {
+            const int ns = min(kRdfStage, total - sb);
+            __syncwarp();
+            for (int t = lane; t < ns; t += 32) {
+                const int gi = sb + t;
+                int a = 0, b = 27;
+                while (b - a > 1) {
+                    const int mid = (a + b) >> 1;
+                    if (s_pre[w][mid] <= gi) a = mid;
+                    else b = mid;
+                }
+                const int o = cell_mols[s_st[w][a] + (gi - s_pre[w][a])];
+                s_p[w][t] = rel(o, a);
+                s_j[w][t] = make_int2(o, a);
+            }
+            __syncwarp();
+            for (int h = 0; h < hn; h++) {
+                const int k = cell_mols[hs + h];
+                const float4 hp = rel(k, 13);
+                auto count = [&](int c) {
+                    if (c < 0) return;
+                    const long long b = rdf_pair_bin(com + 3 * (size_t)k, com + 3 * (size_t)s_j[w][c].x, g, max_r, dr,
+                                                     nbins);
+                    if (b < 0) return;
+                    if (hist_smem) atomicAdd(&s_hist[b], 1u);
+                    else atomicAdd(&bins[b], 1.0);
+                };
+                int qn = 0;
+                for (int c0 = 0; c0 < ns; c0 += 32) {
+                    const int c = c0 + lane;
+                    bool hit = false;
+                    if (c < ns && s_j[w][c].x != k) {
+                        const float4 pj = s_p[w][c];
+                        const float dx = hp.x - pj.x, dy = hp.y - pj.y, dz = hp.z - pj.z;
+                        hit = dx * dx + dy * dy + dz * dz <= pre2;
+                    }
+                    const unsigned m = __ballot_sync(0xffffffffu, hit);
+                    if (hit) s_q[w][qn + __popc(m & lt)] = c;
+                    qn += __popc(m);
+                    if (qn >= 32) {
+                        __syncwarp();
+                        count(s_q[w][lane]);
+                        __syncwarp();
+                        qn -= 32;
+                        if (lane < qn) s_q[w][lane] = s_q[w][32 + lane];
+                        __syncwarp();
+                    }
+                }
+                __syncwarp();
+                count(lane < qn ? s_q[w][lane] : -1);
+                __syncwarp();
+            }
+        }
+    }
+    if (hist_smem) {
+        __syncthreads();
+        for (int b = threadIdx.x; b < nbins; b += blockDim.x)
+            if (s_hist[b]) atomicAdd(&bins[b], (double)s_hist[b]);
     }
 }
 
@@ -1660,9 +1781,11 @@ void launch_rdf(Engine &e, cudaStream_t st, double *bins, bool cells) {
 }
 
 void launch_rdf_bins(Engine &e, cudaStream_t st, double *bins, bool cells, double max_r, double dr, int64_t nbins) {
-    if (cells)
-        k_rdf_cells<<<nblk(e.n_mol, 128), 128, 0, st>>>(e.g, (int)e.n_mol, e.com, e.mol_cell, e.cell_mstart,
-                                                          e.cell_mols, max_r, dr, nbins, bins);
+    if (cells) {
+        const bool hist_smem = nbins <= kRdfSmemBins;
+        k_rdf_cells<<<nblk(e.g.ncell, kRdfWarps), 32 * kRdfWarps, hist_smem ? sizeof(unsigned) * nbins : 0, st>>>(
+            e.g, e.com, e.cell_mstart, e.cell_mols, max_r, dr, nbins, hist_smem, bins);
+    }
     else
         k_rdf_all<<<nblk(e.n_mol, 128), 128, 0, st>>>(e.g, (int)e.n_mol, e.com, max_r, dr, nbins, bins);
 }
