@@ -1036,26 +1036,32 @@ __global__ void k_refresh(int n, const int *__restrict__ slot_site, const double
 // ===========================================================================
 // TemperatureSensor::measure (sites inside [low, high]) + kinetic tensor
 // (PressureSensor::MomentumKernel) over the first n_terms sites.
+// Grid-stride over the sites (a resident grid, so each thread sums several
+// sites before the fixed-tree warp and block reductions; the order is fixed,
+// so the sums are deterministic).  TERMS adds the per-site kinetic tensor of
+// the first n_terms sites.
+template <bool TERMS>
 __global__ void __launch_bounds__(kBlock) k_kinetic(Grid g, int n, int n_terms, const double *__restrict__ r,
                                                     const double *__restrict__ v, const double *__restrict__ m,
                                                     double *__restrict__ partials) {
     __shared__ double s_part[kWarpsPerBlock][8];
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    double vals[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    if (s < n) {
+    constexpr int kVals = TERMS ? 8 : 2;
+    double vals[kVals];
+    for (int k = 0; k < kVals; k++) vals[k] = 0.0;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
         const double x = r[3 * s], y = r[3 * s + 1], z = r[3 * s + 2];
         const double vx = v[3 * s], vy = v[3 * s + 1], vz = v[3 * s + 2], ms = m[s];
         if (x >= g.low[0] && y >= g.low[1] && z >= g.low[2] && x <= g.high[0] && y <= g.high[1] && z <= g.high[2]) {
-            vals[0] = dmul(ms, dadd(dadd(dmul(vx, vx), dmul(vy, vy)), dmul(vz, vz)));
-            vals[1] = 1.0;
+            vals[0] = dadd(vals[0], dmul(ms, dadd(dadd(dmul(vx, vx), dmul(vy, vy)), dmul(vz, vz))));
+            vals[1] = dadd(vals[1], 1.0);
         }
-        if (s < n_terms) {
-            vals[2] = vx * vx * ms; vals[3] = vx * vy * ms; vals[4] = vy * vy * ms;
-            vals[5] = vx * vz * ms; vals[6] = vy * vz * ms; vals[7] = vz * vz * ms;
+        if (TERMS && s < n_terms) {
+            vals[2 % kVals] += vx * vx * ms; vals[3 % kVals] += vx * vy * ms; vals[4 % kVals] += vy * vy * ms;
+            vals[5 % kVals] += vx * vz * ms; vals[6 % kVals] += vy * vz * ms; vals[7 % kVals] += vz * vz * ms;
         }
     }
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    for (int k = 0; k < 8; k++) {
+    for (int k = 0; k < kVals; k++) {
         double xk = vals[k];
         for (int o = 16; o > 0; o >>= 1) xk += __shfl_xor_sync(0xffffffffu, xk, o);
         if (lane == 0) s_part[wib][k] = xk;
@@ -1067,7 +1073,7 @@ __global__ void __launch_bounds__(kBlock) k_kinetic(Grid g, int n, int n_terms, 
         int src = -1;
         if (t == R_MV2) src = 0;
         else if (t == R_NBOX) src = 1;
-        else if (t >= R_K0 && t <= R_K5) src = 2 + t - R_K0;
+        else if (TERMS && t >= R_K0 && t <= R_K5) src = 2 + t - R_K0;
         if (src >= 0)
             for (int w = 0; w < kWarpsPerBlock; w++) acc += s_part[w][src];
         partials[(size_t)blockIdx.x * R_NSLOTS + t] = acc;
@@ -1754,7 +1760,7 @@ void launch_step1(Engine &e, cudaStream_t st) {
                                               e.verlet ? e.rebuild : nullptr);
 }
 
-int kinetic_grid(const Engine &e) { return nblk(e.n, kBlock); }
+int kinetic_grid(const Engine &e) { return std::min(nblk(e.n, kBlock), 152 * 2); }
 
 void launch_pair_table(Engine &e, cudaStream_t st) {
     if (!e.tab_x || !e.tab_s || e.tab_n < 2) return;
@@ -1769,7 +1775,8 @@ void launch_velocity_scale(Engine &e, cudaStream_t st, const double *acc, double
 }
 
 void launch_kinetic(Engine &e, cudaStream_t st, int n_terms) {
-    k_kinetic<<<kinetic_grid(e), kBlock, 0, st>>>(e.g, (int)e.n, n_terms, e.r, e.v, e.m, e.partials);
+    if (n_terms > 0) k_kinetic<true><<<kinetic_grid(e), kBlock, 0, st>>>(e.g, (int)e.n, n_terms, e.r, e.v, e.m, e.partials);
+    else k_kinetic<false><<<kinetic_grid(e), kBlock, 0, st>>>(e.g, (int)e.n, 0, e.r, e.v, e.m, e.partials);
 }
 
 void launch_sum_partials(cudaStream_t st, int nblocks, const double *partials, double *out) {
