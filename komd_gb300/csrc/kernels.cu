@@ -603,7 +603,8 @@ __global__ void __launch_bounds__(kBlock) k_atm_q(AtmParams p) {
     const int i = blockIdx.x * kWarpsPerBlock + wib;
     const float rc2 = (float)p.rc2;
     float gx = 0.f, gy = 0.f, gz = 0.f;
-    float m_e = 0.f, m_t = 0.f, m_w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    float m_e = 0.f, m_w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    int m_t = 0;   // triplet visits (each triplet is visited from its three vertices)
     unsigned lt;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
 
@@ -628,7 +629,7 @@ __global__ void __launch_bounds__(kBlock) k_atm_q(AtmParams p) {
         if (MEASURE) {
             const float vC = s5 * (-1.5f * A * B + 0.375f * (-u + v + w) - 0.9375f * P * (wc * wc));
             m_e += s2 * sv * (1.0f + 0.375f * P * s2) * (1.0f / 3.0f);
-            m_t += 1.0f / 3.0f;
+            m_t++;
             float wt;
             if (p.virial_compat) {
                 const int ca = __float_as_int(ea.w), cb = __float_as_int(eb.w);
@@ -728,13 +729,19 @@ __global__ void __launch_bounds__(kBlock) k_atm_q(AtmParams p) {
         }
     }
     if (MEASURE) {
-        double vals[8] = {m_e, m_t, m_w[0], m_w[1], m_w[2], m_w[3], m_w[4], m_w[5]};
+        // FP32 warp tree over the lanes' FP32 partials, FP64 from the warp sums on
+        float vals[8] = {m_e, 0.f, m_w[0], m_w[1], m_w[2], m_w[3], m_w[4], m_w[5]};
         for (int k = 0; k < 8; k++) {
-            double x = vals[k];
+            float x = vals[k];
             for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
             vals[k] = x;
         }
-        if (lane == 0) for (int k = 0; k < 8; k++) s_part[wib][k] = vals[k];
+        int visits = m_t;   // an exact integer count, a third of a triplet per visit
+        for (int o = 16; o > 0; o >>= 1) visits += __shfl_xor_sync(0xffffffffu, visits, o);
+        if (lane == 0) {
+            for (int k = 0; k < 8; k++) s_part[wib][k] = (double)vals[k];
+            s_part[wib][1] = (double)visits / 3.0;
+        }
         __syncthreads();
         if (threadIdx.x < R_NSLOTS) {
             const int t = threadIdx.x;

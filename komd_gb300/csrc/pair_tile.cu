@@ -242,13 +242,16 @@ __global__ void __launch_bounds__(kTileThreads) k_pair_tile(PairParams p) {
         __syncthreads();
     }
     if (MEASURE) {
-        double vals[8] = {m_u, m_w[0], m_w[1], m_w[2], m_w[3], m_w[4], m_w[5], m_pairs};
+        // the lanes' FP32 partials summed over the warp in FP32 (a fixed tree:
+        // GB300's FP64 pipe made an FP64 tree the bulk of this pass), FP64 from
+        // the warp sums on
+        float vals[8] = {m_u, m_w[0], m_w[1], m_w[2], m_w[3], m_w[4], m_w[5], m_pairs};
         for (int k = 0; k < 8; k++) {
-            double x = vals[k];
+            float x = vals[k];
             for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
             vals[k] = x;
         }
-        if (lane == 0) for (int k = 0; k < 8; k++) s_part[w][k] = vals[k];
+        if (lane == 0) for (int k = 0; k < 8; k++) s_part[w][k] = (double)vals[k];
         __syncthreads();
         if (tid < R_NSLOTS) {
             double s = 0.0;
@@ -567,13 +570,16 @@ __global__ void __launch_bounds__(256, U == 3 ? 4 : 5) k_lj_vlist(PairParams p, 
         if (i < n) lj_site<MEASURE, EMIT, UNIFORM, U, false>(p, i, lane, lt, rc2, rc3sq, nullptr, nullptr, m_u, m_pairs, m_w);
     }
     if (MEASURE) {
-        double vals[8] = {m_u, m_w[0], m_w[1], m_w[2], m_w[3], m_w[4], m_w[5], m_pairs};
+        // the lanes' FP32 partials summed over the warp in FP32 (a fixed tree:
+        // GB300's FP64 pipe made an FP64 tree the bulk of this pass), FP64 from
+        // the warp sums on
+        float vals[8] = {m_u, m_w[0], m_w[1], m_w[2], m_w[3], m_w[4], m_w[5], m_pairs};
         for (int k = 0; k < 8; k++) {
-            double x = vals[k];
+            float x = vals[k];
             for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
             vals[k] = x;
         }
-        if (lane == 0) for (int k = 0; k < 8; k++) s_part[w][k] = vals[k];
+        if (lane == 0) for (int k = 0; k < 8; k++) s_part[w][k] = (double)vals[k];
         __syncthreads();
         const int tid = threadIdx.x;
         if (tid < R_NSLOTS) {
@@ -660,8 +666,8 @@ bool vlist_u3(const Engine &e) {
 }
 
 int launch_lj_vlist(Engine &e, PairParams &p, bool measure, bool emit, cudaStream_t st) {
-    // the measure pass keeps one group per block (its partial sums are per block)
-    const int per = measure ? 1 : vlist_per(e);
+    // a block's partial sums cover all its groups (the lanes' sums run across them)
+    const int per = vlist_per(e);
     const int grid = (vlist_grid(e) + per - 1) / per;
     const bool u3 = vlist_u3(e);
     if (e.uniform) lj_vlist_dispatch<true>(p, (int)e.n, grid, per, measure, emit, u3, st);
