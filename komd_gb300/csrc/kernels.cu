@@ -1249,14 +1249,24 @@ __global__ void k_rdf_all(Grid g, int n_mol, const double *__restrict__ com, dou
         if (o != k) rdf_pair(com + 3 * k, com + 3 * o, g, max_r, dr, nbins, bins);
 }
 
-// Sums the per-block partial rows: one warp per slot, fixed lane-to-block
-// mapping and a fixed shuffle tree, so the result is deterministic.
-__global__ void k_sum_partials(int nblocks, const double *__restrict__ partials, double *__restrict__ out) {
-    const int slot = blockIdx.x, lane = threadIdx.x;
+// Sums the per-block partial rows: one block of 256 threads per slot, a fixed
+// thread-to-row mapping, fixed shuffle trees and a fixed order over the
+// warps, so the result is deterministic.
+constexpr int kSumThreads = 256;
+__global__ void __launch_bounds__(kSumThreads) k_sum_partials(int nblocks, const double *__restrict__ partials,
+                                                              double *__restrict__ out) {
+    __shared__ double s_w[kSumThreads / 32];
+    const int slot = blockIdx.x, t = threadIdx.x, lane = t & 31;
     double s = 0.0;
-    for (int b = lane; b < nblocks; b += 32) s += partials[(size_t)b * R_NSLOTS + slot];
+    for (int b = t; b < nblocks; b += kSumThreads) s += partials[(size_t)b * R_NSLOTS + slot];
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) out[slot] += s;
+    if (lane == 0) s_w[t >> 5] = s;
+    __syncthreads();
+    if (t == 0) {
+        double y = 0.0;
+        for (int w = 0; w < kSumThreads / 32; w++) y += s_w[w];
+        out[slot] += y;
+    }
 }
 
 // Tabulated pair force (IBI_ForceFunctor<IBI_Default>::IBI_Force,
@@ -1787,7 +1797,7 @@ void launch_kinetic(Engine &e, cudaStream_t st, int n_terms) {
 }
 
 void launch_sum_partials(cudaStream_t st, int nblocks, const double *partials, double *out) {
-    k_sum_partials<<<R_NSLOTS, 32, 0, st>>>(nblocks, partials, out);
+    k_sum_partials<<<R_NSLOTS, kSumThreads, 0, st>>>(nblocks, partials, out);
 }
 
 void launch_rdf(Engine &e, cudaStream_t st, double *bins, bool cells) {
