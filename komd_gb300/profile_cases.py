@@ -3,12 +3,16 @@
     python -m komd_gb300.profile_cases exact      [--ncell 40] [--steps 3] [--equil 0]
     python -m komd_gb300.profile_cases surrogate  [--ncell 40] [--steps 3]
     python -m komd_gb300.profile_cases replicas   [--count 64] [--steps 2]
+    python -m komd_gb300.profile_cases tabulated  [--ncell 40] [--steps 3]
 
 `exact`: LJ + FULL ATM argon (rho* 0.8442, T* 0.722, rc 2.5 / 2.0, nu* 0.073,
 cell 2.8, skin 0.3), the benchmark's engine configuration.  `surrogate`: the
 same with the learned three-body term on Glorot-initialised weights (kernel
 cost does not depend on the weights).  `replicas`: `count` uneven replicas
-(2000-20000 atoms) advanced by one batched graph.  Each prints its mean step
+(2000-20000 atoms) advanced by one batched graph.  `tabulated`: the IBI
+tabulated pair force (FP64, per-step cells of edge >= 2.5, a 200-node table
+of the LJ force) on the jittered lattice, then one RDF_Profiler sample (100
+bins to 2.5).  Each prints its mean step
 time; the launches before the measured steps are few, so that a profiler can
 skip to them.
 """
@@ -64,9 +68,27 @@ def replicas(count, steps):
         g.close()
 
 
+def tabulated(ncell, steps):
+    s = lattice.argon_fcc(ncell, rho=0.8442, t_star=0.722, seed=3, jitter=0.02)
+    side = float(np.min(s.high - s.low))
+    cell = side / np.floor(side / 2.5)
+    g = gpu.GpuSystem(s, gpu.make_config(s.low, s.high, cell, cutoff=2.5, terms=gpu.TERM_TABULATED,
+                                         precision=gpu.FP64))
+    x = np.linspace(0.6, 2.5, 200)
+    g.set_pair_table(x, 24.0 * (2.0 * x ** -13 - x ** -7), 1e6, 0.0)
+    g.update_container()
+    g.forces()
+    t0 = time.perf_counter()
+    g.step(steps)
+    dt = (time.perf_counter() - t0) / steps
+    g.rdf_profile(2.5, 100)
+    print(f"tabulated n={s.n}: {dt * 1e3:.3f} ms/step (host clock)")
+    g.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["exact", "surrogate", "replicas"])
+    ap.add_argument("case", choices=["exact", "surrogate", "replicas", "tabulated"])
     ap.add_argument("--ncell", type=int, default=40)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--equil", type=int, default=0)
@@ -74,6 +96,8 @@ def main():
     a = ap.parse_args()
     if a.case == "replicas":
         replicas(a.count, a.steps)
+    elif a.case == "tabulated":
+        tabulated(a.ncell, a.steps)
     else:
         exact(a.ncell, a.steps, a.equil, learned=a.case == "surrogate")
 
