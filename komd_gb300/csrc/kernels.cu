@@ -1273,11 +1273,14 @@ __global__ void __launch_bounds__(kSumThreads) k_sum_partials(int nblocks, const
 // plugins/IBI/IBI_ForceFunctor.cpp:18-37, FunctionPL::evaluateAt,
 // plugins/IBI/IBI_Math.h:30-44): for every pair inside the cutoff (no
 // same-molecule exclusion) F = table(r), force = (dr / r) * F on the site.
-// FP64 with the reference's operation order per pair; the upper node is the
-// first node >= r (binary search, the same node the reference's linear scan
-// finds), and slope[k] = (y[k+1] - y[k]) / (x[k+1] - x[k]) is the quotient the
-// reference forms, computed once with the same IEEE operations.  At r == x[0]
-// the reference reads x[-1]; here the first segment is used.
+// FP64: the exact separation and cutoff test, r = sqrt(r^2) and the table
+// value as the reference forms them (the upper node is the first node >= r,
+// by binary search, the node the reference's linear scan finds, and slope[k] =
+// (y[k+1] - y[k]) / (x[k+1] - x[k]) is the reference's quotient, computed once
+// with the same IEEE operations); dr / r as dr * (1 / r), one division per
+// pair instead of three (within an ulp of the reference's quotients; the FP64
+// pipe bounds this kernel).  At r == x[0] the reference reads x[-1]; here the
+// first segment is used.
 __device__ __forceinline__ double table_eval(double x, int n, const double *__restrict__ xs,
                                              const double *__restrict__ ys, const double *__restrict__ slope,
                                              double lo, double hi) {
@@ -1381,9 +1384,10 @@ __global__ void __launch_bounds__(32 * kTabWarps) k_pair_table(
                 if (r2 > rc2) return;
                 const double r = __dsqrt_rn(r2);
                 const double F = table_eval(r, n, xs, ys, slope, lo, hi);
-                fx = dadd(fx, dmul(ddiv(dx, r), F));
-                fy = dadd(fy, dmul(ddiv(dy, r), F));
-                fz = dadd(fz, dmul(ddiv(dz, r), F));
+                const double ir = ddiv(1.0, r);
+                fx = dadd(fx, dmul(dmul(dx, ir), F));
+                fy = dadd(fy, dmul(dmul(dy, ir), F));
+                fz = dadd(fz, dmul(dmul(dz, ir), F));
             };
             int qn = 0;
             for (int c0 = 0; c0 < ns; c0 += 32) {
