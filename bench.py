@@ -353,12 +353,12 @@ def next_rows_leg(args, stream, local):
             g.close()
 
     out = {}
+    xt = np.linspace(0.6, 2.5, 200)   # table nodes; values: the LJ force -dU/dr
     legs = {
         "ibi_tabulated_fp64": lambda: run(
             gpu.make_config(s.low, s.high, autotune.cell_for(side, 2.5), cutoff=2.5, terms=gpu.TERM_TABULATED,
                             precision=gpu.FP64),
-            table=(np.linspace(0.6, 2.5, 200), 24.0 * (2.0 * np.linspace(0.6, 2.5, 200) ** -13
-                                                       - np.linspace(0.6, 2.5, 200) ** -7), 1e6, 0.0)),
+            table=(xt, 24.0 * (2.0 * xt ** -13 - xt ** -7), 1e6, 0.0)),
         "atm2b_fp32_verlet": lambda: run(
             gpu.make_config(s.low, s.high, autotune.cell_for(side, 2.9), cutoff=2.5, nu=w["nu"],
                             terms=gpu.TERM_LJ | gpu.TERM_ATM2B, virial_mode=gpu.VIRIAL_CORRECT, skin=0.4)),

@@ -1062,9 +1062,11 @@ __global__ void __launch_bounds__(kBlock) k_kinetic(Grid g, int n, int n_terms, 
             vals[0] = dadd(vals[0], dmul(ms, dadd(dadd(dmul(vx, vx), dmul(vy, vy)), dmul(vz, vz))));
             vals[1] = dadd(vals[1], 1.0);
         }
-        if (TERMS && s < n_terms) {
-            vals[2 % kVals] += vx * vx * ms; vals[3 % kVals] += vx * vy * ms; vals[4 % kVals] += vy * vy * ms;
-            vals[5 % kVals] += vx * vz * ms; vals[6 % kVals] += vy * vz * ms; vals[7 % kVals] += vz * vz * ms;
+        if constexpr (TERMS) {
+            if (s < n_terms) {
+                vals[2] += vx * vx * ms; vals[3] += vx * vy * ms; vals[4] += vy * vy * ms;
+                vals[5] += vx * vz * ms; vals[6] += vy * vz * ms; vals[7] += vz * vz * ms;
+            }
         }
     }
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
