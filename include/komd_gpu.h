@@ -129,6 +129,13 @@ int  komd_gpu_create(const komd_config *cfg, int device, komd_gpu **out);
 int  komd_gpu_destroy(komd_gpu *h);
 const char *komd_gpu_last_error(void);
 int  komd_gpu_abi_version(void);
+/* TemperatureSensor's conversion (sensors/TemperatureSensor.cpp:44-47, in
+ * math/SciValue.h arithmetic): T in K from sum(m v^2) and the number of sites
+ * in the box.  The same function the device thermostat evaluates inside the
+ * step graph; it returns for every input (NaN and +-inf give a non-finite T,
+ * zero sites give 0) -- unlike the reference's SciValue loop, which never
+ * ends on an infinite mantissa. */
+double komd_sci_temperature(double mv2, double n_in_box);
 /* Runs the engine's work on a caller-provided cudaStream_t (NULL = engine's own). */
 int  komd_gpu_set_stream(komd_gpu *h, void *cuda_stream);
 /* Domain cells per dimension, floor(L / cell_size) (LinkedCells.cpp:19). */
@@ -329,15 +336,20 @@ int  komd_gpu_kernels_per_step(komd_gpu *h);
  * step loop that must not call cudaMalloc/cudaFree because both implicitly
  * synchronise the device.  r (n*3 doubles) and f (n*3 doubles, overwritten)
  * are device-accessible pointers; the neighbour list the kernels need lives
- * in a fixed static device array inside the library (about 6.3 MB, held on
- * every GPU that loads the library until the process exits), so this call
- * allocates nothing.  Limits: n <= KOMD_NOALLOC_MAX_SITES and at most
+ * in a fixed static device array inside the library (about 6.3 MB), so this
+ * call allocates nothing.  CUDA loads the library's module lazily, so the
+ * array is reserved on a device by the first call there (or at context
+ * creation under CUDA_MODULE_LOADING=EAGER) and held until the process exits:
+ * make that first call before the host application reserves the rest of the
+ * device.  Limits: n <= KOMD_NOALLOC_MAX_SITES and at most
  * KOMD_NOALLOC_NL_CAP neighbours inside cutoff_3b per site (KOMD_ERR_ARG /
- * KOMD_ERR_OVERFLOW otherwise); every box edge >= 2 * cutoff_3b.  The first
- * call on a device resolves the array's device address (set-up) and should
- * come before any stream capture on that device.  All calls share the one
- * array: calls whose GPU work overlaps race and must be serialised by the
- * caller.  Synchronous on cuda_stream (NULL = legacy default stream). */
+ * KOMD_ERR_OVERFLOW otherwise; after KOMD_ERR_OVERFLOW f is undefined);
+ * every box edge >= 2 * cutoff_3b; atm_sign is KOMD_ATM_SIGN_REFERENCE or
+ * KOMD_ATM_SIGN_PHYSICAL (KOMD_ERR_ARG otherwise).  The first call on a
+ * device also resolves the array's device address (set-up) and should come
+ * before any stream capture on that device.  All calls share the one array:
+ * calls whose GPU work overlaps race and must be serialised by the caller.
+ * Synchronous on cuda_stream (NULL = legacy default stream). */
 #define KOMD_NOALLOC_MAX_SITES 4096
 #define KOMD_NOALLOC_NL_CAP 96
 int  komd_gpu_atm_forces_noalloc(int64_t n, const double *r, double *f, const double domain_low[3],

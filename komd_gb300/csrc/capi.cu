@@ -185,6 +185,7 @@ SurParams sur_params(komd_gpu *h) {
     p.w1 = u.w1; p.w1t = u.w1t; p.w2 = u.w2; p.w2t = u.w2t;
     p.b1 = u.b1; p.b2 = u.b2; p.w3 = u.w3;
     p.b3 = u.b3; p.e_scale = u.e_scale; p.e_shift = u.e_shift;
+    p.num_sms = e.num_sms;
     return p;
 }
 
@@ -395,6 +396,8 @@ extern "C" {
 const char *komd_gpu_last_error(void) { return g_last_error.c_str(); }
 int komd_gpu_abi_version(void) { return KOMD_GPU_ABI_VERSION; }
 
+double komd_sci_temperature(double mv2, double n_in_box) { return temperature_from(mv2, n_in_box); }
+
 int komd_gpu_create(const komd_config *cfg, int device, komd_gpu **out) {
     if (!out) return fail(KOMD_ERR_ARG, "null output handle");
     *out = nullptr;
@@ -410,6 +413,11 @@ int komd_gpu_create(const komd_config *cfg, int device, komd_gpu **out) {
     if (!(e.cfg.max_sigma > 0)) e.cfg.max_sigma = 1.0;
     e.g = g;
     e.device = device;
+    {
+        int sms = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) == cudaSuccess && sms > 0)
+            e.num_sms = sms;
+    }
     {
         int pa = 0, pt = 0;
         cudaDeviceGetAttribute(&pa, cudaDevAttrPageableMemoryAccess, device);

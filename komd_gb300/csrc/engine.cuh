@@ -166,18 +166,26 @@ struct AtmParams {
 // repeated /10 and *10, converted as m * 10^e.  10^e is exact for 0 <= e <= 22
 // and 1 / 10^-e (one correctly rounded division) below; host and device
 // evaluate the same IEEE operations, so both give the same temperature.
+// The device thermostat runs this inside the step graph, so both loops are
+// bounded: zero, NaN and +-inf come back unchanged at once (inf / 10 stays
+// inf, and the reference's unbounded loop would never end on it), and no
+// finite double needs more than 400 steps (about 10^308 to 10^-324).
+constexpr int kSciMaxSteps = 400;
 struct SciNum { double m; int e; };
 __host__ __device__ inline SciNum sci_norm(double m, int e) {
     double a = fabs(m);
-    while (a >= 10.0) { m = m / 10.0; e += 1; a = fabs(m); }
-    while (a <= 0.1 && a > 0.0) { m = m * 10.0; e -= 1; a = fabs(m); }
+    if (!(a <= 1.7976931348623157e308) || a == 0.0) return {m, e};   // NaN, +-inf or zero
+    for (int k = 0; k < kSciMaxSteps && a >= 10.0; k++) { m = m / 10.0; e += 1; a = fabs(m); }
+    for (int k = 0; k < kSciMaxSteps && a <= 0.1; k++) { m = m * 10.0; e -= 1; a = fabs(m); }
     return {m, e};
 }
 __host__ __device__ inline double sci_pow10(int e) {
     double p = 1.0;
     const int k = e < 0 ? -e : e;
     for (int i = 0; i < k && i < 22; i++) p = p * 10.0;
-    for (int i = 22; i < k; i++) p = p * 10.0;   // beyond 1e22 no longer exact (not reached here)
+    // beyond 1e22 no longer exact (not reached by finite temperatures); past
+    // 1e309 the product is inf already, so the loop stops there
+    for (int i = 22; i < k && i < 330; i++) p = p * 10.0;
     return e < 0 ? 1.0 / p : p;
 }
 __host__ __device__ inline double sci_temperature(double mv2, double n_in_box) {
@@ -196,6 +204,7 @@ struct Engine {
     komd_config cfg;
     Grid g;
     int device = 0;
+    int num_sms = 152;        // multiprocessors of the device, queried at creation (sizes resident grids)
     cudaStream_t stream = nullptr;
     bool own_stream = false;
 

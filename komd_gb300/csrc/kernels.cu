@@ -1432,15 +1432,22 @@ __global__ void __launch_bounds__(32 * kTabWarps) k_pair_table(
 
 // VelocityScaling (VelocityScaling.cpp:12-25): v *= beta; beta from the
 // caller, or (acc != nullptr) sqrt(T_target / T) with T from the summed
-// kinetic slots as TemperatureSensor computes it
+// kinetic slots as TemperatureSensor computes it.  A non-finite T (an
+// overflowed force upstream) leaves v unscaled and raises E_NONFINITE, which
+// the host reads after the step.
 __global__ void k_velocity_scale(int n, double *__restrict__ v, const double *__restrict__ acc, double t_target,
-                                 double beta_in) {
+                                 double beta_in, int *__restrict__ err) {
     __shared__ double s_beta;
     if (threadIdx.x == 0) {
         double beta = beta_in;
         if (acc) {
             const double t = sci_temperature(acc[R_MV2], acc[R_NBOX]);
-            beta = t > 0.0 ? __dsqrt_rn(__ddiv_rn(t_target, t)) : 1.0;
+            if (!isfinite(t)) {
+                beta = 1.0;
+                if (blockIdx.x == 0 && err) atomicOr(&err[E_NONFINITE], 1);
+            } else {
+                beta = t > 0.0 ? __dsqrt_rn(__ddiv_rn(t_target, t)) : 1.0;
+            }
         }
         s_beta = beta;
     }
@@ -1461,7 +1468,7 @@ void launch_container(Engine &e, cudaStream_t st) {
     // the per-cell counts are zero here: zeroed at allocation, and by the scan
     // of every binning after reading them
     // grid-stride kernels on a resident grid: steps without a rebuild launch few blocks
-    const int res = 152 * 8;
+    const int res = e.num_sms * 8;
     k_com_wrap_bin<<<std::min(nblk(e.n_mol, 256), res), 256, 0, st>>>(g, (int)e.n_mol, e.mol_off, e.r, e.m, e.com, e.mol_cell,
                                                          e.mol_rank, e.cell_count, e.cell_mcount,
                                                          e.verlet ? e.bias : nullptr, rb, e.exact_com,
@@ -1783,7 +1790,7 @@ void launch_step1(Engine &e, cudaStream_t st) {
                                               e.verlet ? e.rebuild : nullptr);
 }
 
-int kinetic_grid(const Engine &e) { return std::min(nblk(e.n, kBlock), 152 * 2); }
+int kinetic_grid(const Engine &e) { return std::min(nblk(e.n, kBlock), e.num_sms * 2); }
 
 void launch_pair_table(Engine &e, cudaStream_t st) {
     if (!e.tab_x || !e.tab_s || e.tab_n < 2) return;
@@ -1793,8 +1800,8 @@ void launch_pair_table(Engine &e, cudaStream_t st) {
 }
 
 void launch_velocity_scale(Engine &e, cudaStream_t st, const double *acc, double beta) {
-    const int blocks = std::min(nblk(3 * e.n, 256), 152 * 8);
-    k_velocity_scale<<<blocks, 256, 0, st>>>((int)e.n, e.v, acc, e.cfg.temperature_target, beta);
+    const int blocks = std::min(nblk(3 * e.n, 256), e.num_sms * 8);
+    k_velocity_scale<<<blocks, 256, 0, st>>>((int)e.n, e.v, acc, e.cfg.temperature_target, beta, e.err);
 }
 
 void launch_kinetic(Engine &e, cudaStream_t st, int n_terms) {

@@ -10,8 +10,13 @@
 //
 // Scratch: the per-site neighbour list inside cutoff_3b, the per-site counts
 // and an overflow flag, in one file-scope __device__ array of fixed size
-// (KOMD_NOALLOC_MAX_SITES x KOMD_NOALLOC_NL_CAP entries, about 6.3 MB).  Every
-// GPU that loads this library holds that array until the process exits.
+// (KOMD_NOALLOC_MAX_SITES x KOMD_NOALLOC_NL_CAP entries, about 6.3 MB).  The
+// array is device memory of this library's module: CUDA loads modules lazily
+// by default (CUDA_MODULE_LOADING=LAZY), so the array is reserved on a device
+// when this module is first used there -- by the first call of the entry
+// point on that device -- and held until the process exits.  A caller whose
+// host application later reserves the rest of the device must therefore make
+// its first call (or run with CUDA_MODULE_LOADING=EAGER) before that.
 //
 // Host code never uses the array's name as an address (on the host it is
 // only a stand-in symbol): the first call on each device resolves the device
@@ -24,7 +29,8 @@
 // rewritten in full and the overflow flag is cleared at the start of every
 // call.  Calls whose GPU work overlaps (concurrent streams, or threads
 // driving the same device) race on the array and must be serialised by the
-// caller.
+// caller.  After KOMD_ERR_OVERFLOW the forces in f are undefined (they come
+// from a truncated neighbour list); the next call starts clean.
 #include <cstdint>
 #include <mutex>
 #include <string>
@@ -181,6 +187,8 @@ extern "C" int komd_gpu_atm_forces_noalloc(int64_t n, const double *r, double *f
         return fail(KOMD_ERR_ARG, "komd_gpu_atm_forces_noalloc handles at most " + std::to_string(kMaxSites) +
                                       " sites (its scratch is a fixed static array); got " + std::to_string(n));
     if (!(cutoff_3b > 0)) return fail(KOMD_ERR_ARG, "cutoff_3b must be > 0");
+    if (atm_sign != KOMD_ATM_SIGN_REFERENCE && atm_sign != KOMD_ATM_SIGN_PHYSICAL)
+        return fail(KOMD_ERR_ARG, "atm_sign must be KOMD_ATM_SIGN_REFERENCE or KOMD_ATM_SIGN_PHYSICAL");
     Box b;
     for (int d = 0; d < 3; d++) {
         b.low[d] = domain_low[d];

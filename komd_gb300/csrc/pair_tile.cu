@@ -627,14 +627,14 @@ int vlist_grid(const Engine &e) { return (int)((e.n + 7) / 8); }
 // blocks (5 per SM), each over a contiguous range of slots
 int vlist_per(const Engine &e) {
     const int groups = vlist_grid(e);
-    const int target = 152 * 5 * 8;
+    const int target = e.num_sms * 5 * 8;
     return groups <= target ? 1 : (groups + target - 1) / target;
 }
 
 void launch_vlist_build(Engine &e, cudaStream_t st) {
     PairParams p = pair_params(e);
     // a resident grid (12 blocks of 4 warps per SM at this kernel's register count)
-    const int blocks = std::min((e.g.ncell + kVbWarps - 1) / kVbWarps, 152 * 12);
+    const int blocks = std::min((e.g.ncell + kVbWarps - 1) / kVbWarps, e.num_sms * 12);
     // the two-home form pays off once many cells hold more than 32 sites
     const double per_cell = (double)e.n / ((double)e.g.nd[0] * e.g.nd[1] * e.g.nd[2]);
     if (per_cell > 26.0) k_vlist_build<true><<<blocks, 32 * kVbWarps, 0, st>>>(p);

@@ -492,7 +492,8 @@ void launch_sur_desc(SurParams &p, cudaStream_t st) { k_sur_desc<<<(p.n + 127) /
 void launch_sur_mlp(SurParams &p, cudaStream_t st) {
     const int tiles = (p.n + 15) / 16;
     int blocks = (tiles + 3) / 4;
-    if (blocks > 152 * 4) blocks = 152 * 4;   // persistent: weights staged once per block
+    const int cap = 4 * (p.num_sms > 0 ? p.num_sms : 152);
+    if (blocks > cap) blocks = cap;   // persistent: weights staged once per block
     k_sur_mlp<<<blocks, 128, 0, st>>>(p);
 }
 void launch_sur_force(SurParams &p, cudaStream_t st) { k_sur_force<<<(p.n + 127) / 128, 128, 0, st>>>(p); }

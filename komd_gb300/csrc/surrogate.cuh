@@ -29,6 +29,7 @@ struct SurParams {
     const __nv_bfloat16 *w1, *w1t, *w2, *w2t;
     const float *b1, *b2, *w3;
     float b3, e_scale, e_shift;
+    int num_sms;                 // multiprocessors of the device (persistent MLP grid)
 };
 
 struct TrainParams {

@@ -29,6 +29,7 @@ MEASURE_TEMPERATURE, MEASURE_ENERGY, MEASURE_PRESSURE, MEASURE_RDF, MEASURE_LJ_H
 
 EXPORTS = [
     "komd_gpu_create", "komd_gpu_destroy", "komd_gpu_last_error", "komd_gpu_abi_version", "komd_gpu_set_stream",
+    "komd_sci_temperature",
     "komd_gpu_grid_dims", "komd_gpu_upload_sites", "komd_gpu_set_state", "komd_gpu_set_topology",
     "komd_gpu_download", "komd_gpu_num_sites", "komd_gpu_update_container", "komd_gpu_forces",
     "komd_gpu_integrate0", "komd_gpu_integrate1", "komd_gpu_step", "komd_gpu_step_host", "komd_gpu_measure",
@@ -98,6 +99,8 @@ def load() -> C.CDLL:
     L.komd_gpu_create.argtypes = [C.POINTER(KomdConfig), I32, C.POINTER(P)]
     L.komd_gpu_destroy.argtypes = [P]
     L.komd_gpu_last_error.restype = C.c_char_p
+    L.komd_sci_temperature.argtypes = [C.c_double, C.c_double]
+    L.komd_sci_temperature.restype = C.c_double
     L.komd_gpu_set_stream.argtypes = [P, P]
     L.komd_gpu_grid_dims.argtypes = [P, P]
     L.komd_gpu_upload_sites.argtypes = [P, I64, P, P, P, P, P, P]

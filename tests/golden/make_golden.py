@@ -11,7 +11,7 @@ compressed .npz files together with the inputs that produced them.
 
 Run from the repo root in a container where the reference is present:
 
-    make -C oracle/ref -j8 && python tests/golden/make_golden.py [case ...]
+    make -C oracle/ref REF=<KoMD checkout> -j8 && python tests/golden/make_golden.py [case ...]
 
 The fixtures are then read by the tests without the reference.
 """

@@ -75,3 +75,52 @@ def test_noalloc_rejects_oversized_input():
                                          high.ctypes.data_as(ctypes.c_void_p), 2.0, 0.073, 1, None)
     assert rc == 1
     assert b"at most 4096 sites" in lib.komd_gpu_last_error()
+
+
+def test_noalloc_rejects_bad_sign():
+    from komd_gb300 import gpu
+    lib = gpu.load()
+    low = np.zeros(3)
+    high = np.full(3, 10.0)
+    dummy = ctypes.c_void_p(1)     # never dereferenced: the argument checks come first
+    for bad in (2, -1, 7):
+        rc = lib.komd_gpu_atm_forces_noalloc(100, dummy, dummy, low.ctypes.data_as(ctypes.c_void_p),
+                                             high.ctypes.data_as(ctypes.c_void_p), 2.0, 0.073, bad, None)
+        assert rc == 1
+        assert b"atm_sign" in lib.komd_gpu_last_error()
+
+
+def test_noalloc_overflow_then_clean_call():
+    """A packed system exceeds the fixed neighbour capacity: the call reports
+    KOMD_ERR_OVERFLOW (its forces are undefined), and the next, normal call
+    on the shared scratch clears the flag and matches the regular entry point."""
+    import torch
+    from komd_gb300 import gpu, lattice
+    lib = gpu.load()
+    # 7^3 = 343 sites on a simple-cubic grid of spacing 4/7 in a box of edge 4.0
+    # (= 2 * cutoff_3b): about 140 neighbours inside 2.0 per site, over the 96 of the scratch
+    g = (np.arange(7) + 0.5) * (4.0 / 7.0)
+    dense = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    r_dense = torch.tensor(dense, dtype=torch.float64, device="cuda")
+    f_dense = torch.zeros_like(r_dense)
+    low = np.zeros(3)
+    high = np.full(3, 4.0)
+    stream = torch.cuda.current_stream().cuda_stream
+    rc = lib.komd_gpu_atm_forces_noalloc(len(dense), ctypes.c_void_p(r_dense.data_ptr()),
+                                         ctypes.c_void_p(f_dense.data_ptr()), low.ctypes.data_as(ctypes.c_void_p),
+                                         high.ctypes.data_as(ctypes.c_void_p), 2.0, 0.073, gpu.ATM_SIGN_PHYSICAL,
+                                         ctypes.c_void_p(stream))
+    assert rc == 3, lib.komd_gpu_last_error().decode()
+    assert b"neighbours" in lib.komd_gpu_last_error()
+    s = lattice.argon_fcc(6, rho=0.8442, t_star=0.722, seed=33, jitter=0.06)
+    r_wrapped, f_ref = _regular_forces(s, gpu.ATM_SIGN_PHYSICAL)
+    r_dev = torch.tensor(r_wrapped, dtype=torch.float64, device="cuda")
+    f_dev = torch.full((s.n, 3), float("nan"), dtype=torch.float64, device="cuda")
+    lo = np.ascontiguousarray(s.low, np.float64)
+    hi = np.ascontiguousarray(s.high, np.float64)
+    rc = lib.komd_gpu_atm_forces_noalloc(s.n, ctypes.c_void_p(r_dev.data_ptr()), ctypes.c_void_p(f_dev.data_ptr()),
+                                         lo.ctypes.data_as(ctypes.c_void_p), hi.ctypes.data_as(ctypes.c_void_p),
+                                         2.0, 0.073, gpu.ATM_SIGN_PHYSICAL, ctypes.c_void_p(stream))
+    assert rc == 0, lib.komd_gpu_last_error().decode()
+    err = rel_rmse(f_dev.cpu().numpy(), f_ref)
+    assert err < FP32_FORCE_RMSE, f"rel RMSE {err:.3e}"
