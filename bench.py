@@ -2,13 +2,14 @@
 
 Workload (default): LJ + Axilrod-Teller-Muto argon, 256,000 atoms on an FCC
 lattice (40^3 unit cells) at rho* = 0.8442, T* = 0.722 (seeded Maxwell-
-Boltzmann, zero momentum), LJ cutoff 2.5, ATM cutoff 2.0, nu* = 0.073, cell
-edge >= 2.8 (23^3 cells), Verlet skin 0.3, dt* = 0.005.  One step = one full
-velocity-Verlet MD step: integrate0 (with the skin test), COM/wrap, binning
-and neighbour-list build when the skin test fired, LJ from the list (which
-also writes the ATM neighbour list), ATM triplet kernel, integrate1.  Forces are
-FP32 arithmetic, integration and reductions FP64, the ATM term is the FULL
-triplet set with F = -grad V (the physical form).
+Boltzmann, zero momentum), LJ cutoff 2.5, ATM cutoff 2.0, nu* = 0.073,
+dt* = 0.005, 400 equilibration steps; the Verlet skin and the cell edge come
+from the autotuner (skin 0.4, 23^3 cells of 2.921 in recent runs).  One step =
+one full velocity-Verlet MD step: integrate0 (with the skin test), COM/wrap,
+binning and the neighbour-list build when the skin test fired, the half-list
+LJ + ATM pass (each pair and each triplet once), the fixed-point flush with
+integrate1.  Forces are FP32 arithmetic, integration and reductions FP64, the
+ATM term is the FULL triplet set with F = -grad V (the physical form).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -190,8 +191,29 @@ def cpu_baseline(w, seed, budget_s=25.0, threads=None):
         if time.perf_counter() - t0 > budget_s or steps >= 50:
             break
     dt = time.perf_counter() - t0
-    return {"value": s.n * steps / dt, "unit": UNIT, "cores": pyoracle.num_threads(), "kind": "port",
-            "sample": f"{steps} full MD step(s) of the {s.n}-atom system ({dt:.1f} s), oracle/komd_oracle.c (OpenMP)"}
+    out = {"value": s.n * steps / dt, "unit": UNIT, "cores": pyoracle.num_threads(), "kind": "port",
+           "sample": f"{steps} full MD step(s) of the {s.n}-atom system ({dt:.1f} s), oracle/komd_oracle.c (OpenMP)"}
+    cal = reference_calibration()
+    if cal:
+        out["calibration"] = cal
+    return out
+
+
+def reference_calibration():
+    """The port's speed against the reference's own OpenMP stock main, timed on
+    the same host cores where the reference builds (oracle/ref/calibrate_cpu.py,
+    committed as oracle/ref/cpu_calibration.json): the port is that many times
+    faster than the reference, so a ratio against the port understates the
+    ratio against the reference by the same factor."""
+    path = os.path.join(ROOT, "oracle", "ref", "cpu_calibration.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as fh:
+        c = json.load(fh)
+    return {"port_over_reference": c["port_over_reference"], "workload": c["workload"], "threads": c["threads"],
+            "host": c["host"], "reference_atom_steps_per_s": c["reference_atom_steps_per_s"],
+            "port_atom_steps_per_s": c["port_atom_steps_per_s"], "reference_build": c["reference_build"],
+            "source": "oracle/ref/cpu_calibration.json (oracle/ref/calibrate_cpu.py)"}
 
 
 def run_reference(args, w, name):
@@ -208,7 +230,7 @@ def run_reference(args, w, name):
                        "sites": 4 * w["ncell"] ** 3},
             "impl": "reference",
             "cpu_baseline": {"value": cb["value"], "unit": UNIT, "cores": cb["cores"], "kind": cb["kind"],
-                             "sample": cb["sample"]},
+                             "sample": cb["sample"], "calibration": cb.get("calibration")},
             "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -310,7 +332,9 @@ def replicas_leg(args, stream, local):
 
 def next_rows_leg(args, stream, local):
     """The rows on either side of the hot path, on the 256k argon lattice
-    (jittered FCC 40^3): steps with the IBI tabulated pair force (IBI_ForceFunctor,
+    (jittered FCC 40^3): the LJ + ATM step with FP64 pair and triplet arithmetic
+    (the precision of the reference's CPU path; per-step cells), steps with the
+    IBI tabulated pair force (IBI_ForceFunctor,
     FP64 on per-step cells, a 200-node table of the LJ force), one RDF_Profiler
     sample (komd_gpu_rdf_profile, 100 bins to 2.5), ATM2B (the LJ force scaled by
     the two-body ATM factor, FP32 on the Verlet list) and the LJ + ATM step with
@@ -362,6 +386,10 @@ def next_rows_leg(args, stream, local):
         "atm2b_fp32_verlet": lambda: run(
             gpu.make_config(s.low, s.high, autotune.cell_for(side, 2.9), cutoff=2.5, nu=w["nu"],
                             terms=gpu.TERM_LJ | gpu.TERM_ATM2B, virial_mode=gpu.VIRIAL_CORRECT, skin=0.4)),
+        "lj_atm_fp64_forces": lambda: run(
+            gpu.make_config(s.low, s.high, autotune.cell_for(side, 2.5), cutoff=2.5, cutoff_3b=2.0, nu=w["nu"],
+                            terms=gpu.TERM_LJ | gpu.TERM_ATM, precision=gpu.FP64, atm_sign=gpu.ATM_SIGN_PHYSICAL,
+                            atm_enum=gpu.ATM_ENUM_FULL, virial_mode=gpu.VIRIAL_CORRECT)),
         "lj_atm_thermostat": lambda: run(
             gpu.make_config(s.low, s.high, autotune.cell_for(side, 2.9), cutoff=2.5, cutoff_3b=2.0, nu=w["nu"],
                             terms=gpu.TERM_LJ | gpu.TERM_ATM, atm_sign=gpu.ATM_SIGN_PHYSICAL,
@@ -656,12 +684,13 @@ def run_ours(args, w, name):
                        "cell_edge": tuned["best"]["cell"] if tuned else w["cell"],
                        "autotune": tuned,
                        "triplets_per_step": triplets, "parallelism": f"replicas x{world}",
-                       "l2": "no flush: inputs larger than L2 -- the Verlet list alone (about 88 MB at 256k) is "
-                             "read every step, and the dominant kernel moves about 121 MB of DRAM traffic per launch"},
+                       "l2": "no flush: inputs larger than L2 -- the Verlet list (about 88 MB at 256k, of which "
+                             "the half-list force pass reads the 44 MB front regions) is read every step, and the "
+                             "dominant kernel moves about 77 MB of DRAM traffic per launch"},
             "gpu_launches": kernels, "list_rebuilds_timed": rebuilds_timed,
             "events_ms_per_step": events_ms / args.steps,
             "kernel_ms": {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()},
-            "roofline": roof, "peak_kind": peak_kind, "traffic_note": "traffic from the committed ncu capture (profiles/traffic.json), lattice state, per launch",
+            "roofline": roof, "peak_kind": peak_kind, "traffic_note": "traffic from the committed ncu capture (profiles/traffic.json) of one launch on the equilibrated benchmark state",
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * s.n * 24, "d2h_bytes_per_step": 3 * s.n * 24},
             "clocks": clk.summary(),
             "energy": {"u_lj_per_atom": obs0["u_lj"] / s.n, "u_atm_per_atom": obs0["u_atm"] / s.n}}

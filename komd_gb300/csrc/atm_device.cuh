@@ -7,9 +7,11 @@
 namespace komd {
 
 // FP32 ATM, FULL triplet set, forces only: every triplet once, from its
-// lowest slot i (the other two members are neighbours of i with larger
-// slots).  One warp per vertex; lane a owns staged neighbour a (a < m, the
-// neighbours above i) and evaluates the round-robin pairs (a, a+d mod m),
+// lowest member i in a total order on the sites (the slot order in k_atm_s;
+// the Verlet rows' order vl_above in the half-list pass), the other two
+// members being neighbours of i above it.  One warp per vertex; lane a owns
+// staged neighbour a (a < m, the neighbours above i) and evaluates the
+// round-robin pairs (a, a+d mod m),
 // d = 1 .. m/2, directly.  Per triplet with A = |e_a|^2, B = |e_b|^2,
 // C = |e_b - e_a|^2 (e = r_i - r_x) and v_X = dV/dX / nu, the forces in units
 // of 2 sign nu are
@@ -114,9 +116,11 @@ __device__ __forceinline__ void atm_sweep(const float4 *se, const float4 *sq, in
 }
 
 // vertices with more than 32 neighbours above them: a plain pair loop with a
-// fixed-point atomic per contribution (rare at liquid densities)
+// fixed-point atomic per contribution (rare at liquid densities); each
+// contribution is scaled by sc first (1 keeps the units of 2 sign nu, and
+// multiplying by 1 is exact)
 __device__ __forceinline__ void atm_pairs_slow(const AtmParams &p, const float4 *se, const float4 *sq, int m, int lane, float rc2,
-                               float &gx, float &gy, float &gz) {
+                               float &gx, float &gy, float &gz, float sc = 1.0f) {
     for (int a = lane; a < m; a += 32) {
         const float4 ea = se[a], qa = sq[a];
         unsigned long long *acca = p.acc + 3 * (size_t)(__float_as_int(ea.w) >> 6);
@@ -130,12 +134,12 @@ __device__ __forceinline__ void atm_pairs_slow(const AtmParams &p, const float4 
             gy += t.vA * ea.y + t.vB * eb.y;
             gz += t.vA * ea.z + t.vB * eb.z;
             unsigned long long *accb = p.acc + 3 * (size_t)(__float_as_int(eb.w) >> 6);
-            atm_fix_add(acca, t.vC * cx - t.vA * ea.x);
-            atm_fix_add(acca + 1, t.vC * cy - t.vA * ea.y);
-            atm_fix_add(acca + 2, t.vC * cz - t.vA * ea.z);
-            atm_fix_add(accb, -t.vC * cx - t.vB * eb.x);
-            atm_fix_add(accb + 1, -t.vC * cy - t.vB * eb.y);
-            atm_fix_add(accb + 2, -t.vC * cz - t.vB * eb.z);
+            atm_fix_add(acca, sc * (t.vC * cx - t.vA * ea.x));
+            atm_fix_add(acca + 1, sc * (t.vC * cy - t.vA * ea.y));
+            atm_fix_add(acca + 2, sc * (t.vC * cz - t.vA * ea.z));
+            atm_fix_add(accb, sc * (-t.vC * cx - t.vB * eb.x));
+            atm_fix_add(accb + 1, sc * (-t.vC * cy - t.vB * eb.y));
+            atm_fix_add(accb + 2, sc * (-t.vC * cz - t.vB * eb.z));
         }
     }
 }
@@ -188,6 +192,44 @@ __device__ __forceinline__ void atm_vertex(const AtmParams &p, int i, const floa
         gz += __shfl_xor_sync(0xffffffffu, gz, o);
     }
     if (lane == 0) atm_vertex_out(p, i, gx, gy, gz);
+}
+
+// the sweep of atm_vertex without its accumulator traffic, for the half-list
+// pass that adds each neighbour's LJ reaction to its share before one
+// fixed-point add per (vertex, neighbour): with m <= 32, lane li < m returns
+// its neighbour's summed share in (ax, ay, az) and minus it in (gx, gy, gz)
+// (the vertex's share is minus the neighbours' total); other lanes return
+// zeros.  With m > 32 the plain pair loop adds every share, scaled by sc, to
+// the accumulators itself, returns ax = ay = az = 0 and the lane's part of
+// the vertex share in (gx, gy, gz).  Units: 2 sign nu.
+__device__ __forceinline__ void atm_vertex_shares(const AtmParams &p, const float4 *se, const float4 *sq, int m, int lane,
+                                                  float rc2, float sc, float &ax, float &ay, float &az, float &gx,
+                                                  float &gy, float &gz) {
+    ax = ay = az = gx = gy = gz = 0.f;
+    const int half = m / 2;
+    if (m <= 32) {
+        float4 ea;
+        if (m <= 16) {
+            const int g = lane >> 4, li = lane & 15;
+            const int h1 = (half + 1) / 2;                     // rounds of the lower half-warp
+            const int d_first = g ? h1 + 1 : 1, d_last = g ? half : h1;
+            atm_sweep(se, sq, m, li, 16 * g, d_first, d_last, h1, rc2, ax, ay, az, ea);
+            ax += __shfl_xor_sync(0xffffffffu, ax, 16);
+            ay += __shfl_xor_sync(0xffffffffu, ay, 16);
+            az += __shfl_xor_sync(0xffffffffu, az, 16);
+        } else {
+            atm_sweep(se, sq, m, lane, 0, 1, half, half, rc2, ax, ay, az, ea);
+        }
+        if (lane < m) {
+            gx = -ax;
+            gy = -ay;
+            gz = -az;
+        } else {
+            ax = ay = az = 0.f;
+        }
+    } else {
+        atm_pairs_slow(p, se, sq, m, lane, rc2, gx, gy, gz, sc);
+    }
 }
 
 }  // namespace komd

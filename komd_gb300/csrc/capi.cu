@@ -254,7 +254,7 @@ bool enqueue_forces(komd_gpu *h, bool measure, double *lj_hist, bool with_step1 
     } else if (e.cfg.terms & KOMD_TERM_ATM) {
         {
             ProfScope ps(h, F_ATM);
-            fused = lj_atm ? launch_atm_flush(e, st, with_step1) : launch_atm(e, st, measure, with_step1);
+            fused = lj_atm ? launch_atm_flush(e, st, with_step1, lj_atm_half(e)) : launch_atm(e, st, measure, with_step1);
         }
         if (measure) launch_sum_partials(st, atm_grid(e), e.partials, h->acc);
     }
@@ -329,6 +329,7 @@ int alloc_verlet(komd_gpu *h, int cap) {
     CK(dalloc(e.bias, 3 * (size_t)e.n));
     CK(dalloc(e.ref4, e.n));
     CK(dalloc(e.slot_cell, e.n));
+    CK(dalloc(e.zkey, e.n));
     CK(dalloc(e.vl, (size_t)cap * (size_t)e.n));
     CK(dalloc(e.vl_count, e.n));
     if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
@@ -516,7 +517,7 @@ int komd_gpu_destroy(komd_gpu *h) {
     dfree(e.nl); dfree(e.nl_count); dfree(e.bonds); dfree(e.angles); dfree(e.partials); dfree(e.err);
     dfree(e.tab_x); dfree(e.tab_y); dfree(e.tab_s); dfree(e.atm_acc);
     dfree(e.rdf); dfree(e.lj_hist); dfree(e.counts); dfree(h->f_scratch); dfree(h->prof); dfree(h->acc); dfree(h->thermo_acc); dfree(e.offtab);
-    dfree(e.nboff); dfree(e.vb_next); dfree(e.rebuild); dfree(e.bias); dfree(e.ref4); dfree(e.slot_cell); dfree(e.vl); dfree(e.vl_count);
+    dfree(e.nboff); dfree(e.vb_next); dfree(e.rebuild); dfree(e.bias); dfree(e.ref4); dfree(e.slot_cell); dfree(e.zkey); dfree(e.vl); dfree(e.vl_count);
     dfree(e.rebuild_count); dfree(e.hdtm); dfree(e.exact_com);
     {
         Surrogate &u = h->sur;

@@ -104,6 +104,24 @@ __host__ __device__ inline int atm_code(int nb, bool crosses, int slot) {
 }
 constexpr int kMaxAtmSlot = (1 << 25) - 1;
 
+// The order in which the Verlet rows put a site's neighbours "above" it (the
+// front region that the half-list pass reads): j is above i when j's z at the
+// last rebuild, quantized to kZq levels over the box and compared by minimum
+// image, is larger, or equal with a larger slot.  Every neighbour pair thus
+// has one owner, and so does every triplet (its lowest member): on integer
+// keys the relation is exactly antisymmetric, and for mutual neighbours
+// (offsets far below half the box) exactly transitive.  Against the slot
+// order it halves each site's neighbourhood by a plane, which balances the
+// owned triplets per site (the slot order gives the first sites of a cell
+// the most).
+constexpr int kZq = 1 << 24;
+__host__ __device__ inline bool vl_above(int zi, int zj, unsigned si, unsigned sj) {
+    int d = zj - zi;
+    if (d > kZq / 2) d -= kZq;
+    else if (d < -kZq / 2) d += kZq;
+    return d > 0 || (d == 0 && sj > si);
+}
+
 struct PairParams {
     Grid g;
     const int *cell_start;     // C+1
@@ -136,6 +154,7 @@ struct PairParams {
     int vl_cap;
     double rl2;                // (cutoff + skin)^2
     const int *slot_cell;
+    const int *zkey;           // per slot: quantized z at the last rebuild (the half-list order)
     int *vb_next;              // Verlet list build: next home cell to take (reset by the scan)
     const float4 *nboff;
     int *rebuild_count;
@@ -255,6 +274,7 @@ struct Engine {
     double *bias = nullptr;
     float4 *ref4 = nullptr;      // per site: that FP32 position at the last rebuild
     int *slot_cell = nullptr;    // per slot: its cell at the last rebuild
+    int *zkey = nullptr;         // per slot: quantized z at the last rebuild (the half-list order)
     int *vb_next = nullptr;      // Verlet list build: work counter over home cells
     float4 *nboff = nullptr;     // per cell x 27: home-relative neighbour-cell offset, w = 1 for an image
     unsigned *vl = nullptr;      // vl_cap entries per slot: same-molecule bit 31 | nb << 26 | slot

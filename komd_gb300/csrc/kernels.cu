@@ -158,7 +158,7 @@ __global__ void __launch_bounds__(kBlock) k_cell_sort(Grid g, const int *__restr
                                                       double *__restrict__ posd, double *__restrict__ seps_d,
                                                       double *__restrict__ sig_d, double *__restrict__ bias,
                                                       float4 *__restrict__ ref4, int *__restrict__ slot_cell,
-                                                      const int *__restrict__ rebuild) {
+                                                      int *__restrict__ zkey, const int *__restrict__ rebuild) {
     const int lane = threadIdx.x & 31;
     if (rebuild && !*rebuild) return;
     for (int cell = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); cell < g.ncell;
@@ -192,6 +192,9 @@ __global__ void __launch_bounds__(kBlock) k_cell_sort(Grid g, const int *__restr
                     bias[3 * s] = cen[0]; bias[3 * s + 1] = cen[1]; bias[3 * s + 2] = cen[2];
                     ref4[s] = p4;
                     slot_cell[slot] = cell;
+                    // the half-list order key: z quantized over the box (see vl_above)
+                    long long q = (long long)floor((z - g.low[2]) / g.L[2] * (double)kZq);
+                    zkey[slot] = (int)(q < 0 ? 0 : (q >= kZq ? kZq - 1 : q));
                 }
                 if (posd) {
                     posd[3 * slot] = x; posd[3 * slot + 1] = y; posd[3 * slot + 2] = z;
@@ -1479,7 +1482,7 @@ void launch_container(Engine &e, cudaStream_t st) {
     k_cell_sort<<<std::min(nblk(g.ncell, kWarpsPerBlock), res), kBlock, 0, st>>>(
         g, e.mol_off, e.cell_mstart, e.cell_start, e.cell_mols, e.r, e.eps, e.sig, e.key, e.slot_site, e.site_slot,
         e.pos4, e.skey, e.seps, e.posd, e.seps_d, e.sig_d, e.verlet ? e.bias : nullptr, e.verlet ? e.ref4 : nullptr,
-        e.verlet ? e.slot_cell : nullptr, rb);
+        e.verlet ? e.slot_cell : nullptr, e.verlet ? e.zkey : nullptr, rb);
     if (e.verlet) {
         if (!e.fused_drift)
             k_refresh<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.slot_site, e.r, e.bias, e.pos4, e.rebuild);
@@ -1528,6 +1531,7 @@ PairParams pair_params(Engine &e) {
     const double rl = std::max(lj ? e.cfg.cutoff : 0.0, atm ? e.cfg.cutoff_3b : 0.0) + e.cfg.skin;
     p.rl2 = rl * rl;
     p.slot_cell = e.slot_cell;
+    p.zkey = e.zkey;
     p.vb_next = e.vb_next;
     p.nboff = e.nboff;
     p.rebuild_count = e.rebuild_count;
@@ -1746,9 +1750,9 @@ AtmParams atm_params(const Engine &e) {
 
 // the fixed-point sums of the once-per-triplet sweep into f (and, with_step1,
 // integrate1 of the step); returns with_step1
-bool launch_atm_flush(Engine &e, cudaStream_t st, bool with_step1) {
+bool launch_atm_flush(Engine &e, cudaStream_t st, bool with_step1, bool force_units) {
     const double sign = e.cfg.atm_sign == KOMD_ATM_SIGN_REFERENCE ? 1.0 : -1.0;
-    const double scale_fix = 2.0 * sign * e.cfg.nu / kAtmFix;
+    const double scale_fix = force_units ? 1.0 / kAtmFix : 2.0 * sign * e.cfg.nu / kAtmFix;
     if (with_step1) {
         k_atm_flush_step1<<<nblk(e.n, kIoBlock), kIoBlock, 0, st>>>((int)e.n, e.site_slot, e.atm_acc, e.f, scale_fix,
                                                                      e.v, e.hdtm, e.err,
@@ -1765,7 +1769,7 @@ bool launch_atm(Engine &e, cudaStream_t st, bool measure, bool with_step1) {
     if (!measure && !compat && e.cfg.precision == KOMD_FP32 && e.atm_acc) {
         // every triplet once (lowest slot), fixed-point scatter, then the flush into f
         k_atm_s<<<atm_grid(e), kBlock, atm_smem(e), st>>>(p);
-        return launch_atm_flush(e, st, with_step1);
+        return launch_atm_flush(e, st, with_step1, false);
     }
     if (e.cfg.precision == KOMD_FP64) atm_dispatch<double>(p, measure, compat, atm_grid(e), atm_smem(e), st);
     else atm_dispatch<float>(p, measure, compat, atm_grid(e), atm_smem(e), st);

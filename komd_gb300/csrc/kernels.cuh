@@ -17,9 +17,13 @@ void launch_limit(Engine &e, cudaStream_t st);
 // integrate1 into its flush: returns true when it did
 bool launch_atm(Engine &e, cudaStream_t st, bool measure, bool with_step1 = false);
 AtmParams atm_params(const Engine &e);
-bool launch_atm_flush(Engine &e, cudaStream_t st, bool with_step1);
+// force_units: the sums are in force units (half-list pass), else in units of 2 sign nu
+bool launch_atm_flush(Engine &e, cudaStream_t st, bool with_step1, bool force_units);
 // LJ forces and the once-per-triplet ATM sweep in one pass (FP32, FULL, Verlet)
 void launch_lj_atm(Engine &e, cudaStream_t st);
+// true when launch_lj_atm runs the half-list form, whose fixed-point sums are
+// in force units (the flush scale is 2^-32) instead of units of 2 sign nu
+bool lj_atm_half(const Engine &e);
 // in_step (step graphs only): the fused drift path when the engine qualifies
 void launch_step0(Engine &e, cudaStream_t st, bool in_step = false);
 void launch_step1(Engine &e, cudaStream_t st);

@@ -275,13 +275,35 @@ __global__ void __launch_bounds__(kTileThreads) k_pair_tile(PairParams p) {
 // memory; every lane tests them all against its site and appends the hits to
 // its row.  Rows hold the pairs inside cutoff + skin by neighbour cell, then
 // by slot (deterministic); bit 31 marks a same-molecule pair (no LJ).
+// A row has two regions: the neighbours above the site (vl_above: larger z
+// at the rebuild, ties by slot) from the front, the others from the back
+// (row[cap-1] downwards); the count word holds both (above | below << 16).
+// The half-list force pass reads the front region alone, full-row readers
+// both (vl_entry).
 // ---------------------------------------------------------------------------
 constexpr int kVbWarps = 4;   // home cells per block
+
+// appends one hit to a two-region row: the front for a neighbour above the
+// site (vl_above), the back otherwise (a full row drops the hit and the count
+// still grows: the caller flags the overflow)
+__device__ __forceinline__ void vl_put(unsigned *row, int cap, int &chi, int &clo, unsigned word, bool up) {
+    if (chi + clo < cap) row[up ? chi : cap - 1 - clo] = word;
+    if (up) chi++; else clo++;
+}
+
+// the count word of a row (both regions clamped so that they never overlap)
+__device__ __forceinline__ int vl_count_word(int chi, int clo, int cap) {
+    const int a = min(chi, cap), b = min(clo, cap - a);
+    return a | (b << 16);
+}
+
+// logical entry k of a full row (the front region, then the back region)
+__device__ __forceinline__ int vl_entry(int k, int chi, int cap) { return k < chi ? k : cap - 1 - (k - chi); }
 
 // one lane's home site in the build: position, key, row and hit count
 struct VbHome {
     float4 p;
-    int key, slot, c;
+    int key, slot, c, clo, zk;
     unsigned self;
     bool active;
 };
@@ -293,6 +315,8 @@ __device__ __forceinline__ void vb_home(const PairParams &p, int hs, int hn, int
     o.key = p.skey[o.slot];
     o.self = (13u << 26) | (unsigned)o.slot;   // the site itself, in the home cell
     o.c = 0;
+    o.clo = 0;
+    o.zk = p.zkey[o.slot];
 }
 
 __device__ __forceinline__ bool vb_hit(const VbHome &o, const float4 &pj, float rl2) {
@@ -300,26 +324,26 @@ __device__ __forceinline__ bool vb_hit(const VbHome &o, const float4 &pj, float 
     return ax * ax + ay * ay + az * az <= rl2;
 }
 
-__device__ __forceinline__ void vb_emit(const PairParams &p, VbHome &o, const uint2 &ww) {
-    if (ww.x != o.self) {
-        if (o.c < p.vl_cap) p.vl[(size_t)o.slot * p.vl_cap + o.c] = ((int)ww.y == o.key ? 0x80000000u : 0u) | ww.x;
-        o.c++;
-    }
+__device__ __forceinline__ void vb_emit(const PairParams &p, VbHome &o, const uint2 &ww, int zk) {
+    if (ww.x != o.self)
+        vl_put(p.vl + (size_t)o.slot * p.vl_cap, p.vl_cap, o.c, o.clo, ((int)ww.y == o.key ? 0x80000000u : 0u) | ww.x,
+               vl_above(o.zk, zk, (unsigned)o.slot, ww.x & 0x3ffffffu));
 }
 
 __device__ __forceinline__ void vb_done(const PairParams &p, const VbHome &o) {
     if (o.active) {
-        p.vl_count[o.slot] = min(o.c, p.vl_cap);
-        if (o.c > p.vl_cap) atomicOr(&p.err[E_VL_OVERFLOW], 1);
+        p.vl_count[o.slot] = vl_count_word(o.c, o.clo, p.vl_cap);
+        if (o.c + o.clo > p.vl_cap) atomicOr(&p.err[E_VL_OVERFLOW], 1);
     }
 }
 
 // the 27 cells around a home cell, staged 32 sites at a time in the warp's
 // shared arrays (position in the home cell's frame; list word without the
-// same-molecule bit and molecule key); visit(jc) tests the jc staged sites
+// same-molecule bit and molecule key; order key); visit(jc) tests the jc
+// staged sites
 template <typename Visit>
 __device__ __forceinline__ void vb_walk(const PairParams &p, int cx, int cy, int cz, const float4 *nbo, float4 *sq,
-                                        uint2 *sw, int lane, Visit &&visit) {
+                                        uint2 *sw, int *sz, int lane, Visit &&visit) {
     for (int nb = 0; nb < 27; nb++) {
         int kx, ky, kz;
         bool cr;
@@ -337,6 +361,7 @@ __device__ __forceinline__ void vb_walk(const PairParams &p, int cx, int cy, int
                 pj.z += o.z;
                 sq[lane] = pj;
                 sw[lane] = make_uint2(((unsigned)nb << 26) | (unsigned)j, (unsigned)p.skey[j]);
+                sz[lane] = p.zkey[j];
             }
             __syncwarp();
             visit(jc);
@@ -351,12 +376,14 @@ template <bool TWO>
 __global__ void __launch_bounds__(32 * kVbWarps) k_vlist_build(PairParams p) {
     __shared__ float4 s_q[kVbWarps][32];
     __shared__ uint2 s_w[kVbWarps][32];
+    __shared__ int s_z[kVbWarps][32];
     if (!*p.rebuild) return;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (blockIdx.x == 0 && threadIdx.x == 0 && p.rebuild_count) atomicAdd(p.rebuild_count, 1);
     const float rl2 = (float)p.rl2;
     float4 *sq = s_q[w];
     uint2 *sw = s_w[w];
+    int *sz = s_z[w];
     // warps take home cells from a counter (reset by the scan of this rebuild):
     // cells differ in cost, and a resident grid keeps every SM busy to the end
     for (;;) {
@@ -376,10 +403,11 @@ __global__ void __launch_bounds__(32 * kVbWarps) k_vlist_build(PairParams p) {
             const int hslot = hs + min(h, hn - 1);
             const float4 hp = p.pos4[hslot];
             const int hkey = p.skey[hslot];
+            const int hz = p.zkey[hslot];
             const unsigned self = (13u << 26) | (unsigned)hslot;   // the site itself, in the home cell
             unsigned *row = p.vl + (size_t)hslot * p.vl_cap;
-            int c = 0;
-            vb_walk(p, cx, cy, cz, nbo, sq, sw, lane, [&](int jc) {
+            int c = 0, clo = 0;
+            vb_walk(p, cx, cy, cz, nbo, sq, sw, sz, lane, [&](int jc) {
                 if (active) {
 #pragma unroll 4
                     for (int t = 0; t < jc; t++) {
@@ -387,17 +415,16 @@ __global__ void __launch_bounds__(32 * kVbWarps) k_vlist_build(PairParams p) {
                         const float ax = hp.x - pj.x, ay = hp.y - pj.y, az = hp.z - pj.z;
                         if (ax * ax + ay * ay + az * az <= rl2) {   // the word is read only for hits
                             const uint2 ww = sw[t];
-                            if (ww.x != self) {
-                                if (c < p.vl_cap) row[c] = ((int)ww.y == hkey ? 0x80000000u : 0u) | ww.x;
-                                c++;
-                            }
+                            if (ww.x != self)
+                                vl_put(row, p.vl_cap, c, clo, ((int)ww.y == hkey ? 0x80000000u : 0u) | ww.x,
+                                       vl_above(hz, sz[t], (unsigned)hslot, ww.x & 0x3ffffffu));
                         }
                     }
                 }
             });
             if (active) {
-                p.vl_count[hslot] = min(c, p.vl_cap);
-                if (c > p.vl_cap) atomicOr(&p.err[E_VL_OVERFLOW], 1);
+                p.vl_count[hslot] = vl_count_word(c, clo, p.vl_cap);
+                if (c + clo > p.vl_cap) atomicOr(&p.err[E_VL_OVERFLOW], 1);
             }
           }
         } else {
@@ -408,19 +435,19 @@ __global__ void __launch_bounds__(32 * kVbWarps) k_vlist_build(PairParams p) {
                 VbHome h0, h1;
                 vb_home(p, hs, hn, hb + lane, h0);
                 if (two) vb_home(p, hs, hn, hb + 32 + lane, h1);
-                vb_walk(p, cx, cy, cz, nbo, sq, sw, lane, [&](int jc) {
+                vb_walk(p, cx, cy, cz, nbo, sq, sw, sz, lane, [&](int jc) {
                     if (two) {   // h0 is active: hn - hb > 32
 #pragma unroll 2
                         for (int t = 0; t < jc; t++) {
                             const float4 pj = sq[t];
                             const uint2 ww = sw[t];   // one read for both homes
-                            if (vb_hit(h0, pj, rl2)) vb_emit(p, h0, ww);
-                            if (h1.active && vb_hit(h1, pj, rl2)) vb_emit(p, h1, ww);
+                            if (vb_hit(h0, pj, rl2)) vb_emit(p, h0, ww, sz[t]);
+                            if (h1.active && vb_hit(h1, pj, rl2)) vb_emit(p, h1, ww, sz[t]);
                         }
                     } else if (h0.active) {
 #pragma unroll 4
                         for (int t = 0; t < jc; t++)
-                            if (vb_hit(h0, sq[t], rl2)) vb_emit(p, h0, sw[t]);
+                            if (vb_hit(h0, sq[t], rl2)) vb_emit(p, h0, sw[t], sz[t]);
                     }
                 });
                 vb_done(p, h0);
@@ -447,7 +474,8 @@ __global__ void __launch_bounds__(32 * kVbWarps) k_vlist_build(PairParams p) {
 template <bool MEASURE, bool EMIT, bool UNIFORM, int U, bool TO_SMEM>
 __device__ __forceinline__ int lj_site(const PairParams &p, int i, int lane, unsigned lt, float rc2, float rc3sq,
                                        float4 *se, float4 *sq, float &m_u, float &m_pairs, float (&m_w)[6]) {
-    const int cnt = p.vl_count[i];
+    const int cw = p.vl_count[i];
+    const int chi = cw & 0xffff, cnt = chi + (cw >> 16);   // both regions of the row
     const float4 pi = p.pos4[i];
     const float sei = UNIFORM ? 0.f : p.seps[i];
     const float4 *off = p.nboff + (size_t)p.slot_cell[i] * 27;
@@ -459,17 +487,11 @@ __device__ __forceinline__ int lj_site(const PairParams &p, int i, int lane, uns
         unsigned e[U];
         float4 o[U], pj[U];
         float sej[U];
-        // rows hold vl_cap entries: the first pass loads speculatively up to the
-        // capacity so that it does not wait for the count; later passes stop at it
-        const int lim = k0 == 0 ? p.vl_cap : cnt;
 #pragma unroll
         for (int u = 0; u < U; u++) {
             const int k = k0 + u * 32 + lane;
-            e[u] = k < lim ? __ldcs(row + k) : 0xffffffffu;   // read once per step: evict first
+            e[u] = k < cnt ? __ldcs(row + vl_entry(k, chi, p.vl_cap)) : 0xffffffffu;   // read once per step: evict first
         }
-#pragma unroll
-        for (int u = 0; u < U; u++)
-            if (k0 + u * 32 + lane >= cnt) e[u] = 0xffffffffu;
 #pragma unroll
         for (int u = 0; u < U; u++) {
             if (e[u] != 0xffffffffu) {
@@ -621,6 +643,204 @@ __global__ void __launch_bounds__(256, 4) k_lj_atm(PairParams p, AtmParams a, in
     }
 }
 
+// ---------------------------------------------------------------------------
+// The half-list LJ + ATM pass (FP32 forces, FULL triplets, Verlet path, no
+// Limit): each pair and each triplet is evaluated once, from its lowest
+// member in the order vl_above.  One warp per site i walks the front region
+// of i's row only (the neighbours above i, about half the row):
+//   1. LJ: the force on i stays in the lanes' registers; the reaction on the
+//      partner j is staged in shared memory (sr) beside the partner's slot;
+//      partners inside cutoff_3b are staged for the triplet sweep as well
+//      (se, sq, at the front of their arrays), LJ-only partners fill sr from
+//      the back;
+//   2. the triplet sweep of atm_vertex_shares leaves each ATM partner's share
+//      in its owner lane;
+//   3. each partner gets its LJ reaction plus its ATM share (in force units)
+//      through ONE 64-bit fixed-point add per component -- integer sums, so
+//      the result does not depend on the order in which warps add;
+//   4. i's own force (its LJ sum plus its ATM share) is written to f; the
+//      flush adds the fixed-point sums of the partners' contributions.
+// Against the full-row pass this reads half the list, evaluates each LJ
+// pair once instead of twice, and converts one FP32 partial per partner.
+// ---------------------------------------------------------------------------
+// what the half-list pass reads of a site before its arithmetic: the count
+// of its front region, the region's first 64 entries (rows hold vl_cap >= 64
+// entries, so both reads stay inside the row; the count masks them, and the
+// entries are read without waiting for it), its position and its cell.
+// (Loading this one site ahead, during the previous site's sweep, was
+// measured slower: the extra live registers spill at the 64-register bound.)
+struct HalfRow {
+    int cnt, cell;
+    unsigned e0, e1;
+    float4 pi;
+};
+
+__device__ __forceinline__ void half_row_load(const PairParams &p, int i, int lane, HalfRow &h) {
+    const unsigned *row = p.vl + (size_t)i * p.vl_cap;
+    h.cnt = p.vl_count[i] & 0xffff;   // the neighbours above i
+    h.e0 = __ldcs(row + lane);        // read once per step: evict first
+    h.e1 = __ldcs(row + 32 + lane);
+    h.pi = p.pos4[i];
+    h.cell = p.slot_cell[i];
+}
+
+template <bool UNIFORM>
+__device__ __forceinline__ void lj_half(const PairParams &p, int i, const HalfRow &h, int lane, unsigned lt, float rc2,
+                                        float rc3sq, float4 *se, float4 *sq, float4 *sr, int capa, int capr,
+                                        int &m_out, int &k_out, float &fx, float &fy, float &fz) {
+    const int cnt = h.cnt;
+    const float4 pi = h.pi;
+    const float sei = UNIFORM ? 0.f : p.seps[i];
+    const float4 *off = p.nboff + (size_t)h.cell * 27;
+    const unsigned *row = p.vl + (size_t)i * p.vl_cap;
+    const float sg2u = p.sig0 * p.sig0, eeu = p.eps0;
+    fx = fy = fz = 0.f;
+    int m = 0, k = 0;
+    for (int k0 = 0; k0 < cnt; k0 += 64) {
+        unsigned e[2];
+        float4 o[2], pj[2];
+        float sej[2];
+        if (k0 == 0) {   // the prefetched first 64 entries
+            e[0] = lane < cnt ? h.e0 : 0xffffffffu;
+            e[1] = 32 + lane < cnt ? h.e1 : 0xffffffffu;
+        } else {
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const int kk = k0 + u * 32 + lane;
+                e[u] = kk < cnt ? __ldcs(row + kk) : 0xffffffffu;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            if (e[u] != 0xffffffffu) {
+                o[u] = off[(e[u] >> 26) & 31u];
+                pj[u] = p.pos4[e[u] & 0x3ffffffu];
+                if (!UNIFORM) sej[u] = p.seps[e[u] & 0x3ffffffu];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const bool valid = e[u] != 0xffffffffu;
+            float dx = 0.f, dy = 0.f, dz = 0.f, r2 = 1e30f;
+            float gx = 0.f, gy = 0.f, gz = 0.f;
+            bool lj = false;
+            if (valid) {
+                dx = pi.x - (pj[u].x + o[u].x);
+                dy = pi.y - (pj[u].y + o[u].y);
+                dz = pi.z - (pj[u].z + o[u].z);
+                r2 = dx * dx + dy * dy + dz * dz;
+                lj = p.use_lj && r2 <= rc2 && !(e[u] >> 31);
+                if (lj) {
+                    const float inv = rcp_approx(r2);
+                    float x, ee;
+                    if (UNIFORM) {
+                        x = sg2u * inv;
+                        ee = eeu;
+                    } else {
+                        const float sg = pi.w + pj[u].w;
+                        x = sg * sg * inv;
+                        ee = sei * sej[u];
+                    }
+                    const float lj6 = x * x * x;
+                    const float fac = 24.0f * ee * (2.0f * lj6 * lj6 - lj6) * inv * p.lj_fscalef;   // ATM2B factor
+                    gx = dx * fac; gy = dy * fac; gz = dz * fac;
+                    fx += gx; fy += gy; fz += gz;
+                }
+            }
+            const bool at = valid && r2 <= rc3sq;   // a triplet partner (LJ or not)
+            const bool lo = lj && !at;              // an LJ-only partner
+            const unsigned ma = __ballot_sync(0xffffffffu, at), ml = __ballot_sync(0xffffffffu, lo);
+            if (at || lo) {
+                const int nb = (int)((e[u] >> 26) & 31u), j = (int)(e[u] & 0x3ffffffu);
+                const int code = nb | (o[u].w != 0.f ? 32 : 0) | (j << 6);
+                const float4 react = make_float4(-gx, -gy, -gz, __int_as_float(code));
+                if (at) {
+                    const int pos = m + __popc(ma & lt);
+                    if (pos < capa) {
+                        se[pos] = make_float4(dx, dy, dz, __int_as_float(code));
+                        sq[pos] = atm_stage_q(r2);
+                        sr[pos] = react;
+                    }
+                } else {
+                    sr[capr - 1 - (k + __popc(ml & lt))] = react;
+                }
+            }
+            m += __popc(ma);
+            k += __popc(ml);
+        }
+    }
+    if (lane == 0 && m > capa) atomicOr(&p.err[E_ATM_OVERFLOW], 1);
+    m_out = min(m, capa);
+    k_out = k;
+}
+
+template <bool UNIFORM>
+__global__ void __launch_bounds__(256, 4) k_lj_atm_half(PairParams p, AtmParams a, float sa, int n, int per) {
+    extern __shared__ float4 s_dyn[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int capa = p.nl_cap, capr = p.vl_cap;
+    float4 *se = s_dyn + (size_t)w * (2 * capa + capr), *sq = se + capa, *sr = sq + capa;
+    const float rc2 = (float)p.rc2, rc3sq = (float)p.rc3sq, rc3f = (float)a.rc2;
+    const unsigned lt = lanemask_lt();
+    for (int it = 0; it < per; it++) {
+        const int i = (blockIdx.x * per + it) * 8 + w;
+        if (i >= n) break;   // warp-uniform; later groups of this block are past n too
+        HalfRow cur;
+        half_row_load(p, i, lane, cur);
+        int m, k;
+        float fx, fy, fz;
+        lj_half<UNIFORM>(p, i, cur, lane, lt, rc2, rc3sq, se, sq, sr, capa, capr, m, k, fx, fy, fz);
+        __syncwarp();
+        float ax, ay, az, gx, gy, gz;
+        atm_vertex_shares(a, se, sq, m, lane, rc3f, sa, ax, ay, az, gx, gy, gz);
+        // every partner: LJ reaction + ATM share (force units), one fixed-point add per component
+        const int tot = m + k;
+        for (int L = lane; L < tot; L += 32) {
+            const float4 rr = sr[L < m ? L : capr - 1 - (L - m)];
+            float vx = rr.x, vy = rr.y, vz = rr.z;
+            if (L == lane) {   // the first trip: lane L < 32 owns partner L's share (zero for m > 32)
+                vx = fmaf(sa, ax, vx);
+                vy = fmaf(sa, ay, vy);
+                vz = fmaf(sa, az, vz);
+            }
+            unsigned long long *acc = a.acc + 3 * (size_t)(__float_as_int(rr.w) >> 6);
+            atm_fix_add(acc, vx);
+            atm_fix_add(acc + 1, vy);
+            atm_fix_add(acc + 2, vz);
+        }
+        // the site's own force: its LJ sum and its ATM share
+        fx = fmaf(sa, gx, fx);
+        fy = fmaf(sa, gy, fy);
+        fz = fmaf(sa, gz, fz);
+        for (int o = 16; o > 0; o >>= 1) {
+            fx += __shfl_xor_sync(0xffffffffu, fx, o);
+            fy += __shfl_xor_sync(0xffffffffu, fy, o);
+            fz += __shfl_xor_sync(0xffffffffu, fz, o);
+        }
+        if (lane == 0) {
+            const int site = p.slot_site[i];
+            p.f[3 * site] = (double)fx;
+            p.f[3 * site + 1] = (double)fy;
+            p.f[3 * site + 2] = (double)fz;
+        }
+        __syncwarp();   // se / sq / sr are refilled by the next site
+    }
+}
+
+// shared memory of the half-list pass: per warp nl_cap staged triplet
+// partners (se, sq) and vl_cap partners' reactions (sr)
+static size_t lj_atm_half_smem(const Engine &e) {
+    return (size_t)8 * sizeof(float4) * (2 * (size_t)e.nl_cap + (size_t)e.vl_cap);
+}
+
+// the half-list pass serves the step when nothing after the pair terms reads
+// or clamps the force of a site before the flush (no Limit, no FENE, no
+// tabulated term) and its staging fits the shared memory of four blocks
+bool lj_atm_half(const Engine &e) {
+    if (e.cfg.terms & (KOMD_TERM_LIMIT | KOMD_TERM_FENE | KOMD_TERM_TABULATED)) return false;
+    return lj_atm_half_smem(e) <= 56 * 1024;
+}
+
 int vlist_grid(const Engine &e) { return (int)((e.n + 7) / 8); }
 
 // groups of 8 slots per block of the force pass: about eight resident waves of
@@ -680,6 +900,18 @@ void launch_lj_atm(Engine &e, cudaStream_t st) {
     const AtmParams a = atm_params(e);
     const int per = vlist_per(e);
     const int grid = (vlist_grid(e) + per - 1) / per;
+    if (lj_atm_half(e)) {
+        const size_t sm = lj_atm_half_smem(e);
+        const float sa = (float)(2.0 * a.sign * a.nu);   // share units (2 sign nu) to force units
+        if (e.uniform) {
+            if (sm > 48 * 1024) cudaFuncSetAttribute(k_lj_atm_half<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            k_lj_atm_half<true><<<grid, 256, sm, st>>>(p, a, sa, (int)e.n, per);
+        } else {
+            if (sm > 48 * 1024) cudaFuncSetAttribute(k_lj_atm_half<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            k_lj_atm_half<false><<<grid, 256, sm, st>>>(p, a, sa, (int)e.n, per);
+        }
+        return;
+    }
     const size_t sm = (size_t)8 * 2 * sizeof(float4) * (size_t)e.nl_cap;
     const bool u3 = vlist_u3(e);
     if (e.uniform) {

@@ -1,12 +1,14 @@
 """Small fixed workloads for kernel profiling (ncu) and quick timing.
 
-    python -m komd_gb300.profile_cases exact      [--ncell 40] [--steps 3] [--equil 0]
+    python -m komd_gb300.profile_cases exact      [--ncell 40] [--steps 3] [--equil 0] [--skin 0.3] [--cell 2.8]
     python -m komd_gb300.profile_cases surrogate  [--ncell 40] [--steps 3]
     python -m komd_gb300.profile_cases replicas   [--count 64] [--steps 2]
     python -m komd_gb300.profile_cases tabulated  [--ncell 40] [--steps 3]
 
 `exact`: LJ + FULL ATM argon (rho* 0.8442, T* 0.722, rc 2.5 / 2.0, nu* 0.073,
-cell 2.8, skin 0.3), the benchmark's engine configuration.  `surrogate`: the
+cell 2.8, skin 0.3 by default; the benchmark's timed configuration is
+--skin 0.4 --cell 0 (cell 0: the smallest edge >= 2.5 + skin that divides the
+box) --equil 400).  `surrogate`: the
 same with the learned three-body term on Glorot-initialised weights (kernel
 cost does not depend on the weights).  `replicas`: `count` uneven replicas
 (2000-20000 atoms) advanced by one batched graph.  `tabulated`: the IBI
@@ -26,10 +28,13 @@ import numpy as np
 from . import gpu, lattice, surrogate
 
 
-def exact(ncell, steps, equil, learned=False):
+def exact(ncell, steps, equil, learned=False, skin=0.3, cell=2.8):
     s = lattice.argon_fcc(ncell, rho=0.8442, t_star=0.722, seed=1)
     terms = gpu.TERM_LJ | gpu.TERM_ATM | (gpu.TERM_ATM_SURROGATE if learned else 0)
-    g = gpu.GpuSystem(s, surrogate.physics_config(s, 2.8, skin=0.3, terms=terms))
+    if cell <= 0:
+        side = float(np.min(s.high - s.low))
+        cell = side / np.floor(side / (2.5 + skin))
+    g = gpu.GpuSystem(s, surrogate.physics_config(s, cell, skin=skin, terms=terms))
     g.update_container()
     g.forces()
     if learned:
@@ -93,13 +98,15 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--equil", type=int, default=0)
     ap.add_argument("--count", type=int, default=64)
+    ap.add_argument("--skin", type=float, default=0.3)
+    ap.add_argument("--cell", type=float, default=2.8)
     a = ap.parse_args()
     if a.case == "replicas":
         replicas(a.count, a.steps)
     elif a.case == "tabulated":
         tabulated(a.ncell, a.steps)
     else:
-        exact(a.ncell, a.steps, a.equil, learned=a.case == "surrogate")
+        exact(a.ncell, a.steps, a.equil, learned=a.case == "surrogate", skin=a.skin, cell=a.cell)
 
 
 if __name__ == "__main__":

@@ -18,6 +18,9 @@
 //   NCOUNT         per-site neighbour count inside the cutoff, read off the
 //                  reference's own pair list with LJ12_6_Force's test
 //   TEMP, UPOT, PRESSURE, RDF  sensor outputs (when enabled in the input)
+//   LJHIST         the LJ sensor's U(r) and F(r) histograms of this step's
+//                  measure alone (sums of u, sums of f, counts of u, counts
+//                  of f per bin; Potential_Sensor's views, zeroed first)
 //
 // usage: komd_ref_harness <input.dat> <out.txt> <n_steps> [dump steps...]
 //        functors are chosen from the input exactly as src/main.cpp:57-66 does.
@@ -47,6 +50,24 @@
 #include "sensors/TemperatureSensor.h"
 #include "container/LinkedCells.h"
 #include "Kokkos_Core.hpp"
+
+// the LJ sensor with its histogram views reachable: Potential_Sensor::measure
+// adds every measure into the views (they are never cleared), so the harness
+// zeroes them before a measure to dump that measure's histograms alone
+struct LJSensorDump : public LJ12_6_Sensor {
+    void clear_hist() {
+        Kokkos::deep_copy(p_data_u, 0.0);
+        Kokkos::deep_copy(p_data_f, 0.0);
+        Kokkos::deep_copy(p_count_u, 0);
+        Kokkos::deep_copy(p_count_f, 0);
+    }
+    void dump_hist(FILE* out) {
+        fprintf(out, "LJHIST %llu\n", (unsigned long long)p_bins);
+        for (uint64_t k = 0; k < p_bins; k++)
+            fprintf(out, "%.17g %.17g %llu %llu\n", p_data_u[k], p_data_f[k], (unsigned long long)p_count_u[k],
+                    (unsigned long long)p_count_f[k]);
+    }
+};
 
 static void dump_vec(FILE* out, const char* key, KW::vec_t<math::d3>& a, uint64_t n) {
     fprintf(out, "%s %llu\n", key, (unsigned long long)n);
@@ -114,10 +135,10 @@ int main(int argc, char** argv) {
             Registry::instance->temperature_sensor_ptr() = temp;
             thermostat = std::make_unique<VelocityScaling>();
         }
-        std::shared_ptr<LJ12_6_Sensor> pot;
+        std::shared_ptr<LJSensorDump> pot;
         std::shared_ptr<PressureSensor> pres;
         std::shared_ptr<RDFSensor> rdf;
-        if (config->enable_sensor_lj) pot = std::make_shared<LJ12_6_Sensor>();
+        if (config->enable_sensor_lj) pot = std::make_shared<LJSensorDump>();
         if (config->enable_sensor_pres) pres = std::make_shared<PressureSensor>();
         auto container = Registry::instance->moleculeContainer();
         container->init();
@@ -179,7 +200,12 @@ int main(int argc, char** argv) {
 
             temp->measure();
             fprintf(out, "TEMP %.17g\n", temp->getTemperature());
-            if (pot) { pot->measure(); fprintf(out, "UPOT %.17g\n", pot->getCurrentPotential()); }
+            if (pot) {
+                pot->clear_hist();
+                pot->measure();
+                fprintf(out, "UPOT %.17g\n", pot->getCurrentPotential());
+                pot->dump_hist(out);
+            }
             if (pres) {
                 pres->measure();
                 const auto& t = pres->getPressureTensor();

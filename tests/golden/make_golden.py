@@ -75,6 +75,10 @@ def parse_dump(path):
             n = int(ln[1])
             cur["ibirdf"] = np.array([float(lines[i + k]) for k in range(n)])
             i += n
+        elif key == "LJHIST":
+            n = int(ln[1])
+            cur["ljhist"] = np.array([[float(x) for x in lines[i + k].split()] for k in range(n)]).T.copy()
+            i += n
         elif key in ("TEMP", "UPOT"):
             cur[key.lower()] = float(ln[1])
         elif key == "NPAIRS":
@@ -128,7 +132,14 @@ def run_case(name, sysm, values, steps, dumps, comps=None, thermostat=False, tab
         shutil.rmtree(tmp, ignore_errors=True)
 
 
-def run_stock(name, sysm, values, comps=None, tables=None):
+def file_tokens(path):
+    """The numbers of a sensor file in reading order; labels such as the
+    viscosity file's "b:" are skipped, the reference's "-nan" reads as NaN."""
+    with open(path) as fh:
+        return np.array([float(t) for t in fh.read().split() if not t.endswith(":")])
+
+
+def run_stock(name, sysm, values, comps=None, tables=None, tokens=False):
     """Runs the reference's unmodified stock main (oracle/_ref/komd_ref_main)
     on a whole input file (plugins included) and stores every text file it
     writes (IBI's rdf_/pot_/force_/update_<iteration>.txt, final_pot.txt), the
@@ -159,7 +170,10 @@ def run_stock(name, sysm, values, comps=None, tables=None):
         names = sorted(f for f in os.listdir(tmp) if f.endswith(".txt") and f not in (tables or {}))
         arrays["files"] = np.asarray(names)
         for f in names:
-            arrays["file_" + f[:-4]] = np.atleast_2d(np.loadtxt(os.path.join(tmp, f)))
+            if tokens:   # sensor files with ragged rows or labels: their numbers in order
+                arrays["tok_" + f[:-4]] = file_tokens(os.path.join(tmp, f))
+            else:
+                arrays["file_" + f[:-4]] = np.atleast_2d(np.loadtxt(os.path.join(tmp, f)))
         ck = [f for f in os.listdir(tmp) if f.startswith("ckpt_") and f.endswith(".ps")]
         if len(ck) != 1:
             raise RuntimeError(f"{name}: expected one checkpoint, found {ck}")
@@ -280,7 +294,17 @@ def main(selected):
                                                 IBI_reload_ppath="pot.txt"),
                   tables={"force.txt": (x, f), "pot.txt": (x, u)})
 
-    cases = dict(ibirun864=ibirun864, ibistop864=ibistop864, ibireload864=ibireload864, ibi864=ibi864, lj864=lj864, ljatm864=ljatm864, atmlist500=atmlist500, fene375=fene375, edge_box=edge_box,
+    def sensors864():
+        # the stock main with the LJ, pressure and viscosity sensors on (and the
+        # always-on thermostat): every file they write at write_freq 10 over 30 steps
+        # -- pot_LJ12_6_<step> (U(r), F(r) histogram means), pot_history_LJ12_6_<step>,
+        # pressures_<step>, viscosity_<step> (Green-Kubo over the per-step tensors)
+        s = lattice.argon_fcc(6, rho=0.8442, t_star=0.722, seed=22, jitter=0.05)
+        run_stock("sensors864", s, ibi_values(s, 30, write_freq=10, enable_sensor_lj=1, enable_sensor_pres=1,
+                                              enable_sensor_visc=1, sensor_visc_no_orig=1, sensor_lj_bins=60),
+                  tokens=True)
+
+    cases = dict(sensors864=sensors864, ibirun864=ibirun864, ibistop864=ibistop864, ibireload864=ibireload864, ibi864=ibi864, lj864=lj864, ljatm864=ljatm864, atmlist500=atmlist500, fene375=fene375, edge_box=edge_box,
                  atm2b864=atm2b864, thermo864=thermo864)
     for name in (selected or list(cases)):
         cases[name]()

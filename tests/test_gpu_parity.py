@@ -110,6 +110,39 @@ def test_sensors_match_reference(name):
         g.close()
 
 
+@pytest.mark.parametrize("name", ["lj864", "ljatm864", "fene375", "edge_box"])
+def test_lj_histograms_match_reference(name):
+    """KOMD_MEASURE_LJ_HIST against the reference's LJ12_6_Sensor histograms
+    (LJ12_6_Sensor.cpp:47-84: per bin of r over 3 max_sigma, the sums of
+    u and of F(r) = 24 eps (2 s12 - s6) / r and their counts, over the pairs
+    the sensor counts once), at every dumped state.  FP64 mode: the same bins
+    and counts, sums to rounding; FP32 mode: counts within the pairs that sit
+    on a bin edge, sums to FP32 accuracy."""
+    from komd_gb300 import gpu
+    z = load_case(name)
+    for step in (int(d) for d in z["dumps"]):
+        ref = z[f"s{step}_ljhist"]
+        nb = ref.shape[1]
+        for prec in (gpu.FP64, gpu.FP32):
+            g, _ = gpu_for_case(z, precision=prec, lj_bins=nb, max_sigma=1.0)
+            r, v = _state_at(z, step)
+            g.set_state(r, v)
+            g.update_container()
+            g.forces()
+            h = g.measure(gpu.MEASURE_ENERGY | gpu.MEASURE_LJ_HIST)["lj_hist"]
+            g.close()
+            if prec == gpu.FP64:
+                assert np.array_equal(h[2], ref[2]) and np.array_equal(h[3], ref[3]), f"{name} step {step}"
+                np.testing.assert_allclose(h[0], ref[0], rtol=1e-11, atol=1e-11 * np.abs(ref[0]).max())
+                np.testing.assert_allclose(h[1], ref[1], rtol=1e-11, atol=1e-11 * np.abs(ref[1]).max())
+            else:
+                assert np.abs(h[2] - ref[2]).sum() <= 4 and h[2].sum() == ref[2].sum(), f"{name} step {step}"
+                scale_u, scale_f = np.abs(ref[0]).max(), np.abs(ref[1]).max()
+                np.testing.assert_allclose(h[0].sum(), ref[0].sum(), rtol=2e-5)
+                assert np.abs(h[0] - ref[0]).max() <= 1e-3 * scale_u
+                assert np.abs(h[1] - ref[1]).max() <= 1e-3 * scale_f
+
+
 def test_fp64_trajectory_follows_reference():
     """100 NVE steps in FP64 mode through the graph-replayed step: positions
     stay on the reference's trajectory."""

@@ -196,3 +196,31 @@ def test_komd_vtk_output(komd_exe, tmp_path):
     ck = komd_io.read_checkpoint(str(tmp_path / "ckpt_50.ps"), low=z["low"], high=z["high"])
     np.testing.assert_allclose(d50["points"], ck.r, rtol=1e-5, atol=1e-5)
     assert np.isfinite(d50["force"]).all() and np.abs(d50["force"]).max() > 0
+
+
+@pytest.mark.gpu
+def test_komd_sensor_files_follow_reference(komd_exe, tmp_path):
+    """sensors864: the reference's stock main with the LJ, pressure and
+    viscosity sensors on wrote pot_LJ12_6_<step> (the U(r) and F(r) histogram
+    means of LJ12_6_Sensor / Potential_Sensor), pot_history_LJ12_6_<step>,
+    pressures_<step> and viscosity_<step> (the Green-Kubo integrals of
+    ViscositySensor) every 10 steps.  `komd` on the same input writes the same
+    files with the same numbers (6 printed digits; empty histogram bins are
+    NaN on both sides)."""
+    def file_tokens(path):   # as tests/golden/make_golden.py reads them: labels skipped, "-nan" is NaN
+        with open(path) as fh:
+            return np.array([float(t) for t in fh.read().split() if not t.endswith(":")])
+
+    z = load_case("sensors864")
+    inp = _write_stock_case(tmp_path, z, extra=dict(gpu_precision="fp64"))
+    out = subprocess.run([komd_exe, inp], capture_output=True, text=True, cwd=tmp_path, timeout=300)
+    assert out.returncode == 0, out.stderr
+    for f in z["files"]:
+        f = str(f)
+        assert (tmp_path / f).exists(), f
+        got = file_tokens(str(tmp_path / f))
+        ref = z["tok_" + f[:-4]]
+        assert got.shape == ref.shape, f
+        # viscosity: correlation sums of the pressure series (6 digits each side)
+        rtol = 2e-4 if f.startswith("viscosity") else 2e-5
+        np.testing.assert_allclose(got, ref, rtol=rtol, atol=1e-9 * np.nanmax(np.abs(ref)), err_msg=f)

@@ -44,11 +44,14 @@ def test_oracle_matches_reference_bitwise(oracle_lib, name):
     dumps = [int(d) for d in z["dumps"]]
     list_atm = bool(z["p_enable_3b"]) and not bool(z["p_enable_3b_direct"])
     rdf_sum, n_rdf = None, 0
+    # the LJ sensor's U(r) / F(r) histograms of each dumped measure (sensor_lj_bins
+    # over 3 max_sigma; max_sigma is the COMP sigma, 1)
+    nbins = int(z["s0_ljhist"].shape[1]) if "s0_ljhist" in z else 0
     for step in range(max(dumps) + 1):
         if step > 0:
             sim.integrate0()
         sim.update_container()
-        sim.forces(ncount=True, with_atm_virial=list_atm)
+        sim.forces(nbins=nbins, max_sigma=1.0, ncount=True, with_atm_virial=list_atm)
         if step > 0:
             sim.integrate1()
         if int(z.get("p_thermostat", 0)):
@@ -71,6 +74,13 @@ def test_oracle_matches_reference_bitwise(oracle_lib, name):
             continue
         assert np.array_equal(sim.ncount, z[p + "ncount"]), f"{name} step {step}: neighbour counts"
         assert sim.lj_out.u_total == pytest.approx(float(z[p + "upot"]), rel=1e-13, abs=1e-12)
+        if nbins:
+            # LJ12_6_Sensor::LJ12_6_Pot (LJ12_6_Sensor.cpp:47-84): same bins, sums and counts
+            hu, hf, cu, cf = sim.hist
+            ref = z[p + "ljhist"]
+            assert np.array_equal(cu, ref[2].astype(np.uint64)) and np.array_equal(cf, ref[3].astype(np.uint64))
+            np.testing.assert_allclose(hu, ref[0], rtol=1e-12, atol=1e-12 * np.abs(ref[0]).max())
+            np.testing.assert_allclose(hf, ref[1], rtol=1e-12, atol=1e-12 * np.abs(ref[1]).max())
         # PressureSensor: momentum over the first getNumMolecules() sites + LJ
         # list virial (+ ATM_Pressure for the list-based ATM only)
         pres = sim.momentum() + np.array(sim.lj_out.virial[:])
