@@ -410,20 +410,23 @@ def drift_leg(args, local, model=None):
     T* 0.722), rc 2.5 / 2.0, nu* 0.073, dt* 0.005, 1000 steps of
     equilibration, then 10^4 steps with the total energy (kinetic + LJ + ATM,
     reduced units) sampled every 500 steps; the drift is the fitted slope per
-    atom per 10^4 steps.  Forms: exact FP32 forces, exact FP64 forces, and
-    the learned three-body term when a trained model is given."""
+    atom per 10^4 steps.  Forms: exact FP32 forces, exact FP64 forces (both
+    with the reference's truncated potentials), the labelled switched-cutoff
+    option (komd_config::switch_width, FP32), and the learned three-body term
+    when a trained model is given."""
     from komd_gb300 import gpu, lattice, surrogate
     out = {}
-    forms = [("fp32_exact", gpu.FP32, False), ("fp64_exact", gpu.FP64, False)]
+    forms = [("fp32_exact", gpu.FP32, False, 0.0), ("fp64_exact", gpu.FP64, False, 0.0),
+             ("fp32_switched_0.3", gpu.FP32, False, 0.3)]
     if model is not None:
-        forms.append(("fp32_learned", gpu.FP32, True))
-    for name, prec, learned in forms:
+        forms.append(("fp32_learned", gpu.FP32, True, 0.0))
+    for name, prec, learned, width in forms:
         s = lattice.argon_fcc(20, rho=0.8442, t_star=0.722, seed=3)
         terms = gpu.TERM_LJ | gpu.TERM_ATM | (gpu.TERM_ATM_SURROGATE if learned else 0)
         skin = 0.3 if prec == gpu.FP32 else 0.0
         cfg = gpu.make_config(s.low, s.high, 2.8, cutoff=2.5, cutoff_3b=2.0, nu=0.073, dt=0.005, terms=terms,
                               precision=prec, atm_sign=gpu.ATM_SIGN_PHYSICAL, atm_enum=gpu.ATM_ENUM_FULL,
-                              virial_mode=gpu.VIRIAL_CORRECT, skin=skin)
+                              virial_mode=gpu.VIRIAL_CORRECT, skin=skin, switch_width=width)
         g = gpu.GpuSystem(s, cfg, device=local)
         if learned:
             g.surrogate_load(model, probe_every=0)
@@ -443,6 +446,9 @@ def drift_leg(args, local, model=None):
         slope = float(np.polyfit(np.asarray(steps, float), e, 1)[0])
         out[name] = {"drift_per_atom_per_1e4_steps": slope * 1e4, "max_abs_dev_per_atom": float(np.abs(e - e[0]).max()),
                      "e_per_atom_start": float(e[0]), "wall_s": wall}
+        if width > 0:
+            out[name]["option"] = (f"switched cutoffs (switch_width {width}): LJ and ATM energies smoothly switched "
+                                   f"off over the last {width} sigma below each cutoff; not the reference's potential")
         g.close()
     out["system"] = ("32,000 atoms FCC 20^3, rho* 0.8442, T* 0.722, LJ rc 2.5 + ATM rc 2.0 (FULL, -grad V), "
                      "nu* 0.073, dt* 0.005, 1000 steps equilibration + 10^4 steps, energy every 500 steps")

@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define KOMD_GPU_ABI_VERSION 1
+#define KOMD_GPU_ABI_VERSION 2
 
 /* status codes */
 enum {
@@ -105,6 +105,17 @@ typedef struct komd_config {
     int32_t thermostat;        /* 1: each step of komd_gpu_step ends with v *= sqrt(T_target / T),
                                   T measured on the device as TemperatureSensor does
                                   (VelocityScaling.cpp:12-25, Simulation.cpp:72) */
+    double switch_width;       /* 0 (default): the reference's truncated LJ and ATM
+                                  (potentials/LJ12_6.cpp:28, potentials/ATM.cpp:43).
+                                  > 0: a labelled option with no reference counterpart --
+                                  the LJ pair energy times S(r^2) and the ATM triplet
+                                  energy times S over its three sides, S the C1
+                                  smoothstep t^2 (3 - 2t), t = (rc^2 - x) / (rc^2 - rs^2),
+                                  rs = cutoff - switch_width (cutoff_3b - switch_width for
+                                  ATM); forces are the exact gradients, so the energy is
+                                  conserved without the jumps of the truncation.  Needs
+                                  the Verlet path (skin > 0, FP32) without Limit, FENE,
+                                  ATM2B, tabulated or learned terms */
 } komd_config;
 
 typedef struct komd_observables {

@@ -65,19 +65,52 @@ __device__ __forceinline__ AtmV atm_derivs(float4 qa, float4 qb, float C) {
     return r;
 }
 
+// atm_derivs under the switched cutoff (AtmParams::sw): the triplet energy
+// V S(A) S(B) S(C) differentiated in the squared sides; sA / dA are S and
+// dS/dx of the lane's own side A, computed once per sweep
+__device__ __forceinline__ AtmV atm_derivs_sw(float4 qa, float4 qb, float C, float sA, float dA, float rc2s,
+                                              float iw) {
+    const float A = qa.x, B = qb.x;
+    const float wc = rsqrtf(C);
+    const float sv = qa.z * qb.z * wc;
+    const float s2 = sv * sv;
+    const float s5 = s2 * s2 * sv;
+    const float S = A + B + C;
+    const float t1 = fmaf(-2.0f, C, S), t2 = fmaf(-2.0f, B, S), t3 = fmaf(-2.0f, A, S);
+    const float u = t2 * t3, v = t1 * t3, w = t1 * t2;
+    const float K = 0.375f * (u + v + w);
+    const float nP = -0.9375f * (t1 * u);
+    const float a15 = -1.5f * A;
+    const float vA = s5 * fmaf(nP, qa.y, fmaf(-0.75f, w, fmaf(-1.5f * B, C, K)));
+    const float vB = s5 * fmaf(nP, qb.y, fmaf(-0.75f, v, fmaf(a15, C, K)));
+    const float vC = s5 * fmaf(nP, wc * wc, fmaf(-0.75f, u, fmaf(a15, B, K)));
+    const float Vn = s2 * sv + 0.375f * (t1 * u) * s5;   // V / nu
+    float sB, dB, sC, dC;
+    sw_eval(B, rc2s, iw, sB, dB);
+    sw_eval(C, rc2s, iw, sC, dC);
+    AtmV r;
+    r.vA = sB * sC * (vA * sA + Vn * dA);
+    r.vB = sA * sC * (vB * sB + Vn * dB);
+    r.vC = sA * sB * (vC * sC + Vn * dC);
+    return r;
+}
+
 // the round-robin sweep of one vertex: lane li = lane - gb owns staged
 // neighbour li < m and plays rounds d = d_first .. d_last (at most m/2) over
 // `rounds` loop trips (rounds past d_last do nothing); the lane's partial sum
 // for its neighbour is returned in (ax, ay, az).  The vertex's own share is
 // not summed here: per triplet g_i = -(g_a + g_b), so the vertex force is
 // minus the sum of its neighbours' shares.
+template <bool SW = false>
 __device__ __forceinline__ void atm_sweep(const float4 *se, const float4 *sq, int m, int li, int gb, int d_first,
                                           int d_last, int rounds, float rc2, float &ax, float &ay, float &az,
-                                          float4 &ea_out) {
+                                          float4 &ea_out, float sw_iw = 0.f) {
     const bool own = li < m;
     const float4 ea = own ? se[li] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 qa = own ? sq[li] : make_float4(1.f, 1.f, 1.f, 0.f);
     ea_out = ea;
+    float sA = 1.f, dA = 0.f;
+    if (SW) sw_eval(qa.x, rc2, sw_iw, sA, dA);
     // partner b = li + d and share source li - d (mod m), stepped per round;
     // d <= m/2 keeps both within one wrap
     int b = li + d_first, src = li - d_first;
@@ -92,7 +125,7 @@ __device__ __forceinline__ void atm_sweep(const float4 *se, const float4 *sq, in
             const float cx = eb.x - ea.x, cy = eb.y - ea.y, cz = eb.z - ea.z;
             const float C = cx * cx + cy * cy + cz * cz;
             if (C <= rc2) {
-                const AtmV v = atm_derivs(qa, sq[b], C);
+                const AtmV v = SW ? atm_derivs_sw(qa, sq[b], C, sA, dA, rc2, sw_iw) : atm_derivs(qa, sq[b], C);
                 const float tx = v.vC * cx, ty = v.vC * cy, tz = v.vC * cz;
                 ax += tx - v.vA * ea.x;
                 ay += ty - v.vA * ea.y;
@@ -119,17 +152,20 @@ __device__ __forceinline__ void atm_sweep(const float4 *se, const float4 *sq, in
 // fixed-point atomic per contribution (rare at liquid densities); each
 // contribution is scaled by sc first (1 keeps the units of 2 sign nu, and
 // multiplying by 1 is exact)
+template <bool SW = false>
 __device__ __forceinline__ void atm_pairs_slow(const AtmParams &p, const float4 *se, const float4 *sq, int m, int lane, float rc2,
                                float &gx, float &gy, float &gz, float sc = 1.0f) {
     for (int a = lane; a < m; a += 32) {
         const float4 ea = se[a], qa = sq[a];
+        float sA = 1.f, dA = 0.f;
+        if (SW) sw_eval(qa.x, rc2, p.sw_iw, sA, dA);
         unsigned long long *acca = p.acc + 3 * (size_t)(__float_as_int(ea.w) >> 6);
         for (int b = a + 1; b < m; b++) {
             const float4 eb = se[b];
             const float cx = eb.x - ea.x, cy = eb.y - ea.y, cz = eb.z - ea.z;
             const float C = cx * cx + cy * cy + cz * cz;
             if (C > rc2) continue;
-            const AtmV t = atm_derivs(qa, sq[b], C);
+            const AtmV t = SW ? atm_derivs_sw(qa, sq[b], C, sA, dA, rc2, p.sw_iw) : atm_derivs(qa, sq[b], C);
             gx += t.vA * ea.x + t.vB * eb.x;
             gy += t.vA * ea.y + t.vB * eb.y;
             gz += t.vA * ea.z + t.vB * eb.z;
@@ -202,6 +238,7 @@ __device__ __forceinline__ void atm_vertex(const AtmParams &p, int i, const floa
 // zeros.  With m > 32 the plain pair loop adds every share, scaled by sc, to
 // the accumulators itself, returns ax = ay = az = 0 and the lane's part of
 // the vertex share in (gx, gy, gz).  Units: 2 sign nu.
+template <bool SW>
 __device__ __forceinline__ void atm_vertex_shares(const AtmParams &p, const float4 *se, const float4 *sq, int m, int lane,
                                                   float rc2, float sc, float &ax, float &ay, float &az, float &gx,
                                                   float &gy, float &gz) {
@@ -213,12 +250,12 @@ __device__ __forceinline__ void atm_vertex_shares(const AtmParams &p, const floa
             const int g = lane >> 4, li = lane & 15;
             const int h1 = (half + 1) / 2;                     // rounds of the lower half-warp
             const int d_first = g ? h1 + 1 : 1, d_last = g ? half : h1;
-            atm_sweep(se, sq, m, li, 16 * g, d_first, d_last, h1, rc2, ax, ay, az, ea);
+            atm_sweep<SW>(se, sq, m, li, 16 * g, d_first, d_last, h1, rc2, ax, ay, az, ea, p.sw_iw);
             ax += __shfl_xor_sync(0xffffffffu, ax, 16);
             ay += __shfl_xor_sync(0xffffffffu, ay, 16);
             az += __shfl_xor_sync(0xffffffffu, az, 16);
         } else {
-            atm_sweep(se, sq, m, lane, 0, 1, half, half, rc2, ax, ay, az, ea);
+            atm_sweep<SW>(se, sq, m, lane, 0, 1, half, half, rc2, ax, ay, az, ea, p.sw_iw);
         }
         if (lane < m) {
             gx = -ax;
@@ -228,7 +265,7 @@ __device__ __forceinline__ void atm_vertex_shares(const AtmParams &p, const floa
             ax = ay = az = 0.f;
         }
     } else {
-        atm_pairs_slow(p, se, sq, m, lane, rc2, gx, gy, gz, sc);
+        atm_pairs_slow<SW>(p, se, sq, m, lane, rc2, gx, gy, gz, sc);
     }
 }
 

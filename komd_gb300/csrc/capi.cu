@@ -369,6 +369,16 @@ int validate(const komd_config *c, Grid &g) {
     if (!(c->delta_t > 0)) return fail(KOMD_ERR_ARG, "delta_t must be > 0");
     if (c->precision != KOMD_FP32 && c->precision != KOMD_FP64) return fail(KOMD_ERR_ARG, "bad precision");
     if (c->skin < 0) return fail(KOMD_ERR_ARG, "skin must be >= 0");
+    if (c->switch_width < 0) return fail(KOMD_ERR_ARG, "switch_width must be >= 0");
+    if (c->switch_width > 0) {
+        // the labelled switched-cutoff option lives on the half-list Verlet path
+        if (!uses_verlet(*c))
+            return fail(KOMD_ERR_ARG, "switch_width > 0 needs the Verlet path (skin > 0, FP32, FULL ATM, CORRECT virial, no FENE)");
+        if (c->terms & (KOMD_TERM_LIMIT | KOMD_TERM_FENE | KOMD_TERM_ATM2B | KOMD_TERM_TABULATED | KOMD_TERM_ATM_SURROGATE | KOMD_TERM_BONDED))
+            return fail(KOMD_ERR_ARG, "switch_width > 0 covers LJ and exact ATM only (no Limit, FENE, ATM2B, tabulated, learned or bonded terms)");
+        if ((lj && !(c->switch_width < c->cutoff)) || (atm && !(c->switch_width < c->cutoff_3b)))
+            return fail(KOMD_ERR_ARG, "switch_width must be below each cutoff");
+    }
     if (uses_verlet(*c)) {
         const double rl = std::max(lj ? c->cutoff : 0.0, atm ? c->cutoff_3b : 0.0) + c->skin;
         if (c->cell_size < rl)

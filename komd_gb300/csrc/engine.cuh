@@ -161,6 +161,8 @@ struct PairParams {
     float eps0, sig0;
     float lj_fscalef;          // ATM2B force factor (1 without ATM2B), force path only
     double lj_fscale;
+    int sw;                    // switched cutoff (komd_config::switch_width > 0)
+    float sw_rc2, sw_iw;       // cutoff^2 and 1 / (cutoff^2 - (cutoff - width)^2)
 };
 
 struct AtmParams {
@@ -178,7 +180,25 @@ struct AtmParams {
     int atm_direct;            // COMPAT + direct: no virial contribution
     double *e_site;            // measure: per-site V/3 sums (site order), optional
     unsigned long long *acc;   // k_atm_s: 3 fixed-point force sums per slot (2^-32 units)
+    int sw;                    // switched cutoff (komd_config::switch_width > 0)
+    float sw_rc2, sw_iw;       // cutoff_3b^2 and 1 / (cutoff_3b^2 - (cutoff_3b - width)^2)
 };
+
+// The switched-cutoff option (komd_config::switch_width): the C1 smoothstep
+// S = t^2 (3 - 2t) of the squared distance x, t = (rc^2 - x) * iw clamped to
+// [0, 1] (iw = 1 / (rc^2 - rs^2)), and dS/dx = -6 t (1 - t) iw.
+__host__ __device__ inline void sw_eval(float x, float rc2, float iw, float &S, float &dS) {
+    float t = (rc2 - x) * iw;
+    t = t < 0.f ? 0.f : (t > 1.f ? 1.f : t);
+    S = t * t * (3.0f - 2.0f * t);
+    dS = -6.0f * t * (1.0f - t) * iw;
+}
+inline void sw_params(double rc, double width, int &on, float &rc2, float &iw) {
+    on = width > 0 ? 1 : 0;
+    const double rs = rc - width;
+    rc2 = (float)(rc * rc);
+    iw = on ? (float)(1.0 / (rc * rc - rs * rs)) : 0.f;
+}
 
 // TemperatureSensor's conversion (TemperatureSensor.cpp:44-47) in SciValue
 // arithmetic (math/SciValue.{h,cpp}): mantissas normalised into (0.1, 10) by

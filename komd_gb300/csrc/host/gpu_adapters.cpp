@@ -59,6 +59,17 @@ komd_config GpuLinkedCells::engineConfig(const Configuration &c, bool device_the
     k.skin = c.gpu_skin;
     k.temperature_target = c.temperature;
     k.thermostat = device_thermostat ? 1 : 0;
+    if (c.gpu_switch_width > 0) {
+        // the switched-cutoff option covers LJ and exact ATM: the always-registered
+        // FENE and Limit functors must have nothing to do (one site per molecule,
+        // an inactive limit), and are left out of the engine's terms
+        for (const Component &comp : Registry::instance->components())
+            if (comp.sites.size() > 1)
+                throw std::runtime_error("gpu_switch_width needs single-site components (FENE acts on multi-site ones)");
+        if (c.limit_factor < 1e29) throw std::runtime_error("gpu_switch_width needs an inactive Limit (limit >= 1e29)");
+        k.terms &= ~(KOMD_TERM_FENE | KOMD_TERM_LIMIT);
+        k.switch_width = c.gpu_switch_width;
+    }
     return k;
 }
 
@@ -246,26 +257,6 @@ double GpuViscositySensor::integrate(const std::vector<std::vector<double>> &ser
     }
     return sum / ndims;
 }
-
-namespace {
-// SciValue (math/SciValue.{h,cpp}): mantissa normalised into (0.1, 10) by /10
-// and *10 steps, products renormalised, converted as m * pow(10, e)
-struct Sci {
-    double m;
-    long long e;
-    Sci(double mm, long long ee) : m(mm), e(ee) { norm(); }
-    explicit Sci(double v) : m(v), e(0) { if (v != 0.0) norm(); }
-    void norm() {
-        double a = std::fabs(m);
-        while (a >= 10.0) { m /= 10.0; e += 1; a = std::fabs(m); }
-        while (a <= 0.1) { m *= 10.0; e -= 1; a = std::fabs(m); }
-    }
-    Sci operator*(const Sci &o) const { return Sci(m * o.m, e + o.e); }
-    Sci operator/(const Sci &o) const { return Sci(m / o.m, e - o.e); }
-    Sci operator*(double o) const { return *this * Sci(o); }
-    double value() const { return m * std::pow(10, e); }
-};
-}  // namespace
 
 void GpuViscositySensor::write(uint64_t simstep) {
     // ViscositySensor::write (ViscositySensor.cpp:37-89): factor =

@@ -4,6 +4,7 @@
 #include <fstream>
 #include <iomanip>
 #include <iostream>
+#include <random>
 #include <sstream>
 #include <stdexcept>
 
@@ -158,6 +159,7 @@ bool FileInput::readFile(const std::string &filename) {
             else if (var == "gpu_skin") c.gpu_skin = std::stod(v);
             else if (var == "gpu_device") c.gpu_device = std::stoi(v);
             else if (var == "gpu_vtk") c.gpu_vtk = std::stoi(v) != 0;
+            else if (var == "gpu_switch_width") c.gpu_switch_width = std::stod(v);
             if (!ok) { std::cerr << "invalid value for " << var << ": " << v << std::endl; return false; }
         }
         // unknown tokens are skipped, as in the reference
@@ -267,6 +269,7 @@ bool CheckpointIO::loadCheckpoint() {
         // A trailing newline ends the file like none (the reference re-reads
         // the last site in that case); partial lines are ignored.
         Molecule mol;
+        next_molecule_id();   // the reference's loader default-constructs one molecule per file
         bool have = false;
         std::string line;
         while (std::getline(file, line)) {
@@ -278,6 +281,7 @@ bool CheckpointIO::loadCheckpoint() {
             if (have && id != mol.id) {
                 container->addMolecule(mol);
                 mol = Molecule();
+                next_molecule_id();   // ... and one per further molecule (then sets the file's id)
             }
             mol.id = id;
             have = true;
@@ -287,6 +291,77 @@ bool CheckpointIO::loadCheckpoint() {
         if (have) container->addMolecule(mol);
     }
     return true;
+}
+
+uint64_t next_molecule_id() {
+    static uint64_t next = 1;   // id 0 went to the reference's Molecule::INVALID
+    return next++;
+}
+
+namespace {
+// the Euler rotation of the generator (PhasespaceGenerator.cpp:12-24), term by
+// term in the reference's order, so that positions round alike
+d3 euler_rotate(double a, double b, double g, const d3 &q) {
+    const double ca = std::cos(a), sa = std::sin(a), cb = std::cos(b), sb = std::sin(b), cg = std::cos(g),
+                 sg = std::sin(g);
+    d3 out;
+    out[0] = cb * cg * q[0] + (sa * sb * cg - ca * sg) * q[1] + (ca * sb * cg + sa * sg) * q[2];
+    out[1] = cb * sg * q[0] + (sa * sb * sg + ca * cg) * q[1] + (ca * sb * sg - sa * cg) * q[2];
+    out[2] = -sb * q[0] + sa * cb * q[1] + ca * cb * q[2];
+    return out;
+}
+
+// one Maxwell-Boltzmann velocity for a molecule of mass m at temperature T (K)
+// (PhasespaceGenerator.cpp:85-95): three standard normal draws, each call with
+// a fresh distribution on the static engine seeded 42, times
+// sqrt(T / m * kB / Da) (m/s) * 1e-2 (A/ps), the constants in SciValue arithmetic
+d3 maxwell_boltzmann(double T, double m) {
+    static std::default_random_engine rng(42);
+    static const double kb_over_da = (Sci(1.380649, -23) / Sci(1.66053906892, -27)).value();
+    double sd = std::sqrt((T / m) * kb_over_da);
+    sd *= Sci(1.0, -2).value();
+    std::normal_distribution<double> normal(0, 1);
+    d3 v;
+    v[0] = normal(rng);
+    v[1] = normal(rng);
+    v[2] = normal(rng);
+    for (int d = 0; d < 3; d++) v[d] *= sd;
+    return v;
+}
+}  // namespace
+
+void PhasespaceGenerator::generate() {
+    auto cfg = Registry::instance->configuration();
+    auto container = Registry::instance->moleculeContainer();
+    auto &components = Registry::instance->components();
+    d3 size;
+    for (int d = 0; d < 3; d++) size[d] = cfg->domainHigh[d] - cfg->domainLow[d];
+    const double num = cfg->density * (size[0] * size[1] * size[2]);
+    const double per_dim = std::pow(num, 1. / 3.);
+    d3 spacing;
+    for (int d = 0; d < 3; d++) spacing[d] = size[d] / per_dim;
+    static std::default_random_engine rng(43);
+    std::uniform_real_distribution<double> uniform(0, M_PI * 2);
+    const double j_to_internal = Sci(6.022140754, 22).value();   // Constants::conv_J_Ei
+    for (const auto &[begin, end, cid] : cfg->phasespace_gen_regions) {
+        const Component &comp = components[cid];
+        for (double z = begin[2] + 0.5; z < end[2]; z += spacing[2])
+            for (double y = begin[1] + 0.5; y < end[1]; y += spacing[1])
+                for (double x = begin[0] + 0.5; x < end[0]; x += spacing[0]) {
+                    Molecule mol;
+                    mol.id = next_molecule_id();
+                    const double alpha = uniform(rng), beta = uniform(rng), gamma = uniform(rng);
+                    double total_mass = 0;
+                    for (const SiteDesc &site : comp.sites) total_mass += site.mass;
+                    const d3 v = maxwell_boltzmann(cfg->temperature, total_mass);
+                    for (const SiteDesc &site : comp.sites) {
+                        const d3 q = euler_rotate(alpha, beta, gamma, site.r);
+                        const d3 pos{x + q[0], y + q[1], z + q[2]};
+                        mol.addSite(site.epsilon * j_to_internal, site.sigma, site.mass, pos, v);
+                    }
+                    container->addMolecule(mol);
+                }
+    }
 }
 
 // ---------------------------------------------------------------------------

@@ -13,6 +13,7 @@
 #pragma once
 
 #include <array>
+#include <cmath>
 #include <cstdint>
 #include <limits>
 #include <memory>
@@ -91,6 +92,9 @@ struct Configuration {
     int gpu_device = 0;                             // gpu_device <int>
     bool gpu_atm2b_physical = false;                // gpu_atm2b physical: ATM2B factor from the loaded density
     bool gpu_vtk = false;                           // gpu_vtk 1: VTK_Output_<step>.vtu as a USE_VTK build writes
+    double gpu_switch_width = 0.0;                  // gpu_switch_width <float>: the labelled switched-cutoff
+                                                    // option (komd_config::switch_width); 0 = the reference's
+                                                    // truncated potentials
 };
 
 struct SiteDesc {
@@ -111,6 +115,44 @@ struct Molecule {
     }
     d3 centerOfMass() const;
 };
+
+// SciValue (math/SciValue.{h,cpp}): mantissa normalised into (0.1, 10) by /10
+// and *10 steps, products renormalised, converted as m * pow(10, e).  The
+// loops are bounded (no finite double needs 400 steps; zero, NaN and inf come
+// back at once) where the reference's would not end on an infinite mantissa.
+struct Sci {
+    double m;
+    long long e;
+    Sci(double mm, long long ee) : m(mm), e(ee) { norm(); }
+    explicit Sci(double v) : m(v), e(0) { if (v != 0.0) norm(); }
+    void norm() {
+        double a = std::fabs(m);
+        if (!(a <= 1.7976931348623157e308) || a == 0.0) return;
+        for (int k = 0; k < 400 && a >= 10.0; k++) { m /= 10.0; e += 1; a = std::fabs(m); }
+        for (int k = 0; k < 400 && a <= 0.1; k++) { m *= 10.0; e -= 1; a = std::fabs(m); }
+    }
+    Sci operator*(const Sci &o) const { return Sci(m * o.m, e + o.e); }
+    Sci operator/(const Sci &o) const { return Sci(m / o.m, e - o.e); }
+    Sci operator*(double o) const { return *this * Sci(o); }
+    double value() const { return m * std::pow(10, e); }
+};
+
+// Molecule::NEXT_ID of the reference (molecule/Molecule.cpp:8-10): every
+// default-constructed molecule takes the next id (0 went to Molecule::INVALID);
+// the checkpoint loader takes ids as KoMD's does and then sets the file's,
+// the phase-space generator keeps them.
+uint64_t next_molecule_id();
+
+// PhasespaceGenerator (util/PhasespaceGenerator.cpp:27-95): molecules of the
+// ps_gen_region entries' components on a grid of spacing L / (rho V)^(1/3)
+// from begin + 0.5, each rotated by random Euler angles (uniform in [0, 2 pi),
+// default_random_engine seeded 43) and given one Maxwell-Boltzmann velocity
+// (normal draws from a default_random_engine seeded 42, std dev
+// sqrt(T / M kB / Da) in A/ps).  Both engines are static, as in the reference:
+// they run on across calls.
+namespace PhasespaceGenerator {
+void generate();
+}
 
 // --- plugin interfaces ------------------------------------------------------
 class MoleculeContainer {

@@ -1,12 +1,16 @@
 // main.cpp -- the `komd` executable: KoMD's stock main (src/main.cpp:37-99)
-// on the GB300 engine.  Usage: komd <input file> [--fused]
+// on the GB300 engine.  Usage: komd <input file> [--fused | --phasespace <out.ps>]
 //   --fused   advance write_freq steps per engine call (CUDA graph replay with
 //             the thermostat on the device); log lines at write steps only
+//   --phasespace <out.ps>   write the initial phase space (checkpoint files and
+//             ps_gen_region molecules) with 17 significant digits and stop,
+//             before any GPU work
 // Input files are KoMD's; the phase space comes from checkpoint_file entries
-// (ps_gen_region inputs are rejected: the phase-space generator is not part of
-// this engine).  The IBI and IBI_Reload plugins run (ibi.h); AdResS and the
+// and ps_gen_region entries (PhasespaceGenerator, as main.cpp:70-71 orders
+// them).  The IBI and IBI_Reload plugins run (ibi.h); AdResS and the
 // FENE and displacement sensors are not available and are reported, not
 // silently skipped.
+#include <cstdio>
 #include <cstring>
 #include <iostream>
 #include <stdexcept>
@@ -22,16 +26,17 @@ int main(int argc, char **argv) {
         return 0;
     }
     bool fused = false;
-    for (int a = 2; a < argc; a++)
+    const char *ps_out = nullptr;
+    for (int a = 2; a < argc; a++) {
         if (std::strcmp(argv[a], "--fused") == 0) fused = true;
+        if (std::strcmp(argv[a], "--phasespace") == 0 && a + 1 < argc) ps_out = argv[++a];
+    }
     try {
         Registry::instance = std::make_unique<Registry>();
         Registry::instance->configuration_ptr() = std::make_shared<Configuration>();
         if (!FileInput::readFile(argv[1])) return 0;
         auto cfg = Registry::instance->configuration();
         if (cfg->enable_one_cell) throw std::runtime_error("not supported anymore");
-        if (!cfg->phasespace_gen_regions.empty())
-            throw std::runtime_error("ps_gen_region: the phase-space generator is not available; use checkpoint_file");
         if (cfg->ADR_enable) throw std::runtime_error("the AdResS plugin is not available in this engine");
         const bool plugins = cfg->IBI_enable || cfg->IBI_reload_enable;
         if (plugins && fused)
@@ -50,6 +55,22 @@ int main(int argc, char **argv) {
         if (cfg->enable_3b) Registry::instance->forceFunctors3b().push_back(std::make_shared<GpuATM>());
         Registry::instance->integrators().push_back(std::make_unique<GpuIntegrator>());
         if (!CheckpointIO::loadCheckpoint()) return 0;
+        PhasespaceGenerator::generate();
+        if (ps_out) {   // the .ps layout of CheckpointIO::writeCheckpoint, full precision
+            FILE *f = std::fopen(ps_out, "w");
+            if (!f) throw std::runtime_error(std::string("cannot write ") + ps_out);
+            bool first = true;
+            for (const Molecule &m : container->molecules())
+                for (size_t q = 0; q < m.r.size(); q++) {
+                    std::fprintf(f, "%s%llu\t%.17g %.17g %.17g\t%.17g %.17g %.17g\t%.17g %.17g %.17g", first ? "" : "\n",
+                                 (unsigned long long)m.id, m.r[q][0], m.r[q][1], m.r[q][2], m.v[q][0], m.v[q][1],
+                                 m.v[q][2], m.mass[q], m.eps[q], m.sig[q]);
+                    first = false;
+                }
+            std::fclose(f);
+            Registry::instance = nullptr;
+            return 0;
+        }
         container->init();
 
         // measurements (main.cpp:74-85)

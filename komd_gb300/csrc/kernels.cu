@@ -624,14 +624,26 @@ __global__ void __launch_bounds__(kBlock) k_atm_q(AtmParams p) {
         const float t1 = A + B - C, t2 = A - B + C, t3 = B + C - A;
         const float u = t2 * t3, v = t1 * t3, w = t1 * t2;
         const float P = t1 * u;
-        const float vA = s5 * (-1.5f * B * C + 0.375f * (u + v - w) - 0.9375f * P * qa.y);
-        const float vB = s5 * (-1.5f * A * C + 0.375f * (u - v + w) - 0.9375f * P * qb.y);
+        float vA = s5 * (-1.5f * B * C + 0.375f * (u + v - w) - 0.9375f * P * qa.y);
+        float vB = s5 * (-1.5f * A * C + 0.375f * (u - v + w) - 0.9375f * P * qb.y);
+        float vC = s5 * (-1.5f * A * B + 0.375f * (-u + v + w) - 0.9375f * P * (wc * wc));
+        float Vn = s2 * sv * (1.0f + 0.375f * P * s2);   // V / nu
+        if (p.sw) {   // switched cutoff: V Sa Sb Sc and its derivatives in A, B, C
+            float Sa, dSa, Sb, dSb, Sc, dSc;
+            sw_eval(A, p.sw_rc2, p.sw_iw, Sa, dSa);
+            sw_eval(B, p.sw_rc2, p.sw_iw, Sb, dSb);
+            sw_eval(C, p.sw_rc2, p.sw_iw, Sc, dSc);
+            const float sbc = Sb * Sc, sac = Sa * Sc, sab = Sa * Sb;
+            vA = sbc * (vA * Sa + Vn * dSa);
+            vB = sac * (vB * Sb + Vn * dSb);
+            vC = sab * (vC * Sc + Vn * dSc);
+            Vn = Vn * Sa * sbc;
+        }
         gx += vA * ea.x + vB * eb.x;
         gy += vA * ea.y + vB * eb.y;
         gz += vA * ea.z + vB * eb.z;
         if (MEASURE) {
-            const float vC = s5 * (-1.5f * A * B + 0.375f * (-u + v + w) - 0.9375f * P * (wc * wc));
-            m_e += s2 * sv * (1.0f + 0.375f * P * s2) * (1.0f / 3.0f);
+            m_e += Vn * (1.0f / 3.0f);
             m_t++;
             float wt;
             if (p.virial_compat) {
@@ -1537,6 +1549,7 @@ PairParams pair_params(Engine &e) {
     p.rebuild_count = e.rebuild_count;
     p.eps0 = e.eps0;
     p.sig0 = e.sig0;
+    sw_params(e.cfg.cutoff, e.cfg.switch_width, p.sw, p.sw_rc2, p.sw_iw);
     return p;
 }
 
@@ -1745,6 +1758,7 @@ AtmParams atm_params(const Engine &e) {
     p.atm_direct = e.cfg.atm_direct;
     p.e_site = e.atm_esite;
     p.acc = e.atm_acc;
+    sw_params(e.cfg.cutoff_3b, e.cfg.switch_width, p.sw, p.sw_rc2, p.sw_iw);
     return p;
 }
 

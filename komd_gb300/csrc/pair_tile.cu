@@ -521,12 +521,18 @@ __device__ __forceinline__ int lj_site(const PairParams &p, int i, int lane, uns
                         ee = sei * sej[u];
                     }
                     const float lj6 = x * x * x;
-                    const float fac0 = 24.0f * ee * (2.0f * lj6 * lj6 - lj6) * inv;
+                    float fac0 = 24.0f * ee * (2.0f * lj6 * lj6 - lj6) * inv;
+                    float usw = 1.0f;
+                    if (p.sw) {   // switched cutoff: U S, force fac S - 2 U dS/dx
+                        float dS;
+                        sw_eval(r2, p.sw_rc2, p.sw_iw, usw, dS);
+                        fac0 = fac0 * usw - 8.0f * ee * (lj6 * lj6 - lj6) * dS;
+                    }
                     const float fac = MEASURE ? fac0 : fac0 * p.lj_fscalef;   // ATM2B factor
                     fx += dx * fac; fy += dy * fac; fz += dz * fac;
                     if (MEASURE) {
                         const float gx = dx * fac, gy = dy * fac, gz = dz * fac;
-                        m_u += 2.0f * ee * (lj6 * lj6 - lj6);
+                        m_u += 2.0f * ee * (lj6 * lj6 - lj6) * usw;
                         m_pairs += 0.5f;
                         m_w[0] += 0.5f * dx * gx;
                         m_w[1] += 0.25f * (dx * gy + dy * gx);
@@ -684,7 +690,7 @@ __device__ __forceinline__ void half_row_load(const PairParams &p, int i, int la
     h.cell = p.slot_cell[i];
 }
 
-template <bool UNIFORM>
+template <bool UNIFORM, bool SW>
 __device__ __forceinline__ void lj_half(const PairParams &p, int i, const HalfRow &h, int lane, unsigned lt, float rc2,
                                         float rc3sq, float4 *se, float4 *sq, float4 *sr, int capa, int capr,
                                         int &m_out, int &k_out, float &fx, float &fy, float &fz) {
@@ -700,7 +706,7 @@ __device__ __forceinline__ void lj_half(const PairParams &p, int i, const HalfRo
         unsigned e[2];
         float4 o[2], pj[2];
         float sej[2];
-        if (k0 == 0) {   // the prefetched first 64 entries
+        if (k0 == 0) {   // the first 64 entries, read with the count
             e[0] = lane < cnt ? h.e0 : 0xffffffffu;
             e[1] = 32 + lane < cnt ? h.e1 : 0xffffffffu;
         } else {
@@ -742,7 +748,12 @@ __device__ __forceinline__ void lj_half(const PairParams &p, int i, const HalfRo
                         ee = sei * sej[u];
                     }
                     const float lj6 = x * x * x;
-                    const float fac = 24.0f * ee * (2.0f * lj6 * lj6 - lj6) * inv * p.lj_fscalef;   // ATM2B factor
+                    float fac = 24.0f * ee * (2.0f * lj6 * lj6 - lj6) * inv * p.lj_fscalef;   // ATM2B factor
+                    if (SW) {   // switched cutoff (no ATM2B with it): U S, force fac S - 2 U dS/dx
+                        float S, dS;
+                        sw_eval(r2, p.sw_rc2, p.sw_iw, S, dS);
+                        fac = fac * S - 8.0f * ee * (lj6 * lj6 - lj6) * dS;
+                    }
                     gx = dx * fac; gy = dy * fac; gz = dz * fac;
                     fx += gx; fy += gy; fz += gz;
                 }
@@ -774,7 +785,7 @@ __device__ __forceinline__ void lj_half(const PairParams &p, int i, const HalfRo
     k_out = k;
 }
 
-template <bool UNIFORM>
+template <bool UNIFORM, bool SW>
 __global__ void __launch_bounds__(256, 4) k_lj_atm_half(PairParams p, AtmParams a, float sa, int n, int per) {
     extern __shared__ float4 s_dyn[];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -789,10 +800,10 @@ __global__ void __launch_bounds__(256, 4) k_lj_atm_half(PairParams p, AtmParams 
         half_row_load(p, i, lane, cur);
         int m, k;
         float fx, fy, fz;
-        lj_half<UNIFORM>(p, i, cur, lane, lt, rc2, rc3sq, se, sq, sr, capa, capr, m, k, fx, fy, fz);
+        lj_half<UNIFORM, SW>(p, i, cur, lane, lt, rc2, rc3sq, se, sq, sr, capa, capr, m, k, fx, fy, fz);
         __syncwarp();
         float ax, ay, az, gx, gy, gz;
-        atm_vertex_shares(a, se, sq, m, lane, rc3f, sa, ax, ay, az, gx, gy, gz);
+        atm_vertex_shares<SW>(a, se, sq, m, lane, rc3f, sa, ax, ay, az, gx, gy, gz);
         // every partner: LJ reaction + ATM share (force units), one fixed-point add per component
         const int tot = m + k;
         for (int L = lane; L < tot; L += 32) {
@@ -827,6 +838,14 @@ __global__ void __launch_bounds__(256, 4) k_lj_atm_half(PairParams p, AtmParams 
     }
 }
 
+template <bool UNIFORM, bool SW>
+static void launch_half(const PairParams &p, const AtmParams &a, float sa, int n, int per, int grid, size_t sm,
+                        cudaStream_t st) {
+    if (sm > 48 * 1024)
+        cudaFuncSetAttribute(k_lj_atm_half<UNIFORM, SW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_lj_atm_half<UNIFORM, SW><<<grid, 256, sm, st>>>(p, a, sa, n, per);
+}
+
 // shared memory of the half-list pass: per warp nl_cap staged triplet
 // partners (se, sq) and vl_cap partners' reactions (sr)
 static size_t lj_atm_half_smem(const Engine &e) {
@@ -838,7 +857,7 @@ static size_t lj_atm_half_smem(const Engine &e) {
 // tabulated term) and its staging fits the shared memory of four blocks
 bool lj_atm_half(const Engine &e) {
     if (e.cfg.terms & (KOMD_TERM_LIMIT | KOMD_TERM_FENE | KOMD_TERM_TABULATED)) return false;
-    return lj_atm_half_smem(e) <= 56 * 1024;
+    return lj_atm_half_smem(e) <= 56 * 1024 || e.cfg.switch_width > 0;   // the switch runs here only
 }
 
 int vlist_grid(const Engine &e) { return (int)((e.n + 7) / 8); }
@@ -903,12 +922,12 @@ void launch_lj_atm(Engine &e, cudaStream_t st) {
     if (lj_atm_half(e)) {
         const size_t sm = lj_atm_half_smem(e);
         const float sa = (float)(2.0 * a.sign * a.nu);   // share units (2 sign nu) to force units
-        if (e.uniform) {
-            if (sm > 48 * 1024) cudaFuncSetAttribute(k_lj_atm_half<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-            k_lj_atm_half<true><<<grid, 256, sm, st>>>(p, a, sa, (int)e.n, per);
+        if (p.sw) {
+            if (e.uniform) launch_half<true, true>(p, a, sa, (int)e.n, per, grid, sm, st);
+            else launch_half<false, true>(p, a, sa, (int)e.n, per, grid, sm, st);
         } else {
-            if (sm > 48 * 1024) cudaFuncSetAttribute(k_lj_atm_half<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-            k_lj_atm_half<false><<<grid, 256, sm, st>>>(p, a, sa, (int)e.n, per);
+            if (e.uniform) launch_half<true, false>(p, a, sa, (int)e.n, per, grid, sm, st);
+            else launch_half<false, false>(p, a, sa, (int)e.n, per, grid, sm, st);
         }
         return;
     }

@@ -51,7 +51,7 @@ class KomdConfig(C.Structure):
         ("rdf_dr", C.c_double), ("terms", C.c_uint32), ("precision", C.c_int32), ("atm_sign", C.c_int32),
         ("atm_enum", C.c_int32), ("virial_mode", C.c_int32), ("atm_direct", C.c_int32), ("lj_bins", C.c_int32),
         ("atm_list_cap", C.c_int32), ("skin", C.c_double), ("temperature_target", C.c_double),
-        ("thermostat", C.c_int32),
+        ("thermostat", C.c_int32), ("switch_width", C.c_double),
     ]
 
 
@@ -160,7 +160,7 @@ def make_config(low, high, cell_size, cutoff=2.5, cutoff_3b=None, nu=0.0, dt=0.0
                 precision=FP32, atm_sign=ATM_SIGN_REFERENCE, atm_enum=ATM_ENUM_COMPAT, virial_mode=VIRIAL_COMPAT,
                 atm_direct=1, stiffness=30.0, limit=1e30, bond_k=0.0, bond_r0=1.0, angle_k=0.0, angle_theta0=0.0,
                 max_sigma=1.0, rdf_max=0.0, rdf_dr=0.0, lj_bins=100, atm_list_cap=0, skin=0.0,
-                thermostat=0, temperature_target=0.0) -> KomdConfig:
+                thermostat=0, temperature_target=0.0, switch_width=0.0) -> KomdConfig:
     c = KomdConfig()
     for d in range(3):
         c.domain_low[d] = float(low[d])
@@ -175,6 +175,7 @@ def make_config(low, high, cell_size, cutoff=2.5, cutoff_3b=None, nu=0.0, dt=0.0
     c.virial_mode, c.atm_direct, c.lj_bins, c.atm_list_cap = int(virial_mode), int(atm_direct), int(lj_bins), int(atm_list_cap)
     c.skin = float(skin)
     c.thermostat, c.temperature_target = int(thermostat), float(temperature_target)
+    c.switch_width = float(switch_width)
     return c
 
 

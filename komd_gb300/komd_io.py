@@ -18,7 +18,7 @@ from __future__ import annotations
 
 import math
 from dataclasses import dataclass, field
-from typing import Dict, List, Tuple
+from typing import Dict, List, Optional, Sequence, Tuple
 
 import numpy as np
 
@@ -115,8 +115,11 @@ def read_input(path: str) -> InputFile:
         return parse_input(fh.read())
 
 
-def format_input(values: dict, checkpoint: str, comps: List[Tuple[int, float, float, float]]) -> str:
-    """Input file text without a trailing newline."""
+def format_input(values: dict, checkpoint: Optional[str], comps: List[tuple],
+                 regions: Sequence[tuple] = ()) -> str:
+    """Input file text without a trailing newline.  comps: (cid, eps in J,
+    sigma, mass[, site position]) per COMP line; regions: (begin xyz, end xyz,
+    cid) per ps_gen_region line; checkpoint None: no checkpoint_file line."""
     out = []
     for k, v in values.items():
         if isinstance(v, (tuple, list)):
@@ -125,9 +128,14 @@ def format_input(values: dict, checkpoint: str, comps: List[Tuple[int, float, fl
             out.append(f"{k} {v!r}")
         else:
             out.append(f"{k} {v}")
-    out.append(f"checkpoint_file {checkpoint} 0 0 0")
-    for cid, eps_j, sig, mass in comps:
-        out.append(f"COMP {cid} {eps_j!r} {sig!r} {mass!r} 0 0 0")
+    if checkpoint is not None:
+        out.append(f"checkpoint_file {checkpoint} 0 0 0")
+    for begin, end, cid in regions:
+        out.append("ps_gen_region " + " ".join(repr(float(x)) for x in (*begin, *end)) + f" {int(cid)}")
+    for c in comps:
+        cid, eps_j, sig, mass = c[:4]
+        r = c[4] if len(c) > 4 else (0.0, 0.0, 0.0)
+        out.append(f"COMP {cid} {eps_j!r} {sig!r} {mass!r} " + " ".join(repr(float(x)) for x in r))
     return "\n".join(out)
 
 

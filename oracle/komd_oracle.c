@@ -395,6 +395,25 @@ void kor_pair_table(int64_t n_pairs, const int64_t *pairs, const double *shifts,
 static double g_lj_fscale = 1.0;
 void kor_set_lj_force_scale(double s) { g_lj_fscale = s; }
 
+/* The switched-cutoff option (not in the reference; off unless set): the LJ
+ * pair energy and the ATM triplet energy are multiplied by the C1 smoothstep
+ * S(x) = t^2 (3 - 2 t), t = (rc^2 - x) / (rc^2 - rs^2) clamped to [0, 1], of
+ * the squared distance x (for ATM the product over the three sides), with
+ * rs = rc - width; forces are the exact gradients of the switched energies.
+ * width 0 keeps the reference's truncated potentials. */
+static double g_sw_lj = 0.0, g_sw_atm = 0.0;
+void kor_set_switch(double lj_width, double atm_width) { g_sw_lj = lj_width; g_sw_atm = atm_width; }
+
+/* S(x) and dS/dx for the switch from rs^2 to rc^2 */
+static void sw_eval(double x, double rc, double width, double *S, double *dS) {
+    const double rc2 = rc * rc, rs = rc - width, rs2 = rs * rs, w = rc2 - rs2;
+    double t = (rc2 - x) / w;
+    if (t >= 1.0) { *S = 1.0; *dS = 0.0; return; }
+    if (t <= 0.0) { *S = 0.0; *dS = 0.0; return; }
+    *S = t * t * (3.0 - 2.0 * t);
+    *dS = -6.0 * t * (1.0 - t) / w;
+}
+
 /* ATM2B::ATM2B (ATM2B.cpp:9-20): 1 - (2 nu rho) / (3 eps sig^6) with rho =
  * molecules / volume and eps, sig of the first site of component 0 (all
  * internal units). */
@@ -430,7 +449,13 @@ void kor_lj(const kor_grid *g, int64_t n_pairs, const int64_t *pairs, const doub
         const double sig2 = sigma * sigma;
         const double lj6 = pow(sig2 * invdr2, 3.0);
         const double lj12 = pow(lj6, 2.0);
-        const double fac = 24.0 * epsilon * (2.0 * lj12 - lj6) * invdr2;
+        double fac = 24.0 * epsilon * (2.0 * lj12 - lj6) * invdr2;
+        double swS = 1.0;
+        if (g_sw_lj > 0.0) {   /* switched cutoff: U S, force fac S - 2 U dS/dx */
+            double dS;
+            sw_eval(dr2, cutoff, g_sw_lj, &swS, &dS);
+            fac = fac * swS - 2.0 * (4.0 * epsilon * (lj12 - lj6)) * dS;
+        }
         double fo[3] = {dr[0] * fac, dr[1] * fac, dr[2] * fac};
         if (g_lj_fscale != 1.0)
             for (int d = 0; d < 3; d++) fo[d] = fo[d] * g_lj_fscale;
@@ -466,7 +491,7 @@ void kor_lj(const kor_grid *g, int64_t n_pairs, const int64_t *pairs, const doub
         /* sensor: ignore entries whose second side is a halo image */
         if (!shift_nonzero(sh1)) {
             const double rpos = sqrt(pow(dr[0], 2) + pow(dr[1], 2) + pow(dr[2], 2));
-            const double u = 4.0 * epsilon * (lj12 - lj6);
+            const double u = 4.0 * epsilon * (lj12 - lj6) * swS;
             u_total += u;
             if (uhist) {
                 const double fr = 24.0 * epsilon * (2.0 * lj12 - lj6) / rpos;
@@ -539,13 +564,19 @@ void kor_lj_cells(const kor_grid *g, const kor_cells *c, const double *r, const 
             const double sig2 = sigma * sigma;
             const double lj6 = pow(sig2 * invdr2, 3.0);
             const double lj12 = pow(lj6, 2.0);
-            const double fac = 24.0 * epsilon * (2.0 * lj12 - lj6) * invdr2;
+            double fac = 24.0 * epsilon * (2.0 * lj12 - lj6) * invdr2;
+            double swS = 1.0;
+            if (g_sw_lj > 0.0) {   /* switched cutoff (kor_set_switch) */
+                double dS;
+                sw_eval(dr2, cutoff, g_sw_lj, &swS, &dS);
+                fac = fac * swS - 2.0 * (4.0 * epsilon * (lj12 - lj6)) * dS;
+            }
             double fo[3] = {dr[0] * fac, dr[1] * fac, dr[2] * fac};
             if (g_lj_fscale != 1.0)
                 for (int d = 0; d < 3; d++) fo[d] = fo[d] * g_lj_fscale;
             if (dom0) for (int d = 0; d < 3; d++) atomic_addd(&f[3 * s0 + d], fo[d]);
             if (dom1) for (int d = 0; d < 3; d++) atomic_addd(&f[3 * s1 + d], -fo[d]);
-            if (dom1) u_total += 4.0 * epsilon * (lj12 - lj6);
+            if (dom1) u_total += 4.0 * epsilon * (lj12 - lj6) * swS;
         }
     }
     free(dc); free(cp); free(sp);
@@ -751,11 +782,25 @@ void kor_atm_vertex(const kor_grid *g, const kor_cells *c, const double *r, doub
                     const double q12 = d12[0] * d12[0] + d12[1] * d12[1] + d12[2] * d12[2];
                     if (q12 > cutoff2) continue;
                     const double a_ = sqrt(nb[u].q), b_ = sqrt(nb[v].q), c_ = sqrt(q12);
-                    const double v01 = kor_atm_comp_force(nu, a_, b_, c_);
-                    const double v02 = kor_atm_comp_force(nu, b_, a_, c_);
+                    double v01 = kor_atm_comp_force(nu, a_, b_, c_);
+                    double v02 = kor_atm_comp_force(nu, b_, a_, c_);
+                    double v12 = kor_atm_comp_force(nu, c_, a_, b_);
+                    double V = kor_atm_energy(nu, a_, b_, c_);
+                    if (g_sw_atm > 0.0) {
+                        /* switched: V Sa Sb Sc; (1/r) dV_sw/dr = S S S (1/r) dV/dr + V (prod of the
+                         * other two S) 2 dS/dx for each side.  comp_force is (1/r) dV/dr with the
+                         * reference's sign (the force adds +grad V) */
+                        double Sa, dSa, Sb, dSb, Sc, dSc;
+                        sw_eval(nb[u].q, cutoff, g_sw_atm, &Sa, &dSa);
+                        sw_eval(nb[v].q, cutoff, g_sw_atm, &Sb, &dSb);
+                        sw_eval(q12, cutoff, g_sw_atm, &Sc, &dSc);
+                        v01 = Sa * Sb * Sc * v01 + V * Sb * Sc * 2.0 * dSa;
+                        v02 = Sa * Sb * Sc * v02 + V * Sa * Sc * 2.0 * dSb;
+                        v12 = Sa * Sb * Sc * v12 + V * Sa * Sb * 2.0 * dSc;
+                        V = V * Sa * Sb * Sc;
+                    }
                     for (int d = 0; d < 3; d++) fi[d] += sgn * (nb[u].d[d] * v01 + nb[v].d[d] * v02);
-                    energy += kor_atm_energy(nu, a_, b_, c_) / 3.0;
-                    const double v12 = kor_atm_comp_force(nu, c_, a_, b_);
+                    energy += V / 3.0;
                     const double p01 = -v01, p02 = -v02, p12 = -v12;
                     const double *e01 = nb[u].d, *e02 = nb[v].d;
                     w[0] += (p01 * e01[0] * e01[0] + p02 * e02[0] * e02[0] + p12 * d12[0] * d12[0]) / 3.0;

@@ -119,6 +119,13 @@ void kor_pair_table(int64_t n_pairs, const int64_t *pairs, const double *shifts,
                     int64_t n_nodes, const double *xs, const double *ys, double lo, double hi, double *f);
 /* ATM2B: the force factor applied by kor_lj / kor_lj_cells while set (1 = LJ12_6) */
 void kor_set_lj_force_scale(double s);
+/* The switched-cutoff option (no reference counterpart; width 0 = off, the
+ * reference's truncated forms): LJ pair energies times S(r^2) from
+ * (cutoff - lj_width)^2 to cutoff^2, ATM triplet energies times the product
+ * of S over the three sides from (cutoff_3b - atm_width)^2 to cutoff_3b^2,
+ * S the C1 smoothstep in the squared distance; forces are the gradients.
+ * Applied by kor_lj, kor_lj_cells and kor_atm_vertex. */
+void kor_set_switch(double lj_width, double atm_width);
 double kor_atm2b_factor(double nu, double n_mol, double volume, double eps, double sig);
 /* kor_lj without a materialised pair list: the same entries in C08 order,
  * generated from the cells (no virial, no histograms). */

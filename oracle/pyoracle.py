@@ -92,6 +92,8 @@ def lib():
         L.kor_pair_table.restype = None
         L.kor_set_lj_force_scale.argtypes = [D]
         L.kor_set_lj_force_scale.restype = None
+        L.kor_set_switch.argtypes = [D, D]
+        L.kor_set_switch.restype = None
         L.kor_atm2b_factor.argtypes = [D, D, D, D, D]
         L.kor_atm2b_factor.restype = D
         L.kor_temperature.restype = D
@@ -123,7 +125,8 @@ class OracleSim:
 
     def __init__(self, sysm, cell_size, cutoff, dt=0.005, nu=0.0, cutoff_atm=None, limit=1e30,
                  stiffness=30.0, lj=True, atm=False, atm_mode="compat", atm_sign=ATM_SIGN_REFERENCE,
-                 fene=False, bonded=None, virial_mode=VIRIAL_COMPAT, lj_force_scale=1.0, table=None):
+                 fene=False, bonded=None, virial_mode=VIRIAL_COMPAT, lj_force_scale=1.0, table=None,
+                 switch_width=0.0):
         self.L = lib()
         self.r = np.ascontiguousarray(sysm.r, dtype=np.float64).copy()
         self.v = np.ascontiguousarray(sysm.v, dtype=np.float64).copy()
@@ -148,6 +151,9 @@ class OracleSim:
         self.atm_mode, self.atm_sign, self.virial_mode = atm_mode, atm_sign, virial_mode
         self.bonded = bonded
         self.lj_force_scale = float(lj_force_scale)   # ATM2B potential_factor (1 = LJ12_6)
+        # the switched-cutoff option (kor_set_switch): width of the switch below
+        # each cutoff, 0 = the reference's truncated potentials
+        self.switch_width = float(switch_width)
         # tabulated pair force (x, y, below, above) in place of / after LJ
         self.table = None if table is None else (np.ascontiguousarray(table[0], np.float64),
                                                  np.ascontiguousarray(table[1], np.float64),
@@ -194,10 +200,12 @@ class OracleSim:
     # --- forces ------------------------------------------------------------
     def forces(self, nbins=0, max_sigma=1.0, with_atm_virial=False, ncount=False, listless=False):
         self.L.kor_set_lj_force_scale(self.lj_force_scale)
+        self.L.kor_set_switch(self.switch_width, self.switch_width)
         try:
             self._forces(nbins, max_sigma, with_atm_virial, ncount, listless)
         finally:
             self.L.kor_set_lj_force_scale(1.0)
+            self.L.kor_set_switch(0.0, 0.0)
 
     def thermostat(self, t_target):
         """VelocityScaling::apply (VelocityScaling.cpp:12-25) after a

@@ -35,6 +35,7 @@
 #include "IO/Logging.h"
 #include "IO/FileInput.h"
 #include "IO/CheckpointIO.h"
+#include "util/PhasespaceGenerator.h"
 #include "potentials/LJ12_6.h"
 #include "potentials/FENE.h"
 #include "potentials/Limit.h"
@@ -99,6 +100,7 @@ int main(int argc, char** argv) {
         }
         Registry::instance->integrators().push_back(std::make_unique<Integrator>());
         CheckpointIO::loadCheckpoint();
+        PhasespaceGenerator::generate();   // ps_gen_region entries, as main.cpp:70-71
         // ATM2B reads the molecule count in its constructor.  main.cpp:57 builds
         // it before CheckpointIO::loadCheckpoint (main.cpp:70), where the count is
         // still 0 and the factor comes out as exactly 1; here it is built after the

@@ -86,14 +86,16 @@ def parse_dump(path):
     return steps
 
 
-def run_case(name, sysm, values, steps, dumps, comps=None, thermostat=False, table=None):
+def run_case(name, sysm, values, steps, dumps, comps=None, thermostat=False, table=None, regions=()):
     tmp = tempfile.mkdtemp(prefix=f"komd_golden_{name}_")
     try:
-        ps = os.path.join(tmp, "in.ps")
-        komd_io.write_checkpoint(ps, sysm)
+        ps = None
+        if sysm is not None:   # else the phase space comes from ps_gen_region entries alone
+            ps = os.path.join(tmp, "in.ps")
+            komd_io.write_checkpoint(ps, sysm)
         comps = comps or [(0, EPS_J, 1.0, 1.0)]
         with open(os.path.join(tmp, "in.dat"), "w") as fh:
-            fh.write(komd_io.format_input(values, ps, comps))
+            fh.write(komd_io.format_input(values, ps, comps, regions))
         env = dict(os.environ, KOMD_HARNESS_THERMOSTAT="1" if thermostat else "0")
         if table is not None:
             tab = os.path.join(tmp, "force.txt")
@@ -105,14 +107,18 @@ def run_case(name, sysm, values, steps, dumps, comps=None, thermostat=False, tab
         if res.returncode != 0:
             raise RuntimeError(f"{name}: harness failed\n{res.stdout}\n{res.stderr}")
         dump = parse_dump(os.path.join(tmp, "out.txt"))
-        arrays = dict(r0=sysm.r, v0=sysm.v, m=sysm.m, eps=sysm.eps, sig=sysm.sig, mol_id=sysm.mol_id,
-                      low=np.asarray(values["domain_low"], float), high=np.asarray(values["domain_high"], float),
+        arrays = dict(low=np.asarray(values["domain_low"], float), high=np.asarray(values["domain_high"], float),
                       dumps=np.array(dumps, np.int64))
+        if sysm is not None:
+            arrays.update(r0=sysm.r, v0=sysm.v, m=sysm.m, eps=sysm.eps, sig=sysm.sig, mol_id=sysm.mol_id)
+        if regions:
+            arrays["regions"] = np.array([[*b, *e, c] for b, e, c in regions], float)
+            arrays["comps"] = np.array([[c[0], c[1], c[2], c[3], *c[4]] for c in comps], float)
         arrays["p_thermostat"] = np.int64(1 if thermostat else 0)
         if table is not None:
             arrays["table_x"], arrays["table_y"] = np.asarray(table[0]), np.asarray(table[1])
         for k in ("cutoff", "cell_size", "delta_t", "limit", "energy_3b", "stiffness", "sensor_rdf_max",
-                  "sensor_rdf_dr", "temperature"):
+                  "sensor_rdf_dr", "temperature", "density"):
             if k in values:
                 arrays["p_" + k] = np.float64(values[k])
         for k in ("enable_3b", "enable_3b_direct", "enable_sensor_rdf", "enable_sensor_lj", "enable_sensor_pres",
@@ -127,7 +133,8 @@ def run_case(name, sysm, values, steps, dumps, comps=None, thermostat=False, tab
                 tab = np.loadtxt(rdf)
                 arrays[f"s{s}_rdf"] = tab[:, 2].copy()
         np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **arrays)
-        print(f"{name}: n={sysm.n} steps={steps} dumps={dumps} -> {name}.npz")
+        n = sysm.n if sysm is not None else len(dump[dumps[0]]["R"])
+        print(f"{name}: n={n} steps={steps} dumps={dumps} -> {name}.npz")
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
 
@@ -294,6 +301,21 @@ def main(selected):
                                                 IBI_reload_ppath="pot.txt"),
                   tables={"force.txt": (x, f), "pot.txt": (x, u)})
 
+    def psgen3site():
+        # PhasespaceGenerator (ps_gen_region, no checkpoint): a bent three-site
+        # component on the generator's grid at density 0.05 per cubic Angstrom in
+        # a 14 x 14 x 14 box, rotated at random, Maxwell-Boltzmann at 120 K;
+        # the harness dumps the generated state at step 0 (and after 5 steps)
+        box = 14.0
+        comps = [(0, EPS_J, 1.0, 1.0, (0.0, 0.0, 0.0)), (0, EPS_J, 1.0, 1.0, (0.97, 0.0, 0.0)),
+                 (0, EPS_J, 1.0, 1.0, (-0.3, 0.92, 0.0))]
+        values = base_values(lattice.System(r=np.zeros((1, 3)), v=np.zeros((1, 3)), m=np.ones(1), eps=np.ones(1),
+                                            sig=np.ones(1), mol_id=np.ones(1, np.uint64), low=np.zeros(3),
+                                            high=np.full(3, box)),
+                             2.5, 2.8, 0.002, 5, density=0.05, temperature=120.0, stiffness=30.0)
+        run_case("psgen3site", None, values, 5, [0, 5], comps=comps,
+                 regions=[((0.0, 0.0, 0.0), (box, box, box), 0)])
+
     def sensors864():
         # the stock main with the LJ, pressure and viscosity sensors on (and the
         # always-on thermostat): every file they write at write_freq 10 over 30 steps
@@ -304,7 +326,7 @@ def main(selected):
                                               enable_sensor_visc=1, sensor_visc_no_orig=1, sensor_lj_bins=60),
                   tokens=True)
 
-    cases = dict(sensors864=sensors864, ibirun864=ibirun864, ibistop864=ibistop864, ibireload864=ibireload864, ibi864=ibi864, lj864=lj864, ljatm864=ljatm864, atmlist500=atmlist500, fene375=fene375, edge_box=edge_box,
+    cases = dict(psgen3site=psgen3site, sensors864=sensors864, ibirun864=ibirun864, ibistop864=ibistop864, ibireload864=ibireload864, ibi864=ibi864, lj864=lj864, ljatm864=ljatm864, atmlist500=atmlist500, fene375=fene375, edge_box=edge_box,
                  atm2b864=atm2b864, thermo864=thermo864)
     for name in (selected or list(cases)):
         cases[name]()

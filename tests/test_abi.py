@@ -28,7 +28,7 @@ def test_library_exports_every_declared_symbol():
 def test_abi_version_and_error_reporting_without_gpu():
     from komd_gb300 import gpu
     lib = gpu.load()
-    assert lib.komd_gpu_abi_version() == 1
+    assert lib.komd_gpu_abi_version() == 2
     # argument validation happens before any device work
     cfg = gpu.make_config([0, 0, 0], [5, 5, 5], 2.5, cutoff=2.5)    # only 2 cells per dimension
     h = ctypes.c_void_p()

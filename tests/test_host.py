@@ -224,3 +224,29 @@ def test_komd_sensor_files_follow_reference(komd_exe, tmp_path):
         # viscosity: correlation sums of the pressure series (6 digits each side)
         rtol = 2e-4 if f.startswith("viscosity") else 2e-5
         np.testing.assert_allclose(got, ref, rtol=rtol, atol=1e-9 * np.nanmax(np.abs(ref)), err_msg=f)
+
+
+def test_phasespace_generator_follows_reference(komd_exe, tmp_path):
+    """ps_gen_region (util/PhasespaceGenerator.cpp:27-95): `komd --phasespace`
+    writes the generated molecules of the psgen3site input -- a bent
+    three-site component on the generator's grid, random Euler rotations from
+    the static engine seeded 43, Maxwell-Boltzmann velocities from the one
+    seeded 42 -- and they equal the reference's generated state (dumped by
+    the harness at step 0) to the last bit.  CPU only: the mode stops before
+    any GPU work."""
+    from komd_gb300 import komd_io
+    z = load_case("psgen3site")
+    comps = [(int(c[0]), float(c[1]), float(c[2]), float(c[3]), tuple(c[4:7])) for c in z["comps"]]
+    regions = [(tuple(r[0:3]), tuple(r[3:6]), int(r[6])) for r in z["regions"]]
+    values = {k[2:]: z[k].item() for k in z if k.startswith("p_") and k != "p_thermostat"}
+    values.update(domain_low=tuple(z["low"]), domain_high=tuple(z["high"]), timesteps=5)
+    inp = tmp_path / "in.dat"
+    inp.write_text(komd_io.format_input(values, None, comps, regions))
+    out = subprocess.run([komd_exe, str(inp), "--phasespace", str(tmp_path / "gen.ps")], capture_output=True,
+                         text=True, cwd=tmp_path, timeout=120)
+    assert out.returncode == 0, out.stderr
+    s = komd_io.read_checkpoint(str(tmp_path / "gen.ps"), low=z["low"], high=z["high"])
+    assert s.n == z["s0_R"].shape[0]
+    assert np.array_equal(s.r, z["s0_R"])
+    assert np.array_equal(s.v, z["s0_V"])
+    assert np.array_equal(np.unique(s.mol_id), np.arange(1, s.n // 3 + 1))   # ids 1.. as Molecule::NEXT_ID gives
