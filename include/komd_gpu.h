@@ -328,6 +328,11 @@ int  komd_batch_step(komd_batch *b, int64_t n_graphs);
 /* Launches only (asynchronous); komd_batch_check synchronises and checks. */
 int  komd_batch_launch(komd_batch *b, int64_t n_graphs);
 int  komd_batch_check(komd_batch *b);
+/* 1 when the batch advances all replicas by one launch per stage of the step
+ * (every replica on the Verlet path with the fused drift and the half-list
+ * LJ + ATM pass: the packed form), 0 when it replays each replica's own
+ * kernels on parallel graph branches; -1 for a null batch. */
+int  komd_batch_form(komd_batch *b);
 
 /* ---- profiling ---------------------------------------------------------- */
 /* When enabled, every kernel launch outside komd_gpu_step's graph is

@@ -1715,8 +1715,12 @@ struct komd_batch {
     std::vector<cudaEvent_t> ev;          // [0] fork, [1..n_streams] joins
     cudaGraphExec_t graph = nullptr;
     int64_t steps = 0;
+    bool packed = false;                  // one launch per stage for all replicas
+    PackedStep pk;
+    std::vector<void *> pk_mem;           // the packed tables (device)
     ~komd_batch() {
         cudaSetDevice(device);
+        for (void *p : pk_mem) cudaFree(p);
         if (graph) cudaGraphExecDestroy(graph);
         for (auto s : branch) cudaStreamDestroy(s);
         for (auto e : ev) cudaEventDestroy(e);
@@ -1725,7 +1729,120 @@ struct komd_batch {
 };
 
 namespace {
+// replicas that all take the step of the Verlet path with the fused drift
+// and the half-list LJ + ATM pass (the benchmark's form) advance by one
+// launch per stage for all of them
+bool packed_ok(const komd_batch *b) {
+    const Engine &e0 = b->reps[0]->e;
+    for (komd_gpu *h : b->reps) {
+        const Engine &e = h->e;
+        if (!(e.verlet && e.fused_drift && fused_lj_atm(h, false) && lj_atm_half(e))) return false;
+        if (e.cfg.thermostat || e.n_bonds > 0 || e.n_angles > 0 || (e.cfg.terms & KOMD_TERM_BONDED)) return false;
+        if (e.uniform != e0.uniform || (e.cfg.switch_width > 0) != (e0.cfg.switch_width > 0)) return false;
+        if (e.hin_r || e.hin_v || e.hout_r || e.hout_f || e.hout_v) return false;
+    }
+    return true;
+}
+
+template <typename T>
+int packed_upload(komd_batch *b, const std::vector<T> &host, T *&dev) {
+    T *p = nullptr;
+    CK(cudaMalloc(reinterpret_cast<void **>(&p), sizeof(T) * std::max<size_t>(host.size(), 1)));
+    b->pk_mem.push_back(p);
+    CK(cudaMemcpy(p, host.data(), sizeof(T) * host.size(), cudaMemcpyHostToDevice));
+    dev = p;
+    return KOMD_OK;
+}
+
+// a stage's per-replica arguments and block ranges
+template <typename T>
+int packed_stage(komd_batch *b, PackedStage &s, const std::vector<T> &args, const std::vector<int> &blocks) {
+    std::vector<int> start(blocks.size() + 1, 0);
+    for (size_t r = 0; r < blocks.size(); r++) start[r + 1] = start[r] + blocks[r];
+    T *a = nullptr;
+    int rc = packed_upload(b, args, a);
+    if (rc) return rc;
+    s.args = a;
+    rc = packed_upload(b, start, s.start);
+    if (rc) return rc;
+    s.blocks = start.back();
+    return KOMD_OK;
+}
+
+int packed_build(komd_batch *b) {
+    PackedStep &pk = b->pk;
+    const int nr = (int)b->reps.size();
+    pk.nrep = nr;
+    pk.uniform = b->reps[0]->e.uniform;
+    pk.sw = b->reps[0]->e.cfg.switch_width > 0;
+    std::vector<Step0Args> s0;
+    std::vector<BinArgs> bi;
+    std::vector<ScanArgs> sc;
+    std::vector<ScatterArgs> sm;
+    std::vector<SortArgs> so;
+    std::vector<FlushArgs> fl;
+    std::vector<PairParams> pp;
+    std::vector<AtmParams> ap;
+    std::vector<float> sa;
+    std::vector<int> n, per, two, b_io, b_cont, b_sort, b_vb, b_force;
+    for (komd_gpu *h : b->reps) {
+        Engine &e = h->e;
+        s0.push_back(step0_args(e));
+        bi.push_back(bin_args(e));
+        sc.push_back(scan_args(e));
+        sm.push_back(scatter_args(e));
+        so.push_back(sort_args(e));
+        fl.push_back(flush_args(e, 1.0 / 4294967296.0));   // the half-list pass sums force units at 2^-32
+        PairParams p = pair_params(e);
+        AtmParams a = atm_params(e);
+        pp.push_back(p);
+        ap.push_back(a);
+        sa.push_back((float)(2.0 * a.sign * a.nu));
+        n.push_back((int)e.n);
+        const int pr = vlist_per(e);
+        per.push_back(pr);
+        two.push_back(vbuild_two(e) ? 1 : 0);
+        b_io.push_back((int)((e.n + 255) / 256));
+        b_cont.push_back(packed_blocks_container(e));
+        b_sort.push_back(std::max(1, std::min((e.g.ncell + kWarpsPerBlock - 1) / kWarpsPerBlock, 8)));
+        b_vb.push_back(packed_blocks_vbuild(e));
+        b_force.push_back((vlist_grid(e) + pr - 1) / pr);
+        pk.force_smem = std::max(pk.force_smem, lj_atm_half_smem(e));
+    }
+    int rc = packed_stage(b, pk.step0, s0, b_io);
+    if (!rc) rc = packed_stage(b, pk.bin, bi, b_cont);
+    if (!rc) rc = packed_stage(b, pk.scan, sc, std::vector<int>(nr, 1));
+    if (!rc) rc = packed_stage(b, pk.scatter, sm, b_cont);
+    if (!rc) rc = packed_stage(b, pk.sort, so, b_sort);
+    if (!rc) rc = packed_stage(b, pk.flush, fl, b_io);
+    std::vector<int> dummy(nr, 0);
+    if (!rc) rc = packed_stage(b, pk.vbuild, dummy, b_vb);
+    if (!rc) rc = packed_stage(b, pk.force, dummy, b_force);
+    if (!rc) rc = packed_upload(b, pp, pk.pp);
+    if (!rc) rc = packed_upload(b, ap, pk.ap);
+    if (!rc) rc = packed_upload(b, sa, pk.sa);
+    if (!rc) rc = packed_upload(b, n, pk.n);
+    if (!rc) rc = packed_upload(b, per, pk.per);
+    if (!rc) rc = packed_upload(b, two, pk.two);
+    return rc;
+}
+
 int batch_capture(komd_batch *b) {
+    if (b->packed) {   // one stream: steps_per_graph x eight stage launches
+        CK(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < b->steps_per_graph; k++) launch_packed_step(b->pk, b->origin);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t le = cudaGetLastError();
+        const cudaError_t ee = cudaStreamEndCapture(b->origin, &graph);
+        if (le != cudaSuccess || ee != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return fail(KOMD_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(le != cudaSuccess ? le : ee));
+        }
+        const cudaError_t ie = cudaGraphInstantiate(&b->graph, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) return fail(KOMD_ERR_CUDA, std::string("batch graph instantiate: ") + cudaGetErrorString(ie));
+        return KOMD_OK;
+    }
     CK(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal));
     cudaError_t ce = cudaEventRecord(b->ev[0], b->origin);
     for (int k = 0; k < b->n_streams && ce == cudaSuccess; k++) ce = cudaStreamWaitEvent(b->branch[k], b->ev[0], 0);
@@ -1802,7 +1919,11 @@ int komd_batch_create(komd_gpu *const *replicas, int32_t n, int32_t n_streams, i
     // the replicas' own queues must be drained before the batch graph runs
     for (auto h : b->reps)
         if (cudaStreamSynchronize(h->e.stream) != cudaSuccess) return bail(fail(KOMD_ERR_CUDA, "replica stream"));
-    int rc = batch_capture(b);
+    int rc = KOMD_OK;
+    b->packed = packed_ok(b);
+    if (b->packed) rc = packed_build(b);
+    if (rc) return bail(rc);
+    rc = batch_capture(b);
     if (rc) return bail(rc);
     *out = b;
     return KOMD_OK;
@@ -1829,6 +1950,11 @@ int komd_batch_launch(komd_batch *b, int64_t n_graphs) {
     for (int64_t k = 0; k < n_graphs; k++) CK(cudaGraphLaunch(b->graph, b->origin));
     b->steps += n_graphs * b->steps_per_graph;
     return KOMD_OK;
+}
+
+int komd_batch_form(komd_batch *b) {
+    if (!b) return fail(KOMD_ERR_ARG, "null batch"), -1;
+    return b->packed ? 1 : 0;
 }
 
 int komd_batch_check(komd_batch *b) {

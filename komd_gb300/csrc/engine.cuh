@@ -200,6 +200,76 @@ inline void sw_params(double rc, double width, int &on, float &rc2, float &iw) {
     iw = on ? (float)(1.0 / (rc * rc - rs * rs)) : 0.f;
 }
 
+// Arguments of the step kernels of the Verlet path, one struct per kernel, so
+// that one launch can serve one system (the struct by value) or all replicas
+// of a batch (an array of them, a block range per replica).
+struct BinArgs {              // k_com_wrap_bin: COM, periodic wrap, binning
+    Grid g;
+    int n_mol;
+    const int *mol_off;
+    double *r;
+    const double *m;
+    double *com;
+    int *mol_cell, *mol_rank, *cell_count, *cell_mcount;
+    double *bias;
+    const int *rebuild;
+    const unsigned char *exact_com;
+    int wrapped;
+};
+struct ScanArgs {             // k_scan2: exclusive scans of the cell counts
+    int nc;
+    int *a, *sa, *b, *sb;
+    const int *rebuild;
+    int *work;
+};
+struct ScatterArgs {          // k_scatter_mol: molecules into their cells
+    int n_mol;
+    const int *mol_cell, *mol_rank, *cell_mstart;
+    int *cell_mols;
+    const int *rebuild;
+};
+struct SortArgs {             // k_cell_sort: slots and the cell-ordered arrays
+    Grid g;
+    const int *mol_off, *cell_mstart, *cell_start, *cell_mols;
+    const double *r, *eps, *sig;
+    const int *key;
+    int *slot_site, *site_slot;
+    float4 *pos4;
+    int *skey;
+    float *seps;
+    double *posd, *seps_d, *sig_d, *bias;
+    float4 *ref4;
+    int *slot_cell, *zkey;
+    const int *rebuild;
+};
+struct Step0Args {            // k_step0_fused: half-kick, drift, wrap, skin test
+    int n;
+    double *r, *v;
+    const double *f, *hdtm;
+    double dt;
+    Grid g;
+    double *bias;
+    const float4 *ref4;
+    float half_skin2;
+    int *rebuild;
+    double *com;
+    const int *site_slot;
+    float4 *pos4;
+    const double *r_in, *v_in;
+    double *r_out;
+};
+struct FlushArgs {            // k_atm_flush_step1: fixed-point sums into f, half-kick
+    int n;
+    const int *site_slot;
+    unsigned long long *acc;
+    double *f;
+    double scale_fix;
+    double *v;
+    const double *hdtm;
+    int *err, *rebuild;
+    double *f_out, *v_out;
+};
+
 // TemperatureSensor's conversion (TemperatureSensor.cpp:44-47) in SciValue
 // arithmetic (math/SciValue.{h,cpp}): mantissas normalised into (0.1, 10) by
 // repeated /10 and *10, converted as m * 10^e.  10^e is exact for 0 <= e <= 22

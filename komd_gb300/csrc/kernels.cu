@@ -23,14 +23,21 @@ namespace komd {
 // container: COM, periodic wrap, binning (LinkedCells.cpp:65-121,390-400;
 // MoleculeContainer.cpp:55-75).  One thread per molecule.
 // ===========================================================================
-__global__ void k_com_wrap_bin(Grid g, int n_mol, const int *__restrict__ mol_off, double *__restrict__ r,
-                               const double *__restrict__ m, double *__restrict__ com, int *__restrict__ mol_cell,
-                               int *__restrict__ mol_rank, int *__restrict__ cell_count, int *__restrict__ cell_mcount,
-                               double *__restrict__ bias, const int *__restrict__ rebuild,
-                               const unsigned char *__restrict__ exact_com, int wrapped) {
-    if (wrapped && rebuild && !*rebuild) return;   // k_step0_fused wrapped this step; no rebuild
-    const bool bin = !(rebuild && !*rebuild);      // no rebuild in this step: cells stay as built
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n_mol; k += gridDim.x * blockDim.x) {
+__device__ __forceinline__ void com_wrap_bin_body(const BinArgs &a, int bid, int nblk) {
+    const Grid &g = a.g;
+    const int n_mol = a.n_mol;
+    const int *__restrict__ mol_off = a.mol_off;
+    double *__restrict__ r = a.r;
+    const double *__restrict__ m = a.m;
+    double *__restrict__ com = a.com;
+    int *__restrict__ mol_cell = a.mol_cell, *__restrict__ mol_rank = a.mol_rank;
+    int *__restrict__ cell_count = a.cell_count, *__restrict__ cell_mcount = a.cell_mcount;
+    double *__restrict__ bias = a.bias;
+    const int *__restrict__ rebuild = a.rebuild;
+    const unsigned char *__restrict__ exact_com = a.exact_com;
+    if (a.wrapped && rebuild && !*rebuild) return;   // k_step0_fused wrapped this step; no rebuild
+    const bool bin = !(rebuild && !*rebuild);        // no rebuild in this step: cells stay as built
+    for (int k = bid * blockDim.x + threadIdx.x; k < n_mol; k += nblk * blockDim.x) {
     const int s0 = mol_off[k], s1 = mol_off[k + 1];
     // com += r * m ; M += m ; com /= M   (updateCOM, no FMA).  For a single
     // site of power-of-two mass the scaling is exact and the result is r
@@ -92,16 +99,18 @@ __global__ void k_com_wrap_bin(Grid g, int n_mol, const int *__restrict__ mol_of
     atomicAdd(&cell_count[cell], s1 - s0);
     }
 }
+__global__ void k_com_wrap_bin(BinArgs a) { com_wrap_bin_body(a, blockIdx.x, gridDim.x); }
 
 // exclusive scan of two count arrays of length nc (one block of 1024 threads,
 // each owning a contiguous chunk); the counts are zeroed once read, ready for
 // the next binning (work: the Verlet list build's cell counter, reset here for
 // this rebuild)
-__global__ void __launch_bounds__(1024) k_scan2(int nc, int *__restrict__ a, int *__restrict__ sa,
-                                                int *__restrict__ b, int *__restrict__ sb,
-                                                const int *__restrict__ rebuild, int *__restrict__ work) {
+__device__ __forceinline__ void scan2_body(const ScanArgs &q) {
     __shared__ int wa[32], wb[32];
-    if (rebuild && !*rebuild) return;
+    const int nc = q.nc;
+    int *__restrict__ a = q.a, *__restrict__ sa = q.sa, *__restrict__ b = q.b, *__restrict__ sb = q.sb;
+    int *__restrict__ work = q.work;
+    if (q.rebuild && !*q.rebuild) return;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     if (work && t == 0) *work = 0;
     const int per = (nc + 1023) / 1024;
@@ -135,34 +144,36 @@ __global__ void __launch_bounds__(1024) k_scan2(int nc, int *__restrict__ a, int
     }
     if (t == 1023) { sa[nc] = wa[31]; sb[nc] = wb[31]; }
 }
+__global__ void __launch_bounds__(1024) k_scan2(ScanArgs q) { scan2_body(q); }
 
-__global__ void k_scatter_mol(int n_mol, const int *__restrict__ mol_cell, const int *__restrict__ mol_rank,
-                              const int *__restrict__ cell_mstart, int *__restrict__ cell_mols,
-                              const int *__restrict__ rebuild) {
-    if (rebuild && !*rebuild) return;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n_mol; k += gridDim.x * blockDim.x)
-        cell_mols[cell_mstart[mol_cell[k]] + mol_rank[k]] = k;
+__device__ __forceinline__ void scatter_mol_body(const ScatterArgs &a, int bid, int nblk) {
+    if (a.rebuild && !*a.rebuild) return;
+    for (int k = bid * blockDim.x + threadIdx.x; k < a.n_mol; k += nblk * blockDim.x)
+        a.cell_mols[a.cell_mstart[a.mol_cell[k]] + a.mol_rank[k]] = k;
 }
+__global__ void k_scatter_mol(ScatterArgs a) { scatter_mol_body(a, blockIdx.x, gridDim.x); }
 
 // One warp per domain cell: order the cell's molecules by index (ascending
 // site index, the reference's cell-list order), assign slots and gather the
 // cell-ordered arrays.
-__global__ void __launch_bounds__(kBlock) k_cell_sort(Grid g, const int *__restrict__ mol_off,
-                                                      const int *__restrict__ cell_mstart,
-                                                      const int *__restrict__ cell_start,
-                                                      const int *__restrict__ cell_mols, const double *__restrict__ r,
-                                                      const double *__restrict__ eps, const double *__restrict__ sig,
-                                                      const int *__restrict__ key, int *__restrict__ slot_site,
-                                                      int *__restrict__ site_slot, float4 *__restrict__ pos4,
-                                                      int *__restrict__ skey, float *__restrict__ seps,
-                                                      double *__restrict__ posd, double *__restrict__ seps_d,
-                                                      double *__restrict__ sig_d, double *__restrict__ bias,
-                                                      float4 *__restrict__ ref4, int *__restrict__ slot_cell,
-                                                      int *__restrict__ zkey, const int *__restrict__ rebuild) {
+__device__ __forceinline__ void cell_sort_body(const SortArgs &a, int bid, int nblk) {
+    const Grid &g = a.g;
+    const int *__restrict__ mol_off = a.mol_off, *__restrict__ cell_mstart = a.cell_mstart;
+    const int *__restrict__ cell_start = a.cell_start, *__restrict__ cell_mols = a.cell_mols;
+    const double *__restrict__ r = a.r, *__restrict__ eps = a.eps, *__restrict__ sig = a.sig;
+    const int *__restrict__ key = a.key;
+    int *__restrict__ slot_site = a.slot_site, *__restrict__ site_slot = a.site_slot;
+    float4 *__restrict__ pos4 = a.pos4;
+    int *__restrict__ skey = a.skey;
+    float *__restrict__ seps = a.seps;
+    double *__restrict__ posd = a.posd, *__restrict__ seps_d = a.seps_d, *__restrict__ sig_d = a.sig_d;
+    double *__restrict__ bias = a.bias;
+    float4 *__restrict__ ref4 = a.ref4;
+    int *__restrict__ slot_cell = a.slot_cell, *__restrict__ zkey = a.zkey;
     const int lane = threadIdx.x & 31;
-    if (rebuild && !*rebuild) return;
-    for (int cell = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5); cell < g.ncell;
-         cell += gridDim.x * kWarpsPerBlock) {
+    if (a.rebuild && !*a.rebuild) return;
+    for (int cell = bid * kWarpsPerBlock + (threadIdx.x >> 5); cell < g.ncell;
+         cell += nblk * kWarpsPerBlock) {
     int cx, cy, cz;
     cell_coords(g, cell, cx, cy, cz);
     const double cen[3] = {cell_centre(g, 0, cx), cell_centre(g, 1, cy), cell_centre(g, 2, cz)};
@@ -206,6 +217,7 @@ __global__ void __launch_bounds__(kBlock) k_cell_sort(Grid g, const int *__restr
     }
     }
 }
+__global__ void __launch_bounds__(kBlock) k_cell_sort(SortArgs a) { cell_sort_body(a, blockIdx.x, gridDim.x); }
 
 // ===========================================================================
 // pair kernel: LJ 12-6 (LJ12_6.cpp:15-43), FENE (FENE.cpp:15-43), the ATM
@@ -952,14 +964,24 @@ __device__ __forceinline__ void rows_out(const double *src_s, double *dst, int b
 // engine's own arrays, or a caller's host buffers reached over the host link);
 // r_out: an extra host copy of the new positions (nullptr: none).  Launched
 // with kIoBlock threads per block.
-__global__ void __launch_bounds__(kIoBlock) k_step0_fused(
-    int n, double *r, double *v, const double *__restrict__ f, const double *__restrict__ hdtm, double dt, Grid g,
-    double *__restrict__ bias, const float4 *__restrict__ ref4, float half_skin2, int *__restrict__ rebuild,
-    double *__restrict__ com, const int *__restrict__ site_slot, float4 *__restrict__ pos4, const double *r_in,
-    const double *v_in, double *r_out) {
+__device__ __forceinline__ void step0_fused_body(const Step0Args &a, int bid) {
     __shared__ double s_r[3 * kIoBlock], s_v[3 * kIoBlock];
+    const int n = a.n;
+    double *r = a.r, *v = a.v;
+    const double *__restrict__ f = a.f, *__restrict__ hdtm = a.hdtm;
+    const double dt = a.dt;
+    const Grid &g = a.g;
+    double *__restrict__ bias = a.bias;
+    const float4 *__restrict__ ref4 = a.ref4;
+    const float half_skin2 = a.half_skin2;
+    int *__restrict__ rebuild = a.rebuild;
+    double *__restrict__ com = a.com;
+    const int *__restrict__ site_slot = a.site_slot;
+    float4 *__restrict__ pos4 = a.pos4;
+    const double *r_in = a.r_in, *v_in = a.v_in;
+    double *r_out = a.r_out;
     const int t = threadIdx.x;
-    const int base = blockIdx.x * blockDim.x, s = base + t;
+    const int base = bid * blockDim.x, s = base + t;
     const int cnt = min((int)blockDim.x, n - base);
     const bool host_in = r_in != r;   // uniform: the whole step reads the caller's buffers
     if (host_in) {
@@ -1023,6 +1045,7 @@ __global__ void __launch_bounds__(kIoBlock) k_step0_fused(
         rows_out(s_r, r_out, base, cnt);
     }
 }
+__global__ void __launch_bounds__(kIoBlock) k_step0_fused(Step0Args a) { step0_fused_body(a, blockIdx.x); }
 
 __global__ void k_step1(int n, double *__restrict__ v, const double *__restrict__ f, const double *__restrict__ hdtm,
                         int *__restrict__ err, int *__restrict__ rebuild) {
@@ -1477,24 +1500,45 @@ __global__ void k_velocity_scale(int n, double *__restrict__ v, const double *__
 // ===========================================================================
 static inline int nblk(long long n, int b) { return (int)((n + b - 1) / b); }
 
+BinArgs bin_args(const Engine &e) {
+    return BinArgs{e.g, (int)e.n_mol, e.mol_off, e.r, e.m, e.com, e.mol_cell, e.mol_rank, e.cell_count, e.cell_mcount,
+                   e.verlet ? e.bias : nullptr, e.verlet ? e.rebuild : nullptr, e.exact_com, e.fused_drift ? 1 : 0};
+}
+ScanArgs scan_args(const Engine &e) {
+    return ScanArgs{e.g.ncell, e.cell_count, e.cell_start, e.cell_mcount, e.cell_mstart,
+                    e.verlet ? e.rebuild : nullptr, e.vb_next};
+}
+ScatterArgs scatter_args(const Engine &e) {
+    return ScatterArgs{(int)e.n_mol, e.mol_cell, e.mol_rank, e.cell_mstart, e.cell_mols,
+                       e.verlet ? e.rebuild : nullptr};
+}
+SortArgs sort_args(const Engine &e) {
+    return SortArgs{e.g, e.mol_off, e.cell_mstart, e.cell_start, e.cell_mols, e.r, e.eps, e.sig, e.key,
+                    e.slot_site, e.site_slot, e.pos4, e.skey, e.seps, e.posd, e.seps_d, e.sig_d,
+                    e.verlet ? e.bias : nullptr, e.verlet ? e.ref4 : nullptr, e.verlet ? e.slot_cell : nullptr,
+                    e.verlet ? e.zkey : nullptr, e.verlet ? e.rebuild : nullptr};
+}
+Step0Args step0_args(const Engine &e) {
+    const float hs = (float)(0.5 * e.cfg.skin);
+    return Step0Args{(int)e.n, e.r, e.v, e.f, e.hdtm, e.cfg.delta_t, e.g, e.bias, e.ref4, hs * hs, e.rebuild, e.com,
+                     e.site_slot, e.pos4, e.hin_r ? e.hin_r : e.r, e.hin_v ? e.hin_v : e.v, e.hout_r};
+}
+FlushArgs flush_args(const Engine &e, double scale_fix) {
+    return FlushArgs{(int)e.n, e.site_slot, e.atm_acc, e.f, scale_fix, e.v, e.hdtm, e.err,
+                     e.verlet ? e.rebuild : nullptr, e.hout_f, e.hout_v};
+}
+
 void launch_container(Engine &e, cudaStream_t st) {
     const Grid &g = e.g;
-    const int *rb = e.verlet ? e.rebuild : nullptr;   // nullptr: rebuild unconditionally
+    // without a Verlet list the rebuild flag is null: the kernels rebuild unconditionally
     // the per-cell counts are zero here: zeroed at allocation, and by the scan
     // of every binning after reading them
     // grid-stride kernels on a resident grid: steps without a rebuild launch few blocks
     const int res = e.num_sms * 8;
-    k_com_wrap_bin<<<std::min(nblk(e.n_mol, 256), res), 256, 0, st>>>(g, (int)e.n_mol, e.mol_off, e.r, e.m, e.com, e.mol_cell,
-                                                         e.mol_rank, e.cell_count, e.cell_mcount,
-                                                         e.verlet ? e.bias : nullptr, rb, e.exact_com,
-                                                         e.fused_drift ? 1 : 0);
-    k_scan2<<<1, 1024, 0, st>>>(g.ncell, e.cell_count, e.cell_start, e.cell_mcount, e.cell_mstart, rb, e.vb_next);
-    k_scatter_mol<<<std::min(nblk(e.n_mol, 256), res), 256, 0, st>>>((int)e.n_mol, e.mol_cell, e.mol_rank, e.cell_mstart,
-                                                        e.cell_mols, rb);
-    k_cell_sort<<<std::min(nblk(g.ncell, kWarpsPerBlock), res), kBlock, 0, st>>>(
-        g, e.mol_off, e.cell_mstart, e.cell_start, e.cell_mols, e.r, e.eps, e.sig, e.key, e.slot_site, e.site_slot,
-        e.pos4, e.skey, e.seps, e.posd, e.seps_d, e.sig_d, e.verlet ? e.bias : nullptr, e.verlet ? e.ref4 : nullptr,
-        e.verlet ? e.slot_cell : nullptr, e.verlet ? e.zkey : nullptr, rb);
+    k_com_wrap_bin<<<std::min(nblk(e.n_mol, 256), res), 256, 0, st>>>(bin_args(e));
+    k_scan2<<<1, 1024, 0, st>>>(scan_args(e));
+    k_scatter_mol<<<std::min(nblk(e.n_mol, 256), res), 256, 0, st>>>(scatter_args(e));
+    k_cell_sort<<<std::min(nblk(g.ncell, kWarpsPerBlock), res), kBlock, 0, st>>>(sort_args(e));
     if (e.verlet) {
         if (!e.fused_drift)
             k_refresh<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.slot_site, e.r, e.bias, e.pos4, e.rebuild);
@@ -1662,13 +1706,18 @@ __global__ void __launch_bounds__(kBlock) k_atm_s(AtmParams p) {
 // the same flush fused with Integrator::integrate1 of the step (ATM is the
 // last force term): f[site] += ..., then v[site] += f[site] * dt/(2m) with
 // k_step1's operations, its non-finite check and the rebuild-flag reset
-__global__ void __launch_bounds__(kIoBlock) k_atm_flush_step1(
-    int n, const int *__restrict__ site_slot, unsigned long long *__restrict__ acc, double *__restrict__ f,
-    double scale_fix, double *__restrict__ v, const double *__restrict__ hdtm, int *__restrict__ err,
-    int *__restrict__ rebuild, double *f_out, double *v_out) {
+__device__ __forceinline__ void flush_step1_body(const FlushArgs &a, int bid) {
     __shared__ double s_f[3 * kIoBlock], s_v[3 * kIoBlock];
+    const int n = a.n;
+    const int *__restrict__ site_slot = a.site_slot;
+    unsigned long long *__restrict__ acc = a.acc;
+    double *__restrict__ f = a.f, *__restrict__ v = a.v;
+    const double scale_fix = a.scale_fix;
+    const double *__restrict__ hdtm = a.hdtm;
+    int *__restrict__ err = a.err, *__restrict__ rebuild = a.rebuild;
+    double *f_out = a.f_out, *v_out = a.v_out;
     const int t = threadIdx.x;
-    const int base = blockIdx.x * blockDim.x, site = base + t;
+    const int base = bid * blockDim.x, site = base + t;
     const int cnt = min((int)blockDim.x, n - base);
     if (rebuild && site == 0) *rebuild = 0;   // every consumer of this step's flag has run
     if (site < n) {
@@ -1703,6 +1752,7 @@ __global__ void __launch_bounds__(kIoBlock) k_atm_flush_step1(
         if (v_out) rows_out(s_v, v_out, base, cnt);
     }
 }
+__global__ void __launch_bounds__(kIoBlock) k_atm_flush_step1(FlushArgs a) { flush_step1_body(a, blockIdx.x); }
 
 // f[site] += 2 sign nu g (fixed point -> FP64) and the accumulators back to 0
 __global__ void k_atm_flush(int n, const int *__restrict__ slot_site, unsigned long long *__restrict__ acc,
@@ -1768,9 +1818,7 @@ bool launch_atm_flush(Engine &e, cudaStream_t st, bool with_step1, bool force_un
     const double sign = e.cfg.atm_sign == KOMD_ATM_SIGN_REFERENCE ? 1.0 : -1.0;
     const double scale_fix = force_units ? 1.0 / kAtmFix : 2.0 * sign * e.cfg.nu / kAtmFix;
     if (with_step1) {
-        k_atm_flush_step1<<<nblk(e.n, kIoBlock), kIoBlock, 0, st>>>((int)e.n, e.site_slot, e.atm_acc, e.f, scale_fix,
-                                                                     e.v, e.hdtm, e.err,
-                                                                     e.verlet ? e.rebuild : nullptr, e.hout_f, e.hout_v);
+        k_atm_flush_step1<<<nblk(e.n, kIoBlock), kIoBlock, 0, st>>>(flush_args(e, scale_fix));
         return true;
     }
     k_atm_flush<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.slot_site, e.atm_acc, e.f, scale_fix);
@@ -1793,9 +1841,7 @@ bool launch_atm(Engine &e, cudaStream_t st, bool measure, bool with_step1) {
 void launch_step0(Engine &e, cudaStream_t st, bool in_step) {
     const float hs = (float)(0.5 * e.cfg.skin);
     if (in_step && e.fused_drift) {
-        k_step0_fused<<<nblk(e.n, kIoBlock), kIoBlock, 0, st>>>((int)e.n, e.r, e.v, e.f, e.hdtm, e.cfg.delta_t, e.g, e.bias,
-                                                       e.ref4, hs * hs, e.rebuild, e.com, e.site_slot, e.pos4,
-                                                       e.hin_r ? e.hin_r : e.r, e.hin_v ? e.hin_v : e.v, e.hout_r);
+        k_step0_fused<<<nblk(e.n, kIoBlock), kIoBlock, 0, st>>>(step0_args(e));
         return;
     }
     k_step0<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.r, e.v, e.f, e.hdtm, e.cfg.delta_t, e.g,
@@ -1859,5 +1905,55 @@ void set_kernel_attributes(Engine &e) {
         cudaFuncSetAttribute(k_atm<double, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     }
 }
+
+// ---- packed replicas (kernels.cuh): the container, drift and flush stages of
+// every replica in one launch each
+__device__ __forceinline__ int packed_rep(const int *__restrict__ start, int nrep, int b) {
+    int lo = 0, hi = nrep;   // start[0] = 0 <= b < start[nrep]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (start[mid] <= b) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+__global__ void __launch_bounds__(kIoBlock) k_step0_fused_p(const Step0Args *a, const int *start, int nrep) {
+    const int r = packed_rep(start, nrep, blockIdx.x);
+    step0_fused_body(a[r], blockIdx.x - start[r]);
+}
+__global__ void k_com_wrap_bin_p(const BinArgs *a, const int *start, int nrep) {
+    const int r = packed_rep(start, nrep, blockIdx.x);
+    com_wrap_bin_body(a[r], blockIdx.x - start[r], start[r + 1] - start[r]);
+}
+__global__ void __launch_bounds__(1024) k_scan2_p(const ScanArgs *a) { scan2_body(a[blockIdx.x]); }
+__global__ void k_scatter_mol_p(const ScatterArgs *a, const int *start, int nrep) {
+    const int r = packed_rep(start, nrep, blockIdx.x);
+    scatter_mol_body(a[r], blockIdx.x - start[r], start[r + 1] - start[r]);
+}
+__global__ void __launch_bounds__(kBlock) k_cell_sort_p(const SortArgs *a, const int *start, int nrep) {
+    const int r = packed_rep(start, nrep, blockIdx.x);
+    cell_sort_body(a[r], blockIdx.x - start[r], start[r + 1] - start[r]);
+}
+__global__ void __launch_bounds__(kIoBlock) k_atm_flush_step1_p(const FlushArgs *a, const int *start, int nrep) {
+    const int r = packed_rep(start, nrep, blockIdx.x);
+    flush_step1_body(a[r], blockIdx.x - start[r]);
+}
+
+int packed_blocks_container(const Engine &e) { return std::max(1, std::min(nblk(e.n_mol, 256), 8)); }
+
+// one step of every replica: the stages of enqueue_step on the Verlet path
+// with the fused drift and the half-list pass, each stage one launch
+void launch_packed_step(const PackedStep &pk, cudaStream_t st) {
+    const int nr = pk.nrep;
+    k_step0_fused_p<<<pk.step0.blocks, kIoBlock, 0, st>>>((const Step0Args *)pk.step0.args, pk.step0.start, nr);
+    k_com_wrap_bin_p<<<pk.bin.blocks, 256, 0, st>>>((const BinArgs *)pk.bin.args, pk.bin.start, nr);
+    k_scan2_p<<<nr, 1024, 0, st>>>((const ScanArgs *)pk.scan.args);
+    k_scatter_mol_p<<<pk.scatter.blocks, 256, 0, st>>>((const ScatterArgs *)pk.scatter.args, pk.scatter.start, nr);
+    k_cell_sort_p<<<pk.sort.blocks, kBlock, 0, st>>>((const SortArgs *)pk.sort.args, pk.sort.start, nr);
+    launch_packed_pair_stages(pk, st, true);
+    launch_packed_pair_stages(pk, st, false);
+    k_atm_flush_step1_p<<<pk.flush.blocks, kIoBlock, 0, st>>>((const FlushArgs *)pk.flush.args, pk.flush.start, nr);
+}
+
 
 }  // namespace komd

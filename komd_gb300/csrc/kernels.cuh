@@ -35,6 +35,42 @@ void launch_rdf(Engine &e, cudaStream_t st, double *bins, bool cells);
 void launch_rdf_bins(Engine &e, cudaStream_t st, double *bins, bool cells, double max_r, double dr, int64_t nbins);
 void set_kernel_attributes(Engine &e);
 int atm_grid(const Engine &e);
+
+// ---- packed replicas: one launch per stage of the step for all replicas of a
+// batch.  Each stage has a device array of per-replica arguments and the
+// first block of every replica (start[r] .. start[r + 1] - 1; start[nrep] is
+// the stage's grid); a block runs the stage's body for its replica with its
+// index inside that replica's range.
+struct PackedStage {
+    void *args = nullptr;     // device array of the stage's argument structs
+    int *start = nullptr;     // device, nrep + 1 entries
+    int blocks = 0;
+};
+struct PackedStep {
+    int nrep = 0;
+    PackedStage step0, bin, scan, scatter, sort, vbuild, force, flush;
+    int *two = nullptr;       // per replica: the two-home form of the list build
+    PairParams *pp = nullptr; // per replica (list build and force pass)
+    AtmParams *ap = nullptr;
+    float *sa = nullptr;      // per replica: 2 sign nu
+    int *n = nullptr, *per = nullptr;
+    size_t force_smem = 0;    // the largest replica's staging
+    bool uniform = true, sw = false;
+};
+BinArgs bin_args(const Engine &e);
+ScanArgs scan_args(const Engine &e);
+ScatterArgs scatter_args(const Engine &e);
+SortArgs sort_args(const Engine &e);
+Step0Args step0_args(const Engine &e);
+FlushArgs flush_args(const Engine &e, double scale_fix);
+int vlist_per(const Engine &e);
+size_t lj_atm_half_smem(const Engine &e);
+// the blocks a stage gives one replica (the same shapes as the single-system launches)
+int packed_blocks_container(const Engine &e);
+int packed_blocks_vbuild(const Engine &e);
+bool vbuild_two(const Engine &e);
+void launch_packed_step(const PackedStep &pk, cudaStream_t st);          // kernels.cu: all eight stages
+void launch_packed_pair_stages(const PackedStep &pk, cudaStream_t st, bool vbuild);   // pair_tile.cu
 int kinetic_grid(const Engine &e);
 size_t atm_smem(const Engine &e);
 }  // namespace komd

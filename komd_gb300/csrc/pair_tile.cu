@@ -373,13 +373,13 @@ __device__ __forceinline__ void vb_walk(const PairParams &p, int cx, int cy, int
 // about 26 sites on average); TWO = true: cells of more than 32 sites walk
 // their neighbourhood once per 64 homes.  Both write the same rows.
 template <bool TWO>
-__global__ void __launch_bounds__(32 * kVbWarps) k_vlist_build(PairParams p) {
+__device__ __forceinline__ void vlist_build_body(const PairParams &p, int bid) {
     __shared__ float4 s_q[kVbWarps][32];
     __shared__ uint2 s_w[kVbWarps][32];
     __shared__ int s_z[kVbWarps][32];
     if (!*p.rebuild) return;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (blockIdx.x == 0 && threadIdx.x == 0 && p.rebuild_count) atomicAdd(p.rebuild_count, 1);
+    if (bid == 0 && threadIdx.x == 0 && p.rebuild_count) atomicAdd(p.rebuild_count, 1);
     const float rl2 = (float)p.rl2;
     float4 *sq = s_q[w];
     uint2 *sw = s_w[w];
@@ -456,6 +456,8 @@ __global__ void __launch_bounds__(32 * kVbWarps) k_vlist_build(PairParams p) {
         }
     }
 }
+template <bool TWO>
+__global__ void __launch_bounds__(32 * kVbWarps) k_vlist_build(PairParams p) { vlist_build_body<TWO>(p, blockIdx.x); }
 
 // ---------------------------------------------------------------------------
 // LJ forces from the Verlet list (every step of the Verlet path): one warp
@@ -786,7 +788,8 @@ __device__ __forceinline__ void lj_half(const PairParams &p, int i, const HalfRo
 }
 
 template <bool UNIFORM, bool SW>
-__global__ void __launch_bounds__(256, 4) k_lj_atm_half(PairParams p, AtmParams a, float sa, int n, int per) {
+__device__ __forceinline__ void lj_atm_half_body(const PairParams &p, const AtmParams &a, float sa, int n, int per,
+                                                 int bid) {
     extern __shared__ float4 s_dyn[];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int capa = p.nl_cap, capr = p.vl_cap;
@@ -794,7 +797,7 @@ __global__ void __launch_bounds__(256, 4) k_lj_atm_half(PairParams p, AtmParams 
     const float rc2 = (float)p.rc2, rc3sq = (float)p.rc3sq, rc3f = (float)a.rc2;
     const unsigned lt = lanemask_lt();
     for (int it = 0; it < per; it++) {
-        const int i = (blockIdx.x * per + it) * 8 + w;
+        const int i = (bid * per + it) * 8 + w;
         if (i >= n) break;   // warp-uniform; later groups of this block are past n too
         HalfRow cur;
         half_row_load(p, i, lane, cur);
@@ -837,6 +840,10 @@ __global__ void __launch_bounds__(256, 4) k_lj_atm_half(PairParams p, AtmParams 
         __syncwarp();   // se / sq / sr are refilled by the next site
     }
 }
+template <bool UNIFORM, bool SW>
+__global__ void __launch_bounds__(256, 4) k_lj_atm_half(PairParams p, AtmParams a, float sa, int n, int per) {
+    lj_atm_half_body<UNIFORM, SW>(p, a, sa, n, per, blockIdx.x);
+}
 
 template <bool UNIFORM, bool SW>
 static void launch_half(const PairParams &p, const AtmParams &a, float sa, int n, int per, int grid, size_t sm,
@@ -848,7 +855,7 @@ static void launch_half(const PairParams &p, const AtmParams &a, float sa, int n
 
 // shared memory of the half-list pass: per warp nl_cap staged triplet
 // partners (se, sq) and vl_cap partners' reactions (sr)
-static size_t lj_atm_half_smem(const Engine &e) {
+size_t lj_atm_half_smem(const Engine &e) {
     return (size_t)8 * sizeof(float4) * (2 * (size_t)e.nl_cap + (size_t)e.vl_cap);
 }
 
@@ -870,13 +877,73 @@ int vlist_per(const Engine &e) {
     return groups <= target ? 1 : (groups + target - 1) / target;
 }
 
+// ---- packed replicas (kernels.cuh): the list build and the half-list pass of
+// every replica in one launch each
+__device__ __forceinline__ int packed_replica(const int *__restrict__ start, int nrep, int b) {
+    int lo = 0, hi = nrep;   // start[0] = 0 <= b < start[nrep]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (start[mid] <= b) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(32 * kVbWarps) k_vlist_build_p(const PairParams *__restrict__ p,
+                                                                const int *__restrict__ two,
+                                                                const int *__restrict__ start, int nrep) {
+    const int r = packed_replica(start, nrep, blockIdx.x);
+    if (two[r]) vlist_build_body<true>(p[r], blockIdx.x - start[r]);
+    else vlist_build_body<false>(p[r], blockIdx.x - start[r]);
+}
+
+template <bool UNIFORM, bool SW>
+__global__ void __launch_bounds__(256, 4) k_lj_atm_half_p(const PairParams *__restrict__ p,
+                                                          const AtmParams *__restrict__ a,
+                                                          const float *__restrict__ sa, const int *__restrict__ n,
+                                                          const int *__restrict__ per, const int *__restrict__ start,
+                                                          int nrep) {
+    const int r = packed_replica(start, nrep, blockIdx.x);
+    lj_atm_half_body<UNIFORM, SW>(p[r], a[r], sa[r], n[r], per[r], blockIdx.x - start[r]);
+}
+
+template <bool UNIFORM, bool SW>
+static void launch_half_p(const PackedStep &pk, cudaStream_t st) {
+    if (pk.force_smem > 48 * 1024)
+        cudaFuncSetAttribute(k_lj_atm_half_p<UNIFORM, SW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)pk.force_smem);
+    k_lj_atm_half_p<UNIFORM, SW><<<pk.force.blocks, 256, pk.force_smem, st>>>(pk.pp, pk.ap, pk.sa, pk.n, pk.per,
+                                                                              pk.force.start, pk.nrep);
+}
+
+void launch_packed_pair_stages(const PackedStep &pk, cudaStream_t st, bool vbuild) {
+    if (vbuild) {
+        k_vlist_build_p<<<pk.vbuild.blocks, 32 * kVbWarps, 0, st>>>(pk.pp, pk.two, pk.vbuild.start, pk.nrep);
+        return;
+    }
+    if (pk.sw) {
+        if (pk.uniform) launch_half_p<true, true>(pk, st);
+        else launch_half_p<false, true>(pk, st);
+    } else {
+        if (pk.uniform) launch_half_p<true, false>(pk, st);
+        else launch_half_p<false, false>(pk, st);
+    }
+}
+
+int packed_blocks_vbuild(const Engine &e) {
+    return std::max(1, std::min((e.g.ncell + kVbWarps - 1) / kVbWarps, 12));
+}
+
+bool vbuild_two(const Engine &e) {
+    return (double)e.n / ((double)e.g.nd[0] * e.g.nd[1] * e.g.nd[2]) > 26.0;
+}
+
 void launch_vlist_build(Engine &e, cudaStream_t st) {
     PairParams p = pair_params(e);
     // a resident grid (12 blocks of 4 warps per SM at this kernel's register count)
     const int blocks = std::min((e.g.ncell + kVbWarps - 1) / kVbWarps, e.num_sms * 12);
     // the two-home form pays off once many cells hold more than 32 sites
-    const double per_cell = (double)e.n / ((double)e.g.nd[0] * e.g.nd[1] * e.g.nd[2]);
-    if (per_cell > 26.0) k_vlist_build<true><<<blocks, 32 * kVbWarps, 0, st>>>(p);
+    if (vbuild_two(e)) k_vlist_build<true><<<blocks, 32 * kVbWarps, 0, st>>>(p);
     else k_vlist_build<false><<<blocks, 32 * kVbWarps, 0, st>>>(p);
 }
 

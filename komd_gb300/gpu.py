@@ -39,6 +39,7 @@ EXPORTS = [
     "komd_mlp_loss_grad", "komd_sur_data_create", "komd_sur_data_destroy", "komd_gpu_surrogate_capture",
     "komd_sur_data_snapshots", "komd_sur_data_sites", "komd_sur_data_get", "komd_sur_fit", "komd_sur_fit_grad",
     "komd_gpu_scale_velocities", "komd_gpu_set_pair_table", "komd_gpu_rdf_profile", "komd_gpu_set_terms", "komd_batch_create", "komd_batch_destroy", "komd_batch_step", "komd_batch_launch", "komd_batch_check",
+    "komd_batch_form",
 ]
 
 
@@ -147,6 +148,7 @@ def load() -> C.CDLL:
     L.komd_batch_step.argtypes = [P, I64]
     L.komd_batch_launch.argtypes = [P, I64]
     L.komd_batch_check.argtypes = [P]
+    L.komd_batch_form.argtypes = [P]
     L.komd_sur_fit_grad.argtypes = [P, P, P, P, C.c_double, C.c_double, C.c_double, C.c_float, C.c_float, P, P]
     _lib = L
     return L
@@ -470,6 +472,11 @@ class Batch:
 
     def launch(self, n_graphs=1):
         self._check(self.L.komd_batch_launch(self.h, int(n_graphs)))
+
+    @property
+    def packed(self) -> bool:
+        """True when one launch per stage advances every replica (komd_batch_form)."""
+        return int(self.L.komd_batch_form(self.h)) == 1
 
     def check(self):
         self._check(self.L.komd_batch_check(self.h))

@@ -1,6 +1,8 @@
 """Batched replicas (komd_batch_*): one CUDA graph advancing several engines
 of uneven sizes must give every replica exactly the trajectory it gets when
-stepped alone through the single-system path."""
+stepped alone through the single-system path -- in the packed form (one
+launch per stage of the step for all replicas) and in the branch form (each
+replica's own kernels on parallel graph branches)."""
 import numpy as np
 import pytest
 
@@ -9,11 +11,11 @@ pytestmark = pytest.mark.gpu
 SPECS = [(11, 2000, 0.75, 1.0), (12, 3100, 0.85, 0.7), (13, 2500, 0.90, 1.4), (14, 2222, 0.80, 0.6)]
 
 
-def _replica(seed, n, rho, t_star):
+def _replica(seed, n, rho, t_star, skin=0.3):
     from komd_gb300 import gpu, lattice, surrogate
     s = lattice.trimmed_fcc(n, rho, t_star, seed)
     cell = float(s.high[0]) / np.floor(float(s.high[0]) / 2.8)
-    cfg = surrogate.physics_config(s, cell, skin=0.3)
+    cfg = surrogate.physics_config(s, cell, skin=skin)
     g = gpu.GpuSystem(s, cfg)
     g.update_container()
     g.forces()
@@ -25,6 +27,7 @@ def test_batch_matches_single_system_path():
     a = [_replica(*sp) for sp in SPECS]
     b = [_replica(*sp) for sp in SPECS]
     batch = gpu.Batch(a, n_streams=3, steps_per_graph=5)
+    assert batch.packed                             # the Verlet path's replicas: one launch per stage
     batch.step(6)                                   # 30 steps
     for g in b:
         g.step(30)
@@ -34,6 +37,25 @@ def test_batch_matches_single_system_path():
         assert np.array_equal(ra, rb)
         assert np.array_equal(va, vb)
         assert np.array_equal(fa, fb)
+    batch.close()
+    for g in a + b:
+        g.close()
+
+
+def test_branch_form_matches_single_system_path():
+    """Replicas on the per-step-cell path (no skin) take the branch form."""
+    from komd_gb300 import gpu
+    a = [_replica(*sp, skin=0.0) for sp in SPECS[:3]]
+    b = [_replica(*sp, skin=0.0) for sp in SPECS[:3]]
+    batch = gpu.Batch(a, n_streams=2, steps_per_graph=4)
+    assert not batch.packed
+    batch.step(3)
+    for g in b:
+        g.step(12)
+    for ga, gb in zip(a, b):
+        ra, va, fa = ga.download()
+        rb, vb, fb = gb.download()
+        assert np.array_equal(ra, rb) and np.array_equal(va, vb) and np.array_equal(fa, fb)
     batch.close()
     for g in a + b:
         g.close()
@@ -152,6 +174,7 @@ def test_batch_512_replicas_full_size():
     reps = [make(*sp) for sp in specs]
     assert 512 * 2000 <= sum(g.n for g in reps) <= 512 * 20000
     batch = gpu.Batch(reps, n_streams=32, steps_per_graph=5)
+    assert batch.packed
     batch.step(2)
     batch.close()
     for k in (0, 137, 511):
