@@ -1785,6 +1785,13 @@ int packed_build(komd_batch *b) {
     std::vector<AtmParams> ap;
     std::vector<float> sa;
     std::vector<int> n, per, two, b_io, b_cont, b_sort, b_vb, b_force;
+    // groups of 8 sites per block of the force pass: about eight resident waves
+    // over all replicas together, each block over a contiguous range of one
+    // replica's slots (the single-system rule, vlist_per, over the batch)
+    long long groups = 0;
+    for (komd_gpu *h : b->reps) groups += vlist_grid(h->e);
+    const long long target = (long long)b->reps[0]->e.num_sms * 5 * 8;
+    const int pr = (int)std::max<long long>(1, (groups + target - 1) / target);
     for (komd_gpu *h : b->reps) {
         Engine &e = h->e;
         s0.push_back(step0_args(e));
@@ -1799,7 +1806,6 @@ int packed_build(komd_batch *b) {
         ap.push_back(a);
         sa.push_back((float)(2.0 * a.sign * a.nu));
         n.push_back((int)e.n);
-        const int pr = vlist_per(e);
         per.push_back(pr);
         two.push_back(vbuild_two(e) ? 1 : 0);
         b_io.push_back((int)((e.n + 255) / 256));
