@@ -111,16 +111,18 @@ __device__ __forceinline__ void atm_sweep(const float4 *se, const float4 *sq, in
     ea_out = ea;
     float sA = 1.f, dA = 0.f;
     if (SW) sw_eval(qa.x, rc2, sw_iw, sA, dA);
+    // the rounds this lane plays: d_first .. d_last, less the round d = m/2 for
+    // the upper half of the lanes (that pair is played by the lower half)
+    int t_act = own ? d_last - d_first + 1 : 0;
+    if (own && (m & 1) == 0 && d_last == (m >> 1) && li >= (m >> 1)) t_act--;
     // partner b = li + d and share source li - d (mod m), stepped per round;
     // d <= m/2 keeps both within one wrap
     int b = li + d_first, src = li - d_first;
     if (b >= m) b -= m;
     if (src < 0) src += m;
     for (int t = 0; t < rounds; t++) {
-        const int d = d_first + t;
-        const bool act = own && d <= d_last;
         float bx = 0.f, by = 0.f, bz = 0.f;
-        if (act && !(2 * d == m && li >= d)) {
+        if (t < t_act) {
             const float4 eb = se[b];
             const float cx = eb.x - ea.x, cy = eb.y - ea.y, cz = eb.z - ea.z;
             const float C = cx * cx + cy * cy + cz * cz;
