@@ -456,6 +456,36 @@ def drift_leg(args, local, model=None):
     return out
 
 
+def three_body_floor_ms(args, g, s, stream, local):
+    """The engine's step with the three-body term made free: the same state,
+    configuration and kernels with the three-body cutoff at 0.5 sigma (no
+    triplet inside it), so the step is the container, the Verlet list, the LJ
+    share of the LJ + ATM pass, the flush and the integration.  No replacement
+    of the three-body term inside this engine can step faster."""
+    import torch
+    from komd_gb300 import gpu, lattice
+    r, v, _ = g.download()
+    sb = lattice.System(r=r, v=v, m=s.m, eps=s.eps, sig=s.sig, mol_id=s.mol_id, low=s.low, high=s.high)
+    cfg = type(g.cfg).from_buffer_copy(g.cfg)
+    cfg.terms = gpu.TERM_LJ | gpu.TERM_ATM
+    cfg.cutoff_3b = 0.5
+    gb = gpu.GpuSystem(sb, cfg, device=local)
+    gb.set_stream(stream.cuda_stream)
+    gb.update_container()
+    gb.forces()
+    gb.step(max(args.warmup, 3))
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    gb.step(args.steps)
+    b.record(stream)
+    torch.cuda.synchronize()
+    triplets = int(gb.measure(gpu.MEASURE_ENERGY)["triplets"])
+    gb.close()
+    return a.elapsed_time(b) / args.steps, triplets
+
+
 def surrogate_leg(args, g, s, stream, local, dist, exact_value, world):
     """FP32 + learned three-body form of the same workload: training set from
     the exact kernel (2000 snapshots of 500 atoms over T* in [0.6, 1.2],
@@ -516,17 +546,27 @@ def surrogate_leg(args, g, s, stream, local, dist, exact_value, world):
     value = world * s.n * args.steps / (ms / 1e3)
     g.last_model = model
     learned_value = world * s.n * args.steps / (learned_ms / 1e3)
+    floor_ms, floor_triplets = three_body_floor_ms(args, g, s, stream, local)
+    exact_ms = world * s.n / exact_value * 1e3
     return {"value": value, "unit": UNIT, "ms_per_step": ms / args.steps, "speedup_vs_exact": value / exact_value,
             "learned_only": {"value": learned_value, "ms_per_step": learned_ms / args.steps,
                              "speedup_vs_exact": learned_value / exact_value,
                              "note": "the learned three-body form without probes (its own cost; no accuracy guard)"},
-            "form": "FP32 LJ + learned three-body term (32-64-64-1 MLP, BF16 tensor-core inference)",
+            "three_body_free_floor": {
+                "ms_per_step": floor_ms, "triplets": floor_triplets, "exact_ms_per_step": exact_ms,
+                "max_speedup_vs_exact": exact_ms / floor_ms,
+                "note": "the same state, configuration and kernels with the three-body cutoff at 0.5 sigma (no "
+                        "triplet): container, Verlet list, LJ share of the pass, flush, integration; no replacement "
+                        "of the three-body term in this engine can step faster"},
+            "form": "FP32 LJ + learned three-body term (32-64-64-1 MLP; BF16 tensor-core inference and training)",
             "force_rmse_3body": {"at_start": rmse0, "probe_last": st["last_rmse"], "probe_max": st["max_rmse"],
                                  "definition": "|F_learned - F_exact| RMS / |F_exact| RMS over sites, three-body term"},
             "energy_r2_3body": float(1.0 - ((e_l - e3) ** 2).sum() / ((e3 - e3.mean()) ** 2).sum()),
             "probe_every": args.sur_probe, "probe_threshold": args.sur_threshold, "probes": st["probes"],
             "fallback": bool(st["fallback"]), "fallback_step": st["fallback_step"],
             "training": {"snapshots": snaps, "sites_per_snapshot": sites, "capture_s": t1 - t0,
+                         "network_kernels": "BF16 tensor cores, FP32 accumulation (k_fit_fwd_tc, k_fit_bwd_tc, "
+                                            "k_fit_grad_tc)",
                          "train_s": model["train_s"], "epochs": args.sur_epochs,
                          "final_loss_energy_force": [float(x) for x in model["loss"][-1]]},
             "kernel_ms": {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()}}

@@ -292,12 +292,16 @@ int32_t komd_sur_data_sites(const komd_sur_data *d);   /* sites per snapshot */
 /* Host copies of one snapshot (snap >= 0) or of all (snap < 0), slot order:
  * raw features (32 per site), energies, forces (3 per site), site ids. */
 int     komd_sur_data_get(komd_sur_data *d, int64_t snap, float *features, float *e3, float *f3, int32_t *site);
+/* arithmetic of the network's forward, reverse and weight-gradient kernels in training */
+#define KOMD_FIT_BF16 0        /* tensor cores: BF16 operands, FP32 accumulation (default) */
+#define KOMD_FIT_FP32 1        /* FP32 SIMT (gradient checks at FP32 tolerance)            */
 typedef struct komd_sur_fit_opts {
     int32_t epochs;            /* passes over the snapshots                         */
     int32_t snaps_per_batch;   /* snapshots per Adam step                           */
     float lr, lr_end;          /* learning rate, decayed geometrically to lr_end    */
     float lam_e, lam_f;        /* weights of the energy and force terms             */
     uint64_t seed;             /* snapshot shuffling                                */
+    int32_t precision;         /* KOMD_FIT_BF16 or KOMD_FIT_FP32                    */
 } komd_sur_fit_opts;
 /* Minimises lam_e * mean (E - (e3 - e_shift)/e_scale)^2
  *         + lam_f * mean |F - F_exact|^2 / f2      (per site, f2 = <|F_exact|^2>)
@@ -306,10 +310,10 @@ typedef struct komd_sur_fit_opts {
 int     komd_sur_fit(komd_sur_data *d, float *params, const float *fmean, const float *fstd, double e_scale,
                      double e_shift, double f2, const komd_sur_fit_opts *opts, float *loss);
 /* Gradient (and the two loss terms) over all snapshots as one batch, from
- * the kernels komd_sur_fit runs. */
+ * the kernels komd_sur_fit runs with the given precision (KOMD_FIT_*). */
 int     komd_sur_fit_grad(komd_sur_data *d, const float *params, const float *fmean, const float *fstd,
                           double e_scale, double e_shift, double f2, float lam_e, float lam_f, float *grad,
-                          double *loss);
+                          double *loss, int32_t precision);
 
 /* ---- batched replicas (no reference counterpart) ----------------------- */
 /* Independent engines (replicas of uneven sizes, each created, uploaded and

@@ -1469,16 +1469,18 @@ struct FitBuffers {
     float *params = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr, *fmean = nullptr, *fstd = nullptr;
     float *E = nullptr, *g = nullptr, *fs = nullptr, *w = nullptr, *rec = nullptr;
     double *loss = nullptr;
+    __nv_bfloat16 *wf = nullptr;
     ~FitBuffers() {
         dfree(snaps); dfree(params); dfree(grad); dfree(m); dfree(v); dfree(fmean); dfree(fstd);
-        dfree(E); dfree(g); dfree(fs); dfree(w); dfree(rec); dfree(loss);
+        dfree(E); dfree(g); dfree(fs); dfree(w); dfree(rec); dfree(loss); dfree(wf);
     }
 };
 
 int fit_setup(komd_sur_data *d, FitBuffers &b, FitParams &p, const float *params, const float *fmean,
               const float *fstd, double e_scale, double e_shift, double f2, float lam_e, float lam_f, int64_t n_snaps,
-              int batch_snaps) {
+              int batch_snaps, int precision) {
     if (!d || !params || !fmean || !fstd) return fail(KOMD_ERR_ARG, "null argument");
+    if (precision != KOMD_FIT_BF16 && precision != KOMD_FIT_FP32) return fail(KOMD_ERR_ARG, "unknown precision");
     if (d->n_snap <= 0) return fail(KOMD_ERR_STATE, "the dataset holds no snapshots");
     if (!(e_scale > 0.0) || !(f2 > 0.0)) return fail(KOMD_ERR_ARG, "e_scale and f2 must be positive");
     CK(cudaSetDevice(d->device));
@@ -1487,7 +1489,7 @@ int fit_setup(komd_sur_data *d, FitBuffers &b, FitParams &p, const float *params
     CK(dalloc(b.snaps, n_snaps)); CK(dalloc(b.params, kSurNParam)); CK(dalloc(b.grad, kSurNParam));
     CK(dalloc(b.m, kSurNParam)); CK(dalloc(b.v, kSurNParam)); CK(dalloc(b.fmean, kSurNF)); CK(dalloc(b.fstd, kSurNF));
     CK(dalloc(b.E, nb)); CK(dalloc(b.g, nb * kSurNF)); CK(dalloc(b.fs, 3 * nb)); CK(dalloc(b.w, nb * kSurNF));
-    CK(dalloc(b.rec, nb * kFitRec)); CK(dalloc(b.loss, 2));
+    CK(dalloc(b.rec, nb * kFitRec)); CK(dalloc(b.loss, 2)); CK(dalloc(b.wf, kFitWf));
     CK(cudaMemcpy(b.params, params, sizeof(float) * kSurNParam, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(b.fmean, fmean, sizeof(float) * kSurNF, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(b.fstd, fstd, sizeof(float) * kSurNF, cudaMemcpyHostToDevice));
@@ -1500,6 +1502,7 @@ int fit_setup(komd_sur_data *d, FitBuffers &b, FitParams &p, const float *params
     p.e_scale = (float)e_scale; p.e_shift = (float)e_shift;
     p.lam_e = lam_e; p.lam_f = lam_f; p.inv_f2 = (float)(1.0 / f2);
     p.E = b.E; p.g = b.g; p.fs = b.fs; p.w = b.w; p.rec = b.rec; p.loss = b.loss;
+    p.wf = b.wf; p.tc = precision == KOMD_FIT_BF16 ? 1 : 0;
     return KOMD_OK;
 }
 
@@ -1607,12 +1610,13 @@ int komd_sur_data_get(komd_sur_data *d, int64_t snap, float *features, float *e3
 }
 
 int komd_sur_fit_grad(komd_sur_data *d, const float *params, const float *fmean, const float *fstd, double e_scale,
-                      double e_shift, double f2, float lam_e, float lam_f, float *grad, double *loss) {
+                      double e_shift, double f2, float lam_e, float lam_f, float *grad, double *loss,
+                      int32_t precision) {
     if (!grad) return fail(KOMD_ERR_ARG, "null argument");
     FitBuffers b;
     FitParams p;
     int rc = fit_setup(d, b, p, params, fmean, fstd, e_scale, e_shift, f2, lam_e, lam_f, d ? d->n_snap : 0,
-                       d ? (int)d->n_snap : 0);
+                       d ? (int)d->n_snap : 0, precision);
     if (rc) return rc;
     std::vector<int> ids((size_t)d->n_snap);
     for (int64_t k = 0; k < d->n_snap; k++) ids[k] = (int)k;
@@ -1635,7 +1639,8 @@ int komd_sur_fit(komd_sur_data *d, float *params, const float *fmean, const floa
     const int bs = (int)std::min<int64_t>(o->snaps_per_batch, std::max<int64_t>(d->n_snap, 1));
     FitBuffers b;
     FitParams p;
-    int rc = fit_setup(d, b, p, params, fmean, fstd, e_scale, e_shift, f2, o->lam_e, o->lam_f, d->n_snap, bs);
+    int rc = fit_setup(d, b, p, params, fmean, fstd, e_scale, e_shift, f2, o->lam_e, o->lam_f, d->n_snap, bs,
+                       o->precision);
     if (rc) return rc;
     const int64_t per_epoch = d->n_snap / bs;
     const int64_t total = per_epoch * o->epochs;

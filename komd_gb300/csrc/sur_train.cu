@@ -1,5 +1,5 @@
 // sur_train.cu -- force-matched training of the learned three-body term
-// (no reference counterpart).  FP32 SIMT kernels.
+// (no reference counterpart).
 //
 // Loss over a batch of nb sites (energies in the network's scaled units
 // E = MLP(x), targets y = (e3 - e_shift) / e_scale; forces in physical units):
@@ -15,9 +15,20 @@
 // Kernels per step: k_fit_fwd (E, g), k_fit_force (learned forces, chain rule),
 // k_fit_adjoint (residual, loss, w), k_fit_bwd (value + tangent reverse sweep
 // into per-site records), k_fit_grad (records -> parameter gradient).
+//
+// Two forms of the network's part (fwd, bwd, grad).  The tensor-core form
+// (FitParams::tc = 1, the default of komd_sur_fit) runs every contraction on
+// mma.sync m16n8k16 with BF16 operands and FP32 accumulation: k_fit_pack
+// rounds the weights to BF16 fragment order each step, k_fit_fwd_tc and
+// k_fit_bwd_tc take one warp per 16 batch sites, and k_fit_grad_tc reduces the
+// BF16 records over the batch as a GEMM (K = batch sites) from ldmatrix-loaded
+// shared-memory tiles.  The FP32 SIMT form (thread per site) is kept for
+// gradient checks at FP32 tolerance.  The descriptor chain rule (k_fit_force,
+// k_fit_adjoint) is FP32 in both.
 #include <cstdint>
 
 #include "sur_device.cuh"
+#include "sur_mma.cuh"
 #include "surrogate.cuh"
 
 namespace komd {
@@ -363,6 +374,397 @@ __global__ void k_fit_adam(float *params, const float *__restrict__ grad, float 
     params[q] -= lr * mh / (sqrtf(vh) + eps);
 }
 
+
+// ===========================================================================
+// tensor-core form
+// ===========================================================================
+namespace {
+// FitParams::wf: W1, W1^T, W2, W2^T as the N x K matrices of load_frag
+constexpr int kWfW1 = 0, kWfW1T = kSurH * kSurNF, kWfW2 = 2 * kSurH * kSurNF, kWfW2T = kWfW2 + kSurH * kSurH;
+static_assert(kWfW2T + kSurH * kSurH == kFitWf, "fragment buffer");
+// BF16 record of one batch site (tensor-core form), element offsets:
+//   left factors  Z1B | ZD1B (dW1), Z2B | ZD2B (dW2)
+//   right factors X | W (dW1),  H1 | HD1 (dW2)
+constexpr int tZ1B = 0, tZD1B = 64, tZ2B = 128, tZD2B = 192, tX = 256, tW = 288, tH1 = 320, tHD1 = 384, kRecTc = 448;
+static_assert(kRecTc * 2 <= kFitRec * 4, "BF16 record inside the record stride");
+constexpr int kGradChunk = 32;            // batch sites per shared-memory stage of k_fit_grad_tc
+constexpr int kRecPad = kRecTc + 8;       // 912-byte rows: the 8 rows of an ldmatrix hit distinct banks
+}  // namespace
+
+// the weight matrices of the parameters, rounded to BF16, in the B-fragment
+// order of load_frag (element (n, k) of an N x K matrix at
+// ((t S + s) 32 + lane) 4 + j with n = 8t + lane/4, k = 16s + 2(lane%4) + (j%2) + 8(j/2))
+__global__ void k_fit_pack(const float *__restrict__ params, __nv_bfloat16 *__restrict__ wf) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= kFitWf) return;
+    const int which = e < kWfW1T ? 0 : e < kWfW2 ? 1 : e < kWfW2T ? 2 : 3;
+    const int base = which == 0 ? kWfW1 : which == 1 ? kWfW1T : which == 2 ? kWfW2 : kWfW2T;
+    const int K = which == 0 ? kSurNF : kSurH;
+    const int q = e - base, j = q & 3, chunk = q >> 2, lane = chunk & 31, ts = chunk >> 5;
+    const int S = K / 16, s = ts % S, t = ts / S;
+    const int n = 8 * t + (lane >> 2), k = 16 * s + 2 * (lane & 3) + (j & 1) + 8 * (j >> 1);
+    const float *W1 = params + kOW1, *W2 = params + kOW2;
+    float v;
+    if (which == 0) v = W1[n * kSurNF + k];        // W1 (64 x 32)
+    else if (which == 1) v = W1[k * kSurNF + n];   // W1^T (32 x 64)
+    else if (which == 2) v = W2[n * kSurH + k];    // W2
+    else v = W2[k * kSurH + n];                    // W2^T
+    wf[e] = __float2bfloat16(v);
+}
+
+// shared-memory copy of the BF16 weights and the FP32 biases (every block of
+// the tensor-core kernels)
+struct FitSmemW {
+    __nv_bfloat16 w1[kSurH * kSurNF], w1t[kSurNF * kSurH], w2[kSurH * kSurH], w2t[kSurH * kSurH];
+    float b1[kSurH], b2[kSurH], w3[kSurH];
+};
+
+__device__ __forceinline__ SurW fit_stage(const FitParams &p, FitSmemW &sw) {
+    sur_stage(p.wf + kWfW1, p.wf + kWfW1T, p.wf + kWfW2, p.wf + kWfW2T, p.params + kOb1, p.params + kOb2,
+              p.params + kOw3, sw.w1, sw.w1t, sw.w2, sw.w2t, sw.b1, sw.b2, sw.w3);
+    __syncthreads();
+    return SurW{sw.w1, sw.w1t, sw.w2, sw.w2t, sw.b1, sw.b2, sw.w3};
+}
+
+__device__ __forceinline__ float fit_target(const FitParams &p, int b) {
+    return (p.e3[fit_site(p, b)] - p.e_shift) / p.e_scale;
+}
+
+// forward + input gradient of 16 batch sites per warp on the tensor cores:
+// the tile's standardised features go to their g rows, which sur_mlp_tile
+// overwrites with dE/dx
+__global__ void __launch_bounds__(128) k_fit_fwd_tc(FitParams p) {
+    __shared__ __align__(16) FitSmemW sw;
+    const SurW W = fit_stage(p, sw);
+    const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
+    const int b0 = (blockIdx.x * 4 + (threadIdx.x >> 5)) * 16;
+    float le = 0.f;
+    if (b0 < p.nb) {
+        for (int q = lane; q < 16 * kSurNF; q += 32) {
+            const int b = b0 + q / kSurNF, k = q % kSurNF;
+            if (b < p.nb) p.g[(size_t)b * kSurNF + k] = (p.x[fit_site(p, b) * kSurNF + k] - p.fmean[k]) / p.fstd[k];
+        }
+        __syncwarp();
+        const int r0 = b0 + g, r1 = r0 + 8;
+        const bool v0 = r0 < p.nb, v1 = r1 < p.nb;
+        float *g0 = p.g + (size_t)min(r0, p.nb - 1) * kSurNF, *g1 = p.g + (size_t)min(r1, p.nb - 1) * kSurNF;
+        float e0, e1;
+        sur_mlp_tile(W, g0, g1, v0, v1, g0, g1, e0, e1, lane);
+        if (tig == 0) {
+            const float b3 = p.params[kOb3];
+            if (v0) {
+                const float E = e0 + b3, d = E - fit_target(p, r0);
+                p.E[r0] = E;
+                le += p.lam_e * d * d / (float)p.nb;
+            }
+            if (v1) {
+                const float E = e1 + b3, d = E - fit_target(p, r1);
+                p.E[r1] = E;
+                le += p.lam_e * d * d / (float)p.nb;
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) le += __shfl_xor_sync(0xffffffffu, le, o);
+    if (lane == 0 && le != 0.f) atomicAdd(&p.loss[0], (double)le);
+}
+
+// sum over the 16 rows of a tile of one C-fragment column pair (rows g and
+// g + 8 in q = 0, 1 and q = 2, 3): complete in the lanes with g == 0
+__device__ __forceinline__ void tile_colsum(const float *c, float &s0, float &s1) {
+    s0 = c[0] + c[2];
+    s1 = c[1] + c[3];
+#pragma unroll
+    for (int o = 4; o < 32; o <<= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    }
+}
+
+__device__ __forceinline__ void st_bf16x2(__nv_bfloat16 *dst, uint32_t v) { *reinterpret_cast<uint32_t *>(dst) = v; }
+
+// value + tangent forward and reverse sweep of 16 batch sites per warp on the
+// tensor cores (the algebra of k_fit_bwd): the BF16 left and right factors of
+// the weight gradients go to the records, and the gradients of the biases,
+// the output weights and the output bias (column sums) straight into grad
+__global__ void __launch_bounds__(128) k_fit_bwd_tc(FitParams p, float *grad) {
+    __shared__ __align__(16) FitSmemW sw;
+    const SurW W = fit_stage(p, sw);
+    const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
+    const int b0 = (blockIdx.x * 4 + (threadIdx.x >> 5)) * 16;
+    if (b0 >= p.nb) return;
+    const int r0 = b0 + g, r1 = r0 + 8;
+    const bool v0 = r0 < p.nb, v1 = r1 < p.nb;
+    const size_t s0 = v0 ? fit_site(p, r0) : 0, s1 = v1 ? fit_site(p, r1) : 0;
+    __nv_bfloat16 *rec = reinterpret_cast<__nv_bfloat16 *>(p.rec);
+    __nv_bfloat16 *q0 = rec + (size_t)(v0 ? r0 : 0) * kRecTc, *q1 = rec + (size_t)(v1 ? r1 : 0) * kRecTc;
+    // A fragments of the standardised features and of the tangent w
+    uint32_t ax[2][4], aw[2][4];
+#pragma unroll
+    for (int s = 0; s < 2; s++) {
+        const int k = 16 * s + tig * 2;
+        float x[2][4], w[2][4];   // [row][k, k + 1, k + 8, k + 9]
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const bool v = h ? v1 : v0;
+            const size_t gs = h ? s1 : s0;
+            const int b = h ? r1 : r0;
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int kk = k + (u & 1) + 8 * (u >> 1);
+                x[h][u] = v ? (p.x[gs * kSurNF + kk] - p.fmean[kk]) / p.fstd[kk] : 0.f;
+                w[h][u] = v ? p.w[(size_t)b * kSurNF + kk] : 0.f;
+            }
+        }
+        ax[s][0] = pack_bf16(x[0][0], x[0][1]);
+        ax[s][1] = pack_bf16(x[1][0], x[1][1]);
+        ax[s][2] = pack_bf16(x[0][2], x[0][3]);
+        ax[s][3] = pack_bf16(x[1][2], x[1][3]);
+        aw[s][0] = pack_bf16(w[0][0], w[0][1]);
+        aw[s][1] = pack_bf16(w[1][0], w[1][1]);
+        aw[s][2] = pack_bf16(w[0][2], w[0][3]);
+        aw[s][3] = pack_bf16(w[1][2], w[1][3]);
+        if (v0) {
+            st_bf16x2(q0 + tX + k, ax[s][0]); st_bf16x2(q0 + tX + k + 8, ax[s][2]);
+            st_bf16x2(q0 + tW + k, aw[s][0]); st_bf16x2(q0 + tW + k + 8, aw[s][2]);
+        }
+        if (v1) {
+            st_bf16x2(q1 + tX + k, ax[s][1]); st_bf16x2(q1 + tX + k + 8, ax[s][3]);
+            st_bf16x2(q1 + tW + k, aw[s][1]); st_bf16x2(q1 + tW + k + 8, aw[s][3]);
+        }
+    }
+    // layer 1: Z1 = X W1^T + b1, ZD1 = W W1^T; H1 = tanh Z1, HD1 = (1 - H1^2) ZD1
+    float h1[8][4], zd1[8][4];
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+        const int c = t * 8 + tig * 2;
+        float az[4] = {W.b1[c], W.b1[c + 1], W.b1[c], W.b1[c + 1]}, ad[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int s = 0; s < 2; s++) {
+            uint32_t B0, B1;
+            load_frag(W.w1, kSurNF / 16, t, s, lane, B0, B1);
+            mma16816(az, ax[s], B0, B1);
+            mma16816(ad, aw[s], B0, B1);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            h1[t][q] = tanh_fast(az[q]);
+            zd1[t][q] = ad[q];
+        }
+    }
+    uint32_t ah[4][4], ahd[4][4];
+#pragma unroll
+    for (int s = 0; s < 4; s++) {
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const int t = 2 * s + u;
+            ah[s][2 * u] = pack_bf16(h1[t][0], h1[t][1]);
+            ah[s][2 * u + 1] = pack_bf16(h1[t][2], h1[t][3]);
+            ahd[s][2 * u] = pack_bf16((1.f - h1[t][0] * h1[t][0]) * zd1[t][0], (1.f - h1[t][1] * h1[t][1]) * zd1[t][1]);
+            ahd[s][2 * u + 1] =
+                pack_bf16((1.f - h1[t][2] * h1[t][2]) * zd1[t][2], (1.f - h1[t][3] * h1[t][3]) * zd1[t][3]);
+            const int c = t * 8 + tig * 2;
+            if (v0) { st_bf16x2(q0 + tH1 + c, ah[s][2 * u]); st_bf16x2(q0 + tHD1 + c, ahd[s][2 * u]); }
+            if (v1) { st_bf16x2(q1 + tH1 + c, ah[s][2 * u + 1]); st_bf16x2(q1 + tHD1 + c, ahd[s][2 * u + 1]); }
+        }
+    }
+    // layer 2: Z2 = H1 W2^T + b2, ZD2 = HD1 W2^T; H2 = tanh Z2
+    float h2[8][4], zd2[8][4];
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+        const int c = t * 8 + tig * 2;
+        float az[4] = {W.b2[c], W.b2[c + 1], W.b2[c], W.b2[c + 1]}, ad[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int s = 0; s < 4; s++) {
+            uint32_t B0, B1;
+            load_frag(W.w2, kSurH / 16, t, s, lane, B0, B1);
+            mma16816(az, ah[s], B0, B1);
+            mma16816(ad, ahd[s], B0, B1);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            h2[t][q] = tanh_fast(az[q]);
+            zd2[t][q] = ad[q];
+        }
+    }
+    // E = w3 . H2 + b3 and a = dL/dE (zero for rows past the batch)
+    float e0 = 0.f, e1 = 0.f;
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+        const int c = t * 8 + tig * 2;
+        e0 += W.w3[c] * h2[t][0] + W.w3[c + 1] * h2[t][1];
+        e1 += W.w3[c] * h2[t][2] + W.w3[c + 1] * h2[t][3];
+    }
+    e0 += __shfl_xor_sync(0xffffffffu, e0, 1);
+    e0 += __shfl_xor_sync(0xffffffffu, e0, 2);
+    e1 += __shfl_xor_sync(0xffffffffu, e1, 1);
+    e1 += __shfl_xor_sync(0xffffffffu, e1, 2);
+    const float b3 = p.params[kOb3];
+    const float a0 = v0 ? 2.f * p.lam_e * (e0 + b3 - fit_target(p, r0)) / (float)p.nb : 0.f;
+    const float a1 = v1 ? 2.f * p.lam_e * (e1 + b3 - fit_target(p, r1)) / (float)p.nb : 0.f;
+    const float m0 = v0 ? 1.f : 0.f, m1 = v1 ? 1.f : 0.f;
+    // layer 2 reverse: z2b = s2 (a w3 - 2 h2 zd2 w3), zd2b = s2 w3 (s2 = 1 - h2^2);
+    // output weight gradient a h2 + s2 zd2 and b2 gradient z2b as column sums
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+        const int c = t * 8 + tig * 2;
+        float g3[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const float a = q < 2 ? a0 : a1, m = q < 2 ? m0 : m1, w3 = W.w3[c + (q & 1)];
+            const float s2 = 1.f - h2[t][q] * h2[t][q];
+            g3[q] = m * (a * h2[t][q] + s2 * zd2[t][q]);
+            const float z2b = s2 * (a * w3 - 2.f * h2[t][q] * zd2[t][q] * w3);
+            h2[t][q] = m * z2b;          // h2 now holds z2b
+            zd2[t][q] = m * s2 * w3;     // zd2 now holds zd2b
+        }
+        float sa, sb;
+        tile_colsum(g3, sa, sb);
+        if (g == 0) { atomicAdd(&grad[kOw3 + c], sa); atomicAdd(&grad[kOw3 + c + 1], sb); }
+        tile_colsum(h2[t], sa, sb);
+        if (g == 0) { atomicAdd(&grad[kOb2 + c], sa); atomicAdd(&grad[kOb2 + c + 1], sb); }
+    }
+    {
+        float sa = a0 + a1;
+#pragma unroll
+        for (int o = 4; o < 32; o <<= 1) sa += __shfl_xor_sync(0xffffffffu, sa, o);
+        if (lane == 0) atomicAdd(&grad[kOb3], sa);
+    }
+    uint32_t az2[4][4], azd2[4][4];
+#pragma unroll
+    for (int s = 0; s < 4; s++) {
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const int t = 2 * s + u;
+            az2[s][2 * u] = pack_bf16(h2[t][0], h2[t][1]);
+            az2[s][2 * u + 1] = pack_bf16(h2[t][2], h2[t][3]);
+            azd2[s][2 * u] = pack_bf16(zd2[t][0], zd2[t][1]);
+            azd2[s][2 * u + 1] = pack_bf16(zd2[t][2], zd2[t][3]);
+            const int c = t * 8 + tig * 2;
+            if (v0) { st_bf16x2(q0 + tZ2B + c, az2[s][2 * u]); st_bf16x2(q0 + tZD2B + c, azd2[s][2 * u]); }
+            if (v1) { st_bf16x2(q1 + tZ2B + c, az2[s][2 * u + 1]); st_bf16x2(q1 + tZD2B + c, azd2[s][2 * u + 1]); }
+        }
+    }
+    // layer 1 reverse: h1b = z2b W2, hd1b = zd2b W2 (B = W2^T rows);
+    // z1b = s1 (h1b - 2 h1 zd1 hd1b), zd1b = s1 hd1b; b1 gradient z1b
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+        float hb[4] = {0.f, 0.f, 0.f, 0.f}, hdb[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int s = 0; s < 4; s++) {
+            uint32_t B0, B1;
+            load_frag(W.w2t, kSurH / 16, t, s, lane, B0, B1);
+            mma16816(hb, az2[s], B0, B1);
+            mma16816(hdb, azd2[s], B0, B1);
+        }
+        float z1b[4], zd1b[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const float m = q < 2 ? m0 : m1;
+            const float s1 = 1.f - h1[t][q] * h1[t][q];
+            z1b[q] = m * s1 * (hb[q] - 2.f * h1[t][q] * zd1[t][q] * hdb[q]);
+            zd1b[q] = m * s1 * hdb[q];
+        }
+        const int c = t * 8 + tig * 2;
+        if (v0) {
+            st_bf16x2(q0 + tZ1B + c, pack_bf16(z1b[0], z1b[1]));
+            st_bf16x2(q0 + tZD1B + c, pack_bf16(zd1b[0], zd1b[1]));
+        }
+        if (v1) {
+            st_bf16x2(q1 + tZ1B + c, pack_bf16(z1b[2], z1b[3]));
+            st_bf16x2(q1 + tZD1B + c, pack_bf16(zd1b[2], zd1b[3]));
+        }
+        float sa, sb;
+        tile_colsum(z1b, sa, sb);
+        if (g == 0) { atomicAdd(&grad[kOb1 + c], sa); atomicAdd(&grad[kOb1 + c + 1], sb); }
+    }
+}
+
+// four 8x8 BF16 matrices from shared memory, transposed (ldmatrix .trans):
+// lane l gives the address of row l % 8 of matrix l / 8
+__device__ __forceinline__ void ldsm_x4_t(const __nv_bfloat16 *row, uint32_t &d0, uint32_t &d1, uint32_t &d2,
+                                          uint32_t &d3) {
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(row);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(d0), "=r"(d1), "=r"(d2), "=r"(d3)
+                 : "r"(a));
+}
+
+// weight gradients from the records as a GEMM over the batch (K = sites):
+//   dW1 = Z1B^T X + ZD1B^T W (64 x 32),  dW2 = Z2B^T H1 + ZD2B^T HD1 (64 x 64)
+// A block stages 32 sites at a time; warp w owns the rows 16 (w / 2) .. +15
+// and six 8-column tiles: W1 columns 0-31 and W2 columns 0-15 (w even) or W2
+// columns 16-63 (w odd).  Each block adds its sums to grad once.
+__global__ void __launch_bounds__(256) k_fit_grad_tc(const __nv_bfloat16 *__restrict__ rec, int nb, float *grad) {
+    __shared__ __align__(16) __nv_bfloat16 s[kGradChunk * kRecPad];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, tig = lane & 3;
+    const int m = warp >> 1, odd = warp & 1;
+    const int mi = lane >> 3, li = lane & 7;
+    float acc[6][4];
+#pragma unroll
+    for (int j = 0; j < 6; j++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) acc[j][q] = 0.f;
+    const int nchunk = (nb + kGradChunk - 1) / kGradChunk;
+    for (int ch = blockIdx.x; ch < nchunk; ch += gridDim.x) {
+        __syncthreads();
+        const int base = ch * kGradChunk;
+        for (int e = threadIdx.x; e < kGradChunk * (kRecTc / 8); e += blockDim.x) {
+            const int r = e / (kRecTc / 8), c = e % (kRecTc / 8);
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (base + r < nb) v = reinterpret_cast<const uint4 *>(rec + (size_t)(base + r) * kRecTc)[c];
+            reinterpret_cast<uint4 *>(s + r * kRecPad)[c] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kb = 0; kb < kGradChunk; kb += 16) {
+            // A (this warp's rows o x sites kb..kb+15): matrices (sites +0 / +8) x (o +0 / +8)
+            const int ar = kb + li + ((mi & 2) ? 8 : 0), ac = 16 * m + ((mi & 1) ? 8 : 0);
+            // B (sites kb..kb+15 x 16 columns): matrices (sites +0 / +8) x (columns +0 / +8)
+            const int br = kb + li + ((mi & 1) ? 8 : 0), bc = (mi & 2) ? 8 : 0;
+#pragma unroll
+            for (int term = 0; term < 2; term++) {
+                uint32_t a[4], b[4];
+                if (!odd) {
+                    // W1: columns 0-31 (tiles 0-3)
+                    ldsm_x4_t(s + ar * kRecPad + (term ? tZD1B : tZ1B) + ac, a[0], a[1], a[2], a[3]);
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        ldsm_x4_t(s + br * kRecPad + (term ? tW : tX) + 16 * h + bc, b[0], b[1], b[2], b[3]);
+                        mma16816(acc[2 * h], a, b[0], b[1]);
+                        mma16816(acc[2 * h + 1], a, b[2], b[3]);
+                    }
+                    // W2: columns 0-15 (tiles 4-5)
+                    ldsm_x4_t(s + ar * kRecPad + (term ? tZD2B : tZ2B) + ac, a[0], a[1], a[2], a[3]);
+                    ldsm_x4_t(s + br * kRecPad + (term ? tHD1 : tH1) + bc, b[0], b[1], b[2], b[3]);
+                    mma16816(acc[4], a, b[0], b[1]);
+                    mma16816(acc[5], a, b[2], b[3]);
+                } else {
+                    // W2: columns 16-63 (tiles 0-5)
+                    ldsm_x4_t(s + ar * kRecPad + (term ? tZD2B : tZ2B) + ac, a[0], a[1], a[2], a[3]);
+#pragma unroll
+                    for (int h = 0; h < 3; h++) {
+                        ldsm_x4_t(s + br * kRecPad + (term ? tHD1 : tH1) + 16 + 16 * h + bc, b[0], b[1], b[2], b[3]);
+                        mma16816(acc[2 * h], a, b[0], b[1]);
+                        mma16816(acc[2 * h + 1], a, b[2], b[3]);
+                    }
+                }
+            }
+        }
+    }
+    // C fragment: rows o = 16 m + g (+8), columns 8 j + 2 tig (+1) of the tile
+#pragma unroll
+    for (int j = 0; j < 6; j++) {
+        int off, ld, col;
+        if (!odd && j < 4) { off = kOW1; ld = kSurNF; col = 8 * j; }
+        else { off = kOW2; ld = kSurH; col = odd ? 16 + 8 * j : 8 * (j - 4); }
+        const int o = 16 * m + g, c = col + 2 * tig;
+        atomicAdd(&grad[off + o * ld + c], acc[j][0]);
+        atomicAdd(&grad[off + o * ld + c + 1], acc[j][1]);
+        atomicAdd(&grad[off + (o + 8) * ld + c], acc[j][2]);
+        atomicAdd(&grad[off + (o + 8) * ld + c + 1], acc[j][3]);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
@@ -376,6 +778,18 @@ void launch_fit_capture(int n, const float4 *nl, const int *nl_count, int nl_cap
 
 // fs (nb x 3) and grad (kSurNParam) must be zero on entry
 void launch_fit_step(FitParams &p, float *grad, cudaStream_t st) {
+    if (p.tc) {
+        const int tiles = (p.nb + 15) / 16;
+        const int chunks = (p.nb + kGradChunk - 1) / kGradChunk;
+        k_fit_pack<<<(kFitWf + 255) / 256, 256, 0, st>>>(p.params, p.wf);
+        k_fit_fwd_tc<<<(tiles + 3) / 4, 128, 0, st>>>(p);
+        k_fit_force<<<(p.nb + 7) / 8, 256, 0, st>>>(p);
+        k_fit_adjoint<<<(p.nb + 7) / 8, 256, 0, st>>>(p);
+        k_fit_bwd_tc<<<(tiles + 3) / 4, 128, 0, st>>>(p, grad);
+        k_fit_grad_tc<<<chunks < 256 ? chunks : 256, 256, 0, st>>>(reinterpret_cast<const __nv_bfloat16 *>(p.rec),
+                                                                   p.nb, grad);
+        return;
+    }
     k_fit_fwd<<<(p.nb + 127) / 128, 128, 0, st>>>(p);
     k_fit_force<<<(p.nb + 7) / 8, 256, 0, st>>>(p);
     k_fit_adjoint<<<(p.nb + 7) / 8, 256, 0, st>>>(p);

@@ -60,8 +60,12 @@ struct FitParams {
     float lam_e, lam_f, inv_f2;          // loss weights; 1 / <|F_exact|^2> per site
     float *E, *g, *fs, *w, *rec;         // per batch site: energy, dE/dx, learned force, tangent, record
     double *loss;                        // [0] energy term, [1] force term (accumulated)
+    __nv_bfloat16 *wf;                   // the weights in BF16 fragment order (tensor-core form)
+    int tc;                              // 1: the network runs on the tensor cores (BF16 operands, FP32
+                                         // accumulation); 0: FP32 SIMT
 };
-constexpr int kFitRec = 580;             // record stride (floats)
+constexpr int kFitRec = 580;             // record stride (floats; the BF16 records of the tensor-core form fit)
+constexpr int kFitWf = 2 * kSurH * kSurNF + 2 * kSurH * kSurH;   // BF16 elements of FitParams::wf
 
 void launch_fit_capture(int n, const float4 *nl, const int *nl_count, int nl_cap, const float *x, const float *mom,
                         const double *e3_site, const double *f3_site, const int *slot_site, float4 *dnl,

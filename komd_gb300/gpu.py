@@ -25,6 +25,7 @@ VIRIAL_COMPAT, VIRIAL_CORRECT = 0, 1
 TERM_LJ, TERM_FENE, TERM_LIMIT, TERM_ATM, TERM_BONDED, TERM_ATM_SURROGATE = 0x01, 0x02, 0x04, 0x08, 0x10, 0x20
 TERM_ATM2B, TERM_TABULATED = 0x40, 0x80
 SUR_NFEAT, SUR_NPARAM = 32, 6337
+FIT_BF16, FIT_FP32 = 0, 1
 MEASURE_TEMPERATURE, MEASURE_ENERGY, MEASURE_PRESSURE, MEASURE_RDF, MEASURE_LJ_HIST = 0x01, 0x02, 0x04, 0x08, 0x10
 
 EXPORTS = [
@@ -71,7 +72,7 @@ class SurrogateStatus(C.Structure):
 
 class SurFitOpts(C.Structure):
     _fields_ = [("epochs", C.c_int32), ("snaps_per_batch", C.c_int32), ("lr", C.c_float), ("lr_end", C.c_float),
-                ("lam_e", C.c_float), ("lam_f", C.c_float), ("seed", C.c_uint64)]
+                ("lam_e", C.c_float), ("lam_f", C.c_float), ("seed", C.c_uint64), ("precision", C.c_int32)]
 
 
 class KomdError(RuntimeError):
@@ -149,7 +150,8 @@ def load() -> C.CDLL:
     L.komd_batch_launch.argtypes = [P, I64]
     L.komd_batch_check.argtypes = [P]
     L.komd_batch_form.argtypes = [P]
-    L.komd_sur_fit_grad.argtypes = [P, P, P, P, C.c_double, C.c_double, C.c_double, C.c_float, C.c_float, P, P]
+    L.komd_sur_fit_grad.argtypes = [P, P, P, P, C.c_double, C.c_double, C.c_double, C.c_float, C.c_float, P, P,
+                                    C.c_int32]
     _lib = L
     return L
 
@@ -414,9 +416,9 @@ class SurData:
         return x, e3, f3, site
 
     def fit(self, params, fmean, fstd, e_scale, e_shift, f2, epochs, snaps_per_batch=4, lr=2e-3, lr_end=1e-4,
-            lam_e=0.1, lam_f=1.0, seed=0):
+            lam_e=0.1, lam_f=1.0, seed=0, precision=FIT_BF16):
         o = SurFitOpts(int(epochs), int(snaps_per_batch), float(lr), float(lr_end), float(lam_e), float(lam_f),
-                       int(seed))
+                       int(seed), int(precision))
         p = np.ascontiguousarray(params, np.float32).copy()
         fm = np.ascontiguousarray(fmean, np.float32)
         fs = np.ascontiguousarray(fstd, np.float32)
@@ -425,14 +427,14 @@ class SurData:
                                         C.byref(o), _p(loss)))
         return p, loss[:2 * int(epochs)].reshape(-1, 2)
 
-    def fit_grad(self, params, fmean, fstd, e_scale, e_shift, f2, lam_e=0.1, lam_f=1.0):
+    def fit_grad(self, params, fmean, fstd, e_scale, e_shift, f2, lam_e=0.1, lam_f=1.0, precision=FIT_BF16):
         p = np.ascontiguousarray(params, np.float32)
         fm = np.ascontiguousarray(fmean, np.float32)
         fs = np.ascontiguousarray(fstd, np.float32)
         g = np.zeros(SUR_NPARAM, np.float32)
         loss = np.zeros(2)
         self._check(self.L.komd_sur_fit_grad(self.h, _p(p), _p(fm), _p(fs), float(e_scale), float(e_shift), float(f2),
-                                             float(lam_e), float(lam_f), _p(g), _p(loss)))
+                                             float(lam_e), float(lam_f), _p(g), _p(loss), int(precision)))
         return g, loss
 
     def close(self):
