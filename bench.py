@@ -402,7 +402,52 @@ def next_rows_leg(args, stream, local):
         except Exception as exc:   # reported in the line; the headline stands on its own
             out[name] = {"error": f"{type(exc).__name__}: {exc}"}
     out["system"] = "256,000 argon atoms, FCC 40^3 jittered by 0.02 sigma, rho* 0.8442; K steps from each step graph"
+    try:
+        out["multisite_300k"] = multisite_leg(stream, local, events_ms)
+    except Exception as exc:
+        out["multisite_300k"] = {"error": f"{type(exc).__name__}: {exc}"}
     return out
+
+
+def multisite_leg(stream, local, events_ms, steps=500):
+    """The multi-site workload: 100,000 flexible 3-site molecules (300,000
+    sites) on a simple-cubic lattice, site density 0.8, T* 1.0, harmonic bonds
+    (k 1000, r0 1) and angles (k 100, 109.47 deg), intermolecular LJ (cutoff
+    2.5) on cells of edge >= 4.2 (the cutoff plus the molecule's diameter, so
+    that the centre-of-mass cells hold every site pair inside the cutoff),
+    FP32 forces, FP64 integration, dt 0.002, all 500 steps timed from the
+    start.  One seeded orientation for all molecules: random orientations at
+    this density overlap sites of neighbouring molecules (see the workload
+    test in tests/test_workloads.py)."""
+    from komd_gb300 import gpu, lattice
+    s = lattice.triatomic_count(100000, rho_site=0.8, t_star=1.0, seed=31, aligned=True)
+    L = float((s.high - s.low)[0])
+    th0 = np.deg2rad(109.47)
+    cfg = gpu.make_config(s.low, s.high, L / np.floor(L / 4.2), cutoff=2.5, dt=0.002,
+                          terms=gpu.TERM_LJ | gpu.TERM_BONDED, bond_k=1000.0, bond_r0=1.0, angle_k=100.0,
+                          angle_theta0=th0, virial_mode=gpu.VIRIAL_CORRECT)
+    g = gpu.GpuSystem(s, cfg, device=local)
+    try:
+        g.set_stream(stream.cuda_stream)
+        g.update_container()
+        g.forces()
+
+        def energy():
+            o = g.measure(gpu.MEASURE_ENERGY | gpu.MEASURE_TEMPERATURE)
+            return (0.5 * o["mv2"] + o["u_lj"] + o["u_bonded"]) / s.n
+
+        e0 = energy()
+        ms = events_ms(lambda: g.step(steps))
+        e1 = energy()
+        r, v, _ = g.download()
+        b = np.linalg.norm(r[s.bonds[:, 0]] - r[s.bonds[:, 1]], axis=1)
+        return dict(value=s.n * steps / (ms / 1e3), unit=UNIT, ms_per_step=ms / steps, steps=steps,
+                    finite=bool(np.isfinite(r).all() and np.isfinite(v).all()),
+                    bond_length_range=[float(b.min()), float(b.max())], energy_per_site=[e0, e1],
+                    config="300,000 sites (100,000 3-site molecules, one seeded orientation), rho_site 0.8, "
+                           "cells >= 4.2, LJ + bonds + angles, FP32 forces, dt 0.002, 500 steps from the start")
+    finally:
+        g.close()
 
 
 def drift_leg(args, local, model=None):

@@ -217,11 +217,13 @@ class OracleSim:
     def _forces(self, nbins, max_sigma, with_atm_virial, ncount, listless):
         if listless:
             # large systems: LJ straight from the cells, no materialised pair list
-            if self.use_fene or self.bonded is not None or nbins or ncount:
-                raise ValueError("listless forces cover LJ, Limit and ATM only")
+            if self.use_fene or nbins or ncount:
+                raise ValueError("listless forces cover LJ, the bonded terms, Limit and ATM only")
             if self.use_lj:
                 self.L.kor_lj_cells(C.byref(self.g), C.byref(self.cells), _p(self.r), _p(self.eps), _p(self.sig),
                                     _p(self.id), self.cutoff, _p(self.f), C.byref(self.lj_out))
+            if self.bonded is not None:
+                self._bonded_forces()
             self.L.kor_limit(self.n, _p(self.eps), _p(self.sig), self.limit, _p(self.f))
             if self.use_atm:
                 self.atm_forces(with_atm_virial)
@@ -246,16 +248,19 @@ class OracleSim:
             self.L.kor_fene(pairs.shape[0], _p(pairs), _p(shifts), _p(self.r), _p(self.eps), _p(self.sig),
                             _p(self.id), self.stiffness, _p(self.f))
         if self.bonded is not None:
-            b = self.bonded
-            bonds = np.ascontiguousarray(b["bonds"], np.int64)
-            angles = np.ascontiguousarray(b["angles"], np.int64)
-            w = np.zeros(6)
-            self.e_bonded = self.L.kor_bonded(bonds.shape[0], _p(bonds), b["kb"], b["r0"], angles.shape[0],
-                                              _p(angles), b["ka"], b["theta0"], _p(self.r), None, _p(self.f), _p(w))
-            self.w_bonded = w
+            self._bonded_forces()
         self.L.kor_limit(self.n, _p(self.eps), _p(self.sig), self.limit, _p(self.f))
         if self.use_atm:
             self.atm_forces(with_atm_virial)
+
+    def _bonded_forces(self):
+        b = self.bonded
+        bonds = np.ascontiguousarray(b["bonds"], np.int64)
+        angles = np.ascontiguousarray(b["angles"], np.int64)
+        w = np.zeros(6)
+        self.e_bonded = self.L.kor_bonded(bonds.shape[0], _p(bonds), b["kb"], b["r0"], angles.shape[0],
+                                          _p(angles), b["ka"], b["theta0"], _p(self.r), None, _p(self.f), _p(w))
+        self.w_bonded = w
 
     def atm_forces(self, with_virial=False):
         if self.atm_mode == "compat":
