@@ -241,9 +241,8 @@ REPLICAS = dict(count=512, n_min=2000, n_max=20000, rho=(0.70, 0.90), t=(0.6, 1.
 
 
 def replica_specs(count, seed):
-    rng = np.random.default_rng(seed)
-    return [(int(rng.integers(1 << 30)), int(rng.integers(REPLICAS["n_min"], REPLICAS["n_max"] + 1)),
-             float(rng.uniform(*REPLICAS["rho"])), float(rng.uniform(*REPLICAS["t"]))) for _ in range(count)]
+    from komd_gb300 import lattice
+    return lattice.replica_specs(count, seed, REPLICAS["n_min"], REPLICAS["n_max"], REPLICAS["rho"], REPLICAS["t"])
 
 
 def replicas_leg(args, stream, local):
@@ -289,7 +288,12 @@ def replicas_leg(args, stream, local):
     tuned = None
     if not args.replica_fixed:
         from komd_gb300 import autotune
-        tuned = autotune.tune_batch(reps, streams=(16, 32, 64), graph_steps=(1, 5, 10), steps=10)
+        # packed batches: groups of replicas on parallel branches (1-8); the branch form wants more branches
+        probe = gpu.Batch(reps[:2], n_streams=1, steps_per_graph=1, stream=stream.cuda_stream)
+        packed = probe.packed
+        probe.close()
+        tuned = autotune.tune_batch(reps, streams=(1, 2, 4, 8) if packed else (16, 32, 64), graph_steps=(1, 5, 10),
+                                    steps=10)
         spg, nstr = tuned["best"]["steps_per_graph"], tuned["best"]["streams"]
     t2 = time.perf_counter()
     batch = gpu.Batch(reps, n_streams=nstr, steps_per_graph=spg, stream=stream.cuda_stream)

@@ -319,7 +319,9 @@ int     komd_sur_fit_grad(komd_sur_data *d, const float *params, const float *fm
 /* Independent engines (replicas of uneven sizes, each created, uploaded and
  * past update_container + forces) advance together: one CUDA graph holds
  * steps_per_graph steps of every replica, spread over n_streams parallel
- * branches.  stream (may be NULL) is the stream the graph is launched on.
+ * branches (the packed form: the replicas split into n_streams contiguous
+ * groups of about equal atom counts, each group one launch per stage on its
+ * own branch).  stream (may be NULL) is the stream the graph is launched on.
  * Replicas must not be modified (upload, set_state, update_container) while
  * the batch exists; the exact forces run (no learned-term probes). */
 typedef struct komd_batch komd_batch;

@@ -1720,8 +1720,8 @@ struct komd_batch {
     std::vector<cudaEvent_t> ev;          // [0] fork, [1..n_streams] joins
     cudaGraphExec_t graph = nullptr;
     int64_t steps = 0;
-    bool packed = false;                  // one launch per stage for all replicas
-    PackedStep pk;
+    bool packed = false;                  // one launch per stage for all replicas of a group
+    std::vector<PackedStep> pk;           // the packed groups (contiguous replica ranges)
     std::vector<void *> pk_mem;           // the packed tables (device)
     ~komd_batch() {
         cudaSetDevice(device);
@@ -1774,12 +1774,12 @@ int packed_stage(komd_batch *b, PackedStage &s, const std::vector<T> &args, cons
     return KOMD_OK;
 }
 
-int packed_build(komd_batch *b) {
-    PackedStep &pk = b->pk;
-    const int nr = (int)b->reps.size();
+int packed_group(komd_batch *b, PackedStep &pk, int r0, int r1, int pr) {
+    const std::vector<komd_gpu *> reps(b->reps.begin() + r0, b->reps.begin() + r1);
+    const int nr = r1 - r0;
     pk.nrep = nr;
-    pk.uniform = b->reps[0]->e.uniform;
-    pk.sw = b->reps[0]->e.cfg.switch_width > 0;
+    pk.uniform = reps[0]->e.uniform;
+    pk.sw = reps[0]->e.cfg.switch_width > 0;
     std::vector<Step0Args> s0;
     std::vector<BinArgs> bi;
     std::vector<ScanArgs> sc;
@@ -1790,14 +1790,7 @@ int packed_build(komd_batch *b) {
     std::vector<AtmParams> ap;
     std::vector<float> sa;
     std::vector<int> n, per, two, b_io, b_cont, b_sort, b_vb, b_force;
-    // groups of 8 sites per block of the force pass: about eight resident waves
-    // over all replicas together, each block over a contiguous range of one
-    // replica's slots (the single-system rule, vlist_per, over the batch)
-    long long groups = 0;
-    for (komd_gpu *h : b->reps) groups += vlist_grid(h->e);
-    const long long target = (long long)b->reps[0]->e.num_sms * 5 * 8;
-    const int pr = (int)std::max<long long>(1, (groups + target - 1) / target);
-    for (komd_gpu *h : b->reps) {
+    for (komd_gpu *h : reps) {
         Engine &e = h->e;
         s0.push_back(step0_args(e));
         bi.push_back(bin_args(e));
@@ -1815,7 +1808,7 @@ int packed_build(komd_batch *b) {
         two.push_back(vbuild_two(e) ? 1 : 0);
         b_io.push_back((int)((e.n + 255) / 256));
         b_cont.push_back(packed_blocks_container(e));
-        b_sort.push_back(std::max(1, std::min((e.g.ncell + kWarpsPerBlock - 1) / kWarpsPerBlock, 8)));
+        b_sort.push_back(std::max(1, std::min((e.g.ncell + kWarpsPerBlock - 1) / kWarpsPerBlock, 16)));
         b_vb.push_back(packed_blocks_vbuild(e));
         b_force.push_back((vlist_grid(e) + pr - 1) / pr);
         pk.force_smem = std::max(pk.force_smem, lj_atm_half_smem(e));
@@ -1838,12 +1831,53 @@ int packed_build(komd_batch *b) {
     return rc;
 }
 
+int packed_build(komd_batch *b) {
+    // groups of 8 sites per block of the force pass: about eight resident waves
+    // over all replicas together, each block over a contiguous range of one
+    // replica's slots (the single-system rule, vlist_per, over the batch)
+    long long groups = 0, atoms = 0;
+    for (komd_gpu *h : b->reps) { groups += vlist_grid(h->e); atoms += h->e.n; }
+    const long long target = (long long)b->reps[0]->e.num_sms * 5 * 8;
+    const int pr = (int)std::max<long long>(1, (groups + target - 1) / target);
+    const int nr = (int)b->reps.size();
+    // one group per graph branch: a group's stage boundaries (where its
+    // launch drains) overlap the other groups' work
+    const int G = std::max(1, std::min(nr, (int)b->branch.size()));
+    b->pk.assign(G, PackedStep());
+    // contiguous ranges of about atoms / G sites each
+    int r0 = 0;
+    long long acc = 0;
+    for (int g = 0; g < G; g++) {
+        int r1 = r0 + 1;
+        acc += b->reps[r0]->e.n;
+        while (r1 < nr - (G - 1 - g) && (g == G - 1 || acc < atoms * (g + 1) / G)) acc += b->reps[r1++]->e.n;
+        if (g == G - 1) r1 = nr;
+        const int rc = packed_group(b, b->pk[g], r0, r1, pr);
+        if (rc) return rc;
+        r0 = r1;
+    }
+    return KOMD_OK;
+}
+
 int batch_capture(komd_batch *b) {
-    if (b->packed) {   // one stream: steps_per_graph x eight stage launches
+    if (b->packed) {   // per group: steps_per_graph x eight stage launches on its own branch
         CK(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal));
-        for (int k = 0; k < b->steps_per_graph; k++) launch_packed_step(b->pk, b->origin);
+        const int G = (int)b->pk.size();
+        cudaError_t ce = cudaSuccess;
+        if (G == 1) {
+            for (int k = 0; k < b->steps_per_graph; k++) launch_packed_step(b->pk[0], b->origin);
+        } else {
+            ce = cudaEventRecord(b->ev[0], b->origin);
+            for (int g = 0; g < G && ce == cudaSuccess; g++) ce = cudaStreamWaitEvent(b->branch[g], b->ev[0], 0);
+            for (int g = 0; g < G && ce == cudaSuccess; g++)
+                for (int k = 0; k < b->steps_per_graph; k++) launch_packed_step(b->pk[g], b->branch[g]);
+            for (int g = 0; g < G && ce == cudaSuccess; g++) {
+                ce = cudaEventRecord(b->ev[1 + g], b->branch[g]);
+                if (ce == cudaSuccess) ce = cudaStreamWaitEvent(b->origin, b->ev[1 + g], 0);
+            }
+        }
         cudaGraph_t graph = nullptr;
-        const cudaError_t le = cudaGetLastError();
+        const cudaError_t le = ce != cudaSuccess ? ce : cudaGetLastError();
         const cudaError_t ee = cudaStreamEndCapture(b->origin, &graph);
         if (le != cudaSuccess || ee != cudaSuccess) {
             if (graph) cudaGraphDestroy(graph);

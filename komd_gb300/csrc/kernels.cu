@@ -1939,7 +1939,10 @@ __global__ void __launch_bounds__(kIoBlock) k_atm_flush_step1_p(const FlushArgs 
     flush_step1_body(a[r], blockIdx.x - start[r]);
 }
 
-int packed_blocks_container(const Engine &e) { return std::max(1, std::min(nblk(e.n_mol, 256), 8)); }
+// blocks per replica of the container stages: on a step without a rebuild
+// they exit at once; on a rebuild step a replica's blocks do its whole
+// binning, so too few of them make a long tail for the launch
+int packed_blocks_container(const Engine &e) { return std::max(1, std::min(nblk(e.n_mol, 256), 16)); }
 
 // one step of every replica: the stages of enqueue_step on the Verlet path
 // with the fused drift and the half-list pass, each stage one launch

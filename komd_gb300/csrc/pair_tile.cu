@@ -931,7 +931,9 @@ void launch_packed_pair_stages(const PackedStep &pk, cudaStream_t st, bool vbuil
 }
 
 int packed_blocks_vbuild(const Engine &e) {
-    return std::max(1, std::min((e.g.ncell + kVbWarps - 1) / kVbWarps, 12));
+    // up to 1024 warps for a rebuilding replica (a warp per home cell here);
+    // the blocks of replicas without a rebuild exit at once
+    return std::max(1, std::min((e.g.ncell + kVbWarps - 1) / kVbWarps, 256));
 }
 
 bool vbuild_two(const Engine &e) {

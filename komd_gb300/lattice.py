@@ -110,6 +110,17 @@ def trimmed_fcc(n_target: int, rho: float, t_star: float, seed: int) -> System:
                   mol_id=np.arange(1, n_target + 1, dtype=np.uint64), low=np.zeros(3), high=L)
 
 
+def replica_specs(count: int, seed: int, n_min: int = 2000, n_max: int = 20000, rho=(0.70, 0.90),
+                  t_star=(0.6, 1.5)) -> list:
+    """(lattice seed, atoms, rho*, T*) of each replica of the batched-replica
+    workload: atom counts uniform in [n_min, n_max], rho* and T* uniform in
+    their ranges, all drawn from one seeded generator (build each with
+    trimmed_fcc)."""
+    rng = np.random.default_rng(seed)
+    return [(int(rng.integers(1 << 30)), int(rng.integers(n_min, n_max + 1)), float(rng.uniform(*rho)),
+             float(rng.uniform(*t_star))) for _ in range(count)]
+
+
 def _rotation(rng: np.random.Generator) -> np.ndarray:
     q = rng.standard_normal(4)
     q /= np.linalg.norm(q)

@@ -2,7 +2,7 @@
 
     python -m komd_gb300.profile_cases exact      [--ncell 40] [--steps 3] [--equil 0] [--skin 0.3] [--cell 2.8]
     python -m komd_gb300.profile_cases surrogate  [--ncell 40] [--steps 3]
-    python -m komd_gb300.profile_cases replicas   [--count 64] [--steps 2]
+    python -m komd_gb300.profile_cases replicas   [--count 64] [--steps 2] [--equil 0] [--groups 4]
     python -m komd_gb300.profile_cases tabulated  [--ncell 40] [--steps 3]
 
 `exact`: LJ + FULL ATM argon (rho* 0.8442, T* 0.722, rc 2.5 / 2.0, nu* 0.073,
@@ -10,8 +10,9 @@ cell 2.8, skin 0.3 by default; the benchmark's timed configuration is
 --skin 0.4 --cell 0 (cell 0: the smallest edge >= 2.5 + skin that divides the
 box) --equil 400).  `surrogate`: the
 same with the learned three-body term on Glorot-initialised weights (kernel
-cost does not depend on the weights).  `replicas`: `count` uneven replicas
-(2000-20000 atoms) advanced by one batched graph.  `tabulated`: the IBI
+cost does not depend on the weights).  `replicas`: the first `count` of the
+benchmark's uneven replicas (2000-20000 atoms) advanced by one batched graph
+(`groups` packed groups) after `equil` steps.  `tabulated`: the IBI
 tabulated pair force (FP64, per-step cells of edge >= 2.5, a 200-node table
 of the LJ force) on the jittered lattice, then one RDF_Profiler sample (100
 bins to 2.5).  Each prints its mean step
@@ -52,18 +53,18 @@ def exact(ncell, steps, equil, learned=False, skin=0.3, cell=2.8):
     g.close()
 
 
-def replicas(count, steps):
-    rng = np.random.default_rng(2027)
+def replicas(count, steps, equil=0, groups=4):
     reps = []
-    for _ in range(count):
-        s = lattice.trimmed_fcc(int(rng.integers(2000, 20001)), float(rng.uniform(0.7, 0.9)),
-                                float(rng.uniform(0.6, 1.5)), int(rng.integers(1 << 30)))
+    for seed, n, rho, t_star in lattice.replica_specs(count, 2027):   # the benchmark's replicas
+        s = lattice.trimmed_fcc(n, rho, t_star, seed)
         L = float(s.high[0])
         g = gpu.GpuSystem(s, surrogate.physics_config(s, L / np.floor(L / 2.8), skin=0.3))
         g.update_container()
         g.forces()
         reps.append(g)
-    b = gpu.Batch(reps, n_streams=32, steps_per_graph=1)
+    b = gpu.Batch(reps, n_streams=groups, steps_per_graph=1)
+    if equil:
+        b.step(equil)
     t0 = time.perf_counter()
     b.step(steps)
     dt = (time.perf_counter() - t0) / steps
@@ -98,11 +99,12 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--equil", type=int, default=0)
     ap.add_argument("--count", type=int, default=64)
+    ap.add_argument("--groups", type=int, default=4)
     ap.add_argument("--skin", type=float, default=0.3)
     ap.add_argument("--cell", type=float, default=2.8)
     a = ap.parse_args()
     if a.case == "replicas":
-        replicas(a.count, a.steps)
+        replicas(a.count, a.steps, a.equil, a.groups)
     elif a.case == "tabulated":
         tabulated(a.ncell, a.steps)
     else:

@@ -22,11 +22,13 @@ def _replica(seed, n, rho, t_star, skin=0.3):
     return g
 
 
-def test_batch_matches_single_system_path():
+@pytest.mark.parametrize("groups", [1, 3])
+def test_batch_matches_single_system_path(groups):
+    """Packed form, all replicas in one group, and in three groups on parallel branches."""
     from komd_gb300 import gpu
     a = [_replica(*sp) for sp in SPECS]
     b = [_replica(*sp) for sp in SPECS]
-    batch = gpu.Batch(a, n_streams=3, steps_per_graph=5)
+    batch = gpu.Batch(a, n_streams=groups, steps_per_graph=5)
     assert batch.packed                             # the Verlet path's replicas: one launch per stage
     batch.step(6)                                   # 30 steps
     for g in b:

@@ -13,13 +13,24 @@ without overlaps and, with no cap, keeps the molecules intact.  The GPU runs
 of this workload use that orientation; these tests record why, at the same
 density on a smaller box, with the oracle's reference-semantics forces.
 """
+import os
+
 import numpy as np
 import pytest
 
 N_MOL = 4096
 RHO_SITE = 0.8
-STEPS = 200
+STEPS = 100
 DT = 0.002
+
+
+@pytest.fixture(autouse=True)
+def _all_cores(oracle_lib):
+    """The oracle on every core (another test may have left it on one)."""
+    keep = oracle_lib.num_threads()
+    oracle_lib.set_threads(os.cpu_count() or 1)
+    yield
+    oracle_lib.set_threads(keep)
 
 
 def _setup(oracle_lib, aligned, limit):
