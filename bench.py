@@ -251,7 +251,8 @@ def replicas_leg(args, stream, local):
     T* ~ U[0.6, 1.5], FP32 forces / FP64 integration; all replicas advance
     in one CUDA-graph launch per graph (komd_batch).  Compared with the same
     replicas stepped one after another through the single-system path; then
-    per-replica RDF (200 bins to 2.5) and virial pressure."""
+    per-replica RDF (200 bins to 2.5), virial pressure and temperature from
+    the batch (komd_batch_measure)."""
     import torch
     from komd_gb300 import gpu, komd_io, lattice
     R = REPLICAS
@@ -298,6 +299,7 @@ def replicas_leg(args, stream, local):
     t2 = time.perf_counter()
     batch = gpu.Batch(reps, n_streams=nstr, steps_per_graph=spg, stream=stream.cuda_stream)
     capture_s = time.perf_counter() - t2
+    form = "packed" if batch.packed else "branch"
     batch.step(max(1, 3 // spg))
     torch.cuda.synchronize()
     n_graphs = max(1, k // spg)
@@ -312,12 +314,14 @@ def replicas_leg(args, stream, local):
     steps = n_graphs * spg
     value = n_atoms * steps / (ms / 1e3)
     seq_value = n_atoms * k / seq_s
+    # per-replica virial pressure, RDF and temperature from the batch (komd_batch_measure)
+    t3 = time.perf_counter()
+    obs = batch.measure(gpu.MEASURE_PRESSURE | gpu.MEASURE_RDF | gpu.MEASURE_TEMPERATURE)
+    measure_s = time.perf_counter() - t3
     batch.close()
-    # per-replica observables after the run
     pres, peaks, temps = [], [], []
     dr = R["rdf_max"] / R["rdf_bins"]
-    for g, vol, n in zip(reps, vols, sizes):
-        o = g.measure(gpu.MEASURE_PRESSURE | gpu.MEASURE_RDF | gpu.MEASURE_TEMPERATURE)
+    for g, o, vol, n in zip(reps, obs, vols, sizes):
         pres.append((o["pressure"][0] + o["pressure"][2] + o["pressure"][5]) / (3.0 * vol))
         r, gr = komd_io.rdf_normalise(o["rdf"], 1, dr, vol, n)
         peaks.append(float(r[int(np.argmax(gr))]))
@@ -327,6 +331,7 @@ def replicas_leg(args, stream, local):
             "ms_per_step": ms / steps, "sequential": {"value": seq_value, "steps": k, "s": seq_s},
             "speedup_vs_sequential": value / seq_value, "streams": nstr, "autotune": tuned,
             "steps_per_graph": spg, "setup_s": setup_s, "capture_s": capture_s, "clocks": clk.summary(),
+            "measure_s": measure_s, "form": form,
             "pressure_star": {"min": float(np.min(pres)), "median": float(np.median(pres)), "max": float(np.max(pres))},
             "rdf_first_peak_r": {"min": float(np.nanmin(peaks)), "median": float(np.nanmedian(peaks)),
                                  "max": float(np.nanmax(peaks))},

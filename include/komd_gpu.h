@@ -334,6 +334,13 @@ int  komd_batch_step(komd_batch *b, int64_t n_graphs);
 /* Launches only (asynchronous); komd_batch_check synchronises and checks. */
 int  komd_batch_launch(komd_batch *b, int64_t n_graphs);
 int  komd_batch_check(komd_batch *b);
+/* Every replica's observables after the batch's steps, as komd_gpu_measure
+ * gives them (same mask; obs: one per replica; rdf: the replicas' RDF bins
+ * one after another, komd_gpu_rdf_bins each, may be NULL).  The measures are
+ * enqueued on the batch's branches behind its graph launches, with one
+ * synchronisation for all; no counterpart in the reference (which has one
+ * system per process). */
+int  komd_batch_measure(komd_batch *b, uint32_t mask, komd_observables *obs, double *rdf);
 /* 1 when the batch advances all replicas by one launch per stage of the step
  * (every replica on the Verlet path with the fused drift and the half-list
  * LJ + ATM pass: the packed form), 0 when it replays each replica's own

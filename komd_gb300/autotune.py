@@ -5,8 +5,8 @@ The physics does not depend on these parameters; only the speed does:
 * single system: the Verlet skin (list length against rebuild frequency) and
   with it the cell edge (the smallest edge >= cutoff + skin that divides the
   box, so that the 27-cell stencil covers the list range);
-* batched replicas: the number of parallel graph branches and the steps
-  captured per graph.
+* batched replicas: the number of parallel graph branches (for a packed
+  batch, the groups of replicas) and the steps captured per graph.
 
 Each candidate is timed on the caller's actual state (positions and
 velocities), after a warm-up that includes the graph capture, by the

@@ -400,6 +400,65 @@ int validate(const komd_config *c, Grid &g) {
     return KOMD_OK;
 }
 
+// the launches of a measure on the engine's stream, and the copies of the
+// sums (acc_h, R_NSLOTS doubles), the RDF and the LJ histograms to the host
+// buffers given (asynchronous: valid once the stream has synchronised)
+int measure_enqueue(komd_gpu *h, uint32_t mask, double *acc_h, double *rdf, double *lj_hist) {
+    Engine &e = h->e;
+    cudaStream_t st = e.stream;
+    ProfScope ps(h, F_MEASURE);
+    CK(cudaMemsetAsync(h->acc, 0, sizeof(double) * R_NSLOTS, st));
+    const bool need_forces = (mask & (KOMD_MEASURE_ENERGY | KOMD_MEASURE_PRESSURE | KOMD_MEASURE_LJ_HIST)) != 0;
+    if (need_forces) {
+        // re-evaluate the force terms into a scratch force buffer (the sensors of
+        // the reference re-run their functors as well); f itself is untouched
+        if (mask & KOMD_MEASURE_LJ_HIST) CK(cudaMemsetAsync(e.lj_hist, 0, sizeof(double) * 4 * e.cfg.lj_bins, st));
+        double *keep = e.f;
+        const uint32_t force_terms = e.cfg.terms;
+        CK(cudaMemsetAsync(h->f_scratch, 0, sizeof(double) * 3 * e.n, st));
+        e.f = h->f_scratch;
+        e.cfg.terms = h->sensor_terms;
+        enqueue_forces(h, true, (mask & KOMD_MEASURE_LJ_HIST) ? e.lj_hist : nullptr);
+        e.cfg.terms = force_terms;
+        e.f = keep;
+    }
+    const int n_terms = e.cfg.virial_mode == KOMD_VIRIAL_COMPAT ? (int)e.n_mol : (int)e.n;
+    launch_kinetic(e, st, n_terms);
+    launch_sum_partials(st, kinetic_grid(e), e.partials, h->acc);
+    if ((mask & KOMD_MEASURE_RDF) && e.rdf_bins > 0) {
+        if (e.verlet) launch_rebuild(h);   // the cells of the last rebuild may be stale
+        CK(cudaMemsetAsync(e.rdf, 0, sizeof(double) * e.rdf_bins, st));
+        double minw = 1e300;
+        for (int d = 0; d < 3; d++) minw = std::min(minw, e.cfg.cell_size);
+        launch_rdf(e, st, e.rdf, e.cfg.rdf_max <= minw);
+    }
+    int rc = check_launch("measure");
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(acc_h, h->acc, sizeof(double) * R_NSLOTS, cudaMemcpyDeviceToHost, st));
+    if (rdf && (mask & KOMD_MEASURE_RDF) && e.rdf_bins > 0)
+        CK(cudaMemcpyAsync(rdf, e.rdf, sizeof(double) * e.rdf_bins, cudaMemcpyDeviceToHost, st));
+    if (lj_hist && (mask & KOMD_MEASURE_LJ_HIST))
+        CK(cudaMemcpyAsync(lj_hist, e.lj_hist, sizeof(double) * 4 * e.cfg.lj_bins, cudaMemcpyDeviceToHost, st));
+    return KOMD_OK;
+}
+
+void measure_fill(const double *acc, komd_observables *obs) {
+    std::memset(obs, 0, sizeof(*obs));
+    obs->mv2 = acc[R_MV2];
+    obs->n_in_box = acc[R_NBOX];
+    obs->temperature = acc[R_NBOX] > 0 ? temperature_from(acc[R_MV2], acc[R_NBOX]) : 0.0;
+    obs->u_lj = acc[R_ULJ];
+    obs->u_atm = acc[R_UATM];
+    obs->u_bonded = acc[R_UBOND];
+    for (int k = 0; k < 6; k++) {
+        obs->kinetic[k] = acc[R_K0 + k];
+        obs->virial[k] = acc[R_W0 + k];
+        obs->pressure[k] = obs->kinetic[k] + obs->virial[k];
+    }
+    obs->pairs_in_cutoff = (int64_t)std::llround(acc[R_PAIRS]);
+    obs->triplets = (int64_t)std::llround(acc[R_TRIPS]);
+}
+
 }  // namespace
 
 extern "C" {
@@ -1097,62 +1156,17 @@ int64_t komd_gpu_rdf_bins(komd_gpu *h) { return h ? h->e.rdf_bins : -1; }
 
 int komd_gpu_measure(komd_gpu *h, uint32_t mask, komd_observables *obs, double *rdf, double *lj_hist) {
     if (!h || !obs) return fail(KOMD_ERR_ARG, "null argument");
-    Engine &e = h->e;
-    if (!e.have_cells) return fail(KOMD_ERR_STATE, "update_container must run before measure");
+    if (!h->e.have_cells) return fail(KOMD_ERR_STATE, "update_container must run before measure");
     std::memset(obs, 0, sizeof(*obs));
-    cudaStream_t st = e.stream;
-    ProfScope ps(h, F_MEASURE);
-    CK(cudaMemsetAsync(h->acc, 0, sizeof(double) * R_NSLOTS, st));
-    const bool need_forces = (mask & (KOMD_MEASURE_ENERGY | KOMD_MEASURE_PRESSURE | KOMD_MEASURE_LJ_HIST)) != 0;
-    if (need_forces) {
-        // re-evaluate the force terms into a scratch force buffer (the sensors of
-        // the reference re-run their functors as well); f itself is untouched
-        if (mask & KOMD_MEASURE_LJ_HIST) CK(cudaMemsetAsync(e.lj_hist, 0, sizeof(double) * 4 * e.cfg.lj_bins, st));
-        double *keep = e.f;
-        const uint32_t force_terms = e.cfg.terms;
-        CK(cudaMemsetAsync(h->f_scratch, 0, sizeof(double) * 3 * e.n, st));
-        e.f = h->f_scratch;
-        e.cfg.terms = h->sensor_terms;
-        enqueue_forces(h, true, (mask & KOMD_MEASURE_LJ_HIST) ? e.lj_hist : nullptr);
-        e.cfg.terms = force_terms;
-        e.f = keep;
-    }
-    const int n_terms = e.cfg.virial_mode == KOMD_VIRIAL_COMPAT ? (int)e.n_mol : (int)e.n;
-    launch_kinetic(e, st, n_terms);
-    launch_sum_partials(st, kinetic_grid(e), e.partials, h->acc);
-    if ((mask & KOMD_MEASURE_RDF) && e.rdf_bins > 0) {
-        if (e.verlet) launch_rebuild(h);   // the cells of the last rebuild may be stale
-        CK(cudaMemsetAsync(e.rdf, 0, sizeof(double) * e.rdf_bins, st));
-        double minw = 1e300;
-        for (int d = 0; d < 3; d++) minw = std::min(minw, e.cfg.cell_size);
-        launch_rdf(e, st, e.rdf, e.cfg.rdf_max <= minw);
-    }
-    int rc = check_launch("measure");
-    if (rc) return rc;
     double acc[R_NSLOTS];
-    CK(cudaMemcpyAsync(acc, h->acc, sizeof(acc), cudaMemcpyDeviceToHost, st));
-    if (rdf && (mask & KOMD_MEASURE_RDF) && e.rdf_bins > 0)
-        CK(cudaMemcpyAsync(rdf, e.rdf, sizeof(double) * e.rdf_bins, cudaMemcpyDeviceToHost, st));
-    if (lj_hist && (mask & KOMD_MEASURE_LJ_HIST))
-        CK(cudaMemcpyAsync(lj_hist, e.lj_hist, sizeof(double) * 4 * e.cfg.lj_bins, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
+    int rc = measure_enqueue(h, mask, acc, rdf, lj_hist);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(h->e.stream));
     int flags[E_NFLAGS];
     rc = read_flags(h, flags, true);
     if (rc) return rc;
     if (flags[E_ATM_OVERFLOW]) return fail(KOMD_ERR_OVERFLOW, "ATM neighbour list overflow during measure");
-    obs->mv2 = acc[R_MV2];
-    obs->n_in_box = acc[R_NBOX];
-    obs->temperature = acc[R_NBOX] > 0 ? temperature_from(acc[R_MV2], acc[R_NBOX]) : 0.0;
-    obs->u_lj = acc[R_ULJ];
-    obs->u_atm = acc[R_UATM];
-    obs->u_bonded = acc[R_UBOND];
-    for (int k = 0; k < 6; k++) {
-        obs->kinetic[k] = acc[R_K0 + k];
-        obs->virial[k] = acc[R_W0 + k];
-        obs->pressure[k] = obs->kinetic[k] + obs->virial[k];
-    }
-    obs->pairs_in_cutoff = (int64_t)std::llround(acc[R_PAIRS]);
-    obs->triplets = (int64_t)std::llround(acc[R_TRIPS]);
+    measure_fill(acc, obs);
     return KOMD_OK;
 }
 
@@ -1723,8 +1737,11 @@ struct komd_batch {
     bool packed = false;                  // one launch per stage for all replicas of a group
     std::vector<PackedStep> pk;           // the packed groups (contiguous replica ranges)
     std::vector<void *> pk_mem;           // the packed tables (device)
+    double *stage = nullptr;              // pinned landing area of komd_batch_measure
+    size_t stage_cap = 0;                 // in doubles
     ~komd_batch() {
         cudaSetDevice(device);
+        if (stage) cudaFreeHost(stage);
         for (void *p : pk_mem) cudaFree(p);
         if (graph) cudaGraphExecDestroy(graph);
         for (auto s : branch) cudaStreamDestroy(s);
@@ -1994,6 +2011,71 @@ int komd_batch_launch(komd_batch *b, int64_t n_graphs) {
     if (!b) return fail(KOMD_ERR_ARG, "null batch");
     for (int64_t k = 0; k < n_graphs; k++) CK(cudaGraphLaunch(b->graph, b->origin));
     b->steps += n_graphs * b->steps_per_graph;
+    return KOMD_OK;
+}
+
+int komd_batch_measure(komd_batch *b, uint32_t mask, komd_observables *obs, double *rdf) {
+    if (!b || !obs) return fail(KOMD_ERR_ARG, "null argument");
+    CK(cudaSetDevice(b->device));
+    const int nr = (int)b->reps.size();
+    size_t bins = 0;
+    for (komd_gpu *h : b->reps) {
+        if (!h->e.have_cells) return fail(KOMD_ERR_STATE, "update_container must run before measure");
+        if ((mask & KOMD_MEASURE_RDF) && h->e.rdf_bins > 0) bins += (size_t)h->e.rdf_bins;
+    }
+    // pinned landing area: per replica the sums and the error flags, then the RDF bins
+    const size_t per = R_NSLOTS + E_NFLAGS;
+    const size_t need = (size_t)nr * per + bins;
+    if (need > b->stage_cap) {
+        if (b->stage) cudaFreeHost(b->stage);
+        b->stage = nullptr;
+        b->stage_cap = 0;
+        CK(cudaMallocHost(reinterpret_cast<void **>(&b->stage), sizeof(double) * need));
+        b->stage_cap = need;
+    }
+    // the measures follow the batch's graph launches on the origin stream and
+    // spread over its branches; the origin waits for all of them
+    CK(cudaEventRecord(b->ev[0], b->origin));
+    const int nb = (int)b->branch.size();
+    for (int k = 0; k < nb; k++) CK(cudaStreamWaitEvent(b->branch[k], b->ev[0], 0));
+    size_t off = (size_t)nr * per;
+    int rc = KOMD_OK;
+    for (int r = 0; r < nr && !rc; r++) {
+        Engine &e = b->reps[r]->e;
+        cudaStream_t keep = e.stream;
+        e.stream = b->branch[r % nb];
+        double *slot = b->stage + (size_t)r * per;
+        const bool with_rdf = (mask & KOMD_MEASURE_RDF) && e.rdf_bins > 0;
+        rc = measure_enqueue(b->reps[r], mask, slot, with_rdf ? b->stage + off : nullptr, nullptr);
+        if (!rc) {
+            // the flags as read_flags reads them (read, then cleared), into the landing area
+            int *fl = reinterpret_cast<int *>(slot + R_NSLOTS);
+            if (cudaMemcpyAsync(fl, e.err, sizeof(int) * E_NFLAGS, cudaMemcpyDeviceToHost, e.stream) != cudaSuccess ||
+                cudaMemsetAsync(e.err, 0, sizeof(int) * E_NFLAGS, e.stream) != cudaSuccess)
+                rc = fail(KOMD_ERR_CUDA, "measure flags");
+        }
+        if (with_rdf) off += (size_t)e.rdf_bins;
+        e.stream = keep;
+    }
+    for (int k = 0; k < nb; k++) {
+        if (cudaEventRecord(b->ev[1 + k], b->branch[k]) == cudaSuccess) cudaStreamWaitEvent(b->origin, b->ev[1 + k], 0);
+    }
+    CK(cudaStreamSynchronize(b->origin));
+    if (rc) return rc;
+    off = (size_t)nr * per;
+    for (int r = 0; r < nr; r++) {
+        const Engine &e = b->reps[r]->e;
+        const double *slot = b->stage + (size_t)r * per;
+        const int *fl = reinterpret_cast<const int *>(slot + R_NSLOTS);
+        if (fl[E_ATM_OVERFLOW])
+            return fail(KOMD_ERR_OVERFLOW, "replica " + std::to_string(r) + ": ATM neighbour list overflow during measure");
+        measure_fill(slot, obs + r);
+        if ((mask & KOMD_MEASURE_RDF) && e.rdf_bins > 0) {
+            if (rdf) std::memcpy(rdf, b->stage + off, sizeof(double) * (size_t)e.rdf_bins);
+            if (rdf) rdf += e.rdf_bins;
+            off += (size_t)e.rdf_bins;
+        }
+    }
     return KOMD_OK;
 }
 

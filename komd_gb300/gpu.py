@@ -8,7 +8,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
-from typing import Dict, Optional
+from typing import Dict, List, Optional
 
 import numpy as np
 
@@ -30,7 +30,7 @@ MEASURE_TEMPERATURE, MEASURE_ENERGY, MEASURE_PRESSURE, MEASURE_RDF, MEASURE_LJ_H
 
 EXPORTS = [
     "komd_gpu_create", "komd_gpu_destroy", "komd_gpu_last_error", "komd_gpu_abi_version", "komd_gpu_set_stream",
-    "komd_sci_temperature",
+    "komd_sci_temperature", "komd_batch_measure",
     "komd_gpu_grid_dims", "komd_gpu_upload_sites", "komd_gpu_set_state", "komd_gpu_set_topology",
     "komd_gpu_download", "komd_gpu_num_sites", "komd_gpu_update_container", "komd_gpu_forces",
     "komd_gpu_integrate0", "komd_gpu_integrate1", "komd_gpu_step", "komd_gpu_step_host", "komd_gpu_measure",
@@ -150,6 +150,7 @@ def load() -> C.CDLL:
     L.komd_batch_launch.argtypes = [P, I64]
     L.komd_batch_check.argtypes = [P]
     L.komd_batch_form.argtypes = [P]
+    L.komd_batch_measure.argtypes = [P, C.c_uint32, P, P]
     L.komd_sur_fit_grad.argtypes = [P, P, P, P, C.c_double, C.c_double, C.c_double, C.c_float, C.c_float, P, P,
                                     C.c_int32]
     _lib = L
@@ -482,6 +483,24 @@ class Batch:
 
     def check(self):
         self._check(self.L.komd_batch_check(self.h))
+
+    def measure(self, mask: int) -> List[Dict[str, object]]:
+        """Every replica's observables (komd_batch_measure), one dict per
+        replica as GpuSystem.measure gives it (no LJ histograms)."""
+        n = len(self.systems)
+        obs = (Observables * n)()
+        bins = [int(self.L.komd_gpu_rdf_bins(g.h)) if mask & MEASURE_RDF else 0 for g in self.systems]
+        rdf = np.zeros(max(sum(bins), 1))
+        self._check(self.L.komd_batch_measure(self.h, int(mask), C.cast(obs, C.c_void_p), _p(rdf)))
+        out, off = [], 0
+        for k in range(n):
+            d = {f: getattr(obs[k], f) for f, _ in Observables._fields_}
+            for f in ("kinetic", "virial", "pressure"):
+                d[f] = np.array(d[f][:])
+            d["rdf"] = rdf[off:off + bins[k]].copy() if bins[k] > 0 else None
+            off += bins[k]
+            out.append(d)
+        return out
 
     def close(self):
         if self.h:

@@ -44,6 +44,45 @@ def test_batch_matches_single_system_path(groups):
         g.close()
 
 
+def test_batch_measure_matches_replica_measures():
+    """komd_batch_measure (every replica's measure enqueued on the batch's
+    branches, one synchronisation) gives each replica what komd_gpu_measure
+    gives it alone: energies, virial, pressure, temperature and the RDF.
+    A measure with the RDF rebuilds the Verlet lists at the current positions
+    (its cells may be stale), which moves the FP32 cell-local coordinates of
+    the next measure's force pass by rounding: the first batched measure
+    agrees with a measure alone to FP32 precision, a second one (lists of the
+    same positions on both sides) to the last bits of the FP64 sums."""
+    from komd_gb300 import gpu
+    a = [_replica_rdf(*sp) for sp in SPECS]
+    batch = gpu.Batch(a, n_streams=2, steps_per_graph=5)
+    batch.step(2)
+    mask = gpu.MEASURE_ENERGY | gpu.MEASURE_PRESSURE | gpu.MEASURE_TEMPERATURE | gpu.MEASURE_RDF
+    first = batch.measure(mask)
+    together = batch.measure(mask)
+    batch.close()
+    for g, t0, t in zip(a, first, together):
+        alone = g.measure(mask)
+        assert np.array_equal(t["rdf"], alone["rdf"]) and np.array_equal(t0["rdf"], alone["rdf"])
+        assert t["rdf"].sum() > 0
+        for k in ("u_lj", "u_atm", "temperature", "mv2", "pairs_in_cutoff", "triplets"):
+            assert t[k] == pytest.approx(alone[k], rel=1e-12, abs=0), k
+            assert t0[k] == pytest.approx(alone[k], rel=1e-6, abs=0), k
+        np.testing.assert_allclose(t["pressure"], alone["pressure"], rtol=1e-12, atol=0)
+        g.close()
+
+
+def _replica_rdf(seed, n, rho, t_star):
+    from komd_gb300 import gpu, lattice, surrogate
+    s = lattice.trimmed_fcc(n, rho, t_star, seed)
+    cfg = surrogate.physics_config(s, float(s.high[0]) / np.floor(float(s.high[0]) / 2.8), skin=0.3)
+    cfg.rdf_max, cfg.rdf_dr = 2.5, 2.5 / 200
+    g = gpu.GpuSystem(s, cfg)
+    g.update_container()
+    g.forces()
+    return g
+
+
 def test_branch_form_matches_single_system_path():
     """Replicas on the per-step-cell path (no skin) take the branch form."""
     from komd_gb300 import gpu
