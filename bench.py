@@ -849,8 +849,8 @@ def main():
     ap.add_argument("--next-steps", type=int, default=20,
                     help="steps timed per configuration of the rows around the path (0 = skip)")
     ap.add_argument("--replica-steps", type=int, default=20)
-    ap.add_argument("--replica-streams", type=int, default=32)
-    ap.add_argument("--replica-graph-steps", type=int, default=5)
+    ap.add_argument("--replica-streams", type=int, default=4)
+    ap.add_argument("--replica-graph-steps", type=int, default=10)
     ap.add_argument("--replica-fixed", action="store_true", help="use --replica-streams/--replica-graph-steps as given")
     ap.add_argument("--sur-probe", type=int, default=50, help="exact-ATM probe interval of the learned form")
     ap.add_argument("--sur-threshold", type=float, default=0.02,
