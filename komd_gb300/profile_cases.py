@@ -4,6 +4,7 @@
     python -m komd_gb300.profile_cases surrogate  [--ncell 40] [--steps 3]
     python -m komd_gb300.profile_cases replicas   [--count 64] [--steps 2] [--equil 0] [--groups 4]
     python -m komd_gb300.profile_cases tabulated  [--ncell 40] [--steps 3]
+    python -m komd_gb300.profile_cases train      [--snaps 40] [--epochs 2] [--batch 4]
 
 `exact`: LJ + FULL ATM argon (rho* 0.8442, T* 0.722, rc 2.5 / 2.0, nu* 0.073,
 cell 2.8, skin 0.3 by default; the benchmark's timed configuration is
@@ -15,7 +16,8 @@ benchmark's uneven replicas (2000-20000 atoms) advanced by one batched graph
 (`groups` packed groups) after `equil` steps.  `tabulated`: the IBI
 tabulated pair force (FP64, per-step cells of edge >= 2.5, a 200-node table
 of the LJ force) on the jittered lattice, then one RDF_Profiler sample (100
-bins to 2.5).  Each prints its mean step
+bins to 2.5).  `train`: force-matched training of the learned term on a small
+dataset from the exact kernel.  Each prints its mean step
 time; the launches before the measured steps are few, so that a profiler can
 skip to them.
 """
@@ -74,6 +76,20 @@ def replicas(count, steps, equil=0, groups=4):
         g.close()
 
 
+def train(snaps, epochs, batch):
+    """Force-matched training on the GPU: a dataset of `snaps` snapshots of 500
+    sites from the exact kernel (the benchmark's training set is 2000), then
+    `epochs` passes of Adam steps over `batch` snapshots each (the network's
+    kernels on the tensor cores)."""
+    data = surrogate.capture(n_points=max(1, snaps // 10), snaps_per_point=10, ncell=5, equil=20, every=5)
+    t0 = time.perf_counter()
+    model = surrogate.fit_forces(data, epochs=epochs, snaps_per_batch=batch)
+    dt = time.perf_counter() - t0
+    print(f"train: {data.snapshots} snapshots x {data.sites} sites, {epochs} epochs: {dt:.3f} s "
+          f"(loss {model['loss'][-1].tolist()})")
+    data.close()
+
+
 def tabulated(ncell, steps):
     s = lattice.argon_fcc(ncell, rho=0.8442, t_star=0.722, seed=3, jitter=0.02)
     side = float(np.min(s.high - s.low))
@@ -94,16 +110,21 @@ def tabulated(ncell, steps):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["exact", "surrogate", "replicas", "tabulated"])
+    ap.add_argument("case", choices=["exact", "surrogate", "replicas", "tabulated", "train"])
     ap.add_argument("--ncell", type=int, default=40)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--equil", type=int, default=0)
     ap.add_argument("--count", type=int, default=64)
     ap.add_argument("--groups", type=int, default=4)
+    ap.add_argument("--snaps", type=int, default=40)
+    ap.add_argument("--epochs", type=int, default=2)
+    ap.add_argument("--batch", type=int, default=4)
     ap.add_argument("--skin", type=float, default=0.3)
     ap.add_argument("--cell", type=float, default=2.8)
     a = ap.parse_args()
-    if a.case == "replicas":
+    if a.case == "train":
+        train(a.snaps, a.epochs, a.batch)
+    elif a.case == "replicas":
         replicas(a.count, a.steps, a.equil, a.groups)
     elif a.case == "tabulated":
         tabulated(a.ncell, a.steps)
