@@ -263,9 +263,23 @@ bool enqueue_forces(komd_gpu *h, bool measure, double *lj_hist, bool with_step1 
 
 void enqueue_step(komd_gpu *h) {
     Engine &e = h->e;
+    // host-buffer step with a pinned position buffer: the drift kernel keeps r on
+    // the device and a copy-engine copy on the side stream writes it back while
+    // the container and force kernels run (joined before the step ends)
+    double *r_async = nullptr;
+    if (e.hout_r && e.hout_r_async && e.side && e.ev_fork && e.ev_join) {
+        r_async = e.hout_r;
+        e.hout_r = nullptr;
+    }
     {
         ProfScope ps(h, F_INTEGRATE);
         launch_step0(e, e.stream, true);
+    }
+    if (r_async) {
+        cudaEventRecord(e.ev_fork, e.stream);
+        cudaStreamWaitEvent(e.side, e.ev_fork, 0);
+        cudaMemcpyAsync(r_async, e.r, sizeof(double) * 3 * (size_t)e.n, cudaMemcpyDeviceToHost, e.side);
+        cudaEventRecord(e.ev_join, e.side);
     }
     {
         ProfScope ps(h, F_CONTAINER);
@@ -282,6 +296,10 @@ void enqueue_step(komd_gpu *h) {
         launch_kinetic(e, e.stream, 0);
         launch_sum_partials(e.stream, kinetic_grid(e), e.partials, h->thermo_acc);
         launch_velocity_scale(e, e.stream, h->thermo_acc, 1.0);
+    }
+    if (r_async) {
+        cudaStreamWaitEvent(e.stream, e.ev_join, 0);
+        e.hout_r = r_async;
     }
 }
 
@@ -499,6 +517,12 @@ int komd_gpu_create(const komd_config *cfg, int device, komd_gpu **out) {
         return fail(KOMD_ERR_CUDA, "stream creation failed");
     }
     e.own_stream = true;
+    if (cudaStreamCreateWithFlags(&e.side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&e.ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&e.ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        komd_gpu_destroy(h);
+        return fail(KOMD_ERR_CUDA, "stream creation failed");
+    }
     if (dalloc(e.cell_count, g.ncell) || dalloc(e.cell_start, g.ncell + 1) || dalloc(e.cell_mcount, g.ncell) ||
         dalloc(e.cell_mstart, g.ncell + 1) || dalloc(e.err, E_NFLAGS) || dalloc(h->acc, R_NSLOTS) || dalloc(h->thermo_acc, R_NSLOTS)) {
         komd_gpu_destroy(h);
@@ -597,6 +621,9 @@ int komd_gpu_destroy(komd_gpu *h) {
     for (auto &p : h->pending) { h->pool.push_back(p.second.first); h->pool.push_back(p.second.second); }
     for (auto ev : h->pool) cudaEventDestroy(ev);
     if (e.own_stream && e.stream) cudaStreamDestroy(e.stream);
+    if (e.side) cudaStreamDestroy(e.side);
+    if (e.ev_fork) cudaEventDestroy(e.ev_fork);
+    if (e.ev_join) cudaEventDestroy(e.ev_join);
     delete h;
     return KOMD_OK;
 }
@@ -989,6 +1016,9 @@ int step_host_direct(komd_gpu *h, int64_t n_steps, double *r, double *v, double 
     const double *rin = device_view(h, r), *vin = device_view(h, v), *fo = device_view(h, f);
     if (!rin || !vin || !fo) return KOMD_OK;
     *applies = true;
+    cudaPointerAttributes pa;
+    const bool r_pinned = cudaPointerGetAttributes(&pa, r) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+    e.hout_r_async = r_pinned;
     double *rout = const_cast<double *>(rin), *vout = const_cast<double *>(vin), *fout = const_cast<double *>(fo);
     if (n_steps == 1) {
         // one launch per call: the step with these buffers bound, captured once

@@ -384,6 +384,11 @@ struct Engine {
     // nullptr outside such a step
     const double *hin_r = nullptr, *hin_v = nullptr;
     double *hout_r = nullptr, *hout_v = nullptr, *hout_f = nullptr;
+    // hout_r is pinned: the step copies the drifted positions back on the copy
+    // engine (side stream) while its force pass runs, instead of in the drift kernel
+    bool hout_r_async = false;
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     unsigned long long *atm_acc = nullptr;   // 3 per slot, fixed-point force sums of k_atm_s (zero between steps)
     // tabulated pair force (KOMD_TERM_TABULATED): F(r) piecewise linear on
     // ascending nodes tab_x, values tab_y, tab_lo below / tab_hi above the nodes
