@@ -130,8 +130,9 @@ def test_autotuner_picks_a_measured_shape():
 @pytest.mark.parametrize("pinned", [True, False])
 def test_step_host_matches_device_path(pinned):
     """komd_gpu_step_host on the fused path reads r, v from the caller's buffers
-    and writes r, v, f back from inside the step's kernels (pinned buffers, or
-    plain pageable memory where the GPU walks the host page tables); the
+    and writes r, v, f back from inside the step's kernels (plain pageable
+    memory where the GPU walks the host page tables; with pinned buffers the
+    positions go back on the copy engine beside the force pass); the
     trajectory is bitwise the one of komd_gpu_step on device-resident state,
     for one step per call and for several."""
     import torch
