@@ -1,7 +1,8 @@
 """The benchmark's timed configuration itself against the FP64 oracle.
 
-The benchmark times LJ + ATM argon at 256,000 atoms on the Verlet path: skin
-0.4 and cell edge 67.184 / 23 = 2.921 (the autotuner's choice), FULL triplets
+The benchmark times LJ + ATM argon at 256,000 atoms on the Verlet path with
+the skin and cell edge its autotuner picks (skin 0.4 on cells of 67.184 / 23
+= 2.921, or 0.6 on cells of 67.184 / 21 = 3.199, in recorded runs), FULL triplets
 with F = -grad V, FP32 pair and triplet arithmetic and FP64 integration,
 after 400 equilibration steps in which the FCC lattice melts.  Here the same
 system and configuration run through komd_gpu_step (the step graph, with its
@@ -77,12 +78,17 @@ def _ambiguous_triplets(r, box, rc, band):
     return count
 
 
-def test_timed_256k_state_matches_oracle(oracle_lib):
+@pytest.mark.parametrize("skin,ncells", [(0.4, 23), (0.6, 21)])
+def test_timed_256k_state_matches_oracle(oracle_lib, skin, ncells):
+    """The autotuner's leading shapes: skin 0.4 on cells of 2.921 (one home
+    site per lane in the list build) and skin 0.6 on cells of 3.199 (27.6
+    sites per cell: the two-home build)."""
     from komd_gb300 import gpu, lattice
     s = lattice.argon_fcc(40, rho=0.8442, t_star=0.722, seed=1)   # the benchmark's system (rank 0)
     L = float((s.high - s.low)[0])
-    cell = L / 23                                                   # 2.921 >= cutoff 2.5 + skin 0.4
-    g = gpu.GpuSystem(s, _cfg(s, cell, 0.4))
+    cell = L / ncells                                               # >= cutoff 2.5 + skin
+    assert cell >= 2.5 + skin
+    g = gpu.GpuSystem(s, _cfg(s, cell, skin))
     g.update_container()
     g.forces()
     g.step(400)                                                     # the benchmark's equilibration
