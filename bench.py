@@ -177,10 +177,14 @@ def committed_traffic(kernel, workload, skin=None):
     return float(e["bytes_per_launch"])
 
 
-def cpu_baseline(w, seed, budget_s=25.0, threads=None):
+def cpu_baseline(w, seed, budget_s=25.0, threads=None, same_config_s=0.0):
     """The oracle's restatement of the reference's algorithm (COMPAT triplet
     enumeration, pair sweep of the reference's cell pairs) on the host cores,
-    on a bounded sample: whole MD steps of the same system until budget_s."""
+    on a bounded sample: whole MD steps of the same system until budget_s.
+    With same_config_s > 0, also the GPU's form (FULL triplets, physical sign)
+    on the same port for about that long (`same_config`): the port's
+    per-vertex triplet enumeration, far faster on the host than the
+    reference's cell-triple sweep that the main sample restates."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
     pyoracle.build()
@@ -204,6 +208,25 @@ def cpu_baseline(w, seed, budget_s=25.0, threads=None):
     cal = reference_calibration()
     if cal:
         out["calibration"] = cal
+    if same_config_s > 0 and w["atm"]:
+        # the GPU's form on the same port: every triplet (FULL) with F = -grad V
+        full = pyoracle.OracleSim(s, w["cell"], w["rc"], dt=w["dt"], nu=w["nu"], cutoff_atm=w["rc3"], atm=True,
+                                  atm_mode="full", atm_sign=pyoracle.ATM_SIGN_PHYSICAL,
+                                  virial_mode=pyoracle.VIRIAL_CORRECT)
+        full.update_container()
+        full.forces(listless=True)
+        t1 = time.perf_counter()
+        n_full = 0
+        while True:
+            full.step(listless=True)
+            n_full += 1
+            if time.perf_counter() - t1 > same_config_s or n_full >= 20:
+                break
+        d1 = time.perf_counter() - t1
+        out["same_config"] = {"value": s.n * n_full / d1, "unit": UNIT,
+                              "form": "FULL triplets, F = -grad V (the GPU's form) with the port's per-vertex "
+                                      "triplet enumeration (kor_atm_vertex), not the reference's cell-triple sweep",
+                              "sample": f"{n_full} full MD step(s) ({d1:.1f} s)"}
     return out
 
 
@@ -799,7 +822,7 @@ def run_ours(args, w, name):
                 "peak_source": "measured here: cuBLAS SGEMM 8192^3, TF32 off", "launch_ms": t_launch * 1e3}
     cb = None
     if not args.no_cpu_baseline:
-        cb = cpu_baseline(w, seed=1, budget_s=args.cpu_budget)
+        cb = cpu_baseline(w, seed=1, budget_s=args.cpu_budget, same_config_s=args.cpu_budget / 2)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp32 forces / fp64 integration",
