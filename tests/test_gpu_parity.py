@@ -428,6 +428,41 @@ def test_verlet_path_matches_rebuild_every_step(oracle_lib):
     b.close()
 
 
+def test_binary_mixture_half_list_pass(oracle_lib):
+    """Two species (sigma 1.0 / 0.88, epsilon 1.0 / 0.6; the reference's
+    combining rules, LJ12_6.cpp:22-25: sigma = (s_i + s_j) / 2, epsilon =
+    sqrt(e_i e_j)) on the benchmark's path: Verlet list with skin, the
+    half-list LJ + ATM pass in its per-pair-parameter form, the fused step
+    kernels.  After 50 steps the forces, the LJ and ATM energies and the
+    virial match the oracle at the engine's positions."""
+    from komd_gb300 import gpu, lattice
+    s = lattice.argon_fcc(10, rho=0.8442, t_star=0.9, seed=43, jitter=0.05)    # 4000 sites, L = 16.8
+    rng = np.random.default_rng(44)
+    b_mask = rng.random(s.n) < 0.3
+    s.sig = np.where(b_mask, 0.88, 1.0)
+    s.eps = np.where(b_mask, 0.6, 1.0)
+    g = gpu.GpuSystem(s, _physics_cfg(s, 0.3, 2.8))
+    g.update_container()
+    g.forces()
+    g.step(50)
+    r, v, f = g.download()
+    obs = g.measure(gpu.MEASURE_ENERGY | gpu.MEASURE_PRESSURE)
+    g.close()
+    sim = oracle_lib.OracleSim(lattice.System(r=r, v=v, m=s.m, eps=s.eps, sig=s.sig, mol_id=s.mol_id, low=s.low,
+                                              high=s.high), 2.8, 2.5, nu=0.073, cutoff_atm=2.0, atm=True,
+                               atm_mode="full", atm_sign=oracle_lib.ATM_SIGN_PHYSICAL,
+                               virial_mode=oracle_lib.VIRIAL_CORRECT)
+    sim.update_container()
+    sim.forces()
+    assert rel_rmse(f, sim.f) < FP32_FORCE_RMSE
+    assert obs["u_lj"] == pytest.approx(sim.lj_out.u_total, rel=1e-5)
+    assert obs["u_atm"] == pytest.approx(sim.atm_out.energy, rel=1e-5)
+    vir = np.array(sim.lj_out.virial[:]) + np.array(sim.atm_out.virial[:])
+    np.testing.assert_allclose(obs["virial"], vir, rtol=0, atol=2e-5 * np.abs(vir).max())
+    # Newton's third law of the once-per-pair and once-per-triplet sums
+    assert np.abs(f.sum(0)).max() < 1e-3 * np.sqrt(s.n) * np.abs(f).mean()
+
+
 def test_verlet_requires_cell_for_skin():
     from komd_gb300 import gpu, lattice
     s = lattice.argon_fcc(10, seed=1)
