@@ -44,6 +44,38 @@ def test_batch_matches_single_system_path(groups):
         g.close()
 
 
+def test_packed_mixture_replicas_match_single_path():
+    """Replicas of a two-species LJ mixture (per-pair LJ parameters) take the
+    packed form too: bitwise the single-system path after 20 steps."""
+    from komd_gb300 import gpu, lattice, surrogate
+
+    def make(seed, n, rho, t_star):
+        s = lattice.trimmed_fcc(n, rho, t_star, seed)
+        rng = np.random.default_rng(seed)
+        mix = rng.random(s.n) < 0.4
+        s.sig = np.where(mix, 0.9, 1.0)
+        s.eps = np.where(mix, 0.7, 1.0)
+        cfg = surrogate.physics_config(s, float(s.high[0]) / np.floor(float(s.high[0]) / 2.8), skin=0.3)
+        g = gpu.GpuSystem(s, cfg)
+        g.update_container()
+        g.forces()
+        return g
+
+    a = [make(*sp) for sp in SPECS[:3]]
+    b = [make(*sp) for sp in SPECS[:3]]
+    batch = gpu.Batch(a, n_streams=2, steps_per_graph=4)
+    assert batch.packed
+    batch.step(5)
+    batch.close()
+    for ga, gb in zip(a, b):
+        gb.step(20)
+        ra, va, fa = ga.download()
+        rb, vb, fb = gb.download()
+        assert np.array_equal(ra, rb) and np.array_equal(va, vb) and np.array_equal(fa, fb)
+        ga.close()
+        gb.close()
+
+
 def test_batch_measure_matches_replica_measures():
     """komd_batch_measure (every replica's measure enqueued on the batch's
     branches, one synchronisation) gives each replica what komd_gpu_measure
