@@ -275,12 +275,13 @@ void enqueue_step(komd_gpu *h) {
         ProfScope ps(h, F_INTEGRATE);
         launch_step0(e, e.stream, true);
     }
-    if (r_async) {
-        cudaEventRecord(e.ev_fork, e.stream);
-        cudaStreamWaitEvent(e.side, e.ev_fork, 0);
-        cudaMemcpyAsync(r_async, e.r, sizeof(double) * 3 * (size_t)e.n, cudaMemcpyDeviceToHost, e.side);
-        cudaEventRecord(e.ev_join, e.side);
-    }
+    bool forked = false;
+    if (r_async)
+        forked = cudaEventRecord(e.ev_fork, e.stream) == cudaSuccess &&
+                 cudaStreamWaitEvent(e.side, e.ev_fork, 0) == cudaSuccess &&
+                 cudaMemcpyAsync(r_async, e.r, sizeof(double) * 3 * (size_t)e.n, cudaMemcpyDeviceToHost,
+                                 e.side) == cudaSuccess &&
+                 cudaEventRecord(e.ev_join, e.side) == cudaSuccess;
     {
         ProfScope ps(h, F_CONTAINER);
         launch_container(e, e.stream);
@@ -298,7 +299,10 @@ void enqueue_step(komd_gpu *h) {
         launch_velocity_scale(e, e.stream, h->thermo_acc, 1.0);
     }
     if (r_async) {
-        cudaStreamWaitEvent(e.stream, e.ev_join, 0);
+        // joined before the step ends; if the side stream could not take the
+        // copy, it runs here on the engine's stream instead
+        if (!forked || cudaStreamWaitEvent(e.stream, e.ev_join, 0) != cudaSuccess)
+            cudaMemcpyAsync(r_async, e.r, sizeof(double) * 3 * (size_t)e.n, cudaMemcpyDeviceToHost, e.stream);
         e.hout_r = r_async;
     }
 }
