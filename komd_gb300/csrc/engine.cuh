@@ -25,6 +25,30 @@
 
 namespace komd {
 
+// Programmatic dependent launch between consecutive kernels of a step: a
+// kernel launched with launch_pdl may become resident before its
+// predecessor has finished; pdl_wait (at its entry, before any memory
+// access) holds it until the predecessor has completed and its writes are
+// visible, and pdl_trigger lets the successor be scheduled once every block
+// of this grid has started.  Both are no-ops without a programmatic launch.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 constexpr int kWarpsPerBlock = 8;
 constexpr int kBlock = 32 * kWarpsPerBlock;
 

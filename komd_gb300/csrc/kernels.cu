@@ -99,7 +99,11 @@ __device__ __forceinline__ void com_wrap_bin_body(const BinArgs &a, int bid, int
     atomicAdd(&cell_count[cell], s1 - s0);
     }
 }
-__global__ void k_com_wrap_bin(BinArgs a) { com_wrap_bin_body(a, blockIdx.x, gridDim.x); }
+__global__ void k_com_wrap_bin(BinArgs a) {
+    pdl_trigger();
+    pdl_wait();
+    com_wrap_bin_body(a, blockIdx.x, gridDim.x);
+}
 
 // exclusive scan of two count arrays of length nc (one block of 1024 threads,
 // each owning a contiguous chunk); the counts are zeroed once read, ready for
@@ -144,14 +148,22 @@ __device__ __forceinline__ void scan2_body(const ScanArgs &q) {
     }
     if (t == 1023) { sa[nc] = wa[31]; sb[nc] = wb[31]; }
 }
-__global__ void __launch_bounds__(1024) k_scan2(ScanArgs q) { scan2_body(q); }
+__global__ void __launch_bounds__(1024) k_scan2(ScanArgs q) {
+    pdl_trigger();
+    pdl_wait();
+    scan2_body(q);
+}
 
 __device__ __forceinline__ void scatter_mol_body(const ScatterArgs &a, int bid, int nblk) {
     if (a.rebuild && !*a.rebuild) return;
     for (int k = bid * blockDim.x + threadIdx.x; k < a.n_mol; k += nblk * blockDim.x)
         a.cell_mols[a.cell_mstart[a.mol_cell[k]] + a.mol_rank[k]] = k;
 }
-__global__ void k_scatter_mol(ScatterArgs a) { scatter_mol_body(a, blockIdx.x, gridDim.x); }
+__global__ void k_scatter_mol(ScatterArgs a) {
+    pdl_trigger();
+    pdl_wait();
+    scatter_mol_body(a, blockIdx.x, gridDim.x);
+}
 
 // One warp per domain cell: order the cell's molecules by index (ascending
 // site index, the reference's cell-list order), assign slots and gather the
@@ -217,7 +229,11 @@ __device__ __forceinline__ void cell_sort_body(const SortArgs &a, int bid, int n
     }
     }
 }
-__global__ void __launch_bounds__(kBlock) k_cell_sort(SortArgs a) { cell_sort_body(a, blockIdx.x, gridDim.x); }
+__global__ void __launch_bounds__(kBlock) k_cell_sort(SortArgs a) {
+    pdl_trigger();
+    pdl_wait();
+    cell_sort_body(a, blockIdx.x, gridDim.x);
+}
 
 // ===========================================================================
 // pair kernel: LJ 12-6 (LJ12_6.cpp:15-43), FENE (FENE.cpp:15-43), the ATM
@@ -1045,7 +1061,10 @@ __device__ __forceinline__ void step0_fused_body(const Step0Args &a, int bid) {
         rows_out(s_r, r_out, base, cnt);
     }
 }
-__global__ void __launch_bounds__(kIoBlock) k_step0_fused(Step0Args a) { step0_fused_body(a, blockIdx.x); }
+__global__ void __launch_bounds__(kIoBlock) k_step0_fused(Step0Args a) {
+    pdl_trigger();
+    step0_fused_body(a, blockIdx.x);
+}
 
 __global__ void k_step1(int n, double *__restrict__ v, const double *__restrict__ f, const double *__restrict__ hdtm,
                         int *__restrict__ err, int *__restrict__ rebuild) {
@@ -1535,10 +1554,10 @@ void launch_container(Engine &e, cudaStream_t st) {
     // of every binning after reading them
     // grid-stride kernels on a resident grid: steps without a rebuild launch few blocks
     const int res = e.num_sms * 8;
-    k_com_wrap_bin<<<std::min(nblk(e.n_mol, 256), res), 256, 0, st>>>(bin_args(e));
-    k_scan2<<<1, 1024, 0, st>>>(scan_args(e));
-    k_scatter_mol<<<std::min(nblk(e.n_mol, 256), res), 256, 0, st>>>(scatter_args(e));
-    k_cell_sort<<<std::min(nblk(g.ncell, kWarpsPerBlock), res), kBlock, 0, st>>>(sort_args(e));
+    launch_pdl(k_com_wrap_bin, std::min(nblk(e.n_mol, 256), res), 256, 0, st, bin_args(e));
+    launch_pdl(k_scan2, 1, 1024, 0, st, scan_args(e));
+    launch_pdl(k_scatter_mol, std::min(nblk(e.n_mol, 256), res), 256, 0, st, scatter_args(e));
+    launch_pdl(k_cell_sort, std::min(nblk(g.ncell, kWarpsPerBlock), res), kBlock, 0, st, sort_args(e));
     if (e.verlet) {
         if (!e.fused_drift)
             k_refresh<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.slot_site, e.r, e.bias, e.pos4, e.rebuild);
@@ -1752,7 +1771,10 @@ __device__ __forceinline__ void flush_step1_body(const FlushArgs &a, int bid) {
         if (v_out) rows_out(s_v, v_out, base, cnt);
     }
 }
-__global__ void __launch_bounds__(kIoBlock) k_atm_flush_step1(FlushArgs a) { flush_step1_body(a, blockIdx.x); }
+__global__ void __launch_bounds__(kIoBlock) k_atm_flush_step1(FlushArgs a) {
+    pdl_wait();
+    flush_step1_body(a, blockIdx.x);
+}
 
 // f[site] += 2 sign nu g (fixed point -> FP64) and the accumulators back to 0
 __global__ void k_atm_flush(int n, const int *__restrict__ slot_site, unsigned long long *__restrict__ acc,
@@ -1818,7 +1840,7 @@ bool launch_atm_flush(Engine &e, cudaStream_t st, bool with_step1, bool force_un
     const double sign = e.cfg.atm_sign == KOMD_ATM_SIGN_REFERENCE ? 1.0 : -1.0;
     const double scale_fix = force_units ? 1.0 / kAtmFix : 2.0 * sign * e.cfg.nu / kAtmFix;
     if (with_step1) {
-        k_atm_flush_step1<<<nblk(e.n, kIoBlock), kIoBlock, 0, st>>>(flush_args(e, scale_fix));
+        launch_pdl(k_atm_flush_step1, nblk(e.n, kIoBlock), kIoBlock, 0, st, flush_args(e, scale_fix));
         return true;
     }
     k_atm_flush<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.slot_site, e.atm_acc, e.f, scale_fix);

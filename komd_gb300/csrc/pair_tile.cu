@@ -457,7 +457,11 @@ __device__ __forceinline__ void vlist_build_body(const PairParams &p, int bid) {
     }
 }
 template <bool TWO>
-__global__ void __launch_bounds__(32 * kVbWarps) k_vlist_build(PairParams p) { vlist_build_body<TWO>(p, blockIdx.x); }
+__global__ void __launch_bounds__(32 * kVbWarps) k_vlist_build(PairParams p) {
+    pdl_trigger();
+    pdl_wait();
+    vlist_build_body<TWO>(p, blockIdx.x);
+}
 
 // ---------------------------------------------------------------------------
 // LJ forces from the Verlet list (every step of the Verlet path): one warp
@@ -842,6 +846,8 @@ __device__ __forceinline__ void lj_atm_half_body(const PairParams &p, const AtmP
 }
 template <bool UNIFORM, bool SW>
 __global__ void __launch_bounds__(256, 4) k_lj_atm_half(PairParams p, AtmParams a, float sa, int n, int per) {
+    pdl_trigger();
+    pdl_wait();
     lj_atm_half_body<UNIFORM, SW>(p, a, sa, n, per, blockIdx.x);
 }
 
@@ -850,7 +856,7 @@ static void launch_half(const PairParams &p, const AtmParams &a, float sa, int n
                         cudaStream_t st) {
     if (sm > 48 * 1024)
         cudaFuncSetAttribute(k_lj_atm_half<UNIFORM, SW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_lj_atm_half<UNIFORM, SW><<<grid, 256, sm, st>>>(p, a, sa, n, per);
+    launch_pdl(k_lj_atm_half<UNIFORM, SW>, grid, 256, sm, st, p, a, sa, n, per);
 }
 
 // shared memory of the half-list pass: per warp nl_cap staged triplet
@@ -945,8 +951,8 @@ void launch_vlist_build(Engine &e, cudaStream_t st) {
     // a resident grid (12 blocks of 4 warps per SM at this kernel's register count)
     const int blocks = std::min((e.g.ncell + kVbWarps - 1) / kVbWarps, e.num_sms * 12);
     // the two-home form pays off once many cells hold more than 32 sites
-    if (vbuild_two(e)) k_vlist_build<true><<<blocks, 32 * kVbWarps, 0, st>>>(p);
-    else k_vlist_build<false><<<blocks, 32 * kVbWarps, 0, st>>>(p);
+    if (vbuild_two(e)) launch_pdl(k_vlist_build<true>, blocks, 32 * kVbWarps, 0, st, p);
+    else launch_pdl(k_vlist_build<false>, blocks, 32 * kVbWarps, 0, st, p);
 }
 
 template <bool UNIFORM>
