@@ -498,13 +498,15 @@ def drift_leg(args, local, model=None):
     atom per 10^4 steps.  Forms: exact FP32 forces, exact FP64 forces (both
     with the reference's truncated potentials), the labelled switched-cutoff
     option (komd_config::switch_width, FP32), and the learned three-body term
-    when a trained model is given."""
+    when a trained model is given, with the truncated LJ and with the
+    switched LJ."""
     from komd_gb300 import gpu, lattice, surrogate
     out = {}
     forms = [("fp32_exact", gpu.FP32, False, 0.0), ("fp64_exact", gpu.FP64, False, 0.0),
              ("fp32_switched_0.3", gpu.FP32, False, 0.3)]
     if model is not None:
         forms.append(("fp32_learned", gpu.FP32, True, 0.0))
+        forms.append(("fp32_learned_switched_0.3", gpu.FP32, True, 0.3))
     for name, prec, learned, width in forms:
         s = lattice.argon_fcc(20, rho=0.8442, t_star=0.722, seed=3)
         terms = gpu.TERM_LJ | gpu.TERM_ATM | (gpu.TERM_ATM_SURROGATE if learned else 0)
@@ -531,7 +533,11 @@ def drift_leg(args, local, model=None):
         slope = float(np.polyfit(np.asarray(steps, float), e, 1)[0])
         out[name] = {"drift_per_atom_per_1e4_steps": slope * 1e4, "max_abs_dev_per_atom": float(np.abs(e - e[0]).max()),
                      "e_per_atom_start": float(e[0]), "wall_s": wall}
-        if width > 0:
+        if width > 0 and learned:
+            out[name]["option"] = (f"switched LJ cutoff (switch_width {width}) with the learned three-body term: the "
+                                   f"LJ energy smoothly switched off over the last {width} sigma below its cutoff; "
+                                   f"not the reference's potential")
+        elif width > 0:
             out[name]["option"] = (f"switched cutoffs (switch_width {width}): LJ and ATM energies smoothly switched "
                                    f"off over the last {width} sigma below each cutoff; not the reference's potential")
         g.close()

@@ -115,7 +115,9 @@ typedef struct komd_config {
                                   ATM); forces are the exact gradients, so the energy is
                                   conserved without the jumps of the truncation.  Needs
                                   the Verlet path (skin > 0, FP32) without Limit, FENE,
-                                  ATM2B, tabulated or learned terms */
+                                  ATM2B, tabulated or bonded terms; with the learned
+                                  three-body term it switches the LJ pair energy (and
+                                  the exact ATM of the probes) */
 } komd_config;
 
 typedef struct komd_observables {

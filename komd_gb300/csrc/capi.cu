@@ -396,8 +396,10 @@ int validate(const komd_config *c, Grid &g) {
         // the labelled switched-cutoff option lives on the half-list Verlet path
         if (!uses_verlet(*c))
             return fail(KOMD_ERR_ARG, "switch_width > 0 needs the Verlet path (skin > 0, FP32, FULL ATM, CORRECT virial, no FENE)");
-        if (c->terms & (KOMD_TERM_LIMIT | KOMD_TERM_FENE | KOMD_TERM_ATM2B | KOMD_TERM_TABULATED | KOMD_TERM_ATM_SURROGATE | KOMD_TERM_BONDED))
-            return fail(KOMD_ERR_ARG, "switch_width > 0 covers LJ and exact ATM only (no Limit, FENE, ATM2B, tabulated, learned or bonded terms)");
+        // with the learned three-body term the LJ pair pass carries the switch
+        // (the learned energy vanishes smoothly at its cutoff by construction)
+        if (c->terms & (KOMD_TERM_LIMIT | KOMD_TERM_FENE | KOMD_TERM_ATM2B | KOMD_TERM_TABULATED | KOMD_TERM_BONDED))
+            return fail(KOMD_ERR_ARG, "switch_width > 0 covers LJ, exact ATM and the learned term only (no Limit, FENE, ATM2B, tabulated or bonded terms)");
         if ((lj && !(c->switch_width < c->cutoff)) || (atm && !(c->switch_width < c->cutoff_3b)))
             return fail(KOMD_ERR_ARG, "switch_width must be below each cutoff");
     }

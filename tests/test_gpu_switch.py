@@ -106,3 +106,48 @@ def test_switched_forces_and_energies_match_oracle(oracle_lib):
         truncated = _oracle(oracle_lib, s, r, v, cell, 0.0)
         assert rel_rmse(f, truncated.f) > 1e-3   # the option does change the forces
     g.close()
+
+
+@pytest.mark.gpu
+def test_switch_with_learned_term_switches_the_lj_part(oracle_lib):
+    """With the learned three-body term the option switches the LJ pair
+    energy: the forces of the learned form with and without the switch
+    differ by exactly what the switch changes in the LJ forces (the oracle's
+    switched and truncated LJ at the same positions), and the LJ energy
+    matches the oracle's switched LJ."""
+    from komd_gb300 import gpu, lattice, surrogate
+    s = lattice.argon_fcc(10, rho=0.8442, t_star=1.0, seed=71, jitter=0.05)    # 4000 sites, L = 16.8
+    cell = 2.8
+    terms = gpu.TERM_LJ | gpu.TERM_ATM | gpu.TERM_ATM_SURROGATE
+    forces, u_lj = {}, {}
+    model = None
+    for width in (0.0, 0.3):
+        cfg = surrogate.physics_config(s, cell, skin=0.3, terms=terms)
+        cfg.switch_width = width
+        g = gpu.GpuSystem(s, cfg)
+        g.update_container()
+        g.forces()
+        if model is None:
+            x, e3, _ = g.surrogate_sample()
+            model = dict(params=surrogate.init_params(5), fmean=x.mean(0).astype(np.float32),
+                         fstd=(x.std(0) + 1e-6).astype(np.float32), e_scale=float(e3.std()), e_shift=float(e3.mean()))
+        g.surrogate_load(model, probe_every=0)
+        g.update_container()
+        g.forces()
+        _, _, forces[width] = g.download()
+        u_lj[width] = g.measure(gpu.MEASURE_ENERGY)["u_lj"]
+        g.close()
+    lj = {}
+    for width in (0.0, 0.3):
+        at = lattice.System(r=s.r, v=s.v, m=s.m, eps=s.eps, sig=s.sig, mol_id=s.mol_id, low=s.low, high=s.high)
+        sim = oracle_lib.OracleSim(at, cell, 2.5, nu=0.073, cutoff_atm=2.0, atm=False,
+                                   virial_mode=oracle_lib.VIRIAL_CORRECT, switch_width=width)
+        sim.update_container()
+        sim.forces(listless=True)
+        lj[width] = (sim.f.copy(), sim.lj_out.u_total)
+    d_gpu = forces[0.3] - forces[0.0]
+    d_ref = lj[0.3][0] - lj[0.0][0]
+    scale = np.sqrt((lj[0.0][0] ** 2).sum(1).mean())
+    assert np.sqrt((d_ref ** 2).sum(1).mean()) > 1e-3 * scale        # the switch changes the LJ forces
+    assert np.sqrt(((d_gpu - d_ref) ** 2).sum(1).mean()) < 1e-5 * scale
+    assert u_lj[0.3] == pytest.approx(lj[0.3][1], rel=1e-5)
