@@ -453,41 +453,58 @@ def multisite_leg(stream, local, events_ms, steps=500):
     """The multi-site workload: 100,000 flexible 3-site molecules (300,000
     sites) on a simple-cubic lattice, site density 0.8, T* 1.0, harmonic bonds
     (k 1000, r0 1) and angles (k 100, 109.47 deg), intermolecular LJ (cutoff
-    2.5) on cells of edge >= 4.2 (the cutoff plus the molecule's diameter, so
-    that the centre-of-mass cells hold every site pair inside the cutoff),
-    FP32 forces, FP64 integration, dt 0.002, all 500 steps timed from the
+    2.5), FP32 forces, FP64 integration, dt 0.002, all 500 steps timed from the
     start.  One seeded orientation for all molecules: random orientations at
     this density overlap sites of neighbouring molecules (see the workload
-    test in tests/test_workloads.py)."""
+    test in tests/test_workloads.py).  Two forms of the same physics:
+      * `value`: the Verlet list, skin 0.3, molecules binned by their centre
+        of mass on cells >= 4.8: cutoff + skin + 2.0, twice a site's largest
+        distance from its molecule's centre (0.84 at rest, below 1.0 up to
+        three standard deviations of the bond and angle at T* 1), so that
+        every site pair inside cutoff + skin is in adjacent cells;
+      * `cell_lists`: the reference's per-step cell lists on cells >= 4.2
+        (cutoff + the molecule's extent), every candidate of the 27 cells
+        tested on every step."""
     from komd_gb300 import gpu, lattice
     s = lattice.triatomic_count(100000, rho_site=0.8, t_star=1.0, seed=31, aligned=True)
     L = float((s.high - s.low)[0])
     th0 = np.deg2rad(109.47)
-    cfg = gpu.make_config(s.low, s.high, L / np.floor(L / 4.2), cutoff=2.5, dt=0.002,
-                          terms=gpu.TERM_LJ | gpu.TERM_BONDED, bond_k=1000.0, bond_r0=1.0, angle_k=100.0,
-                          angle_theta0=th0, virial_mode=gpu.VIRIAL_CORRECT)
-    g = gpu.GpuSystem(s, cfg, device=local)
-    try:
-        g.set_stream(stream.cuda_stream)
-        g.update_container()
-        g.forces()
 
-        def energy():
-            o = g.measure(gpu.MEASURE_ENERGY | gpu.MEASURE_TEMPERATURE)
-            return (0.5 * o["mv2"] + o["u_lj"] + o["u_bonded"]) / s.n
+    def run(skin, reach):
+        cell = L / np.floor(L / reach)
+        cfg = gpu.make_config(s.low, s.high, cell, cutoff=2.5, dt=0.002,
+                              terms=gpu.TERM_LJ | gpu.TERM_BONDED, bond_k=1000.0, bond_r0=1.0, angle_k=100.0,
+                              angle_theta0=th0, virial_mode=gpu.VIRIAL_CORRECT, skin=skin)
+        g = gpu.GpuSystem(s, cfg, device=local)
+        try:
+            g.set_stream(stream.cuda_stream)
+            g.update_container()
+            g.forces()
 
-        e0 = energy()
-        ms = events_ms(lambda: g.step(steps))
-        e1 = energy()
-        r, v, _ = g.download()
-        b = np.linalg.norm(r[s.bonds[:, 0]] - r[s.bonds[:, 1]], axis=1)
-        return dict(value=s.n * steps / (ms / 1e3), unit=UNIT, ms_per_step=ms / steps, steps=steps,
-                    finite=bool(np.isfinite(r).all() and np.isfinite(v).all()),
-                    bond_length_range=[float(b.min()), float(b.max())], energy_per_site=[e0, e1],
-                    config="300,000 sites (100,000 3-site molecules, one seeded orientation), rho_site 0.8, "
-                           "cells >= 4.2, LJ + bonds + angles, FP32 forces, dt 0.002, 500 steps from the start")
-    finally:
-        g.close()
+            def energy():
+                o = g.measure(gpu.MEASURE_ENERGY | gpu.MEASURE_TEMPERATURE)
+                return (0.5 * o["mv2"] + o["u_lj"] + o["u_bonded"]) / s.n
+
+            e0 = energy()
+            g.set_profiling(False)
+            ms = events_ms(lambda: g.step(steps))
+            rebuilds = g.profile().get("list_rebuilds", (0, 0.0))[0] if skin > 0 else steps
+            e1 = energy()
+            r, v, _ = g.download()
+            b = np.linalg.norm(r[s.bonds[:, 0]] - r[s.bonds[:, 1]], axis=1)
+            return dict(value=s.n * steps / (ms / 1e3), unit=UNIT, ms_per_step=ms / steps, steps=steps,
+                        finite=bool(np.isfinite(r).all() and np.isfinite(v).all()),
+                        bond_length_range=[float(b.min()), float(b.max())], energy_per_site=[e0, e1],
+                        skin=skin, cell=cell, list_rebuilds=int(rebuilds))
+        finally:
+            g.close()
+
+    out = run(0.3, 4.8)
+    out["cell_lists"] = run(0.0, 4.2)
+    out["config"] = ("300,000 sites (100,000 3-site molecules, one seeded orientation), rho_site 0.8, "
+                     "LJ + bonds + angles, FP32 forces, dt 0.002, 500 steps from the start; Verlet list with "
+                     "skin 0.3 on cells >= 4.8 (cell_lists: per-step cells >= 4.2)")
+    return out
 
 
 def drift_leg(args, local, model=None):

@@ -546,6 +546,55 @@ def test_multisite_300k_full_size(oracle_lib):
     g.close()
 
 
+def test_multisite_verlet_matches_cell_lists():
+    """Molecules on the Verlet path: 8,000 flexible 3-site molecules (24,000
+    sites, the multi-site workload's density, bonds and angles), binned by
+    their centre of mass on cells >= cutoff + skin + 2.0 (twice a site's
+    largest distance from its molecule's centre, 0.84 at rest), with the
+    same-molecule pairs in the rows but excluded from LJ.  Over 200 steps with
+    list rebuilds the trajectory follows the per-step cell lists' (skin 0, the
+    same cells), the list's forces equal a fresh rebuild's, and the energies
+    agree."""
+    from komd_gb300 import gpu, lattice
+    s = lattice.triatomic_count(8000, rho_site=0.8, t_star=1.0, seed=37, aligned=True)
+    L = float((s.high - s.low)[0])
+    th0 = np.deg2rad(109.47)
+
+    def cfg(skin, reach):
+        return gpu.make_config(s.low, s.high, L / np.floor(L / reach), cutoff=2.5, dt=0.002,
+                               terms=gpu.TERM_LJ | gpu.TERM_BONDED, bond_k=1000.0, bond_r0=1.0, angle_k=100.0,
+                               angle_theta0=th0, virial_mode=gpu.VIRIAL_CORRECT, skin=skin)
+
+    a = gpu.GpuSystem(s, cfg(0.3, 4.8))
+    b = gpu.GpuSystem(s, cfg(0.0, 4.8))
+    for g in (a, b):
+        g.update_container()
+        g.forces()
+    _, _, fa0 = a.download()
+    _, _, fb0 = b.download()
+    assert rel_rmse(fa0, fb0) < 2e-6
+    a.set_profiling(False)
+    for _ in range(20):
+        a.step(10)
+        b.step(10)
+    assert a.profile().get("list_rebuilds", (0, 0.0))[0] >= 2   # the lists were rebuilt on the way
+    ra, va, fa = a.download()
+    rb, vb, fb = b.download()
+    assert np.isfinite(ra).all() and np.isfinite(va).all()
+    assert np.abs(ra - rb).max() < 1e-4
+    assert rel_rmse(fa, fb) < 1e-4
+    oa = a.measure(gpu.MEASURE_ENERGY | gpu.MEASURE_TEMPERATURE)
+    ob = b.measure(gpu.MEASURE_ENERGY | gpu.MEASURE_TEMPERATURE)
+    for key in ("u_lj", "u_bonded", "mv2"):
+        assert oa[key] == pytest.approx(ob[key], rel=1e-4)
+    a.update_container()
+    a.forces()
+    _, _, fresh = a.download()
+    assert rel_rmse(fa, fresh) < 2e-6
+    a.close()
+    b.close()
+
+
 def test_plain_lj_4000_fp64_1000_steps(oracle_lib):
     """The plain LJ workload at its full size and length: 4,000 argon atoms
     (FCC 10^3, rho* 0.8442, T* 0.722), cutoff 2.5, 1000 NVE steps of dt 0.005,
