@@ -32,9 +32,26 @@ __device__ __forceinline__ float4 atm_stage_q(float A) {
     return make_float4(A, ia, rsqrtf(A), 0.f);
 }
 
+// round(x * 2^32) to the nearest integer (ties to even) as int64, for finite
+// |x| < 2^31, built from two 32-bit conversions: GB300 runs FP32 -> int64
+// conversions on its narrow FP64 pipe, FP32 -> int32 on the wide ones.
+// With a = |x|: fl = floor(a) is an integer below 2^31 (the high word), and
+// a - fl is exact (Sterbenz for a >= 1, a itself below 1), so (a - fl) * 2^32
+// is the exact low part in [0, 2^32 - 2^8]; it has a fraction only for
+// a < 2^-9, where rounding it is rounding x * 2^32.  The sign is applied last
+// (round-to-nearest-even is symmetric).  Bitwise equal to rounding x * 2^32
+// to int64 directly over all finite |x| < 2^31; a NaN contributes 0.
+__device__ __forceinline__ long long fix32_rn(float x) {
+    const float a = fabsf(x);
+    const float fl = floorf(a);
+    const unsigned hi = (unsigned)__float2int_rz(fl);
+    const unsigned lo = __float2uint_rn((a - fl) * 4294967296.0f);
+    const long long m = (long long)(((unsigned long long)hi << 32) | lo);
+    return x < 0.f ? -m : m;
+}
+
 __device__ __forceinline__ void atm_fix_add(unsigned long long *acc, float x) {
-    // x * 2^32 is exact in FP32 (a power-of-two scale); one FP32 -> int64 conversion
-    const long long q = __float2ll_rn(x * 4294967296.0f);
+    const long long q = fix32_rn(x);
     if (q != 0) atomicAdd(acc, (unsigned long long)q);
 }
 

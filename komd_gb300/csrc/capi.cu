@@ -614,7 +614,7 @@ int komd_gpu_destroy(komd_gpu *h) {
     dfree(e.cell_count); dfree(e.cell_start); dfree(e.cell_mcount); dfree(e.cell_mstart); dfree(e.cell_mols);
     dfree(e.slot_site); dfree(e.skey); dfree(e.pos4); dfree(e.seps); dfree(e.posd); dfree(e.seps_d); dfree(e.sig_d);
     dfree(e.nl); dfree(e.nl_count); dfree(e.bonds); dfree(e.angles); dfree(e.partials); dfree(e.err);
-    dfree(e.tab_x); dfree(e.tab_y); dfree(e.tab_s); dfree(e.atm_acc);
+    dfree(e.tab_x); dfree(e.tab_y); dfree(e.tab_s); dfree(e.atm_acc); dfree(e.fown);
     dfree(e.rdf); dfree(e.lj_hist); dfree(e.counts); dfree(h->f_scratch); dfree(h->prof); dfree(h->acc); dfree(h->thermo_acc); dfree(e.offtab);
     dfree(e.nboff); dfree(e.vb_next); dfree(e.rebuild); dfree(e.bias); dfree(e.ref4); dfree(e.slot_cell); dfree(e.zkey); dfree(e.vl); dfree(e.vl_count);
     dfree(e.rebuild_count); dfree(e.hdtm); dfree(e.exact_com);
@@ -743,10 +743,12 @@ int komd_gpu_upload_sites(komd_gpu *h, int64_t n, const double *r, const double 
     int rc = alloc_atm_list(h, cap);
     if (rc) return rc;
     dfree(e.atm_acc);
+    dfree(e.fown);
     if ((e.cfg.terms & KOMD_TERM_ATM) && e.cfg.precision == KOMD_FP32 && e.cfg.atm_enum == KOMD_ATM_ENUM_FULL) {
         // fixed-point force sums of the once-per-triplet kernel (kept at zero between launches)
         CK(dalloc(e.atm_acc, 3 * (size_t)n));
         CK(cudaMemset(e.atm_acc, 0, sizeof(unsigned long long) * 3 * n));
+        CK(dalloc(e.fown, (size_t)n));
     }
     if (e.verlet) {
         if (n > kMaxVerletSlot) return fail(KOMD_ERR_ARG, "the Verlet path supports at most 2^26 - 1 sites");
@@ -1850,8 +1852,9 @@ int packed_group(komd_batch *b, PackedStep &pk, int r0, int r1, int pr) {
         sc.push_back(scan_args(e));
         sm.push_back(scatter_args(e));
         so.push_back(sort_args(e));
-        fl.push_back(flush_args(e, 1.0 / 4294967296.0));   // the half-list pass sums force units at 2^-32
+        fl.push_back(flush_args(e, 1.0 / 4294967296.0, half_own(e)));   // the half-list pass sums force units at 2^-32
         PairParams p = pair_params(e);
+        p.fown = half_own(e);
         AtmParams a = atm_params(e);
         pp.push_back(p);
         ap.push_back(a);

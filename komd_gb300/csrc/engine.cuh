@@ -187,6 +187,8 @@ struct PairParams {
     double lj_fscale;
     int sw;                    // switched cutoff (komd_config::switch_width > 0)
     float sw_rc2, sw_iw;       // cutoff^2 and 1 / (cutoff^2 - (cutoff - width)^2)
+    float4 *fown;              // per slot, optional: the half-list pass writes each site's own FP32 force here
+                               // (the flush widens it) instead of FP64 into f
 };
 
 struct AtmParams {
@@ -292,6 +294,7 @@ struct FlushArgs {            // k_atm_flush_step1: fixed-point sums into f, hal
     const double *hdtm;
     int *err, *rebuild;
     double *f_out, *v_out;
+    const float4 *fown;   // optional: the half-list pass's FP32 forces per slot, in place of f's
 };
 
 // TemperatureSensor's conversion (TemperatureSensor.cpp:44-47) in SciValue
@@ -414,6 +417,7 @@ struct Engine {
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     unsigned long long *atm_acc = nullptr;   // 3 per slot, fixed-point force sums of k_atm_s (zero between steps)
+    float4 *fown = nullptr;   // 1 per slot (with atm_acc): the half-list pass's own FP32 force of each site
     // tabulated pair force (KOMD_TERM_TABULATED): F(r) piecewise linear on
     // ascending nodes tab_x, values tab_y, tab_lo below / tab_hi above the nodes
     double *tab_x = nullptr, *tab_y = nullptr, *tab_s = nullptr;   // nodes, values, segment slopes

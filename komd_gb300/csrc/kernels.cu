@@ -1542,9 +1542,9 @@ Step0Args step0_args(const Engine &e) {
     return Step0Args{(int)e.n, e.r, e.v, e.f, e.hdtm, e.cfg.delta_t, e.g, e.bias, e.ref4, hs * hs, e.rebuild, e.com,
                      e.site_slot, e.pos4, e.hin_r ? e.hin_r : e.r, e.hin_v ? e.hin_v : e.v, e.hout_r};
 }
-FlushArgs flush_args(const Engine &e, double scale_fix) {
+FlushArgs flush_args(const Engine &e, double scale_fix, const float4 *own) {
     return FlushArgs{(int)e.n, e.site_slot, e.atm_acc, e.f, scale_fix, e.v, e.hdtm, e.err,
-                     e.verlet ? e.rebuild : nullptr, e.hout_f, e.hout_v};
+                     e.verlet ? e.rebuild : nullptr, e.hout_f, e.hout_v, own};
 }
 
 void launch_container(Engine &e, cudaStream_t st) {
@@ -1613,6 +1613,7 @@ PairParams pair_params(Engine &e) {
     p.eps0 = e.eps0;
     p.sig0 = e.sig0;
     sw_params(e.cfg.cutoff, e.cfg.switch_width, p.sw, p.sw_rc2, p.sw_iw);
+    p.fown = nullptr;   // set by the half-list pass's launchers (half_own)
     return p;
 }
 
@@ -1746,10 +1747,15 @@ __device__ __forceinline__ void flush_step1_body(const FlushArgs &a, int bid) {
         long long q[3];
         double fo[3], vo[3];
         for (int d = 0; d < 3; d++) q[d] = (long long)acc[3 * slot + d];
-        for (int d = 0; d < 3; d++) {
-            fo[d] = f[3 * site + d];
-            vo[d] = v[3 * site + d];
+        if (a.fown) {   // the half-list pass's FP32 force, widened exactly
+            const float4 o = a.fown[slot];
+            fo[0] = (double)o.x;
+            fo[1] = (double)o.y;
+            fo[2] = (double)o.z;
+        } else {
+            for (int d = 0; d < 3; d++) fo[d] = f[3 * site + d];
         }
+        for (int d = 0; d < 3; d++) vo[d] = v[3 * site + d];
         const double c = hdtm[site];
         bool bad = false;
         for (int d = 0; d < 3; d++) {
@@ -1778,14 +1784,21 @@ __global__ void __launch_bounds__(kIoBlock) k_atm_flush_step1(FlushArgs a) {
 
 // f[site] += 2 sign nu g (fixed point -> FP64) and the accumulators back to 0
 __global__ void k_atm_flush(int n, const int *__restrict__ slot_site, unsigned long long *__restrict__ acc,
-                            double *__restrict__ f, double scale_fix) {
+                            double *__restrict__ f, double scale_fix, const float4 *__restrict__ own) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= n) return;
     const int site = slot_site[slot];
     long long q[3];
     double fo[3];
     for (int d = 0; d < 3; d++) q[d] = (long long)acc[3 * slot + d];
-    for (int d = 0; d < 3; d++) fo[d] = f[3 * site + d];
+    if (own) {   // the half-list pass's FP32 force, widened exactly
+        const float4 o = own[slot];
+        fo[0] = (double)o.x;
+        fo[1] = (double)o.y;
+        fo[2] = (double)o.z;
+    } else {
+        for (int d = 0; d < 3; d++) fo[d] = f[3 * site + d];
+    }
     for (int d = 0; d < 3; d++) {
         acc[3 * slot + d] = 0ull;
         f[3 * site + d] = fo[d] + scale_fix * (double)q[d];
@@ -1839,11 +1852,12 @@ AtmParams atm_params(const Engine &e) {
 bool launch_atm_flush(Engine &e, cudaStream_t st, bool with_step1, bool force_units) {
     const double sign = e.cfg.atm_sign == KOMD_ATM_SIGN_REFERENCE ? 1.0 : -1.0;
     const double scale_fix = force_units ? 1.0 / kAtmFix : 2.0 * sign * e.cfg.nu / kAtmFix;
+    const float4 *own = force_units ? half_own(e) : nullptr;   // force_units: the half-list pass ran
     if (with_step1) {
-        launch_pdl(k_atm_flush_step1, nblk(e.n, kIoBlock), kIoBlock, 0, st, flush_args(e, scale_fix));
+        launch_pdl(k_atm_flush_step1, nblk(e.n, kIoBlock), kIoBlock, 0, st, flush_args(e, scale_fix, own));
         return true;
     }
-    k_atm_flush<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.slot_site, e.atm_acc, e.f, scale_fix);
+    k_atm_flush<<<nblk(e.n, 256), 256, 0, st>>>((int)e.n, e.slot_site, e.atm_acc, e.f, scale_fix, own);
     return false;
 }
 

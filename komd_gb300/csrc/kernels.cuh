@@ -24,6 +24,9 @@ void launch_lj_atm(Engine &e, cudaStream_t st);
 // true when launch_lj_atm runs the half-list form, whose fixed-point sums are
 // in force units (the flush scale is 2^-32) instead of units of 2 sign nu
 bool lj_atm_half(const Engine &e);
+// the per-slot FP32 force buffer of the half-list pass, or null where f
+// receives the pass's forces directly (terms that add to f before the flush)
+float4 *half_own(const Engine &e);
 // in_step (step graphs only): the fused drift path when the engine qualifies
 void launch_step0(Engine &e, cudaStream_t st, bool in_step = false);
 void launch_step1(Engine &e, cudaStream_t st);
@@ -62,7 +65,7 @@ ScanArgs scan_args(const Engine &e);
 ScatterArgs scatter_args(const Engine &e);
 SortArgs sort_args(const Engine &e);
 Step0Args step0_args(const Engine &e);
-FlushArgs flush_args(const Engine &e, double scale_fix);
+FlushArgs flush_args(const Engine &e, double scale_fix, const float4 *own = nullptr);
 int vlist_per(const Engine &e);
 size_t lj_atm_half_smem(const Engine &e);
 // the blocks a stage gives one replica (the same shapes as the single-system launches)

@@ -836,10 +836,14 @@ __device__ __forceinline__ void lj_atm_half_body(const PairParams &p, const AtmP
             fz += __shfl_xor_sync(0xffffffffu, fz, o);
         }
         if (lane == 0) {
-            const int site = p.slot_site[i];
-            p.f[3 * site] = (double)fx;
-            p.f[3 * site + 1] = (double)fy;
-            p.f[3 * site + 2] = (double)fz;
+            if (p.fown) {   // FP32 by slot: the flush widens it (no FP64-pipe conversions here)
+                p.fown[i] = make_float4(fx, fy, fz, 0.f);
+            } else {
+                const int site = p.slot_site[i];
+                p.f[3 * site] = (double)fx;
+                p.f[3 * site + 1] = (double)fy;
+                p.f[3 * site + 2] = (double)fz;
+            }
         }
         __syncwarp();   // se / sq / sr are refilled by the next site
     }
@@ -872,6 +876,10 @@ bool lj_atm_half(const Engine &e) {
     if (e.cfg.terms & (KOMD_TERM_LIMIT | KOMD_TERM_FENE | KOMD_TERM_TABULATED)) return false;
     return lj_atm_half_smem(e) <= 56 * 1024 || e.cfg.switch_width > 0;   // the switch runs here only
 }
+
+// the bonded terms add to f between the force pass and the flush, so with
+// them the pass writes f itself
+float4 *half_own(const Engine &e) { return (e.cfg.terms & KOMD_TERM_BONDED) ? nullptr : e.fown; }
 
 int vlist_grid(const Engine &e) { return (int)((e.n + 7) / 8); }
 
@@ -997,6 +1005,7 @@ void launch_lj_atm(Engine &e, cudaStream_t st) {
     if (lj_atm_half(e)) {
         const size_t sm = lj_atm_half_smem(e);
         const float sa = (float)(2.0 * a.sign * a.nu);   // share units (2 sign nu) to force units
+        p.fown = half_own(e);
         if (p.sw) {
             if (e.uniform) launch_half<true, true>(p, a, sa, (int)e.n, per, grid, sm, st);
             else launch_half<false, true>(p, a, sa, (int)e.n, per, grid, sm, st);
