@@ -939,6 +939,22 @@ __device__ __forceinline__ long long dkey(double x) {
     const long long m = b & 0x7fffffffffffffffLL;
     return b < 0 ? -m : m;
 }
+// double -> float rounded to nearest (ties to even) from the bits, in integer
+// instructions (GB300 converts FP64 -> FP32 on its narrow FP64 pipe): the 29
+// dropped mantissa bits decide the rounding, and a carry out of the mantissa
+// moves into the exponent as IEEE rounding does.  Results outside the FP32
+// normal range (zero, subnormal, overflow, NaN) take the conversion
+// instruction.  Bitwise equal to __double2float_rn.
+__device__ __forceinline__ float d2f_rn(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ffu) - 1023 + 127;   // the FP32 biased exponent
+    if (e < 1 || e > 254) return __double2float_rn(x);
+    const unsigned long long mant = b & 0xfffffffffffffULL;
+    unsigned f = ((unsigned)e << 23) | (unsigned)(mant >> 29);
+    const unsigned rest = (unsigned)(mant & 0x1fffffffULL);
+    f += (rest > 0x10000000u || (rest == 0x10000000u && (f & 1u))) ? 1u : 0u;
+    return __uint_as_float(f | ((unsigned)(b >> 32) & 0x80000000u));
+}
 __device__ __forceinline__ bool dkey_nan(double x) {
     return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
 }
@@ -1027,10 +1043,15 @@ __device__ __forceinline__ void step0_fused_body(const Step0Args &a, int bid) {
             off[d] = 0.0;
             const long long kx = dkey(x[d]);
             if (!dkey_nan(x[d])) {
-                if (kx < dkey(g.low[d])) off[d] = g.L[d];
-                if (kx > dkey(g.high[d])) off[d] = -g.L[d];
+                if (kx < dkey(g.low[d])) {
+                    off[d] = g.L[d];
+                    moved = true;
+                }
+                if (kx > dkey(g.high[d])) {
+                    off[d] = -g.L[d];
+                    moved = true;
+                }
             }
-            moved |= (off[d] != 0.0);
         }
         if (moved) {   // r += shift over all three components, as Periodic_Kernel
             for (int d = 0; d < 3; d++) {
@@ -1040,9 +1061,9 @@ __device__ __forceinline__ void step0_fused_body(const Step0Args &a, int bid) {
             }
         }
         float4 p = pos4[site_slot[s]];
-        p.x = __double2float_rn(dsub(x[0], b[0]));
-        p.y = __double2float_rn(dsub(x[1], b[1]));
-        p.z = __double2float_rn(dsub(x[2], b[2]));
+        p.x = d2f_rn(dsub(x[0], b[0]));
+        p.y = d2f_rn(dsub(x[1], b[1]));
+        p.z = d2f_rn(dsub(x[2], b[2]));
         pos4[site_slot[s]] = p;
         {
             const float4 q = ref4[s];
@@ -1747,25 +1768,22 @@ __device__ __forceinline__ void flush_step1_body(const FlushArgs &a, int bid) {
         long long q[3];
         double fo[3], vo[3];
         for (int d = 0; d < 3; d++) q[d] = (long long)acc[3 * slot + d];
-        if (a.fown) {   // the half-list pass's FP32 force, widened exactly
-            const float4 o = a.fown[slot];
-            fo[0] = (double)o.x;
-            fo[1] = (double)o.y;
-            fo[2] = (double)o.z;
-        } else {
+        float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (a.fown) o = a.fown[slot];   // the half-list pass's FP32 force (force units, scale 2^-32)
+        else
             for (int d = 0; d < 3; d++) fo[d] = f[3 * site + d];
-        }
         for (int d = 0; d < 3; d++) vo[d] = v[3 * site + d];
         const double c = hdtm[site];
         bool bad = false;
         for (int d = 0; d < 3; d++) {
             acc[3 * slot + d] = 0ull;
             // scale_fix = scale / 2^32 exactly: the same product as scale * (q / 2^32)
-            const double fd = fo[d] + scale_fix * (double)q[d];
+            const double fd = a.fown ? own_plus_fixed(d == 0 ? o.x : (d == 1 ? o.y : o.z), q[d])
+                                     : fo[d] + scale_fix * (double)q[d];
             f[3 * site + d] = fd;
             const double vv = dadd(vo[d], dmul(fd, c));
             v[3 * site + d] = vv;
-            bad |= !isfinite(vv);
+            bad |= !finite_bits(vv);
             s_f[3 * t + d] = fd;
             s_v[3 * t + d] = vv;
         }
@@ -1791,14 +1809,15 @@ __global__ void k_atm_flush(int n, const int *__restrict__ slot_site, unsigned l
     long long q[3];
     double fo[3];
     for (int d = 0; d < 3; d++) q[d] = (long long)acc[3 * slot + d];
-    if (own) {   // the half-list pass's FP32 force, widened exactly
+    if (own) {   // the half-list pass's FP32 force (force units, scale 2^-32), as k_atm_flush_step1
         const float4 o = own[slot];
-        fo[0] = (double)o.x;
-        fo[1] = (double)o.y;
-        fo[2] = (double)o.z;
-    } else {
-        for (int d = 0; d < 3; d++) fo[d] = f[3 * site + d];
+        for (int d = 0; d < 3; d++) {
+            acc[3 * slot + d] = 0ull;
+            f[3 * site + d] = own_plus_fixed(d == 0 ? o.x : (d == 1 ? o.y : o.z), q[d]);
+        }
+        return;
     }
+    for (int d = 0; d < 3; d++) fo[d] = f[3 * site + d];
     for (int d = 0; d < 3; d++) {
         acc[3 * slot + d] = 0ull;
         f[3 * site + d] = fo[d] + scale_fix * (double)q[d];

@@ -43,3 +43,67 @@ def test_split_conversion_edge_cases():
     assert split_conversion(np.float32(2.0 ** -33)) == 0
     assert split_conversion(np.float32(3 * 2.0 ** -33)) == 2
     assert split_conversion(np.float32(-3 * 2.0 ** -33)) == -2
+
+
+def own_plus_fixed(own, q):
+    """The flush's FP64 force from the FP32 own force and the fixed-point sum
+    (komd_gb300/csrc/atm_device.cuh, own_plus_fixed): the exact int64 sum
+    rounded once, scaled by 2^-32, where the inputs allow; the FP64 form
+    elsewhere."""
+    own = np.asarray(own, np.float32)
+    q = np.asarray(q, np.int64)
+    ub = own.view(np.uint32)
+    ex = (ub >> 23) & 0xff
+    exact = (((ub << 1) == 0) | ((ex >= 118) & (ex < 158))) & (q > -(2 ** 53)) & (q < 2 ** 53)
+    s = split_conversion(own) + q
+    fast = s.astype(np.float64) * 2.0 ** -32
+    slow = own.astype(np.float64) + 2.0 ** -32 * q.astype(np.float64)
+    return np.where(exact, fast, slow), exact
+
+
+def test_own_plus_fixed_equals_fp64_form():
+    rng = np.random.default_rng(9)
+    n = 2_000_000
+    own = (rng.standard_normal(n) * 10.0 ** rng.uniform(-4, 4, n)).astype(np.float32)
+    q = (rng.standard_normal(n) * 2.0 ** rng.uniform(0, 60, n)).astype(np.int64)
+    own[:1000] = 0.0
+    own[1000:2000] = -0.0
+    q[2000:3000] = -split_conversion(own[2000:3000])   # sums that cancel exactly
+    got, exact = own_plus_fixed(own, q)
+    want = own.astype(np.float64) + 2.0 ** -32 * q.astype(np.float64)
+    assert exact.mean() > 0.5
+    assert np.array_equal(got.view(np.int64), want.view(np.int64))
+
+
+def d2f_rn(x):
+    """The fused drift's FP64 -> FP32 rounding from the bits
+    (komd_gb300/csrc/kernels.cu, d2f_rn), the conversion instruction outside
+    the FP32 normal range."""
+    x = np.asarray(x, np.float64)
+    b = x.view(np.uint64)
+    e = ((b >> np.uint64(52)) & np.uint64(0x7ff)).astype(np.int64) - 1023 + 127
+    mant = b & np.uint64(0xfffffffffffff)
+    f = ((np.clip(e, 0, 255).astype(np.uint64) << np.uint64(23)) | (mant >> np.uint64(29))).astype(np.uint64)
+    rest = mant & np.uint64(0x1fffffff)
+    half = np.uint64(0x10000000)
+    up = (rest > half) | ((rest == half) & ((f & np.uint64(1)) == 1))
+    f = (f + up.astype(np.uint64)) | ((b >> np.uint64(32)) & np.uint64(0x80000000))
+    bits = f.astype(np.uint32).view(np.float32)
+    normal = (e >= 1) & (e <= 254)
+    return np.where(normal, bits, x.astype(np.float32))
+
+
+def test_d2f_rn_equals_conversion():
+    rng = np.random.default_rng(13)
+    n = 2_000_000
+    x = rng.standard_normal(n) * 10.0 ** rng.uniform(-45, 40, n)
+    # values on and next to the FP32 rounding ties
+    t = rng.standard_normal(200_000).astype(np.float32).astype(np.float64)
+    ulp = np.spacing(np.abs(t).astype(np.float32)).astype(np.float64)
+    x = np.concatenate([x, t, t + ulp / 2, t - ulp / 2, t + ulp / 2 * (1 + 2.0 ** -30), np.nextafter(t + ulp / 2, 0),
+                        [0.0, -0.0, 3.4028234663852886e38, 3.4028235677973366e38, 1.1754943508222875e-38,
+                         1.1754942e-38, np.inf, -np.inf]])
+    with np.errstate(over="ignore"):
+        got = d2f_rn(x)
+        want = x.astype(np.float32)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
