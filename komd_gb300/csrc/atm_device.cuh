@@ -50,30 +50,6 @@ __device__ __forceinline__ long long fix32_rn(float x) {
     return x < 0.f ? -m : m;
 }
 
-// own + q * 2^-32 for the half-list pass's FP32 own force and a fixed-point
-// sum q, bitwise equal to (double)own + 2^-32 * (double)q with one FP64-pipe
-// instruction instead of four: where own * 2^32 is an integer (|own| in
-// [2^-9, 2^31), or zero) and |q| < 2^53, that expression rounds the exact sum
-// once; here the sum is formed exactly in int64, rounded by one int64 -> FP64
-// conversion and scaled by 2^-32 in the exponent field (exact: a nonzero
-// rounded sum is an integer of magnitude >= 1).  Other inputs take the FP64 form.
-__device__ __forceinline__ double own_plus_fixed(float own, long long q) {
-    const unsigned ub = __float_as_uint(own);
-    const unsigned ex = (ub >> 23) & 0xffu;
-    const bool exact = ((ub << 1) == 0u || (ex >= 118u && ex < 158u)) && q > -(1LL << 53) && q < (1LL << 53);
-    if (exact) {
-        const long long s = fix32_rn(own) + q;
-        if (s == 0) return 0.0;
-        return __longlong_as_double(__double_as_longlong(__ll2double_rn(s)) - (32LL << 52));
-    }
-    return (double)own + (1.0 / 4294967296.0) * (double)q;
-}
-
-// x is neither infinite nor NaN, from the exponent field (integer instructions)
-__device__ __forceinline__ bool finite_bits(double x) {
-    return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
-}
-
 __device__ __forceinline__ void atm_fix_add(unsigned long long *acc, float x) {
     const long long q = fix32_rn(x);
     if (q != 0) atomicAdd(acc, (unsigned long long)q);

@@ -1768,22 +1768,25 @@ __device__ __forceinline__ void flush_step1_body(const FlushArgs &a, int bid) {
         long long q[3];
         double fo[3], vo[3];
         for (int d = 0; d < 3; d++) q[d] = (long long)acc[3 * slot + d];
-        float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (a.fown) o = a.fown[slot];   // the half-list pass's FP32 force (force units, scale 2^-32)
-        else
+        if (a.fown) {   // the half-list pass's FP32 force, widened exactly
+            const float4 o = a.fown[slot];
+            fo[0] = (double)o.x;
+            fo[1] = (double)o.y;
+            fo[2] = (double)o.z;
+        } else {
             for (int d = 0; d < 3; d++) fo[d] = f[3 * site + d];
+        }
         for (int d = 0; d < 3; d++) vo[d] = v[3 * site + d];
         const double c = hdtm[site];
         bool bad = false;
         for (int d = 0; d < 3; d++) {
             acc[3 * slot + d] = 0ull;
             // scale_fix = scale / 2^32 exactly: the same product as scale * (q / 2^32)
-            const double fd = a.fown ? own_plus_fixed(d == 0 ? o.x : (d == 1 ? o.y : o.z), q[d])
-                                     : fo[d] + scale_fix * (double)q[d];
+            const double fd = fo[d] + scale_fix * (double)q[d];
             f[3 * site + d] = fd;
             const double vv = dadd(vo[d], dmul(fd, c));
             v[3 * site + d] = vv;
-            bad |= !finite_bits(vv);
+            bad |= !isfinite(vv);
             s_f[3 * t + d] = fd;
             s_v[3 * t + d] = vv;
         }
@@ -1809,15 +1812,14 @@ __global__ void k_atm_flush(int n, const int *__restrict__ slot_site, unsigned l
     long long q[3];
     double fo[3];
     for (int d = 0; d < 3; d++) q[d] = (long long)acc[3 * slot + d];
-    if (own) {   // the half-list pass's FP32 force (force units, scale 2^-32), as k_atm_flush_step1
+    if (own) {   // the half-list pass's FP32 force, widened exactly
         const float4 o = own[slot];
-        for (int d = 0; d < 3; d++) {
-            acc[3 * slot + d] = 0ull;
-            f[3 * site + d] = own_plus_fixed(d == 0 ? o.x : (d == 1 ? o.y : o.z), q[d]);
-        }
-        return;
+        fo[0] = (double)o.x;
+        fo[1] = (double)o.y;
+        fo[2] = (double)o.z;
+    } else {
+        for (int d = 0; d < 3; d++) fo[d] = f[3 * site + d];
     }
-    for (int d = 0; d < 3; d++) fo[d] = f[3 * site + d];
     for (int d = 0; d < 3; d++) {
         acc[3 * slot + d] = 0ull;
         f[3 * site + d] = fo[d] + scale_fix * (double)q[d];

@@ -1,9 +1,11 @@
-"""The force accumulators' FP32 -> 64-bit fixed-point conversion
-(komd_gb300/csrc/atm_device.cuh, fix32_rn): round(x * 2^32) as int64 built
-from two 32-bit conversions.  This restates the kernel's FP32 steps in numpy
-float32 (the same IEEE operations) and checks them bit for bit against the
-direct rounding of x * 2^32 over random bit patterns and the edge cases: values
-next to integers, the ulp boundary at 2^-9, ties to even, and the signs."""
+"""Two conversions the kernels build from other instructions, restated in
+numpy with the same IEEE operations and checked bit for bit:
+  * the force accumulators' FP32 -> 64-bit fixed-point conversion
+    (komd_gb300/csrc/atm_device.cuh, fix32_rn): round(x * 2^32) as int64 from
+    two 32-bit conversions, over random bit patterns and the edge cases
+    (values next to integers, the ulp boundary at 2^-9, ties to even, signs);
+  * the fused drift's FP64 -> FP32 rounding from the bits
+    (komd_gb300/csrc/kernels.cu, d2f_rn)."""
 import numpy as np
 
 TWO32 = np.float32(4294967296.0)
@@ -43,36 +45,6 @@ def test_split_conversion_edge_cases():
     assert split_conversion(np.float32(2.0 ** -33)) == 0
     assert split_conversion(np.float32(3 * 2.0 ** -33)) == 2
     assert split_conversion(np.float32(-3 * 2.0 ** -33)) == -2
-
-
-def own_plus_fixed(own, q):
-    """The flush's FP64 force from the FP32 own force and the fixed-point sum
-    (komd_gb300/csrc/atm_device.cuh, own_plus_fixed): the exact int64 sum
-    rounded once, scaled by 2^-32, where the inputs allow; the FP64 form
-    elsewhere."""
-    own = np.asarray(own, np.float32)
-    q = np.asarray(q, np.int64)
-    ub = own.view(np.uint32)
-    ex = (ub >> 23) & 0xff
-    exact = (((ub << 1) == 0) | ((ex >= 118) & (ex < 158))) & (q > -(2 ** 53)) & (q < 2 ** 53)
-    s = split_conversion(own) + q
-    fast = s.astype(np.float64) * 2.0 ** -32
-    slow = own.astype(np.float64) + 2.0 ** -32 * q.astype(np.float64)
-    return np.where(exact, fast, slow), exact
-
-
-def test_own_plus_fixed_equals_fp64_form():
-    rng = np.random.default_rng(9)
-    n = 2_000_000
-    own = (rng.standard_normal(n) * 10.0 ** rng.uniform(-4, 4, n)).astype(np.float32)
-    q = (rng.standard_normal(n) * 2.0 ** rng.uniform(0, 60, n)).astype(np.int64)
-    own[:1000] = 0.0
-    own[1000:2000] = -0.0
-    q[2000:3000] = -split_conversion(own[2000:3000])   # sums that cancel exactly
-    got, exact = own_plus_fixed(own, q)
-    want = own.astype(np.float64) + 2.0 ** -32 * q.astype(np.float64)
-    assert exact.mean() > 0.5
-    assert np.array_equal(got.view(np.int64), want.view(np.int64))
 
 
 def d2f_rn(x):
