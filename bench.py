@@ -446,7 +446,48 @@ def next_rows_leg(args, stream, local):
         out["multisite_300k"] = multisite_leg(stream, local, events_ms)
     except Exception as exc:
         out["multisite_300k"] = {"error": f"{type(exc).__name__}: {exc}"}
+    for name, fn in (("plain_lj_4k", lambda: small_leg(stream, local, events_ms, "lj_argon_4k", 1000)),
+                     ("lj_atm_32k", lambda: small_leg(stream, local, events_ms, "lj_atm_argon_32k", 500))):
+        try:
+            out[name] = fn()
+        except Exception as exc:
+            out[name] = {"error": f"{type(exc).__name__}: {exc}"}
     return out
+
+
+def small_leg(stream, local, events_ms, workload, steps):
+    """The small argon workloads at their stated lengths: plain LJ on 4,000
+    atoms (FCC 10^3) for 1000 steps, and LJ + ATM (FULL triplets, F = -grad V)
+    on 32,000 atoms (FCC 20^3) for 500 steps; rho* 0.8442, T* 0.722, dt* 0.005,
+    all steps timed after 3 warm-up steps.  Two forms each: FP32 forces on the
+    Verlet path (skin 0.3, cells >= cutoff + skin) and FP64 forces on per-step
+    cells (cells >= cutoff), FP64 integration in both."""
+    from komd_gb300 import autotune, gpu, lattice
+    w = WORKLOADS[workload]
+    s = lattice.argon_fcc(w["ncell"], rho=w["rho"], t_star=w["t"], seed=5)
+    side = float(np.min(s.high - s.low))
+    terms = gpu.TERM_LJ | (gpu.TERM_ATM if w["atm"] else 0)
+    reach = max(w["rc"], w["rc3"] if w["atm"] else 0.0)
+
+    def run(precision, skin):
+        cfg = gpu.make_config(s.low, s.high, autotune.cell_for(side, reach + skin), cutoff=w["rc"],
+                              cutoff_3b=w["rc3"], nu=w["nu"], dt=w["dt"], terms=terms, precision=precision,
+                              atm_sign=gpu.ATM_SIGN_PHYSICAL, atm_enum=gpu.ATM_ENUM_FULL,
+                              virial_mode=gpu.VIRIAL_CORRECT, skin=skin)
+        g = gpu.GpuSystem(s, cfg, device=local)
+        try:
+            g.set_stream(stream.cuda_stream)
+            g.update_container()
+            g.forces()
+            g.step(3)
+            ms = events_ms(lambda: g.step(steps))
+            return dict(value=s.n * steps / (ms / 1e3), unit=UNIT, ms_per_step=ms / steps)
+        finally:
+            g.close()
+
+    return {"fp32_verlet": run(gpu.FP32, 0.3), "fp64_forces": run(gpu.FP64, 0.0), "sites": s.n, "steps": steps,
+            "config": f"{s.n} argon atoms, rho* {w['rho']}, T* {w['t']}, LJ rc {w['rc']}"
+                      + (f" + ATM rc {w['rc3']} nu* {w['nu']}" if w["atm"] else "") + f", dt* {w['dt']}"}
 
 
 def multisite_leg(stream, local, events_ms, steps=500):
