@@ -595,6 +595,51 @@ def test_multisite_verlet_matches_cell_lists():
     b.close()
 
 
+def test_molecules_with_atm_on_the_half_list_pass():
+    """LJ + ATM (FULL, physical sign) + bonds and angles on the Verlet path:
+    the half-list pass writes f itself (the bonded kernels add to it before
+    the flush) instead of its per-slot FP32 buffer.  2,000 flexible 3-site
+    molecules (6,000 sites, site density 0.8), cells >= cutoff + skin + 2.0.
+    The forces match the per-step cell lists' (skin 0, the same cells) at the
+    start, the trajectories agree over 100 steps with list rebuilds, and the
+    energies agree."""
+    from komd_gb300 import gpu, lattice
+    s = lattice.triatomic_count(2000, rho_site=0.8, t_star=1.0, seed=41, aligned=True)
+    L = float((s.high - s.low)[0])
+    th0 = np.deg2rad(109.47)
+
+    def cfg(skin):
+        return gpu.make_config(s.low, s.high, L / np.floor(L / 4.8), cutoff=2.5, cutoff_3b=2.0, nu=0.073, dt=0.002,
+                               terms=gpu.TERM_LJ | gpu.TERM_ATM | gpu.TERM_BONDED, atm_sign=gpu.ATM_SIGN_PHYSICAL,
+                               atm_enum=gpu.ATM_ENUM_FULL, virial_mode=gpu.VIRIAL_CORRECT, bond_k=1000.0,
+                               bond_r0=1.0, angle_k=100.0, angle_theta0=th0, skin=skin)
+
+    a = gpu.GpuSystem(s, cfg(0.3))
+    b = gpu.GpuSystem(s, cfg(0.0))
+    for g in (a, b):
+        g.update_container()
+        g.forces()
+    _, _, fa0 = a.download()
+    _, _, fb0 = b.download()
+    assert rel_rmse(fa0, fb0) < 2e-6
+    a.set_profiling(False)
+    for _ in range(10):
+        a.step(10)
+        b.step(10)
+    assert a.profile().get("list_rebuilds", (0, 0.0))[0] >= 1
+    ra, va, fa = a.download()
+    rb, vb, fb = b.download()
+    assert np.isfinite(ra).all() and np.isfinite(va).all()
+    assert np.abs(ra - rb).max() < 1e-4
+    assert rel_rmse(fa, fb) < 1e-4
+    oa = a.measure(gpu.MEASURE_ENERGY | gpu.MEASURE_TEMPERATURE)
+    ob = b.measure(gpu.MEASURE_ENERGY | gpu.MEASURE_TEMPERATURE)
+    for key in ("u_lj", "u_atm", "u_bonded", "mv2"):
+        assert oa[key] == pytest.approx(ob[key], rel=1e-4)
+    a.close()
+    b.close()
+
+
 def test_plain_lj_4000_fp64_1000_steps(oracle_lib):
     """The plain LJ workload at its full size and length: 4,000 argon atoms
     (FCC 10^3, rho* 0.8442, T* 0.722), cutoff 2.5, 1000 NVE steps of dt 0.005,
