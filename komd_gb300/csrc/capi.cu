@@ -1835,6 +1835,7 @@ int packed_group(komd_batch *b, PackedStep &pk, int r0, int r1, int pr) {
     pk.nrep = nr;
     pk.uniform = reps[0]->e.uniform;
     pk.sw = reps[0]->e.cfg.switch_width > 0;
+    pk.plain = true;   // cleared below by any replica with the LJ term off or an ATM2B factor
     std::vector<Step0Args> s0;
     std::vector<BinArgs> bi;
     std::vector<ScanArgs> sc;
@@ -1855,6 +1856,7 @@ int packed_group(komd_batch *b, PackedStep &pk, int r0, int r1, int pr) {
         fl.push_back(flush_args(e, 1.0 / 4294967296.0, half_own(e)));   // the half-list pass sums force units at 2^-32
         PairParams p = pair_params(e);
         p.fown = half_own(e);
+        if (!half_plain(p)) pk.plain = false;
         AtmParams a = atm_params(e);
         pp.push_back(p);
         ap.push_back(a);

@@ -27,6 +27,8 @@ bool lj_atm_half(const Engine &e);
 // the per-slot FP32 force buffer of the half-list pass, or null where f
 // receives the pass's forces directly (terms that add to f before the flush)
 float4 *half_own(const Engine &e);
+// LJ on and no ATM2B factor: the half-list pass reads neither per pair
+bool half_plain(const PairParams &p);
 // in_step (step graphs only): the fused drift path when the engine qualifies
 void launch_step0(Engine &e, cudaStream_t st, bool in_step = false);
 void launch_step1(Engine &e, cudaStream_t st);
@@ -59,6 +61,7 @@ struct PackedStep {
     int *n = nullptr, *per = nullptr;
     size_t force_smem = 0;    // the largest replica's staging
     bool uniform = true, sw = false;
+    bool plain = false;       // every replica: LJ on, no ATM2B factor (the half-list pass's PLAIN form)
 };
 BinArgs bin_args(const Engine &e);
 ScanArgs scan_args(const Engine &e);

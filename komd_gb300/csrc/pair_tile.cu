@@ -696,7 +696,9 @@ __device__ __forceinline__ void half_row_load(const PairParams &p, int i, int la
     h.cell = p.slot_cell[i];
 }
 
-template <bool UNIFORM, bool SW>
+// PLAIN: the LJ term is on with no ATM2B factor (use_lj = 1, lj_fscalef = 1),
+// so neither is read per pair (the products are the same: a factor of 1 is exact)
+template <bool UNIFORM, bool SW, bool PLAIN>
 __device__ __forceinline__ void lj_half(const PairParams &p, int i, const HalfRow &h, int lane, unsigned lt, float rc2,
                                         float rc3sq, float4 *se, float4 *sq, float4 *sr, int capa, int capr,
                                         int &m_out, int &k_out, float &fx, float &fy, float &fz) {
@@ -741,7 +743,7 @@ __device__ __forceinline__ void lj_half(const PairParams &p, int i, const HalfRo
                 dy = pi.y - (pj[u].y + o[u].y);
                 dz = pi.z - (pj[u].z + o[u].z);
                 r2 = dx * dx + dy * dy + dz * dz;
-                lj = p.use_lj && r2 <= rc2 && !(e[u] >> 31);
+                lj = (PLAIN || p.use_lj) && r2 <= rc2 && !(e[u] >> 31);
                 if (lj) {
                     const float inv = rcp_approx(r2);
                     float x, ee;
@@ -754,7 +756,8 @@ __device__ __forceinline__ void lj_half(const PairParams &p, int i, const HalfRo
                         ee = sei * sej[u];
                     }
                     const float lj6 = x * x * x;
-                    float fac = 24.0f * ee * (2.0f * lj6 * lj6 - lj6) * inv * p.lj_fscalef;   // ATM2B factor
+                    float fac = 24.0f * ee * (2.0f * lj6 * lj6 - lj6) * inv;
+                    if (!PLAIN) fac *= p.lj_fscalef;   // ATM2B factor
                     if (SW) {   // switched cutoff (no ATM2B with it): U S, force fac S - 2 U dS/dx
                         float S, dS;
                         sw_eval(r2, p.sw_rc2, p.sw_iw, S, dS);
@@ -791,7 +794,7 @@ __device__ __forceinline__ void lj_half(const PairParams &p, int i, const HalfRo
     k_out = k;
 }
 
-template <bool UNIFORM, bool SW>
+template <bool UNIFORM, bool SW, bool PLAIN>
 __device__ __forceinline__ void lj_atm_half_body(const PairParams &p, const AtmParams &a, float sa, int n, int per,
                                                  int bid) {
     extern __shared__ float4 s_dyn[];
@@ -807,7 +810,7 @@ __device__ __forceinline__ void lj_atm_half_body(const PairParams &p, const AtmP
         half_row_load(p, i, lane, cur);
         int m, k;
         float fx, fy, fz;
-        lj_half<UNIFORM, SW>(p, i, cur, lane, lt, rc2, rc3sq, se, sq, sr, capa, capr, m, k, fx, fy, fz);
+        lj_half<UNIFORM, SW, PLAIN>(p, i, cur, lane, lt, rc2, rc3sq, se, sq, sr, capa, capr, m, k, fx, fy, fz);
         __syncwarp();
         float ax, ay, az, gx, gy, gz;
         atm_vertex_shares<SW>(a, se, sq, m, lane, rc3f, sa, ax, ay, az, gx, gy, gz);
@@ -848,19 +851,19 @@ __device__ __forceinline__ void lj_atm_half_body(const PairParams &p, const AtmP
         __syncwarp();   // se / sq / sr are refilled by the next site
     }
 }
-template <bool UNIFORM, bool SW>
+template <bool UNIFORM, bool SW, bool PLAIN>
 __global__ void __launch_bounds__(256, 4) k_lj_atm_half(PairParams p, AtmParams a, float sa, int n, int per) {
     pdl_trigger();
     pdl_wait();
-    lj_atm_half_body<UNIFORM, SW>(p, a, sa, n, per, blockIdx.x);
+    lj_atm_half_body<UNIFORM, SW, PLAIN>(p, a, sa, n, per, blockIdx.x);
 }
 
-template <bool UNIFORM, bool SW>
+template <bool UNIFORM, bool SW, bool PLAIN = false>
 static void launch_half(const PairParams &p, const AtmParams &a, float sa, int n, int per, int grid, size_t sm,
                         cudaStream_t st) {
     if (sm > 48 * 1024)
-        cudaFuncSetAttribute(k_lj_atm_half<UNIFORM, SW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    launch_pdl(k_lj_atm_half<UNIFORM, SW>, grid, 256, sm, st, p, a, sa, n, per);
+        cudaFuncSetAttribute(k_lj_atm_half<UNIFORM, SW, PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    launch_pdl(k_lj_atm_half<UNIFORM, SW, PLAIN>, grid, 256, sm, st, p, a, sa, n, per);
 }
 
 // shared memory of the half-list pass: per warp nl_cap staged triplet
@@ -876,6 +879,8 @@ bool lj_atm_half(const Engine &e) {
     if (e.cfg.terms & (KOMD_TERM_LIMIT | KOMD_TERM_FENE | KOMD_TERM_TABULATED)) return false;
     return lj_atm_half_smem(e) <= 56 * 1024 || e.cfg.switch_width > 0;   // the switch runs here only
 }
+
+bool half_plain(const PairParams &p) { return p.use_lj && p.lj_fscalef == 1.0f; }
 
 // the bonded terms add to f between the force pass and the flush, so with
 // them the pass writes f itself
@@ -911,23 +916,23 @@ __global__ void __launch_bounds__(32 * kVbWarps) k_vlist_build_p(const PairParam
     else vlist_build_body<false>(p[r], blockIdx.x - start[r]);
 }
 
-template <bool UNIFORM, bool SW>
+template <bool UNIFORM, bool SW, bool PLAIN>
 __global__ void __launch_bounds__(256, 4) k_lj_atm_half_p(const PairParams *__restrict__ p,
                                                           const AtmParams *__restrict__ a,
                                                           const float *__restrict__ sa, const int *__restrict__ n,
                                                           const int *__restrict__ per, const int *__restrict__ start,
                                                           int nrep) {
     const int r = packed_replica(start, nrep, blockIdx.x);
-    lj_atm_half_body<UNIFORM, SW>(p[r], a[r], sa[r], n[r], per[r], blockIdx.x - start[r]);
+    lj_atm_half_body<UNIFORM, SW, PLAIN>(p[r], a[r], sa[r], n[r], per[r], blockIdx.x - start[r]);
 }
 
-template <bool UNIFORM, bool SW>
+template <bool UNIFORM, bool SW, bool PLAIN = false>
 static void launch_half_p(const PackedStep &pk, cudaStream_t st) {
     if (pk.force_smem > 48 * 1024)
-        cudaFuncSetAttribute(k_lj_atm_half_p<UNIFORM, SW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(k_lj_atm_half_p<UNIFORM, SW, PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)pk.force_smem);
-    k_lj_atm_half_p<UNIFORM, SW><<<pk.force.blocks, 256, pk.force_smem, st>>>(pk.pp, pk.ap, pk.sa, pk.n, pk.per,
-                                                                              pk.force.start, pk.nrep);
+    k_lj_atm_half_p<UNIFORM, SW, PLAIN><<<pk.force.blocks, 256, pk.force_smem, st>>>(pk.pp, pk.ap, pk.sa, pk.n,
+                                                                                     pk.per, pk.force.start, pk.nrep);
 }
 
 void launch_packed_pair_stages(const PackedStep &pk, cudaStream_t st, bool vbuild) {
@@ -939,7 +944,8 @@ void launch_packed_pair_stages(const PackedStep &pk, cudaStream_t st, bool vbuil
         if (pk.uniform) launch_half_p<true, true>(pk, st);
         else launch_half_p<false, true>(pk, st);
     } else {
-        if (pk.uniform) launch_half_p<true, false>(pk, st);
+        if (pk.uniform && pk.plain) launch_half_p<true, false, true>(pk, st);   // the benchmark's form
+        else if (pk.uniform) launch_half_p<true, false>(pk, st);
         else launch_half_p<false, false>(pk, st);
     }
 }
@@ -1010,7 +1016,8 @@ void launch_lj_atm(Engine &e, cudaStream_t st) {
             if (e.uniform) launch_half<true, true>(p, a, sa, (int)e.n, per, grid, sm, st);
             else launch_half<false, true>(p, a, sa, (int)e.n, per, grid, sm, st);
         } else {
-            if (e.uniform) launch_half<true, false>(p, a, sa, (int)e.n, per, grid, sm, st);
+            if (e.uniform && half_plain(p)) launch_half<true, false, true>(p, a, sa, (int)e.n, per, grid, sm, st);
+            else if (e.uniform) launch_half<true, false>(p, a, sa, (int)e.n, per, grid, sm, st);
             else launch_half<false, false>(p, a, sa, (int)e.n, per, grid, sm, st);
         }
         return;
