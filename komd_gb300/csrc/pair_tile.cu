@@ -771,8 +771,10 @@ __device__ __forceinline__ void lj_half(const PairParams &p, int i, const HalfRo
             const bool lo = lj && !at;              // an LJ-only partner
             const unsigned ma = __ballot_sync(0xffffffffu, at), ml = __ballot_sync(0xffffffffu, lo);
             if (at || lo) {
-                const int nb = (int)((e[u] >> 26) & 31u), j = (int)(e[u] & 0x3ffffffu);
-                const int code = nb | (o[u].w != 0.f ? 32 : 0) | (j << 6);
+                // the partner's slot j at bits 6-30 (j < 2^25 with ATM on): the list word
+                // shifted past its cell and molecule bits.  This pass reads only
+                // code >> 6 (the cell bits of atm_code are for the COMPAT filter)
+                const int code = (int)(e[u] << 6);
                 const float4 react = make_float4(-gx, -gy, -gz, __int_as_float(code));
                 if (at) {
                     const int pos = m + __popc(ma & lt);
