@@ -463,6 +463,46 @@ def test_binary_mixture_half_list_pass(oracle_lib):
     assert np.abs(f.sum(0)).max() < 1e-3 * np.sqrt(s.n) * np.abs(f).mean()
 
 
+def test_atm_only_on_the_half_list_pass(oracle_lib):
+    """ATM without LJ on the Verlet path: the half-list pass in its general
+    form (the LJ switch read per pair; the one-species LJ + ATM case runs a
+    form without it).  4,000 sites, skin 0.3, FULL triplets, physical sign.
+    The forces match the per-step cell lists' and the oracle's, and after 50
+    steps the oracle's at the engine's positions."""
+    from komd_gb300 import gpu, lattice
+    s = lattice.argon_fcc(10, rho=0.8442, t_star=0.9, seed=47, jitter=0.05)
+
+    def cfg(skin):
+        return gpu.make_config(s.low, s.high, 2.8, cutoff=2.0, cutoff_3b=2.0, nu=0.073, dt=0.005,
+                               terms=gpu.TERM_ATM, atm_sign=gpu.ATM_SIGN_PHYSICAL, atm_enum=gpu.ATM_ENUM_FULL,
+                               virial_mode=gpu.VIRIAL_CORRECT, skin=skin)
+
+    def oracle_forces(r, v):
+        sim = oracle_lib.OracleSim(lattice.System(r=r, v=v, m=s.m, eps=s.eps, sig=s.sig, mol_id=s.mol_id,
+                                                  low=s.low, high=s.high), 2.8, 2.0, nu=0.073, cutoff_atm=2.0,
+                                   lj=False, atm=True, atm_mode="full", atm_sign=oracle_lib.ATM_SIGN_PHYSICAL,
+                                   virial_mode=oracle_lib.VIRIAL_CORRECT)
+        sim.update_container()
+        sim.forces()
+        return sim.f
+
+    a = gpu.GpuSystem(s, cfg(0.3))
+    b = gpu.GpuSystem(s, cfg(0.0))
+    for g in (a, b):
+        g.update_container()
+        g.forces()
+    r0, v0, fa = a.download()
+    _, _, fb = b.download()
+    assert rel_rmse(fa, fb) < 2e-6
+    assert rel_rmse(fa, oracle_forces(r0, v0)) < FP32_FORCE_RMSE
+    a.step(50)
+    r, v, f = a.download()
+    assert np.isfinite(r).all()
+    assert rel_rmse(f, oracle_forces(r, v)) < FP32_FORCE_RMSE
+    a.close()
+    b.close()
+
+
 def test_verlet_requires_cell_for_skin():
     from komd_gb300 import gpu, lattice
     s = lattice.argon_fcc(10, seed=1)
