@@ -100,7 +100,11 @@ typedef struct komd_config {
     double skin;               /* Verlet skin: > 0 keeps a neighbour list inside cutoff + skin and
                                   rebuilds cells and list only when a site has moved more than
                                   skin/2 (FP32, no FENE, FULL ATM, CORRECT virial); 0 rebuilds
-                                  every step like LinkedCells::updateContainer */
+                                  every step like LinkedCells::updateContainer.  Cells bin
+                                  molecules by their centre of mass: for multi-site molecules
+                                  choose cell_size >= cutoff + skin + twice a site's largest
+                                  distance from its molecule's centre (only cutoff + skin is
+                                  checked), so that every site pair in range is in adjacent cells */
     double temperature_target; /* VelocityScaling target in K (configuration()->temperature)   */
     int32_t thermostat;        /* 1: each step of komd_gpu_step ends with v *= sqrt(T_target / T),
                                   T measured on the device as TemperatureSensor does
