@@ -835,19 +835,28 @@ __device__ __forceinline__ void lj_atm_half_body(const PairParams &p, const AtmP
         fx = fmaf(sa, gx, fx);
         fy = fmaf(sa, gy, fy);
         fz = fmaf(sa, gz, fz);
-        for (int o = 16; o > 0; o >>= 1) {
-            fx += __shfl_xor_sync(0xffffffffu, fx, o);
-            fy += __shfl_xor_sync(0xffffffffu, fy, o);
-            fz += __shfl_xor_sync(0xffffffffu, fz, o);
+        // the warp sums of (fx, fy, fz) by the butterfly over offsets 16, 8, 4, 2, 1,
+        // the lanes splitting the components on the way: after offset 16 the lanes
+        // below 16 carry x and y, the others z; after offset 8 lanes 0-7 carry x,
+        // 8-15 y, 16-31 z.  Every sum pairs the same partial sums as a butterfly
+        // per component (FP32 addition commutes), so the totals are bitwise those
+        // of 15 shuffles, with 6.
+        float c0;
+        {
+            const bool up16 = (lane & 16) != 0, up8 = (lane & 8) != 0;
+            const float r1 = __shfl_xor_sync(0xffffffffu, up16 ? fx : fz, 16);
+            const float r2 = __shfl_xor_sync(0xffffffffu, fy, 16);
+            c0 = (up16 ? fz : fx) + r1;   // z above 16, x below
+            const float c1 = fy + r2;     // y below 16
+            const float r3 = __shfl_xor_sync(0xffffffffu, (up16 || up8) ? c0 : c1, 8);
+            c0 = ((up16 || !up8) ? c0 : c1) + r3;
+            for (int o = 4; o > 0; o >>= 1) c0 += __shfl_xor_sync(0xffffffffu, c0, o);
         }
-        if (lane == 0) {
-            if (p.fown) {   // FP32 by slot: the flush widens it (no FP64-pipe conversions here)
-                p.fown[i] = make_float4(fx, fy, fz, 0.f);
-            } else {
-                const int site = p.slot_site[i];
-                p.f[3 * site] = (double)fx;
-                p.f[3 * site + 1] = (double)fy;
-                p.f[3 * site + 2] = (double)fz;
+        if ((lane & 7) == 0) {   // lanes 0, 8, 16, 24: x, y, z and the slot's fourth word
+            if (p.fown) {   // FP32 by slot, 16 bytes: the flush widens it (no FP64-pipe conversions here)
+                reinterpret_cast<float *>(p.fown + i)[lane >> 3] = lane < 24 ? c0 : 0.f;
+            } else if (lane < 24) {
+                p.f[3 * (size_t)p.slot_site[i] + (lane >> 3)] = (double)c0;
             }
         }
         __syncwarp();   // se / sq / sr are refilled by the next site
